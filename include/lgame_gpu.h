@@ -1,0 +1,241 @@
+/*
+ * lgame_gpu.h -- C ABI of the GB300 (sm_103a) HEVI time step of L-GAME.
+ *
+ * The library replaces one Fortran module procedure of the reference model:
+ *
+ *   subroutine pchevi(state_old,state_new,tend,bc,grid,diag,total_step_counter,lrad_update,t_0)
+ *   (src/time_stepping/mo_manage_pchevi.F90:27-118, called from src/control.F90:520-524)
+ *
+ * The reference passes Fortran derived types with allocatable components
+ * (src/mo_definitions.F90:29-212), which are not C-interoperable.  This ABI
+ * therefore passes every array as a plain pointer to a contiguous column-major
+ * (Fortran-order) double array with exactly the reference's extents; the array
+ * kinds and their order are fixed by the enums below.  A Fortran host binds it
+ * with iso_c_binding (c_loc of each contiguous allocatable); a C or C++ host
+ * passes pointers directly.
+ *
+ * Index conventions (identical to the reference, src/mo_grid_generator.F90:129-133):
+ *   ji = 1..ny  (y, north to south, fastest varying)
+ *   jk = 1..nx  (x, west to east)
+ *   jl = 1..n_layers (layer 1 = top), levels 1..n_layers+1 (level n_layers+1 = surface)
+ * Staggered extents:
+ *   scalar (ny,nx,nl)      u (ny,nx+1,nl)       v (ny+1,nx,nl)       w (ny,nx,nl+1)
+ *   zeta_x/eta_x (ny+1,nx,nl+1)   zeta_y/eta_y (ny,nx+1,nl+1)   zeta_z/eta_z (ny+1,nx+1,nl)
+ *
+ * Every entry point returns 0 on success or a negative LGAME_ERR_* code and never
+ * calls exit(); lgame_gpu_last_error() describes the last failure of the calling
+ * thread.  The library owns device copies of the grid, two state slots, the
+ * tendencies and the diagnostics that are carried from one step to the next; host
+ * pointers are borrowed for the duration of a call only.
+ */
+#ifndef LGAME_GPU_H
+#define LGAME_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define LGAME_OK                 0
+#define LGAME_ERR_INVALID_ARG   -1  /* null pointer, bad slot, bad field count          */
+#define LGAME_ERR_BAD_DIMS      -2  /* ny/nx/n_layers/n_oro_layers out of range          */
+#define LGAME_ERR_BAD_CONFIG    -3  /* theta_adv_order, precision, dtime ...             */
+#define LGAME_ERR_UNSUPPORTED   -4  /* a physics switch outside the GPU path is on       */
+#define LGAME_ERR_ALLOC         -5  /* device or pinned allocation failed                */
+#define LGAME_ERR_CUDA          -6  /* a CUDA runtime call failed                        */
+#define LGAME_ERR_NONFINITE     -7  /* NaN/Inf found in the new state (check enabled)    */
+#define LGAME_ERR_NO_DEVICE     -8  /* no CUDA device, or not an sm_103 device           */
+#define LGAME_ERR_STATE         -9  /* call out of order (e.g. step before set_grid)     */
+
+/* ---- precision modes ---------------------------------------------------- */
+#define LGAME_PRECISION_FP64   0  /* every operation in FP64, reference operation order */
+#define LGAME_PRECISION_SPLIT  1  /* FP32 explicit stencils and tracer fluxes; FP64
+                                     column solves, background subtraction in the
+                                     pressure gradient, state accumulation and budgets */
+
+/* ---- run configuration ----------------------------------------------------
+ * One field per namelist variable the HEVI step reads (the src/namelists modules),
+ * plus the derived quantities the reference computes once at start-up
+ * (n_levels, n_flat_layers, dtime: mo_run_nml.F90:89-94; n_constituents:
+ * mo_constituents_nml.F90:246-253).  Logical switches are 0/1 ints.
+ * Switches of physics that the GPU step does not implement (diffusion, PBL,
+ * surface fluxes, prognostic soil, non-periodic boundary relaxation) must be 0;
+ * lgame_gpu_create rejects them with LGAME_ERR_UNSUPPORTED. */
+typedef struct lgame_config {
+  /* &run (mo_run_nml.F90:44-46) */
+  int    ny, nx, n_layers, n_oro_layers;
+  double dx, dy, toa;
+  double dtime;                 /* seconds; the reference derives 1.61*sqrt(dx*dy)/1000 */
+  int    theta_adv_order;       /* 2 or 3 */
+  int    llinear, lcorio, luse_bg_state, lplane;
+  /* &constituents (mo_constituents_nml.F90:227) */
+  int    lmoist;                /* 1: 5 condensates + 2 gases (7 constituents); 0: dry (1) */
+  /* &diff (mo_diff_nml.F90:28-29): only the Klemp layer is in the step */
+  int    lklemp;
+  double klemp_damp_max, klemp_begin_rel;
+  int    lmom_diff_h, lmom_diff_v, ltemp_diff_h, ltemp_diff_v, lmass_diff_h, lmass_diff_v;
+  /* &surface (mo_surface_nml.F90:138) */
+  int    lprog_soil_temp, lsfc_sensible_heat_flux, lsfc_phase_trans, lpbl;
+  /* &bc (mo_bc_nml.F90:283) */
+  int    lperiodic, lfreeslip;
+  /* extension: precision and checks (no reference counterpart) */
+  int    precision;             /* LGAME_PRECISION_* */
+  int    check_finite;          /* 1: scan the new state for NaN/Inf after every step */
+} lgame_config;
+
+/* ---- grid arrays (t_grid, src/mo_definitions.F90:29-91) --------------------
+ * Extents in brackets; all double, column-major.  These are exactly the grid
+ * quantities pchevi reads. */
+enum lgame_grid_field {
+  LGAME_GRID_Z_SCALAR = 0,          /* (ny,nx,nl)      */
+  LGAME_GRID_Z_U,                   /* (ny,nx+1,nl)    */
+  LGAME_GRID_Z_V,                   /* (ny+1,nx,nl)    */
+  LGAME_GRID_Z_W,                   /* (ny,nx,nl+1)    */
+  LGAME_GRID_DX,                    /* (ny,nx+1,nl)    */
+  LGAME_GRID_DY,                    /* (ny+1,nx,nl)    */
+  LGAME_GRID_DZ,                    /* (ny,nx,nl+1)    */
+  LGAME_GRID_VOLUME,                /* (ny,nx,nl)      */
+  LGAME_GRID_AREA_X,                /* (ny,nx+1,nl)    */
+  LGAME_GRID_AREA_Y,                /* (ny+1,nx,nl)    */
+  LGAME_GRID_AREA_Z,                /* (ny,nx,nl+1)    */
+  LGAME_GRID_AREA_DUAL_X,           /* (ny+1,nx,nl+1)  */
+  LGAME_GRID_AREA_DUAL_Y,           /* (ny,nx+1,nl+1)  */
+  LGAME_GRID_AREA_DUAL_Z,           /* (ny+1,nx+1,nl)  */
+  LGAME_GRID_Z_AREA_DUAL_Z,         /* (ny+1,nx+1,nl)  */
+  LGAME_GRID_SLOPE_X,               /* (ny,nx+1,nl)    */
+  LGAME_GRID_SLOPE_Y,               /* (ny+1,nx,nl)    */
+  LGAME_GRID_INNER_PRODUCT_WEIGHTS, /* (6,ny,nx,nl)    */
+  LGAME_GRID_THETA_V_BG,            /* (ny,nx,nl)      */
+  LGAME_GRID_EXNER_BG,              /* (ny,nx,nl)      */
+  LGAME_GRID_EXNER_BG_GRAD_U,       /* (ny,nx+1,nl)    */
+  LGAME_GRID_EXNER_BG_GRAD_V,       /* (ny+1,nx,nl)    */
+  LGAME_GRID_EXNER_BG_GRAD_W,       /* (ny,nx,nl+1)    */
+  LGAME_GRID_GRAVITY_M_V,           /* (ny,nx,nl+1)    */
+  LGAME_GRID_GRAVITY_POTENTIAL,     /* (ny,nx,nl)      */
+  LGAME_GRID_FVEC_X,                /* (ny+1,nx)       */
+  LGAME_GRID_FVEC_Y,                /* (ny,nx+1)       */
+  LGAME_GRID_FVEC_Z,                /* (ny+1,nx+1)     */
+  LGAME_GRID_TRSK_WEIGHTS_U,        /* (3,ny)          */
+  LGAME_GRID_TRSK_WEIGHTS_V,        /* (2,ny+1)        */
+  LGAME_GRID_NFIELDS
+};
+
+/* ---- prognostic state (t_state, src/mo_definitions.F90:94-105) ----------- */
+enum lgame_state_field {
+  LGAME_STATE_RHO = 0,        /* (ny,nx,nl,n_constituents) */
+  LGAME_STATE_RHOTHETA_V,     /* (ny,nx,nl)     */
+  LGAME_STATE_THETA_V_PERT,   /* (ny,nx,nl)     */
+  LGAME_STATE_EXNER_PERT,     /* (ny,nx,nl)     */
+  LGAME_STATE_WIND_U,         /* (ny,nx+1,nl)   */
+  LGAME_STATE_WIND_V,         /* (ny+1,nx,nl)   */
+  LGAME_STATE_WIND_W,         /* (ny,nx,nl+1)   */
+  LGAME_STATE_NFIELDS
+};
+
+/* ---- diagnostics carried between steps (t_diag, t_tend) -------------------
+ * These are the arrays whose values survive from one call of pchevi to the next
+ * (or that the host provides), i.e. what a restart needs besides the state. */
+enum lgame_diag_field {
+  LGAME_DIAG_P_GRAD_ACC_NEG_NL_U = 0, /* (ny,nx+1,nl)   */
+  LGAME_DIAG_P_GRAD_ACC_NEG_NL_V,     /* (ny+1,nx,nl)   */
+  LGAME_DIAG_P_GRAD_ACC_NEG_NL_W,     /* (ny,nx,nl+1)   */
+  LGAME_DIAG_P_GRAD_ACC_NEG_L_U,      /* (ny,nx+1,nl)   */
+  LGAME_DIAG_P_GRAD_ACC_NEG_L_V,      /* (ny+1,nx,nl)   */
+  LGAME_DIAG_P_GRAD_ACC_NEG_L_W,      /* (ny,nx,nl+1)   */
+  LGAME_DIAG_P_GRAD_ACC_OLD_U,        /* (ny,nx+1,nl)   */
+  LGAME_DIAG_P_GRAD_ACC_OLD_V,        /* (ny+1,nx,nl)   */
+  LGAME_DIAG_POT_VORT_TEND_X,         /* (ny,nx+1,nl)   */
+  LGAME_DIAG_POT_VORT_TEND_Y,         /* (ny+1,nx,nl)   */
+  LGAME_DIAG_POT_VORT_TEND_Z,         /* (ny,nx,nl+1)   */
+  LGAME_DIAG_V_SQUARED_GRAD_X,        /* (ny,nx+1,nl)   */
+  LGAME_DIAG_V_SQUARED_GRAD_Y,        /* (ny+1,nx,nl)   */
+  LGAME_DIAG_V_SQUARED_GRAD_Z,        /* (ny,nx,nl+1)   */
+  LGAME_DIAG_CONDENSATES_SEDIMENT_HEAT,/* (ny,nx,nl)    */
+  LGAME_DIAG_RADIATION_TENDENCY,      /* (ny,nx,nl)  W m^-3, provided by the host   */
+  LGAME_DIAG_TEMPERATURE,             /* (ny,nx,nl)  of state_old of the last step  */
+  LGAME_DIAG_TEND_RHO,                /* (ny,nx,nl,n_constituents)                  */
+  LGAME_DIAG_TEND_RHOTHETA_V,         /* (ny,nx,nl)     */
+  LGAME_DIAG_TEND_WIND_U,             /* (ny,nx+1,nl)   */
+  LGAME_DIAG_TEND_WIND_V,             /* (ny+1,nx,nl)   */
+  LGAME_DIAG_TEND_WIND_W,             /* (ny,nx,nl+1)   */
+  LGAME_DIAG_NFIELDS
+};
+
+/* Budget vector of lgame_gpu_budgets (mo_write_out.F90:226-304):
+ *   out[0 .. n_constituents-1]  sum(rho(:,:,:,jc)*volume)        (masses)
+ *   out[n_constituents]         sum(rhotheta_v*volume)
+ *   out[n_constituents+1]       0.5*sum(rho_g*|v|^2 *volume)     (kinetic)
+ *   out[n_constituents+2]       sum(rho_g*gravity_potential*volume)
+ *   out[n_constituents+3]       sum(c_d_v*rho_g*temperature*volume) (internal) */
+#define LGAME_BUDGETS_MAX 11
+
+typedef struct lgame_gpu lgame_gpu;   /* opaque context, one per model instance */
+
+/* Creates a context on the current CUDA device and allocates its device memory.
+ * Replaces the allocation block of src/control.F90:99-444 for the arrays pchevi uses. */
+int  lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out);
+
+/* Copies the grid (host, reference layout) to the device once, precomputing nothing
+ * that changes the arithmetic of the FP64 path.  Replaces the grid argument of pchevi
+ * (mo_manage_pchevi.F90:35) for the lifetime of the context.  nfields must equal
+ * LGAME_GRID_NFIELDS. */
+int  lgame_gpu_set_grid(lgame_gpu* ctx, const double* const* fields, int nfields);
+
+/* Host -> device copy of one state slot (slot 0 or 1, the reference's state_1/state_2,
+ * control.F90:30-31).  nfields must equal LGAME_STATE_NFIELDS. */
+int  lgame_gpu_set_state(lgame_gpu* ctx, int slot, const double* const* fields, int nfields);
+/* Device -> host copy of one state slot; synchronises. */
+int  lgame_gpu_get_state(lgame_gpu* ctx, int slot, double* const* fields, int nfields);
+
+/* Host <-> device copies of the carried diagnostics (restart, parity checks, and the
+ * host-provided radiation tendency).  nfields must equal LGAME_DIAG_NFIELDS; a NULL
+ * pointer in set_diag leaves that field unchanged, in get_diag skips it. */
+int  lgame_gpu_set_diag(lgame_gpu* ctx, const double* const* fields, int nfields);
+int  lgame_gpu_get_diag(lgame_gpu* ctx, double* const* fields, int nfields);
+
+/* One HEVI predictor-corrector step entirely on the device: state[new_slot] is
+ * computed from state[old_slot].  Equivalent of
+ *   call pchevi(state_old,state_new,tend,bc,grid,diag,total_step_counter,lrad_update,t_0)
+ * with the periodic domain (the boundary relaxation of mo_boundaries.F90 is not part
+ * of the GPU path).  lrad_update and t_0 are accepted for interface parity; the
+ * radiation tendency is whatever the host last set (or the emulator wrote).
+ * Stream-ordered: returns after enqueueing unless check_finite is on. */
+int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
+                      int total_step_counter, int lrad_update, double t_0);
+
+/* The same step with host buffers: copies state_old from host memory to the device,
+ * runs lgame_gpu_pchevi into slot 1, and copies the new state back to state_new
+ * (host).  This is what a Fortran pchevi_gpu shim with pchevi's exact argument list
+ * would call when the host keeps the authoritative state (mo_manage_pchevi.F90:27). */
+int  lgame_gpu_pchevi_host(lgame_gpu* ctx, const double* const* state_old,
+                           double* const* state_new, int nfields,
+                           int total_step_counter, int lrad_update, double t_0);
+
+/* FP64 domain integrals of one slot (mo_write_out.F90:226-304); out must hold
+ * n_constituents+4 doubles.  Uses the temperature diagnosed at the start of the last
+ * step, as the reference's write_out_integrals does (control.F90:529-535).
+ * Synchronises. */
+int  lgame_gpu_budgets(lgame_gpu* ctx, int slot, double* out, int nout);
+
+/* Blocks until all work of the context has finished. */
+int  lgame_gpu_synchronize(lgame_gpu* ctx);
+
+/* Number of kernels launched by the last lgame_gpu_pchevi call. */
+int  lgame_gpu_kernels_per_step(const lgame_gpu* ctx);
+
+/* Bytes of device memory held by the context. */
+long long lgame_gpu_device_bytes(const lgame_gpu* ctx);
+
+/* Frees all device memory of the context. */
+void lgame_gpu_destroy(lgame_gpu* ctx);
+
+/* Human-readable description of the last error of the calling thread. */
+const char* lgame_gpu_last_error(void);
+
+/* Library version string. */
+const char* lgame_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LGAME_GPU_H */

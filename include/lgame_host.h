@@ -1,0 +1,111 @@
+/*
+ * lgame_host.h -- host side of the drop-in driver: namelist, grid and initial state.
+ *
+ * In the reference these steps run in Fortran before the time loop
+ * (src/control.F90:64-91 namelists, :453 grid_setup, :466 bg_setup, :476 ideal_init).
+ * A Fortran host keeps doing them itself and only binds lgame_gpu.h.  This header
+ * is for hosts without a Fortran compiler (the C++ driver lgame_gpu_run, the Python
+ * bindings): it produces the same grid, background state and idealised initial
+ * state, in the reference's array layout, ready for lgame_gpu_set_grid/set_state.
+ */
+#ifndef LGAME_HOST_H
+#define LGAME_HOST_H
+
+#include <stddef.h>
+#include "lgame_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Every variable of the seven namelist groups of the reference with its default
+ * (mo_run_nml.F90:55-80, mo_io_nml.F90:251-257, mo_constituents_nml.F90:236-238,
+ * mo_diff_nml.F90:39-53, mo_surface_nml.F90:148-154, mo_bc_nml.F90:293-298,
+ * mo_rad_nml.F90:206-211), the derived quantities the reference computes after
+ * reading them, and one extension group &gpu whose defaults leave the reference
+ * behaviour unchanged. */
+typedef struct lgame_namelist {
+  /* &run */
+  int    ny, nx, n_layers, n_oro_layers;
+  double dy, dx;
+  int    run_span_min;
+  double stretching_parameter;
+  int    theta_adv_order;
+  double toa;
+  char   scenario[64];
+  int    llinear;
+  char   run_id[64];
+  int    lcorio;
+  double lat_center, lon_center;
+  int    start_year, start_month, start_day, start_hour, start_minute;
+  int    lplane, luse_bg_state;
+  /* &io */
+  int    dt_write_min, lread_geo, lwrite_grid;
+  char   grid_filename[64], restart_filename[64];
+  int    lwrite_integrals;
+  /* &constituents */
+  int    lmoist;
+  /* &diff */
+  int    lmom_diff_h, lmom_diff_v, ltemp_diff_h, ltemp_diff_v, lmass_diff_h, lmass_diff_v;
+  double h_prandtl, karman;
+  int    lklemp;
+  double klemp_damp_max, klemp_begin_rel;
+  char   diff_coeff_scheme_h[16], diff_coeff_scheme_v[16];
+  double bg_shear, c_s;
+  /* &surface */
+  int    orography_id, lprog_soil_temp, nsoillays, lsfc_sensible_heat_flux, lsfc_phase_trans, lpbl, lsleve;
+  /* &bc */
+  int    n_swamp, lperiodic, lfreeslip, dtime_bc;
+  char   bc_root_filename[64];
+  /* &rad */
+  int    lrad;
+  double dtime_rad;
+  char   rrtmgp_coefficients_file_sw[128], rrtmgp_coefficients_file_lw[128];
+  char   cloud_coefficients_file_sw[128], cloud_coefficients_file_lw[128];
+  /* &gpu (extension; no reference counterpart) */
+  int    precision;          /* 0 fp64, 1 split                                        */
+  double dtime_override;     /* > 0: use this time step instead of 1.61*sqrt(dx*dy)/1000 */
+  int    strict_reference;   /* 1: keep the reference's odd-nx/ny check                */
+  long long seed;            /* seed of the random orography and the moist jet state   */
+  int    n_hills;            /* orography_id=5: number of Gaussian hills               */
+  double hill_height_min, hill_height_max, hill_width_min, hill_width_max;
+  double jet_speed, jet_pressure;  /* scenario "baroclinic_jet" */
+  double t_pert_sigma, rh_mean;
+  int    check_finite;
+  /* derived (mo_run_nml.F90:89-101, mo_constituents_nml.F90:246-253, mo_io_nml.F90:266) */
+  int    n_levels, n_flat_layers, n_condensed_constituents, n_constituents;
+  double eff_hor_res, dtime, dt_write, t_init;
+} lgame_namelist;
+
+/* Fills every field with the reference default. */
+void lgame_namelist_defaults(lgame_namelist* nml);
+/* Reads the Fortran namelist groups from text (the file namelist.nml of the reference,
+ * e.g. run_scripts/schaer.sh:12-65) over the current contents of nml, then derives
+ * n_levels, dtime, ... and runs the reference's sanity checks (mo_run_nml.F90:103-141,
+ * mo_diff_nml.F90:91-98, mo_surface_nml.F90:163-166, control.F90:94-97).  Returns 0 or
+ * LGAME_ERR_BAD_CONFIG / LGAME_ERR_BAD_DIMS with lgame_gpu_last_error() set; never exits. */
+int  lgame_namelist_parse(const char* text, lgame_namelist* nml);
+/* Reads a namelist file (defaults first, then the file). */
+int  lgame_namelist_read_file(const char* path, lgame_namelist* nml);
+/* Translates a namelist into the run configuration of lgame_gpu_create. */
+int  lgame_config_from_namelist(const lgame_namelist* nml, lgame_config* cfg);
+
+/* Host model: grid, background and initial state in the reference's layout. */
+typedef struct lgame_host_model lgame_host_model;
+/* grid_setup + bg_setup + ideal_init (mo_grid_generator.F90:29-1457,
+ * mo_set_initial_state.F90:22-382).  Orography ids 0, 2, 3, 4 as in the reference;
+ * 5 = sum of n_hills seeded Gaussian hills.  Scenarios standard, seabreeze, advection,
+ * schaer, mountain_rest as in the reference; baroclinic_jet = seeded moist jet. */
+int  lgame_host_setup(const lgame_namelist* nml, lgame_host_model** out);
+void lgame_host_destroy(lgame_host_model* m);
+/* Pointers into the model's arrays (owned by the model); *n receives the element count. */
+double* lgame_host_grid_field(lgame_host_model* m, int field, size_t* n);
+double* lgame_host_state_field(lgame_host_model* m, int field, size_t* n);
+double* lgame_host_diag_field(lgame_host_model* m, int field, size_t* n);
+/* 2-D surface fields: 0 oro, 1 sfc_albedo, 2 lat_geo_scalar, 3 lon_geo_scalar */
+double* lgame_host_surface_field(lgame_host_model* m, int field, size_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,679 @@
+// lgame_gpu.cu -- C ABI of the GB300 HEVI step: device memory, host<->device copies and
+// the order of the kernels of one pchevi call (src/time_stepping/mo_manage_pchevi.F90).
+#include "lgame_gpu.h"
+#include "common.h"
+#include "kernels.cuh"
+#include "split.cuh"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace lg;
+
+namespace {
+
+int set_err(int code, const std::string& msg) {
+  lgame_set_error(msg.c_str());
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return set_err(LGAME_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+}  // namespace
+
+struct lgame_gpu {
+  lgame_config cfg;
+  Dims D;
+  cudaStream_t stream = nullptr;
+  std::vector<void*> allocations;
+  long long bytes = 0;
+  bool grid_set = false;
+  int kernels_last_step = 0;
+  // device fields (FP64)
+  double* grid[LGAME_GRID_NFIELDS + 8] = {};
+  double* ipw[6] = {};
+  double* trsk_u[3] = {};
+  double* trsk_v[2] = {};
+  double* damp = nullptr;
+  State st[2];
+  Tend tend;
+  double *pg_nl_u, *pg_nl_v, *pg_nl_w, *pg_l_u, *pg_l_v, *pg_l_w, *pg_old_u, *pg_old_v, *pgcw;
+  double *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
+  // scratch
+  double *theta, *gz, *gx, *gy, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph, *vsq;
+  double* staging = nullptr;
+  size_t staging_elems = 0;
+  double* reduce_buf = nullptr;
+  int* flag = nullptr;
+  Grid<double> G{};
+  SplitCtx* split = nullptr;
+};
+
+namespace {
+
+int dalloc(lgame_gpu* c, double** p, size_t n) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, n * sizeof(double));
+  if (e != cudaSuccess) return set_err(LGAME_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  e = cudaMemset(q, 0, n * sizeof(double));
+  if (e != cudaSuccess) return set_err(LGAME_ERR_CUDA, cudaGetErrorString(e));
+  c->allocations.push_back(q);
+  c->bytes += (long long)(n * sizeof(double));
+  *p = (double*)q;
+  return LGAME_OK;
+}
+
+// host array extents of the reference layout
+struct Ext { size_t n1, n2, n3; };
+Ext ext_s(const Dims& d) { return {(size_t)d.ny, (size_t)d.nx, (size_t)d.nl}; }
+Ext ext_u(const Dims& d) { return {(size_t)d.ny, (size_t)d.nx + 1, (size_t)d.nl}; }
+Ext ext_v(const Dims& d) { return {(size_t)d.ny + 1, (size_t)d.nx, (size_t)d.nl}; }
+Ext ext_w(const Dims& d) { return {(size_t)d.ny, (size_t)d.nx, (size_t)d.nl + 1}; }
+Ext ext_z(const Dims& d) { return {(size_t)d.ny + 1, (size_t)d.nx + 1, (size_t)d.nl}; }
+Ext ext_ex(const Dims& d) { return {(size_t)d.ny + 1, (size_t)d.nx, (size_t)d.nl + 1}; }
+Ext ext_ey(const Dims& d) { return {(size_t)d.ny, (size_t)d.nx + 1, (size_t)d.nl + 1}; }
+
+Ext grid_ext(const Dims& d, int f) {
+  switch (f) {
+    case LGAME_GRID_Z_SCALAR: case LGAME_GRID_VOLUME: case LGAME_GRID_THETA_V_BG:
+    case LGAME_GRID_EXNER_BG: case LGAME_GRID_GRAVITY_POTENTIAL: return ext_s(d);
+    case LGAME_GRID_Z_U: case LGAME_GRID_DX: case LGAME_GRID_AREA_X: case LGAME_GRID_SLOPE_X:
+    case LGAME_GRID_EXNER_BG_GRAD_U: return ext_u(d);
+    case LGAME_GRID_Z_V: case LGAME_GRID_DY: case LGAME_GRID_AREA_Y: case LGAME_GRID_SLOPE_Y:
+    case LGAME_GRID_EXNER_BG_GRAD_V: return ext_v(d);
+    case LGAME_GRID_Z_W: case LGAME_GRID_DZ: case LGAME_GRID_AREA_Z: case LGAME_GRID_EXNER_BG_GRAD_W:
+    case LGAME_GRID_GRAVITY_M_V: return ext_w(d);
+    case LGAME_GRID_AREA_DUAL_X: return ext_ex(d);
+    case LGAME_GRID_AREA_DUAL_Y: return ext_ey(d);
+    case LGAME_GRID_AREA_DUAL_Z: case LGAME_GRID_Z_AREA_DUAL_Z: return ext_z(d);
+    case LGAME_GRID_FVEC_X: return {(size_t)d.ny + 1, (size_t)d.nx, 1};
+    case LGAME_GRID_FVEC_Y: return {(size_t)d.ny, (size_t)d.nx + 1, 1};
+    case LGAME_GRID_FVEC_Z: return {(size_t)d.ny + 1, (size_t)d.nx + 1, 1};
+  }
+  return {0, 0, 0};
+}
+
+Ext diag_ext(const Dims& d, int f) {
+  switch (f) {
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_U: case LGAME_DIAG_P_GRAD_ACC_NEG_L_U: case LGAME_DIAG_P_GRAD_ACC_OLD_U:
+    case LGAME_DIAG_POT_VORT_TEND_X: case LGAME_DIAG_V_SQUARED_GRAD_X: case LGAME_DIAG_TEND_WIND_U: return ext_u(d);
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_V: case LGAME_DIAG_P_GRAD_ACC_NEG_L_V: case LGAME_DIAG_P_GRAD_ACC_OLD_V:
+    case LGAME_DIAG_POT_VORT_TEND_Y: case LGAME_DIAG_V_SQUARED_GRAD_Y: case LGAME_DIAG_TEND_WIND_V: return ext_v(d);
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: case LGAME_DIAG_POT_VORT_TEND_Z:
+    case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: return ext_w(d);
+    default: return ext_s(d);
+  }
+}
+
+// host (column-major, extents e) <-> device (padded), one pitched 3-D copy
+int copy_h2d(lgame_gpu* c, double* dev, const double* host, Ext e) {
+  cudaMemcpy3DParms p = {};
+  p.srcPtr = make_cudaPitchedPtr((void*)host, e.n1 * sizeof(double), e.n1, e.n2);
+  p.dstPtr = make_cudaPitchedPtr(dev, (size_t)c->D.P * sizeof(double), (size_t)c->D.P, (size_t)c->D.NX1);
+  p.extent = make_cudaExtent(e.n1 * sizeof(double), e.n2, e.n3);
+  p.kind = cudaMemcpyHostToDevice;
+  CK(cudaMemcpy3DAsync(&p, c->stream));
+  return LGAME_OK;
+}
+int copy_d2h(lgame_gpu* c, double* host, const double* dev, Ext e) {
+  cudaMemcpy3DParms p = {};
+  p.srcPtr = make_cudaPitchedPtr((void*)dev, (size_t)c->D.P * sizeof(double), (size_t)c->D.P, (size_t)c->D.NX1);
+  p.dstPtr = make_cudaPitchedPtr(host, e.n1 * sizeof(double), e.n1, e.n2);
+  p.extent = make_cudaExtent(e.n1 * sizeof(double), e.n2, e.n3);
+  p.kind = cudaMemcpyDeviceToHost;
+  CK(cudaMemcpy3DAsync(&p, c->stream));
+  return LGAME_OK;
+}
+
+__global__ void k_split_ipw(Dims D, const double* src, double* w1, double* w2, double* w3, double* w4,
+                            double* w5, double* w6) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.z + 1;
+  if (ji > D.ny || jk > D.nx) return;
+  const size_t h = 6 * ((size_t)(ji - 1) + (size_t)D.ny * ((size_t)(jk - 1) + (size_t)D.nx * (size_t)(jl - 1)));
+  const long long q = IX(D, ji, jk, jl);
+  w1[q] = src[h]; w2[q] = src[h + 1]; w3[q] = src[h + 2]; w4[q] = src[h + 3]; w5[q] = src[h + 4]; w6[q] = src[h + 5];
+}
+
+__global__ void k_check_finite(Dims D, State S, int* flag) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.z + 1;
+  bool bad = false;
+  if (ji <= D.ny && jk <= D.nx && jl <= D.nl) {
+    const long long q = IX(D, ji, jk, jl);
+    for (int jc = 0; jc < D.ncons; ++jc) bad |= !isfinite(S.rho[q + (long long)jc * D.fstride]);
+    bad |= !isfinite(S.rt[q]) || !isfinite(S.ep[q]) || !isfinite(S.tp[q]);
+  }
+  if (ji <= D.ny && jk <= D.nx + 1 && jl <= D.nl) bad |= !isfinite(S.u[IX(D, ji, jk, jl)]);
+  if (ji <= D.ny + 1 && jk <= D.nx && jl <= D.nl) bad |= !isfinite(S.v[IX(D, ji, jk, jl)]);
+  if (ji <= D.ny && jk <= D.nx && jl <= D.NL) bad |= !isfinite(S.w[IX(D, ji, jk, jl)]);
+  if (bad) atomicExch(flag, 1);
+}
+
+// deterministic FP64 sums: every block sums a fixed strided subset in a fixed order;
+// the partial sums are then added by one thread in block order.
+constexpr int kRedBlocks = 1024, kRedThreads = 256;
+__global__ void k_budget_partial(Dims D, Grid<double> G, State S, const double* T, double* part, int nq) {
+  __shared__ double sh[kRedThreads];
+  const long long n = (long long)D.ny * D.nx * D.nl;
+  for (int k = 0; k < nq; ++k) {
+    double acc = 0.0;
+    for (long long e = (long long)blockIdx.x * kRedThreads + threadIdx.x; e < n; e += (long long)kRedBlocks * kRedThreads) {
+      const int ji = (int)(e % D.ny) + 1;
+      const int jk = (int)((e / D.ny) % D.nx) + 1;
+      const int jl = (int)(e / ((long long)D.ny * D.nx)) + 1;
+      const long long q = IX(D, ji, jk, jl);
+      const double V = G.volume[q];
+      const double rg = S.rho[q + (long long)(D.g - 1) * D.fstride];
+      double x;
+      if (k < D.ncons) x = S.rho[q + (long long)k * D.fstride] * V;
+      else if (k == D.ncons) x = S.rt[q] * V;
+      else if (k == D.ncons + 1) x = (rg * inner_product_at(D, G, S.u, S.v, S.w, ji, jk, jl)) * V;
+      else if (k == D.ncons + 2) x = (rg * G.gp[q]) * V;
+      else x = (kC_D_V * rg * T[q]) * V;
+      acc = acc + x;
+    }
+    sh[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = kRedThreads / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(long long)k * kRedBlocks + blockIdx.x] = sh[0];
+    __syncthreads();
+  }
+}
+__global__ void k_budget_final(const double* part, double* out, int nq) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int k = 0; k < nq; ++k) {
+    double s = 0.0;
+    for (int b = 0; b < kRedBlocks; ++b) s = s + part[(long long)k * kRedBlocks + b];
+    out[k] = s;
+  }
+}
+
+dim3 blk() { return dim3(32, 8, 1); }
+dim3 grd(const Dims& D, int rows, int cols, int levs) {
+  return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 7) / 8), (unsigned)levs);
+}
+
+int klaunch_check(lgame_gpu* c, const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_err(LGAME_ERR_CUDA, std::string("launch of ") + what + ": " + cudaGetErrorString(e));
+  ++c->kernels_last_step;
+  return LGAME_OK;
+}
+#define LAUNCH(kernel, grid_, ...)                                             \
+  do {                                                                         \
+    kernel<<<grid_, blk(), 0, c->stream>>>(__VA_ARGS__);                       \
+    int rc_ = klaunch_check(c, #kernel);                                       \
+    if (rc_ != LGAME_OK) return rc_;                                           \
+  } while (0)
+
+// theta_v_adv_3rd_order (mo_multiplications.F90:116-204) of theta = theta_v_bg + tp
+// (mode 0) or tp (mode 1): gradient, divergence, edge values into (ou, ov)
+int theta3(lgame_gpu* c, const double* tp, int mode, const double* u, const double* v, double* ou, double* ov) {
+  const Dims& D = c->D;
+  LAUNCH(k_theta, grd(D, D.ny, D.nx, D.nl), D, c->G, tp, c->theta, mode);
+  LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->theta, c->gz);
+  LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->gz, c->gx, c->gy);
+  LAUNCH(k_div_h, grd(D, D.ny, D.nx, D.nl), D, c->G, c->gx, c->gy, c->divf);
+  LAUNCH(k_theta_edges, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->divf, u, v, ou, ov);
+  return LGAME_OK;
+}
+
+// momentum advection of vector_tend_expl, mo_vector_tend_expl.F90:188-229
+int advection(lgame_gpu* c, const State& S) {
+  const Dims& D = c->D;
+  if (!(!D.llinear || D.lcorio)) return LGAME_OK;
+  LAUNCH(k_eta_xy, grd(D, D.ny + 1, D.nx + 1, D.NL), D, c->G, S, c->ex, c->ey);
+  LAUNCH(k_eta_z, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ez);
+  LAUNCH(k_mass_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->uph, c->vph, c->wph);
+  LAUNCH(k_vort_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ex, c->ey, c->ez, c->uph, c->vph, c->wph,
+         c->pvt_x, c->pvt_y, c->pvt_z);
+  if (!D.llinear) {
+    LAUNCH(k_ke, grd(D, D.ny, D.nx, D.nl), D, c->G, S, c->vsq);
+    LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->vsq, c->vsg_z);
+    LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->vsq, c->vsg_z, c->vsg_x, c->vsg_y);
+  }
+  return LGAME_OK;
+}
+
+int step_fp64(lgame_gpu* c, int so, int sn, int step) {
+  const Dims& D = c->D;
+  const State& So = c->st[so];
+  const State& Sn = c->st[sn];
+  const Grid<double>& G = c->G;
+  LAUNCH(k_temperature, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature);
+  PGrad P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw};
+  Carried C{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw,
+            c->vsg_x, c->vsg_y, c->vsg_z, c->pvt_x, c->pvt_y, c->pvt_z};
+  for (int rk = 1; rk <= 2; ++rk) {
+    const State& Sv = (rk == 1) ? So : Sn;   // state of vector_tend_expl
+    if (rk == 1) {
+      // manage_p_grad (mo_p_grad.F90:20-104) and calc_p_grad_condensates_v (:106-120):
+      // theta edge values first (they use gx/gy/gz as scratch), then grad(exner_pert)
+      if (D.theta_order == 3) {
+        int rc = theta3(c, So.tp, 0, So.u, So.v, c->tvu, c->tvv);
+        if (rc != LGAME_OK) return rc;
+        if (D.luse_bg) { rc = theta3(c, So.tp, 1, So.u, So.v, c->tpu, c->tpv); if (rc != LGAME_OK) return rc; }
+      }
+      LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, G, So.ep, c->gz);
+      LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So.ep, c->gz, c->gx, c->gy);
+      LAUNCH(k_pgrad, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, c->gx, c->gy, c->gz, c->tvu, c->tvv, c->tpu, c->tpv,
+             P, step == 0 ? 1 : 0);
+    }
+    if (rk == 2 || step == 0) {
+      int rc = advection(c, Sv);
+      if (rc != LGAME_OK) return rc;
+    }
+    Tend T = c->tend;
+    LAUNCH(k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk);
+    // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
+    const State& Ss = (rk == 1) ? So : Sn;
+    if (D.ncons > 1) LAUNCH(k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
+    if (D.theta_order == 3) {
+      int rc = theta3(c, Ss.tp, 0, Ss.u, Ss.v, c->tvu, c->tvv);
+      if (rc != LGAME_OK) return rc;
+    }
+    LAUNCH(k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->rad,
+           c->csh, T.rho, T.rt);
+    // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
+    {
+      dim3 g2((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 7) / 8), 1);
+      LAUNCH(k_column_ver, g2, D, G, So, Sn, T, rk);
+      if (D.ncons > 1) LAUNCH(k_column_tracers, g2, D, G, So, Sn, T.rho, c->temperature, c->csh, rk);
+    }
+  }
+  return LGAME_OK;
+}
+
+int check_cfg(const lgame_config* cfg) {
+  if (cfg->ny < 3 || cfg->nx < 3) return set_err(LGAME_ERR_BAD_DIMS, "ny and nx must be >= 3");
+  if (cfg->n_layers < 3 || cfg->n_layers > 128) return set_err(LGAME_ERR_BAD_DIMS, "n_layers must be in 3..128");
+  if (cfg->n_oro_layers < 1 || cfg->n_oro_layers >= cfg->n_layers)
+    return set_err(LGAME_ERR_BAD_DIMS, "it must be 1 <= n_oro_layers < n_layers");
+  if (cfg->theta_adv_order != 2 && cfg->theta_adv_order != 3)
+    return set_err(LGAME_ERR_BAD_CONFIG, "theta_adv_order must be 2 or 3");
+  if (!(cfg->dtime > 0.0) || !(cfg->toa > 0.0) || !(cfg->dx > 0.0) || !(cfg->dy > 0.0))
+    return set_err(LGAME_ERR_BAD_CONFIG, "dtime, toa, dx and dy must be positive");
+  if (cfg->precision != LGAME_PRECISION_FP64 && cfg->precision != LGAME_PRECISION_SPLIT)
+    return set_err(LGAME_ERR_BAD_CONFIG, "precision must be LGAME_PRECISION_FP64 or LGAME_PRECISION_SPLIT");
+  if (cfg->lmom_diff_h || cfg->lmom_diff_v || cfg->ltemp_diff_h || cfg->ltemp_diff_v || cfg->lmass_diff_h || cfg->lmass_diff_v)
+    return set_err(LGAME_ERR_UNSUPPORTED, "diffusion (&diff lmom_diff_h ... lmass_diff_v) is not part of the GPU step");
+  if (cfg->lprog_soil_temp || cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl)
+    return set_err(LGAME_ERR_UNSUPPORTED, "surface physics (&surface lprog_soil_temp, lsfc_*, lpbl) is not part of the GPU step");
+  return LGAME_OK;
+}
+
+}  // namespace
+
+extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
+  if (!cfg || !out) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_create: null argument");
+  *out = nullptr;
+  int rc = check_cfg(cfg);
+  if (rc != LGAME_OK) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return set_err(LGAME_ERR_NO_DEVICE, "no CUDA device is visible");
+  }
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, dev));
+  if (prop.major != 10 || prop.minor != 3)
+    return set_err(LGAME_ERR_NO_DEVICE, std::string("this library is built for sm_103 (GB300); device is ") + prop.name);
+  auto* c = new lgame_gpu();
+  c->cfg = *cfg;
+  Dims& D = c->D;
+  D.ny = cfg->ny; D.nx = cfg->nx; D.nl = cfg->n_layers; D.NL = cfg->n_layers + 1;
+  D.nf = cfg->n_layers - cfg->n_oro_layers;
+  D.P = ((D.ny + 1) + 31) / 32 * 32;
+  D.NX1 = D.nx + 1;
+  D.plane = (long long)D.P * D.NX1;
+  D.fstride = D.plane * (D.nl + 1);
+  D.nc = cfg->lmoist ? 5 : 0;
+  D.ncons = D.nc + (cfg->lmoist ? 2 : 1);
+  D.g = D.nc + 1;
+  D.periodic = cfg->lperiodic; D.freeslip = cfg->lfreeslip; D.lcorio = cfg->lcorio; D.llinear = cfg->llinear;
+  D.luse_bg = cfg->luse_bg_state; D.lmoist = cfg->lmoist; D.theta_order = cfg->theta_adv_order; D.lklemp = cfg->lklemp;
+  D.dtime = cfg->dtime; D.toa = cfg->toa; D.dxn = cfg->dx; D.dyn = cfg->dy;
+  auto fail = [&](int code) { lgame_gpu_destroy(c); return code; };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(set_err(LGAME_ERR_CUDA, "cudaStreamCreate failed"));
+  const size_t F = (size_t)D.fstride;
+  // grid
+  for (int f = 0; f < LGAME_GRID_NFIELDS; ++f) {
+    if (f == LGAME_GRID_INNER_PRODUCT_WEIGHTS || f == LGAME_GRID_TRSK_WEIGHTS_U || f == LGAME_GRID_TRSK_WEIGHTS_V) continue;
+    size_t n = (f == LGAME_GRID_FVEC_X || f == LGAME_GRID_FVEC_Y || f == LGAME_GRID_FVEC_Z) ? (size_t)D.plane : F;
+    if ((rc = dalloc(c, &c->grid[f], n)) != LGAME_OK) return fail(rc);
+  }
+  for (int k = 0; k < 6; ++k) if ((rc = dalloc(c, &c->ipw[k], F)) != LGAME_OK) return fail(rc);
+  for (int k = 0; k < 3; ++k) if ((rc = dalloc(c, &c->trsk_u[k], (size_t)D.P)) != LGAME_OK) return fail(rc);
+  for (int k = 0; k < 2; ++k) if ((rc = dalloc(c, &c->trsk_v[k], (size_t)D.P)) != LGAME_OK) return fail(rc);
+  if ((rc = dalloc(c, &c->damp, F)) != LGAME_OK) return fail(rc);
+  // states and tendencies
+  for (int s = 0; s < 2; ++s) {
+    State& S = c->st[s];
+    if ((rc = dalloc(c, &S.rho, F * D.ncons)) || (rc = dalloc(c, &S.rt, F)) || (rc = dalloc(c, &S.tp, F)) ||
+        (rc = dalloc(c, &S.ep, F)) || (rc = dalloc(c, &S.u, F)) || (rc = dalloc(c, &S.v, F)) || (rc = dalloc(c, &S.w, F)))
+      return fail(rc);
+  }
+  if ((rc = dalloc(c, &c->tend.rho, F * D.ncons)) || (rc = dalloc(c, &c->tend.rt, F)) || (rc = dalloc(c, &c->tend.u, F)) ||
+      (rc = dalloc(c, &c->tend.v, F)) || (rc = dalloc(c, &c->tend.w, F)))
+    return fail(rc);
+  double** carried[] = {&c->pg_nl_u, &c->pg_nl_v, &c->pg_nl_w, &c->pg_l_u, &c->pg_l_v, &c->pg_l_w, &c->pg_old_u,
+                        &c->pg_old_v, &c->pgcw, &c->vsg_x, &c->vsg_y, &c->vsg_z, &c->pvt_x, &c->pvt_y, &c->pvt_z,
+                        &c->csh, &c->rad, &c->temperature};
+  for (double** p : carried) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+  double** scratch[] = {&c->theta, &c->gz, &c->gx, &c->gy, &c->divf, &c->tvu, &c->tvv, &c->tpu, &c->tpv,
+                        &c->ex, &c->ey, &c->ez, &c->uph, &c->vph, &c->wph, &c->vsq};
+  for (double** p : scratch) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+  c->staging_elems = 6 * (size_t)D.ny * D.nx * D.nl;
+  if ((rc = dalloc(c, &c->staging, c->staging_elems)) != LGAME_OK) return fail(rc);
+  if ((rc = dalloc(c, &c->reduce_buf, (size_t)kRedBlocks * LGAME_BUDGETS_MAX + LGAME_BUDGETS_MAX)) != LGAME_OK) return fail(rc);
+  {
+    void* q = nullptr;
+    if (cudaMalloc(&q, sizeof(int)) != cudaSuccess) return fail(set_err(LGAME_ERR_ALLOC, "cudaMalloc(flag) failed"));
+    c->allocations.push_back(q);
+    c->flag = (int*)q;
+  }
+  Grid<double>& G = c->G;
+  G.z_scalar = c->grid[LGAME_GRID_Z_SCALAR]; G.z_u = c->grid[LGAME_GRID_Z_U]; G.z_v = c->grid[LGAME_GRID_Z_V];
+  G.z_w = c->grid[LGAME_GRID_Z_W]; G.dx = c->grid[LGAME_GRID_DX]; G.dy = c->grid[LGAME_GRID_DY];
+  G.dz = c->grid[LGAME_GRID_DZ]; G.volume = c->grid[LGAME_GRID_VOLUME]; G.area_x = c->grid[LGAME_GRID_AREA_X];
+  G.area_y = c->grid[LGAME_GRID_AREA_Y]; G.area_z = c->grid[LGAME_GRID_AREA_Z];
+  G.area_dual_x = c->grid[LGAME_GRID_AREA_DUAL_X]; G.area_dual_y = c->grid[LGAME_GRID_AREA_DUAL_Y];
+  G.area_dual_z = c->grid[LGAME_GRID_AREA_DUAL_Z]; G.z_area_dual_z = c->grid[LGAME_GRID_Z_AREA_DUAL_Z];
+  G.slope_x = c->grid[LGAME_GRID_SLOPE_X]; G.slope_y = c->grid[LGAME_GRID_SLOPE_Y];
+  for (int k = 0; k < 6; ++k) G.ipw[k] = c->ipw[k];
+  G.theta_v_bg = c->grid[LGAME_GRID_THETA_V_BG]; G.exner_bg = c->grid[LGAME_GRID_EXNER_BG];
+  G.egu = c->grid[LGAME_GRID_EXNER_BG_GRAD_U]; G.egv = c->grid[LGAME_GRID_EXNER_BG_GRAD_V];
+  G.egw = c->grid[LGAME_GRID_EXNER_BG_GRAD_W]; G.gm = c->grid[LGAME_GRID_GRAVITY_M_V];
+  G.gp = c->grid[LGAME_GRID_GRAVITY_POTENTIAL]; G.fvec_x = c->grid[LGAME_GRID_FVEC_X];
+  G.fvec_y = c->grid[LGAME_GRID_FVEC_Y]; G.fvec_z = c->grid[LGAME_GRID_FVEC_Z];
+  for (int k = 0; k < 3; ++k) G.trsk_u[k] = c->trsk_u[k];
+  for (int k = 0; k < 2; ++k) G.trsk_v[k] = c->trsk_v[k];
+  G.damp = c->damp;
+  if (cfg->precision == LGAME_PRECISION_SPLIT) {
+    if ((rc = split_create(c->D, &c->split, &c->bytes)) != LGAME_OK) return fail(rc);
+  }
+  *out = c;
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfields) {
+  if (!c || !f || nfields != LGAME_GRID_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_grid: bad arguments");
+  for (int i = 0; i < nfields; ++i) if (!f[i]) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_grid: null field");
+  const Dims& D = c->D;
+  int rc;
+  for (int i = 0; i < LGAME_GRID_NFIELDS; ++i) {
+    if (i == LGAME_GRID_INNER_PRODUCT_WEIGHTS || i == LGAME_GRID_TRSK_WEIGHTS_U || i == LGAME_GRID_TRSK_WEIGHTS_V) continue;
+    if ((rc = copy_h2d(c, c->grid[i], f[i], grid_ext(D, i))) != LGAME_OK) return rc;
+  }
+  // inner product weights: (6,ny,nx,nl) -> six padded fields
+  CK(cudaMemcpyAsync(c->staging, f[LGAME_GRID_INNER_PRODUCT_WEIGHTS], 6 * sizeof(double) * (size_t)D.ny * D.nx * D.nl,
+                     cudaMemcpyHostToDevice, c->stream));
+  k_split_ipw<<<grd(D, D.ny, D.nx, D.nl), blk(), 0, c->stream>>>(D, c->staging, c->ipw[0], c->ipw[1], c->ipw[2],
+                                                                  c->ipw[3], c->ipw[4], c->ipw[5]);
+  CK(cudaGetLastError());
+  // TRSK weights (3,ny) and (2,ny+1)
+  std::vector<double> tmp((size_t)D.P, 0.0);
+  for (int k = 0; k < 3; ++k) {
+    for (int i = 0; i < D.ny; ++i) tmp[i] = f[LGAME_GRID_TRSK_WEIGHTS_U][3 * i + k];
+    CK(cudaMemcpyAsync(c->trsk_u[k], tmp.data(), sizeof(double) * D.P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  for (int k = 0; k < 2; ++k) {
+    for (int i = 0; i < D.ny + 1; ++i) tmp[i] = f[LGAME_GRID_TRSK_WEIGHTS_V][2 * i + k];
+    CK(cudaMemcpyAsync(c->trsk_v[k], tmp.data(), sizeof(double) * D.P, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  // Klemp damping prefactor at the w levels, mo_column_solvers.F90:187-196, evaluated on
+  // the host with the same expression as the reference (a grid-only quantity)
+  {
+    const double* zw = f[LGAME_GRID_Z_W];
+    const size_t ny = D.ny, nx = D.nx;
+    std::vector<double> dp(ny * nx * (D.nl + 1), 1.0);
+    const double dsh = c->cfg.klemp_begin_rel * c->cfg.toa;
+    for (int jl = 1; jl <= D.nl - 1; ++jl)
+      for (size_t jk = 0; jk < nx; ++jk)
+        for (size_t ji = 0; ji < ny; ++ji) {
+          const size_t i = ji + ny * (jk + nx * (size_t)jl);  // level jl+1 (0-based jl)
+          const double above = zw[i] - dsh;
+          double coeff;
+          if (above < 0.0 || !c->cfg.lklemp) {
+            coeff = 0.0;
+          } else {
+            const double s = std::sin(0.5 * 3.14159265358979323846 * above / (c->cfg.toa - dsh));
+            coeff = c->cfg.klemp_damp_max * (s * s);
+          }
+          dp[i] = 1.0 + coeff * c->cfg.dtime;
+        }
+    if ((rc = copy_h2d(c, c->damp, dp.data(), ext_w(D))) != LGAME_OK) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (c->split) {
+    if ((rc = split_set_grid(c->split, c->D, c->G, c->stream)) != LGAME_OK) return rc;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  c->grid_set = true;
+  return LGAME_OK;
+}
+
+namespace {
+int state_copy(lgame_gpu* c, int slot, double* const* hf, const double* const* cf, bool h2d) {
+  const Dims& D = c->D;
+  const State& S = c->st[slot];
+  double* dev[LGAME_STATE_NFIELDS] = {S.rho, S.rt, S.tp, S.ep, S.u, S.v, S.w};
+  const Ext ex[LGAME_STATE_NFIELDS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D)};
+  int rc;
+  for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+    const int nrep = (f == LGAME_STATE_RHO) ? D.ncons : 1;
+    const size_t hs = ex[f].n1 * ex[f].n2 * ex[f].n3;
+    for (int r = 0; r < nrep; ++r) {
+      double* d = dev[f] + (size_t)r * D.fstride;
+      if (h2d) {
+        if (!cf[f]) continue;
+        rc = copy_h2d(c, d, cf[f] + r * hs, ex[f]);
+      } else {
+        if (!hf[f]) continue;
+        rc = copy_d2h(c, hf[f] + r * hs, d, ex[f]);
+      }
+      if (rc != LGAME_OK) return rc;
+    }
+  }
+  return LGAME_OK;
+}
+}  // namespace
+
+extern "C" int lgame_gpu_set_state(lgame_gpu* c, int slot, const double* const* f, int nfields) {
+  if (!c || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_state: bad arguments");
+  int rc = state_copy(c, slot, nullptr, f, true);
+  if (rc != LGAME_OK) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_get_state(lgame_gpu* c, int slot, double* const* f, int nfields) {
+  if (!c || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_get_state: bad arguments");
+  int rc = state_copy(c, slot, f, nullptr, false);
+  if (rc != LGAME_OK) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+namespace {
+double* diag_dev(lgame_gpu* c, int f) {
+  switch (f) {
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_U: return c->pg_nl_u;
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_V: return c->pg_nl_v;
+    case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: return c->pg_nl_w;
+    case LGAME_DIAG_P_GRAD_ACC_NEG_L_U: return c->pg_l_u;
+    case LGAME_DIAG_P_GRAD_ACC_NEG_L_V: return c->pg_l_v;
+    case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: return c->pg_l_w;
+    case LGAME_DIAG_P_GRAD_ACC_OLD_U: return c->pg_old_u;
+    case LGAME_DIAG_P_GRAD_ACC_OLD_V: return c->pg_old_v;
+    case LGAME_DIAG_POT_VORT_TEND_X: return c->pvt_x;
+    case LGAME_DIAG_POT_VORT_TEND_Y: return c->pvt_y;
+    case LGAME_DIAG_POT_VORT_TEND_Z: return c->pvt_z;
+    case LGAME_DIAG_V_SQUARED_GRAD_X: return c->vsg_x;
+    case LGAME_DIAG_V_SQUARED_GRAD_Y: return c->vsg_y;
+    case LGAME_DIAG_V_SQUARED_GRAD_Z: return c->vsg_z;
+    case LGAME_DIAG_CONDENSATES_SEDIMENT_HEAT: return c->csh;
+    case LGAME_DIAG_RADIATION_TENDENCY: return c->rad;
+    case LGAME_DIAG_TEMPERATURE: return c->temperature;
+    case LGAME_DIAG_TEND_RHO: return c->tend.rho;
+    case LGAME_DIAG_TEND_RHOTHETA_V: return c->tend.rt;
+    case LGAME_DIAG_TEND_WIND_U: return c->tend.u;
+    case LGAME_DIAG_TEND_WIND_V: return c->tend.v;
+    case LGAME_DIAG_TEND_WIND_W: return c->tend.w;
+  }
+  return nullptr;
+}
+}  // namespace
+
+extern "C" int lgame_gpu_set_diag(lgame_gpu* c, const double* const* f, int nfields) {
+  if (!c || !f || nfields != LGAME_DIAG_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_diag: bad arguments");
+  const Dims& D = c->D;
+  for (int i = 0; i < nfields; ++i) {
+    if (!f[i]) continue;
+    const Ext e = diag_ext(D, i);
+    const int nrep = (i == LGAME_DIAG_TEND_RHO) ? D.ncons : 1;
+    for (int r = 0; r < nrep; ++r) {
+      int rc = copy_h2d(c, diag_dev(c, i) + (size_t)r * D.fstride, f[i] + r * e.n1 * e.n2 * e.n3, e);
+      if (rc != LGAME_OK) return rc;
+    }
+  }
+  if (c->split) {
+    int rc = split_sync_from_fp64(c->split, c->D, c->rad, c->stream);
+    if (rc != LGAME_OK) return rc;
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_get_diag(lgame_gpu* c, double* const* f, int nfields) {
+  if (!c || !f || nfields != LGAME_DIAG_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_get_diag: bad arguments");
+  const Dims& D = c->D;
+  for (int i = 0; i < nfields; ++i) {
+    if (!f[i]) continue;
+    const Ext e = diag_ext(D, i);
+    const int nrep = (i == LGAME_DIAG_TEND_RHO) ? D.ncons : 1;
+    for (int r = 0; r < nrep; ++r) {
+      int rc = copy_d2h(c, f[i] + r * e.n1 * e.n2 * e.n3, diag_dev(c, i) + (size_t)r * D.fstride, e);
+      if (rc != LGAME_OK) return rc;
+    }
+  }
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int total_step_counter, int lrad_update,
+                                double t_0) {
+  (void)lrad_update; (void)t_0;
+  if (!c || old_slot < 0 || old_slot > 1 || new_slot < 0 || new_slot > 1 || old_slot == new_slot || total_step_counter < 0)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi: bad arguments");
+  if (!c->grid_set) return set_err(LGAME_ERR_STATE, "lgame_gpu_pchevi: lgame_gpu_set_grid has not been called");
+  c->kernels_last_step = 0;
+  int rc;
+  if (c->split) {
+    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], c->tend, c->temperature, c->rad, c->csh,
+                    total_step_counter, c->stream, &c->kernels_last_step);
+  } else {
+    rc = step_fp64(c, old_slot, new_slot, total_step_counter);
+  }
+  if (rc != LGAME_OK) return rc;
+  if (c->cfg.check_finite) {
+    const Dims& D = c->D;
+    CK(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
+    k_check_finite<<<grd(D, D.ny + 1, D.nx + 1, D.NL), blk(), 0, c->stream>>>(D, c->st[new_slot], c->flag);
+    CK(cudaGetLastError());
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (h) return set_err(LGAME_ERR_NONFINITE, "non-finite value in the new state");
+  }
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_old, double* const* state_new,
+                                     int nfields, int total_step_counter, int lrad_update, double t_0) {
+  if (!c || !state_old || !state_new || nfields != LGAME_STATE_NFIELDS)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: bad arguments");
+  int rc = state_copy(c, 0, nullptr, state_old, true);
+  if (rc != LGAME_OK) return rc;
+  // state_new starts as a copy of state_old, as in the reference's time loop
+  for (int s = 0; s < 1; ++s) {
+    const Dims& D = c->D;
+    const State& A = c->st[0];
+    const State& B = c->st[1];
+    const size_t F = (size_t)D.fstride * sizeof(double);
+    CK(cudaMemcpyAsync(B.rho, A.rho, F * D.ncons, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.rt, A.rt, F, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.tp, A.tp, F, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.ep, A.ep, F, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.u, A.u, F, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.v, A.v, F, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaMemcpyAsync(B.w, A.w, F, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  rc = lgame_gpu_pchevi(c, 0, 1, total_step_counter, lrad_update, t_0);
+  if (rc != LGAME_OK) return rc;
+  rc = state_copy(c, 1, state_new, nullptr, false);
+  if (rc != LGAME_OK) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_budgets(lgame_gpu* c, int slot, double* out, int nout) {
+  if (!c || !out || slot < 0 || slot > 1) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_budgets: bad arguments");
+  const Dims& D = c->D;
+  const int nq = D.ncons + 4;
+  if (nout < nq) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_budgets: output too small");
+  k_budget_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(D, c->G, c->st[slot], c->temperature, c->reduce_buf, nq);
+  CK(cudaGetLastError());
+  double* dout = c->reduce_buf + (size_t)kRedBlocks * LGAME_BUDGETS_MAX;
+  k_budget_final<<<1, 32, 0, c->stream>>>(c->reduce_buf, dout, nq);
+  CK(cudaGetLastError());
+  std::vector<double> h(nq);
+  CK(cudaMemcpyAsync(h.data(), dout, sizeof(double) * nq, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < nq; ++k) out[k] = h[k];
+  out[D.ncons + 1] = 0.5 * out[D.ncons + 1];
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_synchronize(lgame_gpu* c) {
+  if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_synchronize: null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_kernels_per_step(const lgame_gpu* c) { return c ? c->kernels_last_step : 0; }
+
+extern "C" long long lgame_gpu_device_bytes(const lgame_gpu* c) { return c ? c->bytes : 0; }
+
+extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
+  if (!c) return;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->split) split_destroy(c->split);
+  for (void* p : c->allocations) cudaFree(p);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}

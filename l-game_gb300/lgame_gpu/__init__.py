@@ -1,0 +1,318 @@
+"""Python bindings of liblgame_gpu.so (ctypes over the C ABI of include/lgame_gpu.h and
+include/lgame_host.h).
+
+The library is the product: CUDA kernels for sm_103a behind a C ABI.  This module only
+marshals numpy arrays (Fortran order, the reference's extents) into it.  There is no
+fallback: if the shared library or a CUDA device is missing, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+_PKG = _HERE.parent
+LIB_PATH = _PKG / "_build" / "liblgame_gpu.so"
+
+# ---- status codes and enums (include/lgame_gpu.h) ------------------------------
+OK, ERR_INVALID_ARG, ERR_BAD_DIMS, ERR_BAD_CONFIG, ERR_UNSUPPORTED = 0, -1, -2, -3, -4
+ERR_ALLOC, ERR_CUDA, ERR_NONFINITE, ERR_NO_DEVICE, ERR_STATE = -5, -6, -7, -8, -9
+PRECISION_FP64, PRECISION_SPLIT = 0, 1
+
+GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "area_x", "area_y", "area_z",
+               "area_dual_x", "area_dual_y", "area_dual_z", "z_area_dual_z", "slope_x", "slope_y",
+               "inner_product_weights", "theta_v_bg", "exner_bg", "exner_bg_grad_u", "exner_bg_grad_v",
+               "exner_bg_grad_w", "gravity_m_v", "gravity_potential", "fvec_x", "fvec_y", "fvec_z",
+               "trsk_weights_u", "trsk_weights_v"]
+STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w"]
+DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_w", "p_grad_acc_neg_l_u",
+               "p_grad_acc_neg_l_v", "p_grad_acc_neg_l_w", "p_grad_acc_old_u", "p_grad_acc_old_v",
+               "pot_vort_tend_x", "pot_vort_tend_y", "pot_vort_tend_z", "v_squared_grad_x", "v_squared_grad_y",
+               "v_squared_grad_z", "condensates_sediment_heat", "radiation_tendency", "temperature",
+               "tend_rho", "tend_rhotheta_v", "tend_wind_u", "tend_wind_v", "tend_wind_w"]
+
+
+class Config(C.Structure):
+    """lgame_config (include/lgame_gpu.h)."""
+    _fields_ = [("ny", C.c_int), ("nx", C.c_int), ("n_layers", C.c_int), ("n_oro_layers", C.c_int),
+                ("dx", C.c_double), ("dy", C.c_double), ("toa", C.c_double), ("dtime", C.c_double),
+                ("theta_adv_order", C.c_int), ("llinear", C.c_int), ("lcorio", C.c_int),
+                ("luse_bg_state", C.c_int), ("lplane", C.c_int), ("lmoist", C.c_int), ("lklemp", C.c_int),
+                ("klemp_damp_max", C.c_double), ("klemp_begin_rel", C.c_double),
+                ("lmom_diff_h", C.c_int), ("lmom_diff_v", C.c_int), ("ltemp_diff_h", C.c_int),
+                ("ltemp_diff_v", C.c_int), ("lmass_diff_h", C.c_int), ("lmass_diff_v", C.c_int),
+                ("lprog_soil_temp", C.c_int), ("lsfc_sensible_heat_flux", C.c_int),
+                ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lperiodic", C.c_int),
+                ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int)]
+
+
+def _s(n):
+    return C.c_char * n
+
+
+class Namelist(C.Structure):
+    """lgame_namelist (include/lgame_host.h)."""
+    _fields_ = [
+        ("ny", C.c_int), ("nx", C.c_int), ("n_layers", C.c_int), ("n_oro_layers", C.c_int),
+        ("dy", C.c_double), ("dx", C.c_double), ("run_span_min", C.c_int), ("stretching_parameter", C.c_double),
+        ("theta_adv_order", C.c_int), ("toa", C.c_double), ("scenario", _s(64)), ("llinear", C.c_int),
+        ("run_id", _s(64)), ("lcorio", C.c_int), ("lat_center", C.c_double), ("lon_center", C.c_double),
+        ("start_year", C.c_int), ("start_month", C.c_int), ("start_day", C.c_int), ("start_hour", C.c_int),
+        ("start_minute", C.c_int), ("lplane", C.c_int), ("luse_bg_state", C.c_int),
+        ("dt_write_min", C.c_int), ("lread_geo", C.c_int), ("lwrite_grid", C.c_int),
+        ("grid_filename", _s(64)), ("restart_filename", _s(64)), ("lwrite_integrals", C.c_int),
+        ("lmoist", C.c_int),
+        ("lmom_diff_h", C.c_int), ("lmom_diff_v", C.c_int), ("ltemp_diff_h", C.c_int), ("ltemp_diff_v", C.c_int),
+        ("lmass_diff_h", C.c_int), ("lmass_diff_v", C.c_int), ("h_prandtl", C.c_double), ("karman", C.c_double),
+        ("lklemp", C.c_int), ("klemp_damp_max", C.c_double), ("klemp_begin_rel", C.c_double),
+        ("diff_coeff_scheme_h", _s(16)), ("diff_coeff_scheme_v", _s(16)), ("bg_shear", C.c_double),
+        ("c_s", C.c_double),
+        ("orography_id", C.c_int), ("lprog_soil_temp", C.c_int), ("nsoillays", C.c_int),
+        ("lsfc_sensible_heat_flux", C.c_int), ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lsleve", C.c_int),
+        ("n_swamp", C.c_int), ("lperiodic", C.c_int), ("lfreeslip", C.c_int), ("dtime_bc", C.c_int),
+        ("bc_root_filename", _s(64)),
+        ("lrad", C.c_int), ("dtime_rad", C.c_double), ("rrtmgp_coefficients_file_sw", _s(128)),
+        ("rrtmgp_coefficients_file_lw", _s(128)), ("cloud_coefficients_file_sw", _s(128)),
+        ("cloud_coefficients_file_lw", _s(128)),
+        ("precision", C.c_int), ("dtime_override", C.c_double), ("strict_reference", C.c_int),
+        ("seed", C.c_longlong), ("n_hills", C.c_int), ("hill_height_min", C.c_double),
+        ("hill_height_max", C.c_double), ("hill_width_min", C.c_double), ("hill_width_max", C.c_double),
+        ("jet_speed", C.c_double), ("jet_pressure", C.c_double), ("t_pert_sigma", C.c_double),
+        ("rh_mean", C.c_double), ("check_finite", C.c_int),
+        ("n_levels", C.c_int), ("n_flat_layers", C.c_int), ("n_condensed_constituents", C.c_int),
+        ("n_constituents", C.c_int), ("eff_hor_res", C.c_double), ("dtime", C.c_double), ("dt_write", C.c_double),
+        ("t_init", C.c_double)]
+
+
+class LgameError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None):
+    """Loads liblgame_gpu.so (built by l-game_gb300/build.py); raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: run `python l-game_gb300/build.py` (or __graft_entry__.build())")
+    lib = C.CDLL(str(p))
+    vp, i, d, ll = C.c_void_p, C.c_int, C.c_double, C.c_longlong
+    pp = C.POINTER(C.POINTER(C.c_double))
+    sig = {
+        "lgame_gpu_create": (i, [C.POINTER(Config), C.POINTER(vp)]),
+        "lgame_gpu_set_grid": (i, [vp, pp, i]),
+        "lgame_gpu_set_state": (i, [vp, i, pp, i]),
+        "lgame_gpu_get_state": (i, [vp, i, pp, i]),
+        "lgame_gpu_set_diag": (i, [vp, pp, i]),
+        "lgame_gpu_get_diag": (i, [vp, pp, i]),
+        "lgame_gpu_pchevi": (i, [vp, i, i, i, i, d]),
+        "lgame_gpu_pchevi_host": (i, [vp, pp, pp, i, i, i, d]),
+        "lgame_gpu_budgets": (i, [vp, i, C.POINTER(C.c_double), i]),
+        "lgame_gpu_synchronize": (i, [vp]),
+        "lgame_gpu_kernels_per_step": (i, [vp]),
+        "lgame_gpu_device_bytes": (ll, [vp]),
+        "lgame_gpu_destroy": (None, [vp]),
+        "lgame_gpu_last_error": (C.c_char_p, []),
+        "lgame_gpu_version": (C.c_char_p, []),
+        "lgame_namelist_defaults": (None, [C.POINTER(Namelist)]),
+        "lgame_namelist_parse": (i, [C.c_char_p, C.POINTER(Namelist)]),
+        "lgame_namelist_read_file": (i, [C.c_char_p, C.POINTER(Namelist)]),
+        "lgame_config_from_namelist": (i, [C.POINTER(Namelist), C.POINTER(Config)]),
+        "lgame_host_setup": (i, [C.POINTER(Namelist), C.POINTER(vp)]),
+        "lgame_host_destroy": (None, [vp]),
+        "lgame_host_grid_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
+        "lgame_host_state_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
+        "lgame_host_diag_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
+        "lgame_host_surface_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    return load_library().lgame_gpu_last_error().decode()
+
+
+def check(rc: int, what: str = ""):
+    if rc != OK:
+        raise LgameError(rc, f"{what}: {last_error()}")
+
+
+# ---- shapes (Fortran order, the reference's extents) ----------------------------
+def field_shapes(ny: int, nx: int, nl: int, ncons: int) -> dict[str, tuple]:
+    s, u, v, w = (ny, nx, nl), (ny, nx + 1, nl), (ny + 1, nx, nl), (ny, nx, nl + 1)
+    z, ex, ey = (ny + 1, nx + 1, nl), (ny + 1, nx, nl + 1), (ny, nx + 1, nl + 1)
+    return {
+        "z_scalar": s, "z_u": u, "z_v": v, "z_w": w, "dx": u, "dy": v, "dz": w, "volume": s,
+        "area_x": u, "area_y": v, "area_z": w, "area_dual_x": ex, "area_dual_y": ey, "area_dual_z": z,
+        "z_area_dual_z": z, "slope_x": u, "slope_y": v, "inner_product_weights": (6, ny, nx, nl),
+        "theta_v_bg": s, "exner_bg": s, "exner_bg_grad_u": u, "exner_bg_grad_v": v, "exner_bg_grad_w": w,
+        "gravity_m_v": w, "gravity_potential": s, "fvec_x": (ny + 1, nx), "fvec_y": (ny, nx + 1),
+        "fvec_z": (ny + 1, nx + 1), "trsk_weights_u": (3, ny), "trsk_weights_v": (2, ny + 1),
+        "rho": (ny, nx, nl, ncons), "rhotheta_v": s, "theta_v_pert": s, "exner_pert": s,
+        "wind_u": u, "wind_v": v, "wind_w": w,
+        "p_grad_acc_neg_nl_u": u, "p_grad_acc_neg_nl_v": v, "p_grad_acc_neg_nl_w": w,
+        "p_grad_acc_neg_l_u": u, "p_grad_acc_neg_l_v": v, "p_grad_acc_neg_l_w": w,
+        "p_grad_acc_old_u": u, "p_grad_acc_old_v": v, "pot_vort_tend_x": u, "pot_vort_tend_y": v,
+        "pot_vort_tend_z": w, "v_squared_grad_x": u, "v_squared_grad_y": v, "v_squared_grad_z": w,
+        "condensates_sediment_heat": s, "radiation_tendency": s, "temperature": s,
+        "tend_rho": (ny, nx, nl, ncons), "tend_rhotheta_v": s, "tend_wind_u": u, "tend_wind_v": v, "tend_wind_w": w,
+    }
+
+
+def ptr_array(arrays: list) -> C.Array:
+    """double** for a list of Fortran-ordered float64 arrays (None -> NULL)."""
+    arr = (C.POINTER(C.c_double) * len(arrays))()
+    for k, a in enumerate(arrays):
+        if a is None:
+            arr[k] = C.POINTER(C.c_double)()
+        else:
+            assert a.dtype == np.float64 and a.flags.f_contiguous, "arrays must be float64, Fortran-contiguous"
+            arr[k] = a.ctypes.data_as(C.POINTER(C.c_double))
+    return arr
+
+
+# ---- namelist -------------------------------------------------------------------
+def namelist_from_text(text: str, defaults: bool = True) -> Namelist:
+    lib = load_library()
+    n = Namelist()
+    if defaults:
+        lib.lgame_namelist_defaults(C.byref(n))
+    check(lib.lgame_namelist_parse(text.encode(), C.byref(n)), "lgame_namelist_parse")
+    return n
+
+
+def config_from_namelist(n: Namelist) -> Config:
+    c = Config()
+    check(load_library().lgame_config_from_namelist(C.byref(n), C.byref(c)), "lgame_config_from_namelist")
+    return c
+
+
+class HostModel:
+    """Grid, background state and idealised initial state built by the library's host code
+    (lgame_host_setup): the inputs a Fortran host would pass to the GPU step."""
+
+    def __init__(self, nml: Namelist):
+        self.lib = load_library()
+        self.nml = nml
+        self.h = C.c_void_p()
+        check(self.lib.lgame_host_setup(C.byref(nml), C.byref(self.h)), "lgame_host_setup")
+        self.ny, self.nx, self.nl = nml.ny, nml.nx, nml.n_layers
+        self.ncons = nml.n_constituents
+        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons)
+        self.grid = {f: self._view(self.lib.lgame_host_grid_field, k, f) for k, f in enumerate(GRID_FIELDS)}
+        self.state = {f: self._view(self.lib.lgame_host_state_field, k, f) for k, f in enumerate(STATE_FIELDS)}
+        self.diag = {f: self._view(self.lib.lgame_host_diag_field, k, f) for k, f in enumerate(DIAG_FIELDS)}
+        self.surface = {}
+        for k, name in enumerate(["oro", "sfc_albedo", "lat_geo_scalar", "lon_geo_scalar"]):
+            n = C.c_size_t()
+            p = self.lib.lgame_host_surface_field(self.h, k, C.byref(n))
+            self.surface[name] = np.ctypeslib.as_array(p, shape=(n.value,)).reshape((self.ny, self.nx), order="F")
+
+    def _view(self, fn, k, name):
+        n = C.c_size_t()
+        p = fn(self.h, k, C.byref(n))
+        shape = self.shapes[name]
+        assert int(np.prod(shape)) == n.value, (name, shape, n.value)
+        return np.ctypeslib.as_array(p, shape=(n.value,)).reshape(shape, order="F")
+
+    def copy_state(self) -> dict:
+        return {k: np.asfortranarray(v.copy(order="F")) for k, v in self.state.items()}
+
+    def copy_diag(self) -> dict:
+        return {k: np.asfortranarray(v.copy(order="F")) for k, v in self.diag.items()}
+
+    def close(self):
+        if self.h:
+            self.lib.lgame_host_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuModel:
+    """One GPU context (lgame_gpu_create) with the grid uploaded."""
+
+    def __init__(self, cfg: Config, grid: dict):
+        self.lib = load_library()
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        check(self.lib.lgame_gpu_create(C.byref(cfg), C.byref(self.h)), "lgame_gpu_create")
+        self.ny, self.nx, self.nl = cfg.ny, cfg.nx, cfg.n_layers
+        self.ncons = 7 if cfg.lmoist else 1
+        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons)
+        arrs = [np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
+        check(self.lib.lgame_gpu_set_grid(self.h, ptr_array(arrs), len(arrs)), "lgame_gpu_set_grid")
+
+    def set_state(self, slot: int, state: dict):
+        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in STATE_FIELDS]
+        check(self.lib.lgame_gpu_set_state(self.h, slot, ptr_array(arrs), len(arrs)), "lgame_gpu_set_state")
+
+    def get_state(self, slot: int) -> dict:
+        out = {f: np.zeros(self.shapes[f], order="F") for f in STATE_FIELDS}
+        check(self.lib.lgame_gpu_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]), 7),
+              "lgame_gpu_get_state")
+        return out
+
+    def set_diag(self, diag: dict):
+        arrs = [None if diag.get(f) is None else np.asfortranarray(diag[f], dtype=np.float64) for f in DIAG_FIELDS]
+        check(self.lib.lgame_gpu_set_diag(self.h, ptr_array(arrs), len(arrs)), "lgame_gpu_set_diag")
+
+    def get_diag(self) -> dict:
+        out = {f: np.zeros(self.shapes[f], order="F") for f in DIAG_FIELDS}
+        check(self.lib.lgame_gpu_get_diag(self.h, ptr_array([out[f] for f in DIAG_FIELDS]), len(DIAG_FIELDS)),
+              "lgame_gpu_get_diag")
+        return out
+
+    def pchevi(self, old_slot: int, new_slot: int, step: int, lrad_update: int = 0, t0: float = 0.0):
+        check(self.lib.lgame_gpu_pchevi(self.h, old_slot, new_slot, step, lrad_update, t0), "lgame_gpu_pchevi")
+
+    def pchevi_host(self, state_old: dict, state_new: dict, step: int):
+        a = [state_old[f] for f in STATE_FIELDS]
+        b = [state_new[f] for f in STATE_FIELDS]
+        check(self.lib.lgame_gpu_pchevi_host(self.h, ptr_array(a), ptr_array(b), 7, step, 0, 0.0),
+              "lgame_gpu_pchevi_host")
+
+    def budgets(self, slot: int) -> np.ndarray:
+        out = np.zeros(11)
+        check(self.lib.lgame_gpu_budgets(self.h, slot, out.ctypes.data_as(C.POINTER(C.c_double)), 11),
+              "lgame_gpu_budgets")
+        return out[: self.ncons + 4]
+
+    def synchronize(self):
+        check(self.lib.lgame_gpu_synchronize(self.h), "lgame_gpu_synchronize")
+
+    def kernels_per_step(self) -> int:
+        return self.lib.lgame_gpu_kernels_per_step(self.h)
+
+    def device_bytes(self) -> int:
+        return self.lib.lgame_gpu_device_bytes(self.h)
+
+    def close(self):
+        if self.h:
+            self.lib.lgame_gpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

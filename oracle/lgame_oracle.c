@@ -1,0 +1,275 @@
+/*
+ * lgame_oracle.c -- CPU FP64 restatement of L-GAME's HEVI time step (TEST INFRASTRUCTURE).
+ *
+ * Only tests/, the smoke check and bench.py's CPU-baseline leg load this file.  Each
+ * function restates the Fortran routine cited in its comment: same loop nests, same
+ * left-to-right evaluation order of every expression (Fortran evaluates a*b/c*d as
+ * ((a*b)/c)*d and -a*b as -(a*b)), same boundary branches, and the same "keep the
+ * previous value" behaviour of arrays that an operator does not write (all arrays
+ * start at zero as in src/control.F90:274-444).  Integer powers x**2, x**3, x**4 are
+ * written as x*x, (x*x)*x, (x*x)*(x*x), the multiplication chains gfortran emits.
+ * Compile with -O2 -ffp-contract=off so that no multiply-add is fused.
+ *
+ * Array layout: Fortran column-major with the reference's extents, 1-based index
+ * macros so that the code reads like the Fortran.
+ */
+#include "lgame_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- constants, src/mo_constants.F90:12-37 ------------------------------- */
+static const double r_e = 6371000.789927;
+static const double k_b = 1.380649e-23;
+static const double n_a = 6.02214076e23;
+static const double t_0 = 273.15;
+static const double rho_h2o = 1024.0;
+static const double r_d = 287.057811;
+static const double c_d_v = 717.942189;
+static const double c_v_v = 1396.475121;
+static const double c_d_p = 1005.0;
+#define M_D (6.02214076e23 * 0.004810e-23)  /* n_a*0.004810e-23_wp */
+#define M_V (6.02214076e23 * 0.002991e-23)  /* n_a*0.002991e-23_wp */
+#define IMPL_THERMO_WEIGHT (717.942189 / 1005.0)
+static const double M_PI_ = 3.14159265358979323846;  /* 4._wp*atan(1._wp) */
+
+struct oracle_ctx {
+  int ny, nx, nl, n_levels, n_oro_layers, n_flat_layers;
+  int nc;      /* n_condensed_constituents */
+  int ncons;   /* n_constituents */
+  int lmoist, lperiodic, lfreeslip, lcorio, llinear, luse_bg_state, lklemp, theta_adv_order;
+  double dtime, toa, dx, dy, klemp_damp_max, klemp_begin_rel;
+  /* grid */
+  double *z_scalar, *z_u, *z_v, *z_w, *gdx, *gdy, *gdz, *volume, *area_x, *area_y, *area_z;
+  double *area_dual_x, *area_dual_y, *area_dual_z, *z_area_dual_z, *slope_x, *slope_y, *ipw;
+  double *theta_v_bg, *exner_bg, *exner_bg_grad_u, *exner_bg_grad_v, *exner_bg_grad_w;
+  double *gravity_m_v, *gravity_potential, *fvec_x, *fvec_y, *fvec_z, *trsk_u, *trsk_v;
+  /* two states */
+  double *rho[2], *rhotheta_v[2], *theta_v_pert[2], *exner_pert[2], *wind_u[2], *wind_v[2], *wind_w[2];
+  /* tendencies */
+  double *t_rho, *t_rhotheta_v, *t_wind_u, *t_wind_v, *t_wind_w;
+  /* diagnostics */
+  double *v_squared, *pg_l_u, *pg_l_v, *pg_l_w, *pg_nl_u, *pg_nl_v, *pg_nl_w, *p_grad_condensates_w;
+  double *pg_old_u, *pg_old_v, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z;
+  double *scalar_placeholder, *temperature, *u_placeholder, *v_placeholder, *w_placeholder;
+  double *theta_v_u, *theta_v_v, *zeta_x, *zeta_y, *zeta_z, *eta_x, *eta_y, *eta_z;
+  double *radiation_tendency, *flux_density_u, *flux_density_v, *flux_density_div;
+  double *p_grad_decel_factor, *mom_diff_tend_x, *mom_diff_tend_y, *mom_diff_tend_z;
+  double *heating_diss, *phase_trans_rates, *phase_trans_heating_rate, *temp_diff_heating;
+  double *condensates_sediment_heat, *mass_diff_tendency, *a_rain;
+};
+
+/* extents */
+#define DIMS const int ny = o->ny, nx = o->nx, nl = o->nl; (void)ny; (void)nx; (void)nl
+#define IS(i,j,k) ((size_t)((i)-1) + (size_t)ny*((size_t)((j)-1) + (size_t)nx*(size_t)((k)-1)))
+#define IU(i,j,k) ((size_t)((i)-1) + (size_t)ny*((size_t)((j)-1) + (size_t)(nx+1)*(size_t)((k)-1)))
+#define IV(i,j,k) ((size_t)((i)-1) + (size_t)(ny+1)*((size_t)((j)-1) + (size_t)nx*(size_t)((k)-1)))
+#define IZ(i,j,k) ((size_t)((i)-1) + (size_t)(ny+1)*((size_t)((j)-1) + (size_t)(nx+1)*(size_t)((k)-1)))
+#define IRHO(i,j,k,c) (IS(i,j,k) + (size_t)ny*(size_t)nx*(size_t)nl*(size_t)((c)-1))
+#define IPW(n,i,j,k) ((size_t)((n)-1) + 6*IS(i,j,k))
+#define W(n,i,j,k) (o->ipw[IPW(n,i,j,k)])
+#define TRSKU(n,i) (o->trsk_u[(size_t)((n)-1) + 3*(size_t)((i)-1)])
+#define TRSKV(n,i) (o->trsk_v[(size_t)((n)-1) + 2*(size_t)((i)-1)])
+
+/* ---- allocation ---------------------------------------------------------- */
+static double* zalloc(size_t n) { return (double*)calloc(n ? n : 1, sizeof(double)); }
+
+int oracle_num_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
+  if (!cfg || !out) return LGAME_ERR_INVALID_ARG;
+  if (cfg->ny < 3 || cfg->nx < 3 || cfg->n_layers < 3 || cfg->n_oro_layers < 1 ||
+      cfg->n_oro_layers >= cfg->n_layers || cfg->n_layers > 250) return LGAME_ERR_BAD_DIMS;
+  if (cfg->theta_adv_order != 2 && cfg->theta_adv_order != 3) return LGAME_ERR_BAD_CONFIG;
+  oracle_ctx* o = (oracle_ctx*)calloc(1, sizeof(oracle_ctx));
+  if (!o) return LGAME_ERR_ALLOC;
+  o->ny = cfg->ny; o->nx = cfg->nx; o->nl = cfg->n_layers; o->n_levels = cfg->n_layers + 1;
+  o->n_oro_layers = cfg->n_oro_layers; o->n_flat_layers = cfg->n_layers - cfg->n_oro_layers;
+  o->lmoist = cfg->lmoist; o->nc = cfg->lmoist ? 5 : 0; o->ncons = o->nc + (cfg->lmoist ? 2 : 1);
+  o->lperiodic = cfg->lperiodic; o->lfreeslip = cfg->lfreeslip; o->lcorio = cfg->lcorio;
+  o->llinear = cfg->llinear; o->luse_bg_state = cfg->luse_bg_state; o->lklemp = cfg->lklemp;
+  o->theta_adv_order = cfg->theta_adv_order; o->dtime = cfg->dtime; o->toa = cfg->toa;
+  o->dx = cfg->dx; o->dy = cfg->dy; o->klemp_damp_max = cfg->klemp_damp_max;
+  o->klemp_begin_rel = cfg->klemp_begin_rel;
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
+  const size_t nW = (size_t)ny*nx*(nl+1), nZ = (size_t)(ny+1)*(nx+1)*nl;
+  const size_t nEX = (size_t)(ny+1)*nx*(nl+1), nEY = (size_t)ny*(nx+1)*(nl+1);
+  o->z_scalar = zalloc(nS); o->z_u = zalloc(nU); o->z_v = zalloc(nV); o->z_w = zalloc(nW);
+  o->gdx = zalloc(nU); o->gdy = zalloc(nV); o->gdz = zalloc(nW); o->volume = zalloc(nS);
+  o->area_x = zalloc(nU); o->area_y = zalloc(nV); o->area_z = zalloc(nW);
+  o->area_dual_x = zalloc(nEX); o->area_dual_y = zalloc(nEY); o->area_dual_z = zalloc(nZ);
+  o->z_area_dual_z = zalloc(nZ); o->slope_x = zalloc(nU); o->slope_y = zalloc(nV);
+  o->ipw = zalloc(6*nS); o->theta_v_bg = zalloc(nS); o->exner_bg = zalloc(nS);
+  o->exner_bg_grad_u = zalloc(nU); o->exner_bg_grad_v = zalloc(nV); o->exner_bg_grad_w = zalloc(nW);
+  o->gravity_m_v = zalloc(nW); o->gravity_potential = zalloc(nS);
+  o->fvec_x = zalloc((size_t)(ny+1)*nx); o->fvec_y = zalloc((size_t)ny*(nx+1));
+  o->fvec_z = zalloc((size_t)(ny+1)*(nx+1)); o->trsk_u = zalloc(3*(size_t)ny); o->trsk_v = zalloc(2*(size_t)(ny+1));
+  for (int s = 0; s < 2; ++s) {
+    o->rho[s] = zalloc(nS*o->ncons); o->rhotheta_v[s] = zalloc(nS); o->theta_v_pert[s] = zalloc(nS);
+    o->exner_pert[s] = zalloc(nS); o->wind_u[s] = zalloc(nU); o->wind_v[s] = zalloc(nV); o->wind_w[s] = zalloc(nW);
+  }
+  o->t_rho = zalloc(nS*o->ncons); o->t_rhotheta_v = zalloc(nS); o->t_wind_u = zalloc(nU);
+  o->t_wind_v = zalloc(nV); o->t_wind_w = zalloc(nW);
+  o->v_squared = zalloc(nS); o->pg_l_u = zalloc(nU); o->pg_l_v = zalloc(nV); o->pg_l_w = zalloc(nW);
+  o->pg_nl_u = zalloc(nU); o->pg_nl_v = zalloc(nV); o->pg_nl_w = zalloc(nW);
+  o->p_grad_condensates_w = zalloc(nW); o->pg_old_u = zalloc(nU); o->pg_old_v = zalloc(nV);
+  o->vsg_x = zalloc(nU); o->vsg_y = zalloc(nV); o->vsg_z = zalloc(nW);
+  o->pvt_x = zalloc(nU); o->pvt_y = zalloc(nV); o->pvt_z = zalloc(nW);
+  o->scalar_placeholder = zalloc(nS); o->temperature = zalloc(nS);
+  o->u_placeholder = zalloc(nU); o->v_placeholder = zalloc(nV); o->w_placeholder = zalloc(nW);
+  o->theta_v_u = zalloc(nU); o->theta_v_v = zalloc(nV);
+  o->zeta_x = zalloc(nEX); o->zeta_y = zalloc(nEY); o->zeta_z = zalloc(nZ);
+  o->eta_x = zalloc(nEX); o->eta_y = zalloc(nEY); o->eta_z = zalloc(nZ);
+  o->radiation_tendency = zalloc(nS); o->flux_density_u = zalloc(nU); o->flux_density_v = zalloc(nV);
+  o->flux_density_div = zalloc(nS); o->p_grad_decel_factor = zalloc(nS);
+  o->mom_diff_tend_x = zalloc(nU); o->mom_diff_tend_y = zalloc(nV); o->mom_diff_tend_z = zalloc(nW);
+  o->heating_diss = zalloc(nS); o->phase_trans_rates = zalloc(nS*(o->nc+1));
+  o->phase_trans_heating_rate = zalloc(nS); o->temp_diff_heating = zalloc(nS);
+  o->condensates_sediment_heat = zalloc(nS); o->mass_diff_tendency = zalloc(nS*o->ncons);
+  o->a_rain = zalloc(nS);
+  if (!o->a_rain || !o->mass_diff_tendency || !o->rho[1] || !o->ipw) { oracle_destroy(o); return LGAME_ERR_ALLOC; }
+  *out = o;
+  return LGAME_OK;
+}
+
+void oracle_destroy(oracle_ctx* o) {
+  if (!o) return;
+  double** p = &o->z_scalar;
+  double** end = &o->a_rain;
+  for (; p <= end; ++p) free(*p);
+  free(o);
+}
+
+/* sizes of the interface arrays, in the order of the lgame_gpu.h enums */
+static size_t grid_size(const oracle_ctx* o, int f) {
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
+  const size_t nW = (size_t)ny*nx*(nl+1), nZ = (size_t)(ny+1)*(nx+1)*nl;
+  switch (f) {
+    case LGAME_GRID_Z_SCALAR: case LGAME_GRID_VOLUME: case LGAME_GRID_THETA_V_BG:
+    case LGAME_GRID_EXNER_BG: case LGAME_GRID_GRAVITY_POTENTIAL: return nS;
+    case LGAME_GRID_Z_U: case LGAME_GRID_DX: case LGAME_GRID_AREA_X: case LGAME_GRID_SLOPE_X:
+    case LGAME_GRID_EXNER_BG_GRAD_U: return nU;
+    case LGAME_GRID_Z_V: case LGAME_GRID_DY: case LGAME_GRID_AREA_Y: case LGAME_GRID_SLOPE_Y:
+    case LGAME_GRID_EXNER_BG_GRAD_V: return nV;
+    case LGAME_GRID_Z_W: case LGAME_GRID_DZ: case LGAME_GRID_AREA_Z: case LGAME_GRID_EXNER_BG_GRAD_W:
+    case LGAME_GRID_GRAVITY_M_V: return nW;
+    case LGAME_GRID_AREA_DUAL_X: return (size_t)(ny+1)*nx*(nl+1);
+    case LGAME_GRID_AREA_DUAL_Y: return (size_t)ny*(nx+1)*(nl+1);
+    case LGAME_GRID_AREA_DUAL_Z: case LGAME_GRID_Z_AREA_DUAL_Z: return nZ;
+    case LGAME_GRID_INNER_PRODUCT_WEIGHTS: return 6*nS;
+    case LGAME_GRID_FVEC_X: return (size_t)(ny+1)*nx;
+    case LGAME_GRID_FVEC_Y: return (size_t)ny*(nx+1);
+    case LGAME_GRID_FVEC_Z: return (size_t)(ny+1)*(nx+1);
+    case LGAME_GRID_TRSK_WEIGHTS_U: return 3*(size_t)ny;
+    case LGAME_GRID_TRSK_WEIGHTS_V: return 2*(size_t)(ny+1);
+  }
+  return 0;
+}
+
+int oracle_set_grid(oracle_ctx* o, const double* const* f, int nfields) {
+  if (!o || !f || nfields != LGAME_GRID_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  double* dst[LGAME_GRID_NFIELDS] = {
+    o->z_scalar, o->z_u, o->z_v, o->z_w, o->gdx, o->gdy, o->gdz, o->volume, o->area_x, o->area_y,
+    o->area_z, o->area_dual_x, o->area_dual_y, o->area_dual_z, o->z_area_dual_z, o->slope_x,
+    o->slope_y, o->ipw, o->theta_v_bg, o->exner_bg, o->exner_bg_grad_u, o->exner_bg_grad_v,
+    o->exner_bg_grad_w, o->gravity_m_v, o->gravity_potential, o->fvec_x, o->fvec_y, o->fvec_z,
+    o->trsk_u, o->trsk_v};
+  for (int i = 0; i < LGAME_GRID_NFIELDS; ++i) {
+    if (!f[i]) return LGAME_ERR_INVALID_ARG;
+    memcpy(dst[i], f[i], grid_size(o, i)*sizeof(double));
+  }
+  return LGAME_OK;
+}
+
+static void state_ptrs(oracle_ctx* o, int s, double** p, size_t* n) {
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl;
+  p[0] = o->rho[s]; n[0] = nS*o->ncons;
+  p[1] = o->rhotheta_v[s]; n[1] = nS;
+  p[2] = o->theta_v_pert[s]; n[2] = nS;
+  p[3] = o->exner_pert[s]; n[3] = nS;
+  p[4] = o->wind_u[s]; n[4] = (size_t)ny*(nx+1)*nl;
+  p[5] = o->wind_v[s]; n[5] = (size_t)(ny+1)*nx*nl;
+  p[6] = o->wind_w[s]; n[6] = (size_t)ny*nx*(nl+1);
+}
+
+int oracle_set_state(oracle_ctx* o, int slot, const double* const* f, int nfields) {
+  if (!o || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  double* p[LGAME_STATE_NFIELDS]; size_t n[LGAME_STATE_NFIELDS];
+  state_ptrs(o, slot, p, n);
+  for (int i = 0; i < LGAME_STATE_NFIELDS; ++i) {
+    if (!f[i]) return LGAME_ERR_INVALID_ARG;
+    memcpy(p[i], f[i], n[i]*sizeof(double));
+  }
+  return LGAME_OK;
+}
+
+int oracle_get_state(oracle_ctx* o, int slot, double* const* f, int nfields) {
+  if (!o || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  double* p[LGAME_STATE_NFIELDS]; size_t n[LGAME_STATE_NFIELDS];
+  state_ptrs(o, slot, p, n);
+  for (int i = 0; i < LGAME_STATE_NFIELDS; ++i)
+    if (f[i]) memcpy(f[i], p[i], n[i]*sizeof(double));
+  return LGAME_OK;
+}
+
+static void diag_ptrs(oracle_ctx* o, double** p, size_t* n) {
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
+  const size_t nW = (size_t)ny*nx*(nl+1);
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_NL_U] = o->pg_nl_u; n[LGAME_DIAG_P_GRAD_ACC_NEG_NL_U] = nU;
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_NL_V] = o->pg_nl_v; n[LGAME_DIAG_P_GRAD_ACC_NEG_NL_V] = nV;
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_NL_W] = o->pg_nl_w; n[LGAME_DIAG_P_GRAD_ACC_NEG_NL_W] = nW;
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_L_U] = o->pg_l_u; n[LGAME_DIAG_P_GRAD_ACC_NEG_L_U] = nU;
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_L_V] = o->pg_l_v; n[LGAME_DIAG_P_GRAD_ACC_NEG_L_V] = nV;
+  p[LGAME_DIAG_P_GRAD_ACC_NEG_L_W] = o->pg_l_w; n[LGAME_DIAG_P_GRAD_ACC_NEG_L_W] = nW;
+  p[LGAME_DIAG_P_GRAD_ACC_OLD_U] = o->pg_old_u; n[LGAME_DIAG_P_GRAD_ACC_OLD_U] = nU;
+  p[LGAME_DIAG_P_GRAD_ACC_OLD_V] = o->pg_old_v; n[LGAME_DIAG_P_GRAD_ACC_OLD_V] = nV;
+  p[LGAME_DIAG_POT_VORT_TEND_X] = o->pvt_x; n[LGAME_DIAG_POT_VORT_TEND_X] = nU;
+  p[LGAME_DIAG_POT_VORT_TEND_Y] = o->pvt_y; n[LGAME_DIAG_POT_VORT_TEND_Y] = nV;
+  p[LGAME_DIAG_POT_VORT_TEND_Z] = o->pvt_z; n[LGAME_DIAG_POT_VORT_TEND_Z] = nW;
+  p[LGAME_DIAG_V_SQUARED_GRAD_X] = o->vsg_x; n[LGAME_DIAG_V_SQUARED_GRAD_X] = nU;
+  p[LGAME_DIAG_V_SQUARED_GRAD_Y] = o->vsg_y; n[LGAME_DIAG_V_SQUARED_GRAD_Y] = nV;
+  p[LGAME_DIAG_V_SQUARED_GRAD_Z] = o->vsg_z; n[LGAME_DIAG_V_SQUARED_GRAD_Z] = nW;
+  p[LGAME_DIAG_CONDENSATES_SEDIMENT_HEAT] = o->condensates_sediment_heat; n[LGAME_DIAG_CONDENSATES_SEDIMENT_HEAT] = nS;
+  p[LGAME_DIAG_RADIATION_TENDENCY] = o->radiation_tendency; n[LGAME_DIAG_RADIATION_TENDENCY] = nS;
+  p[LGAME_DIAG_TEMPERATURE] = o->temperature; n[LGAME_DIAG_TEMPERATURE] = nS;
+  p[LGAME_DIAG_TEND_RHO] = o->t_rho; n[LGAME_DIAG_TEND_RHO] = nS*o->ncons;
+  p[LGAME_DIAG_TEND_RHOTHETA_V] = o->t_rhotheta_v; n[LGAME_DIAG_TEND_RHOTHETA_V] = nS;
+  p[LGAME_DIAG_TEND_WIND_U] = o->t_wind_u; n[LGAME_DIAG_TEND_WIND_U] = nU;
+  p[LGAME_DIAG_TEND_WIND_V] = o->t_wind_v; n[LGAME_DIAG_TEND_WIND_V] = nV;
+  p[LGAME_DIAG_TEND_WIND_W] = o->t_wind_w; n[LGAME_DIAG_TEND_WIND_W] = nW;
+}
+
+int oracle_set_diag(oracle_ctx* o, const double* const* f, int nfields) {
+  if (!o || !f || nfields != LGAME_DIAG_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  double* p[LGAME_DIAG_NFIELDS]; size_t n[LGAME_DIAG_NFIELDS];
+  diag_ptrs(o, p, n);
+  for (int i = 0; i < LGAME_DIAG_NFIELDS; ++i)
+    if (f[i]) memcpy(p[i], f[i], n[i]*sizeof(double));
+  return LGAME_OK;
+}
+
+int oracle_get_diag(oracle_ctx* o, double* const* f, int nfields) {
+  if (!o || !f || nfields != LGAME_DIAG_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  double* p[LGAME_DIAG_NFIELDS]; size_t n[LGAME_DIAG_NFIELDS];
+  diag_ptrs(o, p, n);
+  for (int i = 0; i < LGAME_DIAG_NFIELDS; ++i)
+    if (f[i]) memcpy(f[i], p[i], n[i]*sizeof(double));
+  return LGAME_OK;
+}
+
+#include "lgame_oracle_ops.inc"
+#include "lgame_oracle_step.inc"

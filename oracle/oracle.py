@@ -1,0 +1,130 @@
+"""Python binding of the CPU oracle (TEST INFRASTRUCTURE).
+
+Loads oracle/_build/liblgame_oracle.so (built from oracle/ by `make -C oracle`).  Only the
+tests, the smoke check and the CPU-baseline leg of bench.py use this module; the GPU
+library never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "liblgame_oracle.so"
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    srcs = [HERE / "lgame_oracle.c", HERE / "lgame_oracle_ops.inc", HERE / "lgame_oracle_step.inc",
+            HERE / "lgame_oracle.h", HERE.parent / "include" / "lgame_gpu.h", HERE / "Makefile"]
+    if force or not LIB_PATH.exists() or any(s.stat().st_mtime > LIB_PATH.stat().st_mtime for s in srcs):
+        subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "all"], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = C.CDLL(str(LIB_PATH))
+        vp, i = C.c_void_p, C.c_int
+        pp = C.POINTER(C.POINTER(C.c_double))
+        from lgame_gpu import Config  # same struct layout (include/lgame_gpu.h)
+        for name, res, args in [
+            ("oracle_create", i, [C.POINTER(Config), C.POINTER(vp)]),
+            ("oracle_destroy", None, [vp]),
+            ("oracle_set_grid", i, [vp, pp, i]),
+            ("oracle_set_state", i, [vp, i, pp, i]),
+            ("oracle_get_state", i, [vp, i, pp, i]),
+            ("oracle_set_diag", i, [vp, pp, i]),
+            ("oracle_get_diag", i, [vp, pp, i]),
+            ("oracle_pchevi", i, [vp, i, i, i]),
+            ("oracle_budgets", i, [vp, i, C.POINTER(C.c_double), i]),
+            ("oracle_num_threads", i, []),
+            ("oracle_thomas", None, [C.POINTER(C.c_double)] * 5 + [i]),
+        ]:
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """The oracle's context, with the same calls as lgame_gpu.GpuModel."""
+
+    def __init__(self, cfg, grid: dict):
+        from lgame_gpu import GRID_FIELDS, field_shapes, ptr_array
+        self.lib = load()
+        self.h = C.c_void_p()
+        rc = self.lib.oracle_create(C.byref(cfg), C.byref(self.h))
+        if rc != 0:
+            raise RuntimeError(f"oracle_create failed: {rc}")
+        self.ncons = 7 if cfg.lmoist else 1
+        self.shapes = field_shapes(cfg.ny, cfg.nx, cfg.n_layers, self.ncons)
+        arrs = [np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
+        rc = self.lib.oracle_set_grid(self.h, ptr_array(arrs), len(arrs))
+        if rc != 0:
+            raise RuntimeError(f"oracle_set_grid failed: {rc}")
+
+    def set_state(self, slot, state):
+        from lgame_gpu import STATE_FIELDS, ptr_array
+        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in STATE_FIELDS]
+        assert self.lib.oracle_set_state(self.h, slot, ptr_array(arrs), len(arrs)) == 0
+
+    def get_state(self, slot):
+        from lgame_gpu import STATE_FIELDS, ptr_array
+        out = {f: np.zeros(self.shapes[f], order="F") for f in STATE_FIELDS}
+        assert self.lib.oracle_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]), 7) == 0
+        return out
+
+    def set_diag(self, diag):
+        from lgame_gpu import DIAG_FIELDS, ptr_array
+        arrs = [None if diag.get(f) is None else np.asfortranarray(diag[f], dtype=np.float64) for f in DIAG_FIELDS]
+        assert self.lib.oracle_set_diag(self.h, ptr_array(arrs), len(arrs)) == 0
+
+    def get_diag(self):
+        from lgame_gpu import DIAG_FIELDS, ptr_array
+        out = {f: np.zeros(self.shapes[f], order="F") for f in DIAG_FIELDS}
+        assert self.lib.oracle_get_diag(self.h, ptr_array([out[f] for f in DIAG_FIELDS]), len(DIAG_FIELDS)) == 0
+        return out
+
+    def pchevi(self, old_slot, new_slot, step):
+        rc = self.lib.oracle_pchevi(self.h, old_slot, new_slot, step)
+        if rc != 0:
+            raise RuntimeError(f"oracle_pchevi failed: {rc}")
+
+    def budgets(self, slot):
+        out = np.zeros(11)
+        assert self.lib.oracle_budgets(self.h, slot, out.ctypes.data_as(C.POINTER(C.c_double)), 11) == 0
+        return out[: self.ncons + 4]
+
+    def close(self):
+        if self.h:
+            self.lib.oracle_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def thomas(c, d, e, r):
+    """mo_column_solvers.F90:606-640 on numpy vectors (len(d) == n, len(c) == len(e) == n-1)."""
+    lib = load()
+    n = len(d)
+    c = np.ascontiguousarray(np.concatenate([c, [0.0]]), dtype=np.float64)
+    e = np.ascontiguousarray(np.concatenate([e, [0.0]]), dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    x = np.zeros(n)
+    P = C.POINTER(C.c_double)
+    lib.oracle_thomas(c.ctypes.data_as(P), d.ctypes.data_as(P), e.ctypes.data_as(P), r.ctypes.data_as(P),
+                      x.ctypes.data_as(P), n)
+    return x
