@@ -1,0 +1,430 @@
+"""Benchmark of the GB300 HEVI step: HEVI steps/s at 1024x1024x80 (moist, rotated lat-lon).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one pchevi call (two predictor-corrector substeps) over the whole domain.
+`value` is the device-resident step rate of the headline precision path (FP32/FP64 split
+when built, else FP64); the FP64 step is measured beside it.  `e2e` is the same step
+through the C ABI with host buffers (lgame_gpu_pchevi_host: state in from pinned host
+memory, new state back).  The per-kernel roofline comes from CUDA events the library
+records around every launch on its own stream.  The CPU baseline is the oracle (the
+FP64 restatement of the reference, the reference itself cannot be built here) on a
+bounded sub-domain of the same workload, scaled to the full domain by cell count.
+
+N > 1: the path is run as independent replicas, one per GPU (no collective exists in
+the reference's step); value = all replicas' steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for p in (ROOT / "l-game_gb300", ROOT / "tests"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+WORKLOAD = "jet_1024x1024x80"
+METRIC = "HEVI steps/s at 1024x1024x80, FP32/FP64 split vs FP64 at stated error; HBM GB/s"
+# cells of the CPU-baseline sample (same namelist, smaller horizontal extent)
+CPU_SAMPLE = dict(nx=128, ny=128)
+
+
+def read_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+# Algorithmic bytes per cell of one launch of the main kernels (8-byte fields that the
+# kernel must read or write once; SURVEY 8(d) counting applied kernel by kernel).
+# ncons = 7 constituents (moist).  Averages over the rk1/rk2 launches where they differ.
+def kernel_bytes_per_cell(name: str, ncons: int, split: bool) -> float:
+    w = 8.0
+    ntr = ncons - 1
+    table = {
+        # rho_g,rhotheta,exner',theta',w old; tend rho_g,rhotheta,w; (rk2: rho_g,rhotheta,exner' new)/2;
+        # grid volume,exner_bg,theta_bg,z,area_z,damp; writes rho_g,rhotheta,exner',theta',w
+        "k_column_ver": (5 + 3 + 1.5 + 6 + 5) * w,
+        "k_column_ver_s": (5 + 3 + 1.5 + 6 + 5) * w,
+        # per tracer rho old, tend, rho new; w old/new, T, volume, area_z, rho_g, gravity, 2 weights; csh r/w at rk1
+        "k_column_tracers": (3 * ntr + 9 + 1) * w,
+        "k_column_tracers_s": (3 * ntr + 9 + 1) * w,
+        # per tracer rho, tend r/w; u, v new; area_x, area_y, area_z, volume, slopes, 4 weights
+        "k_tracers": (3 * ntr + 2 + 10) * w,
+        "k_eta_z": (2 + 1 + 6 + 3) * w,
+        "k_eta_xy": (3 + 1 + 8 + 2) * w,
+        "k_vort_flux": (6 + 3 + 3 + 6 + 3) * w,
+        "k_gas_theta": (1 + 2 + 2 + 2 + 2 + 3 + 8 + 2) * w,
+        "k_pgrad": (ncons + 2 + 3 + 4 + 9 + 9) * w,
+        "k_tend_wind": (3 * 3 + 15) * w,
+    }
+    if split and name.endswith("_s") is False and name.startswith("ks_"):
+        return table.get(name[1:], 0.0)
+    return table.get(name, 0.0)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines: list[str] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[3 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+def dist_init(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo")
+        return dist
+    return None
+
+
+def reduce_max(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def time_steps(L, g, steps: int, first_step: int):
+    """Device time of `steps` consecutive pchevi calls, CUDA events on the library's stream."""
+    import torch
+    s = torch.cuda.ExternalStream(g.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    e0.record(s)
+    for k in range(first_step, first_step + steps):
+        g.pchevi(k % 2, (k + 1) % 2, k)
+    e1.record(s)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def cpu_baseline(nml_overrides: dict, seconds: float = 12.0, max_steps: int = 8) -> dict:
+    """The oracle (CPU FP64 restatement) on a sub-domain of the workload; steps/s scaled
+    to the full domain by the ratio of cells."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cases
+    import lgame_gpu as L
+    import oracle as O
+    full = cases.namelist(WORKLOAD)
+    n = cases.namelist(WORKLOAD, **nml_overrides)
+    hm = L.HostModel(n)
+    cfg = L.config_from_namelist(n)
+    o = O.Oracle(cfg, hm.grid)
+    o.set_state(0, hm.state)
+    o.set_state(1, hm.state)
+    o.set_diag(hm.diag)
+    o.pchevi(0, 1, 0)  # warm-up (first step includes the step-0 advection)
+    t0 = time.perf_counter()
+    k = 1
+    while True:
+        o.pchevi(k % 2, (k + 1) % 2, k)
+        k += 1
+        el = time.perf_counter() - t0
+        if el > seconds or k > max_steps:
+            break
+    per_step = el / (k - 1)
+    cells_s = n.nx * n.ny * n.n_layers
+    cells_f = full.nx * full.ny * full.n_layers
+    return {"value": 1.0 / (per_step * cells_f / cells_s), "unit": "steps/s", "cores": O.load().oracle_num_threads(),
+            "kind": "port", "sample": f"{k - 1} oracle steps of the {n.nx}x{n.ny}x{n.n_layers} sub-domain of the same "
+                                      f"workload ({per_step:.3f} s/step), scaled by cells x{cells_f / cells_s:.0f}",
+            "sample_s_per_step": per_step}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    dist = dist_init(ws)
+    if rank != 0:
+        barrier(dist)
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import cases
+    import lgame_gpu as L
+    import oracle as O
+    full = cases.namelist(WORKLOAD)
+    n = cases.namelist(WORKLOAD, **CPU_SAMPLE)
+    hm = L.HostModel(n)
+    cfg = L.config_from_namelist(n)
+    o = O.Oracle(cfg, hm.grid)
+    o.set_state(0, hm.state)
+    o.set_state(1, hm.state)
+    o.set_diag(hm.diag)
+    for k in range(args.warmup):
+        o.pchevi(k % 2, (k + 1) % 2, k)
+    t0 = time.perf_counter()
+    for k in range(args.warmup, args.warmup + args.steps):
+        o.pchevi(k % 2, (k + 1) % 2, k)
+    el = time.perf_counter() - t0
+    scale = (full.nx * full.ny * full.n_layers) / (n.nx * n.ny * n.n_layers)
+    value = args.steps / (el * scale)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{WORKLOAD} moist baroclinic jet, rotated lat-lon, dx=2.5 km",
+                       "sample": f"{n.nx}x{n.ny}x{n.n_layers} sub-domain per step, scaled by cells x{scale:.0f}",
+                       "input_vs_l2": "inputs larger than L2 (CPU run)"},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": O.load().oracle_num_threads(),
+                             "kind": "port",
+                             "sample": f"oracle pchevi on {n.nx}x{n.ny}x{n.n_layers}, {args.steps} steps"},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "gpu_launches": 0}
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak_gbs: float, split: bool):
+    g.set_profiling(True)
+    for k in range(first_step, first_step + steps):
+        g.pchevi(k % 2, (k + 1) % 2, k)
+    rep = g.profile_report()
+    g.set_profiling(False)
+    total = sum(v["ms"] for v in rep.values())
+    rows = sorted(rep.items(), key=lambda kv: -kv[1]["ms"])
+    top = rows[0]
+    name, st = top[0], top[1]
+    avg_ms = st["ms"] / st["launches"]
+    bpc = kernel_bytes_per_cell(name, ncons, split)
+    alg = bpc * cells
+    achieved = alg / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
+    shares = {k: round(v["ms"] / total, 4) for k, v in rows}
+    return {"kernel": name, "avg_launch_ms": avg_ms, "alg_bytes_per_launch": alg, "achieved_gbs": achieved,
+            "frac": achieved / peak_gbs, "shares": shares, "rows": rows}
+
+
+def run_ours(args):
+    import torch
+    import cases
+    import lgame_gpu as L
+    ws, rank, lrank = dist_info()
+    dist = dist_init(ws)
+    peaks = read_peaks()
+    t_setup = time.perf_counter()
+    n = cases.namelist(WORKLOAD, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    hm = L.HostModel(n)
+    t_setup = time.perf_counter() - t_setup
+    cells = n.nx * n.ny * n.n_layers
+    ncons = n.n_constituents
+    results = {}
+    precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64] if not args.fp64_only else [L.PRECISION_FP64]
+    clocks = None
+    for prec in precisions:
+        cfg = L.config_from_namelist(n)
+        cfg.precision = prec
+        cfg.device = lrank
+        try:
+            g = L.GpuModel(cfg, hm.grid)
+        except L.LgameError as e:
+            if e.code == L.ERR_UNSUPPORTED:
+                continue
+            raise
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        for k in range(args.warmup):
+            g.pchevi(k % 2, (k + 1) % 2, k)
+        g.synchronize()
+        barrier(dist)
+        sampler = ClockSampler(lrank) if clocks is None else None
+        if sampler:
+            sampler.__enter__()
+        el = time_steps(L, g, args.steps, args.warmup)
+        if sampler:
+            sampler.__exit__()
+            clocks = sampler.summary()
+        barrier(dist)
+        el = reduce_max(dist, el)
+        nk = g.kernels_per_step()
+        prof = profile_kernels(g, 2, args.warmup + args.steps, ncons, cells, peaks["hbm_gbs"],
+                               prec == L.PRECISION_SPLIT)
+        st = g.get_state((args.warmup + args.steps + 2) % 2)
+        finite = all(bool(np.isfinite(v).all()) for v in st.values())
+        results[prec] = {"s_per_step": el / args.steps, "kernels_per_step": nk, "profile": prof, "finite": finite,
+                         "device_gb": g.device_bytes() / 1e9, "model": g}
+        if prec == precisions[0] or len(results) == 1:
+            # end to end through the C ABI with pinned host buffers
+            e2e = measure_e2e(L, g, hm, args)
+            results[prec]["e2e"] = e2e
+        g.close()
+        results[prec].pop("model")
+        torch.cuda.synchronize()
+    if not results:
+        raise RuntimeError("no precision path available")
+    head_prec = L.PRECISION_SPLIT if L.PRECISION_SPLIT in results else L.PRECISION_FP64
+    head = results[head_prec]
+    value = ws * 1.0 / head["s_per_step"]
+    prof = head["profile"]
+    fp64 = results.get(L.PRECISION_FP64)
+    line = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": head["s_per_step"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32/f64 split" if head_prec == L.PRECISION_SPLIT else "f64",
+        "data": "synthetic (seeded moist baroclinic jet over seeded hills; no dataset)",
+        "config": {"workload": f"{WORKLOAD}: moist, 7 constituents, rotated lat-lon, dx=2.5 km, theta_adv_order 3, "
+                               f"dtime {n.dtime:.3f} s", "nx": n.nx, "ny": n.ny, "n_layers": n.n_layers,
+                   "cells": cells, "input_vs_l2": "inputs larger than L2 (device working set "
+                                                  f"{head['device_gb']:.1f} GB)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU", "setup_s": round(t_setup, 1)},
+        "column_updates_per_s": value * n.nx * n.ny,
+        "roofline": {"bound": "hbm", "kernel": prof["kernel"], "achieved": prof["achieved_gbs"],
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": prof["frac"], "traffic": None,
+                     "peak_src": peaks["src"], "avg_launch_ms": prof["avg_launch_ms"],
+                     "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"]},
+        "step_roofline": {"alg_bytes_per_step": 1304.0 * cells if ncons > 1 else 952.0 * cells,
+                          "achieved_gbs": (1304.0 if ncons > 1 else 952.0) * cells / head["s_per_step"] / 1e9,
+                          "peak_gbs": peaks["hbm_gbs"]},
+        "gpu_launches": head["kernels_per_step"] * args.steps,
+        "clocks": clocks,
+        "finite": head["finite"],
+    }
+    if fp64 is not None:
+        line["fp64"] = {"value": ws / fp64["s_per_step"], "ms_per_step": fp64["s_per_step"] * 1e3,
+                        "kernels_per_step": fp64["kernels_per_step"], "top_kernel": fp64["profile"]["kernel"],
+                        "kernel_shares": fp64["profile"]["shares"]}
+        if head_prec != L.PRECISION_FP64:
+            line["split_speedup_vs_fp64"] = fp64["s_per_step"] / head["s_per_step"]
+    if "e2e" in head:
+        line["e2e"] = head["e2e"]
+    else:
+        for r in results.values():
+            if "e2e" in r:
+                line["e2e"] = r["e2e"]
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(CPU_SAMPLE)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def measure_e2e(L, g, hm, args) -> dict:
+    """Steps through lgame_gpu_pchevi_host: every step copies the state in from pinned host
+    memory and the new state back."""
+    import torch
+
+    def pinned_like(a: np.ndarray) -> np.ndarray:
+        t = torch.empty(a.shape[::-1], dtype=torch.float64, pin_memory=True)
+        v = t.numpy().T  # Fortran-ordered view of the pinned buffer
+        v[...] = a
+        return v, t
+
+    keep = []
+    old, new = {}, {}
+    for f in L.STATE_FIELDS:
+        a, t = pinned_like(hm.state[f])
+        b, t2 = pinned_like(np.zeros_like(hm.state[f], order="F"))
+        keep += [t, t2]
+        old[f], new[f] = a, b
+    h2d = sum(v.nbytes for v in old.values())
+    d2h = sum(v.nbytes for v in new.values())
+    k_e2e = max(2, min(args.steps, 5))
+    g.pchevi_host(old, new, 1)  # warm-up
+    g.synchronize()
+    t0 = time.perf_counter()
+    for k in range(k_e2e):
+        g.pchevi_host(old, new, k + 1)
+    el = time.perf_counter() - t0
+    return {"value": k_e2e / el, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": k_e2e, "note": "lgame_gpu_pchevi_host: pinned host state in, new state out, every step"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-only", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nx", type=int, default=0, help="override nx=ny (smaller runs for testing)")
+    ap.add_argument("--ny", type=int, default=0)
+    args = ap.parse_args()
+    if args.nx and not args.ny:
+        args.ny = args.nx
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+    import __graft_entry__
+    __graft_entry__.build()
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

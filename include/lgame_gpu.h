@@ -81,6 +81,7 @@ typedef struct lgame_config {
   /* extension: precision and checks (no reference counterpart) */
   int    precision;             /* LGAME_PRECISION_* */
   int    check_finite;          /* 1: scan the new state for NaN/Inf after every step */
+  int    device;                /* CUDA device ordinal the context lives on          */
 } lgame_config;
 
 /* ---- grid arrays (t_grid, src/mo_definitions.F90:29-91) --------------------
@@ -222,6 +223,19 @@ int  lgame_gpu_synchronize(lgame_gpu* ctx);
 
 /* Number of kernels launched by the last lgame_gpu_pchevi call. */
 int  lgame_gpu_kernels_per_step(const lgame_gpu* ctx);
+
+/* The CUDA stream (cudaStream_t) on which the context launches all its work, so that a
+ * host can record its own CUDA events around the step.  Tracing aid; no reference
+ * counterpart (the reference's only instrumentation is cpu_time, control.F90:545-547). */
+void* lgame_gpu_stream(const lgame_gpu* ctx);
+
+/* Per-kernel tracing: when enabled, every kernel launch of the step is bracketed by a
+ * pair of CUDA events on the context's stream.  lgame_gpu_profile_report synchronises,
+ * writes a JSON object {"kernel name": {"launches": n, "ms": total}, ...} accumulated
+ * since the last report (or since tracing was enabled) into buf, and resets the counts.
+ * Returns the length of the JSON text (or the length needed if len is too small). */
+int  lgame_gpu_set_profiling(lgame_gpu* ctx, int enable);
+int  lgame_gpu_profile_report(lgame_gpu* ctx, char* buf, int len);
 
 /* Bytes of device memory held by the context. */
 long long lgame_gpu_device_bytes(const lgame_gpu* ctx);

@@ -24,7 +24,7 @@ LIB = OUT / "liblgame_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
                f"-I{ROOT / 'include'}", f"-I{CSRC}", "--expt-relaxed-constexpr"]
-CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+CXX_COMMON = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-fopenmp",
               f"-I{ROOT / 'include'}", f"-I{CSRC}"]
 
 # (source, extra flags)
@@ -87,7 +87,8 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             if rc != 0:
                 raise RuntimeError(f"compilation failed: {' '.join(cmd[-3:])}")
     tmp = OUT / "liblgame_gpu.so.tmp"
-    cmd, rc, out = _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "static"])
+    cmd, rc, out = _run([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-cudart", "static",
+                         "-Xcompiler", "-fopenmp"])
     if verbose or rc != 0:
         sys.stderr.write(" ".join(cmd) + "\n" + out)
     if rc != 0:

@@ -138,10 +138,12 @@ double geopot(const M& m, double h) {
 // ---- host operators used by the set-up (mo_gradient_operators.F90) -----------
 void grad_hor_cov(M& m, const Vec& s, Vec& rx, Vec& ry) {
   const int ny = m.ny, nx = m.nx, nl = m.nl;
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 2; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji)
         rx[m.IU(ji, jk, jl)] = (s[m.IS(ji, jk, jl)] - s[m.IS(ji, jk - 1, jl)]) / m.dx[m.IU(ji, jk, jl)];
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 2; ji <= ny; ++ji)
@@ -160,6 +162,7 @@ void grad_hor_cov(M& m, const Vec& s, Vec& rx, Vec& ry) {
   }
 }
 void grad_vert(M& m, const Vec& s, Vec& rz) {
+#pragma omp parallel for schedule(static)
   for (int jl = 2; jl <= m.nl; ++jl)
     for (int jk = 1; jk <= m.nx; ++jk)
       for (int ji = 1; ji <= m.ny; ++ji)
@@ -209,10 +212,12 @@ double remap_y(M& m, const Vec& vc, int ji, int jk, int jl) {  // mo_averaging.F
 }
 void grad_hor(M& m, const Vec& s, Vec& rx, Vec& ry, const Vec& rz) {
   grad_hor_cov(m, s, rx, ry);
+#pragma omp parallel for schedule(static)
   for (int jl = m.nf + 1; jl <= m.nl; ++jl)
     for (int jk = 1; jk <= m.nx + 1; ++jk)
       for (int ji = 1; ji <= m.ny; ++ji)
         rx[m.IU(ji, jk, jl)] = rx[m.IU(ji, jk, jl)] - m.slope_x[m.IU(ji, jk, jl)] * remap_x(m, rz, ji, jk, jl);
+#pragma omp parallel for schedule(static)
   for (int jl = m.nf + 1; jl <= m.nl; ++jl)
     for (int jk = 1; jk <= m.nx; ++jk)
       for (int ji = 1; ji <= m.ny + 1; ++ji)
@@ -409,9 +414,11 @@ int grid_setup(M& m) {
   // vertical grid, :894-951
   double max_oro = -1e300;
   for (double v : m.oro) max_oro = std::fmax(max_oro, v);
-  std::vector<double> vvp(NL + 1);
+  int vgrid_err = 0;
+#pragma omp parallel for schedule(static) reduction(|:vgrid_err)
   for (int jk = 1; jk <= nx; ++jk)
     for (int ji = 1; ji <= ny; ++ji) {
+      std::vector<double> vvp(NL + 1);
       const double zsurf = m.z_w[m.IS(ji, jk, NL)];
       const double os = m.oro_smoothed[m.I2(ji, jk)];
       for (int jl = 1; jl <= NL; ++jl) {
@@ -435,14 +442,17 @@ int grid_setup(M& m) {
         } else {
           vvp[jl] = A;
         }
-        if (jl > 1 && vvp[jl] >= vvp[jl - 1])
-          return fail(LGAME_ERR_BAD_CONFIG, "Problem in vertical grid generation. You might have to change SLEVE parameters.");
+        if (jl > 1 && vvp[jl] >= vvp[jl - 1]) vgrid_err |= 1;
       }
-      if (ji == 1 && jk == 1 && max_oro >= vvp[nf + 1])
-        return fail(LGAME_ERR_BAD_CONFIG, "Maximum of orography larger or equal to the height of the lowest flat level.");
+      if (ji == 1 && jk == 1 && max_oro >= vvp[nf + 1]) vgrid_err |= 2;
       for (int jl = 1; jl <= nl; ++jl) m.z_scalar[m.IS(ji, jk, jl)] = 0.5 * (vvp[jl] + vvp[jl + 1]);
     }
+  if (vgrid_err & 1)
+    return fail(LGAME_ERR_BAD_CONFIG, "Problem in vertical grid generation. You might have to change SLEVE parameters.");
+  if (vgrid_err & 2)
+    return fail(LGAME_ERR_BAD_CONFIG, "Maximum of orography larger or equal to the height of the lowest flat level.");
   // z_u, z_v, :953-991
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int ji = 1; ji <= ny; ++ji) {
       for (int jk = 2; jk <= nx; ++jk)
@@ -455,6 +465,7 @@ int grid_setup(M& m) {
         m.z_u[m.IU(ji, nx + 1, jl)] = m.z_scalar[m.IS(ji, nx, jl)] + 0.5 * (m.z_scalar[m.IS(ji, nx, jl)] - m.z_scalar[m.IS(ji, nx - 1, jl)]);
       }
     }
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk) {
       for (int ji = 2; ji <= ny; ++ji)
@@ -468,10 +479,12 @@ int grid_setup(M& m) {
       }
     }
   // dx, dy, :993-1010
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx + 1; ++jk)
       for (int ji = 1; ji <= ny; ++ji)
         m.dx[m.IU(ji, jk, jl)] = n.lplane ? n.dx : n.dx * std::cos(m.lat_scalar[ji - 1]) * (r_e + m.z_u[m.IU(ji, jk, jl)]) / r_e;
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny + 1; ++ji)
@@ -479,11 +492,13 @@ int grid_setup(M& m) {
   // slopes, :1036
   grad_hor_cov(m, m.z_scalar, m.slope_x, m.slope_y);
   // z_w, :1039-1047
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji)
         m.z_w[m.IS(ji, jk, jl)] = (jl == 1) ? n.toa : 0.5 * (m.z_scalar[m.IS(ji, jk, jl - 1)] + m.z_scalar[m.IS(ji, jk, jl)]);
   // dz, :1068-1078
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= NL; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -499,6 +514,7 @@ int grid_setup(M& m) {
       const double s = r_e + m.z_w[m.IS(ji, jk, NL)];
       m.area_z[m.IS(ji, jk, NL)] = patch_area(m, m.lat_scalar[ji - 1], dlon, dlat) * (s * s) / (r_e * r_e);
     }
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -508,6 +524,7 @@ int grid_setup(M& m) {
   if (n.lplane)
     for (auto& v : m.area_z) v = n.dx * n.dy;
   // vertical areas in x-direction, :1114-1140
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx + 1; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -527,6 +544,7 @@ int grid_setup(M& m) {
         m.area_x[m.IU(ji, jk, jl)] = vertical_face_area(m, lz, uz, ll);
       }
   // vertical areas in y-direction, :1143-1173
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny + 1; ++ji) {
@@ -548,6 +566,7 @@ int grid_setup(M& m) {
         m.area_y[m.IV(ji, jk, jl)] = vertical_face_area(m, lz, uz, ll);
       }
   // horizontal dual areas, :1176-1206
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx + 1; ++jk)
       for (int ji = 1; ji <= ny + 1; ++ji) {
@@ -564,6 +583,7 @@ int grid_setup(M& m) {
         m.area_dual_z[m.IZ(ji, jk, jl)] = a;
       }
   // vertical dual areas in x-direction, :1209-1245 (extents (ny+1,nx,nl+1))
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= NL; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny + 1; ++ji) {
@@ -588,6 +608,7 @@ int grid_setup(M& m) {
         m.area_dual_x[m.IV(ji, jk, jl)] = vertical_face_area(m, lz, uz, ll);
       }
   // vertical dual areas in y-direction, :1248-1284 (extents (ny,nx+1,nl+1))
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= NL; ++jl)
     for (int jk = 1; jk <= nx + 1; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -612,6 +633,7 @@ int grid_setup(M& m) {
         m.area_dual_y[m.IU(ji, jk, jl)] = vertical_face_area(m, lz, uz, ll);
       }
   // volumes, :1287-1296
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -621,6 +643,7 @@ int grid_setup(M& m) {
         m.volume[m.IS(ji, jk, jl)] = v;
       }
   // inner product weights, :1302-1315
+#pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= nl; ++jl)
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji) {
@@ -658,15 +681,16 @@ int grid_setup(M& m) {
 // ---- bg_setup, mo_grid_generator.F90:1389-1457 --------------------------------
 int bg_setup(M& m) {
   const int ny = m.ny, nx = m.nx, nl = m.nl;
+  int pres_err = 0;
+#pragma omp parallel for schedule(static) reduction(|:pres_err)
   for (int jk = 1; jk <= nx; ++jk)
     for (int ji = 1; ji <= ny; ++ji)
       for (int jl = nl; jl >= 1; --jl) {
         const size_t i = m.IS(ji, jk, jl);
         m.gravity_potential[i] = geopot(m, m.z_scalar[i]);
         if (jl == nl) {
-          double p;
-          if (!bg_pres(m.z_scalar[i], &p))
-            return fail(LGAME_ERR_BAD_CONFIG, "Argument of bg_pres is above the inversion height. This is unrealistic in the lowest layer.");
+          double p = p_0;
+          if (!bg_pres(m.z_scalar[i], &p)) pres_err = 1;
           m.exner_bg[i] = std::pow(p / p_0, r_d / c_d_p);
         } else {
           const size_t ib = m.IS(ji, jk, jl + 1);
@@ -677,6 +701,8 @@ int bg_setup(M& m) {
         }
         m.theta_v_bg[i] = bg_temp(m.z_scalar[i]) / m.exner_bg[i];
       }
+  if (pres_err)
+    return fail(LGAME_ERR_BAD_CONFIG, "Argument of bg_pres is above the inversion height. This is unrealistic in the lowest layer.");
   grad_vert(m, m.exner_bg, m.exner_bg_grad_w);
   grad_hor(m, m.exner_bg, m.exner_bg_grad_u, m.exner_bg_grad_v, m.exner_bg_grad_w);
   if (!m.nml.luse_bg_state) {
@@ -707,6 +733,7 @@ void w_free_slip(M& m) {
 void unessential_ideal_init(M& m, const Vec& sp, const Vec& pres_lowest) {
   const int ny = m.ny, nx = m.nx, nl = m.nl, g = m.nml.n_condensed_constituents + 1;
   const size_t nS = (size_t)ny * nx * nl;
+#pragma omp parallel for schedule(static)
   for (int jk = 1; jk <= nx; ++jk)
     for (int ji = 1; ji <= ny; ++ji)
       for (int jl = nl; jl >= 1; --jl) {
@@ -722,6 +749,7 @@ void unessential_ideal_init(M& m, const Vec& sp, const Vec& pres_lowest) {
         }
         m.theta_v_pert[i] = sp[i] / m.exner_pert[i];
       }
+#pragma omp parallel for schedule(static)
   for (size_t i = 0; i < nS; ++i) {
     m.rho[i + nS * (size_t)(g - 1)] = p_0 * std::pow(m.exner_pert[i], c_d_p / r_d) / (r_d * sp[i]);
     m.rhotheta_v[i] = m.rho[i + nS * (size_t)(g - 1)] * m.theta_v_pert[i];
@@ -835,19 +863,31 @@ int ideal_init(M& m) {
     }
     const double amp = n.t_pert_sigma * std::sqrt(2.0 / nmodes);  // each cos mode has variance amp^2/2
     Vec qv(nS, 0.0);
+    // horizontal structure of the perturbation, one value per column
+    Vec tcol((size_t)ny * nx, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int jk = 1; jk <= nx; ++jk)
+      for (int ji = 1; ji <= ny; ++ji) {
+        double tp = 0.0;
+        for (int q = 0; q < nmodes; ++q)
+          tp += std::cos(2.0 * M_PI_ * (kx[q] * (jk - 0.5) / nx + ky[q] * (ji - 0.5) / ny) + ph[q]);
+        tcol[m.I2(ji, jk)] = tp;
+      }
+    const uint64_t seed_h = (uint64_t)n.seed * 0x2545F4914F6CDD1Dull + 0x1234567ull;
+#pragma omp parallel for schedule(static)
     for (int jl = 1; jl <= nl; ++jl)
       for (int jk = 1; jk <= nx; ++jk)
         for (int ji = 1; ji <= ny; ++ji) {
           const size_t i = m.IS(ji, jk, jl);
           const double z = m.z_scalar[i];
-          double tp = 0.0;
-          for (int q = 0; q < nmodes; ++q)
-            tp += std::cos(2.0 * M_PI_ * (kx[q] * (jk - 0.5) / nx + ky[q] * (ji - 0.5) / ny) + ph[q]);
+          const double tp = tcol[m.I2(ji, jk)];
           const double env = std::sin(M_PI_ * z / n.toa);
           const double T = bg_temp(z) + amp * tp * env;
-          // relative humidity and specific humidity (vapour mass / gas mass)
+          // relative humidity (lognormal, a counter-based random number per cell) and
+          // specific humidity (vapour mass / gas mass)
           double rh = 0.0;
-          if (z < 12000.0) rh = std::fmin(0.98, n.rh_mean * std::exp(0.15 * rng.normal() - 0.5 * 0.15 * 0.15)) * (1.0 - z / 12000.0 * 0.7);
+          Rng cell(seed_h ^ (uint64_t)i);
+          if (z < 12000.0) rh = std::fmin(0.98, n.rh_mean * std::exp(0.15 * cell.normal() - 0.5 * 0.15 * 0.15)) * (1.0 - z / 12000.0 * 0.7);
           double pz = 0.0;
           if (!bg_pres(std::fmin(z, inv_height - 1.0), &pz)) pz = 5000.0;
           const double e = rh * e_sat(T);
@@ -861,11 +901,13 @@ int ideal_init(M& m) {
           return fail(LGAME_ERR_BAD_CONFIG, "Argument of bg_pres is above the inversion height.");
     unessential_ideal_init(m, sp, pres_lowest);
     const size_t g = (size_t)nc;  // gas index - 1
+#pragma omp parallel for schedule(static)
     for (size_t i = 0; i < nS; ++i) {
       const double rg = m.rho[i + nS * g];
       m.rho[i + nS * (g + 1)] = qv[i] * rg;
       const double z = m.z_scalar[i];
-      const double r = rng.uniform();
+      Rng cell((seed_h + 0x9E37ull) ^ (uint64_t)i);
+      const double r = cell.uniform();
       if (r > 0.85) {
         if (z > 4000.0 && z < 8000.0) m.rho[i + nS * 3] = 2e-4 * rg * (r - 0.85) / 0.15;  // cloud water
         if (z > 8000.0 && z < 11000.0) m.rho[i + nS * 2] = 5e-5 * rg * (r - 0.85) / 0.15;  // cloud ice

@@ -58,7 +58,18 @@ struct lgame_gpu {
   int* flag = nullptr;
   Grid<double> G{};
   SplitCtx* split = nullptr;
+  // per-kernel tracing
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<const char*, int>> ev_used;  // (kernel name, index of its start event)
+  std::vector<std::pair<std::string, std::pair<int, double>>> prof_acc;
 };
+
+namespace lg {
+// start/stop events around one launch when tracing is on (called from the step code)
+int trace_begin(lgame_gpu* c, const char* name);
+void trace_end(lgame_gpu* c, int slot);
+}
 
 namespace {
 
@@ -218,7 +229,9 @@ int klaunch_check(lgame_gpu* c, const char* what) {
 }
 #define LAUNCH(kernel, grid_, ...)                                             \
   do {                                                                         \
+    const int tr_ = c->profiling ? lg::trace_begin(c, #kernel) : -1;           \
     kernel<<<grid_, blk(), 0, c->stream>>>(__VA_ARGS__);                       \
+    if (tr_ >= 0) lg::trace_end(c, tr_);                                       \
     int rc_ = klaunch_check(c, #kernel);                                       \
     if (rc_ != LGAME_OK) return rc_;                                           \
   } while (0)
@@ -331,8 +344,9 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     cudaGetLastError();
     return set_err(LGAME_ERR_NO_DEVICE, "no CUDA device is visible");
   }
-  int dev = 0;
-  CK(cudaGetDevice(&dev));
+  const int dev = cfg->device;
+  if (dev < 0 || dev >= ndev) return set_err(LGAME_ERR_NO_DEVICE, "lgame_config.device is not a visible device");
+  CK(cudaSetDevice(dev));
   cudaDeviceProp prop;
   CK(cudaGetDeviceProperties(&prop, dev));
   if (prop.major != 10 || prop.minor != 3)
@@ -667,12 +681,63 @@ extern "C" int lgame_gpu_synchronize(lgame_gpu* c) {
 
 extern "C" int lgame_gpu_kernels_per_step(const lgame_gpu* c) { return c ? c->kernels_last_step : 0; }
 
+namespace lg {
+int trace_begin(lgame_gpu* c, const char* name) {
+  const int idx = (int)c->ev_used.size() * 2;
+  while ((int)c->ev_pool.size() < idx + 2) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return -1;
+    c->ev_pool.push_back(e);
+  }
+  cudaEventRecord(c->ev_pool[idx], c->stream);
+  c->ev_used.push_back({name, idx});
+  return idx;
+}
+void trace_end(lgame_gpu* c, int slot) { cudaEventRecord(c->ev_pool[slot + 1], c->stream); }
+}  // namespace lg
+
+extern "C" void* lgame_gpu_stream(const lgame_gpu* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int lgame_gpu_set_profiling(lgame_gpu* c, int enable) {
+  if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_profiling: null context");
+  c->profiling = enable != 0;
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_profile_report(lgame_gpu* c, char* buf, int len) {
+  if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_profile_report: null context");
+  CK(cudaStreamSynchronize(c->stream));
+  for (auto& u : c->ev_used) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev_pool[u.second], c->ev_pool[u.second + 1]);
+    bool found = false;
+    for (auto& a : c->prof_acc)
+      if (a.first == u.first) { a.second.first += 1; a.second.second += ms; found = true; break; }
+    if (!found) c->prof_acc.push_back({u.first, {1, (double)ms}});
+  }
+  c->ev_used.clear();
+  std::string js = "{";
+  for (size_t i = 0; i < c->prof_acc.size(); ++i) {
+    char tmp[256];
+    std::snprintf(tmp, sizeof tmp, "%s\"%s\": {\"launches\": %d, \"ms\": %.6f}", i ? ", " : "",
+                  c->prof_acc[i].first.c_str(), c->prof_acc[i].second.first, c->prof_acc[i].second.second);
+    js += tmp;
+  }
+  js += "}";
+  if (buf && len > (int)js.size()) {  // counts are reset only once they have been handed out
+    std::memcpy(buf, js.c_str(), js.size() + 1);
+    c->prof_acc.clear();
+  }
+  return (int)js.size();
+}
+
 extern "C" long long lgame_gpu_device_bytes(const lgame_gpu* c) { return c ? c->bytes : 0; }
 
 extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
   if (c->split) split_destroy(c->split);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (void* p : c->allocations) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;

@@ -46,7 +46,8 @@ class Config(C.Structure):
                 ("ltemp_diff_v", C.c_int), ("lmass_diff_h", C.c_int), ("lmass_diff_v", C.c_int),
                 ("lprog_soil_temp", C.c_int), ("lsfc_sensible_heat_flux", C.c_int),
                 ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lperiodic", C.c_int),
-                ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int)]
+                ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int),
+                ("device", C.c_int)]
 
 
 def _s(n):
@@ -120,6 +121,9 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_synchronize": (i, [vp]),
         "lgame_gpu_kernels_per_step": (i, [vp]),
         "lgame_gpu_device_bytes": (ll, [vp]),
+        "lgame_gpu_stream": (vp, [vp]),
+        "lgame_gpu_set_profiling": (i, [vp, i]),
+        "lgame_gpu_profile_report": (i, [vp, C.c_char_p, i]),
         "lgame_gpu_destroy": (None, [vp]),
         "lgame_gpu_last_error": (C.c_char_p, []),
         "lgame_gpu_version": (C.c_char_p, []),
@@ -305,6 +309,22 @@ class GpuModel:
 
     def device_bytes(self) -> int:
         return self.lib.lgame_gpu_device_bytes(self.h)
+
+    def stream_handle(self) -> int:
+        """cudaStream_t of the context (for CUDA events recorded by the caller)."""
+        return int(self.lib.lgame_gpu_stream(self.h) or 0)
+
+    def set_profiling(self, enable: bool):
+        check(self.lib.lgame_gpu_set_profiling(self.h, 1 if enable else 0), "lgame_gpu_set_profiling")
+
+    def profile_report(self) -> dict:
+        import json
+        n = self.lib.lgame_gpu_profile_report(self.h, None, 0)
+        if n < 0:
+            check(n, "lgame_gpu_profile_report")
+        buf = C.create_string_buffer(n + 1)
+        self.lib.lgame_gpu_profile_report(self.h, buf, n + 1)
+        return json.loads(buf.value.decode())
 
     def close(self):
         if self.h:

@@ -1,0 +1,77 @@
+"""The C ABI library: it loads, exports every function the headers declare, and rejects
+bad input with error codes (no device needed for these)."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+import cases
+import lgame_gpu as L
+from conftest import has_gpu
+
+INCLUDE = Path(__file__).resolve().parent.parent / "include"
+
+
+def declared_functions():
+    names = []
+    for h in sorted(INCLUDE.glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names += re.findall(r"\b(lgame_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_function():
+    lib = C.CDLL(str(L.LIB_PATH))
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_version_and_error_string():
+    lib = L.load_library()
+    assert b"sm_103a" in lib.lgame_gpu_version()
+    assert isinstance(L.last_error(), str)
+
+
+def _cfg(**kw):
+    n = cases.small_case("schaer")
+    c = L.config_from_namelist(n)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+@pytest.mark.parametrize("field,value,code", [
+    ("n_layers", 2, L.ERR_BAD_DIMS),
+    ("n_layers", 200, L.ERR_BAD_DIMS),
+    ("n_oro_layers", 0, L.ERR_BAD_DIMS),
+    ("theta_adv_order", 5, L.ERR_BAD_CONFIG),
+    ("dtime", -1.0, L.ERR_BAD_CONFIG),
+    ("precision", 9, L.ERR_BAD_CONFIG),
+    ("lmom_diff_h", 1, L.ERR_UNSUPPORTED),
+    ("lpbl", 1, L.ERR_UNSUPPORTED),
+])
+def test_create_rejects_bad_config(field, value, code):
+    lib = L.load_library()
+    h = C.c_void_p()
+    rc = lib.lgame_gpu_create(C.byref(_cfg(**{field: value})), C.byref(h))
+    assert rc == code and not h.value
+
+
+@pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
+def test_create_without_device_reports_no_device():
+    lib = L.load_library()
+    h = C.c_void_p()
+    rc = lib.lgame_gpu_create(C.byref(_cfg()), C.byref(h))
+    assert rc == L.ERR_NO_DEVICE and not h.value
+    assert "device" in L.last_error()
+
+
+def test_null_arguments_are_errors():
+    lib = L.load_library()
+    assert lib.lgame_gpu_create(None, None) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_pchevi(None, 0, 1, 0, 0, 0.0) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_set_grid(None, None, 0) == L.ERR_INVALID_ARG
+    lib.lgame_gpu_destroy(None)
