@@ -46,32 +46,82 @@ def read_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "src": "fallback"}
 
 
-# Algorithmic bytes per cell of one launch of the main kernels (8-byte fields that the
-# kernel must read or write once; SURVEY 8(d) counting applied kernel by kernel).
-# ncons = 7 constituents (moist).  Averages over the rk1/rk2 launches where they differ.
-def kernel_bytes_per_cell(name: str, ncons: int, split: bool) -> float:
-    w = 8.0
+# Algorithmic (compulsory) bytes per cell of one launch: every distinct array a kernel
+# touches, read or written once per cell.  Entries are (n8, nT, n8_oro, nT_oro):
+#   n8  arrays stored in FP64 on both paths (the state, the pressure-gradient products,
+#       the FP64 metrics and reciprocals of the column solvers),
+#   nT  arrays of the kernel's working type (8 B on the FP64 path, 4 B on the split path:
+#       FP32 metric copies, intermediates, tendencies, carried stencil diagnostics),
+#   *_oro  arrays read only in the terrain-following layers jl >= n_flat_layers (slopes,
+#       inner-product weights, area_z), weighted by the fraction of those layers.
+# ntr = number of constituents other than the gas.  Data-dependent reads (the diabatic
+# branch of k_gas_theta) and 1-D/2-D arrays are left out, so these are lower bounds.
+def _kernel_fields(ncons: int) -> dict:
     ntr = ncons - 1
-    table = {
-        # rho_g,rhotheta,exner',theta',w old; tend rho_g,rhotheta,w; (rk2: rho_g,rhotheta,exner' new)/2;
-        # grid volume,exner_bg,theta_bg,z,area_z,damp; writes rho_g,rhotheta,exner',theta',w
-        "k_column_ver": (5 + 3 + 1.5 + 6 + 5) * w,
-        "k_column_ver_s": (5 + 3 + 1.5 + 6 + 5) * w,
-        # per tracer rho old, tend, rho new; w old/new, T, volume, area_z, rho_g, gravity, 2 weights; csh r/w at rk1
-        "k_column_tracers": (3 * ntr + 9 + 1) * w,
-        "k_column_tracers_s": (3 * ntr + 9 + 1) * w,
-        # per tracer rho, tend r/w; u, v new; area_x, area_y, area_z, volume, slopes, 4 weights
-        "k_tracers": (3 * ntr + 2 + 10) * w,
-        "k_eta_z": (2 + 1 + 6 + 3) * w,
-        "k_eta_xy": (3 + 1 + 8 + 2) * w,
-        "k_vort_flux": (6 + 3 + 3 + 6 + 3) * w,
-        "k_gas_theta": (1 + 2 + 2 + 2 + 2 + 3 + 8 + 2) * w,
-        "k_pgrad": (ncons + 2 + 3 + 4 + 9 + 9) * w,
-        "k_tend_wind": (3 * 3 + 15) * w,
+    moist = 2 if ncons > 1 else 0
+    return {
+        "temperature": (2 + moist, 3, 0, 0),          # theta', exner' (+rho_g, rho_v); bg x2, T out
+        "theta": (1, 2, 0, 0),                         # theta'; theta_bg, out
+        "grad_vert": (0, 3, 0, 0),                     # field, dz, out
+        "grad_hor": (0, 5, 0, 5),                      # field, dx, dy, 2 out; slopes, dz-gradient, 2 weights
+        "div_h": (0, 6, 0, 7),                         # 2 in, area_x/y, volume, out; area_z, slopes, 4 weights
+        "theta_edges": (2, 4, 0, 0),                   # u, v; theta, div, 2 out
+        "eta_xy": (4, 11, 0, 0),                       # u, v, w, rho_g; dx,dy,dz,z_u,z_v,z_w,z_scalar,2 dual areas, 2 out
+        "eta_z": (3, 6, 0, 3),                         # u, v, rho_g; dx, dy, area_dual_z, z_area_dual_z, z_scalar, out
+        "mass_flux": (4, 3, 0, 0),                     # rho_g, u, v, w; 3 out
+        "vort_flux": (0, 15, 0, 0),                    # 3 eta, 3 mass fluxes, 6 weights, 3 out
+        "ke": (3, 7, 0, 0),                            # u, v, w; 6 weights, out
+        "tend_wind": (12, 13, 0, 0),                   # u, v old/new, 8 pressure-gradient arrays; 3 tendencies r/w, 7 carried
+        "tracers": (ntr + 2, 2 * ntr + 3, 0, 7),       # rho_jc, u, v; tend r/w per tracer, area_x/y, volume
+        "gas_theta": (3, 9, 0, 7),                     # rho_g, u, v; 2 theta edges, area_x/y, volume, rad, csh, 2 out
     }
-    if split and name.endswith("_s") is False and name.startswith("ks_"):
-        return table.get(name[1:], 0.0)
-    return table.get(name, 0.0)
+
+
+def step_bytes_per_cell(ncons: int, split: bool) -> float:
+    """Compulsory bytes per cell of one step: reads 2P + P + 2G + T + C, writes 2P + T + C
+    with P = ncons + 6 prognostic, T = ncons + 4 tendency, C = 8 carried (+1 sediment
+    heating when moist) and G = 29 grid arrays.  FP64 path: all 8 B (952 B dry, 1304 B
+    moist).  Split path: state 8 B; grid copies, tendencies and the carried stencil
+    diagnostics 4 B; p_grad_acc_old (2 arrays) 8 B."""
+    P, T, C, G = ncons + 6, ncons + 4, 8 + (1 if ncons > 1 else 0), 29
+    if not split:
+        return 8.0 * (3 * P + 2 * G + T + C + 2 * P + T + C)
+    c8, c4 = 2, C - 2
+    return 8.0 * 5 * P + 4.0 * 2 * G + 4.0 * 2 * T + 2 * (8.0 * c8 + 4.0 * c4)
+
+
+def kernel_bytes_per_cell(name: str, ncons: int, split: bool, f_oro: float) -> float:
+    """Algorithmic bytes per cell (ny*nx*n_layers) of one launch of kernel `name`."""
+    ntr = ncons - 1
+    fp64_only = {
+        # state old (rho_g, rho*theta, exner', theta', w), new at rk2 (half the launches),
+        # tendencies, metrics (volume, exner_bg, theta_bg, z_scalar, area_z, damping), 5 writes
+        "k_column_ver": 5 + 3 + 2 + 6 + 5,
+        # per tracer rho old/tend/new; w old/new, T, volume, area_z, rho_g, csh
+        "k_column_tracers": 3 * ntr + 7,
+        # grad exner' (3), theta edges (2 + 2 perturbation), all rho, 3 background gradients,
+        # gravity, 8 products written, 4 previous products read
+        "k_pgrad": 3 + 4 + ncons + 3 + 1 + 8 + 4,
+    }
+    if not split:
+        if name in fp64_only:
+            return fp64_only[name] * 8.0
+        f = _kernel_fields(ncons).get(name[2:])
+        return 0.0 if f is None else 8.0 * (f[0] + f[1] + f_oro * (f[2] + f[3]))
+    split_own = {
+        # FP64: state old 5, new at rk2 2, 5 writes, exner_bg, theta_bg, z_scalar,
+        # inv_volume, inv_area_z, damping; FP32: 3 tendencies, gravity
+        "ks_column_ver": 18 * 8.0 + 4 * 4.0,
+        # FP64: rho old/new per tracer, w old/new, inv_volume, rho_g; FP32: tendency per tracer, T, area_z, csh
+        "ks_column_tracers": (2 * ntr + 4) * 8.0 + (ntr + 3) * 4.0,
+        # FP64: exner', all rho, inv dx/dy/dz, 3 background gradients, 8 products written,
+        # 4 previous read; FP32: 4 theta edges, gravity, pgcw
+        "ks_pgrad": (1 + ncons + 3 + 3 + 8 + 4) * 8.0 + 6 * 4.0,
+    }
+    if name in split_own:
+        return split_own[name]
+    f = _kernel_fields(ncons).get(name[3:])
+    return 0.0 if f is None else 8.0 * (f[0] + f_oro * f[2]) + 4.0 * (f[1] + f_oro * f[3])
 
 
 class ClockSampler:
@@ -249,7 +299,8 @@ def run_reference(args):
     return 0
 
 
-def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak_gbs: float, split: bool):
+def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak_gbs: float, split: bool,
+                    f_oro: float):
     g.set_profiling(True)
     for k in range(first_step, first_step + steps):
         g.pchevi(k % 2, (k + 1) % 2, k)
@@ -260,7 +311,7 @@ def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak
     top = rows[0]
     name, st = top[0], top[1]
     avg_ms = st["ms"] / st["launches"]
-    bpc = kernel_bytes_per_cell(name, ncons, split)
+    bpc = kernel_bytes_per_cell(name, ncons, split, f_oro)
     alg = bpc * cells
     achieved = alg / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
     shares = {k: round(v["ms"] / total, 4) for k, v in rows}
@@ -281,6 +332,7 @@ def run_ours(args):
     t_setup = time.perf_counter() - t_setup
     cells = n.nx * n.ny * n.n_layers
     ncons = n.n_constituents
+    f_oro = (n.n_oro_layers + 1) / n.n_layers
     results = {}
     precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64] if not args.fp64_only else [L.PRECISION_FP64]
     clocks = None
@@ -312,7 +364,7 @@ def run_ours(args):
         el = reduce_max(dist, el)
         nk = g.kernels_per_step()
         prof = profile_kernels(g, 2, args.warmup + args.steps, ncons, cells, peaks["hbm_gbs"],
-                               prec == L.PRECISION_SPLIT)
+                               prec == L.PRECISION_SPLIT, f_oro)
         st = g.get_state((args.warmup + args.steps + 2) % 2)
         finite = all(bool(np.isfinite(v).all()) for v in st.values())
         results[prec] = {"s_per_step": el / args.steps, "kernels_per_step": nk, "profile": prof, "finite": finite,
@@ -330,6 +382,7 @@ def run_ours(args):
     head = results[head_prec]
     value = ws * 1.0 / head["s_per_step"]
     prof = head["profile"]
+    step_b = step_bytes_per_cell(ncons, head_prec == L.PRECISION_SPLIT)
     fp64 = results.get(L.PRECISION_FP64)
     line = {
         "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": args.steps,
@@ -347,9 +400,9 @@ def run_ours(args):
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": prof["frac"], "traffic": None,
                      "peak_src": peaks["src"], "avg_launch_ms": prof["avg_launch_ms"],
                      "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"]},
-        "step_roofline": {"alg_bytes_per_step": 1304.0 * cells if ncons > 1 else 952.0 * cells,
-                          "achieved_gbs": (1304.0 if ncons > 1 else 952.0) * cells / head["s_per_step"] / 1e9,
-                          "peak_gbs": peaks["hbm_gbs"]},
+        "step_roofline": {"alg_bytes_per_cell": step_b, "alg_bytes_per_step": step_b * cells,
+                          "achieved_gbs": step_b * cells / head["s_per_step"] / 1e9,
+                          "peak_gbs": peaks["hbm_gbs"], "frac": step_b * cells / head["s_per_step"] / 1e9 / peaks["hbm_gbs"]},
         "gpu_launches": head["kernels_per_step"] * args.steps,
         "clocks": clocks,
         "finite": head["finite"],

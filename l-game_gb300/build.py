@@ -32,7 +32,7 @@ CUDA_UNITS = [
     ("lgame_gpu.cu", ["-fmad=false"]),
     ("kernels_fp64.cu", ["-fmad=false"]),
     ("column_fp64.cu", ["-fmad=false"]),
-    ("split.cu", ["-fmad=true"]),
+    ("split.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
 ]
 CXX_UNITS = [
     ("host/error.cpp", []),

@@ -31,7 +31,7 @@ __device__ __forceinline__ void thomas(const double* c, const double* d, const d
 // three_band_solver_ver, mo_column_solvers.F90:21-351, plus the array-wide update of
 // theta_v_pert (:346-349) and w_free_slip (mo_inner_product.F90:52-75) of this column,
 // both of which only touch the column itself.
-__global__ void k_column_ver(Dims D, Grid<double> G, State So, State Sn, Tend Tn, int rk_step) {
+__global__ void k_column_ver(Dims D, Grid<double> G, State So, State Sn, Tend<double> Tn, int rk_step) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
@@ -161,7 +161,12 @@ __device__ __forceinline__ double v_fall_solid(double radius) {
   return (radius > (double)250.e-6f) ? 1.0 : 0.001;
 }
 
-// three_band_solver_gen_densities, mo_column_solvers.F90:353-604, all tracers of one column
+// three_band_solver_gen_densities, mo_column_solvers.F90:353-604, all tracers of one column.
+// Quantities that the reference evaluates with the same operands for several tracers or
+// twice per level are evaluated once and reused (identical bits): itw*dtime/volume, the
+// cloud-droplet fall speed of a level, c_p of ice and water at the interface temperature.
+// Rain and graupel use the radius diag%a_rain, which the reference never sets (zero), so
+// their fall speed is exactly 0 (v_fall_liquid with radius 0 returns 0 for finite states).
 __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, const double* t_rho_all,
                                  const double* T, double* csh, int rk_step) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -175,11 +180,19 @@ __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, con
   double vfi[kMaxLayers + 1], vfr[kMaxLayers + 1], vefv[kMaxLayers + 1], v_fall[kMaxLayers + 1];
   double cv[kMaxLayers + 1], dv[kMaxLayers + 1], evec[kMaxLayers + 1], rv[kMaxLayers + 1];
   double sol[kMaxLayers + 1], epr[kMaxLayers + 1], rpr[kMaxLayers + 1];
+  double itwdtv[kMaxLayers + 1], vcloud[kMaxLayers + 1], cpi[kMaxLayers + 2], cpw[kMaxLayers + 2];
+  for (int jl = 1; jl <= nl; ++jl) {
+    const long long i = IX(D, ji, jk, jl);
+    itwdtv[jl] = itw * dtime / G.volume[i];
+    vcloud[jl] = v_fall_liquid(D, G, rho_g_o, T, cloud_r, ji, jk, jl);
+    if (jl >= 2) { cpi[jl] = c_p_ice(T[i]); cpw[jl] = c_p_water(T[i]); }
+  }
   for (int jc = 1; jc <= D.ncons; ++jc) {
     if (jc == D.g) continue;
     const double* rho_o = So.rho + (long long)(jc - 1) * D.fstride;
     double* rho_n = Sn.rho + (long long)(jc - 1) * D.fstride;
     const double* t_rho = t_rho_all + (long long)(jc - 1) * D.fstride;
+    const bool ice = (jc - 1) % 2 == 0;
     for (int jl = 1; jl <= nl - 1; ++jl) {
       const long long a = IX(D, ji, jk, jl), b = IX(D, ji, jk, jl + 1);
       if (rk_step == 1 && jc == 1) csh[a] = 0.0;
@@ -187,12 +200,10 @@ __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, con
       vfr[jl] = Sn.w[b];
       double vf;
       if (jc == 1) vf = 0.5 * (v_fall_solid(snow_r) + v_fall_solid(snow_r));
-      else if (jc == 2 || jc == 5) {  // rain, graupel: radius diag%a_rain = 0 (never set)
-        vf = 0.5 * (v_fall_liquid(D, G, rho_g_o, T, 0.0, ji, jk, jl) + v_fall_liquid(D, G, rho_g_o, T, 0.0, ji, jk, jl + 1));
-      } else if (jc == 3) vf = 0.5 * (v_fall_solid(ice_r) + v_fall_solid(ice_r));
-      else if (jc == 4) {
-        vf = 0.5 * (v_fall_liquid(D, G, rho_g_o, T, cloud_r, ji, jk, jl) + v_fall_liquid(D, G, rho_g_o, T, cloud_r, ji, jk, jl + 1));
-      } else vf = 0.0;
+      else if (jc == 2 || jc == 5) vf = 0.0;
+      else if (jc == 3) vf = 0.5 * (v_fall_solid(ice_r) + v_fall_solid(ice_r));
+      else if (jc == 4) vf = 0.5 * (vcloud[jl] + vcloud[jl + 1]);
+      else vf = 0.0;
       v_fall[jl] = vf;
       vfi[jl] = vfi[jl] - vf;
       vfr[jl] = vfr[jl] - vf;
@@ -201,20 +212,20 @@ __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, con
       const double doi = (vfr[jl] >= 0.0) ? rho_o[b] : rho_o[a];
       const double toi = T[b];
       vfr[jl] = doi * vfr[jl];
-      vefv[jl] = (jc <= nc) ? c_p_cond(jc, toi) * toi * vfr[jl] : 0.0;
+      vefv[jl] = (jc <= nc) ? (ice ? cpi[jl + 1] : cpw[jl + 1]) * toi * vfr[jl] : 0.0;
     }
     if (rk_step == 1 && jc == 1) csh[IX(D, ji, jk, nl)] = 0.0;
     if (jc == 1) v_fall[nl] = v_fall_solid(snow_r);
-    else if (jc == 2 || jc == 5) v_fall[nl] = v_fall_liquid(D, G, rho_g_o, T, 0.0, ji, jk, nl);
+    else if (jc == 2 || jc == 5) v_fall[nl] = 0.0;
     else if (jc == 3) v_fall[nl] = v_fall_solid(ice_r);
-    else if (jc == 4) v_fall[nl] = v_fall_liquid(D, G, rho_g_o, T, cloud_r, ji, jk, nl);
+    else if (jc == 4) v_fall[nl] = vcloud[nl];
     else v_fall[nl] = 0.0;
     for (int jl = 1; jl <= nl - 1; ++jl) {
       if (vfi[jl] >= 0.0) {
         cv[jl] = 0.0;
-        evec[jl] = -itw * dtime / G.volume[IX(D, ji, jk, jl)] * vfi[jl];
+        evec[jl] = -(itwdtv[jl] * vfi[jl]);
       } else {
-        cv[jl] = itw * dtime / G.volume[IX(D, ji, jk, jl + 1)] * vfi[jl];
+        cv[jl] = itwdtv[jl + 1] * vfi[jl];
         evec[jl] = 0.0;
       }
     }
@@ -222,14 +233,14 @@ __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, con
       const long long i = IX(D, ji, jk, jl);
       const double V = G.volume[i];
       if (jl == 1) {
-        dv[jl] = (vfi[1] >= 0.0) ? 1.0 : 1.0 - itw * dtime / V * vfi[1];
+        dv[jl] = (vfi[1] >= 0.0) ? 1.0 : 1.0 - itwdtv[jl] * vfi[1];
       } else if (jl == nl) {
-        dv[jl] = (vfi[jl - 1] >= 0.0) ? 1.0 + itw * dtime / V * vfi[jl - 1] : 1.0;
+        dv[jl] = (vfi[jl - 1] >= 0.0) ? 1.0 + itwdtv[jl] * vfi[jl - 1] : 1.0;
         if (jc <= nc) dv[jl] = dv[jl] + itw * v_fall[jl] * dtime * G.area_z[IX(D, ji, jk, jl + 1)] / V;
       } else {
         double d = 1.0;
-        if (vfi[jl - 1] >= 0.0) d = d + itw * dtime / V * vfi[jl - 1];
-        if (vfi[jl] < 0.0) d = d - itw * dtime / V * vfi[jl];
+        if (vfi[jl - 1] >= 0.0) d = d + itwdtv[jl] * vfi[jl - 1];
+        if (vfi[jl] < 0.0) d = d - itwdtv[jl] * vfi[jl];
         dv[jl] = d;
       }
       double r = rho_o[i] + dtime * t_rho[i];
@@ -243,7 +254,8 @@ __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, con
           r = r - expl_weight * v_fall[jl] * dtime * rho_o[i] * G.area_z[IX(D, ji, jk, jl + 1)] / V;
           if (jc > nc / 4 && rk_step == 1) {  // rain branch and cloud branch, not snow
             const double Tn = T[IX(D, ji, jk, nl)];
-            csh[i] = csh[i] - v_fall[jl] * Tn * c_p_cond(jc, Tn) * rho_o[IX(D, ji, jk, nl)] * G.area_z[IX(D, ji, jk, NL)] / V;
+            csh[i] = csh[i] - v_fall[jl] * Tn * (ice ? cpi[nl] : cpw[nl]) * rho_o[IX(D, ji, jk, nl)] *
+                              G.area_z[IX(D, ji, jk, NL)] / V;
           }
         }
       } else {

@@ -1,61 +1,77 @@
-// kernels.cuh -- pointwise helpers and kernel declarations of the FP64 HEVI step.
+// kernels.cuh -- pointwise helpers and the explicit-tendency kernels of the HEVI step,
+// templated on the type T of the grid metrics, the intermediate fields and the
+// arithmetic.  The state is always FP64.
+//
+//   T = double: the FP64 step (kernels_fp64.cu, -fmad=false): every expression keeps the
+//               reference's operands and left-to-right order, so the results are the
+//               reference's bits.
+//   T = float:  the explicit stencils of the split-precision step (split.cu): the same
+//               expressions in FP32 on FP32 copies of the metrics.
 #pragma once
 
 #include "dev.cuh"
 
 namespace lg {
 
-struct PGrad {  // pressure-gradient arrays of t_diag (mo_definitions.F90:137-146)
-  double *nl_u, *nl_v, *nl_w, *l_u, *l_v, *l_w, *old_u, *old_v, *pgcw;
+template <class T>
+struct PGrad {  // pressure-gradient arrays of t_diag (mo_definitions.F90:137-146), always FP64
+  double *nl_u, *nl_v, *nl_w, *l_u, *l_v, *l_w, *old_u, *old_v;
+  T* pgcw;
 };
 
+template <class T>
 struct Tend {  // t_tend (mo_definitions.F90:108-116)
-  double *rho, *rt, *u, *v, *w;
+  T *rho, *rt, *u, *v, *w;
 };
 
+template <class T>
 struct Carried {  // read-only view of the diagnostics combined into the wind tendency
-  const double *nl_u, *nl_v, *nl_w, *l_u, *l_v, *l_w, *old_u, *old_v, *pgcw;
-  const double *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z;
+  const double *nl_u, *nl_v, *nl_w, *l_u, *l_v, *l_w, *old_u, *old_v;
+  const T *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z;
 };
 
 // ---- edge operators with the reference's boundary branches --------------------
 // Each returns false where the reference leaves the output point untouched
 // (non-periodic boundary edges); periodic jk=nx+1 / ji=ny+1 evaluate the copy source.
 
-// grad_hor_cov x-component at a u point, mo_gradient_operators.F90:33-52
-__device__ __forceinline__ bool grad_x_cov(const Dims& D, const Grid<double>& G, const double* s, int ji, int jk, int jl, double* r) {
+// grad_hor_cov x-component at a u point, mo_gradient_operators.F90:33-52.  The difference
+// is taken in the source type S and rounded to T afterwards (FP64 field, FP32 result).
+template <class T, class S>
+__device__ __forceinline__ bool grad_x_cov(const Dims& D, const Grid<T>& G, const S* s, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
-    *r = (s[IX(D, ji, jk, jl)] - s[IX(D, ji, jk - 1, jl)]) / G.dx[IX(D, ji, jk, jl)];
+    *r = T(s[IX(D, ji, jk, jl)] - s[IX(D, ji, jk - 1, jl)]) / G.dx[IX(D, ji, jk, jl)];
     return true;
   }
   if (!D.periodic) return false;
-  *r = (s[IX(D, ji, 1, jl)] - s[IX(D, ji, D.nx, jl)]) / G.dx[IX(D, ji, 1, jl)];
+  *r = T(s[IX(D, ji, 1, jl)] - s[IX(D, ji, D.nx, jl)]) / G.dx[IX(D, ji, 1, jl)];
   return true;
 }
 
 // grad_hor_cov y-component at a v point, mo_gradient_operators.F90:39-60
-__device__ __forceinline__ bool grad_y_cov(const Dims& D, const Grid<double>& G, const double* s, int ji, int jk, int jl, double* r) {
+template <class T, class S>
+__device__ __forceinline__ bool grad_y_cov(const Dims& D, const Grid<T>& G, const S* s, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
-    *r = (s[IX(D, ji - 1, jk, jl)] - s[IX(D, ji, jk, jl)]) / G.dy[IX(D, ji, jk, jl)];
+    *r = T(s[IX(D, ji - 1, jk, jl)] - s[IX(D, ji, jk, jl)]) / G.dy[IX(D, ji, jk, jl)];
     return true;
   }
   if (!D.periodic) return false;
-  *r = (s[IX(D, D.ny, jk, jl)] - s[IX(D, 1, jk, jl)]) / G.dy[IX(D, 1, jk, jl)];
+  *r = T(s[IX(D, D.ny, jk, jl)] - s[IX(D, 1, jk, jl)]) / G.dy[IX(D, 1, jk, jl)];
   return true;
 }
 
 // theta_v_adv_3rd_order x edge, mo_multiplications.F90:136-183
-__device__ __forceinline__ bool theta_edge_u(const Dims& D, const double* th, const double* Dv, const double* u,
-                                             double c, int ji, int jk, int jl, double* out) {
+template <class T>
+__device__ __forceinline__ bool theta_edge_u(const Dims& D, const T* th, const T* Dv, const double* u,
+                                             T c, int ji, int jk, int jl, T* out) {
   if (jk >= 2 && jk <= D.nx) {
-    double t = 0.5 * (th[IX(D, ji, jk - 1, jl)] + th[IX(D, ji, jk, jl)]);
+    T t = T(0.5) * (th[IX(D, ji, jk - 1, jl)] + th[IX(D, ji, jk, jl)]);
     if (u[IX(D, ji, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, jk - 1, jl)];
     else t = t - c * Dv[IX(D, ji, jk, jl)];
     *out = t;
     return true;
   }
   if (!D.periodic) return false;
-  double t = 0.5 * (th[IX(D, ji, D.nx, jl)] + th[IX(D, ji, 1, jl)]);
+  T t = T(0.5) * (th[IX(D, ji, D.nx, jl)] + th[IX(D, ji, 1, jl)]);
   if (u[IX(D, ji, 1, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, D.nx, jl)];
   else t = t - c * Dv[IX(D, ji, 1, jl)];
   *out = t;
@@ -63,107 +79,141 @@ __device__ __forceinline__ bool theta_edge_u(const Dims& D, const double* th, co
 }
 
 // theta_v_adv_3rd_order y edge, mo_multiplications.F90:152-200
-__device__ __forceinline__ bool theta_edge_v(const Dims& D, const double* th, const double* Dv, const double* v,
-                                             double c, int ji, int jk, int jl, double* out) {
+template <class T>
+__device__ __forceinline__ bool theta_edge_v(const Dims& D, const T* th, const T* Dv, const double* v,
+                                             T c, int ji, int jk, int jl, T* out) {
   if (ji >= 2 && ji <= D.ny) {
-    double t = 0.5 * (th[IX(D, ji, jk, jl)] + th[IX(D, ji - 1, jk, jl)]);
+    T t = T(0.5) * (th[IX(D, ji, jk, jl)] + th[IX(D, ji - 1, jk, jl)]);
     if (v[IX(D, ji, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, jk, jl)];
     else t = t - c * Dv[IX(D, ji - 1, jk, jl)];
     *out = t;
     return true;
   }
   if (!D.periodic) return false;
-  double t = 0.5 * (th[IX(D, 1, jk, jl)] + th[IX(D, D.ny, jk, jl)]);
+  T t = T(0.5) * (th[IX(D, 1, jk, jl)] + th[IX(D, D.ny, jk, jl)]);
   if (v[IX(D, 1, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, 1, jk, jl)];
   else t = t - c * Dv[IX(D, D.ny, jk, jl)];
   *out = t;
   return true;
 }
 
-// scalar_times_vector_h x-component, mo_multiplications.F90:34-54
-__device__ __forceinline__ bool stv_h_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, double* r) {
+// scalar_times_vector_h, mo_multiplications.F90:34-54 (state scalar and vector)
+template <class T>
+__device__ __forceinline__ bool stv_h_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
-    *r = 0.5 * (s[IX(D, ji, jk - 1, jl)] + s[IX(D, ji, jk, jl)]) * vx[IX(D, ji, jk, jl)];
+    *r = T(0.5) * (T(s[IX(D, ji, jk - 1, jl)]) + T(s[IX(D, ji, jk, jl)])) * T(vx[IX(D, ji, jk, jl)]);
     return true;
   }
   if (!D.periodic) return false;
-  *r = 0.5 * (s[IX(D, ji, 1, jl)] + s[IX(D, ji, D.nx, jl)]) * vx[IX(D, ji, 1, jl)];
+  *r = T(0.5) * (T(s[IX(D, ji, 1, jl)]) + T(s[IX(D, ji, D.nx, jl)])) * T(vx[IX(D, ji, 1, jl)]);
   return true;
 }
-__device__ __forceinline__ bool stv_h_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, double* r) {
+template <class T>
+__device__ __forceinline__ bool stv_h_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
-    *r = 0.5 * (s[IX(D, ji - 1, jk, jl)] + s[IX(D, ji, jk, jl)]) * vy[IX(D, ji, jk, jl)];
+    *r = T(0.5) * (T(s[IX(D, ji - 1, jk, jl)]) + T(s[IX(D, ji, jk, jl)])) * T(vy[IX(D, ji, jk, jl)]);
     return true;
   }
   if (!D.periodic) return false;
-  *r = 0.5 * (s[IX(D, 1, jk, jl)] + s[IX(D, D.ny, jk, jl)]) * vy[IX(D, 1, jk, jl)];
+  *r = T(0.5) * (T(s[IX(D, 1, jk, jl)]) + T(s[IX(D, D.ny, jk, jl)])) * T(vy[IX(D, 1, jk, jl)]);
   return true;
 }
 // the same with the scalar and the vector given as functions of the index
-template <class FS, class FV>
-__device__ __forceinline__ bool stv_h_x_fn(const Dims& D, FS s, FV vx, int ji, int jk, int jl, double* r) {
-  if (jk >= 2 && jk <= D.nx) { *r = 0.5 * (s(ji, jk - 1, jl) + s(ji, jk, jl)) * vx(ji, jk, jl); return true; }
+template <class T, class FS, class FV>
+__device__ __forceinline__ bool stv_h_x_fn(const Dims& D, FS s, FV vx, int ji, int jk, int jl, T* r) {
+  if (jk >= 2 && jk <= D.nx) { *r = T(0.5) * (s(ji, jk - 1, jl) + s(ji, jk, jl)) * vx(ji, jk, jl); return true; }
   if (!D.periodic) return false;
-  *r = 0.5 * (s(ji, 1, jl) + s(ji, D.nx, jl)) * vx(ji, 1, jl);
+  *r = T(0.5) * (s(ji, 1, jl) + s(ji, D.nx, jl)) * vx(ji, 1, jl);
   return true;
 }
-template <class FS, class FV>
-__device__ __forceinline__ bool stv_h_y_fn(const Dims& D, FS s, FV vy, int ji, int jk, int jl, double* r) {
-  if (ji >= 2 && ji <= D.ny) { *r = 0.5 * (s(ji - 1, jk, jl) + s(ji, jk, jl)) * vy(ji, jk, jl); return true; }
+template <class T, class FS, class FV>
+__device__ __forceinline__ bool stv_h_y_fn(const Dims& D, FS s, FV vy, int ji, int jk, int jl, T* r) {
+  if (ji >= 2 && ji <= D.ny) { *r = T(0.5) * (s(ji - 1, jk, jl) + s(ji, jk, jl)) * vy(ji, jk, jl); return true; }
   if (!D.periodic) return false;
-  *r = 0.5 * (s(1, jk, jl) + s(D.ny, jk, jl)) * vy(1, jk, jl);
+  *r = T(0.5) * (s(1, jk, jl) + s(D.ny, jk, jl)) * vy(1, jk, jl);
   return true;
 }
 
 // scalar_times_vector_h_upstream, mo_multiplications.F90:222-285
-__device__ __forceinline__ bool upstream_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, double* r) {
+template <class T>
+__device__ __forceinline__ bool upstream_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
     const double u = vx[IX(D, ji, jk, jl)];
-    *r = (u >= 0.0) ? s[IX(D, ji, jk - 1, jl)] * u : s[IX(D, ji, jk, jl)] * u;
+    *r = (u >= 0.0) ? T(s[IX(D, ji, jk - 1, jl)]) * T(u) : T(s[IX(D, ji, jk, jl)]) * T(u);
     return true;
   }
   if (!D.periodic) return false;
   const double u = vx[IX(D, ji, 1, jl)];
-  *r = (u >= 0.0) ? s[IX(D, ji, D.nx, jl)] * u : s[IX(D, ji, 1, jl)] * u;
+  *r = (u >= 0.0) ? T(s[IX(D, ji, D.nx, jl)]) * T(u) : T(s[IX(D, ji, 1, jl)]) * T(u);
   return true;
 }
-__device__ __forceinline__ bool upstream_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, double* r) {
+template <class T>
+__device__ __forceinline__ bool upstream_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
     const double v = vy[IX(D, ji, jk, jl)];
-    *r = (v >= 0.0) ? s[IX(D, ji, jk, jl)] * v : s[IX(D, ji - 1, jk, jl)] * v;
+    *r = (v >= 0.0) ? T(s[IX(D, ji, jk, jl)]) * T(v) : T(s[IX(D, ji - 1, jk, jl)]) * T(v);
     return true;
   }
   if (!D.periodic) return false;
   const double v = vy[IX(D, 1, jk, jl)];
-  *r = (v >= 0.0) ? s[IX(D, 1, jk, jl)] * v : s[IX(D, D.ny, jk, jl)] * v;
+  *r = (v >= 0.0) ? T(s[IX(D, 1, jk, jl)]) * T(v) : T(s[IX(D, D.ny, jk, jl)]) * T(v);
   return true;
 }
 
 // sum(state%rho(:,:,:,1:nc+1),4) in constituent order
-__device__ __forceinline__ double rho_sum_cond_gas(const Dims& D, const double* rho, long long q) {
-  double s = 0.0;
-  for (int jc = 0; jc <= D.nc; ++jc) s = s + rho[q + (long long)jc * D.fstride];
+template <class T>
+__device__ __forceinline__ T rho_sum_cond_gas(const Dims& D, const double* rho, long long q) {
+  T s = T(0);
+  for (int jc = 0; jc <= D.nc; ++jc) s = s + T(rho[q + (long long)jc * D.fstride]);
   return s;
 }
 
-// c_v_mass_weighted_air, mo_derived.F90:157-187
-__device__ __forceinline__ double c_v_mass_weighted_air(const Dims& D, const double* rho, const double* T, long long q) {
-  double c = 0.0;
-  for (int jc = 1; jc <= D.nc; ++jc) c = c + rho[q + (long long)(jc - 1) * D.fstride] * c_p_cond(jc, T[q]);
-  if (D.lmoist) {
-    c = c + (rho[q + (long long)D.nc * D.fstride] - rho[q + (long long)(D.nc + 1) * D.fstride]) * kC_D_V;
-    c = c + rho[q + (long long)(D.nc + 1) * D.fstride] * kC_V_V;
+// c_p of the condensates, mo_dictionary.F90:112-189 (float: the same formulas in FP32)
+__device__ __forceinline__ float c_p_water(float temperature) {
+  float tc = temperature - float(kT_0), c;
+  if (tc >= 0.f) {
+    if (tc > 35.f) tc = 35.f;
+    const float a = tc - 35.f, a2 = a * a;
+    c = 0.9979f + 3.1e-6f * a2 + 3.8e-9f * (a2 * a2);
   } else {
-    c = rho[q + (long long)D.nc * D.fstride] * kC_D_V;
+    if (tc < -37.f) tc = -37.f;
+    const float t2 = tc * tc;
+    c = 1.000938f - 2.7052e-3f * tc - 2.3235e-5f * t2 + 4.3778e-6f * (t2 * tc) + 2.7136e-7f * (t2 * t2);
+  }
+  return 4186.8f * c;
+}
+__device__ __forceinline__ float c_p_ice(float temperature) {
+  float tl = temperature;
+  if (tl > float(kT_0)) tl = float(kT_0);
+  if (tl < 20.f) tl = 20.f;
+  const float q = tl * (1.f / 125.1f);
+  const float c = -2.0572f + 0.14644f * tl + 0.06163f * tl * __expf(-(q * q));
+  return c * float(1.0 / kM_V);
+}
+__device__ __forceinline__ float c_p_cond(int jc, float temperature) {
+  return ((jc - 1) % 2 == 0) ? c_p_ice(temperature) : c_p_water(temperature);
+}
+
+// c_v_mass_weighted_air, mo_derived.F90:157-187
+template <class T>
+__device__ __forceinline__ T c_v_mass_weighted_air(const Dims& D, const double* rho, const T* Tm, long long q) {
+  T c = T(0);
+  for (int jc = 1; jc <= D.nc; ++jc) c = c + T(rho[q + (long long)(jc - 1) * D.fstride]) * c_p_cond(jc, Tm[q]);
+  if (D.lmoist) {
+    c = c + (T(rho[q + (long long)D.nc * D.fstride]) - T(rho[q + (long long)(D.nc + 1) * D.fstride])) * T(kC_D_V);
+    c = c + T(rho[q + (long long)(D.nc + 1) * D.fstride]) * T(kC_V_V);
+  } else {
+    c = T(rho[q + (long long)D.nc * D.fstride]) * T(kC_D_V);
   }
   return c;
 }
 
-// inner_product, mo_inner_product.F90:16-50 (both vectors the same)
-__device__ __forceinline__ double inner_product_at(const Dims& D, const Grid<double>& G, const double* u, const double* v,
-                                                   const double* w, int ji, int jk, int jl) {
-  const double a = u[IX(D, ji, jk + 1, jl)], b = v[IX(D, ji, jk, jl)], c = u[IX(D, ji, jk, jl)];
-  const double d = v[IX(D, ji + 1, jk, jl)], e = w[IX(D, ji, jk, jl)], f = w[IX(D, ji, jk, jl + 1)];
+// inner_product, mo_inner_product.F90:16-50 (both vectors the state wind)
+template <class T>
+__device__ __forceinline__ T inner_product_at(const Dims& D, const Grid<T>& G, const double* u, const double* v,
+                                              const double* w, int ji, int jk, int jl) {
+  const T a = T(u[IX(D, ji, jk + 1, jl)]), b = T(v[IX(D, ji, jk, jl)]), c = T(u[IX(D, ji, jk, jl)]);
+  const T d = T(v[IX(D, ji + 1, jk, jl)]), e = T(w[IX(D, ji, jk, jl)]), f = T(w[IX(D, ji, jk, jl + 1)]);
   return W_(1, ji, jk, jl) * a * a + W_(2, ji, jk, jl) * b * b + W_(3, ji, jk, jl) * c * c
        + W_(4, ji, jk, jl) * d * d + W_(5, ji, jk, jl) * e * e + W_(6, ji, jk, jl) * f * f;
 }
@@ -171,190 +221,476 @@ __device__ __forceinline__ double inner_product_at(const Dims& D, const Grid<dou
 // ---- potential vorticity, mo_vorticities.F90 -----------------------------------
 
 // rel_vort x-component before the division by the area, mo_vorticities.F90:33-93
-// (ji in 1..ny+1, already mapped to 1 for the periodic copy row when appropriate)
-__device__ __forceinline__ double zeta_x_raw(const Dims& D, const Grid<double>& G, const State& S, int ji, int jk, int jl) {
+template <class T>
+__device__ __forceinline__ T zeta_x_raw(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
   const double* v = S.v; const double* w = S.w;
   if (jl <= D.nl) {  // levels 2..nl
     const bool inner = ji >= 2 && ji <= D.ny;
-    if (!inner && !D.periodic) return 0.0;
+    if (!inner && !D.periodic) return T(0);
     const int ii = inner ? ji : 1, im = inner ? ji - 1 : D.ny;
-    return G.dz[IX(D, im, jk, jl)] * w[IX(D, im, jk, jl)]
-         - G.dy[IX(D, ii, jk, jl - 1)] * hcov_y<double, double>(D, G, v, w, ii, jk, jl - 1)
-         - G.dz[IX(D, ii, jk, jl)] * w[IX(D, ii, jk, jl)]
-         + G.dy[IX(D, ii, jk, jl)] * hcov_y<double, double>(D, G, v, w, ii, jk, jl);
+    return G.dz[IX(D, im, jk, jl)] * T(w[IX(D, im, jk, jl)])
+         - G.dy[IX(D, ii, jk, jl - 1)] * hcov_y<T, double>(D, G, v, w, ii, jk, jl - 1)
+         - G.dz[IX(D, ii, jk, jl)] * T(w[IX(D, ii, jk, jl)])
+         + G.dy[IX(D, ii, jk, jl)] * hcov_y<T, double>(D, G, v, w, ii, jk, jl);
   }
   // surface level NL
   const int nl = D.nl, NL = D.NL;
   const bool inner = ji >= 2 && ji <= D.ny;
   int ii = ji;
   if (D.freeslip && D.periodic && ji == D.ny + 1) ii = 1;  // copy made after the free-slip addition
-  double r = -G.dy[IX(D, ii, jk, nl)] * hcov_y<double, double>(D, G, v, w, ii, jk, nl);
+  T r = -G.dy[IX(D, ii, jk, nl)] * hcov_y<T, double>(D, G, v, w, ii, jk, nl);
   if (D.freeslip && (inner || (D.periodic && ii == 1))) {
     const int im = (ii == 1) ? D.ny : ii - 1;
-    r = r + 0.5 * G.dz[IX(D, im, jk, NL)] * w[IX(D, im, jk, NL)]
-          - 0.5 * G.dz[IX(D, ii, jk, NL)] * w[IX(D, ii, jk, NL)]
-          + G.dy[IX(D, ii, jk, nl)] * (v[IX(D, ii, jk, nl)]
-          + (v[IX(D, ii, jk, nl - 1)] - v[IX(D, ii, jk, nl)]) / (G.z_v[IX(D, ii, jk, nl - 1)] - G.z_v[IX(D, ii, jk, nl)])
-          * (0.5 * (G.z_w[IX(D, im, jk, NL)] + G.z_w[IX(D, ii, jk, NL)]) - G.z_v[IX(D, ii, jk, nl)])
-          + 0.5 * (w[IX(D, im, jk, NL)] + w[IX(D, ii, jk, NL)])
+    r = r + T(0.5) * G.dz[IX(D, im, jk, NL)] * T(w[IX(D, im, jk, NL)])
+          - T(0.5) * G.dz[IX(D, ii, jk, NL)] * T(w[IX(D, ii, jk, NL)])
+          + G.dy[IX(D, ii, jk, nl)] * (T(v[IX(D, ii, jk, nl)])
+          + (T(v[IX(D, ii, jk, nl - 1)]) - T(v[IX(D, ii, jk, nl)])) / (G.z_v[IX(D, ii, jk, nl - 1)] - G.z_v[IX(D, ii, jk, nl)])
+          * (T(0.5) * (G.z_w[IX(D, im, jk, NL)] + G.z_w[IX(D, ii, jk, NL)]) - G.z_v[IX(D, ii, jk, nl)])
+          + T(0.5) * (T(w[IX(D, im, jk, NL)]) + T(w[IX(D, ii, jk, NL)]))
           * (G.z_w[IX(D, im, jk, NL)] - G.z_w[IX(D, ii, jk, NL)]) / G.dy[IX(D, ii, jk, nl)]);
   }
   return r;
 }
 
 // rel_vort y-component before the division, mo_vorticities.F90:104-165
-__device__ __forceinline__ double zeta_y_raw(const Dims& D, const Grid<double>& G, const State& S, int ji, int jk, int jl) {
+template <class T>
+__device__ __forceinline__ T zeta_y_raw(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
   const double* u = S.u; const double* w = S.w;
   if (jl <= D.nl) {
     const bool inner = jk >= 2 && jk <= D.nx;
-    if (!inner && !D.periodic) return 0.0;
+    if (!inner && !D.periodic) return T(0);
     const int kk = inner ? jk : 1, km = inner ? jk - 1 : D.nx;
-    return -G.dz[IX(D, ji, kk, jl)] * w[IX(D, ji, kk, jl)]
-         - G.dx[IX(D, ji, kk, jl)] * hcov_x<double, double>(D, G, u, w, ji, kk, jl)
-         + G.dz[IX(D, ji, km, jl)] * w[IX(D, ji, km, jl)]
-         + G.dx[IX(D, ji, kk, jl - 1)] * hcov_x<double, double>(D, G, u, w, ji, kk, jl - 1);
+    return -G.dz[IX(D, ji, kk, jl)] * T(w[IX(D, ji, kk, jl)])
+         - G.dx[IX(D, ji, kk, jl)] * hcov_x<T, double>(D, G, u, w, ji, kk, jl)
+         + G.dz[IX(D, ji, km, jl)] * T(w[IX(D, ji, km, jl)])
+         + G.dx[IX(D, ji, kk, jl - 1)] * hcov_x<T, double>(D, G, u, w, ji, kk, jl - 1);
   }
   const int nl = D.nl, NL = D.NL;
   const bool inner = jk >= 2 && jk <= D.nx;
   int kk = jk;
   if (D.freeslip && D.periodic && jk == D.nx + 1) kk = 1;
-  double r = G.dx[IX(D, ji, kk, nl)] * hcov_x<double, double>(D, G, u, w, ji, kk, nl);
+  T r = G.dx[IX(D, ji, kk, nl)] * hcov_x<T, double>(D, G, u, w, ji, kk, nl);
   if (D.freeslip && (inner || (D.periodic && kk == 1))) {
     const int km = (kk == 1) ? D.nx : kk - 1;
-    r = r + 0.5 * G.dz[IX(D, ji, km, NL)] * w[IX(D, ji, km, NL)]
-          - 0.5 * G.dz[IX(D, ji, kk, NL)] * w[IX(D, ji, kk, NL)]
-          - G.dx[IX(D, ji, kk, nl)] * (u[IX(D, ji, kk, nl)]
-          + (u[IX(D, ji, kk, nl - 1)] - u[IX(D, ji, kk, nl)]) / (G.z_u[IX(D, ji, kk, nl - 1)] - G.z_u[IX(D, ji, kk, nl)])
-          * (0.5 * (G.z_w[IX(D, ji, km, NL)] + G.z_w[IX(D, ji, kk, NL)]) - G.z_u[IX(D, ji, kk, nl)])
-          + 0.5 * (w[IX(D, ji, km, NL)] + w[IX(D, ji, kk, NL)])
+    r = r + T(0.5) * G.dz[IX(D, ji, km, NL)] * T(w[IX(D, ji, km, NL)])
+          - T(0.5) * G.dz[IX(D, ji, kk, NL)] * T(w[IX(D, ji, kk, NL)])
+          - G.dx[IX(D, ji, kk, nl)] * (T(u[IX(D, ji, kk, nl)])
+          + (T(u[IX(D, ji, kk, nl - 1)]) - T(u[IX(D, ji, kk, nl)])) / (G.z_u[IX(D, ji, kk, nl - 1)] - G.z_u[IX(D, ji, kk, nl)])
+          * (T(0.5) * (G.z_w[IX(D, ji, km, NL)] + G.z_w[IX(D, ji, kk, NL)]) - G.z_u[IX(D, ji, kk, nl)])
+          + T(0.5) * (T(w[IX(D, ji, km, NL)]) + T(w[IX(D, ji, kk, NL)]))
           * (G.z_w[IX(D, ji, kk, NL)] - G.z_w[IX(D, ji, km, NL)]) / G.dx[IX(D, ji, kk, nl)]);
   }
   return r;
 }
 
 // density at a horizontal vorticity point (two scalar columns a and b), mo_vorticities.F90:240-266
-__device__ __forceinline__ double rho_avg_h(const Dims& D, const Grid<double>& G, const double* rho,
-                                            int ia, int ka, int ib, int kb, int jl) {
-  const double* zs = G.z_scalar;
+template <class T>
+__device__ __forceinline__ T rho_avg_h(const Dims& D, const Grid<T>& G, const double* rho, int ia, int ka, int ib,
+                                       int kb, int jl) {
+  const T* zs = G.z_scalar;
+  auto R = [&](int i, int k, int l) { return T(rho[IX(D, i, k, l)]); };
   if (jl == 1) {
-    return 0.5 * (rho[IX(D, ia, ka, jl)]
-      + (D.toa - zs[IX(D, ia, ka, jl)]) * (rho[IX(D, ia, ka, jl)] - rho[IX(D, ia, ka, jl + 1)])
+    return T(0.5) * (R(ia, ka, jl)
+      + (T(D.toa) - zs[IX(D, ia, ka, jl)]) * (R(ia, ka, jl) - R(ia, ka, jl + 1))
         / (zs[IX(D, ia, ka, jl)] - zs[IX(D, ia, ka, jl + 1)])
-      + rho[IX(D, ib, kb, jl)]
-      + (D.toa - zs[IX(D, ib, kb, jl)]) * (rho[IX(D, ib, kb, jl)] - rho[IX(D, ib, kb, jl + 1)])
+      + R(ib, kb, jl)
+      + (T(D.toa) - zs[IX(D, ib, kb, jl)]) * (R(ib, kb, jl) - R(ib, kb, jl + 1))
         / (zs[IX(D, ib, kb, jl)] - zs[IX(D, ib, kb, jl + 1)]));
   }
   if (jl == D.NL) {
-    const double* zw = G.z_w;
-    return 0.5 * (rho[IX(D, ia, ka, jl - 1)]
-      + (zw[IX(D, ia, ka, jl)] - zs[IX(D, ia, ka, jl - 1)]) * (rho[IX(D, ia, ka, jl - 2)] - rho[IX(D, ia, ka, jl - 1)])
+    const T* zw = G.z_w;
+    return T(0.5) * (R(ia, ka, jl - 1)
+      + (zw[IX(D, ia, ka, jl)] - zs[IX(D, ia, ka, jl - 1)]) * (R(ia, ka, jl - 2) - R(ia, ka, jl - 1))
         / (zs[IX(D, ia, ka, jl - 2)] - zs[IX(D, ia, ka, jl - 1)])
-      + rho[IX(D, ib, kb, jl - 1)]
-      + (zw[IX(D, ib, kb, jl)] - zs[IX(D, ib, kb, jl - 1)]) * (rho[IX(D, ib, kb, jl - 2)] - rho[IX(D, ib, kb, jl - 1)])
+      + R(ib, kb, jl - 1)
+      + (zw[IX(D, ib, kb, jl)] - zs[IX(D, ib, kb, jl - 1)]) * (R(ib, kb, jl - 2) - R(ib, kb, jl - 1))
         / (zs[IX(D, ib, kb, jl - 2)] - zs[IX(D, ib, kb, jl - 1)]));
   }
-  return 0.25 * (rho[IX(D, ia, ka, jl - 1)] + rho[IX(D, ib, kb, jl - 1)] + rho[IX(D, ia, ka, jl)] + rho[IX(D, ib, kb, jl)]);
+  return T(0.25) * (R(ia, ka, jl - 1) + R(ib, kb, jl - 1) + R(ia, ka, jl) + R(ib, kb, jl));
 }
 
 // eta_x at (ji,jk,jl), jl in 1..nl+1
-__device__ __forceinline__ double eta_x_at(const Dims& D, const Grid<double>& G, const State& S, int ji, int jk, int jl) {
+template <class T>
+__device__ __forceinline__ T eta_x_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
   if (D.periodic && ji == D.ny + 1) ji = 1;  // eta_x(ny+1,:,:) = eta_x(1,:,:) after the division
-  double z = 0.0;
+  T z = T(0);
   if (!D.llinear) {
     const int lev = (jl == 1) ? 2 : jl;  // zeta_x(:,:,1) = zeta_x(:,:,2) after the division
-    z = zeta_x_raw(D, G, S, ji, jk, lev) / G.area_dual_x[IX(D, ji, jk, lev)];
+    z = zeta_x_raw<T>(D, G, S, ji, jk, lev) / G.area_dual_x[IX(D, ji, jk, lev)];
   }
-  double e = D.lcorio ? z + G.fvec_x[IX(D, ji, jk, 1)] : z;
+  T e = D.lcorio ? z + G.fvec_x[IX(D, ji, jk, 1)] : z;
   const bool inner = ji >= 2 && ji <= D.ny;
   if (inner || D.periodic) {
     const int ia = inner ? ji - 1 : D.ny, ib = inner ? ji : 1;
-    e = e / rho_avg_h(D, G, S.rho + (long long)(D.g - 1) * D.fstride, ia, jk, ib, jk, jl);
+    e = e / rho_avg_h<T>(D, G, S.rho + (long long)(D.g - 1) * D.fstride, ia, jk, ib, jk, jl);
   }
   return e;
 }
 
 // eta_y at (ji,jk,jl)
-__device__ __forceinline__ double eta_y_at(const Dims& D, const Grid<double>& G, const State& S, int ji, int jk, int jl) {
+template <class T>
+__device__ __forceinline__ T eta_y_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
   if (D.periodic && jk == D.nx + 1) jk = 1;
-  double z = 0.0;
+  T z = T(0);
   if (!D.llinear) {
     const int lev = (jl == 1) ? 2 : jl;
-    z = zeta_y_raw(D, G, S, ji, jk, lev) / G.area_dual_y[IX(D, ji, jk, lev)];
+    z = zeta_y_raw<T>(D, G, S, ji, jk, lev) / G.area_dual_y[IX(D, ji, jk, lev)];
   }
-  double e = D.lcorio ? z + G.fvec_y[IX(D, ji, jk, 1)] : z;
+  T e = D.lcorio ? z + G.fvec_y[IX(D, ji, jk, 1)] : z;
   const bool inner = jk >= 2 && jk <= D.nx;
   if (inner || D.periodic) {
     const int ka = inner ? jk - 1 : D.nx, kb = inner ? jk : 1;
-    e = e / rho_avg_h(D, G, S.rho + (long long)(D.g - 1) * D.fstride, ji, ka, ji, kb, jl);
+    e = e / rho_avg_h<T>(D, G, S.rho + (long long)(D.g - 1) * D.fstride, ji, ka, ji, kb, jl);
   }
   return e;
 }
 
 // eta_z at (ji,jk,jl), mo_vorticities.F90:176-186 and :377-419
-__device__ __forceinline__ double eta_z_at(const Dims& D, const Grid<double>& G, const State& S, int ji, int jk, int jl) {
+template <class T>
+__device__ __forceinline__ T eta_z_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
   if (D.periodic) {
     if (ji == D.ny + 1) ji = 1;
     if (jk == D.nx + 1) jk = 1;
   }
-  double z = 0.0;
-  if (!D.llinear) z = rel_vort_z_local<double, double>(D, G, S.u, S.v, ji, jk, jl) / G.area_dual_z[IX(D, ji, jk, jl)];
-  double e = D.lcorio ? z + G.fvec_z[IX(D, ji, jk, 1)] : z;
+  T z = T(0);
+  if (!D.llinear) z = rel_vort_z_local<T, double>(D, G, S.u, S.v, ji, jk, jl) / G.area_dual_z[IX(D, ji, jk, jl)];
+  T e = D.lcorio ? z + G.fvec_z[IX(D, ji, jk, 1)] : z;
   const bool inner = ji >= 2 && ji <= D.ny && jk >= 2 && jk <= D.nx;
   if (inner || D.periodic) {
     const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
     const int km = (jk == 1) ? D.nx : jk - 1, im = (ji == 1) ? D.ny : ji - 1;
-    e = e / (0.25 * (rg[IX(D, ji, km, jl)] + rg[IX(D, ji, jk, jl)] + rg[IX(D, im, jk, jl)] + rg[IX(D, im, km, jl)]));
+    e = e / (T(0.25) * (T(rg[IX(D, ji, km, jl)]) + T(rg[IX(D, ji, jk, jl)]) + T(rg[IX(D, im, jk, jl)]) +
+                        T(rg[IX(D, im, km, jl)])));
   }
   return e;
 }
 
 // TRSK term for u, mo_vorticity_flux.F90:33-45 (km, kk, kp: columns jk-1, jk, jk+1)
-__device__ __forceinline__ double trsk_u(const Dims& D, const Grid<double>& G, const double* vp, const double* up,
-                                         const double* ez, int ji, int km, int kk, int kp, int jl) {
-  const double w1 = G.trsk_u[0][ji - 1], w2 = G.trsk_u[1][ji - 1], w3 = G.trsk_u[2][ji - 1];
+template <class T>
+__device__ __forceinline__ T trsk_u(const Dims& D, const Grid<T>& G, const T* vp, const T* up, const T* ez,
+                                    int ji, int km, int kk, int kp, int jl) {
+  const T w1 = G.trsk_u[0][ji - 1], w2 = G.trsk_u[1][ji - 1], w3 = G.trsk_u[2][ji - 1];
 #define EZ(i, k) ez[IX(D, i, k, jl)]
-  return w1 * vp[IX(D, ji, km, jl)] * 0.25 * (EZ(ji, km) + EZ(ji, kk) + EZ(ji, kk) + EZ(ji + 1, kk))
-       + w2 * up[IX(D, ji, km, jl)] * 0.25 * (EZ(ji, km) + EZ(ji + 1, km) + EZ(ji, kk) + EZ(ji + 1, kk))
-       + w3 * vp[IX(D, ji + 1, km, jl)] * 0.25 * (EZ(ji + 1, km) + EZ(ji + 1, kk) + EZ(ji, kk) + EZ(ji + 1, kk))
-       + w3 * vp[IX(D, ji + 1, kk, jl)] * 0.25 * (EZ(ji + 1, kk) + EZ(ji + 1, kp) + EZ(ji, kk) + EZ(ji + 1, kk))
-       + w2 * up[IX(D, ji, kp, jl)] * 0.25 * (EZ(ji + 1, kp) + EZ(ji, kp) + EZ(ji, kk) + EZ(ji + 1, kk))
-       + w1 * vp[IX(D, ji, kk, jl)] * 0.25 * (EZ(ji, kk) + EZ(ji, kp) + EZ(ji, kk) + EZ(ji + 1, kk));
+  return w1 * vp[IX(D, ji, km, jl)] * T(0.25) * (EZ(ji, km) + EZ(ji, kk) + EZ(ji, kk) + EZ(ji + 1, kk))
+       + w2 * up[IX(D, ji, km, jl)] * T(0.25) * (EZ(ji, km) + EZ(ji + 1, km) + EZ(ji, kk) + EZ(ji + 1, kk))
+       + w3 * vp[IX(D, ji + 1, km, jl)] * T(0.25) * (EZ(ji + 1, km) + EZ(ji + 1, kk) + EZ(ji, kk) + EZ(ji + 1, kk))
+       + w3 * vp[IX(D, ji + 1, kk, jl)] * T(0.25) * (EZ(ji + 1, kk) + EZ(ji + 1, kp) + EZ(ji, kk) + EZ(ji + 1, kk))
+       + w2 * up[IX(D, ji, kp, jl)] * T(0.25) * (EZ(ji + 1, kp) + EZ(ji, kp) + EZ(ji, kk) + EZ(ji + 1, kk))
+       + w1 * vp[IX(D, ji, kk, jl)] * T(0.25) * (EZ(ji, kk) + EZ(ji, kp) + EZ(ji, kk) + EZ(ji + 1, kk));
 }
 
 // TRSK term for v, mo_vorticity_flux.F90:72-80 (im, ii: rows ji-1, ji)
-__device__ __forceinline__ double trsk_v(const Dims& D, const Grid<double>& G, const double* up, const double* ez,
-                                         int im, int ii, int jk, int jl) {
-  const double w1 = G.trsk_v[0][ii - 1], w2 = G.trsk_v[1][ii - 1];
-  return w1 * up[IX(D, ii, jk, jl)] * 0.25 * (EZ(ii, jk) + EZ(ii + 1, jk) + EZ(ii, jk) + EZ(ii, jk + 1))
-       + w1 * up[IX(D, ii, jk + 1, jl)] * 0.25 * (EZ(ii, jk + 1) + EZ(ii + 1, jk + 1) + EZ(ii, jk) + EZ(ii, jk + 1))
-       + w2 * up[IX(D, im, jk + 1, jl)] * 0.25 * (EZ(im, jk + 1) + EZ(ii, jk + 1) + EZ(ii, jk) + EZ(ii, jk + 1))
-       + w2 * up[IX(D, im, jk, jl)] * 0.25 * (EZ(im, jk) + EZ(ii, jk) + EZ(ii, jk) + EZ(ii, jk + 1));
+template <class T>
+__device__ __forceinline__ T trsk_v(const Dims& D, const Grid<T>& G, const T* up, const T* ez, int im, int ii, int jk,
+                                    int jl) {
+  const T w1 = G.trsk_v[0][ii - 1], w2 = G.trsk_v[1][ii - 1];
+  return w1 * up[IX(D, ii, jk, jl)] * T(0.25) * (EZ(ii, jk) + EZ(ii + 1, jk) + EZ(ii, jk) + EZ(ii, jk + 1))
+       + w1 * up[IX(D, ii, jk + 1, jl)] * T(0.25) * (EZ(ii, jk + 1) + EZ(ii + 1, jk + 1) + EZ(ii, jk) + EZ(ii, jk + 1))
+       + w2 * up[IX(D, im, jk + 1, jl)] * T(0.25) * (EZ(im, jk + 1) + EZ(ii, jk + 1) + EZ(ii, jk) + EZ(ii, jk + 1))
+       + w2 * up[IX(D, im, jk, jl)] * T(0.25) * (EZ(im, jk) + EZ(ii, jk) + EZ(ii, jk) + EZ(ii, jk + 1));
 #undef EZ
 }
 
-// ---- kernels (kernels_fp64.cu, column_fp64.cu) ----------------------------------
-__global__ void k_temperature(Dims D, Grid<double> G, State S, double* T);
-__global__ void k_theta(Dims D, Grid<double> G, const double* tp, double* out, int mode);
-__global__ void k_grad_vert(Dims D, Grid<double> G, const double* s, double* rz);
-__global__ void k_grad_hor(Dims D, Grid<double> G, const double* s, const double* rz, double* rx, double* ry);
-__global__ void k_div_h(Dims D, Grid<double> G, const double* vx, const double* vy, double* out);
-__global__ void k_theta_edges(Dims D, Grid<double> G, const double* th, const double* Dv, const double* u,
-                              const double* v, double* tvu, double* tvv);
+#define LG_IDX3                                              \
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
+  const int jl = blockIdx.z + 1
+
+// ---- kernels --------------------------------------------------------------------
+
+// temperature_diagnostics, mo_derived.F90:18-38
+template <class T>
+__global__ void k_temperature(Dims D, Grid<T> G, State S, T* Tm) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long i = IX(D, ji, jk, jl);
+  T t = (G.theta_v_bg[i] + T(S.tp[i])) * (G.exner_bg[i] + T(S.ep[i]));
+  if (D.lmoist) {
+    const T rg = T(S.rho[i + (long long)(D.g - 1) * D.fstride]);
+    const T rv = T(S.rho[i + (long long)D.g * D.fstride]);
+    t = t / (T(1) + rv / rg * T(kM_D / kM_V - 1.0));
+  }
+  Tm[i] = t;
+}
+
+// diag%scalar_placeholder = theta_v_bg + theta_v_pert (mode 0) or theta_v_pert (mode 1)
+template <class T>
+__global__ void k_theta(Dims D, Grid<T> G, const double* tp, T* out, int mode) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long i = IX(D, ji, jk, jl);
+  out[i] = mode == 0 ? G.theta_v_bg[i] + T(tp[i]) : T(tp[i]);
+}
+
+// grad_vert, mo_gradient_operators.F90:65-83 (levels 2..nl); launched with blockIdx.z = jl-2
+template <class T, class S>
+__global__ void k_grad_vert(Dims D, Grid<T> G, const S* s, T* rz) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.z + 2;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  rz[IX(D, ji, jk, jl)] = T(s[IX(D, ji, jk, jl - 1)] - s[IX(D, ji, jk, jl)]) / G.dz[IX(D, ji, jk, jl)];
+}
+
+// grad_hor, mo_gradient_operators.F90:17-63 + :85-130, u and v points of layer jl
+template <class T, class S>
+__global__ void k_grad_hor(Dims D, Grid<T> G, const S* s, const T* rz, T* rx, T* ry) {
+  LG_IDX3;
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    T r;
+    if (grad_x_cov<T, S>(D, G, s, ji, jk, jl, &r)) {
+      if (jl > D.nf) r = r - G.slope_x[IX(D, ji, jk, jl)] * remap_x<T, T>(D, G, rz, ji, jk, jl);
+      rx[IX(D, ji, jk, jl)] = r;
+    }
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    T r;
+    if (grad_y_cov<T, S>(D, G, s, ji, jk, jl, &r)) {
+      if (jl > D.nf) r = r - G.slope_y[IX(D, ji, jk, jl)] * remap_y<T, T>(D, G, rz, ji, jk, jl);
+      ry[IX(D, ji, jk, jl)] = r;
+    }
+  }
+}
+
+// div_h, mo_divergence_operators.F90:16-68
+template <class T>
+__global__ void k_div_h(Dims D, Grid<T> G, const T* vx, const T* vy, T* out) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  auto fx = [&](int i, int j, int k) { return vx[IX(D, i, j, k)]; };
+  auto fy = [&](int i, int j, int k) { return vy[IX(D, i, j, k)]; };
+  out[IX(D, ji, jk, jl)] = div_h_at<T>(D, G, fx, fy, ji, jk, jl);
+}
+
+// theta_v_adv_3rd_order edge values, mo_multiplications.F90:134-202
+template <class T>
+__global__ void k_theta_edges(Dims D, Grid<T> G, const T* th, const T* Dv, const double* u, const double* v,
+                              T* tvu, T* tvv) {
+  LG_IDX3;
+  const T c = T(1.0 / 8.0 * D.dyn * D.dxn);
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    T t;
+    if (theta_edge_u<T>(D, th, Dv, u, c, ji, jk, jl, &t)) tvu[IX(D, ji, jk, jl)] = t;
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    T t;
+    if (theta_edge_v<T>(D, th, Dv, v, c, ji, jk, jl, &t)) tvv[IX(D, ji, jk, jl)] = t;
+  }
+}
+
+// calc_pot_vort, mo_vorticities.F90:189-421 with rel_vort :19-187 inlined:
+// eta_x (ny+1,nx,nl+1) and eta_y (ny,nx+1,nl+1)
+template <class T>
+__global__ void k_eta_xy(Dims D, Grid<T> G, State S, T* ex, T* ey) {
+  LG_IDX3;
+  if (jl > D.NL) return;
+  if (ji <= D.ny + 1 && jk <= D.nx) ex[IX(D, ji, jk, jl)] = eta_x_at<T>(D, G, S, ji, jk, jl);
+  if (ji <= D.ny && jk <= D.nx + 1) ey[IX(D, ji, jk, jl)] = eta_y_at<T>(D, G, S, ji, jk, jl);
+}
+
+// eta_z (ny+1,nx+1,nl)
+template <class T>
+__global__ void k_eta_z(Dims D, Grid<T> G, State S, T* ez) {
+  LG_IDX3;
+  if (ji > D.ny + 1 || jk > D.nx + 1) return;
+  ez[IX(D, ji, jk, jl)] = eta_z_at<T>(D, G, S, ji, jk, jl);
+}
+
+// mass flux densities, mo_vector_tend_expl.F90:64-66 (scalar_times_vector_h/_v)
+template <class T>
+__global__ void k_mass_flux(Dims D, Grid<T> G, State S, T* uph, T* vph, T* wph) {
+  LG_IDX3;
+  const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
+    T f;
+    if (stv_h_x<T>(D, rg, S.u, ji, jk, jl, &f)) uph[IX(D, ji, jk, jl)] = f;
+  }
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
+    T f;
+    if (stv_h_y<T>(D, rg, S.v, ji, jk, jl, &f)) vph[IX(D, ji, jk, jl)] = f;
+  }
+  if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    wph[q] = T(0.5) * (T(rg[IX(D, ji, jk, jl - 1)]) + T(rg[q])) * T(S.w[q]);
+  }
+}
+
+// calc_vorticity_flux_term, mo_vorticity_flux.F90:16-171
+template <class T>
+__global__ void k_vort_flux(Dims D, Grid<T> G, State S, const T* ex, const T* ey, const T* ez, const T* uph,
+                            const T* vph, const T* wph, T* px, T* py, T* pz) {
+  LG_IDX3;
+  // vertical mass flux with the free-slip surface value, mo_vector_tend_expl.F90:68-80
+  auto wp = [&](int i, int j, int k) -> T {
+    if (k == D.NL) {
+      if (!D.freeslip) return T(0);
+      const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+      const T dv = T(rg[IX(D, i, j, D.nl)]) + (T(rg[IX(D, i, j, D.nl - 1)]) - T(rg[IX(D, i, j, D.nl)]))
+                   / (G.z_scalar[IX(D, i, j, D.nl - 1)] - G.z_scalar[IX(D, i, j, D.nl)])
+                   * (G.z_w[IX(D, i, j, D.NL)] - G.z_scalar[IX(D, i, j, D.nl)]);
+      return dv * T(S.w[IX(D, i, j, D.NL)]);
+    }
+    return wph[IX(D, i, j, k)];
+  };
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
+    const bool inner = jk >= 2 && jk <= D.nx;
+    if (inner || D.periodic) {
+      const int kk = inner ? jk : 1, km = inner ? jk - 1 : D.nx, kp = kk + 1;
+      T r = trsk_u<T>(D, G, vph, uph, ez, ji, km, kk, kp, jl);
+      r = r - T(0.5) * W_(5, ji, km, jl) * wp(ji, km, jl) * ey[IX(D, ji, kk, jl)]
+            - T(0.5) * W_(6, ji, km, jl) * wp(ji, km, jl + 1) * ey[IX(D, ji, kk, jl + 1)]
+            - T(0.5) * W_(5, ji, kk, jl) * wp(ji, kk, jl) * ey[IX(D, ji, kk, jl)]
+            - T(0.5) * W_(6, ji, kk, jl) * wp(ji, kk, jl + 1) * ey[IX(D, ji, kk, jl + 1)];
+      px[IX(D, ji, jk, jl)] = r;
+    }
+  }
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
+    const bool inner = ji >= 2 && ji <= D.ny;
+    if (inner || D.periodic) {
+      const int ii = inner ? ji : 1, im = inner ? ji - 1 : D.ny;
+      T r = trsk_v<T>(D, G, uph, ez, im, ii, jk, jl);
+      r = r + T(0.5) * W_(5, im, jk, jl) * wp(im, jk, jl) * ex[IX(D, ii, jk, jl)]
+            + T(0.5) * W_(6, im, jk, jl) * wp(im, jk, jl + 1) * ex[IX(D, ii, jk, jl + 1)]
+            + T(0.5) * W_(5, ii, jk, jl) * wp(ii, jk, jl) * ex[IX(D, ii, jk, jl)]
+            + T(0.5) * W_(6, ii, jk, jl) * wp(ii, jk, jl + 1) * ex[IX(D, ii, jk, jl + 1)];
+      py[IX(D, ji, jk, jl)] = r;
+    }
+  }
+  if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
+    pz[IX(D, ji, jk, jl)] = T(0.5) * (
+        W_(1, ji, jk, jl - 1) * uph[IX(D, ji, jk + 1, jl - 1)] * ey[IX(D, ji, jk + 1, jl)]
+      - W_(2, ji, jk, jl - 1) * vph[IX(D, ji, jk, jl - 1)] * ex[IX(D, ji, jk, jl)]
+      + W_(3, ji, jk, jl - 1) * uph[IX(D, ji, jk, jl - 1)] * ey[IX(D, ji, jk, jl)]
+      - W_(4, ji, jk, jl - 1) * vph[IX(D, ji + 1, jk, jl - 1)] * ex[IX(D, ji + 1, jk, jl)]
+      + W_(1, ji, jk, jl) * uph[IX(D, ji, jk + 1, jl)] * ey[IX(D, ji, jk + 1, jl)]
+      - W_(2, ji, jk, jl) * vph[IX(D, ji, jk, jl)] * ex[IX(D, ji, jk, jl)]
+      + W_(3, ji, jk, jl) * uph[IX(D, ji, jk, jl)] * ey[IX(D, ji, jk, jl)]
+      - W_(4, ji, jk, jl) * vph[IX(D, ji + 1, jk, jl)] * ex[IX(D, ji + 1, jk, jl)]);
+  }
+}
+
+// inner_product of the wind with itself, mo_inner_product.F90:16-50
+template <class T>
+__global__ void k_ke(Dims D, Grid<T> G, State S, T* out) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  out[IX(D, ji, jk, jl)] = inner_product_at<T>(D, G, S.u, S.v, S.w, ji, jk, jl);
+}
+
+// combination of the explicit wind tendencies, mo_vector_tend_expl.F90:258-310, and the
+// forward step of the horizontal wind, mo_manage_pchevi.F90:86-89 (in FP64)
+template <class T>
+__global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C, int rk_step) {
+  LG_IDX3;
+  const T new_weight = (rk_step == 2) ? T(0.5) : T(1);
+  const T old_weight = T(1) - new_weight;
+  const T chw = T(0.5 + kIMPL_THERMO_WEIGHT);
+  const T ohw = T(1.0 - (0.5 + kIMPL_THERMO_WEIGHT));
+  const T cvw = T(1.0 - kIMPL_THERMO_WEIGHT);
+  const T no_bg_switch = D.luse_bg ? T(0) : T(1);
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
+    const long long q = IX(D, ji, jk, jl);
+    const T t = old_weight * Tn.u[q] + new_weight * (ohw * T(C.old_u[q]) - chw * (T(C.nl_u[q]) + T(C.l_u[q]))
+                - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
+    Tn.u[q] = t;
+    Sn.u[q] = So.u[q] + D.dtime * double(t);
+  }
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    const T t = old_weight * Tn.v[q] + new_weight * (ohw * T(C.old_v[q]) - chw * (T(C.nl_v[q]) + T(C.l_v[q]))
+                - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
+    Tn.v[q] = t;
+    Sn.v[q] = So.v[q] + D.dtime * double(t);
+  }
+  if (jl <= D.NL && ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (-(cvw * (T(C.nl_w[q]) + T(C.l_w[q])))
+              - no_bg_switch * (T(1) - cvw) * T(C.l_w[q]) - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+  }
+}
+
+// scalar_tend_expl for every constituent other than the gas, mo_scalar_tend_expl.F90:102-128
+// with scalar_times_vector_h_upstream (mo_multiplications.F90:206-287) and div_h_tracers
+// (mo_divergence_operators.F90:70-147) evaluated inline.
+template <class T>
+__global__ void k_tracers(Dims D, Grid<T> G, State Ss, const double* u_new, const double* v_new, T* t_rho,
+                          int rk_step) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  auto wx = [&](int i, int j, int k) { return T(u_new[IX(D, i, j, k)]); };
+  auto wy = [&](int i, int j, int k) { return T(v_new[IX(D, i, j, k)]); };
+  // contravariant vertical velocity corrections do not depend on the constituent
+  T cu = T(0), cl = T(0);
+  if (jl == D.nf) cl = vcc<T>(D, G, wx, wy, ji, jk, jl + 1);
+  else if (jl == D.nl) cu = vcc<T>(D, G, wx, wy, ji, jk, jl);
+  else if (jl > D.nf) { cu = vcc<T>(D, G, wx, wy, ji, jk, jl); cl = vcc<T>(D, G, wx, wy, ji, jk, jl + 1); }
+  const T new_weight = (rk_step == 2) ? T(0.5) : T(1);
+  const T old_weight = T(1) - new_weight;
+  for (int jc = 1; jc <= D.ncons; ++jc) {
+    if (jc == D.g) continue;
+    const double* r = Ss.rho + (long long)(jc - 1) * D.fstride;
+    auto fx = [&](int i, int j, int k) { T f; return upstream_x<T>(D, r, u_new, i, j, k, &f) ? f : T(0); };
+    auto fy = [&](int i, int j, int k) { T f; return upstream_y<T>(D, r, v_new, i, j, k, &f) ? f : T(0); };
+    const T comp_h = fx(ji, jk + 1, jl) * G.area_x[IX(D, ji, jk + 1, jl)]
+                   + fy(ji, jk, jl) * G.area_y[IX(D, ji, jk, jl)]
+                   - fx(ji, jk, jl) * G.area_x[IX(D, ji, jk, jl)]
+                   - fy(ji + 1, jk, jl) * G.area_y[IX(D, ji + 1, jk, jl)];
+    T comp_v = T(0);
+    if (jl == D.nf) {
+      const T dl = (cl <= T(0)) ? T(r[IX(D, ji, jk, jl)]) : T(r[IX(D, ji, jk, jl + 1)]);
+      comp_v = -dl * cl * G.area_z[IX(D, ji, jk, jl + 1)];
+    } else if (jl == D.nl) {
+      const T du = (cu <= T(0)) ? T(r[IX(D, ji, jk, jl - 1)]) : T(r[IX(D, ji, jk, jl)]);
+      comp_v = du * cu * G.area_z[IX(D, ji, jk, jl)];
+    } else if (jl > D.nf) {
+      const T du = (cu <= T(0)) ? T(r[IX(D, ji, jk, jl - 1)]) : T(r[IX(D, ji, jk, jl)]);
+      const T dl = (cl <= T(0)) ? T(r[IX(D, ji, jk, jl)]) : T(r[IX(D, ji, jk, jl + 1)]);
+      comp_v = du * cu * G.area_z[IX(D, ji, jk, jl)] - dl * cl * G.area_z[IX(D, ji, jk, jl + 1)];
+    }
+    const T div = (comp_h + comp_v) / G.volume[q];
+    T* t = t_rho + (long long)(jc - 1) * D.fstride;
+    t[q] = old_weight * t[q] + new_weight * (-div);
+  }
+}
+
+// scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177
+template <class T>
+__global__ void k_gas_theta(Dims D, Grid<T> G, State Ss, const double* u_new, const double* v_new, const T* tvu,
+                            const T* tvv, const T* Tm, const T* rad, const T* csh, T* t_rho, T* t_rt) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  const double* rg = Ss.rho + (long long)(D.g - 1) * D.fstride;
+  auto fx = [&](int i, int j, int k) { T f; return stv_h_x<T>(D, rg, u_new, i, j, k, &f) ? f : T(0); };
+  auto fy = [&](int i, int j, int k) { T f; return stv_h_y<T>(D, rg, v_new, i, j, k, &f) ? f : T(0); };
+  const T div_m = div_h_at<T>(D, G, fx, fy, ji, jk, jl);
+  t_rho[q + (long long)(D.g - 1) * D.fstride] = -div_m;  // old_weight 0, new_weight 1 for the gas
+  T div_t;
+  if (D.theta_order == 2) {
+    auto th = [&](int i, int j, int k) { const long long p = IX(D, i, j, k); return G.theta_v_bg[p] + T(Ss.tp[p]); };
+    auto gx = [&](int i, int j, int k) { T f; return stv_h_x_fn<T>(D, th, fx, i, j, k, &f) ? f : T(0); };
+    auto gy = [&](int i, int j, int k) { T f; return stv_h_y_fn<T>(D, th, fy, i, j, k, &f) ? f : T(0); };
+    div_t = div_h_at<T>(D, G, gx, gy, ji, jk, jl);
+  } else {
+    auto gx = [&](int i, int j, int k) { return tvu[IX(D, i, j, k)] * fx(i, j, k); };
+    auto gy = [&](int i, int j, int k) { return tvv[IX(D, i, j, k)] * fy(i, j, k); };
+    div_t = div_h_at<T>(D, G, gx, gy, ji, jk, jl);
+  }
+  const T heat = rad[q] + csh[q];
+  T x = T(0);
+  if (heat != T(0)) {
+    const T cv = c_v_mass_weighted_air<T>(D, Ss.rho, Tm, q);
+    x = T(kC_D_V) * T(rg[q]) / cv * heat / (T(kC_D_P) * (G.exner_bg[q] + T(Ss.ep[q])));
+  }
+  t_rt[q] = -div_t + x;
+}
+
+// ---- FP64-only kernels (kernels_fp64.cu, column_fp64.cu) -------------------------------
 __global__ void k_pgrad(Dims D, Grid<double> G, State S, const double* gx, const double* gy, const double* gz,
-                        const double* tvu, const double* tvv, const double* tpu, const double* tpv, PGrad P, int lfirst);
-__global__ void k_eta_xy(Dims D, Grid<double> G, State S, double* ex, double* ey);
-__global__ void k_eta_z(Dims D, Grid<double> G, State S, double* ez);
-__global__ void k_mass_flux(Dims D, Grid<double> G, State S, double* uph, double* vph, double* wph);
-__global__ void k_vort_flux(Dims D, Grid<double> G, State S, const double* ex, const double* ey, const double* ez,
-                            const double* uph, const double* vph, const double* wph, double* px, double* py, double* pz);
-__global__ void k_ke(Dims D, Grid<double> G, State S, double* out);
-__global__ void k_tend_wind(Dims D, State So, State Sn, Tend Tn, Carried C, int rk_step);
-__global__ void k_tracers(Dims D, Grid<double> G, State Ss, const double* u_new, const double* v_new,
-                          double* t_rho, int rk_step);
-__global__ void k_gas_theta(Dims D, Grid<double> G, State Ss, const double* u_new, const double* v_new,
-                            const double* tvu, const double* tvv, const double* T, const double* rad,
-                            const double* csh, double* t_rho, double* t_rt);
-__global__ void k_column_ver(Dims D, Grid<double> G, State So, State Sn, Tend Tn, int rk_step);
+                        const double* tvu, const double* tvv, const double* tpu, const double* tpv, PGrad<double> P,
+                        int lfirst);
+__global__ void k_column_ver(Dims D, Grid<double> G, State So, State Sn, Tend<double> Tn, int rk_step);
 __global__ void k_column_tracers(Dims D, Grid<double> G, State So, State Sn, const double* t_rho, const double* T,
                                  double* csh, int rk_step);
 

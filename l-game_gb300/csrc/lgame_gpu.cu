@@ -47,7 +47,7 @@ struct lgame_gpu {
   double* trsk_v[2] = {};
   double* damp = nullptr;
   State st[2];
-  Tend tend;
+  Tend<double> tend;
   double *pg_nl_u, *pg_nl_v, *pg_nl_w, *pg_l_u, *pg_l_v, *pg_l_w, *pg_old_u, *pg_old_v, *pgcw;
   double *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
   // scratch
@@ -216,6 +216,28 @@ __global__ void k_budget_final(const double* part, double* out, int nq) {
   }
 }
 
+// FP64 instantiations of the kernel templates of kernels.cuh (this file is compiled with
+// -fmad=false like the rest of the FP64 step)
+namespace kd {
+const auto k_temperature = lg::k_temperature<double>;
+const auto k_theta = lg::k_theta<double>;
+const auto k_grad_vert = lg::k_grad_vert<double, double>;
+const auto k_grad_hor = lg::k_grad_hor<double, double>;
+const auto k_div_h = lg::k_div_h<double>;
+const auto k_theta_edges = lg::k_theta_edges<double>;
+const auto k_eta_xy = lg::k_eta_xy<double>;
+const auto k_eta_z = lg::k_eta_z<double>;
+const auto k_mass_flux = lg::k_mass_flux<double>;
+const auto k_vort_flux = lg::k_vort_flux<double>;
+const auto k_ke = lg::k_ke<double>;
+const auto k_tend_wind = lg::k_tend_wind<double>;
+const auto k_tracers = lg::k_tracers<double>;
+const auto k_gas_theta = lg::k_gas_theta<double>;
+const auto k_pgrad = lg::k_pgrad;
+const auto k_column_ver = lg::k_column_ver;
+const auto k_column_tracers = lg::k_column_tracers;
+}  // namespace kd
+
 dim3 blk() { return dim3(32, 8, 1); }
 dim3 grd(const Dims& D, int rows, int cols, int levs) {
   return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 7) / 8), (unsigned)levs);
@@ -240,11 +262,11 @@ int klaunch_check(lgame_gpu* c, const char* what) {
 // (mode 0) or tp (mode 1): gradient, divergence, edge values into (ou, ov)
 int theta3(lgame_gpu* c, const double* tp, int mode, const double* u, const double* v, double* ou, double* ov) {
   const Dims& D = c->D;
-  LAUNCH(k_theta, grd(D, D.ny, D.nx, D.nl), D, c->G, tp, c->theta, mode);
-  LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->theta, c->gz);
-  LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->gz, c->gx, c->gy);
-  LAUNCH(k_div_h, grd(D, D.ny, D.nx, D.nl), D, c->G, c->gx, c->gy, c->divf);
-  LAUNCH(k_theta_edges, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->divf, u, v, ou, ov);
+  LAUNCH(kd::k_theta, grd(D, D.ny, D.nx, D.nl), D, c->G, tp, c->theta, mode);
+  LAUNCH(kd::k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->theta, c->gz);
+  LAUNCH(kd::k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->gz, c->gx, c->gy);
+  LAUNCH(kd::k_div_h, grd(D, D.ny, D.nx, D.nl), D, c->G, c->gx, c->gy, c->divf);
+  LAUNCH(kd::k_theta_edges, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->theta, c->divf, u, v, ou, ov);
   return LGAME_OK;
 }
 
@@ -252,15 +274,15 @@ int theta3(lgame_gpu* c, const double* tp, int mode, const double* u, const doub
 int advection(lgame_gpu* c, const State& S) {
   const Dims& D = c->D;
   if (!(!D.llinear || D.lcorio)) return LGAME_OK;
-  LAUNCH(k_eta_xy, grd(D, D.ny + 1, D.nx + 1, D.NL), D, c->G, S, c->ex, c->ey);
-  LAUNCH(k_eta_z, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ez);
-  LAUNCH(k_mass_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->uph, c->vph, c->wph);
-  LAUNCH(k_vort_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ex, c->ey, c->ez, c->uph, c->vph, c->wph,
+  LAUNCH(kd::k_eta_xy, grd(D, D.ny + 1, D.nx + 1, D.NL), D, c->G, S, c->ex, c->ey);
+  LAUNCH(kd::k_eta_z, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ez);
+  LAUNCH(kd::k_mass_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->uph, c->vph, c->wph);
+  LAUNCH(kd::k_vort_flux, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, S, c->ex, c->ey, c->ez, c->uph, c->vph, c->wph,
          c->pvt_x, c->pvt_y, c->pvt_z);
   if (!D.llinear) {
-    LAUNCH(k_ke, grd(D, D.ny, D.nx, D.nl), D, c->G, S, c->vsq);
-    LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->vsq, c->vsg_z);
-    LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->vsq, c->vsg_z, c->vsg_x, c->vsg_y);
+    LAUNCH(kd::k_ke, grd(D, D.ny, D.nx, D.nl), D, c->G, S, c->vsq);
+    LAUNCH(kd::k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, c->G, c->vsq, c->vsg_z);
+    LAUNCH(kd::k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, c->G, c->vsq, c->vsg_z, c->vsg_x, c->vsg_y);
   }
   return LGAME_OK;
 }
@@ -270,9 +292,9 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
   const State& So = c->st[so];
   const State& Sn = c->st[sn];
   const Grid<double>& G = c->G;
-  LAUNCH(k_temperature, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature);
-  PGrad P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw};
-  Carried C{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw,
+  LAUNCH(kd::k_temperature, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature);
+  PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw};
+  Carried<double> C{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw,
             c->vsg_x, c->vsg_y, c->vsg_z, c->pvt_x, c->pvt_y, c->pvt_z};
   for (int rk = 1; rk <= 2; ++rk) {
     const State& Sv = (rk == 1) ? So : Sn;   // state of vector_tend_expl
@@ -284,35 +306,56 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
         if (rc != LGAME_OK) return rc;
         if (D.luse_bg) { rc = theta3(c, So.tp, 1, So.u, So.v, c->tpu, c->tpv); if (rc != LGAME_OK) return rc; }
       }
-      LAUNCH(k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, G, So.ep, c->gz);
-      LAUNCH(k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So.ep, c->gz, c->gx, c->gy);
-      LAUNCH(k_pgrad, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, c->gx, c->gy, c->gz, c->tvu, c->tvv, c->tpu, c->tpv,
+      LAUNCH(kd::k_grad_vert, grd(D, D.ny, D.nx, D.nl - 1), D, G, So.ep, c->gz);
+      LAUNCH(kd::k_grad_hor, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So.ep, c->gz, c->gx, c->gy);
+      LAUNCH(kd::k_pgrad, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, c->gx, c->gy, c->gz, c->tvu, c->tvv, c->tpu, c->tpv,
              P, step == 0 ? 1 : 0);
     }
     if (rk == 2 || step == 0) {
       int rc = advection(c, Sv);
       if (rc != LGAME_OK) return rc;
     }
-    Tend T = c->tend;
-    LAUNCH(k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk);
+    Tend<double> T = c->tend;
+    LAUNCH(kd::k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk);
     // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
     const State& Ss = (rk == 1) ? So : Sn;
-    if (D.ncons > 1) LAUNCH(k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
+    if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
     if (D.theta_order == 3) {
       int rc = theta3(c, Ss.tp, 0, Ss.u, Ss.v, c->tvu, c->tvv);
       if (rc != LGAME_OK) return rc;
     }
-    LAUNCH(k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->rad,
+    LAUNCH(kd::k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->rad,
            c->csh, T.rho, T.rt);
     // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
     {
       dim3 g2((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 7) / 8), 1);
-      LAUNCH(k_column_ver, g2, D, G, So, Sn, T, rk);
-      if (D.ncons > 1) LAUNCH(k_column_tracers, g2, D, G, So, Sn, T.rho, c->temperature, c->csh, rk);
+      LAUNCH(kd::k_column_ver, g2, D, G, So, Sn, T, rk);
+      if (D.ncons > 1) LAUNCH(kd::k_column_tracers, g2, D, G, So, Sn, T.rho, c->temperature, c->csh, rk);
     }
   }
   return LGAME_OK;
 }
+
+// split mode keeps the diagnostics that the FP32 stencils produce in FP32 buffers; they
+// are converted to/from the FP64 arrays of the C ABI on set_diag (to_split) and get_diag
+int split_sync_carried(lgame_gpu* c, bool to_split) {
+  const SplitCarriedF F = split_carried(c->split);
+  const long long n = c->D.fstride;
+  struct Pair { double* d; float* f; long long n; };
+  const Pair pairs[] = {{c->pgcw, F.pgcw, n}, {c->vsg_x, F.vsg_x, n}, {c->vsg_y, F.vsg_y, n}, {c->vsg_z, F.vsg_z, n},
+                        {c->pvt_x, F.pvt_x, n}, {c->pvt_y, F.pvt_y, n}, {c->pvt_z, F.pvt_z, n}, {c->csh, F.csh, n},
+                        {c->rad, F.rad, n}, {c->temperature, F.temperature, n}, {c->tend.rho, F.tend.rho, n * c->D.ncons},
+                        {c->tend.rt, F.tend.rt, n}, {c->tend.u, F.tend.u, n}, {c->tend.v, F.tend.v, n},
+                        {c->tend.w, F.tend.w, n}};
+  for (const Pair& p : pairs) {
+    const int rc = to_split ? split_convert(p.d, p.f, p.n, c->stream) : split_convert_back(p.f, p.d, p.n, c->stream);
+    if (rc != LGAME_OK) return set_err(rc, "conversion of the split-mode diagnostics failed");
+  }
+  return LGAME_OK;
+}
+
+int trace_begin_cb(void* c, const char* name) { return lg::trace_begin((lgame_gpu*)c, name); }
+void trace_end_cb(void* c, int slot) { lg::trace_end((lgame_gpu*)c, slot); }
 
 int check_cfg(const lgame_config* cfg) {
   if (cfg->ny < 3 || cfg->nx < 3) return set_err(LGAME_ERR_BAD_DIMS, "ny and nx must be >= 3");
@@ -576,7 +619,7 @@ extern "C" int lgame_gpu_set_diag(lgame_gpu* c, const double* const* f, int nfie
     }
   }
   if (c->split) {
-    int rc = split_sync_from_fp64(c->split, c->D, c->rad, c->stream);
+    int rc = split_sync_carried(c, true);
     if (rc != LGAME_OK) return rc;
   }
   CK(cudaStreamSynchronize(c->stream));
@@ -586,6 +629,10 @@ extern "C" int lgame_gpu_set_diag(lgame_gpu* c, const double* const* f, int nfie
 extern "C" int lgame_gpu_get_diag(lgame_gpu* c, double* const* f, int nfields) {
   if (!c || !f || nfields != LGAME_DIAG_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_get_diag: bad arguments");
   const Dims& D = c->D;
+  if (c->split) {
+    int rc = split_sync_carried(c, false);
+    if (rc != LGAME_OK) return rc;
+  }
   for (int i = 0; i < nfields; ++i) {
     if (!f[i]) continue;
     const Ext e = diag_ext(D, i);
@@ -608,8 +655,10 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
   c->kernels_last_step = 0;
   int rc;
   if (c->split) {
-    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], c->tend, c->temperature, c->rad, c->csh,
-                    total_step_counter, c->stream, &c->kernels_last_step);
+    PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v,
+                    c->pgcw};
+    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], P, total_step_counter, c->stream,
+                    &c->kernels_last_step, c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
   } else {
     rc = step_fp64(c, old_slot, new_slot, total_step_counter);
   }
@@ -690,6 +739,7 @@ int trace_begin(lgame_gpu* c, const char* name) {
     c->ev_pool.push_back(e);
   }
   cudaEventRecord(c->ev_pool[idx], c->stream);
+  if (std::strncmp(name, "kd::", 4) == 0) name += 4;
   c->ev_used.push_back({name, idx});
   return idx;
 }

@@ -1,5 +1,17 @@
 // split.cuh -- FP32/FP64 split-precision HEVI step (interface used by lgame_gpu.cu).
+//
+// FP32: explicit stencils (vorticity, Poisson-bracket flux, the kinetic-energy gradient's
+//       division by the metric, third-order theta edges), scalar and tracer flux
+//       divergences, tracer fall speeds and vertical fluxes, intermediate and tendency
+//       storage.
+// FP64: the state, its accumulation state_old + dt*tendency, the gradient of the Exner
+//       pressure perturbation and both pressure-gradient products (the hydrostatic
+//       background subtraction), the kinetic energy and its differences (a vertical
+//       difference over a thin layer cancels most of its digits), the vertically implicit
+//       column solves, the budget sums.
 #pragma once
+
+#include <cuda_runtime.h>
 
 #include "kernels.cuh"
 
@@ -7,13 +19,24 @@ namespace lg {
 
 struct SplitCtx;
 
+// diagnostic buffers of the split step that correspond to lgame_gpu.h's carried fields
+struct SplitCarriedF {
+  float *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
+  Tend<float> tend;
+};
+
 int split_create(const Dims& D, SplitCtx** out, long long* bytes);
 void split_destroy(SplitCtx* s);
-// converts the FP64 grid of the context into the FP32 metric copies the stencils read
+// builds the FP32 metric copies and the FP64 reciprocal metrics from the FP64 grid
 int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream);
-// refreshes FP32 copies of host-provided diagnostics (radiation tendency)
-int split_sync_from_fp64(SplitCtx* s, const Dims& D, const double* rad, cudaStream_t stream);
-int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn, const Tend& T,
-               double* temperature, const double* rad, double* csh, int step, cudaStream_t stream, int* nkernels);
+// the FP32 carried buffers of the split step, for conversion to and from FP64 arrays
+SplitCarriedF split_carried(SplitCtx* s);
+// converts n elements FP64 <-> FP32 (field layout identical)
+int split_convert(const double* src, float* dst, long long n, cudaStream_t stream);
+int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream);
+// one step; pg holds the FP64 pressure-gradient arrays (shared with the FP64 path)
+int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn,
+               const PGrad<double>& pg, int step, cudaStream_t stream, int* nkernels,
+               int (*trace_begin)(void*, const char*), void (*trace_end)(void*, int), void* tracer);
 
 }  // namespace lg
