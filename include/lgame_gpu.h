@@ -218,6 +218,28 @@ int  lgame_gpu_pchevi_host(lgame_gpu* ctx, const double* const* state_old,
  * Synchronises. */
 int  lgame_gpu_budgets(lgame_gpu* ctx, int slot, double* out, int nout);
 
+/* The same budget vector as lgame_gpu_budgets (bit for bit), computed without allocating
+ * any memory, host or device.  No counterpart in the reference.
+ *
+ * For hosts that must not allocate inside their time loop: drivers that reserve all
+ * memory at start-up and run the loop under an allocation guard (a malloc hook, or a
+ * device memory pool with a fixed cap), and hosts whose device memory is fully committed
+ * to model state (a 1024x1024x80 split-precision context holds about 108 GB, so a few
+ * ensemble members fill a GPU).  lgame_gpu_budgets allocates a small host array on every
+ * call; this entry point uses a fixed scratch array compiled into the library instead:
+ * 1024*11 + 11 doubles (90,200 bytes) per device, which is why at most LGAME_BUDGETS_MAX
+ * (11) quantities, i.e. n_constituents <= 7, are accepted (more: LGAME_ERR_INVALID_ARG).
+ *
+ * - The first call on each device looks up the scratch address (cudaGetSymbolAddress)
+ *   with that device current; make that first call before any stream capture begins.
+ * - There is one scratch array per device, shared by all contexts on that device: calls
+ *   that overlap in time on one device (several host threads, or several contexts of the
+ *   same device used concurrently) race on it and return wrong sums.  Calls from a single
+ *   host thread never overlap, since the function returns after the result is copied.
+ * - The context's device is made current for the call and the caller's device restored.
+ * Synchronises. */
+int  lgame_gpu_budgets_static(lgame_gpu* ctx, int slot, double* out, int nout);
+
 /* Blocks until all work of the context has finished. */
 int  lgame_gpu_synchronize(lgame_gpu* ctx);
 

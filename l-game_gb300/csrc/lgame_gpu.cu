@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -791,4 +792,105 @@ extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   for (void* p : c->allocations) cudaFree(p);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
+}
+
+// ---- lgame_gpu_budgets_static: the budget sums without any allocation -------------------
+// The same two reduction kernels as lgame_gpu_budgets (so the same sums, bit for bit), with
+// their scratch in a file-scope device array instead of the context's reduce_buf.  The
+// array is part of the loaded module: one instance per device, no cudaMalloc, and the call
+// allocates no host memory either (the result is copied straight into the caller's array).
+//
+// Size: kRedBlocks partial sums for each of at most LGAME_BUDGETS_MAX budget quantities,
+// plus the LGAME_BUDGETS_MAX results: (1024 * 11 + 11) doubles = 90,200 bytes per device.
+// Nothing in it has to start at zero: k_budget_partial writes every partial sum before
+// k_budget_final reads it, and k_budget_final writes every result before it is copied out.
+constexpr int kStaticBudgetDoubles = kRedBlocks * LGAME_BUDGETS_MAX + LGAME_BUDGETS_MAX;
+static __device__ __align__(256) double g_budget_scratch[kStaticBudgetDoubles];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_budget_scratch_mu;
+double* g_budget_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_budget_scratch on device dev (which must be current), looked up
+// with cudaGetSymbolAddress the first time dev is seen and cached afterwards.
+int budget_scratch_address(int dev, double** out) {
+  std::lock_guard<std::mutex> lock(g_budget_scratch_mu);
+  if (!g_budget_scratch_addr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_budget_scratch);
+    if (e != cudaSuccess || !p) {
+      char msg[256];
+      std::snprintf(msg, sizeof msg, "lgame_gpu_budgets_static: cudaGetSymbolAddress of the scratch array on device %d: %s",
+                    dev, cudaGetErrorString(e));
+      lgame_set_error(msg);
+      return LGAME_ERR_CUDA;
+    }
+    g_budget_scratch_addr[dev] = static_cast<double*>(p);
+  }
+  *out = g_budget_scratch_addr[dev];
+  return LGAME_OK;
+}
+
+int budgets_static_on_device(lgame_gpu* c, int slot, double* out, int nq) {
+  double* scratch = nullptr;
+  int rc = budget_scratch_address(c->cfg.device, &scratch);
+  if (rc != LGAME_OK) return rc;
+  const Dims& D = c->D;
+  double* dout = scratch + (size_t)kRedBlocks * LGAME_BUDGETS_MAX;
+  k_budget_partial<<<kRedBlocks, kRedThreads, 0, c->stream>>>(D, c->G, c->st[slot], c->temperature, scratch, nq);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_budget_final<<<1, 32, 0, c->stream>>>(scratch, dout, nq);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, sizeof(double) * nq, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg, "lgame_gpu_budgets_static: %s", cudaGetErrorString(e));
+    lgame_set_error(msg);
+    return LGAME_ERR_CUDA;
+  }
+  out[D.ncons + 1] = 0.5 * out[D.ncons + 1];
+  return LGAME_OK;
+}
+}  // namespace
+
+extern "C" int lgame_gpu_budgets_static(lgame_gpu* c, int slot, double* out, int nout) {
+  if (!c || !out || slot < 0 || slot > 1) {
+    lgame_set_error("lgame_gpu_budgets_static: bad arguments");
+    return LGAME_ERR_INVALID_ARG;
+  }
+  const int nq = c->D.ncons + 4;
+  if (nq > LGAME_BUDGETS_MAX) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg,
+                  "lgame_gpu_budgets_static: %d budget quantities exceed the static scratch, which holds at most "
+                  "LGAME_BUDGETS_MAX = %d (n_constituents <= 7)", nq, LGAME_BUDGETS_MAX);
+    lgame_set_error(msg);
+    return LGAME_ERR_INVALID_ARG;
+  }
+  if (nout < nq) {
+    lgame_set_error("lgame_gpu_budgets_static: output array smaller than n_constituents+4");
+    return LGAME_ERR_INVALID_ARG;
+  }
+  const int dev = c->cfg.device;
+  if (dev < 0 || dev >= kMaxDevices) {
+    lgame_set_error("lgame_gpu_budgets_static: device ordinal outside 0..63");
+    return LGAME_ERR_INVALID_ARG;
+  }
+  // the context's device is made current for the call and the caller's device restored
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) {
+    lgame_set_error("lgame_gpu_budgets_static: cudaGetDevice failed");
+    return LGAME_ERR_CUDA;
+  }
+  if (prev != dev && cudaSetDevice(dev) != cudaSuccess) {
+    lgame_set_error("lgame_gpu_budgets_static: cudaSetDevice failed");
+    return LGAME_ERR_CUDA;
+  }
+  const int rc = budgets_static_on_device(c, slot, out, nq);
+  if (prev != dev) cudaSetDevice(prev);
+  return rc;
 }
