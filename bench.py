@@ -48,8 +48,10 @@ def read_peaks() -> dict:
 
 # Algorithmic (compulsory) bytes per cell of one launch: every distinct array a kernel
 # touches, read or written once per cell.  Entries are (n8, nT, n8_oro, nT_oro):
-#   n8  arrays stored in FP64 on both paths (the state, the pressure-gradient products,
-#       the FP64 metrics and reciprocals of the column solvers),
+#   n8  arrays stored in FP64 (the state, the pressure-gradient products, the FP64 metrics
+#       and reciprocals of the column solvers); the split stencils read the FP32 mirror of
+#       the state instead, so there they count 4 B (except the kinetic energy and the wind
+#       update, which keep FP64 state arrays),
 #   nT  arrays of the kernel's working type (8 B on the FP64 path, 4 B on the split path:
 #       FP32 metric copies, intermediates, tendencies, carried stencil diagnostics),
 #   *_oro  arrays read only in the terrain-following layers jl >= n_flat_layers (slopes,
@@ -74,6 +76,8 @@ def _kernel_fields(ncons: int) -> dict:
         "tend_wind": (12, 13, 0, 0),                   # u, v old/new, 8 pressure-gradient arrays; 3 tendencies r/w, 7 carried
         "tracers": (ntr + 2, 2 * ntr + 3, 0, 7),       # rho_jc, u, v; tend r/w per tracer, area_x/y, volume
         "gas_theta": (3, 9, 0, 7),                     # rho_g, u, v; 2 theta edges, area_x/y, volume, rad, csh, 2 out
+        "gas_flux": (0, 9, 0, 0),                      # rho_g, u, v, 2 theta edges; 4 fluxes out
+        "gas_div": (0, 11, 0, 7),                      # 4 fluxes, area_x/y, volume, rad, csh; 2 tendencies out
     }
 
 
@@ -109,19 +113,32 @@ def kernel_bytes_per_cell(name: str, ncons: int, split: bool, f_oro: float) -> f
         f = _kernel_fields(ncons).get(name[2:])
         return 0.0 if f is None else 8.0 * (f[0] + f[1] + f_oro * (f[2] + f[3]))
     split_own = {
-        # FP64: state old 5, new at rk2 2, 5 writes, exner_bg, theta_bg, z_scalar,
-        # inv_volume, inv_area_z, damping; FP32: 3 tendencies, gravity
-        "ks_column_ver": 18 * 8.0 + 4 * 4.0,
-        # FP64: rho old/new per tracer, w old/new, inv_volume, rho_g; FP32: tendency per tracer, T, area_z, csh
-        "ks_column_tracers": (2 * ntr + 4) * 8.0 + (ntr + 3) * 4.0,
-        # FP64: exner', all rho, inv dx/dy/dz, 3 background gradients, 8 products written,
-        # 4 previous read; FP32: 4 theta edges, gravity, pgcw
-        "ks_pgrad": (1 + ncons + 3 + 3 + 8 + 4) * 8.0 + 6 * 4.0,
+        # FP64: state old (rho_g, rho*theta, exner', theta', w), theta_bg, 5 new values written;
+        # FP32: mirror old (rho_g, rho*theta, exner', w), mirror new at rk2 (3, half the launches),
+        # exner_bg, damping, dz, d(exner_bg), 1/volume, 1/area_z, 3 tendencies, 5 mirror values written
+        "ks_column_ver": 11 * 8.0 + 19.5 * 4.0,
+        # FP64: rho old and new per tracer; FP32: mirror old, tendency and mirror new per tracer,
+        # w old/new, rho_g, T, area_z, 1/volume, sediment heating r/w
+        "ks_column_tracers": 2 * ntr * 8.0 + (3 * ntr + 8) * 4.0,
+        # FP64: exner', its vertical gradient, 1/dx, 1/dy, slopes, 2 weights, 3 background
+        # gradients, gravity, 8 products written, 4 previous read; FP32: all rho (mirror),
+        # 4 theta edges, pgcw
+        "ks_pgrad": 24 * 8.0 + (ncons + 5) * 4.0,
+        # FP64: exner' read, 1/dz read, gradient written
+        "ks_gzp": 3 * 8.0,
     }
     if name in split_own:
         return split_own[name]
-    f = _kernel_fields(ncons).get(name[3:])
-    return 0.0 if f is None else 8.0 * (f[0] + f_oro * f[2]) + 4.0 * (f[1] + f_oro * f[3])
+    base = name[3:]
+    f = _kernel_fields(ncons).get(base)
+    if f is None:
+        return 0.0
+    # the split stencils read the FP32 mirror of the state; the kinetic energy and the wind
+    # update keep FP64 state arrays (the latter also writes the two mirror winds)
+    if base in ("ke", "tend_wind"):
+        extra = 2 if base == "tend_wind" else 0
+        return 8.0 * (f[0] + f_oro * f[2]) + 4.0 * (f[1] + extra + f_oro * f[3])
+    return 4.0 * (f[0] + f[1] + f_oro * (f[2] + f[3]))
 
 
 class ClockSampler:

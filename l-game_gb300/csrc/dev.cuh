@@ -46,9 +46,14 @@ struct Grid {
   const T* damp;                            // Klemp prefactor 1+damping_coeff*dtime at w points
 };
 
-struct State {
-  double *rho, *rt, *tp, *ep, *u, *v, *w;  // rho: ncons fields of fstride each
+// prognostic state on the device; V = double: the state proper, V = float: the FP32 mirror
+// of the split-precision step (rounded copies written by the kernels that update the state)
+template <class V>
+struct StateT {
+  V *rho, *rt, *tp, *ep, *u, *v, *w;  // rho: ncons fields of fstride each
 };
+using State = StateT<double>;
+using StateF = StateT<float>;
 
 // physical constants, src/mo_constants.F90:12-37
 constexpr double kR_E = 6371000.789927;

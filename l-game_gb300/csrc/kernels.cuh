@@ -60,46 +60,46 @@ __device__ __forceinline__ bool grad_y_cov(const Dims& D, const Grid<T>& G, cons
 }
 
 // theta_v_adv_3rd_order x edge, mo_multiplications.F90:136-183
-template <class T>
-__device__ __forceinline__ bool theta_edge_u(const Dims& D, const T* th, const T* Dv, const double* u,
+template <class T, class V>
+__device__ __forceinline__ bool theta_edge_u(const Dims& D, const T* th, const T* Dv, const V* u,
                                              T c, int ji, int jk, int jl, T* out) {
   if (jk >= 2 && jk <= D.nx) {
     T t = T(0.5) * (th[IX(D, ji, jk - 1, jl)] + th[IX(D, ji, jk, jl)]);
-    if (u[IX(D, ji, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, jk - 1, jl)];
+    if (u[IX(D, ji, jk, jl)] >= V(0)) t = t - c * Dv[IX(D, ji, jk - 1, jl)];
     else t = t - c * Dv[IX(D, ji, jk, jl)];
     *out = t;
     return true;
   }
   if (!D.periodic) return false;
   T t = T(0.5) * (th[IX(D, ji, D.nx, jl)] + th[IX(D, ji, 1, jl)]);
-  if (u[IX(D, ji, 1, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, D.nx, jl)];
+  if (u[IX(D, ji, 1, jl)] >= V(0)) t = t - c * Dv[IX(D, ji, D.nx, jl)];
   else t = t - c * Dv[IX(D, ji, 1, jl)];
   *out = t;
   return true;
 }
 
 // theta_v_adv_3rd_order y edge, mo_multiplications.F90:152-200
-template <class T>
-__device__ __forceinline__ bool theta_edge_v(const Dims& D, const T* th, const T* Dv, const double* v,
+template <class T, class V>
+__device__ __forceinline__ bool theta_edge_v(const Dims& D, const T* th, const T* Dv, const V* v,
                                              T c, int ji, int jk, int jl, T* out) {
   if (ji >= 2 && ji <= D.ny) {
     T t = T(0.5) * (th[IX(D, ji, jk, jl)] + th[IX(D, ji - 1, jk, jl)]);
-    if (v[IX(D, ji, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, ji, jk, jl)];
+    if (v[IX(D, ji, jk, jl)] >= V(0)) t = t - c * Dv[IX(D, ji, jk, jl)];
     else t = t - c * Dv[IX(D, ji - 1, jk, jl)];
     *out = t;
     return true;
   }
   if (!D.periodic) return false;
   T t = T(0.5) * (th[IX(D, 1, jk, jl)] + th[IX(D, D.ny, jk, jl)]);
-  if (v[IX(D, 1, jk, jl)] >= 0.0) t = t - c * Dv[IX(D, 1, jk, jl)];
+  if (v[IX(D, 1, jk, jl)] >= V(0)) t = t - c * Dv[IX(D, 1, jk, jl)];
   else t = t - c * Dv[IX(D, D.ny, jk, jl)];
   *out = t;
   return true;
 }
 
 // scalar_times_vector_h, mo_multiplications.F90:34-54 (state scalar and vector)
-template <class T>
-__device__ __forceinline__ bool stv_h_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, T* r) {
+template <class T, class V>
+__device__ __forceinline__ bool stv_h_x(const Dims& D, const V* s, const V* vx, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
     *r = T(0.5) * (T(s[IX(D, ji, jk - 1, jl)]) + T(s[IX(D, ji, jk, jl)])) * T(vx[IX(D, ji, jk, jl)]);
     return true;
@@ -108,8 +108,8 @@ __device__ __forceinline__ bool stv_h_x(const Dims& D, const double* s, const do
   *r = T(0.5) * (T(s[IX(D, ji, 1, jl)]) + T(s[IX(D, ji, D.nx, jl)])) * T(vx[IX(D, ji, 1, jl)]);
   return true;
 }
-template <class T>
-__device__ __forceinline__ bool stv_h_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, T* r) {
+template <class T, class V>
+__device__ __forceinline__ bool stv_h_y(const Dims& D, const V* s, const V* vy, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
     *r = T(0.5) * (T(s[IX(D, ji - 1, jk, jl)]) + T(s[IX(D, ji, jk, jl)])) * T(vy[IX(D, ji, jk, jl)]);
     return true;
@@ -135,34 +135,34 @@ __device__ __forceinline__ bool stv_h_y_fn(const Dims& D, FS s, FV vy, int ji, i
 }
 
 // scalar_times_vector_h_upstream, mo_multiplications.F90:222-285
-template <class T>
-__device__ __forceinline__ bool upstream_x(const Dims& D, const double* s, const double* vx, int ji, int jk, int jl, T* r) {
+template <class T, class V>
+__device__ __forceinline__ bool upstream_x(const Dims& D, const V* s, const V* vx, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
-    const double u = vx[IX(D, ji, jk, jl)];
-    *r = (u >= 0.0) ? T(s[IX(D, ji, jk - 1, jl)]) * T(u) : T(s[IX(D, ji, jk, jl)]) * T(u);
+    const V u = vx[IX(D, ji, jk, jl)];
+    *r = (u >= V(0)) ? T(s[IX(D, ji, jk - 1, jl)]) * T(u) : T(s[IX(D, ji, jk, jl)]) * T(u);
     return true;
   }
   if (!D.periodic) return false;
-  const double u = vx[IX(D, ji, 1, jl)];
-  *r = (u >= 0.0) ? T(s[IX(D, ji, D.nx, jl)]) * T(u) : T(s[IX(D, ji, 1, jl)]) * T(u);
+  const V u = vx[IX(D, ji, 1, jl)];
+  *r = (u >= V(0)) ? T(s[IX(D, ji, D.nx, jl)]) * T(u) : T(s[IX(D, ji, 1, jl)]) * T(u);
   return true;
 }
-template <class T>
-__device__ __forceinline__ bool upstream_y(const Dims& D, const double* s, const double* vy, int ji, int jk, int jl, T* r) {
+template <class T, class V>
+__device__ __forceinline__ bool upstream_y(const Dims& D, const V* s, const V* vy, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
-    const double v = vy[IX(D, ji, jk, jl)];
-    *r = (v >= 0.0) ? T(s[IX(D, ji, jk, jl)]) * T(v) : T(s[IX(D, ji - 1, jk, jl)]) * T(v);
+    const V v = vy[IX(D, ji, jk, jl)];
+    *r = (v >= V(0)) ? T(s[IX(D, ji, jk, jl)]) * T(v) : T(s[IX(D, ji - 1, jk, jl)]) * T(v);
     return true;
   }
   if (!D.periodic) return false;
-  const double v = vy[IX(D, 1, jk, jl)];
-  *r = (v >= 0.0) ? T(s[IX(D, 1, jk, jl)]) * T(v) : T(s[IX(D, D.ny, jk, jl)]) * T(v);
+  const V v = vy[IX(D, 1, jk, jl)];
+  *r = (v >= V(0)) ? T(s[IX(D, 1, jk, jl)]) * T(v) : T(s[IX(D, D.ny, jk, jl)]) * T(v);
   return true;
 }
 
 // sum(state%rho(:,:,:,1:nc+1),4) in constituent order
-template <class T>
-__device__ __forceinline__ T rho_sum_cond_gas(const Dims& D, const double* rho, long long q) {
+template <class T, class V>
+__device__ __forceinline__ T rho_sum_cond_gas(const Dims& D, const V* rho, long long q) {
   T s = T(0);
   for (int jc = 0; jc <= D.nc; ++jc) s = s + T(rho[q + (long long)jc * D.fstride]);
   return s;
@@ -195,8 +195,8 @@ __device__ __forceinline__ float c_p_cond(int jc, float temperature) {
 }
 
 // c_v_mass_weighted_air, mo_derived.F90:157-187
-template <class T>
-__device__ __forceinline__ T c_v_mass_weighted_air(const Dims& D, const double* rho, const T* Tm, long long q) {
+template <class T, class V>
+__device__ __forceinline__ T c_v_mass_weighted_air(const Dims& D, const V* rho, const T* Tm, long long q) {
   T c = T(0);
   for (int jc = 1; jc <= D.nc; ++jc) c = c + T(rho[q + (long long)(jc - 1) * D.fstride]) * c_p_cond(jc, Tm[q]);
   if (D.lmoist) {
@@ -209,9 +209,9 @@ __device__ __forceinline__ T c_v_mass_weighted_air(const Dims& D, const double* 
 }
 
 // inner_product, mo_inner_product.F90:16-50 (both vectors the state wind)
-template <class T>
-__device__ __forceinline__ T inner_product_at(const Dims& D, const Grid<T>& G, const double* u, const double* v,
-                                              const double* w, int ji, int jk, int jl) {
+template <class T, class V>
+__device__ __forceinline__ T inner_product_at(const Dims& D, const Grid<T>& G, const V* u, const V* v,
+                                              const V* w, int ji, int jk, int jl) {
   const T a = T(u[IX(D, ji, jk + 1, jl)]), b = T(v[IX(D, ji, jk, jl)]), c = T(u[IX(D, ji, jk, jl)]);
   const T d = T(v[IX(D, ji + 1, jk, jl)]), e = T(w[IX(D, ji, jk, jl)]), f = T(w[IX(D, ji, jk, jl + 1)]);
   return W_(1, ji, jk, jl) * a * a + W_(2, ji, jk, jl) * b * b + W_(3, ji, jk, jl) * c * c
@@ -221,24 +221,24 @@ __device__ __forceinline__ T inner_product_at(const Dims& D, const Grid<T>& G, c
 // ---- potential vorticity, mo_vorticities.F90 -----------------------------------
 
 // rel_vort x-component before the division by the area, mo_vorticities.F90:33-93
-template <class T>
-__device__ __forceinline__ T zeta_x_raw(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
-  const double* v = S.v; const double* w = S.w;
+template <class T, class V>
+__device__ __forceinline__ T zeta_x_raw(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
+  const V* v = S.v; const V* w = S.w;
   if (jl <= D.nl) {  // levels 2..nl
     const bool inner = ji >= 2 && ji <= D.ny;
     if (!inner && !D.periodic) return T(0);
     const int ii = inner ? ji : 1, im = inner ? ji - 1 : D.ny;
     return G.dz[IX(D, im, jk, jl)] * T(w[IX(D, im, jk, jl)])
-         - G.dy[IX(D, ii, jk, jl - 1)] * hcov_y<T, double>(D, G, v, w, ii, jk, jl - 1)
+         - G.dy[IX(D, ii, jk, jl - 1)] * hcov_y<T, V>(D, G, v, w, ii, jk, jl - 1)
          - G.dz[IX(D, ii, jk, jl)] * T(w[IX(D, ii, jk, jl)])
-         + G.dy[IX(D, ii, jk, jl)] * hcov_y<T, double>(D, G, v, w, ii, jk, jl);
+         + G.dy[IX(D, ii, jk, jl)] * hcov_y<T, V>(D, G, v, w, ii, jk, jl);
   }
   // surface level NL
   const int nl = D.nl, NL = D.NL;
   const bool inner = ji >= 2 && ji <= D.ny;
   int ii = ji;
   if (D.freeslip && D.periodic && ji == D.ny + 1) ii = 1;  // copy made after the free-slip addition
-  T r = -G.dy[IX(D, ii, jk, nl)] * hcov_y<T, double>(D, G, v, w, ii, jk, nl);
+  T r = -G.dy[IX(D, ii, jk, nl)] * hcov_y<T, V>(D, G, v, w, ii, jk, nl);
   if (D.freeslip && (inner || (D.periodic && ii == 1))) {
     const int im = (ii == 1) ? D.ny : ii - 1;
     r = r + T(0.5) * G.dz[IX(D, im, jk, NL)] * T(w[IX(D, im, jk, NL)])
@@ -253,23 +253,23 @@ __device__ __forceinline__ T zeta_x_raw(const Dims& D, const Grid<T>& G, const S
 }
 
 // rel_vort y-component before the division, mo_vorticities.F90:104-165
-template <class T>
-__device__ __forceinline__ T zeta_y_raw(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
-  const double* u = S.u; const double* w = S.w;
+template <class T, class V>
+__device__ __forceinline__ T zeta_y_raw(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
+  const V* u = S.u; const V* w = S.w;
   if (jl <= D.nl) {
     const bool inner = jk >= 2 && jk <= D.nx;
     if (!inner && !D.periodic) return T(0);
     const int kk = inner ? jk : 1, km = inner ? jk - 1 : D.nx;
     return -G.dz[IX(D, ji, kk, jl)] * T(w[IX(D, ji, kk, jl)])
-         - G.dx[IX(D, ji, kk, jl)] * hcov_x<T, double>(D, G, u, w, ji, kk, jl)
+         - G.dx[IX(D, ji, kk, jl)] * hcov_x<T, V>(D, G, u, w, ji, kk, jl)
          + G.dz[IX(D, ji, km, jl)] * T(w[IX(D, ji, km, jl)])
-         + G.dx[IX(D, ji, kk, jl - 1)] * hcov_x<T, double>(D, G, u, w, ji, kk, jl - 1);
+         + G.dx[IX(D, ji, kk, jl - 1)] * hcov_x<T, V>(D, G, u, w, ji, kk, jl - 1);
   }
   const int nl = D.nl, NL = D.NL;
   const bool inner = jk >= 2 && jk <= D.nx;
   int kk = jk;
   if (D.freeslip && D.periodic && jk == D.nx + 1) kk = 1;
-  T r = G.dx[IX(D, ji, kk, nl)] * hcov_x<T, double>(D, G, u, w, ji, kk, nl);
+  T r = G.dx[IX(D, ji, kk, nl)] * hcov_x<T, V>(D, G, u, w, ji, kk, nl);
   if (D.freeslip && (inner || (D.periodic && kk == 1))) {
     const int km = (kk == 1) ? D.nx : kk - 1;
     r = r + T(0.5) * G.dz[IX(D, ji, km, NL)] * T(w[IX(D, ji, km, NL)])
@@ -284,8 +284,8 @@ __device__ __forceinline__ T zeta_y_raw(const Dims& D, const Grid<T>& G, const S
 }
 
 // density at a horizontal vorticity point (two scalar columns a and b), mo_vorticities.F90:240-266
-template <class T>
-__device__ __forceinline__ T rho_avg_h(const Dims& D, const Grid<T>& G, const double* rho, int ia, int ka, int ib,
+template <class T, class V>
+__device__ __forceinline__ T rho_avg_h(const Dims& D, const Grid<T>& G, const V* rho, int ia, int ka, int ib,
                                        int kb, int jl) {
   const T* zs = G.z_scalar;
   auto R = [&](int i, int k, int l) { return T(rho[IX(D, i, k, l)]); };
@@ -310,8 +310,8 @@ __device__ __forceinline__ T rho_avg_h(const Dims& D, const Grid<T>& G, const do
 }
 
 // eta_x at (ji,jk,jl), jl in 1..nl+1
-template <class T>
-__device__ __forceinline__ T eta_x_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
+template <class T, class V>
+__device__ __forceinline__ T eta_x_at(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
   if (D.periodic && ji == D.ny + 1) ji = 1;  // eta_x(ny+1,:,:) = eta_x(1,:,:) after the division
   T z = T(0);
   if (!D.llinear) {
@@ -328,8 +328,8 @@ __device__ __forceinline__ T eta_x_at(const Dims& D, const Grid<T>& G, const Sta
 }
 
 // eta_y at (ji,jk,jl)
-template <class T>
-__device__ __forceinline__ T eta_y_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
+template <class T, class V>
+__device__ __forceinline__ T eta_y_at(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
   if (D.periodic && jk == D.nx + 1) jk = 1;
   T z = T(0);
   if (!D.llinear) {
@@ -346,18 +346,18 @@ __device__ __forceinline__ T eta_y_at(const Dims& D, const Grid<T>& G, const Sta
 }
 
 // eta_z at (ji,jk,jl), mo_vorticities.F90:176-186 and :377-419
-template <class T>
-__device__ __forceinline__ T eta_z_at(const Dims& D, const Grid<T>& G, const State& S, int ji, int jk, int jl) {
+template <class T, class V>
+__device__ __forceinline__ T eta_z_at(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
   if (D.periodic) {
     if (ji == D.ny + 1) ji = 1;
     if (jk == D.nx + 1) jk = 1;
   }
   T z = T(0);
-  if (!D.llinear) z = rel_vort_z_local<T, double>(D, G, S.u, S.v, ji, jk, jl) / G.area_dual_z[IX(D, ji, jk, jl)];
+  if (!D.llinear) z = rel_vort_z_local<T, V>(D, G, S.u, S.v, ji, jk, jl) / G.area_dual_z[IX(D, ji, jk, jl)];
   T e = D.lcorio ? z + G.fvec_z[IX(D, ji, jk, 1)] : z;
   const bool inner = ji >= 2 && ji <= D.ny && jk >= 2 && jk <= D.nx;
   if (inner || D.periodic) {
-    const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+    const V* rg = S.rho + (long long)(D.g - 1) * D.fstride;
     const int km = (jk == 1) ? D.nx : jk - 1, im = (ji == 1) ? D.ny : ji - 1;
     e = e / (T(0.25) * (T(rg[IX(D, ji, km, jl)]) + T(rg[IX(D, ji, jk, jl)]) + T(rg[IX(D, im, jk, jl)]) +
                         T(rg[IX(D, im, km, jl)])));
@@ -399,8 +399,8 @@ __device__ __forceinline__ T trsk_v(const Dims& D, const Grid<T>& G, const T* up
 // ---- kernels --------------------------------------------------------------------
 
 // temperature_diagnostics, mo_derived.F90:18-38
-template <class T>
-__global__ void k_temperature(Dims D, Grid<T> G, State S, T* Tm) {
+template <class T, class V = double>
+__global__ void k_temperature(Dims D, Grid<T> G, StateT<V> S, T* Tm) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long i = IX(D, ji, jk, jl);
@@ -414,8 +414,8 @@ __global__ void k_temperature(Dims D, Grid<T> G, State S, T* Tm) {
 }
 
 // diag%scalar_placeholder = theta_v_bg + theta_v_pert (mode 0) or theta_v_pert (mode 1)
-template <class T>
-__global__ void k_theta(Dims D, Grid<T> G, const double* tp, T* out, int mode) {
+template <class T, class V = double>
+__global__ void k_theta(Dims D, Grid<T> G, const V* tp, T* out, int mode) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long i = IX(D, ji, jk, jl);
@@ -463,8 +463,8 @@ __global__ void k_div_h(Dims D, Grid<T> G, const T* vx, const T* vy, T* out) {
 }
 
 // theta_v_adv_3rd_order edge values, mo_multiplications.F90:134-202
-template <class T>
-__global__ void k_theta_edges(Dims D, Grid<T> G, const T* th, const T* Dv, const double* u, const double* v,
+template <class T, class V = double>
+__global__ void k_theta_edges(Dims D, Grid<T> G, const T* th, const T* Dv, const V* u, const V* v,
                               T* tvu, T* tvv) {
   LG_IDX3;
   const T c = T(1.0 / 8.0 * D.dyn * D.dxn);
@@ -480,8 +480,8 @@ __global__ void k_theta_edges(Dims D, Grid<T> G, const T* th, const T* Dv, const
 
 // calc_pot_vort, mo_vorticities.F90:189-421 with rel_vort :19-187 inlined:
 // eta_x (ny+1,nx,nl+1) and eta_y (ny,nx+1,nl+1)
-template <class T>
-__global__ void k_eta_xy(Dims D, Grid<T> G, State S, T* ex, T* ey) {
+template <class T, class V = double>
+__global__ void k_eta_xy(Dims D, Grid<T> G, StateT<V> S, T* ex, T* ey) {
   LG_IDX3;
   if (jl > D.NL) return;
   if (ji <= D.ny + 1 && jk <= D.nx) ex[IX(D, ji, jk, jl)] = eta_x_at<T>(D, G, S, ji, jk, jl);
@@ -489,18 +489,18 @@ __global__ void k_eta_xy(Dims D, Grid<T> G, State S, T* ex, T* ey) {
 }
 
 // eta_z (ny+1,nx+1,nl)
-template <class T>
-__global__ void k_eta_z(Dims D, Grid<T> G, State S, T* ez) {
+template <class T, class V = double>
+__global__ void k_eta_z(Dims D, Grid<T> G, StateT<V> S, T* ez) {
   LG_IDX3;
   if (ji > D.ny + 1 || jk > D.nx + 1) return;
   ez[IX(D, ji, jk, jl)] = eta_z_at<T>(D, G, S, ji, jk, jl);
 }
 
 // mass flux densities, mo_vector_tend_expl.F90:64-66 (scalar_times_vector_h/_v)
-template <class T>
-__global__ void k_mass_flux(Dims D, Grid<T> G, State S, T* uph, T* vph, T* wph) {
+template <class T, class V = double>
+__global__ void k_mass_flux(Dims D, Grid<T> G, StateT<V> S, T* uph, T* vph, T* wph) {
   LG_IDX3;
-  const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+  const V* rg = S.rho + (long long)(D.g - 1) * D.fstride;
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     T f;
     if (stv_h_x<T>(D, rg, S.u, ji, jk, jl, &f)) uph[IX(D, ji, jk, jl)] = f;
@@ -516,15 +516,15 @@ __global__ void k_mass_flux(Dims D, Grid<T> G, State S, T* uph, T* vph, T* wph) 
 }
 
 // calc_vorticity_flux_term, mo_vorticity_flux.F90:16-171
-template <class T>
-__global__ void k_vort_flux(Dims D, Grid<T> G, State S, const T* ex, const T* ey, const T* ez, const T* uph,
+template <class T, class V = double>
+__global__ void k_vort_flux(Dims D, Grid<T> G, StateT<V> S, const T* ex, const T* ey, const T* ez, const T* uph,
                             const T* vph, const T* wph, T* px, T* py, T* pz) {
   LG_IDX3;
   // vertical mass flux with the free-slip surface value, mo_vector_tend_expl.F90:68-80
   auto wp = [&](int i, int j, int k) -> T {
     if (k == D.NL) {
       if (!D.freeslip) return T(0);
-      const double* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+      const V* rg = S.rho + (long long)(D.g - 1) * D.fstride;
       const T dv = T(rg[IX(D, i, j, D.nl)]) + (T(rg[IX(D, i, j, D.nl - 1)]) - T(rg[IX(D, i, j, D.nl)]))
                    / (G.z_scalar[IX(D, i, j, D.nl - 1)] - G.z_scalar[IX(D, i, j, D.nl)])
                    * (G.z_w[IX(D, i, j, D.NL)] - G.z_scalar[IX(D, i, j, D.nl)]);
@@ -570,8 +570,8 @@ __global__ void k_vort_flux(Dims D, Grid<T> G, State S, const T* ex, const T* ey
 }
 
 // inner_product of the wind with itself, mo_inner_product.F90:16-50
-template <class T>
-__global__ void k_ke(Dims D, Grid<T> G, State S, T* out) {
+template <class T, class V = double>
+__global__ void k_ke(Dims D, Grid<T> G, StateT<V> S, T* out) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   out[IX(D, ji, jk, jl)] = inner_product_at<T>(D, G, S.u, S.v, S.w, ji, jk, jl);
@@ -580,40 +580,45 @@ __global__ void k_ke(Dims D, Grid<T> G, State S, T* out) {
 // combination of the explicit wind tendencies, mo_vector_tend_expl.F90:258-310, and the
 // forward step of the horizontal wind, mo_manage_pchevi.F90:86-89 (in FP64)
 template <class T>
-__global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C, int rk_step) {
+// mu, mv (may be null): FP32 mirrors of the new u, v, written beside the FP64 values
+__global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C, int rk_step, float* mu, float* mv) {
   LG_IDX3;
   const T new_weight = (rk_step == 2) ? T(0.5) : T(1);
   const T old_weight = T(1) - new_weight;
-  const T chw = T(0.5 + kIMPL_THERMO_WEIGHT);
-  const T ohw = T(1.0 - (0.5 + kIMPL_THERMO_WEIGHT));
-  const T cvw = T(1.0 - kIMPL_THERMO_WEIGHT);
-  const T no_bg_switch = D.luse_bg ? T(0) : T(1);
+  // the pressure-gradient combinations are formed in FP64 (the products are FP64; without a
+  // background state they are O(g) and cancel gravity), in the reference's operation order
+  const double chw_d = 0.5 + kIMPL_THERMO_WEIGHT, ohw_d = 1.0 - (0.5 + kIMPL_THERMO_WEIGHT);
+  const double cvw_d = 1.0 - kIMPL_THERMO_WEIGHT, no_bg_d = D.luse_bg ? 0.0 : 1.0;
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
-    const T t = old_weight * Tn.u[q] + new_weight * (ohw * T(C.old_u[q]) - chw * (T(C.nl_u[q]) + T(C.l_u[q]))
-                - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
+    const double pg = ohw_d * C.old_u[q] - chw_d * (C.nl_u[q] + C.l_u[q]);
+    const T t = old_weight * Tn.u[q] + new_weight * (T(pg) - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
     Tn.u[q] = t;
-    Sn.u[q] = So.u[q] + D.dtime * double(t);
+    const double un = So.u[q] + D.dtime * double(t);
+    Sn.u[q] = un;
+    if (mu) mu[q] = float(un);
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    const T t = old_weight * Tn.v[q] + new_weight * (ohw * T(C.old_v[q]) - chw * (T(C.nl_v[q]) + T(C.l_v[q]))
-                - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
+    const double pg = ohw_d * C.old_v[q] - chw_d * (C.nl_v[q] + C.l_v[q]);
+    const T t = old_weight * Tn.v[q] + new_weight * (T(pg) - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
     Tn.v[q] = t;
-    Sn.v[q] = So.v[q] + D.dtime * double(t);
+    const double vn = So.v[q] + D.dtime * double(t);
+    Sn.v[q] = vn;
+    if (mv) mv[q] = float(vn);
   }
   if (jl <= D.NL && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (-(cvw * (T(C.nl_w[q]) + T(C.l_w[q])))
-              - no_bg_switch * (T(1) - cvw) * T(C.l_w[q]) - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+    const double pg = -(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q];
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (T(pg) - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
   }
 }
 
 // scalar_tend_expl for every constituent other than the gas, mo_scalar_tend_expl.F90:102-128
 // with scalar_times_vector_h_upstream (mo_multiplications.F90:206-287) and div_h_tracers
 // (mo_divergence_operators.F90:70-147) evaluated inline.
-template <class T>
-__global__ void k_tracers(Dims D, Grid<T> G, State Ss, const double* u_new, const double* v_new, T* t_rho,
+template <class T, class V = double>
+__global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, T* t_rho,
                           int rk_step) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
@@ -629,7 +634,7 @@ __global__ void k_tracers(Dims D, Grid<T> G, State Ss, const double* u_new, cons
   const T old_weight = T(1) - new_weight;
   for (int jc = 1; jc <= D.ncons; ++jc) {
     if (jc == D.g) continue;
-    const double* r = Ss.rho + (long long)(jc - 1) * D.fstride;
+    const V* r = Ss.rho + (long long)(jc - 1) * D.fstride;
     auto fx = [&](int i, int j, int k) { T f; return upstream_x<T>(D, r, u_new, i, j, k, &f) ? f : T(0); };
     auto fy = [&](int i, int j, int k) { T f; return upstream_y<T>(D, r, v_new, i, j, k, &f) ? f : T(0); };
     const T comp_h = fx(ji, jk + 1, jl) * G.area_x[IX(D, ji, jk + 1, jl)]
@@ -655,13 +660,13 @@ __global__ void k_tracers(Dims D, Grid<T> G, State Ss, const double* u_new, cons
 }
 
 // scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177
-template <class T>
-__global__ void k_gas_theta(Dims D, Grid<T> G, State Ss, const double* u_new, const double* v_new, const T* tvu,
+template <class T, class V = double>
+__global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, const T* tvu,
                             const T* tvv, const T* Tm, const T* rad, const T* csh, T* t_rho, T* t_rt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
-  const double* rg = Ss.rho + (long long)(D.g - 1) * D.fstride;
+  const V* rg = Ss.rho + (long long)(D.g - 1) * D.fstride;
   auto fx = [&](int i, int j, int k) { T f; return stv_h_x<T>(D, rg, u_new, i, j, k, &f) ? f : T(0); };
   auto fy = [&](int i, int j, int k) { T f; return stv_h_y<T>(D, rg, v_new, i, j, k, &f) ? f : T(0); };
   const T div_m = div_h_at<T>(D, G, fx, fy, ji, jk, jl);

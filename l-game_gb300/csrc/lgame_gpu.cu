@@ -59,6 +59,7 @@ struct lgame_gpu {
   int* flag = nullptr;
   Grid<double> G{};
   SplitCtx* split = nullptr;
+  bool mirror_valid[2] = {false, false};  // split mode: FP32 mirror of the slot matches its FP64 state
   // per-kernel tracing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -317,7 +318,7 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       if (rc != LGAME_OK) return rc;
     }
     Tend<double> T = c->tend;
-    LAUNCH(kd::k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk);
+    LAUNCH(kd::k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk, (float*)nullptr, (float*)nullptr);
     // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
     const State& Ss = (rk == 1) ? So : Sn;
     if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
@@ -564,6 +565,7 @@ extern "C" int lgame_gpu_set_state(lgame_gpu* c, int slot, const double* const* 
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_state: bad arguments");
   int rc = state_copy(c, slot, nullptr, f, true);
   if (rc != LGAME_OK) return rc;
+  c->mirror_valid[slot] = false;
   CK(cudaStreamSynchronize(c->stream));
   return LGAME_OK;
 }
@@ -658,8 +660,15 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
   if (c->split) {
     PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v,
                     c->pgcw};
-    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], P, total_step_counter, c->stream,
-                    &c->kernels_last_step, c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
+    for (int slot : {old_slot, new_slot}) {
+      if (c->mirror_valid[slot]) continue;
+      if ((rc = split_refresh_mirror(c->split, c->D, slot, c->st[slot], c->stream)) != LGAME_OK)
+        return set_err(rc, "lgame_gpu_pchevi: refresh of the FP32 state mirror failed");
+      c->mirror_valid[slot] = true;
+    }
+    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
+                    total_step_counter, c->stream, &c->kernels_last_step,
+                    c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
   } else {
     rc = step_fp64(c, old_slot, new_slot, total_step_counter);
   }
@@ -683,6 +692,7 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: bad arguments");
   int rc = state_copy(c, 0, nullptr, state_old, true);
   if (rc != LGAME_OK) return rc;
+  c->mirror_valid[0] = c->mirror_valid[1] = false;
   // state_new starts as a copy of state_old, as in the reference's time loop
   for (int s = 0; s < 1; ++s) {
     const Dims& D = c->D;

@@ -1,11 +1,18 @@
 // split.cu -- FP32/FP64 split-precision HEVI step (compiled with -fmad=true, -prec-div=false).
 //
-// The explicit stencils are the templates of kernels.cuh instantiated for float, reading
-// the FP64 state and FP32 copies of the metrics.  This file adds the parts that stay in
-// FP64 in this mode -- the pressure gradient and both column solvers -- written for the
-// FP64 pipe of this GPU: multiply-adds and reciprocals seeded in FP32 and refined by two
-// Newton steps in FP64 instead of FP64 divisions (one division costs ~10 FMA slots), and
-// metric reciprocals computed once at set-up.
+// The explicit stencils are the templates of kernels.cuh instantiated for float.  They read
+// an FP32 mirror of the state: a rounded copy of every prognostic field, written by the
+// kernels that update the FP64 state (k_tend_wind for u and v, the two column solvers for
+// the rest) and refreshed from the FP64 state whenever the host replaces it.  On this GPU a
+// conversion between FP64 and FP32 costs as much as an FP64 operation (both ~2 per clock
+// per SM, against 128 FP32 operations), so converting each state value once when it is
+// written, instead of at every stencil use, takes the FP32 stencils off the FP64 pipe.
+//
+// This file adds the parts that stay in FP64 in this mode -- the pressure gradient and the
+// two column solvers -- written to spend as few FP64 operations per cell as the precision
+// split allows: coefficients that only scale an increment (the partial derivatives of the
+// implicit system, fall speeds, fluxes) come from the FP32 mirror; the right-hand sides,
+// the substitution sweeps of the tridiagonal solves and the state updates are FP64.
 #include "split.cuh"
 #include "common.h"
 #include "lgame_gpu.h"
@@ -17,21 +24,24 @@ namespace lg {
 
 namespace {
 
-// 1/x to full FP64 precision: FP32 reciprocal, then two Newton-Raphson steps in FP64
-// (relative error 2^-23 -> 2^-46 -> below 2^-52).  |x| must lie in the FP32 normal range.
-__device__ __forceinline__ double drcp(double x) {
-  double r = (double)__frcp_rn((float)x);
-  double e = fma(-x, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-x, r, 1.0);
-  return fma(r, e, r);
-}
-
 constexpr int kMaxL = 128;
 
-struct GridX {  // FP64 reciprocal metrics of the FP64 parts
+struct GridX {  // FP64 reciprocal metrics and FP32 metric differences of the FP64 parts
   const double *inv_dx, *inv_dy, *inv_dz, *inv_volume, *inv_area_z;
+  // FP32: 1/volume, 1/area_z, and at w level jl (2..nl) z_scalar(jl-1)-z_scalar(jl) and
+  // exner_bg(jl-1)-exner_bg(jl), differenced in FP64 before rounding (no cancellation)
+  const float *inv_volume_f, *inv_area_z_f, *dzs_f, *deb_f;
 };
+
+// x / d to FP64 accuracy for an FP32 divisor d in the normal range: the correctly rounded
+// FP32 reciprocal (relative error <= 2^-24) and one correction of the quotient in FP64,
+// which leaves a relative error of ~2^-48.  Five FP64-pipe operations instead of a
+// conversion and an FP64 division (about eight).
+__device__ __forceinline__ double div_f(double x, float d) {
+  const double r = (double)__frcp_rn(d);
+  const double q0 = x * r;
+  return fma(fma(-q0, (double)d, x), r, q0);
+}
 
 }  // namespace
 
@@ -46,6 +56,12 @@ struct SplitCtx {
   float *th, *gx, *gy, *gz, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph;
   // kinetic energy in FP64: its vertical differences over thin layers cancel most digits
   double* vsq = nullptr;
+  // FP64 vertical gradient of exner' at w points (0 at the top and surface levels)
+  double* gzd = nullptr;
+  // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
+  float *fu = nullptr, *fv = nullptr, *gu = nullptr, *gv = nullptr;
+  // FP32 mirrors of the two state slots
+  StateF mir[2]{};
   SplitCarriedF C{};
 };
 
@@ -78,13 +94,28 @@ __global__ void k_recip(const double* a, double* b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = (a[i] != 0.0) ? 1.0 / a[i] : 0.0;
 }
+// FP32 metric reciprocals and vertical differences of the column solver (set-up only)
+__global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, float* dzs, float* deb) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx || jl > D.NL) return;
+  const long long q = IX(D, ji, jk, jl);
+  iaz[q] = (G.area_z[q] != 0.0) ? float(1.0 / G.area_z[q]) : 0.f;
+  if (jl <= D.nl) ivol[q] = float(1.0 / G.volume[q]);
+  if (jl >= 2 && jl <= D.nl) {
+    const long long a = IX(D, ji, jk, jl - 1);
+    dzs[q] = float(G.z_scalar[a] - G.z_scalar[q]);
+    deb[q] = float(G.exner_bg[a] - G.exner_bg[q]);
+  }
+}
 
 // ---- pressure gradient, mo_p_grad.F90:20-120, FP64 products ---------------------------
 // gradient of the Exner pressure perturbation in FP64 (the small differences of a small
 // field), theta edge values in FP32 (third order) or FP64 (second order), the background
-// term theta'*grad(Pi_bg) in FP64, the condensate deceleration factor in FP32.
-__global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const float* tvu, const float* tvv,
-                         const float* tpu, const float* tpv, PGrad<double> P, float* pgcw, int lfirst) {
+// term theta'*grad(Pi_bg) in FP64, the condensate deceleration factor in FP32 from the
+// mirror densities.
+__global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd, const float* mrho,
+                         const float* tvu, const float* tvv, const float* tpu, const float* tpv, PGrad<double> P,
+                         float* pgcw, int lfirst) {
   LG_IDX3;
   const double ubs = D.luse_bg ? 1.0 : 0.0;
   const double* ep = S.ep;
@@ -95,17 +126,14 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const float* 
   auto cond_frac = [&](long long q) -> float {
     if (D.nc == 0) return 0.f;
     float c = 0.f;
-    for (int jc = 0; jc < D.nc; ++jc) c += float(S.rho[q + (long long)jc * D.fstride]);
-    return c / (c + float(S.rho[q + (long long)(D.g - 1) * D.fstride]));
+    for (int jc = 0; jc < D.nc; ++jc) c += mrho[q + (long long)jc * D.fstride];
+    return c / (c + mrho[q + (long long)(D.g - 1) * D.fstride]);
   };
   auto decel = [&](int i, int j, int k) {
     return float(kC_D_P) - float(kC_D_P) * cond_frac(IX(D, i, j, k));
   };
-  // vertical gradient of exner_pert at a w point of column (i,j), 0 at the boundary levels
-  auto gzp = [&](int i, int j, int k) -> double {
-    if (k < 2 || k > D.nl) return 0.0;
-    return (ep[IX(D, i, j, k - 1)] - ep[IX(D, i, j, k)]) * X.inv_dz[IX(D, i, j, k)];
-  };
+  // vertical gradient of exner_pert at a w point of column (i,j) (ks_gzp), 0 at the boundary levels
+  auto gzp = [&](int i, int j, int k) -> double { return gzd[IX(D, i, j, k)]; };
   auto remapx = [&](int ji_, int jk_, int jl_) -> double {  // mo_averaging.F90:56-95 on gzp
     const int a = (jk_ == 1 || jk_ == D.nx + 1) ? D.nx : jk_ - 1, b = (jk_ == 1 || jk_ == D.nx + 1) ? 1 : jk_;
     double r = G.ipw[4][IX(D, ji_, a, jl_)] * gzp(ji_, a, jl_) + G.ipw[4][IX(D, ji_, b, jl_)] * gzp(ji_, b, jl_);
@@ -131,7 +159,7 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const float* 
       double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
       if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
       const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : (double)tvu[qr];
-      const double de = 0.5 * ((double)decel(ji, ka, jl) + (double)decel(ji, kk, jl));
+      const double de = (double)(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
       const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
@@ -156,7 +184,7 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const float* 
       double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
       if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
       const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : (double)tvv[qr];
-      const double de = 0.5 * ((double)decel(ia, jk, jl) + (double)decel(ii, jk, jl));
+      const double de = (double)(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
       const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
@@ -172,149 +200,260 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const float* 
   }
   if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl), qa = IX(D, ji, jk, jl - 1);
-    const double de = 0.5 * ((double)decel(ji, jk, jl - 1) + (double)decel(ji, jk, jl));
+    const float fa = cond_frac(qa), fb = cond_frac(q);
+    const double de = (double)(0.5f * ((float(kC_D_P) - float(kC_D_P) * fa) + (float(kC_D_P) - float(kC_D_P) * fb)));
     P.nl_w[q] = de * (0.5 * (theta(ji, jk, jl - 1) + theta(ji, jk, jl)) * gzp(ji, jk, jl));
     if (D.luse_bg) P.l_w[q] = de * (0.5 * (S.tp[qa] + S.tp[q]) * G.egw[q]);
-    const float da = -cond_frac(qa), db = -cond_frac(q);
-    pgcw[q] = 0.5f * (da + db) * float(G.gm[q]);
+    pgcw[q] = 0.5f * (-fa - fb) * float(G.gm[q]);
   }
 }
 
-// ---- three_band_solver_ver, mo_column_solvers.F90:21-351, FP64 --------------------------
-// Same system as the reference; the explicit predictions take the FP32 tendencies, the
-// partial derivatives alpha, beta, gamma are formed unscaled and multiplied by the
-// reciprocal volume, divisions are drcp() multiplications.
-__global__ void ks_column_ver(Dims D, Grid<double> G, GridX X, State So, State Sn, Tend<float> Tn, int rk_step) {
+// vertical gradient of exner_pert at the w levels 2..nl (grad_vert, mo_gradient_operators.F90:65-83)
+__global__ void ks_gzp(Dims D, GridX X, const double* ep, double* gzd) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.z + 2;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  const long long q = IX(D, ji, jk, jl);
+  gzd[q] = (ep[IX(D, ji, jk, jl - 1)] - ep[q]) * X.inv_dz[q];
+}
+
+// horizontal gas mass fluxes and theta_v fluxes of scalar_tend_expl, mo_scalar_tend_expl.F90:106-138:
+// rho_g*u at u points, rho_g*v at v points (scalar_times_vector_h), times the theta_v edge
+// values (third order: tvu, tvv; second order: the mean of the two cells).  Each face is
+// computed once here and read by ks_gas_div; the reference's untouched boundary faces are 0.
+__global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_new, const float* v_new,
+                            const float* tvu, const float* tvv, float* fu, float* fv, float* gu, float* gv) {
+  LG_IDX3;
+  if (jl > D.nl) return;
+  const float* rg = Ss.rho + (long long)(D.g - 1) * D.fstride;
+  auto th = [&](int i, int j, int k) { const long long p = IX(D, i, j, k); return GF.theta_v_bg[p] + Ss.tp[p]; };
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    const long long q = IX(D, ji, jk, jl);
+    float f = 0.f, g = 0.f;
+    if (stv_h_x<float>(D, rg, u_new, ji, jk, jl, &f)) {
+      if (D.theta_order == 2) {
+        const int ka = (jk >= 2 && jk <= D.nx) ? jk - 1 : D.nx, kb = (jk >= 2 && jk <= D.nx) ? jk : 1;
+        g = 0.5f * (th(ji, ka, jl) + th(ji, kb, jl)) * f;
+      } else {
+        g = tvu[q] * f;
+      }
+    }
+    fu[q] = f;
+    gu[q] = g;
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    float f = 0.f, g = 0.f;
+    if (stv_h_y<float>(D, rg, v_new, ji, jk, jl, &f)) {
+      if (D.theta_order == 2) {
+        const int ia = (ji >= 2 && ji <= D.ny) ? ji - 1 : D.ny, ib = (ji >= 2 && ji <= D.ny) ? ji : 1;
+        g = 0.5f * (th(ia, jk, jl) + th(ib, jk, jl)) * f;
+      } else {
+        g = tvv[q] * f;
+      }
+    }
+    fv[q] = f;
+    gv[q] = g;
+  }
+}
+
+// divergences of the gas and theta_v fluxes and the diabatic rho*theta_v term,
+// mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1)
+__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* fu, const float* fv, const float* gu,
+                           const float* gv, const float* Tm, const float* rad, const float* csh, float* t_rho,
+                           float* t_rt) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  auto fx = [&](int i, int j, int k) { return fu[IX(D, i, j, k)]; };
+  auto fy = [&](int i, int j, int k) { return fv[IX(D, i, j, k)]; };
+  auto gx = [&](int i, int j, int k) { return gu[IX(D, i, j, k)]; };
+  auto gy = [&](int i, int j, int k) { return gv[IX(D, i, j, k)]; };
+  t_rho[q + (long long)(D.g - 1) * D.fstride] = -div_h_at<float>(D, GF, fx, fy, ji, jk, jl);
+  const float div_t = div_h_at<float>(D, GF, gx, gy, ji, jk, jl);
+  const float heat = rad[q] + csh[q];
+  float x = 0.f;
+  if (heat != 0.f) {
+    const float cv = c_v_mass_weighted_air<float>(D, Ss.rho, Tm, q);
+    x = float(kC_D_V) * Ss.rho[q + (long long)(D.g - 1) * D.fstride] / cv * heat /
+        (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
+  }
+  t_rt[q] = -div_t + x;
+}
+
+// ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
+// The reference's implicit system for the vertical mass-flux increments at levels 2..nl,
+// one thread per column, streamed top to bottom.  FP32 (from the mirror): the partial
+// derivatives alpha, beta, gamma, the interface theta and density weights, the matrix and
+// its elimination multipliers.  FP64: the explicit predictions of theta' and exner', the
+// right-hand side (where the pressure-gradient and buoyancy terms balance), the forward
+// and back substitution, and the new rho_g, rho*theta_v, exner', w.  theta' is formed as
+// (rho*theta_v - theta_bg*rho)/rho with the small numerator in FP64.
+__global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Grid<float> GF, GridX X, State So,
+                                                     State Sn, StateF Mo, StateF Mn, Tend<float> Tn, int rk_step) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
-  const int nl = D.nl;
-  const double dt = D.dtime, idt = 1.0 / D.dtime;
+  const int nl = D.nl, n = nl - 1;
+  const float dtf = float(D.dtime), idtf = float(1.0 / D.dtime);
+  const double idtd = 1.0 / D.dtime;
   const long long goff = (long long)(D.g - 1) * D.fstride;
+  const float rdcv = float(kR_D / kC_D_V);
+  const float ic2 = float(1.0 / (kIMPL_THERMO_WEIGHT * (D.dtime * D.dtime) * kC_D_P));
+  const float ic1 = float(1.0 / (kIMPL_THERMO_WEIGHT * D.dtime * kC_D_P));
+  const StateF& Mu = (rk_step == 1) ? Mo : Mn;  // state_new_used, mo_column_solvers.F90:69-73
+
+  // unscaled alpha, beta, gamma; theta of state_new_used (FP32, and FP64 without a background
+  // state, where theta * d(exner')/dz carries the whole hydrostatic balance)
+  struct Lay { float a, b, g, th, ro, iv; double thd; };
   const State& Su = (rk_step == 1) ? So : Sn;
-  const double* rho_o = So.rho + goff;
-  const double* rho_u = Su.rho + goff;
-  double* rho_n = Sn.rho + goff;
-  const float* t_rho = Tn.rho + goff;
-  const double rdcv = kR_D / kC_D_V;
-  const double ic2 = 1.0 / (kIMPL_THERMO_WEIGHT * (dt * dt) * kC_D_P);
-  const double ic1 = 1.0 / (kIMPL_THERMO_WEIGHT * dt * kC_D_P);
-
-  double au[kMaxL + 1], bu[kMaxL + 1], gu[kMaxL + 1];     // unscaled partial derivatives
-  double rho_e[kMaxL + 1], rt_e[kMaxL + 1], ep_e[kMaxL + 1], tp_e[kMaxL + 1], thu[kMaxL + 1];
-  double irio[kMaxL + 1], rie[kMaxL + 1], ti[kMaxL + 1];
-  double cv[kMaxL + 1], dv[kMaxL + 1], ev[kMaxL + 1], rv[kMaxL + 1], epr[kMaxL + 1], rpr[kMaxL + 1];
-
-  for (int jl = 1; jl <= nl; ++jl) {
+  auto layer = [&](int jl) -> Lay {
     const long long i = IX(D, ji, jk, jl);
-    const double tr = (double)t_rho[i], trt = (double)Tn.rt[i];
-    const double ro = rho_o[i], rto = So.rt[i];
-    rho_e[jl] = fma(dt, tr, ro);
-    rt_e[jl] = fma(dt, trt, rto);
-    const double iro = drcp(ro), irto = drcp(rto);
-    double a = -rto * iro * iro, b = iro, g = rdcv * irto * (G.exner_bg[i] + So.ep[i]);
+    Lay L;
+    L.thd = D.luse_bg ? 0.0 : Su.rt[i] / Su.rho[goff + i];
+    const float ro = Mo.rho[goff + i], rto = Mo.rt[i];
+    const float iro = 1.f / ro, irto = 1.f / rto;
+    L.a = -rto * iro * iro;
+    L.b = iro;
+    L.g = rdcv * irto * (GF.exner_bg[i] + Mo.ep[i]);
     if (rk_step == 2) {
-      const double ru = rho_u[i], rtu = Su.rt[i];
-      const double iru = drcp(ru), irtu = drcp(rtu);
-      a = 0.5 * (a - rtu * iru * iru);
-      b = 0.5 * (b + iru);
-      g = 0.5 * (g + rdcv * irtu * (G.exner_bg[i] + Su.ep[i]));
-      thu[jl] = rtu * iru;
+      const float ru = Mu.rho[goff + i], rtu = Mu.rt[i];
+      const float iru = 1.f / ru, irtu = 1.f / rtu;
+      L.a = 0.5f * (L.a - rtu * iru * iru);
+      L.b = 0.5f * (L.b + iru);
+      L.g = 0.5f * (L.g + rdcv * irtu * (GF.exner_bg[i] + Mu.ep[i]));
+      L.th = rtu * iru;
     } else {
-      thu[jl] = rto * iro;
+      L.th = rto * iro;
     }
-    au[jl] = a; bu[jl] = b; gu[jl] = g;
-    tp_e[jl] = So.tp[i] + dt * (a * tr + b * trt);
-    ep_e[jl] = So.ep[i] + dt * g * trt;
-  }
-  for (int jl = 1; jl <= nl - 1; ++jl) {
-    const long long a = IX(D, ji, jk, jl), b = IX(D, ji, jk, jl + 1);
-    irio[jl] = drcp(0.5 * (rho_o[a] + rho_o[b]));
-    rie[jl] = 0.5 * (rho_e[jl] + rho_e[jl + 1]);
-    ti[jl] = 0.5 * (thu[jl] + thu[jl + 1]);
-  }
-  for (int jl = 1; jl <= nl - 1; ++jl) {
-    const long long a = IX(D, ji, jk, jl), b = IX(D, ji, jk, jl + 1);
-    const double iva = X.inv_volume[a], ivb = X.inv_volume[b];
-    const double dz = G.z_scalar[a] - G.z_scalar[b];
-    const double deb = G.exner_bg[a] - G.exner_bg[b];
-    const double dp = G.damp[b];
-    const double wo = So.w[b];
-    const double t = ti[jl];
-    // scaled derivatives (divided by the volume) as in the reference
-    const double al0 = au[jl] * iva, al1 = au[jl + 1] * ivb, be0 = bu[jl] * iva, be1 = bu[jl + 1] * ivb;
-    const double ga0 = gu[jl] * iva, ga1 = gu[jl + 1] * ivb;
-    dv[jl] = -(t * t) * (ga0 + ga1) + 0.5 * deb * (al1 - al0 + t * (be1 - be0))
-             - dz * ic2 * irio[jl] * (2.0 * X.inv_area_z[b] + dt * wo * 0.5 * (ivb - iva)) * dp;
-    rv[jl] = -(wo + dt * (double)Tn.w[b]) * dz * ic2 + t * (ep_e[jl] - ep_e[jl + 1]) * idt
-             + 0.5 * idt * (tp_e[jl] + tp_e[jl + 1]) * deb - dz * ic2 * wo * rie[jl] * irio[jl];
-  }
-  for (int jl = 1; jl <= nl - 2; ++jl) {
-    const long long a = IX(D, ji, jk, jl), b = IX(D, ji, jk, jl + 1), c = IX(D, ji, jk, jl + 2);
-    const double ivb = X.inv_volume[b];
-    const double al1 = au[jl + 1] * ivb, be1 = bu[jl + 1] * ivb, ga1 = gu[jl + 1] * ivb;
-    cv[jl] = ti[jl + 1] * ga1 * ti[jl] + 0.5 * (G.exner_bg[b] - G.exner_bg[c]) * (al1 + be1 * ti[jl])
-             - (G.z_scalar[b] - G.z_scalar[c]) * ic1 * 0.5 * So.w[c] * ivb * irio[jl + 1] * G.damp[c];
-    ev[jl] = ti[jl] * ga1 * ti[jl + 1] - 0.5 * (G.exner_bg[a] - G.exner_bg[b]) * (al1 + be1 * ti[jl + 1])
-             + (G.z_scalar[a] - G.z_scalar[b]) * ic1 * 0.5 * So.w[b] * ivb * irio[jl] * G.damp[b];
-  }
-  // Thomas, one reciprocal per row
-  const int n = nl - 1;
-  {
-    const double id = drcp(dv[1]);
-    epr[1] = ev[1] * id;
-    rpr[1] = rv[1] * id;
-    for (int jl = 2; jl <= n; ++jl) {
-      const double iden = drcp(dv[jl] - epr[jl - 1] * cv[jl - 1]);
-      if (jl <= n - 1) epr[jl] = ev[jl] * iden;
-      rpr[jl] = (rv[jl] - rpr[jl - 1] * cv[jl - 1]) * iden;
+    L.ro = ro;
+    L.iv = X.inv_volume_f[i];
+    return L;
+  };
+  // explicit predictions of theta_v' and exner' (FP64 state plus FP32 increments) and of rho_g (FP32)
+  auto predict = [&](int jl, const Lay& L, double* tpe, double* epe, float* rhe) {
+    const long long i = IX(D, ji, jk, jl);
+    const float tr = Tn.rho[goff + i], trt = Tn.rt[i];
+    *tpe = So.tp[i] + (double)(dtf * (L.a * tr + L.b * trt));
+    *epe = So.ep[i] + (double)(dtf * L.g * trt);
+    *rhe = L.ro + dtf * tr;
+  };
+
+  float epr[kMaxL + 1];   // elimination multipliers (FP32)
+  double rpr[kMaxL + 1];  // substituted right-hand side, then the solution (FP64)
+  float tis[kMaxL + 1];   // interface theta
+  float gs[kMaxL + 1];    // gamma of each layer
+  Lay L0 = layer(1), L1 = layer(2), L2{};
+  double tpe0, epe0, tpe1, epe1, tpe2 = 0.0, epe2 = 0.0;
+  float rhe0, rhe1, rhe2 = 0.f;
+  predict(1, L0, &tpe0, &epe0, &rhe0);
+  predict(2, L1, &tpe1, &epe1, &rhe1);
+  gs[1] = L0.g;
+  float cv_prev = 0.f, epr_prev = 0.f;
+  double rpr_prev = 0.0;
+  for (int jl = 1; jl <= n; ++jl) {  // row jl: level jl+1 between layers jl (a) and jl+1 (b)
+    const long long ib = IX(D, ji, jk, jl + 1);
+    gs[jl + 1] = L1.g;
+    const float ti = 0.5f * (L0.th + L1.th);
+    tis[jl] = ti;
+    const float irio = 2.f / (L0.ro + L1.ro);
+    const float dz = X.dzs_f[ib], deb = X.deb_f[ib], dp = GF.damp[ib];
+    const double wo = So.w[ib];
+    const float wof = Mo.w[ib];
+    const float al0 = L0.a * L0.iv, al1 = L1.a * L1.iv, be0 = L0.b * L0.iv, be1 = L1.b * L1.iv;
+    const float ga0 = L0.g * L0.iv, ga1 = L1.g * L1.iv;
+    const float dv = -(ti * ti) * (ga0 + ga1) + 0.5f * deb * (al1 - al0 + ti * (be1 - be0))
+                     - dz * ic2 * irio * (2.f * X.inv_area_z_f[ib] + dtf * wof * 0.5f * (L1.iv - L0.iv)) * dp;
+    const float rie = 0.5f * (rhe0 + rhe1);
+    double rv = (wo + (double)(dtf * Tn.w[ib])) * (double)(-dz * ic2);
+    rv = fma(D.luse_bg ? (double)(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
+    rv = fma((double)(0.5f * idtf * deb), tpe0 + tpe1, rv);
+    rv = fma((double)(-dz * ic2 * rie * irio), wo, rv);
+    // couplings with row jl+1 (layer b's derivatives), which need layer jl+2
+    float cv = 0.f, ev = 0.f;
+    if (jl < n) {
+      L2 = layer(jl + 2);
+      predict(jl + 2, L2, &tpe2, &epe2, &rhe2);
+      const long long ic = IX(D, ji, jk, jl + 2);
+      const float ti_n = 0.5f * (L1.th + L2.th);
+      const float irio_n = 2.f / (L1.ro + L2.ro);
+      cv = ti_n * ga1 * ti + 0.5f * X.deb_f[ic] * (al1 + be1 * ti)
+           - X.dzs_f[ic] * ic1 * 0.5f * Mo.w[ic] * L1.iv * irio_n * GF.damp[ic];
+      ev = ti * ga1 * ti_n - 0.5f * deb * (al1 + be1 * ti_n) + dz * ic1 * 0.5f * wof * L1.iv * irio * dp;
     }
-    double s = rpr[n];
-    rv[n] = s;
-    for (int jl = n - 1; jl >= 1; --jl) {
-      s = rpr[jl] - epr[jl] * s;
-      rv[jl] = s;  // solution
-    }
+    const float piv = dv - epr_prev * cv_prev;
+    const double x = (jl == 1) ? rv : fma(-(double)cv_prev, rpr_prev, rv);
+    rpr_prev = div_f(x, piv);
+    rpr[jl] = rpr_prev;
+    epr_prev = ev / piv;
+    epr[jl] = epr_prev;
+    cv_prev = cv;
+    L0 = L1; L1 = L2;
+    tpe0 = tpe1; epe0 = epe1; rhe0 = rhe1;
+    tpe1 = tpe2; epe1 = epe2; rhe1 = rhe2;
   }
-  const double* sol = rv;
+  double s = rpr[n];
+  for (int jl = n - 1; jl >= 1; --jl) {
+    s = fma(-(double)epr[jl], s, rpr[jl]);
+    rpr[jl] = s;
+  }
+  // new state, mo_column_solvers.F90:300-345
+  float rn_prev = 0.f;
   for (int jl = 1; jl <= nl; ++jl) {
     const long long i = IX(D, ji, jk, jl);
-    const double iv = X.inv_volume[i];
-    const double s0 = (jl >= 2) ? sol[jl - 1] : 0.0;
-    const double s1 = (jl <= nl - 1) ? sol[jl] : 0.0;
-    const double t0 = (jl >= 2) ? ti[jl - 1] : 0.0;
-    const double t1 = (jl <= nl - 1) ? ti[jl] : 0.0;
-    const double rn = rho_e[jl] + dt * (s1 - s0) * iv;
-    const double rtn = rt_e[jl] + dt * (t1 * s1 - t0 * s0) * iv;
-    rho_n[i] = rn;
+    const double s0 = (jl >= 2) ? rpr[jl - 1] : 0.0;
+    const double s1 = (jl <= n) ? rpr[jl] : 0.0;
+    const float t0 = (jl >= 2) ? tis[jl - 1] : 0.f;
+    const float t1 = (jl <= n) ? tis[jl] : 0.f;
+    const double dtv = (double)(dtf * X.inv_volume_f[i]);
+    const double rto = So.rt[i];
+    const double rho_e = So.rho[goff + i] + (double)(dtf * Tn.rho[goff + i]);
+    const double rt_e = rto + (double)(dtf * Tn.rt[i]);
+    const double rn = fma(dtv, s1 - s0, rho_e);
+    const double rtn = fma(dtv, fma(-(double)t0, s0, (double)t1 * s1), rt_e);
+    const double epn = fma((double)gs[jl], rtn - rto, So.ep[i]);
+    const float rnf = (float)rn;
+    const float tpf = (float)fma(-G.theta_v_bg[i], rn, rtn) / rnf;
+    Sn.rho[goff + i] = rn;
     Sn.rt[i] = rtn;
-    Sn.ep[i] = So.ep[i] + gu[jl] * (rtn - So.rt[i]);
-    Sn.tp[i] = rtn * drcp(rn) - G.theta_v_bg[i];
+    Sn.ep[i] = epn;
+    Sn.tp[i] = (double)tpf;
+    Mn.rho[goff + i] = rnf;
+    Mn.rt[i] = (float)rtn;
+    Mn.ep[i] = (float)epn;
+    Mn.tp[i] = tpf;
+    if (jl >= 2) {  // w at level jl from the increment at that level
+      const float rin = 0.5f * (rn_prev + rnf);
+      const float irio = 2.f / (Mo.rho[goff + IX(D, ji, jk, jl - 1)] + Mo.rho[goff + i]);
+      const double wo = So.w[i];
+      const double wn = fma(-(double)rin, wo, (double)(2.f * X.inv_area_z_f[i]) * s0) * (double)irio;
+      Sn.w[i] = wn;
+      Mn.w[i] = (float)wn;
+    }
+    rn_prev = rnf;
   }
-  for (int jl = 2; jl <= nl; ++jl) {
-    const long long i = IX(D, ji, jk, jl);
-    const double rin = 0.5 * (rho_n[IX(D, ji, jk, jl - 1)] + rho_n[i]);
-    Sn.w[i] = (2.0 * sol[jl - 1] * X.inv_area_z[i] - rin * So.w[i]) * irio[jl - 1];
-  }
-  if (D.freeslip) {
+  if (D.freeslip) {  // w_free_slip, mo_inner_product.F90:52-75, with the new u, v
     const int m = nl;
-    Sn.w[IX(D, ji, jk, m + 1)] =
+    const double wf =
         G.ipw[0][IX(D, ji, jk, m)] * Sn.u[IX(D, ji, jk + 1, m)] * G.slope_x[IX(D, ji, jk + 1, m)]
       + G.ipw[1][IX(D, ji, jk, m)] * Sn.v[IX(D, ji, jk, m)] * G.slope_y[IX(D, ji, jk, m)]
       + G.ipw[2][IX(D, ji, jk, m)] * Sn.u[IX(D, ji, jk, m)] * G.slope_x[IX(D, ji, jk, m)]
       + G.ipw[3][IX(D, ji, jk, m)] * Sn.v[IX(D, ji + 1, jk, m)] * G.slope_y[IX(D, ji + 1, jk, m)];
+    Sn.w[IX(D, ji, jk, m + 1)] = wf;
+    Mn.w[IX(D, ji, jk, m + 1)] = (float)wf;
   }
 }
 
 // v_fall_liquid, mo_derived.F90:218-263, in FP32
-__device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>& GF, const double* rho_g,
+__device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>& GF, const float* rho_g,
                                                 const float* Tm, float radius, int ji, int jk, int jl) {
   float g;
   if (jl == 1) g = GF.gm[IX(D, ji, jk, jl + 1)];
   else if (jl == D.nl) g = GF.gm[IX(D, ji, jk, jl)];
   else g = GF.ipw[4][IX(D, ji, jk, jl)] * GF.gm[IX(D, ji, jk, jl)] + GF.ipw[5][IX(D, ji, jk, jl)] * GF.gm[IX(D, ji, jk, jl + 1)];
   const long long i = IX(D, ji, jk, jl);
-  const float rg = float(rho_g[i]);
+  const float rg = rho_g[i];
   const float pm = float(kM_D / kN_A);
   const float tv = sqrtf(8.f * float(kK_B) / (float(kPI) * pm) * Tm[i]);
   const float mfp = 1.f / (1.41421356f * (rg / pm) * (4.f * float(kPI) * (130e-12f * 130e-12f)));
@@ -325,107 +464,116 @@ __device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>
 }
 
 // ---- three_band_solver_gen_densities, mo_column_solvers.F90:353-604 ----------------------
-// fall speeds, vertical fluxes and matrix coefficients in FP32; the explicit prediction
-// rho_old + dt*tendency and the Thomas solve in FP64.
-__global__ void ks_column_tracers(Dims D, Grid<double> G, Grid<float> GF, GridX X, State So, State Sn,
-                                  const float* t_rho_all, const float* Tm, float* csh, int rk_step) {
+// One thread per column, one top-to-bottom sweep per tracer.  Fall speeds, vertical fluxes,
+// the implicit-upwind matrix and its multipliers in FP32 from the mirror; the explicit
+// prediction rho_old + dt*tendency and both substitution sweeps in FP64.  Each interface
+// couples its two cells in one direction only (the upwind side), so the pivots are the
+// diagonal entries themselves.
+__global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
+                                                         StateF Mo, StateF Mn, const float* t_rho_all,
+                                                         const float* Tm, float* csh, int rk_step) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
   const int nl = D.nl, NL = D.NL, nc = D.nc;
   const float dt = float(D.dtime);
-  const double dtd = D.dtime;
   const float itw = 0.5f, ew = 0.5f;
-  const double* rho_g_o = So.rho + (long long)(D.g - 1) * D.fstride;
-  float vfi[kMaxL + 1], vfr[kMaxL + 1], vefv[kMaxL + 1], vcl[kMaxL + 1], itv[kMaxL + 1], cpi[kMaxL + 2], cpw[kMaxL + 2];
-  double cv[kMaxL + 1], dv[kMaxL + 1], ev[kMaxL + 1], rv[kMaxL + 1], epr[kMaxL + 1], rpr[kMaxL + 1];
-  for (int jl = 1; jl <= nl; ++jl) {
-    const long long i = IX(D, ji, jk, jl);
-    itv[jl] = itw * dt * float(X.inv_volume[i]);
-    vcl[jl] = vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, jl);
-    if (jl >= 2) { cpi[jl] = c_p_ice(Tm[i]); cpw[jl] = c_p_water(Tm[i]); }
-  }
+  const float* rho_g_o = Mo.rho + (long long)(D.g - 1) * D.fstride;
+  const float az_sfc = GF.area_z[IX(D, ji, jk, NL)];
+  float epr[kMaxL + 1];
+  double rpr[kMaxL + 1];
+  if (rk_step == 1)
+    for (int jl = 1; jl <= nl; ++jl) csh[IX(D, ji, jk, jl)] = 0.f;
   for (int jc = 1; jc <= D.ncons; ++jc) {
     if (jc == D.g) continue;
-    const double* rho_o = So.rho + (long long)(jc - 1) * D.fstride;
-    double* rho_n = Sn.rho + (long long)(jc - 1) * D.fstride;
-    const float* t_rho = t_rho_all + (long long)(jc - 1) * D.fstride;
+    const long long off = (long long)(jc - 1) * D.fstride;
+    const double* rho_o = So.rho + off;
+    const float* mro = Mo.rho + off;
+    double* rho_n = Sn.rho + off;
+    float* mrn = Mn.rho + off;
+    const float* t_rho = t_rho_all + off;
     const bool ice = (jc - 1) % 2 == 0;
-    float vsurf = 0.f;
-    for (int jl = 1; jl <= nl - 1; ++jl) {
-      const long long a = IX(D, ji, jk, jl), b = IX(D, ji, jk, jl + 1);
-      if (rk_step == 1 && jc == 1) csh[a] = 0.f;
-      float vf = 0.f;
-      if (jc == 1) vf = 1.f;               // snow radius 500 um > 250 um
-      else if (jc == 3) vf = 0.001f;       // cloud ice
-      else if (jc == 4) vf = 0.5f * (vcl[jl] + vcl[jl + 1]);
-      const float az = GF.area_z[b];
-      vfi[jl] = az * (float(So.w[b]) - vf);
-      float fr = az * (float(Sn.w[b]) - vf);
-      fr = ((fr >= 0.f) ? float(rho_o[b]) : float(rho_o[a])) * fr;
-      vfr[jl] = fr;
-      const float toi = Tm[b];
-      vefv[jl] = (jc <= nc) ? (ice ? cpi[jl + 1] : cpw[jl + 1]) * toi * fr : 0.f;
-    }
-    if (rk_step == 1 && jc == 1) csh[IX(D, ji, jk, nl)] = 0.f;
-    if (jc == 1) vsurf = 1.f;
-    else if (jc == 3) vsurf = 0.001f;
-    else if (jc == 4) vsurf = vcl[nl];
-    for (int jl = 1; jl <= nl - 1; ++jl) {
-      if (vfi[jl] >= 0.f) { cv[jl] = 0.0; ev[jl] = -(double)(itv[jl] * vfi[jl]); }
-      else { cv[jl] = (double)(itv[jl + 1] * vfi[jl]); ev[jl] = 0.0; }
-    }
+    const bool cond = jc <= nc;
+    const bool heat = rk_step == 1 && cond;
+    // fall speeds: snow (radius 500 um above 250 um) 1 m/s, cloud ice 0.001 m/s, cloud water
+    // v_fall_liquid at radius 12 um, rain and graupel 0 (their radius is never set)
+    float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
+    const float vsurf = (jc == 1) ? 1.f : (jc == 3) ? 0.001f
+                      : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
+    float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
+    float itv_a = itw * dt * X.inv_volume_f[IX(D, ji, jk, 1)];
+    float epr_prev = 0.f, cv_prev = 0.f;
+    double rpr_prev = 0.0;
     for (int jl = 1; jl <= nl; ++jl) {
       const long long i = IX(D, ji, jk, jl);
-      const float iv = float(X.inv_volume[i]);
-      float d;
-      if (jl == 1) {
-        d = (vfi[1] >= 0.f) ? 1.f : 1.f - itv[1] * vfi[1];
-      } else if (jl == nl) {
-        d = (vfi[jl - 1] >= 0.f) ? 1.f + itv[jl] * vfi[jl - 1] : 1.f;
-        if (jc <= nc) d += itw * vsurf * dt * GF.area_z[IX(D, ji, jk, jl + 1)] * iv;
-      } else {
-        d = 1.f;
-        if (vfi[jl - 1] >= 0.f) d += itv[jl] * vfi[jl - 1];
-        if (vfi[jl] < 0.f) d -= itv[jl] * vfi[jl];
+      const float iv = X.inv_volume_f[i];
+      // the interface below the cell (between jl and jl+1)
+      float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f;
+      if (jl <= nl - 1) {
+        const long long b = IX(D, ji, jk, jl + 1);
+        itv_b = itw * dt * X.inv_volume_f[b];
+        float vf = 0.f;
+        if (jc == 1) vf = 1.f;
+        else if (jc == 3) vf = 0.001f;
+        else if (jc == 4) {
+          const float vcl_b = vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, jl + 1);
+          vf = 0.5f * (vcl_a + vcl_b);
+          vcl_a = vcl_b;
+        }
+        const float az = GF.area_z[b];
+        vfi = az * (Mo.w[b] - vf);
+        float fr = az * (Mn.w[b] - vf);
+        fr = ((fr >= 0.f) ? mro[b] : mro[i]) * fr;
+        vfr = fr;
+        if (cond) vefv = (ice ? c_p_ice(Tm[b]) : c_p_water(Tm[b])) * Tm[b] * fr;
       }
-      dv[jl] = d;
-      double r = fma(dtd, (double)t_rho[i], rho_o[i]);
-      float fl;
+      // diagonal entry, explicit flux part and sediment heating of cell jl
+      float d, fl;
       if (jl == 1) {
-        fl = ew * dt * vfr[jl] * iv;
-        if (rk_step == 1 && jc <= nc) csh[i] += vefv[jl] * iv;
+        d = (vfi >= 0.f) ? 1.f : 1.f - itv_a * vfi;
+        fl = ew * dt * vfr * iv;
+        if (heat) csh[i] += vefv * iv;
       } else if (jl == nl) {
-        fl = -ew * dt * vfr[jl - 1] * iv;
-        if (rk_step == 1 && jc <= nc) csh[i] -= vefv[jl - 1] * iv;
-        if (jc <= nc) {
-          fl -= ew * vsurf * dt * float(rho_o[i]) * GF.area_z[IX(D, ji, jk, jl + 1)] * iv;
+        d = (vfi_up >= 0.f) ? 1.f + itv_a * vfi_up : 1.f;
+        fl = -ew * dt * vfr_up * iv;
+        if (heat) csh[i] -= vefv_up * iv;
+        if (cond) {
+          d += itw * vsurf * dt * az_sfc * iv;
+          fl -= ew * vsurf * dt * mro[i] * az_sfc * iv;
           if (jc > nc / 4 && rk_step == 1) {
-            const float Tn = Tm[IX(D, ji, jk, nl)];
-            csh[i] -= vsurf * Tn * (ice ? cpi[nl] : cpw[nl]) * float(rho_o[IX(D, ji, jk, nl)]) *
-                      GF.area_z[IX(D, ji, jk, NL)] * iv;
+            const float Tn = Tm[i];
+            csh[i] -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * mro[i] * az_sfc * iv;
           }
         }
       } else {
-        fl = ew * dt * (vfr[jl] - vfr[jl - 1]) * iv;
-        if (rk_step == 1 && jc <= nc) csh[i] += (vefv[jl] - vefv[jl - 1]) * iv;
+        d = 1.f;
+        if (vfi_up >= 0.f) d += itv_a * vfi_up;
+        if (vfi < 0.f) d -= itv_a * vfi;
+        fl = ew * dt * (vfr - vfr_up) * iv;
+        if (heat) csh[i] += (vefv - vefv_up) * iv;
       }
-      rv[jl] = r + (double)fl;
+      // couplings: row jl to jl+1 (upward flux below) and row jl+1 to jl (downward flux below)
+      const float ev = (jl <= nl - 1 && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
+      const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
+      // forward substitution in FP64 (the pivot equals d: one of e, c of an interface is 0)
+      const float piv = d - epr_prev * cv_prev;
+      double x = rho_o[i] + (double)(dt * t_rho[i] + fl);
+      if (cv_prev != 0.f) x = fma(-(double)cv_prev, rpr_prev, x);
+      rpr_prev = div_f(x, piv);
+      rpr[jl] = rpr_prev;
+      epr_prev = ev / piv;
+      epr[jl] = epr_prev;
+      cv_prev = cv;
+      vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
     }
-    // Thomas in FP64, one reciprocal per row
-    double id = drcp(dv[1]);
-    epr[1] = ev[1] * id;
-    rpr[1] = rv[1] * id;
-    for (int jl = 2; jl <= nl; ++jl) {
-      id = drcp(dv[jl] - epr[jl - 1] * cv[jl - 1]);
-      if (jl <= nl - 1) epr[jl] = ev[jl] * id;
-      rpr[jl] = (rv[jl] - rpr[jl - 1] * cv[jl - 1]) * id;
-    }
+    // back substitution; negative densities are clipped on output (mo_column_solvers.F90:587-591)
     double s = rpr[nl];
-    rho_n[IX(D, ji, jk, nl)] = s < 0.0 ? 0.0 : s;
-    for (int jl = nl - 1; jl >= 1; --jl) {
-      s = rpr[jl] - epr[jl] * s;
-      rho_n[IX(D, ji, jk, jl)] = s < 0.0 ? 0.0 : s;
+    for (int jl = nl; jl >= 1; --jl) {
+      if (jl < nl) s = (epr[jl] != 0.f) ? fma(-(double)epr[jl], s, rpr[jl]) : rpr[jl];
+      const double o = s < 0.0 ? 0.0 : s;
+      const long long i = IX(D, ji, jk, jl);
+      rho_n[i] = o;
+      mrn[i] = (float)o;
     }
   }
 }
@@ -434,6 +582,9 @@ dim3 sblk() { return dim3(32, 8, 1); }
 dim3 sgrd(int rows, int cols, int levs) {
   return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 7) / 8), (unsigned)levs);
 }
+// column kernels: 128 threads, 32 rows x 4 columns
+dim3 cblk() { return dim3(32, 4, 1); }
+dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 3) / 4), 1u); }
 
 }  // namespace
 
@@ -454,6 +605,15 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
                        &s->ex, &s->ey, &s->ez, &s->uph, &s->vph, &s->wph};
   for (float** p : scratch) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
+  if ((rc = salloc(s, &s->gzd, F, bytes))) return fail(rc);
+  float** fl[] = {&s->fu, &s->fv, &s->gu, &s->gv};
+  for (float** p : fl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
+  for (int k = 0; k < 2; ++k) {
+    StateF& M = s->mir[k];
+    if ((rc = salloc(s, &M.rho, F * D.ncons, bytes))) return fail(rc);
+    float** mf[] = {&M.rt, &M.tp, &M.ep, &M.u, &M.v, &M.w};
+    for (float** p : mf) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
+  }
   SplitCarriedF& C = s->C;
   float** car[] = {&C.pgcw, &C.vsg_x, &C.vsg_y, &C.vsg_z, &C.pvt_x, &C.pvt_y, &C.pvt_z, &C.csh, &C.rad, &C.temperature,
                    &C.tend.rt, &C.tend.u, &C.tend.v, &C.tend.w};
@@ -480,6 +640,17 @@ int split_convert_back(const float* src, double* dst, long long n, cudaStream_t 
   return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
 }
 
+int split_refresh_mirror(SplitCtx* s, const Dims& D, int slot, const State& S, cudaStream_t stream) {
+  const long long F = D.fstride;
+  const StateF& M = s->mir[slot];
+  if (split_convert(S.rho, M.rho, F * D.ncons, stream)) return LGAME_ERR_CUDA;
+  const double* src[] = {S.rt, S.tp, S.ep, S.u, S.v, S.w};
+  float* dst[] = {M.rt, M.tp, M.ep, M.u, M.v, M.w};
+  for (int k = 0; k < 6; ++k)
+    if (split_convert(src[k], dst[k], F, stream)) return LGAME_ERR_CUDA;
+  return LGAME_OK;
+}
+
 int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream) {
   const long long F = D.fstride;
   const double* src[] = {G.z_scalar, G.z_u, G.z_v, G.z_w, G.dx, G.dy, G.dz, G.volume, G.area_x, G.area_y, G.area_z,
@@ -499,6 +670,11 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   k_recip<<<1216, 256, 0, stream>>>(G.dz, s->inv_dz, F);
   k_recip<<<1216, 256, 0, stream>>>(G.volume, s->inv_volume, F);
   k_recip<<<1216, 256, 0, stream>>>(G.area_z, s->inv_area_z, F);
+  float* ivol = s->gf[28];
+  float* iaz = s->gf[29];
+  float* dzs = s->gf[30];
+  float* deb = s->gf[31];
+  k_grid_extra<<<sgrd(D.ny, D.nx, D.NL), sblk(), 0, stream>>>(D, G, ivol, iaz, dzs, deb);
   if (cudaGetLastError() != cudaSuccess) return LGAME_ERR_CUDA;
   Grid<float>& GF = s->GF;
   float** g = s->gf;
@@ -510,21 +686,23 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   for (int k = 0; k < 6; ++k) GF.ipw[k] = s->ipw[k];
   for (int k = 0; k < 3; ++k) GF.trsk_u[k] = s->trsk_u[k];
   for (int k = 0; k < 2; ++k) GF.trsk_v[k] = s->trsk_v[k];
-  s->GX = GridX{s->inv_dx, s->inv_dy, s->inv_dz, s->inv_volume, s->inv_area_z};
+  s->GX = GridX{s->inv_dx, s->inv_dy, s->inv_dz, s->inv_volume, s->inv_area_z, ivol, iaz, dzs, deb};
   return LGAME_OK;
 }
 
-int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn,
+int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn, int so, int sn,
                const PGrad<double>& pg, int step, cudaStream_t stream, int* nk,
                int (*tb)(void*, const char*), void (*te)(void*, int), void* tracer) {
   const Grid<float>& GF = s->GF;
   const SplitCarriedF& C = s->C;
   const Tend<float> T = C.tend;
+  const StateF& Mo = s->mir[so];
+  const StateF& Mn = s->mir[sn];
   int launches = 0;
-#define SL(name, kernel, grid_, ...)                                            \
+#define SL(name, kernel, grid_, block_, ...)                                    \
   do {                                                                          \
     const int tr_ = tb ? tb(tracer, name) : -1;                                 \
-    kernel<<<grid_, sblk(), 0, stream>>>(__VA_ARGS__);                          \
+    kernel<<<grid_, block_, 0, stream>>>(__VA_ARGS__);                          \
     if (tr_ >= 0) te(tracer, tr_);                                              \
     cudaError_t e_ = cudaGetLastError();                                        \
     if (e_ != cudaSuccess) {                                                    \
@@ -533,54 +711,64 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     }                                                                           \
     ++launches;                                                                 \
   } while (0)
-  auto theta3f = [&](const double* tp, int mode, const double* u, const double* v, float* ou, float* ov) -> int {
-    SL("ks_theta", k_theta<float>, sgrd(D.ny, D.nx, D.nl), D, GF, tp, s->th, mode);
-    SL("ks_grad_vert", (k_grad_vert<float, float>), sgrd(D.ny, D.nx, D.nl - 1), D, GF, s->th, s->gz);
-    SL("ks_grad_hor", (k_grad_hor<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, s->th, s->gz, s->gx, s->gy);
-    SL("ks_div_h", k_div_h<float>, sgrd(D.ny, D.nx, D.nl), D, GF, s->gx, s->gy, s->divf);
-    SL("ks_theta_edges", k_theta_edges<float>, sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, s->th, s->divf, u, v, ou, ov);
+  const dim3 B = sblk();
+  auto theta3f = [&](const float* tp, int mode, const float* u, const float* v, float* ou, float* ov) -> int {
+    SL("ks_theta", (k_theta<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, tp, s->th, mode);
+    SL("ks_grad_vert", (k_grad_vert<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->th, s->gz);
+    SL("ks_grad_hor", (k_grad_hor<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->gz, s->gx,
+       s->gy);
+    SL("ks_div_h", k_div_h<float>, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->gx, s->gy, s->divf);
+    SL("ks_theta_edges", (k_theta_edges<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->divf, u,
+       v, ou, ov);
     return LGAME_OK;
   };
-  SL("ks_temperature", k_temperature<float>, sgrd(D.ny, D.nx, D.nl), D, GF, So, C.temperature);
+  SL("ks_temperature", (k_temperature<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, Mo, C.temperature);
   Carried<float> CC{pg.nl_u, pg.nl_v, pg.nl_w, pg.l_u, pg.l_v, pg.l_w, pg.old_u, pg.old_v, C.pgcw,
                     C.vsg_x, C.vsg_y, C.vsg_z, C.pvt_x, C.pvt_y, C.pvt_z};
   for (int rk = 1; rk <= 2; ++rk) {
     const State& Sv = (rk == 1) ? So : Sn;
+    const StateF& Mv = (rk == 1) ? Mo : Mn;
     if (rk == 1) {
       if (D.theta_order == 3) {
-        int rc = theta3f(So.tp, 0, So.u, So.v, s->tvu, s->tvv);
+        int rc = theta3f(Mo.tp, 0, Mo.u, Mo.v, s->tvu, s->tvv);
         if (rc) return rc;
-        if (D.luse_bg) { rc = theta3f(So.tp, 1, So.u, So.v, s->tpu, s->tpv); if (rc) return rc; }
+        if (D.luse_bg) { rc = theta3f(Mo.tp, 1, Mo.u, Mo.v, s->tpu, s->tpv); if (rc) return rc; }
       }
-      SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), D, G, s->GX, So, s->tvu, s->tvv, s->tpu, s->tpv, pg,
-         C.pgcw, step == 0 ? 1 : 0);
+      SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl - 1), B, D, s->GX, So.ep, s->gzd);
+      SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, Mo.rho, s->tvu, s->tvv,
+         s->tpu, s->tpv, pg, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
-      SL("ks_eta_xy", k_eta_xy<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), D, GF, Sv, s->ex, s->ey);
-      SL("ks_eta_z", k_eta_z<float>, sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, Sv, s->ez);
-      SL("ks_mass_flux", k_mass_flux<float>, sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, Sv, s->uph, s->vph, s->wph);
-      SL("ks_vort_flux", k_vort_flux<float>, sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, Sv, s->ex, s->ey, s->ez, s->uph,
-         s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
+      SL("ks_eta_xy", (k_eta_xy<float, float>), sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
+      SL("ks_eta_z", (k_eta_z<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ez);
+      SL("ks_mass_flux", (k_mass_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->uph, s->vph,
+         s->wph);
+      SL("ks_vort_flux", (k_vort_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
+         s->ez, s->uph, s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
       if (!D.llinear) {
-        SL("ks_ke", k_ke<double>, sgrd(D.ny, D.nx, D.nl), D, G, Sv, s->vsq);
-        SL("ks_grad_vert", (k_grad_vert<float, double>), sgrd(D.ny, D.nx, D.nl - 1), D, GF, s->vsq, C.vsg_z);
-        SL("ks_grad_hor", (k_grad_hor<float, double>), sgrd(D.ny + 1, D.nx + 1, D.nl), D, GF, s->vsq, C.vsg_z,
+        SL("ks_ke", (k_ke<double, double>), sgrd(D.ny, D.nx, D.nl), B, D, G, Sv, s->vsq);
+        SL("ks_grad_vert", (k_grad_vert<float, double>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->vsq, C.vsg_z);
+        SL("ks_grad_hor", (k_grad_hor<float, double>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->vsq, C.vsg_z,
            C.vsg_x, C.vsg_y);
       }
     }
-    SL("ks_tend_wind", k_tend_wind<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, CC, rk);
-    const State& Ss = (rk == 1) ? So : Sn;
-    if (D.ncons > 1) SL("ks_tracers", k_tracers<float>, sgrd(D.ny, D.nx, D.nl), D, GF, Ss, Sn.u, Sn.v, T.rho, rk);
+    SL("ks_tend_wind", k_tend_wind<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, rk, Mn.u, Mn.v);
+    const StateF& Ms = (rk == 1) ? Mo : Mn;
+    if (D.ncons > 1)
+      SL("ks_tracers", (k_tracers<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, Mn.u, Mn.v, T.rho, rk);
     if (D.theta_order == 3) {
-      int rc = theta3f(Ss.tp, 0, Ss.u, Ss.v, s->tvu, s->tvv);
+      int rc = theta3f(Ms.tp, 0, Ms.u, Ms.v, s->tvu, s->tvv);
       if (rc) return rc;
     }
-    SL("ks_gas_theta", k_gas_theta<float>, sgrd(D.ny, D.nx, D.nl), D, GF, Ss, Sn.u, Sn.v, s->tvu, s->tvv,
-       C.temperature, C.rad, C.csh, T.rho, T.rt);
-    const dim3 g2 = sgrd(D.ny, D.nx, 1);
-    SL("ks_column_ver", ks_column_ver, g2, D, G, s->GX, So, Sn, T, rk);
+    SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
+       s->fv, s->gu, s->gv);
+    SL("ks_gas_div", ks_gas_div, sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, s->fu, s->fv, s->gu, s->gv, C.temperature,
+       C.rad, C.csh, T.rho, T.rt);
+    const dim3 gc = cgrd(D.ny, D.nx);
+    SL("ks_column_ver", ks_column_ver, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
     if (D.ncons > 1)
-      SL("ks_column_tracers", ks_column_tracers, g2, D, G, GF, s->GX, So, Sn, T.rho, C.temperature, C.csh, rk);
+      SL("ks_column_tracers", ks_column_tracers, gc, cblk(), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature,
+         C.csh, rk);
   }
 #undef SL
   *nk = launches;

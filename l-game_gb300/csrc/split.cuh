@@ -2,13 +2,14 @@
 //
 // FP32: explicit stencils (vorticity, Poisson-bracket flux, the kinetic-energy gradient's
 //       division by the metric, third-order theta edges), scalar and tracer flux
-//       divergences, tracer fall speeds and vertical fluxes, intermediate and tendency
-//       storage.
+//       divergences, tracer fall speeds and vertical fluxes, the coefficients of the
+//       implicit systems, intermediate and tendency storage, and a mirror of the state
+//       (each FP64 state value rounded once when it is written).
 // FP64: the state, its accumulation state_old + dt*tendency, the gradient of the Exner
 //       pressure perturbation and both pressure-gradient products (the hydrostatic
 //       background subtraction), the kinetic energy and its differences (a vertical
-//       difference over a thin layer cancels most of its digits), the vertically implicit
-//       column solves, the budget sums.
+//       difference over a thin layer cancels most of its digits), the right-hand sides and
+//       substitution sweeps of the vertically implicit column solves, the budget sums.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,8 +35,11 @@ SplitCarriedF split_carried(SplitCtx* s);
 // converts n elements FP64 <-> FP32 (field layout identical)
 int split_convert(const double* src, float* dst, long long n, cudaStream_t stream);
 int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream);
-// one step; pg holds the FP64 pressure-gradient arrays (shared with the FP64 path)
-int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn,
+// FP32 mirror of state slot `slot` recomputed from the FP64 state S (after the host wrote S)
+int split_refresh_mirror(SplitCtx* s, const Dims& D, int slot, const State& S, cudaStream_t stream);
+// one step from slot so (state So) to slot sn (state Sn); pg holds the FP64 pressure-gradient
+// arrays (shared with the FP64 path).  The mirrors of both slots must be current.
+int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn, int so, int sn,
                const PGrad<double>& pg, int step, cudaStream_t stream, int* nkernels,
                int (*trace_begin)(void*, const char*), void (*trace_end)(void*, int), void* tracer);
 
