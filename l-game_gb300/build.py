@@ -33,11 +33,13 @@ CUDA_UNITS = [
     ("kernels_fp64.cu", ["-fmad=false"]),
     ("column_fp64.cu", ["-fmad=false"]),
     ("split.cu", ["-fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
+    ("emulator.cu", []),
 ]
 CXX_UNITS = [
     ("host/error.cpp", []),
     ("host/namelist.cpp", []),
     ("host/setup.cpp", []),
+    ("host/teacher.cpp", []),
 ]
 
 

@@ -1,0 +1,901 @@
+// emulator.cu -- radiation emulator: an MLP trained and run on the GPU with hand-written
+// BF16 tensor-core kernels (tcgen05.mma, accumulators in tensor memory).
+//
+// GEMM kernel: one CTA of 128 threads computes a 128 x BN tile of C = A * B^T (A: M x K,
+// B: N x K, both K-major BF16).  Per K block of 64 the threads stage the A and B tiles in
+// shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core
+// matrices: element (r, k) at (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes), one
+// elected thread issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and
+// an FP32 accumulator in BN columns of tensor memory) and commits them to an mbarrier; the
+// block waits on it (bounded) before the tiles are overwritten.  The epilogue reads the
+// accumulator with tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31 = tile rows) and
+// applies one of the fused epilogues (bias + GELU with BF16 and transposed BF16 copies,
+// bias only, GELU derivative for the backward pass, or plain FP32 partial sums for split-K).
+//
+// Every wait on an mbarrier is bounded; on time-out the kernel records an error code, waits
+// (bounded) once more for its own tensor-core work, frees its tensor memory and returns.
+#include "lgame_emulator.h"
+#include "common.h"
+#include "emulator.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace emu {
+
+typedef __nv_bfloat16 bf16;
+
+// ---- tcgen05 / mbarrier primitives (inline PTX) ---------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading (K) and stride (M/N) byte
+// offsets between core matrices, fixed version bits 46-48 = 0b001, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
+// both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
+__host__ __device__ constexpr uint32_t instr_desc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void tc_alloc(uint32_t dst_smem, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// bounded wait for the completion of phase `parity`; false on time-out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (it > 64) __nanosleep(64);
+  }
+  return false;
+}
+// 16 consecutive FP32 accumulator columns of this thread's lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  return 0.5f * (1.f + erff(z * 0.70710678f)) + z * 0.39894228f * __expf(-0.5f * z * z);
+}
+
+// ---- the GEMM -------------------------------------------------------------------------------
+template <int BN>
+__global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
+                                                 int ldb, int M, int N, int K, int kchunk, Epi ep, int* err) {
+  constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ uint64_t mbar;
+  __shared__ uint32_t tmem_base;
+  uint8_t* sA = smem;                  // 128 x 64 BF16 = 16 KB
+  uint8_t* sB = smem + 128 * 64 * 2;   // BN x 64 BF16
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * 128;
+  const int k0 = blockIdx.z * kchunk, k1 = min(K, k0 + kchunk);
+  const uint32_t mb = smem_u32(&mbar);
+  if (warp == 0) tc_alloc(smem_u32(&tmem_base), kCols);
+  if (tid == 0) mbar_init(mb, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  const uint32_t idesc = instr_desc(128, BN);
+  const uint32_t aS = smem_u32(sA), bS = smem_u32(sB);
+  uint32_t phase = 0;
+  bool failed = false;
+  for (int kb = k0; kb < k1; kb += 64) {
+    // stage the tiles: 16-byte chunks (8 elements) into core-matrix order
+    for (int c = tid; c < 128 * 8; c += 128) {
+      const int r = c >> 3, kc = c & 7;
+      const uint4 v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + kb + kc * 8);
+      *reinterpret_cast<uint4*>(sA + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = v;
+    }
+    for (int c = tid; c < BN * 8; c += 128) {
+      const int r = c >> 3, kc = c & 7;
+      const uint4 v = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + kb + kc * 8);
+      *reinterpret_cast<uint4*>(sB + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = v;
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {  // K = 16 per instruction: two core matrices along K
+        const uint64_t ad = smem_desc(aS + s * 256, 128, 1024);
+        const uint64_t bd = smem_desc(bS + s * 256, 128, 1024);
+        tc_mma(tmem, ad, bd, idesc, (kb > k0 || s > 0) ? 1u : 0u);
+      }
+      tc_commit(mb);
+    }
+    const bool ok = mbar_wait(mb, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+  }
+  tc_fence_after();
+  if (failed) {
+    if (tid == 0) atomicExch(err, 1);
+    mbar_wait(mb, phase ^ 1u);  // bounded: let this block's tensor-core work drain
+  } else {
+    const int m = m0 + warp * 32 + lane;  // tile row of this thread
+    for (int c = 0; c < BN; c += 16) {
+      float v[16];
+      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
+      const int nb = n0 + c;
+      switch (ep.kind) {
+        case kEpiF32: {
+          float* out = ep.c + (size_t)blockIdx.z * ep.split_stride + (size_t)m * ep.ldc + nb;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) out[j] = v[j];
+          break;
+        }
+        case kEpiBias: {
+          float* out = ep.c + (size_t)m * ep.ldc + nb;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) out[j] = v[j] + ep.bias[nb + j];
+          break;
+        }
+        case kEpiBiasGelu: {
+          float* z = ep.c + (size_t)m * ep.ldc + nb;
+          bf16* h = ep.h + (size_t)m * ep.ldh + nb;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float zz = v[j] + ep.bias[nb + j];
+            z[j] = zz;
+            const bf16 g = __float2bfloat16_rn(gelu(zz));
+            h[j] = g;
+            ep.ht[(size_t)(nb + j) * ep.ldt + m] = g;
+          }
+          break;
+        }
+        case kEpiGeluBwd: {
+          const float* zp = ep.zprev + (size_t)m * ep.ldc + nb;
+          float* d32 = ep.c + (size_t)m * ep.ldc + nb;
+          bf16* h = ep.h + (size_t)m * ep.ldh + nb;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const float d = v[j] * gelu_grad(zp[j]);
+            d32[j] = d;
+            const bf16 g = __float2bfloat16_rn(d);
+            h[j] = g;
+            ep.ht[(size_t)(nb + j) * ep.ldt + m] = g;
+          }
+          break;
+        }
+        default: break;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc_dealloc(tmem, kCols);
+}
+
+template <int BN>
+int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
+                   int* err, cudaStream_t st) {
+  const size_t shm = (size_t)128 * 64 * 2 + (size_t)BN * 64 * 2;
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+      return LGAME_ERR_CUDA;
+    attr_set = true;
+  }
+  const int kchunk = ((K / splits + 63) / 64) * 64;
+  const dim3 grid((unsigned)(N / BN), (unsigned)(M / 128), (unsigned)((K + kchunk - 1) / kchunk));
+  k_gemm<BN><<<grid, 128, shm, st>>>(A, lda, B, ldb, M, N, K, kchunk, ep, err);
+  return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
+}
+
+int launch_gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
+                int* err, cudaStream_t st) {
+  if (M % 128 || K % 64 || N % 64 || splits < 1) return LGAME_ERR_INVALID_ARG;
+  if (N % 256 == 0) return launch_gemm_bn<256>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+  if (N % 192 == 0) return launch_gemm_bn<192>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+  if (N % 128 == 0) return launch_gemm_bn<128>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+  return launch_gemm_bn<64>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+}
+
+// ---- element-wise and reduction kernels ------------------------------------------------------
+// standardised, zero-padded BF16 inputs, row-major and transposed
+__global__ void k_prep_x(const float* __restrict__ x, int nin, int nin_pad, int batch, const float* mean,
+                         const float* istd, bf16* X, bf16* XT) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch * nin_pad) return;
+  const int r = i / nin_pad, c = i % nin_pad;
+  const float v = (c < nin) ? (x[(size_t)r * nin + c] - mean[c]) * istd[c] : 0.f;
+  const bf16 b = __float2bfloat16_rn(v);
+  X[i] = b;
+  XT[(size_t)c * batch + r] = b;
+}
+__global__ void k_prep_y(const float* __restrict__ y, int nout, int nout_pad, int batch, const float* mean,
+                         const float* istd, float* Yt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch * nout_pad) return;
+  const int r = i / nout_pad, c = i % nout_pad;
+  Yt[i] = (c < nout) ? (y[(size_t)r * nout + c] - mean[c]) * istd[c] : 0.f;
+}
+// loss partial sums per block and the output gradient dL/dY = 2 (Y - Yt) / (batch * nout)
+__global__ void k_loss_dy(const float* Y, const float* Yt, int nout, int nout_pad, int batch, float* d32, bf16* db,
+                          bf16* dbt, float* part) {
+  __shared__ float sh[256];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.f;
+  if (i < batch * nout_pad) {
+    const int r = i / nout_pad, c = i % nout_pad;
+    float d = 0.f;
+    if (c < nout) {
+      const float e = Y[i] - Yt[i];
+      l = e * e;
+      d = 2.f * e / (float)((double)batch * nout);
+    }
+    d32[i] = d;
+    const bf16 b = __float2bfloat16_rn(d);
+    db[i] = b;
+    dbt[(size_t)c * batch + r] = b;
+  }
+  sh[threadIdx.x] = l;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+// deterministic sums: column sums of a rows x cols matrix (one block per column), and the
+// sum of a vector (one block)
+__global__ void k_colsum(const float* a, int rows, int cols, float* out) {
+  __shared__ float sh[256];
+  const int c = blockIdx.x;
+  float s = 0.f;
+  for (int r = threadIdx.x; r < rows; r += 256) s += a[(size_t)r * cols + c];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int k = 128; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[c] = sh[0];
+}
+// split-K partials of dW^T (in x out) summed and written transposed as dW (out x in)
+__global__ void k_splitk_reduce_t(const float* part, int splits, int rows_in, int cols_out, float* gw) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows_in * cols_out) return;
+  const int r = i / cols_out, c = i % cols_out;
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(size_t)z * rows_in * cols_out + i];
+  gw[(size_t)c * rows_in + r] = s;
+}
+__global__ void k_splitk_reduce(const float* part, int splits, long long n, float* out) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(size_t)z * n + i];
+  out[i] = s;
+}
+// Adam update of one parameter matrix (rows x cols) and its BF16 copies (row-major, transposed)
+__global__ void k_adam(float* p, const float* g, float* m, float* v, long long n, int cols, float lr, float b1, float b2,
+                       float c1, float c2, float eps, bf16* pb, bf16* pbt, int rows) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  p[i] = pi;
+  if (pb) {
+    const bf16 b = __float2bfloat16_rn(pi);
+    pb[i] = b;
+    const long long r = i / cols, c = i % cols;
+    pbt[(size_t)c * rows + r] = b;
+  }
+}
+__global__ void k_to_bf16_t(const float* p, long long n, int cols, int rows, bf16* pb, bf16* pbt) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const bf16 b = __float2bfloat16_rn(p[i]);
+  pb[i] = b;
+  const long long r = i / cols, c = i % cols;
+  pbt[(size_t)c * rows + r] = b;
+}
+__global__ void k_denorm(const float* Y, int nout, int nout_pad, int batch, const float* mean, const float* std_,
+                         float* y) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= batch * nout) return;
+  const int r = i / nout, c = i % nout;
+  y[i] = Y[(size_t)r * nout_pad + c] * std_[c] + mean[c];
+}
+__global__ void k_gather_rows(const float* src, const long long* idx, int batch, int ncol, float* dst) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)batch * ncol) return;
+  const long long r = i / ncol, c = i % ncol;
+  dst[i] = src[idx[r] * ncol + c];
+}
+
+inline unsigned blocks(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
+
+}  // namespace emu
+
+using namespace emu;
+
+struct lgame_emu {
+  int nlev = 0, nin = 0, nin_pad = 0, hidden = 0, nout = 0, nout_pad = 0, bmax = 0, device = 0;
+  cudaStream_t st = nullptr;
+  std::vector<void*> allocs;
+  int rows[4], cols[4];              // layer l: rows = outputs (padded), cols = inputs (padded)
+  float *W[4], *b[4], *gW[4], *gb[4], *mW[4], *vW[4], *mb[4], *vb[4];
+  bf16 *Wb[4], *WTb[4];
+  float *xmean, *xistd, *ymean, *ystd, *yistd;
+  float *xraw, *yraw, *Yt, *Y, *Z[3], *dZ32[4], *part, *lpart, *yout;
+  bf16 *X, *XT, *H[3], *HT[3], *dZb[4], *dZT[4];
+  int* err = nullptr;
+  long long adam_t = 0;
+  int splits = 32;
+  // dataset on the device
+  float *dsx = nullptr, *dsy = nullptr;
+  long long dsn = 0;
+  long long* idx = nullptr;
+  // statistics
+  long long gemm_launches = 0;
+  double gemm_flop = 0.0;
+};
+
+namespace {
+
+int emu_fail(int code, const std::string& msg) {
+  lgame_set_error(msg.c_str());
+  return code;
+}
+#define ECK(call)                                                                                    \
+  do {                                                                                               \
+    cudaError_t e_ = (call);                                                                         \
+    if (e_ != cudaSuccess) return emu_fail(LGAME_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int ealloc(lgame_emu* e, T** p, size_t n) {
+  void* q = nullptr;
+  if (cudaMalloc(&q, n * sizeof(T)) != cudaSuccess) return emu_fail(LGAME_ERR_ALLOC, "emulator: cudaMalloc failed");
+  if (cudaMemset(q, 0, n * sizeof(T)) != cudaSuccess) return emu_fail(LGAME_ERR_CUDA, "emulator: cudaMemset failed");
+  e->allocs.push_back(q);
+  *p = (T*)q;
+  return LGAME_OK;
+}
+
+int check_err(lgame_emu* e) {
+  int h = 0;
+  ECK(cudaMemcpyAsync(&h, e->err, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+  ECK(cudaStreamSynchronize(e->st));
+  if (h) return emu_fail(LGAME_ERR_CUDA, "emulator: a tensor-core GEMM timed out waiting for its mbarrier");
+  return LGAME_OK;
+}
+
+int gemm(lgame_emu* e, const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep) {
+  const int rc = launch_gemm(A, lda, B, ldb, M, N, K, splits, ep, e->err, e->st);
+  if (rc != LGAME_OK) return emu_fail(rc, "emulator: GEMM launch failed");
+  e->gemm_launches++;
+  e->gemm_flop += 2.0 * M * N * (double)K;
+  return LGAME_OK;
+}
+
+// forward pass of `batch` prepared rows (X, XT); output Y (standardised, padded)
+int forward(lgame_emu* e, int batch) {
+  const int Hd = e->hidden;
+  const bf16* in = e->X;
+  int ldin = e->nin_pad;
+  for (int l = 0; l < 3; ++l) {
+    Epi ep{};
+    ep.kind = kEpiBiasGelu;
+    ep.bias = e->b[l];
+    ep.c = e->Z[l];
+    ep.ldc = Hd;
+    ep.h = e->H[l];
+    ep.ldh = Hd;
+    ep.ht = e->HT[l];
+    ep.ldt = batch;
+    int rc = gemm(e, in, ldin, e->Wb[l], e->cols[l], batch, Hd, e->cols[l], 1, ep);
+    if (rc) return rc;
+    in = e->H[l];
+    ldin = Hd;
+  }
+  Epi ep{};
+  ep.kind = kEpiBias;
+  ep.bias = e->b[3];
+  ep.c = e->Y;
+  ep.ldc = e->nout_pad;
+  return gemm(e, in, Hd, e->Wb[3], Hd, batch, e->nout_pad, Hd, 1, ep);
+}
+
+// prepared inputs from host or device raw rows
+int prep_x(lgame_emu* e, const float* xraw_dev, int batch) {
+  k_prep_x<<<blocks((long long)batch * e->nin_pad), 256, 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, e->xmean,
+                                                                      e->xistd, e->X, e->XT);
+  ECK(cudaGetLastError());
+  return LGAME_OK;
+}
+
+// loss and gradients of one prepared batch (X, XT, Yt); grads in gW, gb; loss partials in lpart
+int backward(lgame_emu* e, int batch, int* nparts) {
+  const int Hd = e->hidden, no = e->nout_pad;
+  const int np = (int)blocks((long long)batch * no);
+  k_loss_dy<<<np, 256, 0, e->st>>>(e->Y, e->Yt, e->nout, no, batch, e->dZ32[3], e->dZb[3], e->dZT[3], e->lpart);
+  ECK(cudaGetLastError());
+  *nparts = np;
+  for (int l = 3; l >= 0; --l) {
+    // dW_l^T (in x out) = act_{l-1}^T (in x batch) * dZ_l^T (out x batch)^T, split over the batch
+    const bf16* actT = (l == 0) ? e->XT : e->HT[l - 1];
+    const int nin_l = e->cols[l], nout_l = e->rows[l];
+    Epi ep{};
+    ep.kind = kEpiF32;
+    ep.c = e->part;
+    ep.ldc = nout_l;
+    ep.split_stride = (long long)nin_l * nout_l;
+    const int splits = std::min(e->splits, batch / 64);
+    int rc = gemm(e, actT, batch, e->dZT[l], batch, nin_l, nout_l, batch, splits, ep);
+    if (rc) return rc;
+    const int kchunk = ((batch / splits + 63) / 64) * 64;
+    const int zs = (batch + kchunk - 1) / kchunk;
+    k_splitk_reduce_t<<<blocks((long long)nin_l * nout_l), 256, 0, e->st>>>(e->part, zs, nin_l, nout_l, e->gW[l]);
+    ECK(cudaGetLastError());
+    k_colsum<<<nout_l, 256, 0, e->st>>>(e->dZ32[l], batch, nout_l, e->gb[l]);
+    ECK(cudaGetLastError());
+    if (l == 0) break;
+    // dZ_{l-1} = (dZ_l * W_l) .* gelu'(Z_{l-1}): A = dZ_l (batch x out), B = W_l^T (in x out)
+    Epi eb{};
+    eb.kind = kEpiGeluBwd;
+    eb.zprev = e->Z[l - 1];
+    eb.c = e->dZ32[l - 1];
+    eb.ldc = Hd;
+    eb.h = e->dZb[l - 1];
+    eb.ldh = Hd;
+    eb.ht = e->dZT[l - 1];
+    eb.ldt = batch;
+    rc = gemm(e, e->dZb[l], nout_l, e->WTb[l], nout_l, batch, Hd, nout_l, 1, eb);
+    if (rc) return rc;
+  }
+  return LGAME_OK;
+}
+
+int adam(lgame_emu* e, float lr) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  e->adam_t++;
+  const float c1 = (float)(1.0 / (1.0 - std::pow(0.9, (double)e->adam_t)));
+  const float c2 = (float)(1.0 / (1.0 - std::pow(0.999, (double)e->adam_t)));
+  for (int l = 0; l < 4; ++l) {
+    const long long n = (long long)e->rows[l] * e->cols[l];
+    k_adam<<<blocks(n), 256, 0, e->st>>>(e->W[l], e->gW[l], e->mW[l], e->vW[l], n, e->cols[l], lr, b1, b2, c1, c2, eps,
+                                         e->Wb[l], e->WTb[l], e->rows[l]);
+    k_adam<<<blocks(e->rows[l]), 256, 0, e->st>>>(e->b[l], e->gb[l], e->mb[l], e->vb[l], e->rows[l], 1, lr, b1, b2, c1,
+                                                  c2, eps, nullptr, nullptr, 1);
+    ECK(cudaGetLastError());
+  }
+  return LGAME_OK;
+}
+
+int loss_from_parts(lgame_emu* e, int nparts, int batch, float* loss) {
+  std::vector<float> h(nparts);
+  ECK(cudaMemcpyAsync(h.data(), e->lpart, sizeof(float) * nparts, cudaMemcpyDeviceToHost, e->st));
+  ECK(cudaStreamSynchronize(e->st));
+  double s = 0.0;
+  for (float v : h) s += v;
+  if (loss) *loss = (float)(s / ((double)batch * e->nout));
+  return LGAME_OK;
+}
+
+int upload_batch(lgame_emu* e, const float* x, const float* y, int batch) {
+  ECK(cudaMemcpyAsync(e->xraw, x, sizeof(float) * (size_t)batch * e->nin, cudaMemcpyHostToDevice, e->st));
+  int rc = prep_x(e, e->xraw, batch);
+  if (rc) return rc;
+  if (y) {
+    ECK(cudaMemcpyAsync(e->yraw, y, sizeof(float) * (size_t)batch * e->nout, cudaMemcpyHostToDevice, e->st));
+    k_prep_y<<<blocks((long long)batch * e->nout_pad), 256, 0, e->st>>>(e->yraw, e->nout, e->nout_pad, batch, e->ymean,
+                                                                         e->yistd, e->Yt);
+    ECK(cudaGetLastError());
+  }
+  return LGAME_OK;
+}
+
+int refresh_bf16(lgame_emu* e) {
+  for (int l = 0; l < 4; ++l) {
+    const long long n = (long long)e->rows[l] * e->cols[l];
+    k_to_bf16_t<<<blocks(n), 256, 0, e->st>>>(e->W[l], n, e->cols[l], e->rows[l], e->Wb[l], e->WTb[l]);
+    ECK(cudaGetLastError());
+  }
+  return LGAME_OK;
+}
+
+}  // namespace
+
+namespace emu {
+// device-side inference for the coupling code: n rows of raw features (device) -> heating
+// rates (device, n x nout), in batches of bmax
+int infer_device(lgame_emu* e, const float* x_dev, long long n, float* y_dev, cudaStream_t st) {
+  if (cudaStreamSynchronize(st) != cudaSuccess) return LGAME_ERR_CUDA;
+  for (long long r0 = 0; r0 < n; r0 += e->bmax) {
+    const int b = (int)std::min<long long>(e->bmax, n - r0);
+    const int bp = ((b + 127) / 128) * 128;
+    if (bp != b) ECK(cudaMemsetAsync(e->xraw, 0, sizeof(float) * (size_t)bp * e->nin, e->st));
+    ECK(cudaMemcpyAsync(e->xraw, x_dev + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyDeviceToDevice,
+                        e->st));
+    int rc = prep_x(e, e->xraw, bp);
+    if (rc) return rc;
+    rc = forward(e, bp);
+    if (rc) return rc;
+    k_denorm<<<blocks((long long)b * e->nout), 256, 0, e->st>>>(e->Y, e->nout, e->nout_pad, b, e->ymean, e->ystd,
+                                                                 y_dev + r0 * e->nout);
+    ECK(cudaGetLastError());
+  }
+  ECK(cudaStreamSynchronize(e->st));
+  return check_err(e);
+}
+int nin_of(const lgame_emu* e) { return e->nin; }
+int nout_of(const lgame_emu* e) { return e->nout; }
+int nlev_of(const lgame_emu* e) { return e->nlev; }
+}  // namespace emu
+
+extern "C" int lgame_emu_create(int nlev, int hidden, int batch_max, unsigned long long seed, int device,
+                                lgame_emu** out) {
+  if (!out || nlev < 3 || nlev > LGAME_RAD_NLEV_MAX || hidden < 256 || hidden % 256 || batch_max < 128 ||
+      batch_max % 128)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_create: bad arguments (nlev 3..128, hidden % 256, batch_max % 128)");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev)
+    return emu_fail(LGAME_ERR_NO_DEVICE, "lgame_emu_create: no CUDA device");
+  ECK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  ECK(cudaGetDeviceProperties(&prop, device));
+  if (prop.major != 10 || prop.minor != 3)
+    return emu_fail(LGAME_ERR_NO_DEVICE, "lgame_emu_create: the tensor-core kernels need an sm_103 GPU");
+  auto* e = new lgame_emu();
+  auto fail = [&](int rc) { lgame_emu_destroy(e); return rc; };
+  e->nlev = nlev;
+  e->nin = 4 * nlev + 2;
+  e->nin_pad = ((e->nin + 63) / 64) * 64;
+  e->hidden = hidden;
+  e->nout = 2 * nlev;
+  e->nout_pad = ((e->nout + 63) / 64) * 64;
+  e->bmax = batch_max;
+  e->device = device;
+  if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) return fail(LGAME_ERR_CUDA);
+  const int Hd = hidden;
+  const int rows[4] = {Hd, Hd, Hd, e->nout_pad}, cols[4] = {e->nin_pad, Hd, Hd, Hd};
+  int rc;
+  for (int l = 0; l < 4; ++l) {
+    e->rows[l] = rows[l];
+    e->cols[l] = cols[l];
+    const size_t n = (size_t)rows[l] * cols[l];
+    if ((rc = ealloc(e, &e->W[l], n)) || (rc = ealloc(e, &e->gW[l], n)) || (rc = ealloc(e, &e->mW[l], n)) ||
+        (rc = ealloc(e, &e->vW[l], n)) || (rc = ealloc(e, &e->Wb[l], n)) || (rc = ealloc(e, &e->WTb[l], n)) ||
+        (rc = ealloc(e, &e->b[l], rows[l])) || (rc = ealloc(e, &e->gb[l], rows[l])) ||
+        (rc = ealloc(e, &e->mb[l], rows[l])) || (rc = ealloc(e, &e->vb[l], rows[l])))
+      return fail(rc);
+  }
+  const size_t B = batch_max;
+  if ((rc = ealloc(e, &e->xmean, e->nin)) || (rc = ealloc(e, &e->xistd, e->nin)) || (rc = ealloc(e, &e->ymean, e->nout)) ||
+      (rc = ealloc(e, &e->ystd, e->nout)) || (rc = ealloc(e, &e->yistd, e->nout)) ||
+      (rc = ealloc(e, &e->xraw, B * e->nin)) || (rc = ealloc(e, &e->yraw, B * e->nout)) ||
+      (rc = ealloc(e, &e->Yt, B * e->nout_pad)) || (rc = ealloc(e, &e->Y, B * e->nout_pad)) ||
+      (rc = ealloc(e, &e->X, B * e->nin_pad)) || (rc = ealloc(e, &e->XT, B * e->nin_pad)) ||
+      (rc = ealloc(e, &e->yout, B * e->nout)) || (rc = ealloc(e, &e->err, 1)))
+    return fail(rc);
+  for (int l = 0; l < 3; ++l)
+    if ((rc = ealloc(e, &e->Z[l], B * Hd)) || (rc = ealloc(e, &e->H[l], B * Hd)) || (rc = ealloc(e, &e->HT[l], B * Hd)))
+      return fail(rc);
+  for (int l = 0; l < 4; ++l) {
+    const size_t w = (l == 3) ? e->nout_pad : Hd;
+    if ((rc = ealloc(e, &e->dZ32[l], B * w)) || (rc = ealloc(e, &e->dZb[l], B * w)) || (rc = ealloc(e, &e->dZT[l], B * w)))
+      return fail(rc);
+  }
+  size_t pmax = 0;
+  for (int l = 0; l < 4; ++l) pmax = std::max(pmax, (size_t)rows[l] * cols[l]);
+  if ((rc = ealloc(e, &e->part, pmax * e->splits)) || (rc = ealloc(e, &e->lpart, B * e->nout_pad / 256 + 1)))
+    return fail(rc);
+  // identity normalisation, Xavier-uniform weights (splitmix64), zero biases
+  std::vector<float> one(std::max(e->nin, e->nout), 1.f);
+  ECK(cudaMemcpy(e->xistd, one.data(), sizeof(float) * e->nin, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->ystd, one.data(), sizeof(float) * e->nout, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->yistd, one.data(), sizeof(float) * e->nout, cudaMemcpyHostToDevice));
+  uint64_t s = seed ? seed : 0x9E3779B97F4A7C15ull;
+  auto next = [&]() {
+    s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) / 9007199254740992.0;
+  };
+  const int real_in[4] = {e->nin, Hd, Hd, Hd}, real_out[4] = {Hd, Hd, Hd, e->nout};
+  for (int l = 0; l < 4; ++l) {
+    std::vector<float> w((size_t)rows[l] * cols[l], 0.f);
+    const double a = std::sqrt(6.0 / (real_in[l] + real_out[l]));
+    for (int r = 0; r < real_out[l]; ++r)
+      for (int c = 0; c < real_in[l]; ++c) w[(size_t)r * cols[l] + c] = (float)((2.0 * next() - 1.0) * a);
+    ECK(cudaMemcpy(e->W[l], w.data(), sizeof(float) * w.size(), cudaMemcpyHostToDevice));
+  }
+  if ((rc = refresh_bf16(e))) return fail(rc);
+  ECK(cudaStreamSynchronize(e->st));
+  *out = e;
+  return LGAME_OK;
+}
+
+extern "C" void lgame_emu_destroy(lgame_emu* e) {
+  if (!e) return;
+  if (e->st) cudaStreamSynchronize(e->st);
+  for (void* p : e->allocs) cudaFree(p);
+  if (e->dsx) cudaFree(e->dsx);
+  if (e->dsy) cudaFree(e->dsy);
+  if (e->idx) cudaFree(e->idx);
+  if (e->st) cudaStreamDestroy(e->st);
+  delete e;
+}
+
+extern "C" long long lgame_emu_num_params(const lgame_emu* e) {
+  if (!e) return 0;
+  const long long H = e->hidden;
+  return H * e->nin + H + 2 * (H * H + H) + (long long)e->nout * H + e->nout;
+}
+
+namespace {
+// walk the real (unpadded) parameters in the public order: fn(device ptr, row length, rows, row stride)
+template <class F>
+void for_params(lgame_emu* e, F fn) {
+  const int real_in[4] = {e->nin, e->hidden, e->hidden, e->hidden};
+  const int real_out[4] = {e->hidden, e->hidden, e->hidden, e->nout};
+  for (int l = 0; l < 4; ++l) {
+    fn(e->W[l], real_in[l], real_out[l], e->cols[l], l, false);
+    fn(e->b[l], real_out[l], 1, real_out[l], l, true);
+  }
+}
+}  // namespace
+
+extern "C" int lgame_emu_get_params(lgame_emu* e, float* out) {
+  if (!e || !out) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_get_params: bad arguments");
+  size_t off = 0;
+  int rc = LGAME_OK;
+  for_params(e, [&](float* d, int len, int nrows, int stride, int, bool) {
+    if (rc) return;
+    if (cudaMemcpy2D(out + off, len * sizeof(float), d, stride * sizeof(float), len * sizeof(float), nrows,
+                     cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_get_params: copy failed");
+    off += (size_t)len * nrows;
+  });
+  return rc;
+}
+
+extern "C" int lgame_emu_set_params(lgame_emu* e, const float* in) {
+  if (!e || !in) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_set_params: bad arguments");
+  size_t off = 0;
+  int rc = LGAME_OK;
+  for_params(e, [&](float* d, int len, int nrows, int stride, int, bool) {
+    if (rc) return;
+    if (cudaMemcpy2D(d, stride * sizeof(float), in + off, len * sizeof(float), len * sizeof(float), nrows,
+                     cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_set_params: copy failed");
+    off += (size_t)len * nrows;
+  });
+  if (rc) return rc;
+  rc = refresh_bf16(e);
+  if (rc) return rc;
+  ECK(cudaStreamSynchronize(e->st));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_emu_set_normalization(lgame_emu* e, const float* xm, const float* xs, const float* ym,
+                                           const float* ys) {
+  if (!e || !xm || !xs || !ym || !ys) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_set_normalization: bad arguments");
+  std::vector<float> xi(e->nin), yi(e->nout);
+  for (int i = 0; i < e->nin; ++i) xi[i] = xs[i] > 0.f ? 1.f / xs[i] : 0.f;
+  for (int i = 0; i < e->nout; ++i) yi[i] = ys[i] > 0.f ? 1.f / ys[i] : 0.f;
+  ECK(cudaMemcpy(e->xmean, xm, sizeof(float) * e->nin, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->xistd, xi.data(), sizeof(float) * e->nin, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->ymean, ym, sizeof(float) * e->nout, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->ystd, ys, sizeof(float) * e->nout, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->yistd, yi.data(), sizeof(float) * e->nout, cudaMemcpyHostToDevice));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_emu_loss_grad(lgame_emu* e, const float* x, const float* y, int batch, float* loss, float* grads) {
+  if (!e || !x || !y || batch < 128 || batch % 128 || batch > e->bmax)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_loss_grad: bad arguments (batch a multiple of 128 <= batch_max)");
+  int rc = upload_batch(e, x, y, batch);
+  if (!rc) rc = forward(e, batch);
+  int np = 0;
+  if (!rc) rc = backward(e, batch, &np);
+  if (!rc) rc = loss_from_parts(e, np, batch, loss);
+  if (!rc) rc = check_err(e);
+  if (rc) return rc;
+  if (grads) {
+    size_t off = 0;
+    const int real_in[4] = {e->nin, e->hidden, e->hidden, e->hidden};
+    const int real_out[4] = {e->hidden, e->hidden, e->hidden, e->nout};
+    for (int l = 0; l < 4; ++l) {
+      ECK(cudaMemcpy2D(grads + off, real_in[l] * sizeof(float), e->gW[l], e->cols[l] * sizeof(float),
+                       real_in[l] * sizeof(float), real_out[l], cudaMemcpyDeviceToHost));
+      off += (size_t)real_in[l] * real_out[l];
+      ECK(cudaMemcpy(grads + off, e->gb[l], sizeof(float) * real_out[l], cudaMemcpyDeviceToHost));
+      off += real_out[l];
+    }
+  }
+  return LGAME_OK;
+}
+
+extern "C" int lgame_emu_train_step(lgame_emu* e, const float* x, const float* y, int batch, float lr, float* loss) {
+  if (!e || !x || !y || batch < 128 || batch % 128 || batch > e->bmax)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_train_step: bad arguments");
+  int rc = upload_batch(e, x, y, batch);
+  if (!rc) rc = forward(e, batch);
+  int np = 0;
+  if (!rc) rc = backward(e, batch, &np);
+  if (!rc) rc = adam(e, lr);
+  if (!rc) rc = loss_from_parts(e, np, batch, loss);
+  if (!rc) rc = check_err(e);
+  return rc;
+}
+
+extern "C" int lgame_emu_set_dataset(lgame_emu* e, const float* x, const float* y, long long n) {
+  if (!e || !x || !y || n < e->bmax) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_set_dataset: bad arguments");
+  if (e->dsx) cudaFree(e->dsx);
+  if (e->dsy) cudaFree(e->dsy);
+  if (e->idx) cudaFree(e->idx);
+  e->dsx = e->dsy = nullptr;
+  e->idx = nullptr;
+  ECK(cudaMalloc(&e->dsx, sizeof(float) * (size_t)n * e->nin));
+  ECK(cudaMalloc(&e->dsy, sizeof(float) * (size_t)n * e->nout));
+  ECK(cudaMalloc(&e->idx, sizeof(long long) * (size_t)e->bmax));
+  ECK(cudaMemcpy(e->dsx, x, sizeof(float) * (size_t)n * e->nin, cudaMemcpyHostToDevice));
+  ECK(cudaMemcpy(e->dsy, y, sizeof(float) * (size_t)n * e->nout, cudaMemcpyHostToDevice));
+  e->dsn = n;
+  return LGAME_OK;
+}
+
+extern "C" int lgame_emu_train_epoch(lgame_emu* e, int batch, float lr, unsigned long long seed, float* mean_loss) {
+  if (!e || !e->dsx || batch < 128 || batch % 128 || batch > e->bmax)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_train_epoch: no dataset or bad batch");
+  // shuffled order (Fisher-Yates with splitmix64), whole batches only
+  std::vector<long long> perm(e->dsn);
+  for (long long i = 0; i < e->dsn; ++i) perm[i] = i;
+  uint64_t s = seed ^ 0xD1B54A32D192ED03ull;
+  auto next = [&]() {
+    s += 0x9E3779B97F4A7C15ull;
+    uint64_t z = s;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  };
+  for (long long i = e->dsn - 1; i > 0; --i) std::swap(perm[i], perm[(long long)(next() % (uint64_t)(i + 1))]);
+  const long long nb = e->dsn / batch;
+  double acc = 0.0;
+  for (long long k = 0; k < nb; ++k) {
+    ECK(cudaMemcpyAsync(e->idx, perm.data() + k * batch, sizeof(long long) * batch, cudaMemcpyHostToDevice, e->st));
+    k_gather_rows<<<blocks((long long)batch * e->nin), 256, 0, e->st>>>(e->dsx, e->idx, batch, e->nin, e->xraw);
+    k_gather_rows<<<blocks((long long)batch * e->nout), 256, 0, e->st>>>(e->dsy, e->idx, batch, e->nout, e->yraw);
+    ECK(cudaGetLastError());
+    int rc = prep_x(e, e->xraw, batch);
+    if (rc) return rc;
+    k_prep_y<<<blocks((long long)batch * e->nout_pad), 256, 0, e->st>>>(e->yraw, e->nout, e->nout_pad, batch, e->ymean,
+                                                                         e->yistd, e->Yt);
+    rc = forward(e, batch);
+    int np = 0;
+    if (!rc) rc = backward(e, batch, &np);
+    if (!rc) rc = adam(e, lr);
+    float l = 0.f;
+    if (!rc) rc = loss_from_parts(e, np, batch, &l);
+    if (rc) return rc;
+    acc += l;
+  }
+  if (mean_loss) *mean_loss = nb ? (float)(acc / nb) : 0.f;
+  return check_err(e);
+}
+
+extern "C" int lgame_emu_infer(lgame_emu* e, const float* x, long long n, float* y) {
+  if (!e || !x || !y || n < 0) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_infer: bad arguments");
+  for (long long r0 = 0; r0 < n; r0 += e->bmax) {
+    const int b = (int)std::min<long long>(e->bmax, n - r0);
+    const int bp = ((b + 127) / 128) * 128;
+    if (bp != b) ECK(cudaMemsetAsync(e->xraw, 0, sizeof(float) * (size_t)bp * e->nin, e->st));
+    ECK(cudaMemcpyAsync(e->xraw, x + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyHostToDevice, e->st));
+    int rc = prep_x(e, e->xraw, bp);
+    if (!rc) rc = forward(e, bp);
+    if (rc) return rc;
+    k_denorm<<<blocks((long long)b * e->nout), 256, 0, e->st>>>(e->Y, e->nout, e->nout_pad, b, e->ymean, e->ystd,
+                                                                 e->yout);
+    ECK(cudaGetLastError());
+    ECK(cudaMemcpyAsync(y + r0 * e->nout, e->yout, sizeof(float) * (size_t)b * e->nout, cudaMemcpyDeviceToHost, e->st));
+  }
+  ECK(cudaStreamSynchronize(e->st));
+  return check_err(e);
+}
+
+extern "C" int lgame_emu_gemm_bf16(lgame_emu* e, const unsigned short* a, const unsigned short* b, float* c, int m,
+                                   int n, int k) {
+  if (!e || !a || !b || !c || m <= 0 || n <= 0 || k <= 0 || m % 128 || k % 64 || n % 64)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_gemm_bf16: bad arguments (M % 128, K % 64, N % 64)");
+  bf16 *da = nullptr, *db = nullptr;
+  float* dc = nullptr;
+  ECK(cudaMalloc(&da, sizeof(bf16) * (size_t)m * k));
+  ECK(cudaMalloc(&db, sizeof(bf16) * (size_t)n * k));
+  ECK(cudaMalloc(&dc, sizeof(float) * (size_t)m * n));
+  int rc = LGAME_OK;
+  if (cudaMemcpy(da, a, sizeof(bf16) * (size_t)m * k, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(db, b, sizeof(bf16) * (size_t)n * k, cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_gemm_bf16: upload failed");
+  if (!rc) {
+    Epi ep{};
+    ep.kind = kEpiF32;
+    ep.c = dc;
+    ep.ldc = n;
+    rc = gemm(e, da, k, db, k, m, n, k, 1, ep);
+  }
+  if (!rc && cudaStreamSynchronize(e->st) != cudaSuccess) rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_gemm_bf16: kernel failed");
+  if (!rc) rc = check_err(e);
+  if (!rc && cudaMemcpy(c, dc, sizeof(float) * (size_t)m * n, cudaMemcpyDeviceToHost) != cudaSuccess)
+    rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_gemm_bf16: download failed");
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dc);
+  return rc;
+}
+
+extern "C" int lgame_emu_stats(lgame_emu* e, long long* launches, double* flop) {
+  if (!e) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_stats: null");
+  if (launches) *launches = e->gemm_launches;
+  if (flop) *flop = e->gemm_flop;
+  e->gemm_launches = 0;
+  e->gemm_flop = 0.0;
+  return LGAME_OK;
+}

@@ -1,12 +1,15 @@
 // lgame_gpu.cu -- C ABI of the GB300 HEVI step: device memory, host<->device copies and
 // the order of the kernels of one pchevi call (src/time_stepping/mo_manage_pchevi.F90).
 #include "lgame_gpu.h"
+#include "lgame_emulator.h"
 #include "common.h"
+#include "emulator.cuh"
 #include "kernels.cuh"
 #include "split.cuh"
 
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -903,4 +906,221 @@ extern "C" int lgame_gpu_budgets_static(lgame_gpu* c, int slot, double* out, int
   const int rc = budgets_static_on_device(c, slot, out, nq);
   if (prev != dev) cudaSetDevice(prev);
   return rc;
+}
+
+// ---- radiation: emulator features, heating rates -> power density, one emulator update ------
+// (include/lgame_emulator.h; the reference's seam is update_rad_fluxes,
+// src/radiation/mo_manage_radiation_calls.F90:17-59)
+namespace {
+
+struct RadBuffers {
+  double *albedo = nullptr, *lat = nullptr, *lon = nullptr;
+  float *features = nullptr, *heating = nullptr;
+  long long ncol = 0;
+  int nlev = 0;
+};
+std::mutex g_rad_mu;
+std::vector<std::pair<const lgame_gpu*, RadBuffers>> g_rad;  // per context
+
+RadBuffers* rad_of(const lgame_gpu* c) {
+  for (auto& p : g_rad)
+    if (p.first == c) return &p.second;
+  return nullptr;
+}
+
+// coszenith, mo_rterrtmgp_coupler.F90:550-629 (the sun's direction from the Earth's rotation
+// and revolution relative to the winter solstice 2019-12-20 12:00 UTC), 0 at night
+__device__ double coszenith(double lat, double lon, double t) {
+  const double omega = 7.292115e-5, omega_rev = 1.99099e-7, obliquity = 0.409092592843564;
+  const double tt = t - 1576843200.0;
+  const double rot = omega * tt;
+  const double n1 = cos(lat) * cos(lon), n2 = cos(lat) * sin(lon), n3 = sin(lat);
+  const double s1 = -cos(rot) * cos(obliquity) * n1 + sin(rot) * cos(obliquity) * n2 + sin(obliquity) * n3;
+  const double s2 = -sin(rot) * n1 - cos(rot) * n2;
+  const double s3 = cos(rot) * sin(obliquity) * n1 - sin(rot) * sin(obliquity) * n2 + cos(obliquity) * n3;
+  (void)s3;
+  const double c = -(s1 * cos(omega_rev * tt) + s2 * sin(omega_rev * tt));
+  return c < 0.0 ? 0.0 : c;
+}
+
+// one thread per column: T, dry-air pressure, vapour and ozone densities of every layer,
+// albedo and cos(zenith); column index ji + ny*(jk-1), 4*nl+2 floats per column
+__global__ void k_rad_features(Dims D, Grid<double> G, State S, const double* albedo, const double* lat,
+                               const double* lon, double t, float* X) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long col = (ji - 1) + (long long)D.ny * (jk - 1);
+  const int nl = D.nl, nf = 4 * nl + 2;
+  float* x = X + col * nf;
+  const double sigma = 20e3 / sqrt(8.0 * log(2.0));  // calc_o3_vmr: FWHM 20 km, maximum 8.5e-6 at 34 km
+  const double m_o3 = 0.0479982;                       // kg/mol
+  for (int jl = 1; jl <= nl; ++jl) {
+    const long long i = IX(D, ji, jk, jl);
+    const double rd = S.rho[i + (long long)(D.g - 1) * D.fstride];
+    const double rv = D.lmoist ? S.rho[i + (long long)D.g * D.fstride] : 0.0;
+    double T = (G.theta_v_bg[i] + S.tp[i]) * (G.exner_bg[i] + S.ep[i]);  // temperature_diagnostics
+    if (D.lmoist) T = T / (1.0 + rv / rd * (kM_D / kM_V - 1.0));
+    const double dz = G.z_scalar[i] - 34e3;
+    const double vmr = 8.5e-6 * exp(-dz * dz / (2.0 * sigma * sigma));
+    x[jl - 1] = (float)T;
+    x[nl + jl - 1] = (float)(kR_D * rd * T);
+    x[2 * nl + jl - 1] = (float)rv;
+    x[3 * nl + jl - 1] = (float)(vmr * rd * m_o3 / kM_D);
+  }
+  x[4 * nl] = (float)albedo[col];
+  x[4 * nl + 1] = (float)coszenith(lat[col], lon[col], t);
+}
+
+// radiation_tendency (W m^-3) = (shortwave + longwave heating rate)/86400 * rho_gas * c_d_p
+__global__ void k_rad_apply(Dims D, State S, const float* heat, double* rad, float* rad_f) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  const long long col = (ji - 1) + (long long)D.ny * (jk - 1);
+  const long long i = IX(D, ji, jk, jl);
+  const float hr = heat[col * 2 * D.nl + (jl - 1)] + heat[col * 2 * D.nl + D.nl + (jl - 1)];
+  double rho = S.rho[i + (long long)(D.g - 1) * D.fstride];
+  if (D.lmoist) rho += S.rho[i + (long long)D.g * D.fstride];
+  const double q = (double)hr / 86400.0 * rho * kC_D_P;
+  rad[i] = q;
+  if (rad_f) rad_f[i] = (float)q;
+}
+
+int rad_buffers(lgame_gpu* c, RadBuffers** out) {
+  std::lock_guard<std::mutex> lk(g_rad_mu);
+  RadBuffers* r = rad_of(c);
+  if (!r) {
+    g_rad.push_back({c, RadBuffers{}});
+    r = &g_rad.back().second;
+  }
+  const Dims& D = c->D;
+  if (!r->features) {
+    r->ncol = (long long)D.ny * D.nx;
+    r->nlev = D.nl;
+    const size_t nf = 4 * (size_t)D.nl + 2;
+    if (cudaMalloc(&r->albedo, sizeof(double) * r->ncol) != cudaSuccess ||
+        cudaMalloc(&r->lat, sizeof(double) * r->ncol) != cudaSuccess ||
+        cudaMalloc(&r->lon, sizeof(double) * r->ncol) != cudaSuccess ||
+        cudaMalloc(&r->features, sizeof(float) * r->ncol * nf) != cudaSuccess ||
+        cudaMalloc(&r->heating, sizeof(float) * r->ncol * 2 * D.nl) != cudaSuccess)
+      return set_err(LGAME_ERR_ALLOC, "radiation buffers: cudaMalloc failed");
+    c->allocations.push_back(r->albedo);
+    c->allocations.push_back(r->lat);
+    c->allocations.push_back(r->lon);
+    c->allocations.push_back(r->features);
+    c->allocations.push_back(r->heating);
+    c->bytes += (long long)(sizeof(double) * 3 * r->ncol + sizeof(float) * r->ncol * (nf + 2 * D.nl));
+    cudaMemset(r->albedo, 0, sizeof(double) * r->ncol);
+    cudaMemset(r->lat, 0, sizeof(double) * r->ncol);
+    cudaMemset(r->lon, 0, sizeof(double) * r->ncol);
+  }
+  *out = r;
+  return LGAME_OK;
+}
+
+int rad_features_dev(lgame_gpu* c, RadBuffers* r, int slot, double t) {
+  const Dims& D = c->D;
+  k_rad_features<<<dim3((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 3) / 4)), dim3(32, 4), 0, c->stream>>>(
+      D, c->G, c->st[slot], r->albedo, r->lat, r->lon, t, r->features);
+  CK(cudaGetLastError());
+  return LGAME_OK;
+}
+
+int rad_apply_dev(lgame_gpu* c, RadBuffers* r, int slot) {
+  const Dims& D = c->D;
+  float* rad_f = c->split ? split_carried(c->split).rad : nullptr;
+  k_rad_apply<<<grd(D, D.ny, D.nx, D.nl), blk(), 0, c->stream>>>(D, c->st[slot], r->heating, c->rad, rad_f);
+  CK(cudaGetLastError());
+  return LGAME_OK;
+}
+}  // namespace
+
+extern "C" int lgame_gpu_rad_set_surface(lgame_gpu* c, const double* albedo, const double* lat, const double* lon) {
+  if (!c || !albedo || !lat || !lon) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_set_surface: bad arguments");
+  RadBuffers* r = nullptr;
+  int rc = rad_buffers(c, &r);
+  if (rc) return rc;
+  const size_t n = sizeof(double) * r->ncol;
+  CK(cudaMemcpy(r->albedo, albedo, n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(r->lat, lat, n, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(r->lon, lon, n, cudaMemcpyHostToDevice));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_rad_features(lgame_gpu* c, int slot, double t, float* features) {
+  if (!c || slot < 0 || slot > 1) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_features: bad arguments");
+  if (!c->grid_set) return set_err(LGAME_ERR_STATE, "lgame_gpu_rad_features: lgame_gpu_set_grid has not been called");
+  RadBuffers* r = nullptr;
+  int rc = rad_buffers(c, &r);
+  if (!rc) rc = rad_features_dev(c, r, slot, t);
+  if (rc) return rc;
+  if (features)
+    CK(cudaMemcpyAsync(features, r->features, sizeof(float) * r->ncol * (4 * (size_t)r->nlev + 2), cudaMemcpyDeviceToHost,
+                       c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_rad_apply_heating(lgame_gpu* c, int slot, const float* heating) {
+  if (!c || !heating || slot < 0 || slot > 1)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_apply_heating: bad arguments");
+  RadBuffers* r = nullptr;
+  int rc = rad_buffers(c, &r);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(r->heating, heating, sizeof(float) * r->ncol * 2 * r->nlev, cudaMemcpyHostToDevice, c->stream));
+  rc = rad_apply_dev(c, r, slot);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_rad_update(lgame_gpu* c, lgame_emu* emu, int slot, double t, int sample_stride,
+                                    double bound, double* report) {
+  if (!c || !emu || slot < 0 || slot > 1 || sample_stride < 0)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_update: bad arguments");
+  if (emu::nlev_of(emu) != c->D.nl)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_update: the emulator's nlev differs from n_layers");
+  const auto t0 = std::chrono::steady_clock::now();
+  RadBuffers* r = nullptr;
+  int rc = rad_buffers(c, &r);
+  if (!rc) rc = rad_features_dev(c, r, slot, t);
+  if (rc) return rc;
+  rc = emu::infer_device(emu, r->features, r->ncol, r->heating, c->stream);
+  if (rc) return rc;
+  const int nl = r->nlev, nf = 4 * nl + 2, nh = 2 * nl;
+  double rms = 0.0;
+  long long nsample = 0;
+  bool fallback = false;
+  if (sample_stride > 0) {
+    nsample = (r->ncol + sample_stride - 1) / sample_stride;
+    std::vector<float> xs((size_t)nsample * nf), he((size_t)nsample * nh), ht((size_t)nsample * nh);
+    CK(cudaMemcpy2DAsync(xs.data(), sizeof(float) * nf, r->features, sizeof(float) * nf * sample_stride,
+                         sizeof(float) * nf, nsample, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpy2DAsync(he.data(), sizeof(float) * nh, r->heating, sizeof(float) * nh * sample_stride,
+                         sizeof(float) * nh, nsample, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    rc = lgame_rad_teacher(xs.data(), nsample, nl, ht.data());
+    if (rc) return rc;
+    double s = 0.0;
+    for (size_t k = 0; k < he.size(); ++k) s += (double)(he[k] - ht[k]) * (double)(he[k] - ht[k]);
+    rms = std::sqrt(s / (double)he.size());
+    if (rms > bound) {  // fallback: the teacher for every column
+      fallback = true;
+      std::vector<float> xa((size_t)r->ncol * nf), ha((size_t)r->ncol * nh);
+      CK(cudaMemcpy(xa.data(), r->features, sizeof(float) * xa.size(), cudaMemcpyDeviceToHost));
+      rc = lgame_rad_teacher(xa.data(), r->ncol, nl, ha.data());
+      if (rc) return rc;
+      CK(cudaMemcpy(r->heating, ha.data(), sizeof(float) * ha.size(), cudaMemcpyHostToDevice));
+    }
+  }
+  rc = rad_apply_dev(c, r, slot);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));
+  if (report) {
+    report[0] = rms;
+    report[1] = fallback ? 1.0 : 0.0;
+    report[2] = (double)nsample;
+    report[3] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return LGAME_OK;
 }

@@ -107,6 +107,7 @@ def load_library(path: str | os.PathLike | None = None):
         raise FileNotFoundError(f"{p} is missing: run `python l-game_gb300/build.py` (or __graft_entry__.build())")
     lib = C.CDLL(str(p))
     vp, i, d, ll = C.c_void_p, C.c_int, C.c_double, C.c_longlong
+    fp = C.POINTER(C.c_float)
     pp = C.POINTER(C.POINTER(C.c_double))
     sig = {
         "lgame_gpu_create": (i, [C.POINTER(Config), C.POINTER(vp)]),
@@ -137,6 +138,26 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_host_state_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
         "lgame_host_diag_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
         "lgame_host_surface_field": (C.POINTER(C.c_double), [vp, i, C.POINTER(C.c_size_t)]),
+        "lgame_gpu_budgets_static": (i, [vp, i, C.POINTER(C.c_double), i]),
+        # radiation emulator (include/lgame_emulator.h)
+        "lgame_rad_teacher": (i, [fp, ll, i, fp]),
+        "lgame_emu_create": (i, [i, i, i, C.c_ulonglong, i, C.POINTER(vp)]),
+        "lgame_emu_destroy": (None, [vp]),
+        "lgame_emu_num_params": (ll, [vp]),
+        "lgame_emu_get_params": (i, [vp, fp]),
+        "lgame_emu_set_params": (i, [vp, fp]),
+        "lgame_emu_set_normalization": (i, [vp, fp, fp, fp, fp]),
+        "lgame_emu_loss_grad": (i, [vp, fp, fp, i, fp, fp]),
+        "lgame_emu_train_step": (i, [vp, fp, fp, i, C.c_float, fp]),
+        "lgame_emu_set_dataset": (i, [vp, fp, fp, ll]),
+        "lgame_emu_train_epoch": (i, [vp, i, C.c_float, C.c_ulonglong, fp]),
+        "lgame_emu_infer": (i, [vp, fp, ll, fp]),
+        "lgame_emu_gemm_bf16": (i, [vp, C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), fp, i, i, i]),
+        "lgame_emu_stats": (i, [vp, C.POINTER(ll), C.POINTER(d)]),
+        "lgame_gpu_rad_set_surface": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
+        "lgame_gpu_rad_features": (i, [vp, i, d, fp]),
+        "lgame_gpu_rad_apply_heating": (i, [vp, i, fp]),
+        "lgame_gpu_rad_update": (i, [vp, vp, i, d, i, d, C.POINTER(d)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
