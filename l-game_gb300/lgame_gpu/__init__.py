@@ -229,7 +229,8 @@ def config_from_namelist(n: Namelist) -> Config:
 
 class HostModel:
     """Grid, background state and idealised initial state built by the library's host code
-    (lgame_host_setup): the inputs a Fortran host would pass to the GPU step."""
+    (lgame_host_setup): the inputs a Fortran host would pass to the GPU step.  grid, state,
+    diag and surface are numpy views of the library's arrays, valid while this object lives."""
 
     def __init__(self, nml: Namelist):
         self.lib = load_library()

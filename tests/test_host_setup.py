@@ -61,11 +61,12 @@ def test_background_is_hydrostatic_and_periodic(hills):
 
 
 def test_random_hills_are_seeded_and_bounded():
-    a = L.HostModel(cases.small_case("hills")).surface["oro"].copy()
-    b = L.HostModel(cases.small_case("hills")).surface["oro"].copy()
+    # the arrays are views into each model's memory: keep the models alive while reading them
+    ma, mb = L.HostModel(cases.small_case("hills")), L.HostModel(cases.small_case("hills"))
+    a, b = ma.surface["oro"], mb.surface["oro"]
     np.testing.assert_array_equal(a, b)
-    c = L.HostModel(cases.namelist(cases.SMALL["hills"][0], **{**cases.SMALL["hills"][1], "seed": 99})).surface["oro"]
-    assert not np.array_equal(a, c)
+    mc = L.HostModel(cases.namelist(cases.SMALL["hills"][0], **{**cases.SMALL["hills"][1], "seed": 99}))
+    assert not np.array_equal(a, mc.surface["oro"])
     assert a.min() >= 0 and a.max() > 100
 
 
