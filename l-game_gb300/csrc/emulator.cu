@@ -6,8 +6,10 @@
 // shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core
 // matrices: element (r, k) at (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes), one
 // elected thread issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and
-// an FP32 accumulator in BN columns of tensor memory) and commits them to an mbarrier; the
-// block waits on it (bounded) before the tiles are overwritten.  The epilogue reads the
+// an FP32 accumulator in BN columns of tensor memory) and commits them to the stage's
+// mbarrier.  Three stages filled with cp.async: while the tensor core works on one K block
+// the copies of the next two are in flight; a stage is refilled only after the commit of the
+// MMAs that read it (bounded wait).  The epilogue reads the
 // accumulator with tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31 = tile rows) and
 // applies one of the fused epilogues (bias + GELU with BF16 and transposed BF16 copies,
 // bias only, GELU derivative for the backward pass, or plain FP32 partial sums for split-K).
@@ -113,61 +115,97 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 // ---- the GEMM -------------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+constexpr int kStages = 3;
+
 template <int BN>
 __global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
                                                  int ldb, int M, int N, int K, int kchunk, Epi ep, int* err) {
   constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;
+  constexpr int kStage = 128 * 64 * 2 + BN * 64 * 2;  // A tile (16 KB) + B tile per stage
   extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t mbar;
+  __shared__ uint64_t mbar[kStages];
   __shared__ uint32_t tmem_base;
-  uint8_t* sA = smem;                  // 128 x 64 BF16 = 16 KB
-  uint8_t* sB = smem + 128 * 64 * 2;   // BN x 64 BF16
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * 128;
   const int k0 = blockIdx.z * kchunk, k1 = min(K, k0 + kchunk);
-  const uint32_t mb = smem_u32(&mbar);
+  const int nk = (k1 - k0 + 63) / 64;
+  const uint32_t sbase = smem_u32(smem);
   if (warp == 0) tc_alloc(smem_u32(&tmem_base), kCols);
-  if (tid == 0) mbar_init(mb, 1);
+  if (tid == 0)
+    for (int i = 0; i < kStages; ++i) mbar_init(smem_u32(&mbar[i]), 1);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
   const uint32_t idesc = instr_desc(128, BN);
-  const uint32_t aS = smem_u32(sA), bS = smem_u32(sB);
-  uint32_t phase = 0;
-  bool failed = false;
-  for (int kb = k0; kb < k1; kb += 64) {
-    // stage the tiles: 16-byte chunks (8 elements) into core-matrix order
+  // asynchronous copies of K block kb into stage st, in core-matrix order
+  auto load = [&](int kb, int st) {
+    const uint32_t a = sbase + st * kStage, b = a + 128 * 64 * 2;
     for (int c = tid; c < 128 * 8; c += 128) {
       const int r = c >> 3, kc = c & 7;
-      const uint4 v = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + kb + kc * 8);
-      *reinterpret_cast<uint4*>(sA + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = v;
+      cp_async16(a + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, A + (size_t)(m0 + r) * lda + kb + kc * 8);
     }
     for (int c = tid; c < BN * 8; c += 128) {
       const int r = c >> 3, kc = c & 7;
-      const uint4 v = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + kb + kc * 8);
-      *reinterpret_cast<uint4*>(sB + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16) = v;
+      cp_async16(b + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, B + (size_t)(n0 + r) * ldb + kb + kc * 8);
     }
+  };
+  uint32_t ph[kStages] = {};
+  bool failed = false;
+  // prologue: the first kStages-1 blocks in flight (one copy group per block, empty ones too)
+  for (int i = 0; i < kStages - 1; ++i) {
+    if (i < nk) load(k0 + 64 * i, i);
+    cp_async_commit();
+  }
+  int it = 0;
+  for (; it < nk; ++it) {
+    const int st = it % kStages;
+    // refill the stage of block it-1 with block it+kStages-1 once its MMAs have finished
+    const int nxt = it + kStages - 1;
+    if (it >= 1 && nxt < nk) {
+      const int sp = (it - 1) % kStages;
+      const bool ok = mbar_wait(smem_u32(&mbar[sp]), ph[sp]);
+      if (__syncthreads_or(!ok)) { failed = true; break; }  // ph[sp] still names the pending phase
+      ph[sp] ^= 1u;
+    }
+    if (nxt < nk) load(k0 + 64 * nxt, nxt % kStages);
+    cp_async_commit();
+    cp_async_wait<kStages - 1>();  // block it has landed
     fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc_fence_after();
+      const uint32_t aS = sbase + st * kStage, bS = aS + 128 * 64 * 2;
 #pragma unroll
       for (int s = 0; s < 4; ++s) {  // K = 16 per instruction: two core matrices along K
         const uint64_t ad = smem_desc(aS + s * 256, 128, 1024);
         const uint64_t bd = smem_desc(bS + s * 256, 128, 1024);
-        tc_mma(tmem, ad, bd, idesc, (kb > k0 || s > 0) ? 1u : 0u);
+        tc_mma(tmem, ad, bd, idesc, (it > 0 || s > 0) ? 1u : 0u);
       }
-      tc_commit(mb);
+      tc_commit(smem_u32(&mbar[st]));
     }
-    const bool ok = mbar_wait(mb, phase);
-    phase ^= 1u;
-    if (__syncthreads_or(!ok)) { failed = true; break; }
+  }
+  cp_async_wait<0>();
+  // the last commit completes after every earlier tensor-core operation of this thread;
+  // its phase: the number of earlier waits on that stage (all earlier uses were waited on)
+  const int last = it - 1;
+  if (last >= 0) {
+    const int st = last % kStages;
+    const bool ok = mbar_wait(smem_u32(&mbar[st]), ph[st]);
+    if (__syncthreads_or(!ok)) failed = true;
   }
   tc_fence_after();
   if (failed) {
     if (tid == 0) atomicExch(err, 1);
-    mbar_wait(mb, phase ^ 1u);  // bounded: let this block's tensor-core work drain
+    // bounded: let this block's last committed tensor-core work drain before the memory is freed
+    if (it > 0) mbar_wait(smem_u32(&mbar[(it - 1) % kStages]), ph[(it - 1) % kStages]);
   } else {
     const int m = m0 + warp * 32 + lane;  // tile row of this thread
     for (int c = 0; c < BN; c += 16) {
@@ -226,7 +264,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int
 template <int BN>
 int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
                    int* err, cudaStream_t st) {
-  const size_t shm = (size_t)128 * 64 * 2 + (size_t)BN * 64 * 2;
+  const size_t shm = kStages * ((size_t)128 * 64 * 2 + (size_t)BN * 64 * 2);
   static bool attr_set = false;
   if (!attr_set) {
     if (cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
@@ -242,10 +280,21 @@ int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N,
 int launch_gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
                 int* err, cudaStream_t st) {
   if (M % 128 || K % 64 || N % 64 || splits < 1) return LGAME_ERR_INVALID_ARG;
-  if (N % 256 == 0) return launch_gemm_bn<256>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
-  if (N % 192 == 0) return launch_gemm_bn<192>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
-  if (N % 128 == 0) return launch_gemm_bn<128>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
-  return launch_gemm_bn<64>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+  // the widest tile that still gives at least one CTA per SM (152), else the narrowest
+  const long long tiles_m = (long long)(M / 128) * splits;
+  const int cand[4] = {256, 192, 128, 64};
+  int bn = 0;
+  for (int c : cand)
+    if (N % c == 0 && tiles_m * (N / c) >= 152) { bn = c; break; }
+  if (!bn)
+    for (int c : {64, 128, 192, 256})
+      if (N % c == 0) { bn = c; break; }
+  switch (bn) {
+    case 256: return launch_gemm_bn<256>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+    case 192: return launch_gemm_bn<192>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+    case 128: return launch_gemm_bn<128>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+    default: return launch_gemm_bn<64>(A, lda, B, ldb, M, N, K, splits, ep, err, st);
+  }
 }
 
 // ---- element-wise and reduction kernels ------------------------------------------------------
@@ -364,6 +413,11 @@ __global__ void k_gather_rows(const float* src, const long long* idx, int batch,
   if (i >= (long long)batch * ncol) return;
   const long long r = i / ncol, c = i % ncol;
   dst[i] = src[idx[r] * ncol + c];
+}
+
+__global__ void k_fill_pattern(bf16* a, long long n, int salt) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) a[i] = __float2bfloat16_rn((float)((i * 2654435761LL + salt) % 2001 - 1000) * 1e-3f);
 }
 
 inline unsigned blocks(long long n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -898,4 +952,44 @@ extern "C" int lgame_emu_stats(lgame_emu* e, long long* launches, double* flop) 
   e->gemm_launches = 0;
   e->gemm_flop = 0.0;
   return LGAME_OK;
+}
+
+extern "C" int lgame_emu_time_gemm(lgame_emu* e, int m, int n, int k, int reps, double* ms) {
+  if (!e || !ms || m <= 0 || n <= 0 || k <= 0 || m % 128 || k % 64 || n % 64 || reps < 1)
+    return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_time_gemm: bad arguments");
+  bf16 *da = nullptr, *db = nullptr;
+  float* dc = nullptr;
+  cudaEvent_t a0 = nullptr, a1 = nullptr;
+  int rc = LGAME_OK;
+  if (cudaMalloc(&da, sizeof(bf16) * (size_t)m * k) != cudaSuccess || cudaMalloc(&db, sizeof(bf16) * (size_t)n * k) != cudaSuccess ||
+      cudaMalloc(&dc, sizeof(float) * (size_t)m * n) != cudaSuccess || cudaEventCreate(&a0) != cudaSuccess ||
+      cudaEventCreate(&a1) != cudaSuccess)
+    rc = emu_fail(LGAME_ERR_ALLOC, "lgame_emu_time_gemm: allocation failed");
+  if (!rc) {
+    k_fill_pattern<<<blocks((long long)m * k), 256, 0, e->st>>>(da, (long long)m * k, 1);
+    k_fill_pattern<<<blocks((long long)n * k), 256, 0, e->st>>>(db, (long long)n * k, 7);
+    Epi ep{};
+    ep.kind = kEpiF32;
+    ep.c = dc;
+    ep.ldc = n;
+    rc = gemm(e, da, k, db, k, m, n, k, 1, ep);
+    if (!rc) cudaEventRecord(a0, e->st);
+    for (int r = 0; r < reps && !rc; ++r) rc = gemm(e, da, k, db, k, m, n, k, 1, ep);
+    if (!rc) {
+      cudaEventRecord(a1, e->st);
+      if (cudaEventSynchronize(a1) != cudaSuccess) rc = emu_fail(LGAME_ERR_CUDA, "lgame_emu_time_gemm: kernel failed");
+    }
+    if (!rc) rc = check_err(e);
+    if (!rc) {
+      float t = 0.f;
+      cudaEventElapsedTime(&t, a0, a1);
+      *ms = t / reps;
+    }
+  }
+  if (a0) cudaEventDestroy(a0);
+  if (a1) cudaEventDestroy(a1);
+  cudaFree(da);
+  cudaFree(db);
+  cudaFree(dc);
+  return rc;
 }

@@ -33,14 +33,26 @@ struct GridX {  // FP64 reciprocal metrics and FP32 metric differences of the FP
   const float *inv_volume_f, *inv_area_z_f, *dzs_f, *deb_f;
 };
 
+// Exact FP32 -> FP64 widening in integer operations: the exponent is rebiased (127 -> 1023)
+// and the 23 mantissa bits shifted into place.  Zero keeps its sign; subnormals, infinities
+// and NaN take the hardware conversion.  On this GPU the hardware conversion issues on the
+// FP64 pipe (~2 per clock per SM); these integer operations issue on the integer pipes.
+__device__ __forceinline__ double wide(float f) {
+  const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+  if (a - 0x00800000u < 0x7F000000u)  // normal numbers
+    return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(a << 29));
+  if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return (double)f;
+}
+
 // x / d to FP64 accuracy for an FP32 divisor d in the normal range: the correctly rounded
 // FP32 reciprocal (relative error <= 2^-24) and one correction of the quotient in FP64,
 // which leaves a relative error of ~2^-48.  Five FP64-pipe operations instead of a
 // conversion and an FP64 division (about eight).
 __device__ __forceinline__ double div_f(double x, float d) {
-  const double r = (double)__frcp_rn(d);
+  const double r = wide(__frcp_rn(d));
   const double q0 = x * r;
-  return fma(fma(-q0, (double)d, x), r, q0);
+  return fma(fma(-q0, wide(d), x), r, q0);
 }
 
 }  // namespace
@@ -158,12 +170,12 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
       const long long qr = IX(D, ji, kk, jl);
       double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
       if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : (double)tvu[qr];
-      const double de = (double)(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
+      const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : wide(tvu[qr]);
+      const double de = wide(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
       const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : (double)tpu[qr];
+        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : wide(tpu[qr]);
         lv = de * (tp * G.egu[qr]);
         P.l_u[q] = lv;
       }
@@ -183,12 +195,12 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
       const long long qr = IX(D, ii, jk, jl);
       double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
       if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : (double)tvv[qr];
-      const double de = (double)(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
+      const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : wide(tvv[qr]);
+      const double de = wide(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
       const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : (double)tpv[qr];
+        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : wide(tpv[qr]);
         lv = de * (tp * G.egv[qr]);
         P.l_v[q] = lv;
       }
@@ -201,7 +213,7 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
   if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl), qa = IX(D, ji, jk, jl - 1);
     const float fa = cond_frac(qa), fb = cond_frac(q);
-    const double de = (double)(0.5f * ((float(kC_D_P) - float(kC_D_P) * fa) + (float(kC_D_P) - float(kC_D_P) * fb)));
+    const double de = wide(0.5f * ((float(kC_D_P) - float(kC_D_P) * fa) + (float(kC_D_P) - float(kC_D_P) * fb)));
     P.nl_w[q] = de * (0.5 * (theta(ji, jk, jl - 1) + theta(ji, jk, jl)) * gzp(ji, jk, jl));
     if (D.luse_bg) P.l_w[q] = de * (0.5 * (S.tp[qa] + S.tp[q]) * G.egw[q]);
     pgcw[q] = 0.5f * (-fa - fb) * float(G.gm[q]);
@@ -260,9 +272,10 @@ __global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_ne
 
 // divergences of the gas and theta_v fluxes and the diabatic rho*theta_v term,
 // mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1)
-__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* fu, const float* fv, const float* gu,
-                           const float* gv, const float* Tm, const float* rad, const float* csh, float* t_rho,
-                           float* t_rt) {
+__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* __restrict__ fu,
+                           const float* __restrict__ fv, const float* __restrict__ gu, const float* __restrict__ gv,
+                           const float* __restrict__ Tm, const float* __restrict__ rad, const float* __restrict__ csh,
+                           float* __restrict__ t_rho, float* __restrict__ t_rt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -335,8 +348,8 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
   auto predict = [&](int jl, const Lay& L, double* tpe, double* epe, float* rhe) {
     const long long i = IX(D, ji, jk, jl);
     const float tr = Tn.rho[goff + i], trt = Tn.rt[i];
-    *tpe = So.tp[i] + (double)(dtf * (L.a * tr + L.b * trt));
-    *epe = So.ep[i] + (double)(dtf * L.g * trt);
+    *tpe = So.tp[i] + wide(dtf * (L.a * tr + L.b * trt));
+    *epe = So.ep[i] + wide(dtf * L.g * trt);
     *rhe = L.ro + dtf * tr;
   };
 
@@ -366,10 +379,10 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const float dv = -(ti * ti) * (ga0 + ga1) + 0.5f * deb * (al1 - al0 + ti * (be1 - be0))
                      - dz * ic2 * irio * (2.f * X.inv_area_z_f[ib] + dtf * wof * 0.5f * (L1.iv - L0.iv)) * dp;
     const float rie = 0.5f * (rhe0 + rhe1);
-    double rv = (wo + (double)(dtf * Tn.w[ib])) * (double)(-dz * ic2);
-    rv = fma(D.luse_bg ? (double)(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
-    rv = fma((double)(0.5f * idtf * deb), tpe0 + tpe1, rv);
-    rv = fma((double)(-dz * ic2 * rie * irio), wo, rv);
+    double rv = (wo + wide(dtf * Tn.w[ib])) * wide(-dz * ic2);
+    rv = fma(D.luse_bg ? wide(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
+    rv = fma(wide(0.5f * idtf * deb), tpe0 + tpe1, rv);
+    rv = fma(wide(-dz * ic2 * rie * irio), wo, rv);
     // couplings with row jl+1 (layer b's derivatives), which need layer jl+2
     float cv = 0.f, ev = 0.f;
     if (jl < n) {
@@ -383,7 +396,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
       ev = ti * ga1 * ti_n - 0.5f * deb * (al1 + be1 * ti_n) + dz * ic1 * 0.5f * wof * L1.iv * irio * dp;
     }
     const float piv = dv - epr_prev * cv_prev;
-    const double x = (jl == 1) ? rv : fma(-(double)cv_prev, rpr_prev, rv);
+    const double x = (jl == 1) ? rv : fma(-wide(cv_prev), rpr_prev, rv);
     rpr_prev = div_f(x, piv);
     rpr[jl] = rpr_prev;
     epr_prev = ev / piv;
@@ -395,7 +408,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
   }
   double s = rpr[n];
   for (int jl = n - 1; jl >= 1; --jl) {
-    s = fma(-(double)epr[jl], s, rpr[jl]);
+    s = fma(-wide(epr[jl]), s, rpr[jl]);
     rpr[jl] = s;
   }
   // new state, mo_column_solvers.F90:300-345
@@ -406,19 +419,19 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const double s1 = (jl <= n) ? rpr[jl] : 0.0;
     const float t0 = (jl >= 2) ? tis[jl - 1] : 0.f;
     const float t1 = (jl <= n) ? tis[jl] : 0.f;
-    const double dtv = (double)(dtf * X.inv_volume_f[i]);
+    const double dtv = wide(dtf * X.inv_volume_f[i]);
     const double rto = So.rt[i];
-    const double rho_e = So.rho[goff + i] + (double)(dtf * Tn.rho[goff + i]);
-    const double rt_e = rto + (double)(dtf * Tn.rt[i]);
+    const double rho_e = So.rho[goff + i] + wide(dtf * Tn.rho[goff + i]);
+    const double rt_e = rto + wide(dtf * Tn.rt[i]);
     const double rn = fma(dtv, s1 - s0, rho_e);
-    const double rtn = fma(dtv, fma(-(double)t0, s0, (double)t1 * s1), rt_e);
-    const double epn = fma((double)gs[jl], rtn - rto, So.ep[i]);
+    const double rtn = fma(dtv, fma(-wide(t0), s0, wide(t1) * s1), rt_e);
+    const double epn = fma(wide(gs[jl]), rtn - rto, So.ep[i]);
     const float rnf = (float)rn;
     const float tpf = (float)fma(-G.theta_v_bg[i], rn, rtn) / rnf;
     Sn.rho[goff + i] = rn;
     Sn.rt[i] = rtn;
     Sn.ep[i] = epn;
-    Sn.tp[i] = (double)tpf;
+    Sn.tp[i] = wide(tpf);
     Mn.rho[goff + i] = rnf;
     Mn.rt[i] = (float)rtn;
     Mn.ep[i] = (float)epn;
@@ -427,7 +440,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
       const float rin = 0.5f * (rn_prev + rnf);
       const float irio = 2.f / (Mo.rho[goff + IX(D, ji, jk, jl - 1)] + Mo.rho[goff + i]);
       const double wo = So.w[i];
-      const double wn = fma(-(double)rin, wo, (double)(2.f * X.inv_area_z_f[i]) * s0) * (double)irio;
+      const double wn = fma(-wide(rin), wo, wide(2.f * X.inv_area_z_f[i]) * s0) * wide(irio);
       Sn.w[i] = wn;
       Mn.w[i] = (float)wn;
     }
@@ -557,8 +570,8 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
       const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
       // forward substitution in FP64 (the pivot equals d: one of e, c of an interface is 0)
       const float piv = d - epr_prev * cv_prev;
-      double x = rho_o[i] + (double)(dt * t_rho[i] + fl);
-      if (cv_prev != 0.f) x = fma(-(double)cv_prev, rpr_prev, x);
+      double x = rho_o[i] + wide(dt * t_rho[i] + fl);
+      if (cv_prev != 0.f) x = fma(-wide(cv_prev), rpr_prev, x);
       rpr_prev = div_f(x, piv);
       rpr[jl] = rpr_prev;
       epr_prev = ev / piv;
@@ -569,7 +582,7 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
     // back substitution; negative densities are clipped on output (mo_column_solvers.F90:587-591)
     double s = rpr[nl];
     for (int jl = nl; jl >= 1; --jl) {
-      if (jl < nl) s = (epr[jl] != 0.f) ? fma(-(double)epr[jl], s, rpr[jl]) : rpr[jl];
+      if (jl < nl) s = (epr[jl] != 0.f) ? fma(-wide(epr[jl]), s, rpr[jl]) : rpr[jl];
       const double o = s < 0.0 ? 0.0 : s;
       const long long i = IX(D, ji, jk, jl);
       rho_n[i] = o;

@@ -154,6 +154,7 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_emu_infer": (i, [vp, fp, ll, fp]),
         "lgame_emu_gemm_bf16": (i, [vp, C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), fp, i, i, i]),
         "lgame_emu_stats": (i, [vp, C.POINTER(ll), C.POINTER(d)]),
+        "lgame_emu_time_gemm": (i, [vp, i, i, i, i, C.POINTER(d)]),
         "lgame_gpu_rad_set_surface": (i, [vp, C.POINTER(d), C.POINTER(d), C.POINTER(d)]),
         "lgame_gpu_rad_features": (i, [vp, i, d, fp]),
         "lgame_gpu_rad_apply_heating": (i, [vp, i, fp]),

@@ -138,6 +138,12 @@ class Emulator:
               "lgame_emu_gemm_bf16")
         return c
 
+    def time_gemm(self, m: int, n: int, k: int, reps: int = 20) -> float:
+        """Milliseconds per launch of the tensor-core GEMM (M x K by N x K, device data)."""
+        ms = C.c_double()
+        check(self.lib.lgame_emu_time_gemm(self.h, m, n, k, reps, C.byref(ms)), "lgame_emu_time_gemm")
+        return float(ms.value)
+
     def stats(self) -> tuple[int, float]:
         n, f = C.c_longlong(), C.c_double()
         check(self.lib.lgame_emu_stats(self.h, C.byref(n), C.byref(f)), "lgame_emu_stats")

@@ -56,11 +56,13 @@ SMALL = {
                                                         dy=6000.0, n_hills=6, hill_width_min=6000.0,
                                                         hill_width_max=15000.0, lperiodic=False, lfreeslip=False)),
     "jet": ("jet_1024x1024x80", dict(nx=20, ny=18, n_layers=24, n_oro_layers=18, dx=5000.0, dy=5000.0, n_hills=5,
+                                     hill_height_min=200.0, hill_height_max=1500.0,
                                      hill_width_min=8000.0, hill_width_max=20000.0)),
     "jet_plane": ("jet_1024x1024x80", dict(nx=15, ny=13, n_layers=20, n_oro_layers=14, dx=5000.0, dy=5000.0,
                                            lplane=True, orography_id=0, lcorio=False)),
     "jet_order2_nobg": ("jet_1024x1024x80", dict(nx=16, ny=15, n_layers=20, n_oro_layers=14, dx=5000.0, dy=5000.0,
-                                                 n_hills=4, hill_width_min=8000.0, hill_width_max=20000.0,
+                                                 n_hills=4, hill_height_min=200.0, hill_height_max=1500.0,
+                                                 hill_width_min=8000.0, hill_width_max=20000.0,
                                                  theta_adv_order=2, luse_bg_state=False, lklemp=False)),
 }
 
