@@ -212,44 +212,48 @@ __global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int
       float v[16];
       tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
       const int nb = n0 + c;
+      // row-major outputs as 16-byte vector stores (16 FP32 = 4 x float4, 16 BF16 = 2 x uint4);
+      // the transposed BF16 copies are written element-wise, coalesced across the warp's rows
       switch (ep.kind) {
-        case kEpiF32: {
-          float* out = ep.c + (size_t)blockIdx.z * ep.split_stride + (size_t)m * ep.ldc + nb;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) out[j] = v[j];
-          break;
-        }
+        case kEpiF32:
         case kEpiBias: {
-          float* out = ep.c + (size_t)m * ep.ldc + nb;
+          float4* out = reinterpret_cast<float4*>(ep.c + (ep.kind == kEpiF32 ? (size_t)blockIdx.z * ep.split_stride : 0) +
+                                                  (size_t)m * ep.ldc + nb);
+          if (ep.kind == kEpiBias)
 #pragma unroll
-          for (int j = 0; j < 16; ++j) out[j] = v[j] + ep.bias[nb + j];
+            for (int j = 0; j < 16; ++j) v[j] += ep.bias[nb + j];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
           break;
         }
-        case kEpiBiasGelu: {
-          float* z = ep.c + (size_t)m * ep.ldc + nb;
-          bf16* h = ep.h + (size_t)m * ep.ldh + nb;
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float zz = v[j] + ep.bias[nb + j];
-            z[j] = zz;
-            const bf16 g = __float2bfloat16_rn(gelu(zz));
-            h[j] = g;
-            ep.ht[(size_t)(nb + j) * ep.ldt + m] = g;
-          }
-          break;
-        }
+        case kEpiBiasGelu:
         case kEpiGeluBwd: {
-          const float* zp = ep.zprev + (size_t)m * ep.ldc + nb;
-          float* d32 = ep.c + (size_t)m * ep.ldc + nb;
-          bf16* h = ep.h + (size_t)m * ep.ldh + nb;
+          float z[16];
+          if (ep.kind == kEpiBiasGelu) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float d = v[j] * gelu_grad(zp[j]);
-            d32[j] = d;
-            const bf16 g = __float2bfloat16_rn(d);
-            h[j] = g;
-            ep.ht[(size_t)(nb + j) * ep.ldt + m] = g;
+            for (int j = 0; j < 16; ++j) z[j] = v[j] + ep.bias[nb + j];
+          } else {
+            const float4* zp = reinterpret_cast<const float4*>(ep.zprev + (size_t)m * ep.ldc + nb);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const float4 t = zp[q];
+              z[4 * q] = v[4 * q] * gelu_grad(t.x);
+              z[4 * q + 1] = v[4 * q + 1] * gelu_grad(t.y);
+              z[4 * q + 2] = v[4 * q + 2] * gelu_grad(t.z);
+              z[4 * q + 3] = v[4 * q + 3] * gelu_grad(t.w);
+            }
           }
+          float4* zo = reinterpret_cast<float4*>(ep.c + (size_t)m * ep.ldc + nb);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) zo[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
+          __align__(16) bf16 hb[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(ep.kind == kEpiBiasGelu ? gelu(z[j]) : z[j]);
+          uint4* ho = reinterpret_cast<uint4*>(ep.h + (size_t)m * ep.ldh + nb);
+          ho[0] = reinterpret_cast<const uint4*>(hb)[0];
+          ho[1] = reinterpret_cast<const uint4*>(hb)[1];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) ep.ht[(size_t)(nb + j) * ep.ldt + m] = hb[j];
           break;
         }
         default: break;

@@ -618,8 +618,8 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
 // with scalar_times_vector_h_upstream (mo_multiplications.F90:206-287) and div_h_tracers
 // (mo_divergence_operators.F90:70-147) evaluated inline.
 template <class T, class V = double>
-__global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* __restrict__ u_new, const V* __restrict__ v_new,
-                          T* __restrict__ t_rho, int rk_step) {
+__device__ __forceinline__ void tracers_body(const Dims& D, const Grid<T>& G, const StateT<V>& Ss, const V* u_new,
+                                             const V* v_new, T* t_rho, int rk_step) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -634,7 +634,7 @@ __global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* __restrict__
   const T old_weight = T(1) - new_weight;
   for (int jc = 1; jc <= D.ncons; ++jc) {
     if (jc == D.g) continue;
-    const V* __restrict__ r = Ss.rho + (long long)(jc - 1) * D.fstride;
+    const V* r = Ss.rho + (long long)(jc - 1) * D.fstride;
     auto fx = [&](int i, int j, int k) { T f; return upstream_x<T>(D, r, u_new, i, j, k, &f) ? f : T(0); };
     auto fy = [&](int i, int j, int k) { T f; return upstream_y<T>(D, r, v_new, i, j, k, &f) ? f : T(0); };
     const T comp_h = fx(ji, jk + 1, jl) * G.area_x[IX(D, ji, jk + 1, jl)]
@@ -657,6 +657,11 @@ __global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* __restrict__
     T* t = t_rho + (long long)(jc - 1) * D.fstride;
     t[q] = old_weight * t[q] + new_weight * (-div);
   }
+}
+
+template <class T, class V = double>
+__global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, T* t_rho, int rk_step) {
+  tracers_body<T, V>(D, G, Ss, u_new, v_new, t_rho, rk_step);
 }
 
 // scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177

@@ -272,10 +272,9 @@ __global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_ne
 
 // divergences of the gas and theta_v fluxes and the diabatic rho*theta_v term,
 // mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1)
-__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* __restrict__ fu,
-                           const float* __restrict__ fv, const float* __restrict__ gu, const float* __restrict__ gv,
-                           const float* __restrict__ Tm, const float* __restrict__ rad, const float* __restrict__ csh,
-                           float* __restrict__ t_rho, float* __restrict__ t_rt) {
+__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* fu, const float* fv, const float* gu,
+                           const float* gv, const float* Tm, const float* rad, const float* csh, float* t_rho,
+                           float* t_rt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -293,6 +292,13 @@ __global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* __res
         (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
   }
   t_rt[q] = -div_t + x;
+}
+
+// the tracer tendencies of the split step: the body of k_tracers with the register count
+// capped so that four blocks of 256 threads share an SM (the kernel waits on loads)
+__global__ void __launch_bounds__(256, 4) ks_tracers(Dims D, Grid<float> GF, StateF Ss, const float* u_new,
+                                                     const float* v_new, float* t_rho, int rk_step) {
+  tracers_body<float, float>(D, GF, Ss, u_new, v_new, t_rho, rk_step);
 }
 
 // ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
@@ -768,7 +774,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_tend_wind", k_tend_wind<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, rk, Mn.u, Mn.v);
     const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (D.ncons > 1)
-      SL("ks_tracers", (k_tracers<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, Mn.u, Mn.v, T.rho, rk);
+      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, Mn.u, Mn.v, T.rho, rk);
     if (D.theta_order == 3) {
       int rc = theta3f(Ms.tp, 0, Ms.u, Ms.v, s->tvu, s->tvv);
       if (rc) return rc;
