@@ -154,8 +154,11 @@ def kernel_bytes_per_cell(name: str, ncons: int, split: bool, f_oro: float) -> f
         # exner_bg, damping, dz, d(exner_bg), 1/volume, 1/area_z, 3 tendencies, 5 mirror values written
         "ks_column_ver": 11 * 8.0 + 19.5 * 4.0,
         # FP64: rho old and new per tracer; FP32: mirror old, tendency and mirror new per tracer,
-        # w old/new, rho_g, T, area_z, 1/volume, sediment heating r/w
-        "ks_column_tracers": 2 * ntr * 8.0 + (3 * ntr + 8) * 4.0,
+        # w old/new, rho_g, T, area_z, 1/volume, and one sediment-heating plane per condensate
+        # written in the first of the two launches of a step
+        "ks_column_tracers": 2 * ntr * 8.0 + (3 * ntr + 6 + 0.5 * max(ncons - 2, 0)) * 4.0,
+        # the condensate planes read, their sum written
+        "ks_csh_sum": (max(ncons - 2, 0) + 1) * 4.0,
         # FP64: exner', its vertical gradient, 1/dx, 1/dy, slopes, 2 weights, 3 background
         # gradients, gravity, 8 products written, 4 previous read; FP32: all rho (mirror),
         # 4 theta edges, pgcw

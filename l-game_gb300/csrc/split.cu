@@ -72,6 +72,8 @@ struct SplitCtx {
   double* gzd = nullptr;
   // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
   float *fu = nullptr, *fv = nullptr, *gu = nullptr, *gv = nullptr;
+  // sediment heating of each condensate (nc planes), summed into the carried csh
+  float* csh_part = nullptr;
   // FP32 mirrors of the two state slots
   StateF mir[2]{};
   SplitCarriedF C{};
@@ -483,17 +485,21 @@ __device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>
 }
 
 // ---- three_band_solver_gen_densities, mo_column_solvers.F90:353-604 ----------------------
-// One thread per column, one top-to-bottom sweep per tracer.  Fall speeds, vertical fluxes,
+// One thread per (column, tracer), one top-to-bottom sweep.  Fall speeds, vertical fluxes,
 // the implicit-upwind matrix and its multipliers in FP32 from the mirror; the explicit
 // prediction rho_old + dt*tendency and both substitution sweeps in FP64.  Each interface
 // couples its two cells in one direction only (the upwind side), so the pivots are the
-// diagonal entries themselves.
+// diagonal entries themselves.  The tracer is the fastest block index, so the blocks of one
+// column tile run together and share the column's w, temperature and volume reads through
+// L2.  A condensate's sediment heating goes to its own plane of csh_part (rk_step 1 only);
+// ks_csh_sum adds the planes in condensate order.
 __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
                                                          StateF Mo, StateF Mn, const float* t_rho_all,
-                                                         const float* Tm, float* csh, int rk_step) {
-  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  if (ji > D.ny || jk > D.nx) return;
+                                                         const float* Tm, float* csh_part, int rk_step) {
+  const int ji = blockIdx.y * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jc = (int)blockIdx.x + 1 + ((int)blockIdx.x + 1 >= D.g ? 1 : 0);
+  if (ji > D.ny || jk > D.nx || jc > D.ncons) return;
   const int nl = D.nl, NL = D.NL, nc = D.nc;
   const float dt = float(D.dtime);
   const float itw = 0.5f, ew = 0.5f;
@@ -501,100 +507,108 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
   const float az_sfc = GF.area_z[IX(D, ji, jk, NL)];
   float epr[kMaxL + 1];
   double rpr[kMaxL + 1];
-  if (rk_step == 1)
-    for (int jl = 1; jl <= nl; ++jl) csh[IX(D, ji, jk, jl)] = 0.f;
-  for (int jc = 1; jc <= D.ncons; ++jc) {
-    if (jc == D.g) continue;
-    const long long off = (long long)(jc - 1) * D.fstride;
-    const double* rho_o = So.rho + off;
-    const float* mro = Mo.rho + off;
-    double* rho_n = Sn.rho + off;
-    float* mrn = Mn.rho + off;
-    const float* t_rho = t_rho_all + off;
-    const bool ice = (jc - 1) % 2 == 0;
-    const bool cond = jc <= nc;
-    const bool heat = rk_step == 1 && cond;
-    // fall speeds: snow (radius 500 um above 250 um) 1 m/s, cloud ice 0.001 m/s, cloud water
-    // v_fall_liquid at radius 12 um, rain and graupel 0 (their radius is never set)
-    float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
-    const float vsurf = (jc == 1) ? 1.f : (jc == 3) ? 0.001f
-                      : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
-    float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
-    float itv_a = itw * dt * X.inv_volume_f[IX(D, ji, jk, 1)];
-    float epr_prev = 0.f, cv_prev = 0.f;
-    double rpr_prev = 0.0;
-    for (int jl = 1; jl <= nl; ++jl) {
-      const long long i = IX(D, ji, jk, jl);
-      const float iv = X.inv_volume_f[i];
-      // the interface below the cell (between jl and jl+1)
-      float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f;
-      if (jl <= nl - 1) {
-        const long long b = IX(D, ji, jk, jl + 1);
-        itv_b = itw * dt * X.inv_volume_f[b];
-        float vf = 0.f;
-        if (jc == 1) vf = 1.f;
-        else if (jc == 3) vf = 0.001f;
-        else if (jc == 4) {
-          const float vcl_b = vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, jl + 1);
-          vf = 0.5f * (vcl_a + vcl_b);
-          vcl_a = vcl_b;
-        }
-        const float az = GF.area_z[b];
-        vfi = az * (Mo.w[b] - vf);
-        float fr = az * (Mn.w[b] - vf);
-        fr = ((fr >= 0.f) ? mro[b] : mro[i]) * fr;
-        vfr = fr;
-        if (cond) vefv = (ice ? c_p_ice(Tm[b]) : c_p_water(Tm[b])) * Tm[b] * fr;
+  const long long off = (long long)(jc - 1) * D.fstride;
+  const double* rho_o = So.rho + off;
+  const float* mro = Mo.rho + off;
+  double* rho_n = Sn.rho + off;
+  float* mrn = Mn.rho + off;
+  const float* t_rho = t_rho_all + off;
+  float* csh = csh_part + off;  // condensates only: jc <= nc
+  const bool ice = (jc - 1) % 2 == 0;
+  const bool cond = jc <= nc;
+  const bool heat = rk_step == 1 && cond;
+  // fall speeds: snow (radius 500 um above 250 um) 1 m/s, cloud ice 0.001 m/s, cloud water
+  // v_fall_liquid at radius 12 um, rain and graupel 0 (their radius is never set)
+  float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
+  const float vsurf = (jc == 1) ? 1.f : (jc == 3) ? 0.001f
+                    : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
+  float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
+  float itv_a = itw * dt * X.inv_volume_f[IX(D, ji, jk, 1)];
+  float epr_prev = 0.f, cv_prev = 0.f;
+  double rpr_prev = 0.0;
+  for (int jl = 1; jl <= nl; ++jl) {
+    const long long i = IX(D, ji, jk, jl);
+    const float iv = X.inv_volume_f[i];
+    // the interface below the cell (between jl and jl+1)
+    float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f;
+    if (jl <= nl - 1) {
+      const long long b = IX(D, ji, jk, jl + 1);
+      itv_b = itw * dt * X.inv_volume_f[b];
+      float vf = 0.f;
+      if (jc == 1) vf = 1.f;
+      else if (jc == 3) vf = 0.001f;
+      else if (jc == 4) {
+        const float vcl_b = vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, jl + 1);
+        vf = 0.5f * (vcl_a + vcl_b);
+        vcl_a = vcl_b;
       }
-      // diagonal entry, explicit flux part and sediment heating of cell jl
-      float d, fl;
-      if (jl == 1) {
-        d = (vfi >= 0.f) ? 1.f : 1.f - itv_a * vfi;
-        fl = ew * dt * vfr * iv;
-        if (heat) csh[i] += vefv * iv;
-      } else if (jl == nl) {
-        d = (vfi_up >= 0.f) ? 1.f + itv_a * vfi_up : 1.f;
-        fl = -ew * dt * vfr_up * iv;
-        if (heat) csh[i] -= vefv_up * iv;
-        if (cond) {
-          d += itw * vsurf * dt * az_sfc * iv;
-          fl -= ew * vsurf * dt * mro[i] * az_sfc * iv;
-          if (jc > nc / 4 && rk_step == 1) {
-            const float Tn = Tm[i];
-            csh[i] -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * mro[i] * az_sfc * iv;
-          }
+      const float az = GF.area_z[b];
+      vfi = az * (Mo.w[b] - vf);
+      float fr = az * (Mn.w[b] - vf);
+      fr = ((fr >= 0.f) ? mro[b] : mro[i]) * fr;
+      vfr = fr;
+      if (cond) vefv = (ice ? c_p_ice(Tm[b]) : c_p_water(Tm[b])) * Tm[b] * fr;
+    }
+    // diagonal entry, explicit flux part and sediment heating of cell jl
+    float d, fl, h = 0.f;
+    if (jl == 1) {
+      d = (vfi >= 0.f) ? 1.f : 1.f - itv_a * vfi;
+      fl = ew * dt * vfr * iv;
+      h = vefv * iv;
+    } else if (jl == nl) {
+      d = (vfi_up >= 0.f) ? 1.f + itv_a * vfi_up : 1.f;
+      fl = -ew * dt * vfr_up * iv;
+      h = -vefv_up * iv;
+      if (cond) {
+        d += itw * vsurf * dt * az_sfc * iv;
+        fl -= ew * vsurf * dt * mro[i] * az_sfc * iv;
+        if (jc > nc / 4) {
+          const float Tn = Tm[i];
+          h -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * mro[i] * az_sfc * iv;
         }
-      } else {
-        d = 1.f;
-        if (vfi_up >= 0.f) d += itv_a * vfi_up;
-        if (vfi < 0.f) d -= itv_a * vfi;
-        fl = ew * dt * (vfr - vfr_up) * iv;
-        if (heat) csh[i] += (vefv - vefv_up) * iv;
       }
-      // couplings: row jl to jl+1 (upward flux below) and row jl+1 to jl (downward flux below)
-      const float ev = (jl <= nl - 1 && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
-      const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
-      // forward substitution in FP64 (the pivot equals d: one of e, c of an interface is 0)
-      const float piv = d - epr_prev * cv_prev;
-      double x = rho_o[i] + wide(dt * t_rho[i] + fl);
-      if (cv_prev != 0.f) x = fma(-wide(cv_prev), rpr_prev, x);
-      rpr_prev = div_f(x, piv);
-      rpr[jl] = rpr_prev;
-      epr_prev = ev / piv;
-      epr[jl] = epr_prev;
-      cv_prev = cv;
-      vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
+    } else {
+      d = 1.f;
+      if (vfi_up >= 0.f) d += itv_a * vfi_up;
+      if (vfi < 0.f) d -= itv_a * vfi;
+      fl = ew * dt * (vfr - vfr_up) * iv;
+      h = (vefv - vefv_up) * iv;
     }
-    // back substitution; negative densities are clipped on output (mo_column_solvers.F90:587-591)
-    double s = rpr[nl];
-    for (int jl = nl; jl >= 1; --jl) {
-      if (jl < nl) s = (epr[jl] != 0.f) ? fma(-wide(epr[jl]), s, rpr[jl]) : rpr[jl];
-      const double o = s < 0.0 ? 0.0 : s;
-      const long long i = IX(D, ji, jk, jl);
-      rho_n[i] = o;
-      mrn[i] = (float)o;
-    }
+    if (heat) csh[i] = h;
+    // couplings: row jl to jl+1 (upward flux below) and row jl+1 to jl (downward flux below)
+    const float ev = (jl <= nl - 1 && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
+    const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
+    // forward substitution in FP64 (the pivot equals d: one of e, c of an interface is 0)
+    const float piv = d - epr_prev * cv_prev;
+    double x = rho_o[i] + wide(dt * t_rho[i] + fl);
+    if (cv_prev != 0.f) x = fma(-wide(cv_prev), rpr_prev, x);
+    rpr_prev = div_f(x, piv);
+    rpr[jl] = rpr_prev;
+    epr_prev = ev / piv;
+    epr[jl] = epr_prev;
+    cv_prev = cv;
+    vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
   }
+  // back substitution; negative densities are clipped on output (mo_column_solvers.F90:587-591)
+  double s = rpr[nl];
+  for (int jl = nl; jl >= 1; --jl) {
+    if (jl < nl) s = (epr[jl] != 0.f) ? fma(-wide(epr[jl]), s, rpr[jl]) : rpr[jl];
+    const double o = s < 0.0 ? 0.0 : s;
+    const long long i = IX(D, ji, jk, jl);
+    rho_n[i] = o;
+    mrn[i] = (float)o;
+  }
+}
+
+// sediment heating of all condensates: the per-condensate planes of ks_column_tracers added
+// in condensate order (the order of the reference's accumulation over jc)
+__global__ void ks_csh_sum(Dims D, const float* csh_part, float* csh) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  float h = 0.f;
+  for (int jc = 0; jc < D.nc; ++jc) h += csh_part[q + (long long)jc * D.fstride];
+  csh[q] = h;
 }
 
 dim3 sblk() { return dim3(32, 8, 1); }
@@ -625,6 +639,7 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
   for (float** p : scratch) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->gzd, F, bytes))) return fail(rc);
+  if (D.nc > 0 && (rc = salloc(s, &s->csh_part, F * D.nc, bytes))) return fail(rc);
   float** fl[] = {&s->fu, &s->fv, &s->gu, &s->gv};
   for (float** p : fl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   for (int k = 0; k < 2; ++k) {
@@ -785,9 +800,13 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
        C.rad, C.csh, T.rho, T.rt);
     const dim3 gc = cgrd(D.ny, D.nx);
     SL("ks_column_ver", ks_column_ver, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
-    if (D.ncons > 1)
-      SL("ks_column_tracers", ks_column_tracers, gc, cblk(), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature,
-         C.csh, rk);
+    if (D.ncons > 1) {
+      const dim3 gt((unsigned)(D.ncons - 1), gc.x, gc.y);
+      SL("ks_column_tracers", ks_column_tracers, gt, cblk(), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature,
+         s->csh_part, rk);
+      if (rk == 1 && D.nc > 0)
+        SL("ks_csh_sum", ks_csh_sum, sgrd(D.ny, D.nx, D.nl), B, D, s->csh_part, C.csh);
+    }
   }
 #undef SL
   *nk = launches;
