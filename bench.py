@@ -390,7 +390,11 @@ def run_ours(args):
     ncons = n.n_constituents
     f_oro = (n.n_oro_layers + 1) / n.n_layers
     results = {}
-    precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64] if not args.fp64_only else [L.PRECISION_FP64]
+    precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64]
+    if args.fp64_only:
+        precisions = [L.PRECISION_FP64]
+    elif args.split_only:
+        precisions = [L.PRECISION_SPLIT]
     clocks = None
     for prec in precisions:
         cfg = L.config_from_namelist(n)
@@ -523,6 +527,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-only", action="store_true")
+    ap.add_argument("--split-only", action="store_true", help="measure the split step alone (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-emulator", action="store_true")
     ap.add_argument("--nx", type=int, default=0, help="override nx=ny (smaller runs for testing)")

@@ -28,7 +28,50 @@ struct Dims {
   int nc, ncons, g;         // condensates, constituents, gas index (1-based) = nc+1
   int periodic, freeslip, lcorio, llinear, luse_bg, lmoist, theta_order, lklemp;
   double dtime, toa, dxn, dyn;  // namelist dx, dy
+  double theta_edge_c;          // 1/8*dy*dx of the third-order theta edges, formed once on the host
 };
+
+// ---- FP32 <-> FP64 conversions in integer operations ------------------------------
+// On this GPU a hardware conversion between FP32 and FP64 issues on the FP64 pipe (about
+// two per clock per SM, against 128 FP32 operations), so the split-precision kernels,
+// which convert every value they move between the two precisions, do it with integer
+// operations.  Both give the hardware's results bit for bit.
+
+// FP32 -> FP64, exact: the exponent is rebiased (127 -> 1023) and the 23 mantissa bits
+// shifted into place.  Zero keeps its sign; subnormals, infinities and NaN take the
+// hardware conversion.
+__device__ __forceinline__ double wide(float f) {
+  const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
+  if (a - 0x00800000u < 0x7F000000u)  // normal numbers
+    return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(a << 29));
+  if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return (double)f;
+}
+
+// FP64 -> FP32, rounded to nearest (ties to even), for results in the normal FP32 range
+// (2^-126 <= |x| < 2^128): the top 23 of the 52 mantissa bits are kept and the 29 dropped
+// bits decide the rounding; a carry out of the mantissa moves into the exponent (up to
+// infinity, as the rounding requires).  Zero, FP32-subnormal results, overflow and NaN take
+// the hardware conversion.
+__device__ __forceinline__ float narrow(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned e = (hi >> 20) & 0x7FFu;
+  if (e - 897u < 254u) {
+    const unsigned m = ((hi & 0xFFFFFu) << 3) | (lo >> 29);
+    const unsigned f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+    const unsigned rest = lo & 0x1FFFFFFFu;
+    return __uint_as_float(f + ((rest + (m & 1u) + 0x0FFFFFFFu) >> 29));
+  }
+  return (float)x;
+}
+
+// conversion of a value of type S to type T (identity when the types agree)
+template <class T, class S>
+__device__ __forceinline__ T cvt(S x) {
+  if constexpr (sizeof(T) == 4 && sizeof(S) == 8) return narrow(x);
+  else if constexpr (sizeof(T) == 8 && sizeof(S) == 4) return wide(x);
+  else return T(x);
+}
 
 __host__ __device__ __forceinline__ long long IX(const Dims& d, int i, int j, int k) {
   return (long long)(i - 1) + (long long)d.P * ((long long)(j - 1) + (long long)d.NX1 * (long long)(k - 1));

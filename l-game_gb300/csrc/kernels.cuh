@@ -39,11 +39,11 @@ struct Carried {  // read-only view of the diagnostics combined into the wind te
 template <class T, class S>
 __device__ __forceinline__ bool grad_x_cov(const Dims& D, const Grid<T>& G, const S* s, int ji, int jk, int jl, T* r) {
   if (jk >= 2 && jk <= D.nx) {
-    *r = T(s[IX(D, ji, jk, jl)] - s[IX(D, ji, jk - 1, jl)]) / G.dx[IX(D, ji, jk, jl)];
+    *r = cvt<T>(s[IX(D, ji, jk, jl)] - s[IX(D, ji, jk - 1, jl)]) / G.dx[IX(D, ji, jk, jl)];
     return true;
   }
   if (!D.periodic) return false;
-  *r = T(s[IX(D, ji, 1, jl)] - s[IX(D, ji, D.nx, jl)]) / G.dx[IX(D, ji, 1, jl)];
+  *r = cvt<T>(s[IX(D, ji, 1, jl)] - s[IX(D, ji, D.nx, jl)]) / G.dx[IX(D, ji, 1, jl)];
   return true;
 }
 
@@ -51,11 +51,11 @@ __device__ __forceinline__ bool grad_x_cov(const Dims& D, const Grid<T>& G, cons
 template <class T, class S>
 __device__ __forceinline__ bool grad_y_cov(const Dims& D, const Grid<T>& G, const S* s, int ji, int jk, int jl, T* r) {
   if (ji >= 2 && ji <= D.ny) {
-    *r = T(s[IX(D, ji - 1, jk, jl)] - s[IX(D, ji, jk, jl)]) / G.dy[IX(D, ji, jk, jl)];
+    *r = cvt<T>(s[IX(D, ji - 1, jk, jl)] - s[IX(D, ji, jk, jl)]) / G.dy[IX(D, ji, jk, jl)];
     return true;
   }
   if (!D.periodic) return false;
-  *r = T(s[IX(D, D.ny, jk, jl)] - s[IX(D, 1, jk, jl)]) / G.dy[IX(D, 1, jk, jl)];
+  *r = cvt<T>(s[IX(D, D.ny, jk, jl)] - s[IX(D, 1, jk, jl)]) / G.dy[IX(D, 1, jk, jl)];
   return true;
 }
 
@@ -291,10 +291,10 @@ __device__ __forceinline__ T rho_avg_h(const Dims& D, const Grid<T>& G, const V*
   auto R = [&](int i, int k, int l) { return T(rho[IX(D, i, k, l)]); };
   if (jl == 1) {
     return T(0.5) * (R(ia, ka, jl)
-      + (T(D.toa) - zs[IX(D, ia, ka, jl)]) * (R(ia, ka, jl) - R(ia, ka, jl + 1))
+      + (cvt<T>(D.toa) - zs[IX(D, ia, ka, jl)]) * (R(ia, ka, jl) - R(ia, ka, jl + 1))
         / (zs[IX(D, ia, ka, jl)] - zs[IX(D, ia, ka, jl + 1)])
       + R(ib, kb, jl)
-      + (T(D.toa) - zs[IX(D, ib, kb, jl)]) * (R(ib, kb, jl) - R(ib, kb, jl + 1))
+      + (cvt<T>(D.toa) - zs[IX(D, ib, kb, jl)]) * (R(ib, kb, jl) - R(ib, kb, jl + 1))
         / (zs[IX(D, ib, kb, jl)] - zs[IX(D, ib, kb, jl + 1)]));
   }
   if (jl == D.NL) {
@@ -429,7 +429,7 @@ __global__ void k_grad_vert(Dims D, Grid<T> G, const S* s, T* rz) {
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const int jl = blockIdx.z + 2;
   if (ji > D.ny || jk > D.nx || jl > D.nl) return;
-  rz[IX(D, ji, jk, jl)] = T(s[IX(D, ji, jk, jl - 1)] - s[IX(D, ji, jk, jl)]) / G.dz[IX(D, ji, jk, jl)];
+  rz[IX(D, ji, jk, jl)] = cvt<T>(s[IX(D, ji, jk, jl - 1)] - s[IX(D, ji, jk, jl)]) / G.dz[IX(D, ji, jk, jl)];
 }
 
 // grad_hor, mo_gradient_operators.F90:17-63 + :85-130, u and v points of layer jl
@@ -467,7 +467,7 @@ template <class T, class V = double>
 __global__ void k_theta_edges(Dims D, Grid<T> G, const T* th, const T* Dv, const V* u, const V* v,
                               T* tvu, T* tvv) {
   LG_IDX3;
-  const T c = T(1.0 / 8.0 * D.dyn * D.dxn);
+  const T c = cvt<T>(D.theta_edge_c);
   if (ji <= D.ny && jk <= D.nx + 1) {
     T t;
     if (theta_edge_u<T>(D, th, Dv, u, c, ji, jk, jl, &t)) tvu[IX(D, ji, jk, jl)] = t;
@@ -589,28 +589,37 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
   // background state they are O(g) and cancel gravity), in the reference's operation order
   const double chw_d = 0.5 + kIMPL_THERMO_WEIGHT, ohw_d = 1.0 - (0.5 + kIMPL_THERMO_WEIGHT);
   const double cvw_d = 1.0 - kIMPL_THERMO_WEIGHT, no_bg_d = D.luse_bg ? 0.0 : 1.0;
+  // FP32 tendencies with a background state: the sum nl + l, where the two products cancel,
+  // is the only FP64 operation; the previous substep's value (already a net force) and that
+  // sum are rounded to FP32 and combined there, as the FP32 tendency is rounded anyway
+  constexpr bool f32 = sizeof(T) == 4;
+  const bool pg32 = f32 && D.luse_bg;
+  auto pg_h = [&](const double* old, const double* nl, const double* l, long long q) -> T {
+    if (pg32) return T(ohw_d) * cvt<T>(old[q]) - T(chw_d) * cvt<T>(nl[q] + l[q]);
+    return cvt<T>(ohw_d * old[q] - chw_d * (nl[q] + l[q]));
+  };
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
-    const double pg = ohw_d * C.old_u[q] - chw_d * (C.nl_u[q] + C.l_u[q]);
-    const T t = old_weight * Tn.u[q] + new_weight * (T(pg) - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
+    const T t = old_weight * Tn.u[q] + new_weight * (pg_h(C.old_u, C.nl_u, C.l_u, q) - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
     Tn.u[q] = t;
-    const double un = So.u[q] + D.dtime * double(t);
+    const double un = So.u[q] + D.dtime * cvt<double>(t);
     Sn.u[q] = un;
-    if (mu) mu[q] = float(un);
+    if (mu) mu[q] = narrow(un);
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    const double pg = ohw_d * C.old_v[q] - chw_d * (C.nl_v[q] + C.l_v[q]);
-    const T t = old_weight * Tn.v[q] + new_weight * (T(pg) - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
+    const T t = old_weight * Tn.v[q] + new_weight * (pg_h(C.old_v, C.nl_v, C.l_v, q) - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
     Tn.v[q] = t;
-    const double vn = So.v[q] + D.dtime * double(t);
+    const double vn = So.v[q] + D.dtime * cvt<double>(t);
     Sn.v[q] = vn;
-    if (mv) mv[q] = float(vn);
+    if (mv) mv[q] = narrow(vn);
   }
   if (jl <= D.NL && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    const double pg = -(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q];
-    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (T(pg) - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+    T pg;
+    if (pg32) pg = -(T(cvw_d) * cvt<T>(C.nl_w[q] + C.l_w[q]));
+    else pg = cvt<T>(-(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q]);
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (pg - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
   }
 }
 

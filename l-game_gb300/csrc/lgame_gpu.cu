@@ -414,6 +414,7 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   D.periodic = cfg->lperiodic; D.freeslip = cfg->lfreeslip; D.lcorio = cfg->lcorio; D.llinear = cfg->llinear;
   D.luse_bg = cfg->luse_bg_state; D.lmoist = cfg->lmoist; D.theta_order = cfg->theta_adv_order; D.lklemp = cfg->lklemp;
   D.dtime = cfg->dtime; D.toa = cfg->toa; D.dxn = cfg->dx; D.dyn = cfg->dy;
+  D.theta_edge_c = 1.0 / 8.0 * D.dyn * D.dxn;  // the device expression, evaluated once
   auto fail = [&](int code) { lgame_gpu_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(LGAME_ERR_CUDA, "cudaStreamCreate failed"));

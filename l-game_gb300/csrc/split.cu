@@ -33,26 +33,15 @@ struct GridX {  // FP64 reciprocal metrics and FP32 metric differences of the FP
   const float *inv_volume_f, *inv_area_z_f, *dzs_f, *deb_f;
 };
 
-// Exact FP32 -> FP64 widening in integer operations: the exponent is rebiased (127 -> 1023)
-// and the 23 mantissa bits shifted into place.  Zero keeps its sign; subnormals, infinities
-// and NaN take the hardware conversion.  On this GPU the hardware conversion issues on the
-// FP64 pipe (~2 per clock per SM); these integer operations issue on the integer pipes.
-__device__ __forceinline__ double wide(float f) {
-  const unsigned u = __float_as_uint(f), a = u & 0x7FFFFFFFu;
-  if (a - 0x00800000u < 0x7F000000u)  // normal numbers
-    return __hiloint2double((int)((u & 0x80000000u) | ((a >> 3) + (896u << 20))), (int)(a << 29));
-  if (a == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-  return (double)f;
-}
-
-// x / d to FP64 accuracy for an FP32 divisor d in the normal range: the correctly rounded
-// FP32 reciprocal (relative error <= 2^-24) and one correction of the quotient in FP64,
-// which leaves a relative error of ~2^-48.  Five FP64-pipe operations instead of a
-// conversion and an FP64 division (about eight).
+// x / d to FP64 accuracy for an FP32 divisor d in the normal range.  r = 1/d correctly
+// rounded in FP32; the residual 1 - d*r of a correctly rounded reciprocal is exact in FP32,
+// so r + (1 - d*r)*r is 1/d to ~2^-48 as an unevaluated pair of FP32 numbers (the
+// correction step of Markstein's division), and x*(r + r_lo) costs two FP64-pipe operations
+// (relative error below 2^-47) instead of a conversion and an FP64 division.
 __device__ __forceinline__ double div_f(double x, float d) {
-  const double r = wide(__frcp_rn(d));
-  const double q0 = x * r;
-  return fma(fma(-q0, wide(d), x), r, q0);
+  const float r = __frcp_rn(d);
+  const float r_lo = __fmaf_rn(-d, r, 1.f) * r;
+  return fma(x, wide(r_lo), x * wide(r));
 }
 
 }  // namespace
@@ -131,7 +120,6 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
                          const float* tvu, const float* tvv, const float* tpu, const float* tpv, PGrad<double> P,
                          float* pgcw, int lfirst) {
   LG_IDX3;
-  const double ubs = D.luse_bg ? 1.0 : 0.0;
   const double* ep = S.ep;
   auto theta = [&](int i, int j, int k) { const long long q = IX(D, i, j, k); return G.theta_v_bg[q] + S.tp[q]; };
   // condensate mass fraction sum(rho_cond)/sum(rho): the reference's rho_g/sum(rho) and
@@ -166,50 +154,54 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
     const long long q = IX(D, ji, jk, jl);
     const bool inner = jk >= 2 && jk <= D.nx;
     const double nl_prev = P.nl_u[q], l_prev = P.l_u[q];
-    if (!lfirst) P.old_u[q] = -nl_prev - ubs * l_prev;
+    if (!lfirst) P.old_u[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
     if (inner || D.periodic) {
       const int kk = inner ? jk : 1, ka = inner ? jk - 1 : D.nx;
       const long long qr = IX(D, ji, kk, jl);
       double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
       if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : wide(tvu[qr]);
-      const double de = wide(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
-      const double nlv = de * (te * g);
+      const float def = 0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl));
+      const double de = wide(def);
+      // third order: the edge theta is FP32, so decel*theta is formed in FP32 (one more
+      // FP32 rounding of an FP32 factor) and the FP64 gradient is multiplied once
+      const double nlv = (D.theta_order == 2) ? de * (0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) * g)
+                                              : wide(def * tvu[qr]) * g;
       double lv = l_prev;
       if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : wide(tpu[qr]);
-        lv = de * (tp * G.egu[qr]);
+        lv = (D.theta_order == 2) ? de * (0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) * G.egu[qr])
+                                  : wide(def * tpu[qr]) * G.egu[qr];
         P.l_u[q] = lv;
       }
       P.nl_u[q] = nlv;
-      if (lfirst) P.old_u[q] = -nlv - ubs * lv;
+      if (lfirst) P.old_u[q] = D.luse_bg ? -nlv - lv : -nlv;
     } else if (lfirst) {
-      P.old_u[q] = -nl_prev - ubs * l_prev;
+      P.old_u[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
     }
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
     const bool inner = ji >= 2 && ji <= D.ny;
     const double nl_prev = P.nl_v[q], l_prev = P.l_v[q];
-    if (!lfirst) P.old_v[q] = -nl_prev - ubs * l_prev;
+    if (!lfirst) P.old_v[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
     if (inner || D.periodic) {
       const int ii = inner ? ji : 1, ia = inner ? ji - 1 : D.ny;
       const long long qr = IX(D, ii, jk, jl);
       double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
       if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : wide(tvv[qr]);
-      const double de = wide(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
-      const double nlv = de * (te * g);
+      const float def = 0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl));
+      const double de = wide(def);
+      const double nlv = (D.theta_order == 2) ? de * (0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) * g)
+                                              : wide(def * tvv[qr]) * g;
       double lv = l_prev;
       if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : wide(tpv[qr]);
-        lv = de * (tp * G.egv[qr]);
+        lv = (D.theta_order == 2) ? de * (0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) * G.egv[qr])
+                                  : wide(def * tpv[qr]) * G.egv[qr];
         P.l_v[q] = lv;
       }
       P.nl_v[q] = nlv;
-      if (lfirst) P.old_v[q] = -nlv - ubs * lv;
+      if (lfirst) P.old_v[q] = D.luse_bg ? -nlv - lv : -nlv;
     } else if (lfirst) {
-      P.old_v[q] = -nl_prev - ubs * l_prev;
+      P.old_v[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
     }
   }
   if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
@@ -296,11 +288,90 @@ __global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* fu, c
   t_rt[q] = -div_t + x;
 }
 
-// the tracer tendencies of the split step: the body of k_tracers with the register count
-// capped so that four blocks of 256 threads share an SM (the kernel waits on loads)
-__global__ void __launch_bounds__(256, 4) ks_tracers(Dims D, Grid<float> GF, StateF Ss, const float* u_new,
+// scalar_tend_expl for the tracers, mo_scalar_tend_expl.F90:24-104 (upstream fluxes,
+// mo_scalar_tend_expl.F90:56-82; vertical upstream term with the contravariant correction,
+// mo_averaging.F90:16-54), split step.  The velocity through each of the six faces of the
+// cell, times the face area, and the index of the face's upwind cell are found once per
+// cell; the tracer loop then only loads densities at known addresses, and every tracer's
+// divergence is formed before the first tendency is stored, so no load waits on a velocity
+// or on an earlier store.  The first substep (new weight 1) does not read the old tendency.
+constexpr int kTracers = 6;  // moist: five condensates and water vapour (the gas has its own kernel)
+__global__ void __launch_bounds__(256, 4) ks_tracers(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* u_new,
                                                      const float* v_new, float* t_rho, int rk_step) {
-  tracers_body<float, float>(D, GF, Ss, u_new, v_new, t_rho, rk_step);
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  // horizontal faces: flux = rho(upwind cell) * velocity, 0 on a non-periodic boundary
+  auto face_x = [&](int kf, float* a, long long* up) {
+    int kk = kf, ka = kf - 1, kb = kf;
+    if (kf < 2 || kf > D.nx) {
+      if (!D.periodic) { *a = 0.f; *up = q; return; }
+      kk = 1; ka = D.nx; kb = 1;
+    }
+    const float u = u_new[IX(D, ji, kk, jl)];
+    *a = u * GF.area_x[IX(D, ji, kf, jl)];
+    *up = IX(D, ji, (u >= 0.f) ? ka : kb, jl);
+  };
+  auto face_y = [&](int i_f, float* a, long long* up) {
+    int ii = i_f, ia = i_f, ib = i_f - 1;
+    if (i_f < 2 || i_f > D.ny) {
+      if (!D.periodic) { *a = 0.f; *up = q; return; }
+      ii = 1; ia = 1; ib = D.ny;
+    }
+    const float v = v_new[IX(D, ii, jk, jl)];
+    *a = v * GF.area_y[IX(D, i_f, jk, jl)];
+    *up = IX(D, (v >= 0.f) ? ia : ib, jk, jl);
+  };
+  float a_e, a_n, a_w, a_s, a_u = 0.f, a_l = 0.f;
+  long long i_e, i_n, i_w, i_s, i_u = q, i_l = q;
+  face_x(jk + 1, &a_e, &i_e);
+  face_y(ji, &a_n, &i_n);
+  face_x(jk, &a_w, &i_w);
+  face_y(ji + 1, &a_s, &i_s);
+  // vertical faces: the contravariant vertical velocity correction at the upper (jl) and
+  // lower (jl+1) interface inside the terrain-following layers; the upwind cell by its sign
+  auto wx = [&](int i, int j, int k) { return u_new[IX(D, i, j, k)]; };
+  auto wy = [&](int i, int j, int k) { return v_new[IX(D, i, j, k)]; };
+  // (the top terrain-following layer nf has only its lower face, the lowest layer nl only
+  // its upper one, unless it is layer nf itself)
+  if (jl > D.nf) {
+    const float cu = vcc<float>(D, GF, wx, wy, ji, jk, jl);
+    a_u = cu * GF.area_z[IX(D, ji, jk, jl)];
+    i_u = (cu <= 0.f) ? IX(D, ji, jk, jl - 1) : q;
+  }
+  if (jl == D.nf || (jl > D.nf && jl < D.nl)) {
+    const float cl = vcc<float>(D, GF, wx, wy, ji, jk, jl + 1);
+    a_l = cl * GF.area_z[IX(D, ji, jk, jl + 1)];
+    i_l = (cl <= 0.f) ? q : IX(D, ji, jk, jl + 1);
+  }
+  const float iv = X.inv_volume_f[q];
+  float dv[kTracers];
+#pragma unroll
+  for (int t = 0; t < kTracers; ++t) {
+    const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+    const float* r = Ss.rho + (long long)(jc - 1) * D.fstride;
+    const float comp = r[i_e] * a_e + r[i_n] * a_n - r[i_w] * a_w - r[i_s] * a_s + r[i_u] * a_u - r[i_l] * a_l;
+    dv[t] = comp * iv;
+  }
+  if (rk_step == 1) {
+#pragma unroll
+    for (int t = 0; t < kTracers; ++t) {
+      const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+      t_rho[q + (long long)(jc - 1) * D.fstride] = -dv[t];
+    }
+  } else {
+    float o[kTracers];
+#pragma unroll
+    for (int t = 0; t < kTracers; ++t) {
+      const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+      o[t] = t_rho[q + (long long)(jc - 1) * D.fstride];
+    }
+#pragma unroll
+    for (int t = 0; t < kTracers; ++t) {
+      const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+      t_rho[q + (long long)(jc - 1) * D.fstride] = 0.5f * o[t] - 0.5f * dv[t];
+    }
+  }
 }
 
 // ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
@@ -387,10 +458,12 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const float dv = -(ti * ti) * (ga0 + ga1) + 0.5f * deb * (al1 - al0 + ti * (be1 - be0))
                      - dz * ic2 * irio * (2.f * X.inv_area_z_f[ib] + dtf * wof * 0.5f * (L1.iv - L0.iv)) * dp;
     const float rie = 0.5f * (rhe0 + rhe1);
-    double rv = (wo + wide(dtf * Tn.w[ib])) * wide(-dz * ic2);
+    // the two w terms, -dz*ic2*(w_old + dt*tend_w) and -dz*ic2*rie*irio*w_old, with their FP32
+    // coefficients combined (one FP64 multiply-add on w_old; the tendency increment is FP32)
+    const float cw = -dz * ic2;
+    double rv = fma(wide(cw + cw * rie * irio), wo, wide(cw * (dtf * Tn.w[ib])));
     rv = fma(D.luse_bg ? wide(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
     rv = fma(wide(0.5f * idtf * deb), tpe0 + tpe1, rv);
-    rv = fma(wide(-dz * ic2 * rie * irio), wo, rv);
     // couplings with row jl+1 (layer b's derivatives), which need layer jl+2
     float cv = 0.f, ev = 0.f;
     if (jl < n) {
@@ -432,25 +505,26 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const double rho_e = So.rho[goff + i] + wide(dtf * Tn.rho[goff + i]);
     const double rt_e = rto + wide(dtf * Tn.rt[i]);
     const double rn = fma(dtv, s1 - s0, rho_e);
-    const double rtn = fma(dtv, fma(-wide(t0), s0, wide(t1) * s1), rt_e);
+    const float dtvf = dtf * X.inv_volume_f[i];
+    const double rtn = fma(wide(dtvf * t1), s1, fma(-wide(dtvf * t0), s0, rt_e));
     const double epn = fma(wide(gs[jl]), rtn - rto, So.ep[i]);
-    const float rnf = (float)rn;
-    const float tpf = (float)fma(-G.theta_v_bg[i], rn, rtn) / rnf;
+    const float rnf = narrow(rn);
+    const float tpf = narrow(fma(-G.theta_v_bg[i], rn, rtn)) / rnf;
     Sn.rho[goff + i] = rn;
     Sn.rt[i] = rtn;
     Sn.ep[i] = epn;
     Sn.tp[i] = wide(tpf);
     Mn.rho[goff + i] = rnf;
-    Mn.rt[i] = (float)rtn;
-    Mn.ep[i] = (float)epn;
+    Mn.rt[i] = narrow(rtn);
+    Mn.ep[i] = narrow(epn);
     Mn.tp[i] = tpf;
     if (jl >= 2) {  // w at level jl from the increment at that level
       const float rin = 0.5f * (rn_prev + rnf);
       const float irio = 2.f / (Mo.rho[goff + IX(D, ji, jk, jl - 1)] + Mo.rho[goff + i]);
       const double wo = So.w[i];
-      const double wn = fma(-wide(rin), wo, wide(2.f * X.inv_area_z_f[i]) * s0) * wide(irio);
+      const double wn = fma(-wide(rin * irio), wo, wide(2.f * X.inv_area_z_f[i] * irio) * s0);
       Sn.w[i] = wn;
-      Mn.w[i] = (float)wn;
+      Mn.w[i] = narrow(wn);
     }
     rn_prev = rnf;
   }
@@ -462,7 +536,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
       + G.ipw[2][IX(D, ji, jk, m)] * Sn.u[IX(D, ji, jk, m)] * G.slope_x[IX(D, ji, jk, m)]
       + G.ipw[3][IX(D, ji, jk, m)] * Sn.v[IX(D, ji + 1, jk, m)] * G.slope_y[IX(D, ji + 1, jk, m)];
     Sn.w[IX(D, ji, jk, m + 1)] = wf;
-    Mn.w[IX(D, ji, jk, m + 1)] = (float)wf;
+    Mn.w[IX(D, ji, jk, m + 1)] = narrow(wf);
   }
 }
 
@@ -485,14 +559,20 @@ __device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>
 }
 
 // ---- three_band_solver_gen_densities, mo_column_solvers.F90:353-604 ----------------------
-// One thread per (column, tracer), one top-to-bottom sweep.  Fall speeds, vertical fluxes,
-// the implicit-upwind matrix and its multipliers in FP32 from the mirror; the explicit
-// prediction rho_old + dt*tendency and both substitution sweeps in FP64.  Each interface
-// couples its two cells in one direction only (the upwind side), so the pivots are the
-// diagonal entries themselves.  The tracer is the fastest block index, so the blocks of one
-// column tile run together and share the column's w, temperature and volume reads through
-// L2.  A condensate's sediment heating goes to its own plane of csh_part (rk_step 1 only);
-// ks_csh_sum adds the planes in condensate order.
+// One thread per (column, tracer), one top-to-bottom elimination and one bottom-to-top
+// substitution.  The reference's system  d_l s_l + e_l s_{l+1} + c_{l-1} s_{l-1} = rho_l + inc_l
+// (implicit-upwind vertical flux and sedimentation, inc = dt*tendency + explicit flux part)
+// is solved for the increment delta = s - rho_old:
+//   d_l delta_l + e_l delta_{l+1} + c_{l-1} delta_{l-1} = inc_l - (d_l - 1) rho_l - e_l rho_{l+1} - c_{l-1} rho_{l-1}
+// The coefficients are FP32 (fall speeds and fluxes from the mirror), and so are the right-hand
+// side and both substitutions, whose rounding errors are then relative to the flux terms (the
+// size of delta) and not to the density; the new density rho_old + delta is formed in FP64,
+// the one FP64 operation per cell.  d - 1 is accumulated on its own, so the diagonal's
+// rounding near 1 does not enter.  Each interface couples its two cells in one direction only
+// (the upwind side), so the pivots are the diagonal entries themselves.  The tracer is the
+// fastest block index, so the blocks of one column tile run together and share the column's
+// w, temperature and volume reads through L2.  A condensate's sediment heating goes to its own
+// plane of csh_part (rk_step 1 only); ks_csh_sum adds the planes in condensate order.
 __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
                                                          StateF Mo, StateF Mn, const float* t_rho_all,
                                                          const float* Tm, float* csh_part, int rk_step) {
@@ -505,8 +585,6 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
   const float itw = 0.5f, ew = 0.5f;
   const float* rho_g_o = Mo.rho + (long long)(D.g - 1) * D.fstride;
   const float az_sfc = GF.area_z[IX(D, ji, jk, NL)];
-  float epr[kMaxL + 1];
-  double rpr[kMaxL + 1];
   const long long off = (long long)(jc - 1) * D.fstride;
   const double* rho_o = So.rho + off;
   const float* mro = Mo.rho + off;
@@ -517,6 +595,8 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
   const bool ice = (jc - 1) % 2 == 0;
   const bool cond = jc <= nc;
   const bool heat = rk_step == 1 && cond;
+  float epr[kMaxL + 1];  // elimination multipliers
+  float rpr[kMaxL + 1];  // eliminated right-hand sides of the increment
   // fall speeds: snow (radius 500 um above 250 um) 1 m/s, cloud ice 0.001 m/s, cloud water
   // v_fall_liquid at radius 12 um, rain and graupel 0 (their radius is never set)
   float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
@@ -524,13 +604,13 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
                     : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
   float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
   float itv_a = itw * dt * X.inv_volume_f[IX(D, ji, jk, 1)];
-  float epr_prev = 0.f, cv_prev = 0.f;
-  double rpr_prev = 0.0;
+  float epr_prev = 0.f, cv_prev = 0.f, rpr_prev = 0.f;
+  float ro_up = 0.f, ro = mro[IX(D, ji, jk, 1)];  // mirror densities of the cells above and here
   for (int jl = 1; jl <= nl; ++jl) {
     const long long i = IX(D, ji, jk, jl);
     const float iv = X.inv_volume_f[i];
     // the interface below the cell (between jl and jl+1)
-    float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f;
+    float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f, ro_dn = 0.f;
     if (jl <= nl - 1) {
       const long long b = IX(D, ji, jk, jl + 1);
       itv_b = itw * dt * X.inv_volume_f[b];
@@ -543,34 +623,35 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
         vcl_a = vcl_b;
       }
       const float az = GF.area_z[b];
+      ro_dn = mro[b];
       vfi = az * (Mo.w[b] - vf);
       float fr = az * (Mn.w[b] - vf);
-      fr = ((fr >= 0.f) ? mro[b] : mro[i]) * fr;
+      fr = ((fr >= 0.f) ? ro_dn : ro) * fr;
       vfr = fr;
       if (cond) vefv = (ice ? c_p_ice(Tm[b]) : c_p_water(Tm[b])) * Tm[b] * fr;
     }
-    // diagonal entry, explicit flux part and sediment heating of cell jl
-    float d, fl, h = 0.f;
+    // d - 1, explicit flux part and sediment heating of cell jl
+    float dm1, fl, h = 0.f;
     if (jl == 1) {
-      d = (vfi >= 0.f) ? 1.f : 1.f - itv_a * vfi;
+      dm1 = (vfi >= 0.f) ? 0.f : -itv_a * vfi;
       fl = ew * dt * vfr * iv;
       h = vefv * iv;
     } else if (jl == nl) {
-      d = (vfi_up >= 0.f) ? 1.f + itv_a * vfi_up : 1.f;
+      dm1 = (vfi_up >= 0.f) ? itv_a * vfi_up : 0.f;
       fl = -ew * dt * vfr_up * iv;
       h = -vefv_up * iv;
       if (cond) {
-        d += itw * vsurf * dt * az_sfc * iv;
-        fl -= ew * vsurf * dt * mro[i] * az_sfc * iv;
+        dm1 += itw * vsurf * dt * az_sfc * iv;
+        fl -= ew * vsurf * dt * ro * az_sfc * iv;
         if (jc > nc / 4) {
           const float Tn = Tm[i];
-          h -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * mro[i] * az_sfc * iv;
+          h -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * ro * az_sfc * iv;
         }
       }
     } else {
-      d = 1.f;
-      if (vfi_up >= 0.f) d += itv_a * vfi_up;
-      if (vfi < 0.f) d -= itv_a * vfi;
+      dm1 = 0.f;
+      if (vfi_up >= 0.f) dm1 += itv_a * vfi_up;
+      if (vfi < 0.f) dm1 -= itv_a * vfi;
       fl = ew * dt * (vfr - vfr_up) * iv;
       h = (vefv - vefv_up) * iv;
     }
@@ -578,25 +659,28 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
     // couplings: row jl to jl+1 (upward flux below) and row jl+1 to jl (downward flux below)
     const float ev = (jl <= nl - 1 && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
     const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
-    // forward substitution in FP64 (the pivot equals d: one of e, c of an interface is 0)
-    const float piv = d - epr_prev * cv_prev;
-    double x = rho_o[i] + wide(dt * t_rho[i] + fl);
-    if (cv_prev != 0.f) x = fma(-wide(cv_prev), rpr_prev, x);
-    rpr_prev = div_f(x, piv);
+    // right-hand side of the increment and forward elimination (pivot = d: one of e, c of an
+    // interface is 0)
+    const float rhs = (dt * t_rho[i] + fl) - dm1 * ro - ev * ro_dn - cv_prev * ro_up;
+    const float piv = (1.f + dm1) - epr_prev * cv_prev;
+    rpr_prev = (rhs - cv_prev * rpr_prev) / piv;
     rpr[jl] = rpr_prev;
     epr_prev = ev / piv;
     epr[jl] = epr_prev;
     cv_prev = cv;
     vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
+    ro_up = ro; ro = ro_dn;
   }
-  // back substitution; negative densities are clipped on output (mo_column_solvers.F90:587-591)
-  double s = rpr[nl];
+  // back substitution; the new density rho_old + delta in FP64, negative densities clipped on
+  // output (mo_column_solvers.F90:587-591; the sign is read from the high word)
+  float dl = 0.f;
   for (int jl = nl; jl >= 1; --jl) {
-    if (jl < nl) s = (epr[jl] != 0.f) ? fma(-wide(epr[jl]), s, rpr[jl]) : rpr[jl];
-    const double o = s < 0.0 ? 0.0 : s;
+    dl = rpr[jl] - epr[jl] * dl;
     const long long i = IX(D, ji, jk, jl);
+    const double sn = rho_o[i] + wide(dl);
+    const double o = __double2hiint(sn) < 0 ? 0.0 : sn;
     rho_n[i] = o;
-    mrn[i] = (float)o;
+    mrn[i] = narrow(o);
   }
 }
 
@@ -622,6 +706,10 @@ dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsig
 }  // namespace
 
 int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
+  if (D.ncons > 1 && D.ncons != kTracers + 1) {
+    lgame_set_error("split precision: the tracer kernel is built for five condensates and water vapour");
+    return LGAME_ERR_UNSUPPORTED;
+  }
   auto* s = new SplitCtx();
   const size_t F = (size_t)D.fstride;
   int rc = LGAME_OK;
@@ -789,7 +877,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_tend_wind", k_tend_wind<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, rk, Mn.u, Mn.v);
     const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (D.ncons > 1)
-      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, Mn.u, Mn.v, T.rho, rk);
+      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk);
     if (D.theta_order == 3) {
       int rc = theta3f(Ms.tp, 0, Ms.u, Ms.v, s->tvu, s->tvv);
       if (rc) return rc;
