@@ -160,16 +160,16 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
       const long long qr = IX(D, ji, kk, jl);
       double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
       if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
-      const float def = 0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl));
-      const double de = wide(def);
-      // third order: the edge theta is FP32, so decel*theta is formed in FP32 (one more
-      // FP32 rounding of an FP32 factor) and the FP64 gradient is multiplied once
-      const double nlv = (D.theta_order == 2) ? de * (0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) * g)
-                                              : wide(def * tvu[qr]) * g;
+      // decel and the edge theta are FP32 values; their product with the gradient is FP64
+      // (an extra FP32 rounding of either product would unbalance the two terms, which
+      // cancel in an atmosphere at rest)
+      const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : wide(tvu[qr]);
+      const double de = wide(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
+      const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
-        lv = (D.theta_order == 2) ? de * (0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) * G.egu[qr])
-                                  : wide(def * tpu[qr]) * G.egu[qr];
+        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : wide(tpu[qr]);
+        lv = de * (tp * G.egu[qr]);
         P.l_u[q] = lv;
       }
       P.nl_u[q] = nlv;
@@ -188,14 +188,13 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
       const long long qr = IX(D, ii, jk, jl);
       double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
       if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
-      const float def = 0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl));
-      const double de = wide(def);
-      const double nlv = (D.theta_order == 2) ? de * (0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) * g)
-                                              : wide(def * tvv[qr]) * g;
+      const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : wide(tvv[qr]);
+      const double de = wide(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
+      const double nlv = de * (te * g);
       double lv = l_prev;
       if (D.luse_bg) {
-        lv = (D.theta_order == 2) ? de * (0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) * G.egv[qr])
-                                  : wide(def * tpv[qr]) * G.egv[qr];
+        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : wide(tpv[qr]);
+        lv = de * (tp * G.egv[qr]);
         P.l_v[q] = lv;
       }
       P.nl_v[q] = nlv;
@@ -264,28 +263,121 @@ __global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_ne
   }
 }
 
-// divergences of the gas and theta_v fluxes and the diabatic rho*theta_v term,
-// mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1)
-__global__ void ks_gas_div(Dims D, Grid<float> GF, StateF Ss, const float* fu, const float* fv, const float* gu,
-                           const float* gv, const float* Tm, const float* rad, const float* csh, float* t_rho,
-                           float* t_rt) {
-  LG_IDX3;
-  if (ji > D.ny || jk > D.nx) return;
+// ---- column-marching divergences -------------------------------------------------------
+// div_h with the contravariant vertical correction (div_h_at above: div_h,
+// mo_divergence_operators.F90:16-68, and vertical_contravariant_corr, mo_averaging.F90:16-54)
+// evaluated by one thread per column walking down the levels.  The correction at the
+// interface between layers l-1 and l is -(h(l-1) + h(l)), h(l) being half the slope-weighted
+// sum of layer l's four face values (only h(l) at the top interface of the terrain-following
+// layers, l = nf+1).  Each layer's faces are loaded once per column, each h once, and each
+// interface's correction serves the cells on both sides of it; the next layer's loads are
+// issued before the current layer's result is stored.
+
+// the four face values of layer l of column (ji, jk) -- x at the east (jk+1) and west (jk)
+// u points, y at the north (ji) and south (ji+1) v points -- and h(l)
+struct LayerFaces { float xe, yn, xw, ys, h; };
+
+template <class FX, class FY>
+__device__ __forceinline__ LayerFaces layer_faces(const Dims& D, const Grid<float>& G, FX fx, FY fy, int ji, int jk,
+                                                  int l) {
+  LayerFaces f;
+  f.xe = fx(ji, jk + 1, l);
+  f.yn = fy(ji, jk, l);
+  f.xw = fx(ji, jk, l);
+  f.ys = fy(ji + 1, jk, l);
+  f.h = 0.f;
+  if (l >= D.nf + 1) {
+    const long long p = IX(D, ji, jk, l);
+    f.h = 0.5f * f.xe * G.slope_x[IX(D, ji, jk + 1, l)] * G.ipw[0][p] + 0.5f * f.yn * G.slope_y[p] * G.ipw[1][p]
+        + 0.5f * f.xw * G.slope_x[p] * G.ipw[2][p] + 0.5f * f.ys * G.slope_y[IX(D, ji + 1, jk, l)] * G.ipw[3][p];
+  }
+  return f;
+}
+
+// contravariant corrections at the upper (cu, interface jl) and lower (cl, interface jl+1)
+// face of cell jl, and which of them the reference's branches use (mo_divergence_operators.F90:
+// the top terrain-following layer nf has only its lower face, the lowest layer only its upper
+// one unless it is layer nf itself)
+struct VertFaces { float cu, cl; bool up, lo; };
+__device__ __forceinline__ VertFaces vert_faces(const Dims& D, float h_prev, float h_cur, float h_next, int jl) {
+  VertFaces v;
+  v.up = jl > D.nf;
+  v.lo = jl == D.nf || (jl > D.nf && jl < D.nl);
+  v.cu = (jl == D.nf + 1) ? -h_cur : -(h_prev + h_cur);
+  v.cl = (jl + 1 == D.nf + 1) ? -h_next : -(h_cur + h_next);
+  return v;
+}
+
+// the divergence of cell jl from its layer's faces and the corrections of its two interfaces
+__device__ __forceinline__ float div_col(const Dims& D, const Grid<float>& G, const GridX& X, const LayerFaces& c,
+                                         const VertFaces& v, int ji, int jk, int jl) {
   const long long q = IX(D, ji, jk, jl);
+  const float comp_h = c.xe * G.area_x[IX(D, ji, jk + 1, jl)] + c.yn * G.area_y[q] - c.xw * G.area_x[q]
+                     - c.ys * G.area_y[IX(D, ji + 1, jk, jl)];
+  float comp_v = 0.f;
+  if (v.up) comp_v += v.cu * G.area_z[q];
+  if (v.lo) comp_v -= v.cl * G.area_z[IX(D, ji, jk, jl + 1)];
+  return (comp_h + comp_v) * X.inv_volume_f[q];
+}
+
+// div_h of a stored horizontal vector field (the third-order theta chain)
+__global__ void __launch_bounds__(128) ks_div_h(Dims D, Grid<float> GF, GridX X, const float* vx, const float* vy,
+                                                float* out) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (ji > D.ny || jk > D.nx) return;
+  auto fx = [&](int i, int j, int k) { return vx[IX(D, i, j, k)]; };
+  auto fy = [&](int i, int j, int k) { return vy[IX(D, i, j, k)]; };
+  LayerFaces cur = layer_faces(D, GF, fx, fy, ji, jk, 1), nxt{};
+  float h_prev = 0.f;
+  for (int jl = 1; jl <= D.nl; ++jl) {
+    nxt.h = 0.f;
+    if (jl < D.nl || jl == D.nf) nxt = layer_faces(D, GF, fx, fy, ji, jk, jl + 1);
+    out[IX(D, ji, jk, jl)] = div_col(D, GF, X, cur, vert_faces(D, h_prev, cur.h, nxt.h, jl), ji, jk, jl);
+    h_prev = cur.h;
+    cur = nxt;
+  }
+}
+
+// divergences of the gas and theta_v fluxes and the diabatic rho*theta_v term,
+// mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1), column-marching
+__global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* fu,
+                                                  const float* fv, const float* gu, const float* gv, const float* Tm,
+                                                  const float* rad, const float* csh, float* t_rho, float* t_rt) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long goff = (long long)(D.g - 1) * D.fstride;
   auto fx = [&](int i, int j, int k) { return fu[IX(D, i, j, k)]; };
   auto fy = [&](int i, int j, int k) { return fv[IX(D, i, j, k)]; };
   auto gx = [&](int i, int j, int k) { return gu[IX(D, i, j, k)]; };
   auto gy = [&](int i, int j, int k) { return gv[IX(D, i, j, k)]; };
-  t_rho[q + (long long)(D.g - 1) * D.fstride] = -div_h_at<float>(D, GF, fx, fy, ji, jk, jl);
-  const float div_t = div_h_at<float>(D, GF, gx, gy, ji, jk, jl);
-  const float heat = rad[q] + csh[q];
-  float x = 0.f;
-  if (heat != 0.f) {
-    const float cv = c_v_mass_weighted_air<float>(D, Ss.rho, Tm, q);
-    x = float(kC_D_V) * Ss.rho[q + (long long)(D.g - 1) * D.fstride] / cv * heat /
-        (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
+  LayerFaces mc = layer_faces(D, GF, fx, fy, ji, jk, 1), mn{};
+  LayerFaces tc = layer_faces(D, GF, gx, gy, ji, jk, 1), tn{};
+  float mh_prev = 0.f, th_prev = 0.f;
+  for (int jl = 1; jl <= D.nl; ++jl) {
+    const long long q = IX(D, ji, jk, jl);
+    mn.h = 0.f;
+    tn.h = 0.f;
+    if (jl < D.nl || jl == D.nf) {
+      mn = layer_faces(D, GF, fx, fy, ji, jk, jl + 1);
+      tn = layer_faces(D, GF, gx, gy, ji, jk, jl + 1);
+    }
+    const float heat = rad[q] + csh[q];
+    const float div_m = div_col(D, GF, X, mc, vert_faces(D, mh_prev, mc.h, mn.h, jl), ji, jk, jl);
+    const float div_t = div_col(D, GF, X, tc, vert_faces(D, th_prev, tc.h, tn.h, jl), ji, jk, jl);
+    float x = 0.f;
+    if (heat != 0.f) {
+      const float cv = c_v_mass_weighted_air<float>(D, Ss.rho, Tm, q);
+      x = float(kC_D_V) * Ss.rho[q + goff] / cv * heat / (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
+    }
+    t_rho[q + goff] = -div_m;
+    t_rt[q] = -div_t + x;
+    mh_prev = mc.h;
+    th_prev = tc.h;
+    mc = mn;
+    tc = tn;
   }
-  t_rt[q] = -div_t + x;
 }
 
 // scalar_tend_expl for the tracers, mo_scalar_tend_expl.F90:24-104 (upstream fluxes,
@@ -458,12 +550,15 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const float dv = -(ti * ti) * (ga0 + ga1) + 0.5f * deb * (al1 - al0 + ti * (be1 - be0))
                      - dz * ic2 * irio * (2.f * X.inv_area_z_f[ib] + dtf * wof * 0.5f * (L1.iv - L0.iv)) * dp;
     const float rie = 0.5f * (rhe0 + rhe1);
-    // the two w terms, -dz*ic2*(w_old + dt*tend_w) and -dz*ic2*rie*irio*w_old, with their FP32
-    // coefficients combined (one FP64 multiply-add on w_old; the tendency increment is FP32)
-    const float cw = -dz * ic2;
-    double rv = fma(wide(cw + cw * rie * irio), wo, wide(cw * (dtf * Tn.w[ib])));
+    // The products of FP32 coefficients with FP64 values here and in the state update below
+    // stay FP64 products of the FP32 factors: merging two FP32 factors into one rounded
+    // coefficient (e.g. -dz*ic2*(1 + rie*irio) for w_old) saves two FP64 operations per cell
+    // but lets an atmosphere at rest over hills drift about four times faster (1e-8 instead
+    // of 3e-9 m/s of spurious wind after 3 h at 256 x 256 x 50).
+    double rv = (wo + wide(dtf * Tn.w[ib])) * wide(-dz * ic2);
     rv = fma(D.luse_bg ? wide(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
     rv = fma(wide(0.5f * idtf * deb), tpe0 + tpe1, rv);
+    rv = fma(wide(-dz * ic2 * rie * irio), wo, rv);
     // couplings with row jl+1 (layer b's derivatives), which need layer jl+2
     float cv = 0.f, ev = 0.f;
     if (jl < n) {
@@ -505,8 +600,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     const double rho_e = So.rho[goff + i] + wide(dtf * Tn.rho[goff + i]);
     const double rt_e = rto + wide(dtf * Tn.rt[i]);
     const double rn = fma(dtv, s1 - s0, rho_e);
-    const float dtvf = dtf * X.inv_volume_f[i];
-    const double rtn = fma(wide(dtvf * t1), s1, fma(-wide(dtvf * t0), s0, rt_e));
+    const double rtn = fma(dtv, fma(-wide(t0), s0, wide(t1) * s1), rt_e);
     const double epn = fma(wide(gs[jl]), rtn - rto, So.ep[i]);
     const float rnf = narrow(rn);
     const float tpf = narrow(fma(-G.theta_v_bg[i], rn, rtn)) / rnf;
@@ -522,7 +616,7 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
       const float rin = 0.5f * (rn_prev + rnf);
       const float irio = 2.f / (Mo.rho[goff + IX(D, ji, jk, jl - 1)] + Mo.rho[goff + i]);
       const double wo = So.w[i];
-      const double wn = fma(-wide(rin * irio), wo, wide(2.f * X.inv_area_z_f[i] * irio) * s0);
+      const double wn = fma(-wide(rin), wo, wide(2.f * X.inv_area_z_f[i]) * s0) * wide(irio);
       Sn.w[i] = wn;
       Mn.w[i] = narrow(wn);
     }
@@ -839,7 +933,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_grad_vert", (k_grad_vert<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->th, s->gz);
     SL("ks_grad_hor", (k_grad_hor<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->gz, s->gx,
        s->gy);
-    SL("ks_div_h", k_div_h<float>, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->gx, s->gy, s->divf);
+    SL("ks_div_h", ks_div_h, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, s->gx, s->gy, s->divf);
     SL("ks_theta_edges", (k_theta_edges<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->divf, u,
        v, ou, ov);
     return LGAME_OK;
@@ -884,8 +978,8 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     }
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
        s->fv, s->gu, s->gv);
-    SL("ks_gas_div", ks_gas_div, sgrd(D.ny, D.nx, D.nl), B, D, GF, Ms, s->fu, s->fv, s->gu, s->gv, C.temperature,
-       C.rad, C.csh, T.rho, T.rt);
+    SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
+       C.temperature, C.rad, C.csh, T.rho, T.rt);
     const dim3 gc = cgrd(D.ny, D.nx);
     SL("ks_column_ver", ks_column_ver, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
     if (D.ncons > 1) {

@@ -85,15 +85,14 @@ def test_nonperiodic_edges_untouched():
         assert np.all(d[f][0, :, :] == 0) and np.all(d[f][-1, :, :] == 0), f
 
 
-def test_deterministic_and_thread_independent():
+def test_deterministic_and_thread_independent(tmp_path):
     code = ("import sys; sys.path[:0]=%r; import test_oracle as t, numpy as np; "
             "hm,o,b0,b1,st=t._run('jet',3); np.save(sys.argv[1], np.concatenate([v.ravel() for v in st.values()]))")
     here = Path(__file__).resolve().parent
     paths = [str(here), str(here.parent / "l-game_gb300"), str(here.parent / "oracle")]
     outs = []
     for threads in ("1", "3"):
-        f = here.parent / "_work" / f"det_{threads}.npy"
-        f.parent.mkdir(exist_ok=True)
+        f = tmp_path / f"det_{threads}.npy"
         env = dict(os.environ, OMP_NUM_THREADS=threads)
         subprocess.run([sys.executable, "-c", code % paths, str(f)], check=True, env=env, cwd=str(here))
         outs.append(np.load(f))
