@@ -474,7 +474,7 @@ __global__ void __launch_bounds__(256, 4) ks_tracers(Dims D, Grid<float> GF, Gri
 // right-hand side (where the pressure-gradient and buoyancy terms balance), the forward
 // and back substitution, and the new rho_g, rho*theta_v, exner', w.  theta' is formed as
 // (rho*theta_v - theta_bg*rho)/rho with the small numerator in FP64.
-__global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Grid<float> GF, GridX X, State So,
+__global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, Grid<float> GF, GridX X, State So,
                                                      State Sn, StateF Mo, StateF Mn, Tend<float> Tn, int rk_step) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -587,23 +587,43 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     s = fma(-wide(epr[jl]), s, rpr[jl]);
     rpr[jl] = s;
   }
-  // new state, mo_column_solvers.F90:300-345
-  float rn_prev = 0.f;
+  // new state, mo_column_solvers.F90:300-345.  The inputs of the next level are loaded before
+  // the current level's results are stored (a store may alias a later load, which stops the
+  // compiler from moving the loads itself).
+  struct StateIn { double rt, rho, ep, bg, w; float ivf, iaz, mro, trho, trt; };
+  auto state_in = [&](int m) {
+    StateIn r;
+    const long long p = IX(D, ji, jk, m);
+    r.rt = So.rt[p];
+    r.rho = So.rho[goff + p];
+    r.ep = So.ep[p];
+    r.bg = G.theta_v_bg[p];
+    r.w = So.w[p];
+    r.ivf = X.inv_volume_f[p];
+    r.iaz = X.inv_area_z_f[p];
+    r.mro = Mo.rho[goff + p];
+    r.trho = Tn.rho[goff + p];
+    r.trt = Tn.rt[p];
+    return r;
+  };
+  StateIn in_cur = state_in(1), in_nxt{};
+  float rn_prev = 0.f, mro_prev = 0.f;
   for (int jl = 1; jl <= nl; ++jl) {
+    if (jl < nl) in_nxt = state_in(jl + 1);
     const long long i = IX(D, ji, jk, jl);
     const double s0 = (jl >= 2) ? rpr[jl - 1] : 0.0;
     const double s1 = (jl <= n) ? rpr[jl] : 0.0;
     const float t0 = (jl >= 2) ? tis[jl - 1] : 0.f;
     const float t1 = (jl <= n) ? tis[jl] : 0.f;
-    const double dtv = wide(dtf * X.inv_volume_f[i]);
-    const double rto = So.rt[i];
-    const double rho_e = So.rho[goff + i] + wide(dtf * Tn.rho[goff + i]);
-    const double rt_e = rto + wide(dtf * Tn.rt[i]);
+    const double dtv = wide(dtf * in_cur.ivf);
+    const double rto = in_cur.rt;
+    const double rho_e = in_cur.rho + wide(dtf * in_cur.trho);
+    const double rt_e = rto + wide(dtf * in_cur.trt);
     const double rn = fma(dtv, s1 - s0, rho_e);
     const double rtn = fma(dtv, fma(-wide(t0), s0, wide(t1) * s1), rt_e);
-    const double epn = fma(wide(gs[jl]), rtn - rto, So.ep[i]);
+    const double epn = fma(wide(gs[jl]), rtn - rto, in_cur.ep);
     const float rnf = narrow(rn);
-    const float tpf = narrow(fma(-G.theta_v_bg[i], rn, rtn)) / rnf;
+    const float tpf = narrow(fma(-in_cur.bg, rn, rtn)) / rnf;
     Sn.rho[goff + i] = rn;
     Sn.rt[i] = rtn;
     Sn.ep[i] = epn;
@@ -614,13 +634,14 @@ __global__ void __launch_bounds__(128) ks_column_ver(Dims D, Grid<double> G, Gri
     Mn.tp[i] = tpf;
     if (jl >= 2) {  // w at level jl from the increment at that level
       const float rin = 0.5f * (rn_prev + rnf);
-      const float irio = 2.f / (Mo.rho[goff + IX(D, ji, jk, jl - 1)] + Mo.rho[goff + i]);
-      const double wo = So.w[i];
-      const double wn = fma(-wide(rin), wo, wide(2.f * X.inv_area_z_f[i]) * s0) * wide(irio);
+      const float irio = 2.f / (mro_prev + in_cur.mro);
+      const double wn = fma(-wide(rin), in_cur.w, wide(2.f * in_cur.iaz) * s0) * wide(irio);
       Sn.w[i] = wn;
       Mn.w[i] = narrow(wn);
     }
     rn_prev = rnf;
+    mro_prev = in_cur.mro;
+    in_cur = in_nxt;
   }
   if (D.freeslip) {  // w_free_slip, mo_inner_product.F90:52-75, with the new u, v
     const int m = nl;
@@ -696,18 +717,37 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
   float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
   const float vsurf = (jc == 1) ? 1.f : (jc == 3) ? 0.001f
                     : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
+  // The level loop is software-pipelined: the inputs of level m (1/volume, area_z, the old
+  // mirror density, old and new w, temperature, tendency) are loaded two iterations ahead,
+  // before the current level's results are stored, so two levels of loads are in flight per
+  // thread (a store may alias a later load, which stops the compiler from doing this).
+  struct LevelIn { float iv, az, ro, wo, wn, tm, tr; };
+  auto level_in = [&](int m) {
+    LevelIn r;
+    const long long p = IX(D, ji, jk, m);
+    r.iv = X.inv_volume_f[p];
+    r.az = GF.area_z[p];
+    r.ro = mro[p];
+    r.wo = Mo.w[p];
+    r.wn = Mn.w[p];
+    r.tm = cond ? Tm[p] : 0.f;  // condensates only
+    r.tr = t_rho[p];
+    return r;
+  };
+  LevelIn cur = level_in(1), nxt{}, nn{};
+  if (nl >= 2) nxt = level_in(2);
   float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
-  float itv_a = itw * dt * X.inv_volume_f[IX(D, ji, jk, 1)];
+  float itv_a = itw * dt * cur.iv;
   float epr_prev = 0.f, cv_prev = 0.f, rpr_prev = 0.f;
-  float ro_up = 0.f, ro = mro[IX(D, ji, jk, 1)];  // mirror densities of the cells above and here
+  float ro_up = 0.f;  // mirror density of the cell above
   for (int jl = 1; jl <= nl; ++jl) {
+    if (jl + 2 <= nl) nn = level_in(jl + 2);
     const long long i = IX(D, ji, jk, jl);
-    const float iv = X.inv_volume_f[i];
+    const float iv = cur.iv, ro = cur.ro;
     // the interface below the cell (between jl and jl+1)
     float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f, ro_dn = 0.f;
     if (jl <= nl - 1) {
-      const long long b = IX(D, ji, jk, jl + 1);
-      itv_b = itw * dt * X.inv_volume_f[b];
+      itv_b = itw * dt * nxt.iv;
       float vf = 0.f;
       if (jc == 1) vf = 1.f;
       else if (jc == 3) vf = 0.001f;
@@ -716,13 +756,13 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
         vf = 0.5f * (vcl_a + vcl_b);
         vcl_a = vcl_b;
       }
-      const float az = GF.area_z[b];
-      ro_dn = mro[b];
-      vfi = az * (Mo.w[b] - vf);
-      float fr = az * (Mn.w[b] - vf);
+      const float az = nxt.az;
+      ro_dn = nxt.ro;
+      vfi = az * (nxt.wo - vf);
+      float fr = az * (nxt.wn - vf);
       fr = ((fr >= 0.f) ? ro_dn : ro) * fr;
       vfr = fr;
-      if (cond) vefv = (ice ? c_p_ice(Tm[b]) : c_p_water(Tm[b])) * Tm[b] * fr;
+      if (cond) vefv = (ice ? c_p_ice(nxt.tm) : c_p_water(nxt.tm)) * nxt.tm * fr;
     }
     // d - 1, explicit flux part and sediment heating of cell jl
     float dm1, fl, h = 0.f;
@@ -738,7 +778,7 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
         dm1 += itw * vsurf * dt * az_sfc * iv;
         fl -= ew * vsurf * dt * ro * az_sfc * iv;
         if (jc > nc / 4) {
-          const float Tn = Tm[i];
+          const float Tn = cur.tm;
           h -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * ro * az_sfc * iv;
         }
       }
@@ -755,7 +795,7 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
     const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
     // right-hand side of the increment and forward elimination (pivot = d: one of e, c of an
     // interface is 0)
-    const float rhs = (dt * t_rho[i] + fl) - dm1 * ro - ev * ro_dn - cv_prev * ro_up;
+    const float rhs = (dt * cur.tr + fl) - dm1 * ro - ev * ro_dn - cv_prev * ro_up;
     const float piv = (1.f + dm1) - epr_prev * cv_prev;
     rpr_prev = (rhs - cv_prev * rpr_prev) / piv;
     rpr[jl] = rpr_prev;
@@ -763,15 +803,21 @@ __global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF,
     epr[jl] = epr_prev;
     cv_prev = cv;
     vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
-    ro_up = ro; ro = ro_dn;
+    ro_up = ro;
+    cur = nxt;
+    nxt = nn;
   }
   // back substitution; the new density rho_old + delta in FP64, negative densities clipped on
-  // output (mo_column_solvers.F90:587-591; the sign is read from the high word)
+  // output (mo_column_solvers.F90:587-591; the sign is read from the high word).  The old
+  // density of the next level up is loaded before the current level is stored.
   float dl = 0.f;
+  double ro_next = rho_o[IX(D, ji, jk, nl)];
   for (int jl = nl; jl >= 1; --jl) {
-    dl = rpr[jl] - epr[jl] * dl;
     const long long i = IX(D, ji, jk, jl);
-    const double sn = rho_o[i] + wide(dl);
+    const double ro_old = ro_next;
+    if (jl > 1) ro_next = rho_o[i - D.plane];
+    dl = rpr[jl] - epr[jl] * dl;
+    const double sn = ro_old + wide(dl);
     const double o = __double2hiint(sn) < 0 ? 0.0 : sn;
     rho_n[i] = o;
     mrn[i] = narrow(o);
