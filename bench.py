@@ -117,6 +117,19 @@ def _kernel_fields(ncons: int) -> dict:
     }
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per cell of one launch of each
+# split-step kernel, averaged over its launches in one step, from the one-pass ncu launch list
+# of the full 1024x1024x80 workload summarised in profiles/split_step_jet_1024_launches.md.
+# `roofline.traffic` is this figure times the cells of the run (bytes moved per launch of the
+# dominant kernel); traffic above the algorithmic bytes is re-reads and per-thread stacks.
+MEASURED_DRAM_BYTES_PER_CELL = {
+    "ks_column_tracers": 316.1, "ks_column_ver": 253.6, "ks_pgrad": 289.0, "ks_tracers": 172.7,
+    "ks_tend_wind": 157.3, "ks_div_h": 45.3, "ks_gas_div": 89.2, "ks_eta_xy": 93.7,
+    "ks_theta_edges": 23.7, "ks_vort_flux": 88.6, "ks_ke": 84.1, "ks_gas_flux": 35.8, "ks_eta_z": 40.5,
+    "ks_mass_flux": 27.5, "ks_temperature": 27.8, "ks_csh_sum": 23.8, "ks_gzp": 23.5,
+}
+
+
 def step_bytes_per_cell(ncons: int, split: bool) -> float:
     """Compulsory bytes per cell of one step: reads 2P + P + 2G + T + C, writes 2P + T + C
     with P = ncons + 6 prognostic, T = ncons + 4 tendency, C = 8 carried (+1 sediment
@@ -371,8 +384,10 @@ def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak
     alg = bpc * cells
     achieved = alg / (avg_ms / 1e3) / 1e9 if avg_ms > 0 else 0.0
     shares = {k: round(v["ms"] / total, 4) for k, v in rows}
+    dram = MEASURED_DRAM_BYTES_PER_CELL.get(name) if split else None
     return {"kernel": name, "avg_launch_ms": avg_ms, "alg_bytes_per_launch": alg, "achieved_gbs": achieved,
-            "frac": achieved / peak_gbs, "shares": shares, "rows": rows}
+            "frac": achieved / peak_gbs, "shares": shares, "rows": rows,
+            "traffic": None if dram is None else dram * cells}
 
 
 def run_ours(args):
@@ -457,7 +472,9 @@ def run_ours(args):
                    "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU", "setup_s": round(t_setup, 1)},
         "column_updates_per_s": value * n.nx * n.ny,
         "roofline": {"bound": "hbm", "kernel": prof["kernel"], "achieved": prof["achieved_gbs"],
-                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": prof["frac"], "traffic": None,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": prof["frac"], "traffic": prof["traffic"],
+                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum per cell, "
+                                    "profiles/split_step_jet_1024_launches.md, times the cells of this run",
                      "peak_src": peaks["src"], "avg_launch_ms": prof["avg_launch_ms"],
                      "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"]},
         "step_roofline": {"alg_bytes_per_cell": step_b, "alg_bytes_per_step": step_b * cells,
