@@ -325,7 +325,11 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
     // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
     const State& Ss = (rk == 1) ? So : Sn;
     if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
-    if (D.theta_order == 3) {
+    // theta_v_adv_3rd_order of the state used here: in the first substep that is state_old,
+    // whose edges manage_p_grad's call above already left in tvu/tvv (nothing in between
+    // writes state_old or tvu/tvv), so only the second substep recomputes them -- the same
+    // values the reference recomputes
+    if (D.theta_order == 3 && rk == 2) {
       int rc = theta3(c, Ss.tp, 0, Ss.u, Ss.v, c->tvu, c->tvv);
       if (rc != LGAME_OK) return rc;
     }

@@ -59,10 +59,10 @@ struct SplitCtx {
   double* vsq = nullptr;
   // FP64 vertical gradient of exner' at w points (0 at the top and surface levels)
   double* gzd = nullptr;
-  // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
-  float *fu = nullptr, *fv = nullptr, *gu = nullptr, *gv = nullptr;
   // sediment heating of each condensate (nc planes), summed into the carried csh
   float* csh_part = nullptr;
+  // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
+  float *fu = nullptr, *fv = nullptr, *gu = nullptr, *gv = nullptr;
   // FP32 mirrors of the two state slots
   StateF mir[2]{};
   SplitCarriedF C{};
@@ -277,6 +277,16 @@ __global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_ne
 // u points, y at the north (ji) and south (ji+1) v points -- and h(l)
 struct LayerFaces { float xe, yn, xw, ys, h; };
 
+// h(l) of a layer whose four face values are set
+__device__ __forceinline__ void layer_h(const Dims& D, const Grid<float>& G, LayerFaces& f, int ji, int jk, int l) {
+  f.h = 0.f;
+  if (l >= D.nf + 1) {
+    const long long p = IX(D, ji, jk, l);
+    f.h = 0.5f * f.xe * G.slope_x[IX(D, ji, jk + 1, l)] * G.ipw[0][p] + 0.5f * f.yn * G.slope_y[p] * G.ipw[1][p]
+        + 0.5f * f.xw * G.slope_x[p] * G.ipw[2][p] + 0.5f * f.ys * G.slope_y[IX(D, ji + 1, jk, l)] * G.ipw[3][p];
+  }
+}
+
 template <class FX, class FY>
 __device__ __forceinline__ LayerFaces layer_faces(const Dims& D, const Grid<float>& G, FX fx, FY fy, int ji, int jk,
                                                   int l) {
@@ -285,12 +295,7 @@ __device__ __forceinline__ LayerFaces layer_faces(const Dims& D, const Grid<floa
   f.yn = fy(ji, jk, l);
   f.xw = fx(ji, jk, l);
   f.ys = fy(ji + 1, jk, l);
-  f.h = 0.f;
-  if (l >= D.nf + 1) {
-    const long long p = IX(D, ji, jk, l);
-    f.h = 0.5f * f.xe * G.slope_x[IX(D, ji, jk + 1, l)] * G.ipw[0][p] + 0.5f * f.yn * G.slope_y[p] * G.ipw[1][p]
-        + 0.5f * f.xw * G.slope_x[p] * G.ipw[2][p] + 0.5f * f.ys * G.slope_y[IX(D, ji + 1, jk, l)] * G.ipw[3][p];
-  }
+  layer_h(D, G, f, ji, jk, l);
   return f;
 }
 
@@ -582,13 +587,11 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
     tpe0 = tpe1; epe0 = epe1; rhe0 = rhe1;
     tpe1 = tpe2; epe1 = epe2; rhe1 = rhe2;
   }
-  double s = rpr[n];
-  for (int jl = n - 1; jl >= 1; --jl) {
-    s = fma(-wide(epr[jl]), s, rpr[jl]);
-    rpr[jl] = s;
-  }
-  // new state, mo_column_solvers.F90:300-345.  The inputs of the next level are loaded before
-  // the current level's results are stored (a store may alias a later load, which stops the
+  // back substitution fused with the new state, mo_column_solvers.F90:300-345, bottom to top:
+  // layer jl needs the solutions of the rows above (w level jl) and below it (w level jl+1),
+  // and w at level jl+1 the new densities of layers jl and jl+1, all known once the
+  // substitution has reached row jl-1.  The inputs of the layer above are loaded before the
+  // current layer's results are stored (a store may alias a later load, which stops the
   // compiler from moving the loads itself).
   struct StateIn { double rt, rho, ep, bg, w; float ivf, iaz, mro, trho, trt; };
   auto state_in = [&](int m) {
@@ -606,13 +609,15 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
     r.trt = Tn.rt[p];
     return r;
   };
-  StateIn in_cur = state_in(1), in_nxt{};
-  float rn_prev = 0.f, mro_prev = 0.f;
-  for (int jl = 1; jl <= nl; ++jl) {
-    if (jl < nl) in_nxt = state_in(jl + 1);
+  StateIn in_cur = state_in(nl), in_up{}, in_below{};
+  double s1 = 0.0;        // solution at the interface below the layer (w level jl+1)
+  float rnf_below = 0.f;  // new rho_g of the layer below
+  for (int jl = nl; jl >= 1; --jl) {
+    if (jl > 1) in_up = state_in(jl - 1);
     const long long i = IX(D, ji, jk, jl);
-    const double s0 = (jl >= 2) ? rpr[jl - 1] : 0.0;
-    const double s1 = (jl <= n) ? rpr[jl] : 0.0;
+    // solution of row jl-1 (w level jl), the interface above the layer
+    double s0 = 0.0;
+    if (jl >= 2) s0 = (jl - 1 == n) ? rpr[n] : fma(-wide(epr[jl - 1]), s1, rpr[jl - 1]);
     const float t0 = (jl >= 2) ? tis[jl - 1] : 0.f;
     const float t1 = (jl <= n) ? tis[jl] : 0.f;
     const double dtv = wide(dtf * in_cur.ivf);
@@ -632,16 +637,18 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
     Mn.rt[i] = narrow(rtn);
     Mn.ep[i] = narrow(epn);
     Mn.tp[i] = tpf;
-    if (jl >= 2) {  // w at level jl from the increment at that level
-      const float rin = 0.5f * (rn_prev + rnf);
-      const float irio = 2.f / (mro_prev + in_cur.mro);
-      const double wn = fma(-wide(rin), in_cur.w, wide(2.f * in_cur.iaz) * s0) * wide(irio);
-      Sn.w[i] = wn;
-      Mn.w[i] = narrow(wn);
+    if (jl <= n) {  // w at level jl+1 from the increment there, between this layer and the one below
+      const long long ib = i + D.plane;
+      const float rin = 0.5f * (rnf + rnf_below);
+      const float irio = 2.f / (in_cur.mro + in_below.mro);
+      const double wn = fma(-wide(rin), in_below.w, wide(2.f * in_below.iaz) * s1) * wide(irio);
+      Sn.w[ib] = wn;
+      Mn.w[ib] = narrow(wn);
     }
-    rn_prev = rnf;
-    mro_prev = in_cur.mro;
-    in_cur = in_nxt;
+    s1 = s0;
+    rnf_below = rnf;
+    in_below = in_cur;
+    in_cur = in_up;
   }
   if (D.freeslip) {  // w_free_slip, mo_inner_product.F90:52-75, with the new u, v
     const int m = nl;
@@ -1018,7 +1025,10 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (D.ncons > 1)
       SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk);
-    if (D.theta_order == 3) {
+    // third-order theta edges of the state used here; in the first substep that is the old
+    // state, whose edges the pressure gradient's call above already left in tvu/tvv (nothing
+    // in between writes the old mirror or tvu/tvv), so only the second substep recomputes them
+    if (D.theta_order == 3 && rk == 2) {
       int rc = theta3f(Ms.tp, 0, Ms.u, Ms.v, s->tvu, s->tvv);
       if (rc) return rc;
     }
