@@ -57,8 +57,10 @@ struct SplitCtx {
   float *th, *gx, *gy, *gz, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph;
   // kinetic energy in FP64: its vertical differences over thin layers cancel most digits
   double* vsq = nullptr;
-  // FP64 vertical gradient of exner' at w points (0 at the top and surface levels)
+  // FP64 vertical gradient of exner' at w points (0 at the top and surface levels), and per
+  // column and terrain-following layer l half its weighted sum 0.5*(W5*gz(l) + W6*gz(l+1))
   double* gzd = nullptr;
+  double* rmz = nullptr;
   // sediment heating of each condensate (nc planes), summed into the carried csh
   float* csh_part = nullptr;
   // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
@@ -116,7 +118,8 @@ __global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, fl
 // field), theta edge values in FP32 (third order) or FP64 (second order), the background
 // term theta'*grad(Pi_bg) in FP64, the condensate deceleration factor in FP32 from the
 // mirror densities.
-__global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd, const float* mrho,
+__global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd, const double* rmz,
+                         const float* mrho,
                          const float* tvu, const float* tvv, const float* tpu, const float* tpv, PGrad<double> P,
                          float* pgcw, int lfirst) {
   LG_IDX3;
@@ -136,19 +139,17 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
   };
   // vertical gradient of exner_pert at a w point of column (i,j) (ks_gzp), 0 at the boundary levels
   auto gzp = [&](int i, int j, int k) -> double { return gzd[IX(D, i, j, k)]; };
-  auto remapx = [&](int ji_, int jk_, int jl_) -> double {  // mo_averaging.F90:56-95 on gzp
+  // remap_ver2hor_x/_y (mo_averaging.F90:56-136) of gzp at a u or v face: the sum over the
+  // face's two columns a and b of 0.5*(W5*gz(l) + W6*gz(l+1)), each column's term formed once
+  // in ks_gzp (the reference adds the four products in the order W5a, W5b, W6a, W6b; here
+  // the pairs of a column are added first, an FP64 rounding difference)
+  auto remapx = [&](int ji_, int jk_, int jl_) -> double {
     const int a = (jk_ == 1 || jk_ == D.nx + 1) ? D.nx : jk_ - 1, b = (jk_ == 1 || jk_ == D.nx + 1) ? 1 : jk_;
-    double r = G.ipw[4][IX(D, ji_, a, jl_)] * gzp(ji_, a, jl_) + G.ipw[4][IX(D, ji_, b, jl_)] * gzp(ji_, b, jl_);
-    if (jl_ < D.nl || D.freeslip)
-      r += G.ipw[5][IX(D, ji_, a, jl_)] * gzp(ji_, a, jl_ + 1) + G.ipw[5][IX(D, ji_, b, jl_)] * gzp(ji_, b, jl_ + 1);
-    return 0.5 * r;
+    return rmz[IX(D, ji_, a, jl_)] + rmz[IX(D, ji_, b, jl_)];
   };
   auto remapy = [&](int ji_, int jk_, int jl_) -> double {
     const int a = (ji_ == 1 || ji_ == D.ny + 1) ? D.ny : ji_ - 1, b = (ji_ == 1 || ji_ == D.ny + 1) ? 1 : ji_;
-    double r = G.ipw[4][IX(D, a, jk_, jl_)] * gzp(a, jk_, jl_) + G.ipw[4][IX(D, b, jk_, jl_)] * gzp(b, jk_, jl_);
-    if (jl_ < D.nl || D.freeslip)
-      r += G.ipw[5][IX(D, a, jk_, jl_)] * gzp(a, jk_, jl_ + 1) + G.ipw[5][IX(D, b, jk_, jl_)] * gzp(b, jk_, jl_ + 1);
-    return 0.5 * r;
+    return rmz[IX(D, a, jk_, jl_)] + rmz[IX(D, b, jk_, jl_)];
   };
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
@@ -213,14 +214,29 @@ __global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double*
   }
 }
 
-// vertical gradient of exner_pert at the w levels 2..nl (grad_vert, mo_gradient_operators.F90:65-83)
-__global__ void ks_gzp(Dims D, GridX X, const double* ep, double* gzd) {
+// vertical gradient of exner_pert at the w levels 2..nl (grad_vert, mo_gradient_operators.F90:65-83),
+// and in the terrain-following layers l > nf the column's half of the remap of that gradient
+// to the horizontal faces, 0.5*(W5(l)*gz(l) + W6(l)*gz(l+1)) (mo_averaging.F90:56-136; the W6
+// term only where l < nl or with a free-slip surface), gz being 0 at levels 1 and nl+1
+__global__ void ks_gzp(Dims D, Grid<double> G, GridX X, const double* ep, double* gzd, double* rmz) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 2;
+  const int jl = blockIdx.z + 1;
   if (ji > D.ny || jk > D.nx || jl > D.nl) return;
   const long long q = IX(D, ji, jk, jl);
-  gzd[q] = (ep[IX(D, ji, jk, jl - 1)] - ep[q]) * X.inv_dz[q];
+  double gz = 0.0;
+  if (jl >= 2) {
+    gz = (ep[IX(D, ji, jk, jl - 1)] - ep[q]) * X.inv_dz[q];
+    gzd[q] = gz;
+  }
+  if (jl > D.nf) {
+    double r = G.ipw[4][q] * gz;
+    if (jl < D.nl || D.freeslip) {
+      const double gz1 = (jl < D.nl) ? (ep[q] - ep[q + D.plane]) * X.inv_dz[q + D.plane] : 0.0;
+      r += G.ipw[5][q] * gz1;
+    }
+    rmz[q] = 0.5 * r;
+  }
 }
 
 // horizontal gas mass fluxes and theta_v fluxes of scalar_tend_expl, mo_scalar_tend_expl.F90:106-138:
@@ -873,7 +889,7 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
                        &s->ex, &s->ey, &s->ez, &s->uph, &s->vph, &s->wph};
   for (float** p : scratch) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
-  if ((rc = salloc(s, &s->gzd, F, bytes))) return fail(rc);
+  if ((rc = salloc(s, &s->gzd, F, bytes)) || (rc = salloc(s, &s->rmz, F, bytes))) return fail(rc);
   if (D.nc > 0 && (rc = salloc(s, &s->csh_part, F * D.nc, bytes))) return fail(rc);
   float** fl[] = {&s->fu, &s->fv, &s->gu, &s->gv};
   for (float** p : fl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
@@ -1003,9 +1019,9 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
         if (rc) return rc;
         if (D.luse_bg) { rc = theta3f(Mo.tp, 1, Mo.u, Mo.v, s->tpu, s->tpv); if (rc) return rc; }
       }
-      SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl - 1), B, D, s->GX, So.ep, s->gzd);
-      SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, Mo.rho, s->tvu, s->tvv,
-         s->tpu, s->tpv, pg, C.pgcw, step == 0 ? 1 : 0);
+      SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl), B, D, G, s->GX, So.ep, s->gzd, s->rmz);
+      SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, s->rmz, Mo.rho, s->tvu,
+         s->tvv, s->tpu, s->tpv, pg, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
       SL("ks_eta_xy", (k_eta_xy<float, float>), sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
