@@ -54,7 +54,7 @@ struct SplitCtx {
   float *ipw[6] = {}, *trsk_u[3] = {}, *trsk_v[2] = {};
   double *inv_dx = nullptr, *inv_dy = nullptr, *inv_dz = nullptr, *inv_volume = nullptr, *inv_area_z = nullptr;
   // FP32 intermediates
-  float *th, *gx, *gy, *gz, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph;
+  float *gx, *gy, *gz, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph;
   // kinetic energy in FP64: its vertical differences over thin layers cancel most digits
   double* vsq = nullptr;
   // FP64 vertical gradient of exner' at w points (0 at the top and surface levels), and per
@@ -63,6 +63,10 @@ struct SplitCtx {
   double* rmz = nullptr;
   // sediment heating of each condensate (nc planes), summed into the carried csh
   float* csh_part = nullptr;
+  // divergence of the gradient of theta_bg (the third-order theta chain of the background),
+  // and the background's x and y edge averages as FP32 pairs
+  float* dbg = nullptr;
+  float2 *tbu = nullptr, *tbv = nullptr;
   // horizontal gas mass fluxes and theta_v fluxes of the scalar tendency
   float *fu = nullptr, *fv = nullptr, *gu = nullptr, *gv = nullptr;
   // FP32 mirrors of the two state slots
@@ -276,6 +280,70 @@ __global__ void ks_gas_flux(Dims D, Grid<float> GF, StateF Ss, const float* u_ne
     }
     fv[q] = f;
     gv[q] = g;
+  }
+}
+
+// theta_v_adv_3rd_order edge values, mo_multiplications.F90:134-202, from theta' and dv, the
+// divergence of the gradient of theta'.  The chain theta -> gradient -> divergence is linear,
+// so the full theta_v edge is the background's part plus theta''s: 0.5*(theta_bg,a +
+// theta_bg,b) - c*dbg, with dbg the background's divergence and both formed once in FP64 at
+// set-up (split_set_grid; the face average is kept as an FP32 pair hi + lo), plus
+// 0.5*(theta'_a + theta'_b) - c*dv.  Adding the small parts first and hi last rounds the
+// ~300 K edge value once, where theta_bg + theta' rounded per cell cost one to two units of
+// the last place; the FP32 differences are taken of theta' rather than of theta_v.  With
+// tpu/tpv given, the edges of theta' alone (the background-subtracted edges of the pressure
+// gradient) come from the same pass.  The upwind cell of the correction follows the face
+// velocity as in the reference.
+__global__ void ks_theta_edges(Dims D, const float* tp, const float* dv, const float* dbg, const float2* tbu,
+                               const float2* tbv, const float* u, const float* v, float* tvu, float* tvv, float* tpu,
+                               float* tpv) {
+  LG_IDX3;
+  const float c = narrow(D.theta_edge_c);
+  auto edge = [&](long long a, long long b, long long up, long long q, float2 bgf, float* ov, float* op) {
+    const float d = dv[up];
+    const float pe = 0.5f * (tp[a] + tp[b]);
+    ov[q] = bgf.x + (bgf.y + ((pe - c * d) - c * dbg[up]));
+    if (op) op[q] = pe - c * d;
+  };
+  if (ji <= D.ny && jk <= D.nx + 1) {  // x edges: cells west (a) and east (b) of the face
+    const bool in = jk >= 2 && jk <= D.nx;
+    if (in || D.periodic) {
+      const int ka = in ? jk - 1 : D.nx, kb = in ? jk : 1;
+      const long long a = IX(D, ji, ka, jl), b = IX(D, ji, kb, jl), q = IX(D, ji, jk, jl);
+      edge(a, b, (u[IX(D, ji, kb, jl)] >= 0.f) ? a : b, q, tbu[q], tvu, tpu);
+    }
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {  // y edges: cells south (a, row ji) and north (b, row ji-1)
+    const bool in = ji >= 2 && ji <= D.ny;
+    if (in || D.periodic) {
+      const int ia = in ? ji : 1, ib = in ? ji - 1 : D.ny;
+      const long long a = IX(D, ia, jk, jl), b = IX(D, ib, jk, jl), q = IX(D, ji, jk, jl);
+      edge(a, b, (v[IX(D, ia, jk, jl)] >= 0.f) ? a : b, q, tbv[q], tvv, tpv);
+    }
+  }
+}
+
+// the background's face averages 0.5*(theta_bg,a + theta_bg,b) at the x and y edges, in FP64,
+// kept as FP32 pairs (hi = the rounded value, lo = the rounded remainder)
+__global__ void k_bg_faces(Dims D, Grid<double> G, float2* tbu, float2* tbv) {
+  LG_IDX3;
+  auto pair = [](double x) {
+    const float hi = narrow(x);
+    return make_float2(hi, narrow(x - wide(hi)));
+  };
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    const bool in = jk >= 2 && jk <= D.nx;
+    if (in || D.periodic) {
+      const int ka = in ? jk - 1 : D.nx, kb = in ? jk : 1;
+      tbu[IX(D, ji, jk, jl)] = pair(0.5 * (G.theta_v_bg[IX(D, ji, ka, jl)] + G.theta_v_bg[IX(D, ji, kb, jl)]));
+    }
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    const bool in = ji >= 2 && ji <= D.ny;
+    if (in || D.periodic) {
+      const int ia = in ? ji : 1, ib = in ? ji - 1 : D.ny;
+      tbv[IX(D, ji, jk, jl)] = pair(0.5 * (G.theta_v_bg[IX(D, ia, jk, jl)] + G.theta_v_bg[IX(D, ib, jk, jl)]));
+    }
   }
 }
 
@@ -885,12 +953,14 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
       (rc = salloc(s, &s->inv_dz, F, bytes)) || (rc = salloc(s, &s->inv_volume, F, bytes)) ||
       (rc = salloc(s, &s->inv_area_z, F, bytes)))
     return fail(rc);
-  float** scratch[] = {&s->th, &s->gx, &s->gy, &s->gz, &s->divf, &s->tvu, &s->tvv, &s->tpu, &s->tpv,
+  float** scratch[] = {&s->gx, &s->gy, &s->gz, &s->divf, &s->tvu, &s->tvv, &s->tpu, &s->tpv,
                        &s->ex, &s->ey, &s->ez, &s->uph, &s->vph, &s->wph};
   for (float** p : scratch) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->gzd, F, bytes)) || (rc = salloc(s, &s->rmz, F, bytes))) return fail(rc);
   if (D.nc > 0 && (rc = salloc(s, &s->csh_part, F * D.nc, bytes))) return fail(rc);
+  if ((rc = salloc(s, &s->dbg, F, bytes)) || (rc = salloc(s, &s->tbu, F, bytes)) || (rc = salloc(s, &s->tbv, F, bytes)))
+    return fail(rc);
   float** fl[] = {&s->fu, &s->fv, &s->gu, &s->gv};
   for (float** p : fl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   for (int k = 0; k < 2; ++k) {
@@ -972,6 +1042,29 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   for (int k = 0; k < 3; ++k) GF.trsk_u[k] = s->trsk_u[k];
   for (int k = 0; k < 2; ++k) GF.trsk_v[k] = s->trsk_v[k];
   s->GX = GridX{s->inv_dx, s->inv_dy, s->inv_dz, s->inv_volume, s->inv_area_z, ivol, iaz, dzs, deb};
+  // the third-order theta chain of the background, in FP64 on temporary arrays that start at 0
+  // (the levels and boundary faces the chain does not write are read as 0)
+  double* tmp[4] = {};
+  bool ok = true;
+  for (double*& t : tmp) {
+    ok = ok && cudaMalloc(&t, (size_t)F * sizeof(double)) == cudaSuccess &&
+         cudaMemsetAsync(t, 0, (size_t)F * sizeof(double), stream) == cudaSuccess;
+  }
+  if (ok) {
+    const dim3 B = sblk();
+    k_grad_vert<double, double><<<sgrd(D.ny, D.nx, D.nl - 1), B, 0, stream>>>(D, G, G.theta_v_bg, tmp[0]);
+    k_grad_hor<double, double><<<sgrd(D.ny + 1, D.nx + 1, D.nl), B, 0, stream>>>(D, G, G.theta_v_bg, tmp[0], tmp[1],
+                                                                                  tmp[2]);
+    k_div_h<double><<<sgrd(D.ny, D.nx, D.nl), B, 0, stream>>>(D, G, tmp[1], tmp[2], tmp[3]);
+    k_to_float<<<1216, 256, 0, stream>>>(tmp[3], s->dbg, F);
+    k_bg_faces<<<sgrd(D.ny + 1, D.nx + 1, D.nl), B, 0, stream>>>(D, G, s->tbu, s->tbv);
+    ok = cudaGetLastError() == cudaSuccess && cudaStreamSynchronize(stream) == cudaSuccess;
+  }
+  for (double* t : tmp) if (t) cudaFree(t);
+  if (!ok) {
+    lgame_set_error("split set-up: theta chain of the background state failed");
+    return LGAME_ERR_CUDA;
+  }
   return LGAME_OK;
 }
 
@@ -997,14 +1090,15 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     ++launches;                                                                 \
   } while (0)
   const dim3 B = sblk();
-  auto theta3f = [&](const float* tp, int mode, const float* u, const float* v, float* ou, float* ov) -> int {
-    SL("ks_theta", (k_theta<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, tp, s->th, mode);
-    SL("ks_grad_vert", (k_grad_vert<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->th, s->gz);
-    SL("ks_grad_hor", (k_grad_hor<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->gz, s->gx,
-       s->gy);
+  // third-order theta edges: the gradient of theta' (read from the mirror), its divergence and
+  // the edges of theta_bg + theta' (and of theta' alone when pu/pv are given)
+  auto theta3f = [&](const float* tp, const float* u, const float* v, float* ou, float* ov, float* pu,
+                     float* pv) -> int {
+    SL("ks_grad_vert", (k_grad_vert<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, tp, s->gz);
+    SL("ks_grad_hor", (k_grad_hor<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, tp, s->gz, s->gx, s->gy);
     SL("ks_div_h", ks_div_h, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, s->gx, s->gy, s->divf);
-    SL("ks_theta_edges", (k_theta_edges<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->th, s->divf, u,
-       v, ou, ov);
+    SL("ks_theta_edges", ks_theta_edges, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, tp, s->divf, s->dbg, s->tbu, s->tbv, u,
+       v, ou, ov, pu, pv);
     return LGAME_OK;
   };
   SL("ks_temperature", (k_temperature<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, Mo, C.temperature);
@@ -1014,10 +1108,10 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     const State& Sv = (rk == 1) ? So : Sn;
     const StateF& Mv = (rk == 1) ? Mo : Mn;
     if (rk == 1) {
-      if (D.theta_order == 3) {
-        int rc = theta3f(Mo.tp, 0, Mo.u, Mo.v, s->tvu, s->tvv);
+      if (D.theta_order == 3) {  // the edges of theta_v and, with a background state, of theta'
+        const int rc = theta3f(Mo.tp, Mo.u, Mo.v, s->tvu, s->tvv, D.luse_bg ? s->tpu : nullptr,
+                               D.luse_bg ? s->tpv : nullptr);
         if (rc) return rc;
-        if (D.luse_bg) { rc = theta3f(Mo.tp, 1, Mo.u, Mo.v, s->tpu, s->tpv); if (rc) return rc; }
       }
       SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl), B, D, G, s->GX, So.ep, s->gzd, s->rmz);
       SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, s->rmz, Mo.rho, s->tvu,
@@ -1045,7 +1139,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     // state, whose edges the pressure gradient's call above already left in tvu/tvv (nothing
     // in between writes the old mirror or tvu/tvv), so only the second substep recomputes them
     if (D.theta_order == 3 && rk == 2) {
-      int rc = theta3f(Ms.tp, 0, Ms.u, Ms.v, s->tvu, s->tvv);
+      const int rc = theta3f(Ms.tp, Ms.u, Ms.v, s->tvu, s->tvv, nullptr, nullptr);
       if (rc) return rc;
     }
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
