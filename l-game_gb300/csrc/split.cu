@@ -778,8 +778,10 @@ __device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>
 // (the upwind side), so the pivots are the diagonal entries themselves.  The tracer is the
 // fastest block index, so the blocks of one column tile run together and share the column's
 // w, temperature and volume reads through L2.  A condensate's sediment heating goes to its own
-// plane of csh_part (rk_step 1 only); ks_csh_sum adds the planes in condensate order.
-__global__ void __launch_bounds__(128) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
+// plane of csh_part (rk_step 1 only); ks_csh_sum adds the planes in condensate order.  The
+// level loop waits on memory, so the register cap buys residency: twelve blocks per SM
+// (40 registers) ran 6 % faster than nine.
+__global__ void __launch_bounds__(128, 12) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
                                                          StateF Mo, StateF Mn, const float* t_rho_all,
                                                          const float* Tm, float* csh_part, int rk_step) {
   const int ji = blockIdx.y * blockDim.x + threadIdx.x + 1;
