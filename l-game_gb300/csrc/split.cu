@@ -121,11 +121,12 @@ __global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, fl
 // gradient of the Exner pressure perturbation in FP64 (the small differences of a small
 // field), theta edge values in FP32 (third order) or FP64 (second order), the background
 // term theta'*grad(Pi_bg) in FP64, the condensate deceleration factor in FP32 from the
-// mirror densities.
-__global__ void ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd, const double* rmz,
-                         const float* mrho,
-                         const float* tvu, const float* tvv, const float* tpu, const float* tpv, PGrad<double> P,
-                         float* pgcw, int lfirst) {
+// mirror densities.  Six resident blocks of 256 threads per SM (40 registers) ran 12 % faster
+// than five.
+__global__ void __launch_bounds__(256, 6) ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd,
+                                                  const double* rmz, const float* mrho, const float* tvu,
+                                                  const float* tvv, const float* tpu, const float* tpv,
+                                                  PGrad<double> P, float* pgcw, int lfirst) {
   LG_IDX3;
   const double* ep = S.ep;
   auto theta = [&](int i, int j, int k) { const long long q = IX(D, i, j, k); return G.theta_v_bg[q] + S.tp[q]; };
@@ -476,8 +477,9 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
 // cell; the tracer loop then only loads densities at known addresses, and every tracer's
 // divergence is formed before the first tendency is stored, so no load waits on a velocity
 // or on an earlier store.  The first substep (new weight 1) does not read the old tendency.
+// Five resident blocks of 256 threads per SM (48 registers) ran 4 % faster than four.
 constexpr int kTracers = 6;  // moist: five condensates and water vapour (the gas has its own kernel)
-__global__ void __launch_bounds__(256, 4) ks_tracers(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* u_new,
+__global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* u_new,
                                                      const float* v_new, float* t_rho, int rk_step) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
