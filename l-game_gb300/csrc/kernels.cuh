@@ -517,8 +517,9 @@ __global__ void k_mass_flux(Dims D, Grid<T> G, StateT<V> S, T* uph, T* vph, T* w
 
 // calc_vorticity_flux_term, mo_vorticity_flux.F90:16-171
 template <class T, class V = double>
-__global__ void k_vort_flux(Dims D, Grid<T> G, StateT<V> S, const T* ex, const T* ey, const T* ez, const T* uph,
-                            const T* vph, const T* wph, T* px, T* py, T* pz) {
+__device__ __forceinline__ void vort_flux_body(const Dims& D, const Grid<T>& G, const StateT<V>& S, const T* ex,
+                                               const T* ey, const T* ez, const T* uph, const T* vph, const T* wph,
+                                               T* px, T* py, T* pz) {
   LG_IDX3;
   // vertical mass flux with the free-slip surface value, mo_vector_tend_expl.F90:68-80
   auto wp = [&](int i, int j, int k) -> T {
@@ -567,6 +568,12 @@ __global__ void k_vort_flux(Dims D, Grid<T> G, StateT<V> S, const T* ex, const T
       + W_(3, ji, jk, jl) * uph[IX(D, ji, jk, jl)] * ey[IX(D, ji, jk, jl)]
       - W_(4, ji, jk, jl) * vph[IX(D, ji + 1, jk, jl)] * ex[IX(D, ji + 1, jk, jl)]);
   }
+}
+
+template <class T, class V = double>
+__global__ void k_vort_flux(Dims D, Grid<T> G, StateT<V> S, const T* ex, const T* ey, const T* ez, const T* uph,
+                            const T* vph, const T* wph, T* px, T* py, T* pz) {
+  vort_flux_body<T, V>(D, G, S, ex, ey, ez, uph, vph, wph, px, py, pz);
 }
 
 // inner_product of the wind with itself, mo_inner_product.F90:16-50

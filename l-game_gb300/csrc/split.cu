@@ -557,6 +557,27 @@ __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, Gri
   }
 }
 
+// the potential vorticity and its flux (calc_pot_vort, mo_vorticities.F90:189-421; vorticity
+// flux, mo_vorticity_flux.F90:16-171) of the split step: the FP32 bodies of k_eta_xy, k_eta_z
+// and k_vort_flux with register caps that keep six to seven blocks of 256 threads resident
+__global__ void __launch_bounds__(256, 6) ks_eta_xy(Dims D, Grid<float> G, StateF S, float* ex, float* ey) {
+  LG_IDX3;
+  if (jl > D.NL) return;
+  if (ji <= D.ny + 1 && jk <= D.nx) ex[IX(D, ji, jk, jl)] = eta_x_at<float>(D, G, S, ji, jk, jl);
+  if (ji <= D.ny && jk <= D.nx + 1) ey[IX(D, ji, jk, jl)] = eta_y_at<float>(D, G, S, ji, jk, jl);
+}
+__global__ void __launch_bounds__(256, 7) ks_eta_z(Dims D, Grid<float> G, StateF S, float* ez) {
+  LG_IDX3;
+  if (ji > D.ny + 1 || jk > D.nx + 1) return;
+  ez[IX(D, ji, jk, jl)] = eta_z_at<float>(D, G, S, ji, jk, jl);
+}
+__global__ void __launch_bounds__(256, 6) ks_vort_flux(Dims D, Grid<float> G, StateF S, const float* ex,
+                                                       const float* ey, const float* ez, const float* uph,
+                                                       const float* vph, const float* wph, float* px, float* py,
+                                                       float* pz) {
+  vort_flux_body<float, float>(D, G, S, ex, ey, ez, uph, vph, wph, px, py, pz);
+}
+
 // ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
 // The reference's implicit system for the vertical mass-flux increments at levels 2..nl,
 // one thread per column, streamed top to bottom.  FP32 (from the mirror): the partial
@@ -1122,11 +1143,11 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
          s->tvv, s->tpu, s->tpv, pg, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
-      SL("ks_eta_xy", (k_eta_xy<float, float>), sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
-      SL("ks_eta_z", (k_eta_z<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ez);
+      SL("ks_eta_xy", ks_eta_xy, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
+      SL("ks_eta_z", ks_eta_z, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ez);
       SL("ks_mass_flux", (k_mass_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->uph, s->vph,
          s->wph);
-      SL("ks_vort_flux", (k_vort_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
+      SL("ks_vort_flux", ks_vort_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
          s->ez, s->uph, s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
       if (!D.llinear) {
         SL("ks_ke", (k_ke<double, double>), sgrd(D.ny, D.nx, D.nl), B, D, G, Sv, s->vsq);
