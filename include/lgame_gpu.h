@@ -207,7 +207,11 @@ int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
 /* The same step with host buffers: copies state_old from host memory to the device,
  * runs lgame_gpu_pchevi into slot 1, and copies the new state back to state_new
  * (host).  This is what a Fortran pchevi_gpu shim with pchevi's exact argument list
- * would call when the host keeps the authoritative state (mo_manage_pchevi.F90:27). */
+ * would call when the host keeps the authoritative state (mo_manage_pchevi.F90:27).
+ * When every array is page-locked and mapped (cudaHostAlloc / cudaHostRegister with
+ * mapping; on Grace systems the GPU then reaches it over the coherent CPU-GPU link), the
+ * GPU reads and writes the host arrays itself and fills the FP32 state mirror in the
+ * same pass; otherwise the copy engines move the state.  Slots 0 and 1 are used. */
 int  lgame_gpu_pchevi_host(lgame_gpu* ctx, const double* const* state_old,
                            double* const* state_new, int nfields,
                            int total_step_counter, int lrad_update, double t_0);

@@ -152,6 +152,48 @@ int copy_d2h(lgame_gpu* c, double* host, const double* dev, Ext e) {
   return LGAME_OK;
 }
 
+// State transfer by the GPU itself over the coherent CPU-GPU link, for host arrays the GPU can
+// address (page-locked and mapped: cudaPointerGetAttributes gives a device pointer).  One
+// thread per element of a column-major host array of extent n1 x n2 x (n3*nrep) (nrep
+// constituents back to back), coalesced along n1 on both sides.  k_state_in writes the padded
+// FP64 field of both state slots and, with m0/m1 given, the FP32 mirror of both (rounded to
+// nearest, as the mirror refresh does); k_state_out writes a slot's field back to the host.
+__global__ void k_state_in(Dims D, const double* src, int n1, int n2, int n3, double* d0, double* d1, float* m0,
+                           float* m1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n1) return;
+  const int j = blockIdx.y, z = blockIdx.z, c = z / n3, k = z % n3;
+  const long long h = i + (long long)n1 * (j + (long long)n2 * z);
+  const long long q = (long long)c * D.fstride + i + (long long)D.P * (j + (long long)D.NX1 * k);
+  const double v = src[h];
+  d0[q] = v;
+  d1[q] = v;
+  if (m0) {
+    const float f = narrow(v);
+    m0[q] = f;
+    m1[q] = f;
+  }
+}
+__global__ void k_state_out(Dims D, const double* s, int n1, int n2, int n3, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n1) return;
+  const int j = blockIdx.y, z = blockIdx.z, c = z / n3, k = z % n3;
+  dst[i + (long long)n1 * (j + (long long)n2 * z)] =
+      s[(long long)c * D.fstride + i + (long long)D.P * (j + (long long)D.NX1 * k)];
+}
+
+// the device address of a host array the GPU can read and write directly, or null
+const double* device_view(const double* host) {
+  if (!host) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer may leave an error behind
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return (const double*)a.devicePointer;
+}
+
 __global__ void k_split_ipw(Dims D, const double* src, double* w1, double* w2, double* w3, double* w4,
                             double* w5, double* w6) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -698,14 +740,43 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
                                      int nfields, int total_step_counter, int lrad_update, double t_0) {
   if (!c || !state_old || !state_new || nfields != LGAME_STATE_NFIELDS)
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: bad arguments");
-  int rc = state_copy(c, 0, nullptr, state_old, true);
-  if (rc != LGAME_OK) return rc;
-  c->mirror_valid[0] = c->mirror_valid[1] = false;
-  // state_new starts as a copy of state_old, as in the reference's time loop
-  for (int s = 0; s < 1; ++s) {
-    const Dims& D = c->D;
-    const State& A = c->st[0];
-    const State& B = c->st[1];
+  const Dims& D = c->D;
+  const Ext ex[LGAME_STATE_NFIELDS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D)};
+  const State& A = c->st[0];
+  const State& B = c->st[1];
+  double* da[LGAME_STATE_NFIELDS] = {A.rho, A.rt, A.tp, A.ep, A.u, A.v, A.w};
+  double* db[LGAME_STATE_NFIELDS] = {B.rho, B.rt, B.tp, B.ep, B.u, B.v, B.w};
+  const double* vin[LGAME_STATE_NFIELDS];
+  double* vout[LGAME_STATE_NFIELDS];
+  // the GPU moves the state itself when every array is one it can address; a null array (not
+  // copied) or an unregistered one takes the copy engines, as before
+  bool direct_in = true, direct_out = true;
+  for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+    direct_in = direct_in && (vin[f] = device_view(state_old[f])) != nullptr;
+    direct_out = direct_out && (vout[f] = const_cast<double*>(device_view(state_new[f]))) != nullptr;
+  }
+  auto grid_of = [&](int f) {
+    const int nrep = (f == LGAME_STATE_RHO) ? D.ncons : 1;
+    return dim3((unsigned)((ex[f].n1 + 255) / 256), (unsigned)ex[f].n2, (unsigned)(ex[f].n3 * nrep));
+  };
+  if (direct_in) {
+    // state_old into slot 0 and, as the reference's time loop starts state_new as a copy of
+    // state_old, into slot 1, with the FP32 mirrors of both in split mode
+    StateF m0{}, m1{};
+    if (c->split) { m0 = split_mirror(c->split, 0); m1 = split_mirror(c->split, 1); }
+    float* ma[LGAME_STATE_NFIELDS] = {m0.rho, m0.rt, m0.tp, m0.ep, m0.u, m0.v, m0.w};
+    float* mb[LGAME_STATE_NFIELDS] = {m1.rho, m1.rt, m1.tp, m1.ep, m1.u, m1.v, m1.w};
+    for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+      k_state_in<<<grid_of(f), 256, 0, c->stream>>>(D, vin[f], (int)ex[f].n1, (int)ex[f].n2, (int)ex[f].n3, da[f],
+                                                     db[f], ma[f], mb[f]);
+      CK(cudaGetLastError());
+    }
+    c->mirror_valid[0] = c->mirror_valid[1] = c->split != nullptr;
+  } else {
+    int rc = state_copy(c, 0, nullptr, state_old, true);
+    if (rc != LGAME_OK) return rc;
+    c->mirror_valid[0] = c->mirror_valid[1] = false;
+    // state_new starts as a copy of state_old, as in the reference's time loop
     const size_t F = (size_t)D.fstride * sizeof(double);
     CK(cudaMemcpyAsync(B.rho, A.rho, F * D.ncons, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(B.rt, A.rt, F, cudaMemcpyDeviceToDevice, c->stream));
@@ -715,10 +786,17 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     CK(cudaMemcpyAsync(B.v, A.v, F, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(B.w, A.w, F, cudaMemcpyDeviceToDevice, c->stream));
   }
-  rc = lgame_gpu_pchevi(c, 0, 1, total_step_counter, lrad_update, t_0);
+  int rc = lgame_gpu_pchevi(c, 0, 1, total_step_counter, lrad_update, t_0);
   if (rc != LGAME_OK) return rc;
-  rc = state_copy(c, 1, state_new, nullptr, false);
-  if (rc != LGAME_OK) return rc;
+  if (direct_out) {
+    for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+      k_state_out<<<grid_of(f), 256, 0, c->stream>>>(D, db[f], (int)ex[f].n1, (int)ex[f].n2, (int)ex[f].n3, vout[f]);
+      CK(cudaGetLastError());
+    }
+  } else {
+    rc = state_copy(c, 1, state_new, nullptr, false);
+    if (rc != LGAME_OK) return rc;
+  }
   CK(cudaStreamSynchronize(c->stream));
   return LGAME_OK;
 }

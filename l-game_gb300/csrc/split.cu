@@ -1010,6 +1010,7 @@ void split_destroy(SplitCtx* s) {
 }
 
 SplitCarriedF split_carried(SplitCtx* s) { return s->C; }
+StateF split_mirror(SplitCtx* s, int slot) { return s->mir[slot]; }
 
 int split_convert(const double* src, float* dst, long long n, cudaStream_t stream) {
   k_to_float<<<1216, 256, 0, stream>>>(src, dst, n);

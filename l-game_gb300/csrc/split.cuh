@@ -35,6 +35,8 @@ SplitCarriedF split_carried(SplitCtx* s);
 // converts n elements FP64 <-> FP32 (field layout identical)
 int split_convert(const double* src, float* dst, long long n, cudaStream_t stream);
 int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream);
+// the FP32 mirror of state slot `slot` (its arrays; for writers that fill it themselves)
+StateF split_mirror(SplitCtx* s, int slot);
 // FP32 mirror of state slot `slot` recomputed from the FP64 state S (after the host wrote S)
 int split_refresh_mirror(SplitCtx* s, const Dims& D, int slot, const State& S, cudaStream_t stream);
 // one step from slot so (state So) to slot sn (state Sn); pg holds the FP64 pressure-gradient
