@@ -402,6 +402,22 @@ int split_sync_carried(lgame_gpu* c, bool to_split) {
     const int rc = to_split ? split_convert(p.d, p.f, p.n, c->stream) : split_convert_back(p.f, p.d, p.n, c->stream);
     if (rc != LGAME_OK) return set_err(rc, "conversion of the split-mode diagnostics failed");
   }
+  // with a background state the split step keeps the pressure-gradient terms the wind update
+  // uses in FP32 (net nl + l, previous -(nl + l)); p_grad_acc_old lives only in that form
+  if (c->D.luse_bg) {
+    int rc = LGAME_OK;
+    if (to_split) {
+      if (!rc) rc = split_net(c->pg_nl_u, c->pg_l_u, F.pnet_u, n, c->stream);
+      if (!rc) rc = split_net(c->pg_nl_v, c->pg_l_v, F.pnet_v, n, c->stream);
+      if (!rc) rc = split_net(c->pg_nl_w, c->pg_l_w, F.pnet_w, n, c->stream);
+      if (!rc) rc = split_convert(c->pg_old_u, F.pold_u, n, c->stream);
+      if (!rc) rc = split_convert(c->pg_old_v, F.pold_v, n, c->stream);
+    } else {
+      if (!rc) rc = split_convert_back(F.pold_u, c->pg_old_u, n, c->stream);
+      if (!rc) rc = split_convert_back(F.pold_v, c->pg_old_v, n, c->stream);
+    }
+    if (rc != LGAME_OK) return set_err(rc, "conversion of the split-mode pressure-gradient terms failed");
+  }
   return LGAME_OK;
 }
 

@@ -95,6 +95,10 @@ __global__ void k_to_float(const double* a, float* b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
 }
+__global__ void k_net(const double* a, const double* b, float* net, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    net[i] = narrow(a[i] + b[i]);
+}
 __global__ void k_to_double(const float* a, double* b, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     b[i] = (double)a[i];
@@ -126,7 +130,7 @@ __global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, fl
 __global__ void __launch_bounds__(256, 6) ks_pgrad(Dims D, Grid<double> G, GridX X, State S, const double* gzd,
                                                   const double* rmz, const float* mrho, const float* tvu,
                                                   const float* tvv, const float* tpu, const float* tpv,
-                                                  PGrad<double> P, float* pgcw, int lfirst) {
+                                                  PGrad<double> P, SplitCarriedF PF, float* pgcw, int lfirst) {
   LG_IDX3;
   const double* ep = S.ep;
   auto theta = [&](int i, int j, int k) { const long long q = IX(D, i, j, k); return G.theta_v_bg[q] + S.tp[q]; };
@@ -156,65 +160,94 @@ __global__ void __launch_bounds__(256, 6) ks_pgrad(Dims D, Grid<double> G, GridX
     const int a = (ji_ == 1 || ji_ == D.ny + 1) ? D.ny : ji_ - 1, b = (ji_ == 1 || ji_ == D.ny + 1) ? 1 : ji_;
     return rmz[IX(D, a, jk_, jl_)] + rmz[IX(D, b, jk_, jl_)];
   };
-  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
-    const long long q = IX(D, ji, jk, jl);
+  // the products of the u face (jk) and the v face (ji) of layer jl: nl = decel*theta_edge*grad,
+  // l = decel*theta'_edge*grad(Pi_bg) (with a background state); false at non-periodic edges.
+  // decel and the edge theta are FP32 values; their product with the gradient is FP64 (an
+  // extra FP32 rounding of either product would unbalance the two terms, which cancel in an
+  // atmosphere at rest)
+  auto face_u = [&](double* nlv, double* lv) -> bool {
     const bool inner = jk >= 2 && jk <= D.nx;
-    const double nl_prev = P.nl_u[q], l_prev = P.l_u[q];
-    if (!lfirst) P.old_u[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
-    if (inner || D.periodic) {
-      const int kk = inner ? jk : 1, ka = inner ? jk - 1 : D.nx;
-      const long long qr = IX(D, ji, kk, jl);
-      double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
-      if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
-      // decel and the edge theta are FP32 values; their product with the gradient is FP64
-      // (an extra FP32 rounding of either product would unbalance the two terms, which
-      // cancel in an atmosphere at rest)
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : wide(tvu[qr]);
-      const double de = wide(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
-      const double nlv = de * (te * g);
-      double lv = l_prev;
-      if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : wide(tpu[qr]);
-        lv = de * (tp * G.egu[qr]);
-        P.l_u[q] = lv;
-      }
-      P.nl_u[q] = nlv;
-      if (lfirst) P.old_u[q] = D.luse_bg ? -nlv - lv : -nlv;
-    } else if (lfirst) {
-      P.old_u[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
+    if (!inner && !D.periodic) return false;
+    const int kk = inner ? jk : 1, ka = inner ? jk - 1 : D.nx;
+    const long long qr = IX(D, ji, kk, jl);
+    double g = (ep[qr] - ep[IX(D, ji, ka, jl)]) * X.inv_dx[qr];
+    if (jl > D.nf) g -= G.slope_x[qr] * remapx(ji, kk, jl);
+    const double te = (D.theta_order == 2) ? 0.5 * (theta(ji, ka, jl) + theta(ji, kk, jl)) : wide(tvu[qr]);
+    const double de = wide(0.5f * (decel(ji, ka, jl) + decel(ji, kk, jl)));
+    *nlv = de * (te * g);
+    if (D.luse_bg) {
+      const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ji, ka, jl)] + S.tp[qr]) : wide(tpu[qr]);
+      *lv = de * (tp * G.egu[qr]);
     }
+    return true;
+  };
+  auto face_v = [&](double* nlv, double* lv) -> bool {
+    const bool inner = ji >= 2 && ji <= D.ny;
+    if (!inner && !D.periodic) return false;
+    const int ii = inner ? ji : 1, ia = inner ? ji - 1 : D.ny;
+    const long long qr = IX(D, ii, jk, jl);
+    double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
+    if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
+    const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : wide(tvv[qr]);
+    const double de = wide(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
+    *nlv = de * (te * g);
+    if (D.luse_bg) {
+      const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : wide(tpv[qr]);
+      *lv = de * (tp * G.egv[qr]);
+    }
+    return true;
+  };
+  // Both products are stored in FP64 (the reference's diagnostics).  With a background state
+  // the wind update uses only the net nl + l and the previous substep's -(nl + l), both rounded
+  // to FP32, so those are also kept in FP32 (net, old): the same values the update would round,
+  // read at a third of the bytes.  p_grad_acc_old is updated in that form only.  Without a
+  // background state nl alone carries the hydrostatic balance and the update reads the FP64
+  // arrays.
+  auto update = [&](const bool face, const double nlv, const double lv, double* nl, double* l, double* old,
+                    float* net_f, float* old_f, long long q) {
+    if (D.luse_bg) {
+      const float net_prev = net_f[q];
+      float o = -net_prev;
+      if (face) {
+        nl[q] = nlv;
+        l[q] = lv;
+        const float net = narrow(nlv + lv);
+        net_f[q] = net;
+        if (lfirst) o = -net;
+      }
+      old_f[q] = o;
+    } else {
+      const double nl_prev = nl[q];
+      if (!lfirst) old[q] = -nl_prev;
+      if (face) {
+        nl[q] = nlv;
+        if (lfirst) old[q] = -nlv;
+      } else if (lfirst) {
+        old[q] = -nl_prev;
+      }
+    }
+  };
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
+    double nlv = 0.0, lv = 0.0;
+    const bool face = face_u(&nlv, &lv);
+    update(face, nlv, lv, P.nl_u, P.l_u, P.old_u, PF.pnet_u, PF.pold_u, IX(D, ji, jk, jl));
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
-    const long long q = IX(D, ji, jk, jl);
-    const bool inner = ji >= 2 && ji <= D.ny;
-    const double nl_prev = P.nl_v[q], l_prev = P.l_v[q];
-    if (!lfirst) P.old_v[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
-    if (inner || D.periodic) {
-      const int ii = inner ? ji : 1, ia = inner ? ji - 1 : D.ny;
-      const long long qr = IX(D, ii, jk, jl);
-      double g = (ep[IX(D, ia, jk, jl)] - ep[qr]) * X.inv_dy[qr];
-      if (jl > D.nf) g -= G.slope_y[qr] * remapy(ii, jk, jl);
-      const double te = (D.theta_order == 2) ? 0.5 * (theta(ia, jk, jl) + theta(ii, jk, jl)) : wide(tvv[qr]);
-      const double de = wide(0.5f * (decel(ia, jk, jl) + decel(ii, jk, jl)));
-      const double nlv = de * (te * g);
-      double lv = l_prev;
-      if (D.luse_bg) {
-        const double tp = (D.theta_order == 2) ? 0.5 * (S.tp[IX(D, ia, jk, jl)] + S.tp[qr]) : wide(tpv[qr]);
-        lv = de * (tp * G.egv[qr]);
-        P.l_v[q] = lv;
-      }
-      P.nl_v[q] = nlv;
-      if (lfirst) P.old_v[q] = D.luse_bg ? -nlv - lv : -nlv;
-    } else if (lfirst) {
-      P.old_v[q] = D.luse_bg ? -nl_prev - l_prev : -nl_prev;
-    }
+    double nlv = 0.0, lv = 0.0;
+    const bool face = face_v(&nlv, &lv);
+    update(face, nlv, lv, P.nl_v, P.l_v, P.old_v, PF.pnet_v, PF.pold_v, IX(D, ji, jk, jl));
   }
   if (jl >= 2 && jl <= D.nl && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl), qa = IX(D, ji, jk, jl - 1);
     const float fa = cond_frac(qa), fb = cond_frac(q);
     const double de = wide(0.5f * ((float(kC_D_P) - float(kC_D_P) * fa) + (float(kC_D_P) - float(kC_D_P) * fb)));
-    P.nl_w[q] = de * (0.5 * (theta(ji, jk, jl - 1) + theta(ji, jk, jl)) * gzp(ji, jk, jl));
-    if (D.luse_bg) P.l_w[q] = de * (0.5 * (S.tp[qa] + S.tp[q]) * G.egw[q]);
+    const double nlw = de * (0.5 * (theta(ji, jk, jl - 1) + theta(ji, jk, jl)) * gzp(ji, jk, jl));
+    P.nl_w[q] = nlw;
+    if (D.luse_bg) {
+      const double lw = de * (0.5 * (S.tp[qa] + S.tp[q]) * G.egw[q]);
+      P.l_w[q] = lw;
+      PF.pnet_w[q] = narrow(nlw + lw);
+    }
     pgcw[q] = 0.5f * (-fa - fb) * float(G.gm[q]);
   }
 }
@@ -576,6 +609,50 @@ __global__ void __launch_bounds__(256, 6) ks_vort_flux(Dims D, Grid<float> G, St
                                                        const float* vph, const float* wph, float* px, float* py,
                                                        float* pz) {
   vort_flux_body<float, float>(D, G, S, ex, ey, ez, uph, vph, wph, px, py, pz);
+}
+
+// combination of the explicit wind tendencies, mo_vector_tend_expl.F90:258-310, and the
+// forward step of the horizontal wind, mo_manage_pchevi.F90:86-89 (FP64 state), split step:
+// the body of k_tend_wind<float> with the pressure-gradient terms of a background state read
+// in the FP32 form ks_pgrad keeps for it (net nl + l and the previous substep's -(nl + l), the
+// values k_tend_wind rounds to FP32 itself); without a background state the FP64 arrays.
+// mu, mv: the FP32 mirrors of the new u, v.
+__global__ void ks_tend_wind(Dims D, State So, State Sn, Tend<float> Tn, Carried<float> C, SplitCarriedF PF,
+                             int rk_step, float* mu, float* mv) {
+  LG_IDX3;
+  const float new_weight = (rk_step == 2) ? 0.5f : 1.f;
+  const float old_weight = 1.f - new_weight;
+  const double chw_d = 0.5 + kIMPL_THERMO_WEIGHT, ohw_d = 1.0 - (0.5 + kIMPL_THERMO_WEIGHT);
+  const double cvw_d = 1.0 - kIMPL_THERMO_WEIGHT, no_bg_d = D.luse_bg ? 0.0 : 1.0;
+  auto pg_h = [&](const float* old_f, const float* net_f, const double* old, const double* nl, const double* l,
+                  long long q) -> float {
+    if (D.luse_bg) return float(ohw_d) * old_f[q] - float(chw_d) * net_f[q];
+    return narrow(ohw_d * old[q] - chw_d * (nl[q] + l[q]));
+  };
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
+    const long long q = IX(D, ji, jk, jl);
+    const float t = old_weight * Tn.u[q] +
+                    new_weight * (pg_h(PF.pold_u, PF.pnet_u, C.old_u, C.nl_u, C.l_u, q) - 0.5f * C.vsg_x[q] + C.pvt_x[q]);
+    Tn.u[q] = t;
+    const double un = So.u[q] + D.dtime * wide(t);
+    Sn.u[q] = un;
+    mu[q] = narrow(un);
+  }
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    const float t = old_weight * Tn.v[q] +
+                    new_weight * (pg_h(PF.pold_v, PF.pnet_v, C.old_v, C.nl_v, C.l_v, q) - 0.5f * C.vsg_y[q] + C.pvt_y[q]);
+    Tn.v[q] = t;
+    const double vn = So.v[q] + D.dtime * wide(t);
+    Sn.v[q] = vn;
+    mv[q] = narrow(vn);
+  }
+  if (jl <= D.NL && ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    const float pg = D.luse_bg ? -(float(cvw_d) * PF.pnet_w[q])
+                               : narrow(-(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q]);
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (pg - 0.5f * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+  }
 }
 
 // ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
@@ -996,7 +1073,8 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
   }
   SplitCarriedF& C = s->C;
   float** car[] = {&C.pgcw, &C.vsg_x, &C.vsg_y, &C.vsg_z, &C.pvt_x, &C.pvt_y, &C.pvt_z, &C.csh, &C.rad, &C.temperature,
-                   &C.tend.rt, &C.tend.u, &C.tend.v, &C.tend.w};
+                   &C.tend.rt, &C.tend.u, &C.tend.v, &C.tend.w, &C.pnet_u, &C.pnet_v, &C.pnet_w, &C.pold_u,
+                   &C.pold_v};
   for (float** p : car) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &C.tend.rho, F * D.ncons, bytes))) return fail(rc);
   *out = s;
@@ -1011,6 +1089,11 @@ void split_destroy(SplitCtx* s) {
 
 SplitCarriedF split_carried(SplitCtx* s) { return s->C; }
 StateF split_mirror(SplitCtx* s, int slot) { return s->mir[slot]; }
+
+int split_net(const double* a, const double* b, float* net, long long n, cudaStream_t stream) {
+  k_net<<<1216, 256, 0, stream>>>(a, b, net, n);
+  return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
+}
 
 int split_convert(const double* src, float* dst, long long n, cudaStream_t stream) {
   k_to_float<<<1216, 256, 0, stream>>>(src, dst, n);
@@ -1141,7 +1224,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
       }
       SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl), B, D, G, s->GX, So.ep, s->gzd, s->rmz);
       SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, s->rmz, Mo.rho, s->tvu,
-         s->tvv, s->tpu, s->tpv, pg, C.pgcw, step == 0 ? 1 : 0);
+         s->tvv, s->tpu, s->tpv, pg, C, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
       SL("ks_eta_xy", ks_eta_xy, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
@@ -1157,7 +1240,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
            C.vsg_x, C.vsg_y);
       }
     }
-    SL("ks_tend_wind", k_tend_wind<float>, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, rk, Mn.u, Mn.v);
+    SL("ks_tend_wind", ks_tend_wind, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, C, rk, Mn.u, Mn.v);
     const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (D.ncons > 1)
       SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk);

@@ -24,6 +24,9 @@ struct SplitCtx;
 struct SplitCarriedF {
   float *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
   Tend<float> tend;
+  // with a background state: the net pressure-gradient terms nl + l of u, v, w and the previous
+  // substep's values -(nl + l) of u, v, rounded to FP32 (the only form the wind update uses)
+  float *pnet_u, *pnet_v, *pnet_w, *pold_u, *pold_v;
 };
 
 int split_create(const Dims& D, SplitCtx** out, long long* bytes);
@@ -32,6 +35,8 @@ void split_destroy(SplitCtx* s);
 int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream);
 // the FP32 carried buffers of the split step, for conversion to and from FP64 arrays
 SplitCarriedF split_carried(SplitCtx* s);
+// net = narrow(a + b) for n elements (the net pressure-gradient buffers from the FP64 arrays)
+int split_net(const double* a, const double* b, float* net, long long n, cudaStream_t stream);
 // converts n elements FP64 <-> FP32 (field layout identical)
 int split_convert(const double* src, float* dst, long long n, cudaStream_t stream);
 int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream);
