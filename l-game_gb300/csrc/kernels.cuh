@@ -391,10 +391,14 @@ __device__ __forceinline__ T trsk_v(const Dims& D, const Grid<T>& G, const T* up
 #undef EZ
 }
 
+// 3-D launches: blockIdx.x tiles the rows (ji), blockIdx.y is the level and blockIdx.z tiles
+// the columns (jk), so blocks launched one after another cover one level's row tiles and then
+// the same rows one level down: the vertical neighbours a stencil reads are still in L2
+// (with the columns in blockIdx.y they were a whole level plane of blocks apart)
 #define LG_IDX3                                              \
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;  \
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;  \
-  const int jl = blockIdx.z + 1
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;  \
+  const int jl = blockIdx.y + 1
 
 // ---- kernels --------------------------------------------------------------------
 
@@ -422,12 +426,12 @@ __global__ void k_theta(Dims D, Grid<T> G, const V* tp, T* out, int mode) {
   out[i] = mode == 0 ? G.theta_v_bg[i] + T(tp[i]) : T(tp[i]);
 }
 
-// grad_vert, mo_gradient_operators.F90:65-83 (levels 2..nl); launched with blockIdx.z = jl-2
+// grad_vert, mo_gradient_operators.F90:65-83 (levels 2..nl); launched with blockIdx.y = jl-2
 template <class T, class S>
 __global__ void k_grad_vert(Dims D, Grid<T> G, const S* s, T* rz) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 2;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 2;
   if (ji > D.ny || jk > D.nx || jl > D.nl) return;
   rz[IX(D, ji, jk, jl)] = cvt<T>(s[IX(D, ji, jk, jl - 1)] - s[IX(D, ji, jk, jl)]) / G.dz[IX(D, ji, jk, jl)];
 }

@@ -13,8 +13,8 @@ __global__ void k_pgrad(Dims D, Grid<double> G, State S, const double* gx, const
                         const double* tvu, const double* tvv, const double* tpu, const double* tpv,
                         PGrad<double> P, int lfirst) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
   const double use_bg_switch = D.luse_bg ? 1.0 : 0.0;
   auto theta = [&](int i, int j, int k) { const long long q = IX(D, i, j, k); return G.theta_v_bg[q] + S.tp[q]; };
   auto thetap = [&](int i, int j, int k) { return S.tp[IX(D, i, j, k)]; };

@@ -197,8 +197,8 @@ const double* device_view(const double* host) {
 __global__ void k_split_ipw(Dims D, const double* src, double* w1, double* w2, double* w3, double* w4,
                             double* w5, double* w6) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
   const size_t h = 6 * ((size_t)(ji - 1) + (size_t)D.ny * ((size_t)(jk - 1) + (size_t)D.nx * (size_t)(jl - 1)));
   const long long q = IX(D, ji, jk, jl);
@@ -207,8 +207,8 @@ __global__ void k_split_ipw(Dims D, const double* src, double* w1, double* w2, d
 
 __global__ void k_check_finite(Dims D, State S, int* flag) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
   bool bad = false;
   if (ji <= D.ny && jk <= D.nx && jl <= D.nl) {
     const long long q = IX(D, ji, jk, jl);
@@ -286,8 +286,9 @@ const auto k_column_tracers = lg::k_column_tracers;
 }  // namespace kd
 
 dim3 blk() { return dim3(32, 8, 1); }
+// x: row tiles, y: levels, z: column tiles (see LG_IDX3)
 dim3 grd(const Dims& D, int rows, int cols, int levs) {
-  return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 7) / 8), (unsigned)levs);
+  return dim3((unsigned)((rows + 31) / 32), (unsigned)levs, (unsigned)((cols + 7) / 8));
 }
 
 int klaunch_check(lgame_gpu* c, const char* what) {

@@ -258,8 +258,8 @@ __global__ void __launch_bounds__(256, 6) ks_pgrad(Dims D, Grid<double> G, GridX
 // term only where l < nl or with a free-slip surface), gz being 0 at levels 1 and nl+1
 __global__ void ks_gzp(Dims D, Grid<double> G, GridX X, const double* ep, double* gzd, double* rmz) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
-  const int jl = blockIdx.z + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
   if (ji > D.ny || jk > D.nx || jl > D.nl) return;
   const long long q = IX(D, ji, jk, jl);
   double gz = 0.0;
@@ -1029,8 +1029,9 @@ __global__ void ks_csh_sum(Dims D, const float* csh_part, float* csh) {
 }
 
 dim3 sblk() { return dim3(32, 8, 1); }
+// x: row tiles, y: levels, z: column tiles (see LG_IDX3)
 dim3 sgrd(int rows, int cols, int levs) {
-  return dim3((unsigned)((rows + 31) / 32), (unsigned)((cols + 7) / 8), (unsigned)levs);
+  return dim3((unsigned)((rows + 31) / 32), (unsigned)levs, (unsigned)((cols + 7) / 8));
 }
 // column kernels: 128 threads, 32 rows x 4 columns
 dim3 cblk() { return dim3(32, 4, 1); }
