@@ -263,6 +263,14 @@ void* lgame_gpu_stream(const lgame_gpu* ctx);
 int  lgame_gpu_set_profiling(lgame_gpu* ctx, int enable);
 int  lgame_gpu_profile_report(lgame_gpu* ctx, char* buf, int len);
 
+/* The step as a CUDA graph (on by default): after step 0 every call of lgame_gpu_pchevi for
+ * a given (old_slot, new_slot) pair launches the same kernels with the same arguments, so the
+ * library captures that sequence once per pair, at its first use, and then launches the
+ * graph: one host launch instead of about 30 (the split step: 31), which matters where the
+ * kernels are short (small grids).  Results are the same bits either way.  Graphs are not
+ * used while per-kernel tracing is on.  No counterpart in the reference (a CPU program). */
+int  lgame_gpu_set_graphs(lgame_gpu* ctx, int enable);
+
 /* Bytes of device memory held by the context. */
 long long lgame_gpu_device_bytes(const lgame_gpu* ctx);
 

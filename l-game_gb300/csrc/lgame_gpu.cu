@@ -63,6 +63,11 @@ struct lgame_gpu {
   Grid<double> G{};
   SplitCtx* split = nullptr;
   bool mirror_valid[2] = {false, false};  // split mode: FP32 mirror of the slot matches its FP64 state
+  // the step as a CUDA graph, one per (old, new) slot pair, captured at its first use after
+  // step 0 (every later step launches the same kernels with the same arguments)
+  bool use_graphs = true;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_kernels[2] = {0, 0};
   // per-kernel tracing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -725,19 +730,51 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
   c->kernels_last_step = 0;
   int rc;
   if (c->split) {
-    PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v,
-                    c->pgcw};
     for (int slot : {old_slot, new_slot}) {
       if (c->mirror_valid[slot]) continue;
       if ((rc = split_refresh_mirror(c->split, c->D, slot, c->st[slot], c->stream)) != LGAME_OK)
         return set_err(rc, "lgame_gpu_pchevi: refresh of the FP32 state mirror failed");
       c->mirror_valid[slot] = true;
     }
-    rc = split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
-                    total_step_counter, c->stream, &c->kernels_last_step,
-                    c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
+  }
+  auto launch_step = [&]() -> int {
+    if (c->split) {
+      PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v,
+                      c->pgcw};
+      return split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
+                        total_step_counter, c->stream, &c->kernels_last_step,
+                        c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
+    }
+    return step_fp64(c, old_slot, new_slot, total_step_counter);
+  };
+  // After step 0 a step is the same sequence of launches for a given slot pair, so it runs as
+  // a CUDA graph (one launch from the host instead of ~30).  Not with per-kernel tracing,
+  // whose events are recorded between the launches.
+  if (c->use_graphs && !c->profiling && total_step_counter > 0) {
+    cudaGraphExec_t& exec = c->graph[old_slot];
+    if (!exec) {
+      CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      rc = launch_step();
+      cudaGraph_t graph = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+      if (rc != LGAME_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+      }
+      if (e != cudaSuccess) return set_err(LGAME_ERR_CUDA, std::string("capture of the step: ") + cudaGetErrorString(e));
+      const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (ei != cudaSuccess) {
+        exec = nullptr;
+        return set_err(LGAME_ERR_CUDA, std::string("instantiation of the step graph: ") + cudaGetErrorString(ei));
+      }
+      c->graph_kernels[old_slot] = c->kernels_last_step;
+    }
+    CK(cudaGraphLaunch(exec, c->stream));
+    c->kernels_last_step = c->graph_kernels[old_slot];
+    rc = LGAME_OK;
   } else {
-    rc = step_fp64(c, old_slot, new_slot, total_step_counter);
+    rc = launch_step();
   }
   if (rc != LGAME_OK) return rc;
   if (c->cfg.check_finite) {
@@ -862,6 +899,12 @@ void trace_end(lgame_gpu* c, int slot) { cudaEventRecord(c->ev_pool[slot + 1], c
 
 extern "C" void* lgame_gpu_stream(const lgame_gpu* c) { return c ? (void*)c->stream : nullptr; }
 
+extern "C" int lgame_gpu_set_graphs(lgame_gpu* c, int enable) {
+  if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_graphs: null context");
+  c->use_graphs = enable != 0;
+  return LGAME_OK;
+}
+
 extern "C" int lgame_gpu_set_profiling(lgame_gpu* c, int enable) {
   if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_profiling: null context");
   c->profiling = enable != 0;
@@ -900,6 +943,7 @@ extern "C" long long lgame_gpu_device_bytes(const lgame_gpu* c) { return c ? c->
 extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (cudaGraphExec_t g : c->graph) if (g) cudaGraphExecDestroy(g);
   if (c->split) split_destroy(c->split);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (void* p : c->allocations) cudaFree(p);

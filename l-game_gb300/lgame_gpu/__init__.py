@@ -124,6 +124,7 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_device_bytes": (ll, [vp]),
         "lgame_gpu_stream": (vp, [vp]),
         "lgame_gpu_set_profiling": (i, [vp, i]),
+        "lgame_gpu_set_graphs": (i, [vp, i]),
         "lgame_gpu_profile_report": (i, [vp, C.c_char_p, i]),
         "lgame_gpu_destroy": (None, [vp]),
         "lgame_gpu_last_error": (C.c_char_p, []),
@@ -339,6 +340,10 @@ class GpuModel:
 
     def set_profiling(self, enable: bool):
         check(self.lib.lgame_gpu_set_profiling(self.h, 1 if enable else 0), "lgame_gpu_set_profiling")
+
+    def set_graphs(self, enable: bool):
+        """Launch each step after step 0 as a captured CUDA graph (the default) or kernel by kernel."""
+        check(self.lib.lgame_gpu_set_graphs(self.h, 1 if enable else 0), "lgame_gpu_set_graphs")
 
     def profile_report(self) -> dict:
         import json
