@@ -2,14 +2,13 @@
 // BF16 tensor-core kernels (tcgen05.mma, accumulators in tensor memory).
 //
 // GEMM kernel: one CTA of 128 threads computes a 128 x BN tile of C = A * B^T (A: M x K,
-// B: N x K, both K-major BF16).  Per K block of 64 the threads stage the A and B tiles in
-// shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core
-// matrices: element (r, k) at (r/8)*1024 + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes), one
-// elected thread issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and
-// an FP32 accumulator in BN columns of tensor memory) and commits them to the stage's
-// mbarrier.  Three stages filled with cp.async: while the tensor core works on one K block
-// the copies of the next two are in flight; a stage is refilled only after the commit of the
-// MMAs that read it (bounded wait).  The epilogue reads the
+// B: N x K, both K-major BF16).  The K blocks of 64 reach shared memory by TMA
+// (cp.async.bulk.tensor, 128-byte swizzle: 8-row x 128-byte atoms, 16-byte chunks XOR-ed by
+// the row), issued by one producer thread into a three-stage ring; one MMA thread waits for
+// a stage to fill, issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and
+// an FP32 accumulator in BN columns of tensor memory; the K=16 steps advance the descriptors
+// 32 bytes inside the swizzle atom) and commits them to the stage's "empty" mbarrier, which
+// releases it to the producer.  A last commit signals the epilogue, which reads the
 // accumulator with tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31 = tile rows) and
 // applies one of the fused epilogues (bias + GELU with BF16 and transposed BF16 copies,
 // bias only, GELU derivative for the backward pass, or plain FP32 partial sums for split-K).
@@ -20,6 +19,7 @@
 #include "common.h"
 #include "emulator.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -39,15 +39,29 @@ typedef __nv_bfloat16 bf16;
 // ---- tcgen05 / mbarrier primitives (inline PTX) ---------------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-// shared-memory matrix descriptor: start address, leading (K) and stride (M/N) byte
-// offsets between core matrices, fixed version bits 46-48 = 0b001, no swizzle
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+// shared-memory matrix descriptor of a K-major tile of 8-row x 128-byte atoms with the
+// 128-byte swizzle: start address >> 4, stride 1024 bytes between 8-row groups (bits 32-45),
+// fixed version bits 46-48 = 0b001, layout type 2 at bits 61-63; the leading offset (bits
+// 16-29) is not used when a row of the tile is one atom wide
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024u >> 4) << 32;
   d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
   return d;
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+// one box of a 2-D tensor map (inner coordinate c0, outer c1) into shared memory, completing
+// on the mbarrier's transaction count
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(map), "r"(c0), "r"(c1), "r"(mbar)
+      : "memory");
 }
 // instruction descriptor, kind::f16: D = F32 (bits 4-5 = 1), A = B = BF16 (bits 7-9, 10-12 = 1),
 // both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28
@@ -74,7 +88,6 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
 }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -115,97 +128,77 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 // ---- the GEMM -------------------------------------------------------------------------------
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
 constexpr int kStages = 3;
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B,
-                                                 int ldb, int M, int N, int K, int kchunk, Epi ep, int* err) {
+__global__ void __launch_bounds__(128, 1) k_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                 const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
+                                                 int kchunk, Epi ep, int* err) {
   constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;
-  constexpr int kStage = 128 * 64 * 2 + BN * 64 * 2;  // A tile (16 KB) + B tile per stage
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t mbar[kStages];
+  constexpr uint32_t kA = 128 * 64 * 2, kB = BN * 64 * 2, kStage = kA + kB;  // bytes per stage
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kStages], empty[kStages], done;
   __shared__ uint32_t tmem_base;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int n0 = blockIdx.x * BN, m0 = blockIdx.y * 128;
   const int k0 = blockIdx.z * kchunk, k1 = min(K, k0 + kchunk);
-  const int nk = (k1 - k0 + 63) / 64;
-  const uint32_t sbase = smem_u32(smem);
+  const int nk = (k1 - k0) / 64;
+  const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;  // swizzle atoms are 1024-byte aligned
   if (warp == 0) tc_alloc(smem_u32(&tmem_base), kCols);
-  if (tid == 0)
-    for (int i = 0; i < kStages; ++i) mbar_init(smem_u32(&mbar[i]), 1);
+  if (tid == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(smem_u32(&full[i]), 1);
+      mbar_init(smem_u32(&empty[i]), 1);
+    }
+    mbar_init(smem_u32(&done), 1);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = tmem_base;
-  const uint32_t idesc = instr_desc(128, BN);
-  // asynchronous copies of K block kb into stage st, in core-matrix order
-  auto load = [&](int kb, int st) {
-    const uint32_t a = sbase + st * kStage, b = a + 128 * 64 * 2;
-    for (int c = tid; c < 128 * 8; c += 128) {
-      const int r = c >> 3, kc = c & 7;
-      cp_async16(a + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, A + (size_t)(m0 + r) * lda + kb + kc * 8);
-    }
-    for (int c = tid; c < BN * 8; c += 128) {
-      const int r = c >> 3, kc = c & 7;
-      cp_async16(b + (r >> 3) * 1024 + kc * 128 + (r & 7) * 16, B + (size_t)(n0 + r) * ldb + kb + kc * 8);
-    }
-  };
-  uint32_t ph[kStages] = {};
   bool failed = false;
-  // prologue: the first kStages-1 blocks in flight (one copy group per block, empty ones too)
-  for (int i = 0; i < kStages - 1; ++i) {
-    if (i < nk) load(k0 + 64 * i, i);
-    cp_async_commit();
-  }
-  int it = 0;
-  for (; it < nk; ++it) {
-    const int st = it % kStages;
-    // refill the stage of block it-1 with block it+kStages-1 once its MMAs have finished
-    const int nxt = it + kStages - 1;
-    if (it >= 1 && nxt < nk) {
-      const int sp = (it - 1) % kStages;
-      const bool ok = mbar_wait(smem_u32(&mbar[sp]), ph[sp]);
-      if (__syncthreads_or(!ok)) { failed = true; break; }  // ph[sp] still names the pending phase
-      ph[sp] ^= 1u;
-    }
-    if (nxt < nk) load(k0 + 64 * nxt, nxt % kStages);
-    cp_async_commit();
-    cp_async_wait<kStages - 1>();  // block it has landed
-    fence_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      tc_fence_after();
-      const uint32_t aS = sbase + st * kStage, bS = aS + 128 * 64 * 2;
-#pragma unroll
-      for (int s = 0; s < 4; ++s) {  // K = 16 per instruction: two core matrices along K
-        const uint64_t ad = smem_desc(aS + s * 256, 128, 1024);
-        const uint64_t bd = smem_desc(bS + s * 256, 128, 1024);
-        tc_mma(tmem, ad, bd, idesc, (it > 0 || s > 0) ? 1u : 0u);
+  if (warp == 0 && lane == 0) {
+    // producer: K block it into stage it % kStages once the MMAs of block it - kStages released it
+    int issued = 0;
+    for (; issued < nk; ++issued) {
+      const int st = issued % kStages;
+      if (issued >= kStages && !mbar_wait(smem_u32(&empty[st]), (uint32_t)((issued / kStages - 1) & 1))) {
+        failed = true;
+        break;
       }
-      tc_commit(smem_u32(&mbar[st]));
+      const uint32_t a = sbase + st * kStage;
+      mbar_arrive_expect_tx(smem_u32(&full[st]), kStage);
+      tma_load_2d(a, &tmA, k0 + 64 * issued, m0, smem_u32(&full[st]));
+      tma_load_2d(a + kA, &tmB, k0 + 64 * issued, n0, smem_u32(&full[st]));
     }
+    // after a time-out, wait (bounded) for the copies still in flight before the CTA exits
+    if (failed)
+      for (int it = max(0, issued - kStages); it < issued; ++it)
+        mbar_wait(smem_u32(&full[it % kStages]), (uint32_t)((it / kStages) & 1));
+  } else if (warp == 1 && lane == 0) {
+    // MMA thread: four K=16 steps per block, the block's stage released by its commit
+    const uint32_t idesc = instr_desc(128, BN);
+    for (int it = 0; it < nk; ++it) {
+      const int st = it % kStages;
+      if (!mbar_wait(smem_u32(&full[st]), (uint32_t)((it / kStages) & 1))) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a = sbase + st * kStage;
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+        tc_mma(tmem, smem_desc_sw128(a + s * 32), smem_desc_sw128(a + kA + s * 32), idesc, (it > 0 || s > 0) ? 1u : 0u);
+      tc_commit(smem_u32(&empty[st]));
+    }
+    // arrives once every tensor-core operation issued above has completed (also after a failure)
+    tc_commit(smem_u32(&done));
   }
-  cp_async_wait<0>();
-  // the last commit completes after every earlier tensor-core operation of this thread;
-  // its phase: the number of earlier waits on that stage (all earlier uses were waited on)
-  const int last = it - 1;
-  if (last >= 0) {
-    const int st = last % kStages;
-    const bool ok = mbar_wait(smem_u32(&mbar[st]), ph[st]);
-    if (__syncthreads_or(!ok)) failed = true;
-  }
+  __syncwarp();
+  const bool ok = mbar_wait(smem_u32(&done), 0);
   tc_fence_after();
-  if (failed) {
+  if (__syncthreads_or(failed || !ok)) {
     if (tid == 0) atomicExch(err, 1);
-    // bounded: let this block's last committed tensor-core work drain before the memory is freed
-    if (it > 0) mbar_wait(smem_u32(&mbar[(it - 1) % kStages]), ph[(it - 1) % kStages]);
   } else {
     const int m = m0 + warp * 32 + lane;  // tile row of this thread
     for (int c = 0; c < BN; c += 16) {
@@ -265,19 +258,53 @@ __global__ void __launch_bounds__(128, 1) k_gemm(const bf16* __restrict__ A, int
   if (warp == 0) tc_dealloc(tmem, kCols);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+// tensor map of a K-major BF16 matrix (rows x K, leading dimension ld elements) in boxes of
+// 64 (K) x box_rows with the 128-byte swizzle; the encoder rejects unaligned bases and strides
+int tensor_map(CUtensorMap* map, const bf16* base, int rows, int K, int ld, int box_rows) {
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return LGAME_ERR_CUDA;
+  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
+  const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
+  const cuuint32_t estride[2] = {1u, 1u};
+  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estride,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? LGAME_OK : LGAME_ERR_INVALID_ARG;
+}
+
 template <int BN>
 int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
                    int* err, cudaStream_t st) {
-  const size_t shm = kStages * ((size_t)128 * 64 * 2 + (size_t)BN * 64 * 2);
+  const size_t shm = kStages * ((size_t)128 * 64 * 2 + (size_t)BN * 64 * 2) + 1024;  // + alignment slack
   static bool attr_set = false;
   if (!attr_set) {
     if (cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
       return LGAME_ERR_CUDA;
     attr_set = true;
   }
+  CUtensorMap ma, mb;
+  int rc = tensor_map(&ma, A, M, K, lda, 128);
+  if (rc == LGAME_OK) rc = tensor_map(&mb, B, N, K, ldb, BN);
+  if (rc != LGAME_OK) return rc;
   const int kchunk = ((K / splits + 63) / 64) * 64;
   const dim3 grid((unsigned)(N / BN), (unsigned)(M / 128), (unsigned)((K + kchunk - 1) / kchunk));
-  k_gemm<BN><<<grid, 128, shm, st>>>(A, lda, B, ldb, M, N, K, kchunk, ep, err);
+  k_gemm<BN><<<grid, 128, shm, st>>>(ma, mb, M, N, K, kchunk, ep, err);
   return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
 }
 
