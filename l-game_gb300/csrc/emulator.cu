@@ -329,16 +329,25 @@ int launch_gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, in
 }
 
 // ---- element-wise and reduction kernels ------------------------------------------------------
-// standardised, zero-padded BF16 inputs, row-major and transposed
-__global__ void k_prep_x(const float* __restrict__ x, int nin, int nin_pad, int batch, const float* mean,
-                         const float* istd, bf16* X, bf16* XT) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= batch * nin_pad) return;
-  const int r = i / nin_pad, c = i % nin_pad;
-  const float v = (c < nin) ? (x[(size_t)r * nin + c] - mean[c]) * istd[c] : 0.f;
-  const bf16 b = __float2bfloat16_rn(v);
-  X[i] = b;
-  XT[(size_t)c * batch + r] = b;
+// Kernels that write a matrix and its transpose work on 32 x 32 tiles (blocks of 32 x 8
+// threads): a warp reads and writes a row of the tile, and the transposed copy goes out
+// through shared memory, so that both sides are coalesced.
+//
+// standardised, zero-padded BF16 inputs, row-major and transposed; grid (nin_pad/32, batch/32)
+__global__ void __launch_bounds__(256) k_prep_x(const float* __restrict__ x, int nin, int nin_pad, int batch,
+                                                const float* mean, const float* istd, bf16* X, bf16* XT) {
+  __shared__ bf16 t[32][34];
+  const int c = blockIdx.x * 32 + threadIdx.x, r0 = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const int r = r0 + j;
+    const float v = (c < nin) ? (x[(size_t)r * nin + c] - mean[c]) * istd[c] : 0.f;
+    const bf16 b = __float2bfloat16_rn(v);
+    X[(size_t)r * nin_pad + c] = b;
+    t[j][threadIdx.x] = b;
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8)
+    XT[(size_t)(blockIdx.x * 32 + j) * batch + r0 + threadIdx.x] = t[threadIdx.x][j];
 }
 __global__ void k_prep_y(const float* __restrict__ y, int nout, int nout_pad, int batch, const float* mean,
                          const float* istd, float* Yt) {
@@ -347,47 +356,62 @@ __global__ void k_prep_y(const float* __restrict__ y, int nout, int nout_pad, in
   const int r = i / nout_pad, c = i % nout_pad;
   Yt[i] = (c < nout) ? (y[(size_t)r * nout + c] - mean[c]) * istd[c] : 0.f;
 }
-// loss partial sums per block and the output gradient dL/dY = 2 (Y - Yt) / (batch * nout)
-__global__ void k_loss_dy(const float* Y, const float* Yt, int nout, int nout_pad, int batch, float* d32, bf16* db,
-                          bf16* dbt, float* part) {
+// loss partial sums per tile and the output gradient dL/dY = 2 (Y - Yt) / (batch * nout),
+// in FP32, BF16 and transposed BF16; grid (nout_pad/32, batch/32), one partial per block
+__global__ void __launch_bounds__(256) k_loss_dy(const float* Y, const float* Yt, int nout, int nout_pad, int batch,
+                                                 float* d32, bf16* db, bf16* dbt, float* part) {
+  __shared__ bf16 t[32][34];
   __shared__ float sh[256];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blockIdx.x * 32 + threadIdx.x, r0 = blockIdx.y * 32;
+  const float scale = 2.f / (float)((double)batch * nout);
   float l = 0.f;
-  if (i < batch * nout_pad) {
-    const int r = i / nout_pad, c = i % nout_pad;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    const size_t i = (size_t)(r0 + j) * nout_pad + c;
     float d = 0.f;
     if (c < nout) {
       const float e = Y[i] - Yt[i];
-      l = e * e;
-      d = 2.f * e / (float)((double)batch * nout);
+      l += e * e;
+      d = e * scale;
     }
     d32[i] = d;
     const bf16 b = __float2bfloat16_rn(d);
     db[i] = b;
-    dbt[(size_t)c * batch + r] = b;
+    t[j][threadIdx.x] = b;
   }
-  sh[threadIdx.x] = l;
+  const int tid = threadIdx.y * 32 + threadIdx.x;
+  sh[tid] = l;
   __syncthreads();
-  for (int s = 128; s > 0; s >>= 1) {
-    if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+  for (int j = threadIdx.y; j < 32; j += 8)
+    dbt[(size_t)(blockIdx.x * 32 + j) * batch + r0 + threadIdx.x] = t[threadIdx.x][j];
+  for (int w = 128; w > 0; w >>= 1) {
+    if (tid < w) sh[tid] += sh[tid + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+  if (tid == 0) part[blockIdx.y * gridDim.x + blockIdx.x] = sh[0];
 }
-// deterministic sums: column sums of a rows x cols matrix (one block per column), and the
-// sum of a vector (one block)
-__global__ void k_colsum(const float* a, int rows, int cols, float* out) {
-  __shared__ float sh[256];
-  const int c = blockIdx.x;
+// deterministic column sums of a rows x cols matrix in two passes: partial sums of 32
+// columns over one chunk of rows per block (grid (cols/32, chunks), warps read rows), then
+// the chunks' partials summed in order
+__global__ void __launch_bounds__(256) k_colsum_part(const float* a, int rows, int cols, float* part) {
+  __shared__ float sh[8][33];
+  const int c = blockIdx.x * 32 + threadIdx.x;
+  const int per = rows / gridDim.y, r0 = blockIdx.y * per;
   float s = 0.f;
-  for (int r = threadIdx.x; r < rows; r += 256) s += a[(size_t)r * cols + c];
-  sh[threadIdx.x] = s;
+  for (int r = r0 + threadIdx.y; r < r0 + per; r += 8) s += a[(size_t)r * cols + c];
+  sh[threadIdx.y][threadIdx.x] = s;
   __syncthreads();
-  for (int k = 128; k > 0; k >>= 1) {
-    if ((int)threadIdx.x < k) sh[threadIdx.x] += sh[threadIdx.x + k];
-    __syncthreads();
+  if (threadIdx.y == 0) {
+    float t = sh[0][threadIdx.x];
+    for (int k = 1; k < 8; ++k) t += sh[k][threadIdx.x];
+    part[(size_t)blockIdx.y * cols + c] = t;
   }
-  if (threadIdx.x == 0) out[c] = sh[0];
+}
+__global__ void k_colsum_fin(const float* part, int chunks, int cols, float* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= cols) return;
+  float s = 0.f;
+  for (int k = 0; k < chunks; ++k) s += part[(size_t)k * cols + c];
+  out[c] = s;
 }
 // split-K partials of dW^T (in x out) summed and written transposed as dW (out x in)
 __global__ void k_splitk_reduce_t(const float* part, int splits, int rows_in, int cols_out, float* gw) {
@@ -446,6 +470,21 @@ __global__ void k_gather_rows(const float* src, const long long* idx, int batch,
   dst[i] = src[idx[r] * ncol + c];
 }
 
+// the loss partials of one batch summed in FP64 into out[0] (one block of 256 threads),
+// so that an epoch keeps every batch's loss on the device until its end
+__global__ void k_loss_total(const float* part, int n, double* out) {
+  __shared__ double sh[256];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += part[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = sh[0];
+}
+
 __global__ void k_fill_pattern(bf16* a, long long n, int salt) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i < n) a[i] = __float2bfloat16_rn((float)((i * 2654435761LL + salt) % 2001 - 1000) * 1e-3f);
@@ -465,7 +504,7 @@ struct lgame_emu {
   float *W[4], *b[4], *gW[4], *gb[4], *mW[4], *vW[4], *mb[4], *vb[4];
   bf16 *Wb[4], *WTb[4];
   float *xmean, *xistd, *ymean, *ystd, *yistd;
-  float *xraw, *yraw, *Yt, *Y, *Z[3], *dZ32[4], *part, *lpart, *yout;
+  float *xraw, *yraw, *Yt, *Y, *Z[3], *dZ32[4], *part, *lpart, *cpart, *yout;
   bf16 *X, *XT, *H[3], *HT[3], *dZb[4], *dZT[4];
   int* err = nullptr;
   long long adam_t = 0;
@@ -473,7 +512,8 @@ struct lgame_emu {
   // dataset on the device
   float *dsx = nullptr, *dsy = nullptr;
   long long dsn = 0;
-  long long* idx = nullptr;
+  long long* idx = nullptr;  // one epoch's shuffled order (dsn entries)
+  double* lsum = nullptr;    // per-batch loss sums of one epoch (dsn / 128 entries)
   // statistics
   long long gemm_launches = 0;
   double gemm_flop = 0.0;
@@ -547,8 +587,8 @@ int forward(lgame_emu* e, int batch) {
 
 // prepared inputs from host or device raw rows
 int prep_x(lgame_emu* e, const float* xraw_dev, int batch) {
-  k_prep_x<<<blocks((long long)batch * e->nin_pad), 256, 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, e->xmean,
-                                                                      e->xistd, e->X, e->XT);
+  k_prep_x<<<dim3(e->nin_pad / 32, batch / 32), dim3(32, 8), 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, e->xmean,
+                                                                        e->xistd, e->X, e->XT);
   ECK(cudaGetLastError());
   return LGAME_OK;
 }
@@ -556,8 +596,9 @@ int prep_x(lgame_emu* e, const float* xraw_dev, int batch) {
 // loss and gradients of one prepared batch (X, XT, Yt); grads in gW, gb; loss partials in lpart
 int backward(lgame_emu* e, int batch, int* nparts) {
   const int Hd = e->hidden, no = e->nout_pad;
-  const int np = (int)blocks((long long)batch * no);
-  k_loss_dy<<<np, 256, 0, e->st>>>(e->Y, e->Yt, e->nout, no, batch, e->dZ32[3], e->dZb[3], e->dZT[3], e->lpart);
+  const int np = (no / 32) * (batch / 32);
+  k_loss_dy<<<dim3(no / 32, batch / 32), dim3(32, 8), 0, e->st>>>(e->Y, e->Yt, e->nout, no, batch, e->dZ32[3], e->dZb[3],
+                                                                  e->dZT[3], e->lpart);
   ECK(cudaGetLastError());
   *nparts = np;
   for (int l = 3; l >= 0; --l) {
@@ -576,7 +617,9 @@ int backward(lgame_emu* e, int batch, int* nparts) {
     const int zs = (batch + kchunk - 1) / kchunk;
     k_splitk_reduce_t<<<blocks((long long)nin_l * nout_l), 256, 0, e->st>>>(e->part, zs, nin_l, nout_l, e->gW[l]);
     ECK(cudaGetLastError());
-    k_colsum<<<nout_l, 256, 0, e->st>>>(e->dZ32[l], batch, nout_l, e->gb[l]);
+    const int chunks = batch / 128;  // rows per chunk: 128
+    k_colsum_part<<<dim3(nout_l / 32, chunks), dim3(32, 8), 0, e->st>>>(e->dZ32[l], batch, nout_l, e->cpart);
+    k_colsum_fin<<<blocks(nout_l), 256, 0, e->st>>>(e->cpart, chunks, nout_l, e->gb[l]);
     ECK(cudaGetLastError());
     if (l == 0) break;
     // dZ_{l-1} = (dZ_l * W_l) .* gelu'(Z_{l-1}): A = dZ_l (batch x out), B = W_l^T (in x out)
@@ -728,7 +771,8 @@ extern "C" int lgame_emu_create(int nlev, int hidden, int batch_max, unsigned lo
   }
   size_t pmax = 0;
   for (int l = 0; l < 4; ++l) pmax = std::max(pmax, (size_t)rows[l] * cols[l]);
-  if ((rc = ealloc(e, &e->part, pmax * e->splits)) || (rc = ealloc(e, &e->lpart, B * e->nout_pad / 256 + 1)))
+  if ((rc = ealloc(e, &e->part, pmax * e->splits)) || (rc = ealloc(e, &e->lpart, B * e->nout_pad / 256 + 1)) ||
+      (rc = ealloc(e, &e->cpart, (B / 128) * std::max((size_t)Hd, (size_t)e->nout_pad))))
     return fail(rc);
   // identity normalisation, Xavier-uniform weights (splitmix64), zero biases
   std::vector<float> one(std::max(e->nin, e->nout), 1.f);
@@ -765,6 +809,7 @@ extern "C" void lgame_emu_destroy(lgame_emu* e) {
   if (e->dsx) cudaFree(e->dsx);
   if (e->dsy) cudaFree(e->dsy);
   if (e->idx) cudaFree(e->idx);
+  if (e->lsum) cudaFree(e->lsum);
   if (e->st) cudaStreamDestroy(e->st);
   delete e;
 }
@@ -877,11 +922,14 @@ extern "C" int lgame_emu_set_dataset(lgame_emu* e, const float* x, const float* 
   if (e->dsx) cudaFree(e->dsx);
   if (e->dsy) cudaFree(e->dsy);
   if (e->idx) cudaFree(e->idx);
+  if (e->lsum) cudaFree(e->lsum);
   e->dsx = e->dsy = nullptr;
   e->idx = nullptr;
+  e->lsum = nullptr;
   ECK(cudaMalloc(&e->dsx, sizeof(float) * (size_t)n * e->nin));
   ECK(cudaMalloc(&e->dsy, sizeof(float) * (size_t)n * e->nout));
-  ECK(cudaMalloc(&e->idx, sizeof(long long) * (size_t)e->bmax));
+  ECK(cudaMalloc(&e->idx, sizeof(long long) * (size_t)n));
+  ECK(cudaMalloc(&e->lsum, sizeof(double) * (size_t)(n / 128 + 1)));
   ECK(cudaMemcpy(e->dsx, x, sizeof(float) * (size_t)n * e->nin, cudaMemcpyHostToDevice));
   ECK(cudaMemcpy(e->dsy, y, sizeof(float) * (size_t)n * e->nout, cudaMemcpyHostToDevice));
   e->dsn = n;
@@ -904,11 +952,13 @@ extern "C" int lgame_emu_train_epoch(lgame_emu* e, int batch, float lr, unsigned
   };
   for (long long i = e->dsn - 1; i > 0; --i) std::swap(perm[i], perm[(long long)(next() % (uint64_t)(i + 1))]);
   const long long nb = e->dsn / batch;
-  double acc = 0.0;
+  // the whole order goes up once and every batch's loss stays on the device: the batches are
+  // enqueued back to back with one synchronisation at the end of the epoch
+  ECK(cudaMemcpyAsync(e->idx, perm.data(), sizeof(long long) * (size_t)e->dsn, cudaMemcpyHostToDevice, e->st));
   for (long long k = 0; k < nb; ++k) {
-    ECK(cudaMemcpyAsync(e->idx, perm.data() + k * batch, sizeof(long long) * batch, cudaMemcpyHostToDevice, e->st));
-    k_gather_rows<<<blocks((long long)batch * e->nin), 256, 0, e->st>>>(e->dsx, e->idx, batch, e->nin, e->xraw);
-    k_gather_rows<<<blocks((long long)batch * e->nout), 256, 0, e->st>>>(e->dsy, e->idx, batch, e->nout, e->yraw);
+    const long long* idx = e->idx + k * batch;
+    k_gather_rows<<<blocks((long long)batch * e->nin), 256, 0, e->st>>>(e->dsx, idx, batch, e->nin, e->xraw);
+    k_gather_rows<<<blocks((long long)batch * e->nout), 256, 0, e->st>>>(e->dsy, idx, batch, e->nout, e->yraw);
     ECK(cudaGetLastError());
     int rc = prep_x(e, e->xraw, batch);
     if (rc) return rc;
@@ -918,13 +968,18 @@ extern "C" int lgame_emu_train_epoch(lgame_emu* e, int batch, float lr, unsigned
     int np = 0;
     if (!rc) rc = backward(e, batch, &np);
     if (!rc) rc = adam(e, lr);
-    float l = 0.f;
-    if (!rc) rc = loss_from_parts(e, np, batch, &l);
     if (rc) return rc;
-    acc += l;
+    k_loss_total<<<1, 256, 0, e->st>>>(e->lpart, np, e->lsum + k);
+    ECK(cudaGetLastError());
   }
+  std::vector<double> ls((size_t)nb);
+  if (nb) ECK(cudaMemcpyAsync(ls.data(), e->lsum, sizeof(double) * (size_t)nb, cudaMemcpyDeviceToHost, e->st));
+  const int rc = check_err(e);  // synchronises the stream
+  if (rc) return rc;
+  double acc = 0.0;
+  for (long long k = 0; k < nb; ++k) acc += (float)(ls[(size_t)k] / ((double)batch * e->nout));
   if (mean_loss) *mean_loss = nb ? (float)(acc / nb) : 0.f;
-  return check_err(e);
+  return LGAME_OK;
 }
 
 extern "C" int lgame_emu_infer(lgame_emu* e, const float* x, long long n, float* y) {
