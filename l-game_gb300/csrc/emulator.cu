@@ -333,14 +333,15 @@ int launch_gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, in
 // threads): a warp reads and writes a row of the tile, and the transposed copy goes out
 // through shared memory, so that both sides are coalesced.
 //
-// standardised, zero-padded BF16 inputs, row-major and transposed; grid (nin_pad/32, batch/32)
+// standardised, zero-padded BF16 inputs, row-major and transposed; grid (nin_pad/32, batch/32);
+// rows >= valid (padding of the last batch) are zero and not read
 __global__ void __launch_bounds__(256) k_prep_x(const float* __restrict__ x, int nin, int nin_pad, int batch,
-                                                const float* mean, const float* istd, bf16* X, bf16* XT) {
+                                                int valid, const float* mean, const float* istd, bf16* X, bf16* XT) {
   __shared__ bf16 t[32][34];
   const int c = blockIdx.x * 32 + threadIdx.x, r0 = blockIdx.y * 32;
   for (int j = threadIdx.y; j < 32; j += 8) {
     const int r = r0 + j;
-    const float v = (c < nin) ? (x[(size_t)r * nin + c] - mean[c]) * istd[c] : 0.f;
+    const float v = (c < nin && r < valid) ? (x[(size_t)r * nin + c] - mean[c]) * istd[c] : 0.f;
     const bf16 b = __float2bfloat16_rn(v);
     X[(size_t)r * nin_pad + c] = b;
     t[j][threadIdx.x] = b;
@@ -585,10 +586,11 @@ int forward(lgame_emu* e, int batch) {
   return gemm(e, in, Hd, e->Wb[3], Hd, batch, e->nout_pad, Hd, 1, ep);
 }
 
-// prepared inputs from host or device raw rows
-int prep_x(lgame_emu* e, const float* xraw_dev, int batch) {
-  k_prep_x<<<dim3(e->nin_pad / 32, batch / 32), dim3(32, 8), 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, e->xmean,
-                                                                        e->xistd, e->X, e->XT);
+// prepared inputs of `batch` rows (a multiple of 128) from raw rows the GPU can read (device
+// memory or page-locked host memory), of which the first `valid` hold data
+int prep_x(lgame_emu* e, const float* xraw_dev, int batch, int valid) {
+  k_prep_x<<<dim3(e->nin_pad / 32, batch / 32), dim3(32, 8), 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, valid,
+                                                                        e->xmean, e->xistd, e->X, e->XT);
   ECK(cudaGetLastError());
   return LGAME_OK;
 }
@@ -666,7 +668,7 @@ int loss_from_parts(lgame_emu* e, int nparts, int batch, float* loss) {
 
 int upload_batch(lgame_emu* e, const float* x, const float* y, int batch) {
   ECK(cudaMemcpyAsync(e->xraw, x, sizeof(float) * (size_t)batch * e->nin, cudaMemcpyHostToDevice, e->st));
-  int rc = prep_x(e, e->xraw, batch);
+  int rc = prep_x(e, e->xraw, batch, batch);
   if (rc) return rc;
   if (y) {
     ECK(cudaMemcpyAsync(e->yraw, y, sizeof(float) * (size_t)batch * e->nout, cudaMemcpyHostToDevice, e->st));
@@ -696,10 +698,7 @@ int infer_device(lgame_emu* e, const float* x_dev, long long n, float* y_dev, cu
   for (long long r0 = 0; r0 < n; r0 += e->bmax) {
     const int b = (int)std::min<long long>(e->bmax, n - r0);
     const int bp = ((b + 127) / 128) * 128;
-    if (bp != b) ECK(cudaMemsetAsync(e->xraw, 0, sizeof(float) * (size_t)bp * e->nin, e->st));
-    ECK(cudaMemcpyAsync(e->xraw, x_dev + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyDeviceToDevice,
-                        e->st));
-    int rc = prep_x(e, e->xraw, bp);
+    int rc = prep_x(e, x_dev + r0 * e->nin, bp, b);
     if (rc) return rc;
     rc = forward(e, bp);
     if (rc) return rc;
@@ -960,7 +959,7 @@ extern "C" int lgame_emu_train_epoch(lgame_emu* e, int batch, float lr, unsigned
     k_gather_rows<<<blocks((long long)batch * e->nin), 256, 0, e->st>>>(e->dsx, idx, batch, e->nin, e->xraw);
     k_gather_rows<<<blocks((long long)batch * e->nout), 256, 0, e->st>>>(e->dsy, idx, batch, e->nout, e->yraw);
     ECK(cudaGetLastError());
-    int rc = prep_x(e, e->xraw, batch);
+    int rc = prep_x(e, e->xraw, batch, batch);
     if (rc) return rc;
     k_prep_y<<<blocks((long long)batch * e->nout_pad), 256, 0, e->st>>>(e->yraw, e->nout, e->nout_pad, batch, e->ymean,
                                                                          e->yistd, e->Yt);
@@ -982,20 +981,37 @@ extern "C" int lgame_emu_train_epoch(lgame_emu* e, int batch, float lr, unsigned
   return LGAME_OK;
 }
 
+// the device address of a host array the GPU can read and write directly (page-locked and
+// mapped), or null
+void* mapped_view(const void* host) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer may leave an error behind
+    return nullptr;
+  }
+  return (a.type == cudaMemoryTypeHost) ? a.devicePointer : nullptr;
+}
+
+// Page-locked x and y are read and written by the kernels themselves over the CPU-GPU link
+// (no staging copies); other host arrays go through copies to and from device buffers.
 extern "C" int lgame_emu_infer(lgame_emu* e, const float* x, long long n, float* y) {
   if (!e || !x || !y || n < 0) return emu_fail(LGAME_ERR_INVALID_ARG, "lgame_emu_infer: bad arguments");
+  const float* xv = (const float*)mapped_view(x);
+  float* yv = (float*)mapped_view(y);
   for (long long r0 = 0; r0 < n; r0 += e->bmax) {
     const int b = (int)std::min<long long>(e->bmax, n - r0);
     const int bp = ((b + 127) / 128) * 128;
-    if (bp != b) ECK(cudaMemsetAsync(e->xraw, 0, sizeof(float) * (size_t)bp * e->nin, e->st));
-    ECK(cudaMemcpyAsync(e->xraw, x + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyHostToDevice, e->st));
-    int rc = prep_x(e, e->xraw, bp);
+    const float* src = xv ? xv + r0 * e->nin : e->xraw;
+    if (!xv)
+      ECK(cudaMemcpyAsync(e->xraw, x + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyHostToDevice, e->st));
+    int rc = prep_x(e, src, bp, b);
     if (!rc) rc = forward(e, bp);
     if (rc) return rc;
     k_denorm<<<blocks((long long)b * e->nout), 256, 0, e->st>>>(e->Y, e->nout, e->nout_pad, b, e->ymean, e->ystd,
-                                                                 e->yout);
+                                                                 yv ? yv + r0 * e->nout : e->yout);
     ECK(cudaGetLastError());
-    ECK(cudaMemcpyAsync(y + r0 * e->nout, e->yout, sizeof(float) * (size_t)b * e->nout, cudaMemcpyDeviceToHost, e->st));
+    if (!yv)
+      ECK(cudaMemcpyAsync(y + r0 * e->nout, e->yout, sizeof(float) * (size_t)b * e->nout, cudaMemcpyDeviceToHost, e->st));
   }
   ECK(cudaStreamSynchronize(e->st));
   return check_err(e);

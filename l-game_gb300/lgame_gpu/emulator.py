@@ -121,11 +121,17 @@ class Emulator:
               "lgame_emu_train_epoch")
         return float(loss[0])
 
-    def infer(self, x) -> np.ndarray:
+    def infer(self, x, out: np.ndarray | None = None) -> np.ndarray:
+        """Heating rates of the rows of x (n x nin); `out` (n x nout, C-contiguous float32)
+        receives them when given.  Page-locked x and out are read and written by the GPU
+        directly."""
         x = _f32(x)
-        y = np.zeros((x.shape[0], self.nout), np.float32)
-        check(self.lib.lgame_emu_infer(self.h, _fp(x), x.shape[0], _fp(y)), "lgame_emu_infer")
-        return y
+        if out is None:
+            out = np.zeros((x.shape[0], self.nout), np.float32)
+        if out.dtype != np.float32 or out.shape != (x.shape[0], self.nout) or not out.flags.c_contiguous:
+            raise ValueError("infer: out must be a C-contiguous float32 array of shape (n, nout)")
+        check(self.lib.lgame_emu_infer(self.h, _fp(x), x.shape[0], _fp(out)), "lgame_emu_infer")
+        return out
 
     def gemm_bf16(self, a_bits: np.ndarray, b_bits: np.ndarray) -> np.ndarray:
         a = np.ascontiguousarray(a_bits, np.uint16)

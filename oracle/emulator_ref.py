@@ -46,16 +46,14 @@ def unflatten(p: np.ndarray, nin: int, hidden: int, nout: int):
     return out
 
 
-def loss_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray, nin: int, hidden: int, nout: int,
-              norm=None, bf16: bool = True):
-    """(loss, flat gradient) of one batch; norm = (x_mean, x_std, y_mean, y_std) or None."""
+def _forward(params, x, nin, hidden, nout, norm, bf16):
+    """Standardised outputs of the rows of x with the activations and pre-activations of the
+    hidden layers; BF16 rounding of operands (and FP32 pre-activations) as on the GPU."""
     W1, b1, W2, b2, W3, b3, W4, b4 = unflatten(params, nin, hidden, nout)
     x = np.asarray(x, np.float64)
-    y = np.asarray(y, np.float64)
     if norm is not None:
-        xm, xs, ym, ys = (np.asarray(v, np.float64) for v in norm)
+        xm, xs = (np.asarray(v, np.float64) for v in norm[:2])
         x = (x - xm) / xs
-        y = (y - ym) / ys
     r = bf16_round if bf16 else (lambda a: np.asarray(a, np.float64))
     if bf16:  # the GPU standardises in float32 before rounding
         x = np.asarray(x, np.float32)
@@ -70,6 +68,25 @@ def loss_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray, nin: int, hidden
         zs.append(z)
         acts.append(r(gelu(z)))
     out = acts[-1] @ r(Ws[3]).T + bs[3]
+    return out, acts, zs, Ws, r
+
+
+def predict(params: np.ndarray, x: np.ndarray, nin: int, hidden: int, nout: int, norm, bf16: bool = True):
+    """Heating rates of the rows of x (inference): the network's outputs de-standardised with
+    norm = (x_mean, x_std, y_mean, y_std)."""
+    out = _forward(params, x, nin, hidden, nout, norm, bf16)[0]
+    ym, ys = (np.asarray(v, np.float64) for v in norm[2:])
+    return out * ys + ym
+
+
+def loss_grad(params: np.ndarray, x: np.ndarray, y: np.ndarray, nin: int, hidden: int, nout: int,
+              norm=None, bf16: bool = True):
+    """(loss, flat gradient) of one batch; norm = (x_mean, x_std, y_mean, y_std) or None."""
+    out, acts, zs, Ws, r = _forward(params, x, nin, hidden, nout, norm, bf16)
+    y = np.asarray(y, np.float64)
+    if norm is not None:
+        ym, ys = (np.asarray(v, np.float64) for v in norm[2:])
+        y = (y - ym) / ys
     B = x.shape[0]
     e = out - y
     loss = float(np.mean(e * e))

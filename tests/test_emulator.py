@@ -115,6 +115,28 @@ def test_gradients_match_oracle():
 
 
 @pytest.mark.gpu
+def test_inference_matches_oracle_and_pinned_equals_pageable():
+    """Inference over a ragged number of columns (several batches, the last one padded)
+    against the oracle's forward pass, and the direct path for page-locked host arrays
+    against the copy path for ordinary ones, bit for bit."""
+    torch = pytest.importorskip("torch")
+    emu, _, _, norm = _emu_and_data()
+    n = 700
+    x = synthetic_columns(n, 20, 11)
+    y = emu.infer(x)
+    yo = R.predict(emu.get_params(), x, emu.nin, emu.hidden, emu.nout, norm)
+    ys = norm[3].astype(np.float64)
+    assert np.linalg.norm((y - yo) / ys) / np.linalg.norm((yo - norm[2]) / ys) < 1e-3
+    assert np.max(np.abs(y - yo) / ys) < 2e-2
+    xp = torch.empty((n, emu.nin), dtype=torch.float32, pin_memory=True).numpy()
+    yp = torch.zeros((n, emu.nout), dtype=torch.float32, pin_memory=True).numpy()
+    xp[...] = x
+    emu.infer(xp, out=yp)
+    np.testing.assert_array_equal(yp, y)
+    emu.close()
+
+
+@pytest.mark.gpu
 def test_params_roundtrip_and_determinism():
     emu, x, y, _ = _emu_and_data()
     p = emu.get_params()
