@@ -508,6 +508,9 @@ def run_ours(args):
         for r in results.values():
             if "e2e" in r:
                 line["e2e"] = r["e2e"]
+    if rank == 0 and ws == 1 and not args.no_boundaries:
+        del hm
+        line["boundary_relaxation"] = boundary_bench(args, peaks)
     if rank == 0 and ws == 1 and not args.no_emulator:
         line["emulator"] = emulator_bench(peaks)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -516,6 +519,59 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     barrier(dist)
     return 0
+
+
+def boundary_bench(args, peaks, n_swamp: int = 5, reps: int = 20) -> dict:
+    """Lateral boundary relaxation (mo_boundaries.F90:19-97) on the workload made non-periodic,
+    split precision, swamp layer n_swamp points wide (the reference's default), both boundary
+    levels equal to the initial state: the step with the relaxation at its end, and
+    lgame_gpu_update_boundaries alone (CUDA events on the library's stream; its two kernels,
+    ks_bc_rim over the swamp layer and ks_bc_thermo over all scalar points).  Algorithmic
+    bytes: at every scalar point rho_gas, rhotheta_v, theta_v_bg, the background rhotheta_v
+    and exner_bg read and theta_v_pert, exner_pert written in FP64 and FP32 (64 B); in the
+    swamp layer also both levels, the state and the relaxed FP64 value and FP32 mirror of
+    every field (36 B each)."""
+    import torch
+    import cases
+    import lgame_gpu as L
+    n = cases.namelist(WORKLOAD, lperiodic=False, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    hm = L.HostModel(n)
+    cfg = L.config_from_namelist(n)
+    cfg.precision = L.PRECISION_SPLIT
+    g = L.GpuModel(cfg, hm.grid)
+    g.set_state(0, hm.state)
+    g.set_state(1, hm.state)
+    g.set_diag(hm.diag)
+    lev = {f: hm.state[f] for f in L.BC_FIELDS}
+    g.bc_setup(n_swamp, 10800, 0.0, None)
+    g.set_bc(1, lev)
+    g.set_bc(2, lev)
+    del hm, lev
+    for k in range(args.warmup):
+        g.pchevi(k % 2, (k + 1) % 2, k)
+    el = time_steps(L, g, args.steps, args.warmup)
+    s = torch.cuda.ExternalStream(g.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.synchronize()
+    t_now = (args.warmup + args.steps) * n.dtime
+    e0.record(s)
+    for r in range(reps):
+        g.update_boundaries(r % 2, t_now)
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    st = g.get_state(0)
+    finite = all(bool(np.isfinite(v).all()) for v in st.values())
+    g.close()
+    cells = n.nx * n.ny * n.n_layers
+    rim = 1.0 - max(n.ny - 2 * n_swamp, 0) * max(n.nx - 2 * n_swamp, 0) / (n.ny * n.nx)
+    per_cell = 64.0 + rim * 36.0 * (n.n_constituents + 4)
+    gbs = per_cell * cells / (ms * 1e-3) / 1e9
+    return {"kernel": "ks_bc_rim + ks_bc_thermo", "n_swamp": n_swamp, "ms_per_step_with_relaxation": el / args.steps * 1e3,
+            "avg_launch_ms": ms, "alg_bytes_per_cell": per_cell, "swamp_fraction": rim,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / peaks["hbm_gbs"], "peak_src": peaks["src"]},
+            "finite": finite}
 
 
 def measure_e2e(L, g, hm, args) -> dict:
@@ -559,6 +615,7 @@ def main():
     ap.add_argument("--split-only", action="store_true", help="measure the split step alone (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-emulator", action="store_true")
+    ap.add_argument("--no-boundaries", action="store_true", help="skip the non-periodic boundary-relaxation run")
     ap.add_argument("--nx", type=int, default=0, help="override nx=ny (smaller runs for testing)")
     ap.add_argument("--ny", type=int, default=0)
     args = ap.parse_args()

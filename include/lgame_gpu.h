@@ -172,6 +172,13 @@ enum lgame_diag_field {
 
 typedef struct lgame_gpu lgame_gpu;   /* opaque context, one per model instance */
 
+/* Supplier of boundary data for the lateral relaxation (the role of read_boundaries,
+ * mo_boundaries.F90:99-123): called when a boundary update needs a new level, with the
+ * valid time the reference would read (t_update, seconds) and the time index (1 or 2)
+ * the level goes to.  It must hand the level over with lgame_gpu_set_bc (or, for the
+ * oracle, oracle_set_bc) before it returns, and returns 0, or nonzero to fail the step. */
+typedef int (*lgame_bc_loader)(void* user, double t_update, int time_index);
+
 /* Creates a context on the current CUDA device and allocates its device memory.
  * Replaces the allocation block of src/control.F90:99-444 for the arrays pchevi uses. */
 int  lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out);
@@ -197,10 +204,12 @@ int  lgame_gpu_get_diag(lgame_gpu* ctx, double* const* fields, int nfields);
 /* One HEVI predictor-corrector step entirely on the device: state[new_slot] is
  * computed from state[old_slot].  Equivalent of
  *   call pchevi(state_old,state_new,tend,bc,grid,diag,total_step_counter,lrad_update,t_0)
- * with the periodic domain (the boundary relaxation of mo_boundaries.F90 is not part
- * of the GPU path).  lrad_update and t_0 are accepted for interface parity; the
- * radiation tendency is whatever the host last set (or the emulator wrote).
- * Stream-ordered: returns after enqueueing unless check_finite is on. */
+ * In a non-periodic run with boundary data set up (lgame_gpu_bc_setup), the step ends
+ * with lgame_gpu_update_boundaries(ctx, new_slot, (total_step_counter+1)*dtime), as the
+ * reference's does (mo_manage_pchevi.F90:114-116).  lrad_update and t_0 are accepted for
+ * interface parity; the radiation tendency is whatever the host last set (or the
+ * emulator wrote).  Stream-ordered: returns after enqueueing unless check_finite is on
+ * or a boundary level has to be loaded. */
 int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
                       int total_step_counter, int lrad_update, double t_0);
 
@@ -270,6 +279,35 @@ int  lgame_gpu_profile_report(lgame_gpu* ctx, char* buf, int len);
  * kernels are short (small grids).  Results are the same bits either way.  Graphs are not
  * used while per-kernel tracing is on.  No counterpart in the reference (a CPU program). */
 int  lgame_gpu_set_graphs(lgame_gpu* ctx, int enable);
+
+/* ---- lateral boundary relaxation (src/io/mo_boundaries.F90) --------------------------
+ * Turns on the relaxation of a non-periodic run (lperiodic = 0; else LGAME_ERR_STATE):
+ * the rescale factors of a swamp layer n_swamp points wide (setup_bc_factor,
+ * mo_boundaries.F90:125-170: sin^2 of pi/2*max(1 - d/n_swamp, 0), d the index distance
+ * from the edge), the interval dtime_bc (s) between boundary levels, t_latest_bc (s) the
+ * valid time of the level in time index 1 on the clock of the step's t_now, i.e. time
+ * since the start (the reference's default, 0), and the loader of later levels.  Level
+ * indices start as old = 1, new = 2 (control.F90:358-359); both levels are zero until set.
+ * Without this call the step applies no relaxation (the reference would relax toward
+ * all-zero boundary data in idealised non-periodic runs, which empties the outer ring). */
+int  lgame_gpu_bc_setup(lgame_gpu* ctx, int n_swamp, int dtime_bc, double t_latest_bc,
+                        lgame_bc_loader loader, void* user);
+/* One boundary level into time index 1 or 2 (bc%rho(:,:,:,:,i) ... bc%wind_w(:,:,:,i)):
+ * rho (ny,nx,n_layers,n_constituents), rhotheta_v (ny,nx,n_layers), wind_u
+ * (ny,nx+1,n_layers), wind_v (ny+1,nx,n_layers), wind_w (ny,nx,n_layers+1), host arrays
+ * in the reference layout. */
+int  lgame_gpu_set_bc(lgame_gpu* ctx, int time_index, const double* rho, const double* rhotheta_v,
+                      const double* wind_u, const double* wind_v, const double* wind_w);
+/* update_boundaries(state, bc, t_now, grid), mo_boundaries.F90:19-97, on state slot `slot`:
+ * time weights old = 1 - (t_now - t_latest_bc)/dtime_bc and new = 1 - old; if old < 0
+ * the loader is asked for the level of t_latest_bc + dtime_bc into the old index, the
+ * indices swap and t_latest_bc advances by dtime_bc (the weights are not recomputed, as in
+ * the reference); then every point becomes factor*(old*bc_old + new*bc_new) +
+ * (1 - factor)*state for rho, rhotheta_v, u, v, w, and theta_v_pert and exner_pert are
+ * recomputed from rho and rhotheta_v over the whole domain. */
+int  lgame_gpu_update_boundaries(lgame_gpu* ctx, int slot, double t_now);
+/* The boundary bookkeeping: level indices (1-based) and t_latest_bc. */
+int  lgame_gpu_bc_state(lgame_gpu* ctx, int* index_old, int* index_new, double* t_latest_bc);
 
 /* Bytes of device memory held by the context. */
 long long lgame_gpu_device_bytes(const lgame_gpu* ctx);

@@ -108,6 +108,7 @@ constexpr double kR_D = 287.057811;
 constexpr double kC_D_V = 717.942189;
 constexpr double kC_V_V = 1396.475121;
 constexpr double kC_D_P = 1005.0;
+constexpr double kP_0 = 100000.0;
 constexpr double kM_D = 6.02214076e23 * 0.004810e-23;
 constexpr double kM_V = 6.02214076e23 * 0.002991e-23;
 constexpr double kIMPL_THERMO_WEIGHT = 717.942189 / 1005.0;

@@ -9,6 +9,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -68,6 +69,17 @@ struct lgame_gpu {
   bool use_graphs = true;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   int graph_kernels[2] = {0, 0};
+  // lateral boundary relaxation (t_bc, mo_definitions.F90:117-131): two levels in the
+  // state's padded layout, the rescale factors on the padded plane, the bookkeeping
+  bool bc_on = false;
+  int bc_index_old = 1, bc_index_new = 2, dtime_bc = 0;
+  double t_latest_bc = 0.0;
+  lgame_bc_loader bc_loader = nullptr;
+  void* bc_user = nullptr;
+  State bc_lev[2]{};
+  double *bcf_s = nullptr, *bcf_u = nullptr, *bcf_v = nullptr;
+  int* bc_rim = nullptr;  // plane indices of the swamp layer (any factor nonzero), split path
+  int bc_nrim = 0;
   // per-kernel tracing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -224,6 +236,50 @@ __global__ void k_check_finite(Dims D, State S, int* flag) {
   if (ji <= D.ny + 1 && jk <= D.nx && jl <= D.nl) bad |= !isfinite(S.v[IX(D, ji, jk, jl)]);
   if (ji <= D.ny && jk <= D.nx && jl <= D.NL) bad |= !isfinite(S.w[IX(D, ji, jk, jl)]);
   if (bad) atomicExch(flag, 1);
+}
+
+// update_boundaries, mo_boundaries.F90:19-97, one thread per point of the padded grid:
+// x = factor*(w_old*x_old + w_new*x_new) + (1 - factor)*x for rho (every constituent),
+// rhotheta_v and w at scalar columns, u and v at their points (the factors on the padded
+// plane), then theta_v_pert and exner_pert from the relaxed rho and rhotheta_v (:92-95).
+// With an FP32 mirror (split precision) every changed value is also written rounded.
+__global__ void k_bc_update(Dims D, State S, StateF M, State B0, State B1, const double* fs, const double* fu,
+                            const double* fv, double ow, double nw, const double* theta_v_bg, const double* exner_bg) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
+  const long long p = (long long)(ji - 1) + (long long)D.P * (jk - 1);
+  const bool mir = M.rho != nullptr;
+  auto relax = [&](double f, const double* b0, const double* b1, double* x, float* xm, long long q) {
+    const double r = f * (ow * b0[q] + nw * b1[q]) + (1.0 - f) * x[q];
+    x[q] = r;
+    if (mir) xm[q] = narrow(r);
+    return r;
+  };
+  if (ji <= D.ny && jk <= D.nx) {
+    const double f = fs[p];
+    if (jl <= D.nl) {
+      const long long q = IX(D, ji, jk, jl);
+      double rho_g = 0.0;
+      for (int jc = 0; jc < D.ncons; ++jc) {
+        const long long qc = q + (long long)jc * D.fstride;
+        const double r = relax(f, B0.rho, B1.rho, S.rho, M.rho, qc);
+        if (jc == D.g - 1) rho_g = r;
+      }
+      const double rt = relax(f, B0.rt, B1.rt, S.rt, M.rt, q);
+      const double tp = rt / rho_g - theta_v_bg[q];
+      const double ep = pow(kR_D * rt / kP_0, kR_D / kC_D_V) - exner_bg[q];
+      S.tp[q] = tp;
+      S.ep[q] = ep;
+      if (mir) {
+        M.tp[q] = narrow(tp);
+        M.ep[q] = narrow(ep);
+      }
+    }
+    if (jl <= D.NL) relax(f, B0.w, B1.w, S.w, M.w, IX(D, ji, jk, jl));
+  }
+  if (ji <= D.ny && jk <= D.nx + 1 && jl <= D.nl) relax(fu[p], B0.u, B1.u, S.u, M.u, IX(D, ji, jk, jl));
+  if (ji <= D.ny + 1 && jk <= D.nx && jl <= D.nl) relax(fv[p], B0.v, B1.v, S.v, M.v, IX(D, ji, jk, jl));
 }
 
 // deterministic FP64 sums: every block sums a fixed strided subset in a fixed order;
@@ -600,6 +656,8 @@ extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfie
   }
   if (c->split) {
     if ((rc = split_set_grid(c->split, c->D, c->G, c->stream)) != LGAME_OK) return rc;
+    // a new background for the boundary relaxation of a context already set up for it
+    if (c->bc_on && (rc = split_bc_prepare(c->split, c->D, c->G, c->stream)) != LGAME_OK) return set_err(rc, "split_bc_prepare");
   }
   CK(cudaStreamSynchronize(c->stream));
   c->grid_set = true;
@@ -777,6 +835,11 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
     rc = launch_step();
   }
   if (rc != LGAME_OK) return rc;
+  // mo_manage_pchevi.F90:114-116
+  if (!c->cfg.lperiodic && c->bc_on) {
+    if ((rc = lgame_gpu_update_boundaries(c, new_slot, (total_step_counter + 1) * c->D.dtime)) != LGAME_OK) return rc;
+    c->kernels_last_step += (c->split && c->bc_nrim > 0) ? 2 : 1;
+  }
   if (c->cfg.check_finite) {
     const Dims& D = c->D;
     CK(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
@@ -899,6 +962,139 @@ void trace_end(lgame_gpu* c, int slot) { cudaEventRecord(c->ev_pool[slot + 1], c
 
 extern "C" void* lgame_gpu_stream(const lgame_gpu* c) { return c ? (void*)c->stream : nullptr; }
 
+// ---- lateral boundary relaxation, src/io/mo_boundaries.F90 -----------------------------
+
+namespace {
+// setup_bc_factor, mo_boundaries.F90:125-170, into a padded plane (row pitch P): for the
+// points ji = 1..n1, jk = 1..n2, sin^2(pi/2*max(1 - d/n_swamp, 0)) with d the index
+// distance to the nearest edge of that staggering (converted to double before the division)
+void bc_factors(int n_swamp, int n1, int n2, int P, std::vector<double>& out) {
+  const double pi = 3.14159265358979323846;
+  for (int jk = 1; jk <= n2; ++jk)
+    for (int ji = 1; ji <= n1; ++ji) {
+      const int d = std::min(std::min(ji - 1, jk - 1), std::min(n1 - ji, n2 - jk));
+      double f = 1.0 - (double)d / n_swamp;
+      if (f < 0.0) f = 0.0;
+      const double sn = std::sin(0.5 * pi * f);
+      out[(size_t)(ji - 1) + (size_t)P * (jk - 1)] = sn * sn;
+    }
+}
+}  // namespace
+
+extern "C" int lgame_gpu_bc_setup(lgame_gpu* c, int n_swamp, int dtime_bc, double t_latest_bc, lgame_bc_loader loader,
+                                  void* user) {
+  if (!c || n_swamp < 1 || dtime_bc < 1)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_bc_setup: bad arguments (n_swamp >= 1, dtime_bc >= 1)");
+  if (c->cfg.lperiodic) return set_err(LGAME_ERR_STATE, "lgame_gpu_bc_setup: the run is periodic (lperiodic = 1)");
+  const Dims& D = c->D;
+  if (!c->bcf_s) {
+    for (State& L : c->bc_lev) {
+      int rc = dalloc(c, &L.rho, (size_t)D.fstride * D.ncons);
+      if (!rc) rc = dalloc(c, &L.rt, D.fstride);
+      if (!rc) rc = dalloc(c, &L.u, D.fstride);
+      if (!rc) rc = dalloc(c, &L.v, D.fstride);
+      if (!rc) rc = dalloc(c, &L.w, D.fstride);
+      if (rc) return rc;
+    }
+    int rc = dalloc(c, &c->bcf_s, D.plane);
+    if (!rc) rc = dalloc(c, &c->bcf_u, D.plane);
+    if (!rc) rc = dalloc(c, &c->bcf_v, D.plane);
+    if (rc) return rc;
+  }
+  std::vector<double> h((size_t)D.plane);
+  std::vector<char> any((size_t)D.plane, 0);
+  double* dst[3] = {c->bcf_s, c->bcf_u, c->bcf_v};
+  const int n1[3] = {D.ny, D.ny, D.ny + 1}, n2[3] = {D.nx, D.nx + 1, D.nx};
+  for (int k = 0; k < 3; ++k) {
+    std::fill(h.begin(), h.end(), 0.0);
+    bc_factors(n_swamp, n1[k], n2[k], D.P, h);
+    for (size_t i = 0; i < h.size(); ++i) any[i] |= (h[i] != 0.0);
+    CK(cudaMemcpy(dst[k], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+  }
+  std::vector<int> rim;
+  for (size_t i = 0; i < any.size(); ++i)
+    if (any[i]) rim.push_back((int)i);
+  if (c->bc_rim) cudaFree(c->bc_rim);
+  c->bc_rim = nullptr;
+  c->bc_nrim = (int)rim.size();
+  if (!rim.empty()) {
+    CK(cudaMalloc(&c->bc_rim, sizeof(int) * rim.size()));
+    CK(cudaMemcpy(c->bc_rim, rim.data(), sizeof(int) * rim.size(), cudaMemcpyHostToDevice));
+  }
+  if (c->split) {
+    if (!c->grid_set) return set_err(LGAME_ERR_STATE, "lgame_gpu_bc_setup: lgame_gpu_set_grid has not been called");
+    const int rc = split_bc_prepare(c->split, D, c->G, c->stream);
+    if (rc != LGAME_OK) return set_err(rc, "lgame_gpu_bc_setup: background rhotheta_v for the split path failed");
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  c->bc_index_old = 1;  // control.F90:358-359
+  c->bc_index_new = 2;
+  c->dtime_bc = dtime_bc;
+  c->t_latest_bc = t_latest_bc;
+  c->bc_loader = loader;
+  c->bc_user = user;
+  c->bc_on = true;
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_set_bc(lgame_gpu* c, int time_index, const double* rho, const double* rhotheta_v,
+                                const double* wind_u, const double* wind_v, const double* wind_w) {
+  if (!c || time_index < 1 || time_index > 2 || !rho || !rhotheta_v || !wind_u || !wind_v || !wind_w)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_bc: bad arguments");
+  if (!c->bc_on) return set_err(LGAME_ERR_STATE, "lgame_gpu_set_bc: lgame_gpu_bc_setup has not been called");
+  const Dims& D = c->D;
+  const State& L = c->bc_lev[time_index - 1];
+  const Ext es = ext_s(D);
+  int rc = LGAME_OK;
+  for (int r = 0; r < D.ncons && !rc; ++r) rc = copy_h2d(c, L.rho + (size_t)r * D.fstride, rho + r * es.n1 * es.n2 * es.n3, es);
+  if (!rc) rc = copy_h2d(c, L.rt, rhotheta_v, es);
+  if (!rc) rc = copy_h2d(c, L.u, wind_u, ext_u(D));
+  if (!rc) rc = copy_h2d(c, L.v, wind_v, ext_v(D));
+  if (!rc) rc = copy_h2d(c, L.w, wind_w, ext_w(D));
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(c->stream));  // the host arrays may be reused on return
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_update_boundaries(lgame_gpu* c, int slot, double t_now) {
+  if (!c || slot < 0 || slot > 1) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_update_boundaries: bad arguments");
+  if (!c->bc_on) return set_err(LGAME_ERR_STATE, "lgame_gpu_update_boundaries: lgame_gpu_bc_setup has not been called");
+  const double old_weight = 1.0 - (t_now - c->t_latest_bc) / c->dtime_bc;
+  if (old_weight < 0.0) {
+    // read_boundaries(bc, t_latest_bc+dtime_bc, bc%index_old), then the index swap (:37-47)
+    if (!c->bc_loader)
+      return set_err(LGAME_ERR_STATE, "lgame_gpu_update_boundaries: a new boundary level is due and there is no loader");
+    if (c->bc_loader(c->bc_user, c->t_latest_bc + c->dtime_bc, c->bc_index_old) != 0)
+      return set_err(LGAME_ERR_STATE, "lgame_gpu_update_boundaries: the boundary loader failed");
+    c->bc_index_old = c->bc_index_new;
+    c->bc_index_new = (c->bc_index_old == 1) ? 2 : 1;
+    c->t_latest_bc = c->t_latest_bc + c->dtime_bc;
+  }
+  const double new_weight = 1.0 - old_weight;
+  const Dims& D = c->D;
+  StateF M{};
+  if (c->split && c->mirror_valid[slot]) M = split_mirror(c->split, slot);
+  if (c->split) {
+    const int rc = split_bc_update(c->split, D, c->G, c->st[slot], M, c->bc_lev[c->bc_index_old - 1],
+                                   c->bc_lev[c->bc_index_new - 1], c->bc_rim, c->bc_nrim, c->bcf_s, c->bcf_u, c->bcf_v,
+                                   old_weight, new_weight, c->stream);
+    return rc == LGAME_OK ? LGAME_OK : set_err(rc, "lgame_gpu_update_boundaries: launch of the split kernels failed");
+  }
+  k_bc_update<<<grd(D, D.ny + 1, D.nx + 1, D.NL), blk(), 0, c->stream>>>(
+      D, c->st[slot], M, c->bc_lev[c->bc_index_old - 1], c->bc_lev[c->bc_index_new - 1], c->bcf_s, c->bcf_u, c->bcf_v,
+      old_weight, new_weight, c->G.theta_v_bg, c->G.exner_bg);
+  return klaunch_check(c, "k_bc_update");
+}
+
+extern "C" int lgame_gpu_bc_state(lgame_gpu* c, int* index_old, int* index_new, double* t_latest_bc) {
+  if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_bc_state: null context");
+  if (!c->bc_on) return set_err(LGAME_ERR_STATE, "lgame_gpu_bc_state: lgame_gpu_bc_setup has not been called");
+  if (index_old) *index_old = c->bc_index_old;
+  if (index_new) *index_new = c->bc_index_new;
+  if (t_latest_bc) *t_latest_bc = c->t_latest_bc;
+  return LGAME_OK;
+}
+
 extern "C" int lgame_gpu_set_graphs(lgame_gpu* c, int enable) {
   if (!c) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_graphs: null context");
   c->use_graphs = enable != 0;
@@ -947,6 +1143,7 @@ extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   if (c->split) split_destroy(c->split);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (void* p : c->allocations) cudaFree(p);
+  if (c->bc_rim) cudaFree(c->bc_rim);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }

@@ -72,6 +72,8 @@ struct SplitCtx {
   // FP32 mirrors of the two state slots
   StateF mir[2]{};
   SplitCarriedF C{};
+  // rhotheta_v of the background state, p_0/r_d*exner_bg^(c_d_v/r_d) (boundary relaxation)
+  double* rtbg = nullptr;
 };
 
 namespace {
@@ -1102,6 +1104,121 @@ int split_convert(const double* src, float* dst, long long n, cudaStream_t strea
 }
 int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream) {
   k_to_double<<<1216, 256, 0, stream>>>(src, dst, n);
+  return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
+}
+
+// ---- lateral boundary relaxation (mo_boundaries.F90:19-97) in split precision -------------
+namespace {
+__global__ void k_rtbg(const double* exner_bg, double* rtbg, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    rtbg[i] = kP_0 / kR_D * pow(exner_bg[i], kC_D_V / kR_D);
+}
+
+// Two kernels.  ks_bc_rim relaxes the swamp layer only: one thread per (listed plane point,
+// level), the points being those where any of the three rescale factors is nonzero, with the
+// FP64 blend x = f*(w_old*x_old + w_new*x_new) + (1 - f)*x of every field (FP32 mirror rounded
+// from it).  Everywhere else the reference's 0*(...) + 1*x is x (for finite boundary data and
+// a nonzero x), so nothing is written there.  ks_bc_thermo then recomputes theta_v_pert and
+// exner_pert at every scalar point with one FP64 operation each:
+//   theta_v_pert = (rhotheta_v - rho_gas*theta_v_bg)/rho_gas, the numerator in FP64 and
+//                  the division in FP32 (relative error ~1e-7 of theta_v_pert),
+//   exner_pert   = (r_d*rhotheta_v/p_0)^(r_d/c_d_v) - exner_bg
+//                = exner_bg*((1 + d)^kappa - 1) = exner_bg*expm1(kappa*log1p(d)),
+//                  d = (rhotheta_v - rt_bg)/rt_bg with rt_bg the background's rhotheta_v,
+//                  in FP32 after the FP64 difference (relative error ~1e-7 of exner_pert).
+// Keeping the blend out of the second kernel matters on this GPU: a warp covers 32 rows, so
+// with one kernel every warp that touches the swamp layer issued the whole FP64 blend.
+
+// (1 + d)^kappa - 1 in FP32 for |d| <= 0.25 from series with multiply-adds only:
+// log1p(d) = 2 atanh(s) = 2 (s + s^3/3 + ... + s^13/13), s = d/(2 + d), |s| <= 1/7, and
+// expm1(y) = y + y^2/2! + ... + y^8/8!, |y| = |kappa log1p(d)| <= 0.12 (truncation errors
+// below 1e-11 relative); larger |d| goes through log1pf and expm1f.
+__device__ __forceinline__ float pow1p_m1(float d, float kappa) {
+  if (fabsf(d) > 0.25f) return expm1f(kappa * log1pf(d));
+  const float sv = d / (2.f + d), s2 = sv * sv;
+  float t = 1.f / 13.f;
+  t = fmaf(t, s2, 1.f / 11.f);
+  t = fmaf(t, s2, 1.f / 9.f);
+  t = fmaf(t, s2, 1.f / 7.f);
+  t = fmaf(t, s2, 1.f / 5.f);
+  t = fmaf(t, s2, 1.f / 3.f);
+  t = fmaf(t, s2, 1.f);
+  const float y = kappa * (2.f * sv * t);
+  float e = 1.f / 40320.f;
+  e = fmaf(e, y, 1.f / 5040.f);
+  e = fmaf(e, y, 1.f / 720.f);
+  e = fmaf(e, y, 1.f / 120.f);
+  e = fmaf(e, y, 1.f / 24.f);
+  e = fmaf(e, y, 1.f / 6.f);
+  e = fmaf(e, y, 0.5f);
+  e = fmaf(e, y, 1.f);
+  return y * e;
+}
+// the factors are +0 or positive: a bit test instead of an FP64 comparison
+__device__ __forceinline__ bool nonzero(double f) { return __double_as_longlong(f) != 0; }
+
+// grid (ceil(nrim/128), NL), 128 threads; rim[r] = plane index (ji-1) + P*(jk-1)
+__global__ void __launch_bounds__(128) ks_bc_rim(Dims D, State S, StateF M, State B0, State B1, const int* rim, int nrim,
+                                                 const double* fs, const double* fu, const double* fv, double ow,
+                                                 double nw) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrim) return;
+  const int p = rim[r], ji = p % D.P + 1, jk = p / D.P + 1, jl = blockIdx.y + 1;
+  const bool mir = M.rho != nullptr;
+  auto relax = [&](double f, const double* b0, const double* b1, double* x, float* xm, long long q) {
+    const double v = f * (ow * b0[q] + nw * b1[q]) + (1.0 - f) * x[q];
+    x[q] = v;
+    if (mir) xm[q] = narrow(v);
+  };
+  const long long q = IX(D, ji, jk, jl);
+  if (ji <= D.ny && jk <= D.nx && nonzero(fs[p])) {
+    const double f = fs[p];
+    if (jl <= D.nl) {
+      for (int jc = 0; jc < D.ncons; ++jc) relax(f, B0.rho, B1.rho, S.rho, M.rho, q + (long long)jc * D.fstride);
+      relax(f, B0.rt, B1.rt, S.rt, M.rt, q);
+    }
+    relax(f, B0.w, B1.w, S.w, M.w, q);
+  }
+  if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1 && nonzero(fu[p])) relax(fu[p], B0.u, B1.u, S.u, M.u, q);
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx && nonzero(fv[p])) relax(fv[p], B0.v, B1.v, S.v, M.v, q);
+}
+
+__global__ void __launch_bounds__(256) ks_bc_thermo(Dims D, State S, StateF M, const double* theta_v_bg,
+                                                    const double* exner_bg, const double* rtbg) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  const double rho_g = S.rho[q + (long long)(D.g - 1) * D.fstride], rt = S.rt[q];
+  const double tb = theta_v_bg[q], rb = rtbg[q], eb = exner_bg[q];
+  const float tpf = narrow(fma(-rho_g, tb, rt)) / narrow(rho_g);
+  const float d = narrow(rt - rb) / narrow(rb);
+  const float epf = narrow(eb) * pow1p_m1(d, (float)(kR_D / kC_D_V));
+  S.tp[q] = wide(tpf);
+  S.ep[q] = wide(epf);
+  if (M.tp) {
+    M.tp[q] = tpf;
+    M.ep[q] = epf;
+  }
+}
+}  // namespace
+
+int split_bc_prepare(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream) {
+  if (!s->rtbg) {
+    long long bytes = 0;
+    if (salloc(s, &s->rtbg, (size_t)D.fstride, &bytes)) return LGAME_ERR_ALLOC;
+  }
+  k_rtbg<<<1216, 256, 0, stream>>>(G.exner_bg, s->rtbg, D.fstride);
+  return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
+}
+
+int split_bc_update(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S, const StateF& M, const State& B0,
+                    const State& B1, const int* rim, int nrim, const double* fs, const double* fu, const double* fv,
+                    double ow, double nw, cudaStream_t stream) {
+  if (!s->rtbg) return LGAME_ERR_STATE;
+  if (nrim > 0)
+    ks_bc_rim<<<dim3((unsigned)((nrim + 127) / 128), (unsigned)D.NL), 128, 0, stream>>>(D, S, M, B0, B1, rim, nrim, fs, fu,
+                                                                                        fv, ow, nw);
+  ks_bc_thermo<<<sgrd(D.ny, D.nx, D.nl), dim3(32, 8), 0, stream>>>(D, S, M, G.theta_v_bg, G.exner_bg, s->rtbg);
   return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
 }
 

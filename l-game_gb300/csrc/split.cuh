@@ -42,6 +42,15 @@ int split_convert(const double* src, float* dst, long long n, cudaStream_t strea
 int split_convert_back(const float* src, double* dst, long long n, cudaStream_t stream);
 // the FP32 mirror of state slot `slot` (its arrays; for writers that fill it themselves)
 StateF split_mirror(SplitCtx* s, int slot);
+// lateral boundary relaxation: split_bc_prepare forms the background's rhotheta_v once (after
+// the grid is set), split_bc_update relaxes state S (mirror M, may be empty) toward the levels
+// B0 (weight ow) and B1 (weight nw) with the rescale factors fs, fu, fv on the padded plane, at
+// the nrim plane points rim[] (plane indices where any factor is nonzero), and recomputes
+// theta_v_pert and exner_pert (two launches)
+int split_bc_prepare(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream);
+int split_bc_update(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S, const StateF& M, const State& B0,
+                    const State& B1, const int* rim, int nrim, const double* fs, const double* fu, const double* fv,
+                    double ow, double nw, cudaStream_t stream);
 // FP32 mirror of state slot `slot` recomputed from the FP64 state S (after the host wrote S)
 int split_refresh_mirror(SplitCtx* s, const Dims& D, int slot, const State& S, cudaStream_t stream);
 // one step from slot so (state So) to slot sn (state Sn); pg holds the FP64 pressure-gradient

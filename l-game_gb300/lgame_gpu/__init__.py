@@ -28,6 +28,27 @@ GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "are
                "exner_bg_grad_w", "gravity_m_v", "gravity_potential", "fvec_x", "fvec_y", "fvec_z",
                "trsk_weights_u", "trsk_weights_v"]
 STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w"]
+# one level of lateral boundary data (t_bc, mo_definitions.F90:117-131), state-field shapes
+BC_FIELDS = ["rho", "rhotheta_v", "wind_u", "wind_v", "wind_w"]
+# lgame_bc_loader: (user, t_update, time_index) -> 0 on success
+BC_LOADER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_int)
+
+
+def bc_callback(model, loader):
+    """A C loader for model.bc_setup: loader(t_update, time_index) returns the level (a dict
+    of BC_FIELDS arrays), which goes to model.set_bc(time_index, ...); None gives a null loader."""
+    if loader is None:
+        return BC_LOADER()
+
+    def cb(user, t_update, time_index):
+        try:
+            model.set_bc(time_index, loader(t_update, time_index))
+            return 0
+        except Exception:  # reported to the library as a failed load
+            import traceback
+            traceback.print_exc()
+            return 1
+    return BC_LOADER(cb)
 DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_w", "p_grad_acc_neg_l_u",
                "p_grad_acc_neg_l_v", "p_grad_acc_neg_l_w", "p_grad_acc_old_u", "p_grad_acc_old_v",
                "pot_vort_tend_x", "pot_vort_tend_y", "pot_vort_tend_z", "v_squared_grad_x", "v_squared_grad_y",
@@ -125,6 +146,10 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_stream": (vp, [vp]),
         "lgame_gpu_set_profiling": (i, [vp, i]),
         "lgame_gpu_set_graphs": (i, [vp, i]),
+        "lgame_gpu_bc_setup": (i, [vp, i, i, d, BC_LOADER, vp]),
+        "lgame_gpu_set_bc": (i, [vp, i] + [C.POINTER(C.c_double)] * 5),
+        "lgame_gpu_update_boundaries": (i, [vp, i, d]),
+        "lgame_gpu_bc_state": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(d)]),
         "lgame_gpu_profile_report": (i, [vp, C.c_char_p, i]),
         "lgame_gpu_destroy": (None, [vp]),
         "lgame_gpu_last_error": (C.c_char_p, []),
@@ -344,6 +369,27 @@ class GpuModel:
     def set_graphs(self, enable: bool):
         """Launch each step after step 0 as a captured CUDA graph (the default) or kernel by kernel."""
         check(self.lib.lgame_gpu_set_graphs(self.h, 1 if enable else 0), "lgame_gpu_set_graphs")
+
+    # lateral boundary relaxation (mo_boundaries.F90)
+    def bc_setup(self, n_swamp: int, dtime_bc: int, t_latest_bc: float = 0.0, loader=None):
+        """Relaxation toward boundary data at the end of every step of this non-periodic run;
+        loader(t_update, time_index) -> dict of BC_FIELDS supplies later levels."""
+        self._bc_cb = bc_callback(self, loader)
+        check(self.lib.lgame_gpu_bc_setup(self.h, n_swamp, dtime_bc, t_latest_bc, self._bc_cb, None),
+              "lgame_gpu_bc_setup")
+
+    def set_bc(self, time_index: int, bc: dict):
+        arrs = [np.asfortranarray(bc[f], dtype=np.float64) for f in BC_FIELDS]
+        dp = C.POINTER(C.c_double)
+        check(self.lib.lgame_gpu_set_bc(self.h, time_index, *[a.ctypes.data_as(dp) for a in arrs]), "lgame_gpu_set_bc")
+
+    def update_boundaries(self, slot: int, t_now: float):
+        check(self.lib.lgame_gpu_update_boundaries(self.h, slot, t_now), "lgame_gpu_update_boundaries")
+
+    def bc_state(self) -> tuple[int, int, float]:
+        io, inew, t = C.c_int(), C.c_int(), C.c_double()
+        check(self.lib.lgame_gpu_bc_state(self.h, C.byref(io), C.byref(inew), C.byref(t)), "lgame_gpu_bc_state")
+        return io.value, inew.value, t.value
 
     def profile_report(self) -> dict:
         import json

@@ -36,6 +36,7 @@ static const double c_d_p = 1005.0;
 #define M_V (6.02214076e23 * 0.002991e-23)  /* n_a*0.002991e-23_wp */
 #define IMPL_THERMO_WEIGHT (717.942189 / 1005.0)
 static const double M_PI_ = 3.14159265358979323846;  /* 4._wp*atan(1._wp) */
+static const double p_0 = 100000.0;
 
 struct oracle_ctx {
   int ny, nx, nl, n_levels, n_oro_layers, n_flat_layers;
@@ -61,6 +62,14 @@ struct oracle_ctx {
   double *p_grad_decel_factor, *mom_diff_tend_x, *mom_diff_tend_y, *mom_diff_tend_z;
   double *heating_diss, *phase_trans_rates, *phase_trans_heating_rate, *temp_diff_heating;
   double *condensates_sediment_heat, *mass_diff_tendency, *a_rain;
+  /* lateral boundary conditions (t_bc, mo_definitions.F90:117-131): two time levels, the
+   * rescale factors, the level indices (1-based) and the time of the older level */
+  int bc_on, bc_index_old, bc_index_new, dtime_bc;
+  double t_latest_bc;
+  double *bc_rho[2], *bc_rhotheta_v[2], *bc_wind_u[2], *bc_wind_v[2], *bc_wind_w[2];
+  double *scalar_bc_factor, *u_bc_factor, *v_bc_factor;
+  lgame_bc_loader bc_loader;
+  void* bc_user;
 };
 
 /* extents */
@@ -148,6 +157,11 @@ void oracle_destroy(oracle_ctx* o) {
   double** p = &o->z_scalar;
   double** end = &o->a_rain;
   for (; p <= end; ++p) free(*p);
+  for (int i = 0; i < 2; ++i) {
+    free(o->bc_rho[i]); free(o->bc_rhotheta_v[i]); free(o->bc_wind_u[i]); free(o->bc_wind_v[i]);
+    free(o->bc_wind_w[i]);
+  }
+  free(o->scalar_bc_factor); free(o->u_bc_factor); free(o->v_bc_factor);
   free(o);
 }
 
@@ -268,6 +282,163 @@ int oracle_get_diag(oracle_ctx* o, double* const* f, int nfields) {
   diag_ptrs(o, p, n);
   for (int i = 0; i < LGAME_DIAG_NFIELDS; ++i)
     if (f[i]) memcpy(f[i], p[i], n[i]*sizeof(double));
+  return LGAME_OK;
+}
+
+/* ---- lateral boundary conditions, src/io/mo_boundaries.F90 ------------------------- */
+
+/* setup_bc_factor, mo_boundaries.F90:125-170.  dist_from_boundary is real(wp) in the
+ * Fortran: the integer minimum converts to double before the division by n_swamp. */
+static void setup_bc_factor(oracle_ctx* o, int n_swamp) {
+  DIMS;
+  for (int ji = 1; ji <= ny; ++ji)
+    for (int jk = 1; jk <= nx; ++jk) {
+      int d = ji - 1; if (jk - 1 < d) d = jk - 1; if (ny - ji < d) d = ny - ji; if (nx - jk < d) d = nx - jk;
+      double f = 1.0 - (double)d/n_swamp;
+      if (f < 0.0) f = 0.0;
+      const double sn = sin(0.5*M_PI_*f);
+      o->scalar_bc_factor[(ji-1) + (size_t)ny*(jk-1)] = sn*sn;
+    }
+  for (int ji = 1; ji <= ny; ++ji)
+    for (int jk = 1; jk <= nx+1; ++jk) {
+      int d = ji - 1; if (jk - 1 < d) d = jk - 1; if (ny - ji < d) d = ny - ji; if (nx + 1 - jk < d) d = nx + 1 - jk;
+      double f = 1.0 - (double)d/n_swamp;
+      if (f < 0.0) f = 0.0;
+      const double sn = sin(0.5*M_PI_*f);
+      o->u_bc_factor[(ji-1) + (size_t)ny*(jk-1)] = sn*sn;
+    }
+  for (int ji = 1; ji <= ny+1; ++ji)
+    for (int jk = 1; jk <= nx; ++jk) {
+      int d = ji - 1; if (jk - 1 < d) d = jk - 1; if (ny + 1 - ji < d) d = ny + 1 - ji; if (nx - jk < d) d = nx - jk;
+      double f = 1.0 - (double)d/n_swamp;
+      if (f < 0.0) f = 0.0;
+      const double sn = sin(0.5*M_PI_*f);
+      o->v_bc_factor[(ji-1) + (size_t)(ny+1)*(jk-1)] = sn*sn;
+    }
+}
+
+int oracle_bc_setup(oracle_ctx* o, int n_swamp, int dtime_bc, double t_latest_bc, lgame_bc_loader loader,
+                    void* user) {
+  if (!o || n_swamp < 1 || dtime_bc < 1) return LGAME_ERR_INVALID_ARG;
+  if (o->lperiodic) return LGAME_ERR_STATE;
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
+  const size_t nW = (size_t)ny*nx*(nl+1);
+  if (!o->scalar_bc_factor) {
+    for (int i = 0; i < 2; ++i) {
+      o->bc_rho[i] = zalloc(nS*o->ncons); o->bc_rhotheta_v[i] = zalloc(nS); o->bc_wind_u[i] = zalloc(nU);
+      o->bc_wind_v[i] = zalloc(nV); o->bc_wind_w[i] = zalloc(nW);
+    }
+    o->scalar_bc_factor = zalloc((size_t)ny*nx); o->u_bc_factor = zalloc((size_t)ny*(nx+1));
+    o->v_bc_factor = zalloc((size_t)(ny+1)*nx);
+  }
+  setup_bc_factor(o, n_swamp);
+  o->bc_index_old = 1;  /* control.F90:358-359 */
+  o->bc_index_new = 2;
+  o->dtime_bc = dtime_bc;
+  o->t_latest_bc = t_latest_bc;
+  o->bc_loader = loader;
+  o->bc_user = user;
+  o->bc_on = 1;
+  return LGAME_OK;
+}
+
+int oracle_set_bc(oracle_ctx* o, int time_index, const double* rho, const double* rhotheta_v,
+                  const double* wind_u, const double* wind_v, const double* wind_w) {
+  if (!o || !o->bc_on || time_index < 1 || time_index > 2 || !rho || !rhotheta_v || !wind_u || !wind_v || !wind_w)
+    return LGAME_ERR_INVALID_ARG;
+  DIMS;
+  const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
+  const size_t nW = (size_t)ny*nx*(nl+1);
+  const int t = time_index - 1;
+  memcpy(o->bc_rho[t], rho, nS*o->ncons*sizeof(double));
+  memcpy(o->bc_rhotheta_v[t], rhotheta_v, nS*sizeof(double));
+  memcpy(o->bc_wind_u[t], wind_u, nU*sizeof(double));
+  memcpy(o->bc_wind_v[t], wind_v, nV*sizeof(double));
+  memcpy(o->bc_wind_w[t], wind_w, nW*sizeof(double));
+  return LGAME_OK;
+}
+
+/* update_boundaries, mo_boundaries.F90:19-97 */
+int oracle_update_boundaries(oracle_ctx* o, int slot, double t_now) {
+  if (!o || !o->bc_on || slot < 0 || slot > 1) return LGAME_ERR_INVALID_ARG;
+  DIMS;
+  const int nc = o->nc, ncons = o->ncons;
+  const double old_weight = 1.0 - (t_now - o->t_latest_bc)/o->dtime_bc;
+  if (old_weight < 0.0) {
+    /* read_boundaries(bc, t_latest_bc+dtime_bc, bc%index_old), then the index swap */
+    if (!o->bc_loader || o->bc_loader(o->bc_user, o->t_latest_bc + o->dtime_bc, o->bc_index_old) != 0)
+      return LGAME_ERR_STATE;
+    o->bc_index_old = o->bc_index_new;
+    o->bc_index_new = 1;
+    if (o->bc_index_old == 1) o->bc_index_new = 2;
+    o->t_latest_bc = o->t_latest_bc + o->dtime_bc;
+  }
+  const double new_weight = 1.0 - old_weight;
+  const int io = o->bc_index_old - 1, in = o->bc_index_new - 1;
+  double* rho = o->rho[slot]; double* rt = o->rhotheta_v[slot];
+  double* u = o->wind_u[slot]; double* v = o->wind_v[slot]; double* w = o->wind_w[slot];
+  #pragma omp parallel for
+  for (int ji = 1; ji <= ny; ++ji)
+    for (int jk = 1; jk <= nx; ++jk) {
+      const double f = o->scalar_bc_factor[(ji-1) + (size_t)ny*(jk-1)];
+      for (int jl = 1; jl <= nl; ++jl) {
+        for (int jc = 1; jc <= ncons; ++jc) {
+          const size_t q = IRHO(ji,jk,jl,jc);
+          rho[q] = f*(old_weight*o->bc_rho[io][q] + new_weight*o->bc_rho[in][q]) + (1.0 - f)*rho[q];
+        }
+        const size_t q = IS(ji,jk,jl);
+        rt[q] = f*(old_weight*o->bc_rhotheta_v[io][q] + new_weight*o->bc_rhotheta_v[in][q]) + (1.0 - f)*rt[q];
+      }
+      for (int jl = 1; jl <= nl+1; ++jl) {
+        const size_t q = IS(ji,jk,jl);
+        w[q] = f*(old_weight*o->bc_wind_w[io][q] + new_weight*o->bc_wind_w[in][q]) + (1.0 - f)*w[q];
+      }
+    }
+  #pragma omp parallel for
+  for (int ji = 1; ji <= ny; ++ji)
+    for (int jk = 1; jk <= nx+1; ++jk) {
+      const double f = o->u_bc_factor[(ji-1) + (size_t)ny*(jk-1)];
+      for (int jl = 1; jl <= nl; ++jl) {
+        const size_t q = IU(ji,jk,jl);
+        u[q] = f*(old_weight*o->bc_wind_u[io][q] + new_weight*o->bc_wind_u[in][q]) + (1.0 - f)*u[q];
+      }
+    }
+  #pragma omp parallel for
+  for (int ji = 1; ji <= ny+1; ++ji)
+    for (int jk = 1; jk <= nx; ++jk) {
+      const double f = o->v_bc_factor[(ji-1) + (size_t)(ny+1)*(jk-1)];
+      for (int jl = 1; jl <= nl; ++jl) {
+        const size_t q = IV(ji,jk,jl);
+        v[q] = f*(old_weight*o->bc_wind_v[io][q] + new_weight*o->bc_wind_v[in][q]) + (1.0 - f)*v[q];
+      }
+    }
+  /* theta_v_pert and exner_pert from the relaxed state, mo_boundaries.F90:92-95 */
+  const size_t nS = (size_t)ny*nx*nl;
+  const double* rho_g = rho + nS*(size_t)nc;
+  double* tp = o->theta_v_pert[slot]; double* ep = o->exner_pert[slot];
+  #pragma omp parallel for
+  for (size_t i = 0; i < nS; ++i) {
+    tp[i] = rt[i]/rho_g[i] - o->theta_v_bg[i];
+    ep[i] = pow(r_d*rt[i]/p_0, r_d/c_d_v) - o->exner_bg[i];
+  }
+  return LGAME_OK;
+}
+
+int oracle_bc_state(oracle_ctx* o, int* index_old, int* index_new, double* t_latest_bc) {
+  if (!o || !o->bc_on) return LGAME_ERR_STATE;
+  if (index_old) *index_old = o->bc_index_old;
+  if (index_new) *index_new = o->bc_index_new;
+  if (t_latest_bc) *t_latest_bc = o->t_latest_bc;
+  return LGAME_OK;
+}
+
+int oracle_bc_factors(oracle_ctx* o, double* scalar_f, double* u_f, double* v_f) {
+  if (!o || !o->bc_on) return LGAME_ERR_STATE;
+  DIMS;
+  if (scalar_f) memcpy(scalar_f, o->scalar_bc_factor, (size_t)ny*nx*sizeof(double));
+  if (u_f) memcpy(u_f, o->u_bc_factor, (size_t)ny*(nx+1)*sizeof(double));
+  if (v_f) memcpy(v_f, o->v_bc_factor, (size_t)(ny+1)*nx*sizeof(double));
   return LGAME_OK;
 }
 

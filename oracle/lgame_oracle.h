@@ -34,8 +34,20 @@ int  oracle_set_state(oracle_ctx* o, int slot, const double* const* fields, int 
 int  oracle_get_state(oracle_ctx* o, int slot, double* const* fields, int nfields);
 int  oracle_set_diag(oracle_ctx* o, const double* const* fields, int nfields);
 int  oracle_get_diag(oracle_ctx* o, double* const* fields, int nfields);
-/* one step, exactly mo_manage_pchevi.F90:27-118 (periodic / no boundary relaxation) */
+/* one step, exactly mo_manage_pchevi.F90:27-118; a non-periodic run with boundary data set
+ * up ends with oracle_update_boundaries(o, new_slot, (total_step_counter+1)*dtime) */
 int  oracle_pchevi(oracle_ctx* o, int old_slot, int new_slot, int total_step_counter);
+/* lateral boundary relaxation, mo_boundaries.F90 (same contract as lgame_gpu_bc_setup,
+ * lgame_gpu_set_bc, lgame_gpu_update_boundaries and lgame_gpu_bc_state) */
+int  oracle_bc_setup(oracle_ctx* o, int n_swamp, int dtime_bc, double t_latest_bc, lgame_bc_loader loader,
+                     void* user);
+int  oracle_set_bc(oracle_ctx* o, int time_index, const double* rho, const double* rhotheta_v,
+                   const double* wind_u, const double* wind_v, const double* wind_w);
+int  oracle_update_boundaries(oracle_ctx* o, int slot, double t_now);
+int  oracle_bc_state(oracle_ctx* o, int* index_old, int* index_new, double* t_latest_bc);
+/* the rescale factors of setup_bc_factor (mo_boundaries.F90:125-170) after oracle_bc_setup:
+ * scalar (ny x nx), u (ny x (nx+1)), v ((ny+1) x nx), column-major */
+int  oracle_bc_factors(oracle_ctx* o, double* scalar_f, double* u_f, double* v_f);
 int  oracle_budgets(oracle_ctx* o, int slot, double* out, int nout);
 /* number of OpenMP threads the oracle runs with */
 int  oracle_num_threads(void);

@@ -33,7 +33,8 @@ def load():
         lib = C.CDLL(str(LIB_PATH))
         vp, i = C.c_void_p, C.c_int
         pp = C.POINTER(C.POINTER(C.c_double))
-        from lgame_gpu import Config  # same struct layout (include/lgame_gpu.h)
+        from lgame_gpu import BC_LOADER, Config  # same struct layout (include/lgame_gpu.h)
+        dp = C.POINTER(C.c_double)
         for name, res, args in [
             ("oracle_create", i, [C.POINTER(Config), C.POINTER(vp)]),
             ("oracle_destroy", None, [vp]),
@@ -46,6 +47,11 @@ def load():
             ("oracle_budgets", i, [vp, i, C.POINTER(C.c_double), i]),
             ("oracle_num_threads", i, []),
             ("oracle_thomas", None, [C.POINTER(C.c_double)] * 5 + [i]),
+            ("oracle_bc_setup", i, [vp, i, i, C.c_double, BC_LOADER, vp]),
+            ("oracle_set_bc", i, [vp, i] + [dp] * 5),
+            ("oracle_update_boundaries", i, [vp, i, C.c_double]),
+            ("oracle_bc_state", i, [vp, C.POINTER(i), C.POINTER(i), dp]),
+            ("oracle_bc_factors", i, [vp, dp, dp, dp]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -97,6 +103,37 @@ class Oracle:
         rc = self.lib.oracle_pchevi(self.h, old_slot, new_slot, step)
         if rc != 0:
             raise RuntimeError(f"oracle_pchevi failed: {rc}")
+
+    # lateral boundary relaxation (mo_boundaries.F90), as lgame_gpu.GpuModel
+    def bc_setup(self, n_swamp, dtime_bc, t_latest_bc=0.0, loader=None):
+        from lgame_gpu import bc_callback
+        self._bc_cb = bc_callback(self, loader)
+        rc = self.lib.oracle_bc_setup(self.h, n_swamp, dtime_bc, t_latest_bc, self._bc_cb, None)
+        if rc != 0:
+            raise RuntimeError(f"oracle_bc_setup failed: {rc}")
+
+    def set_bc(self, time_index, bc):
+        from lgame_gpu import BC_FIELDS
+        arrs = [np.asfortranarray(bc[f], dtype=np.float64) for f in BC_FIELDS]
+        dp = C.POINTER(C.c_double)
+        assert self.lib.oracle_set_bc(self.h, time_index, *[a.ctypes.data_as(dp) for a in arrs]) == 0
+
+    def update_boundaries(self, slot, t_now):
+        rc = self.lib.oracle_update_boundaries(self.h, slot, t_now)
+        if rc != 0:
+            raise RuntimeError(f"oracle_update_boundaries failed: {rc}")
+
+    def bc_state(self):
+        io, inew, t = C.c_int(), C.c_int(), C.c_double()
+        assert self.lib.oracle_bc_state(self.h, C.byref(io), C.byref(inew), C.byref(t)) == 0
+        return io.value, inew.value, t.value
+
+    def bc_factors(self):
+        ny, nx = self.shapes["rhotheta_v"][:2]
+        fs, fu, fv = (np.zeros(sh, order="F") for sh in [(ny, nx), (ny, nx + 1), (ny + 1, nx)])
+        dp = C.POINTER(C.c_double)
+        assert self.lib.oracle_bc_factors(self.h, *[a.ctypes.data_as(dp) for a in (fs, fu, fv)]) == 0
+        return fs, fu, fv
 
     def budgets(self, slot):
         out = np.zeros(11)
