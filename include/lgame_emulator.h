@@ -68,7 +68,9 @@ int  lgame_emu_train_step(lgame_emu* emu, const float* x, const float* y, int ba
 /* Training data resident on the device: upload once, then epochs over shuffled batches. */
 int  lgame_emu_set_dataset(lgame_emu* emu, const float* x, const float* y, long long n);
 int  lgame_emu_train_epoch(lgame_emu* emu, int batch, float lr, unsigned long long seed, float* mean_loss);
-/* Heating rates of n columns (host arrays, any n; processed in batches of batch_max). */
+/* Heating rates of n columns (host arrays, any n; processed in batches of batch_max).
+ * Page-locked x and y are read and written by the GPU directly over the CPU-GPU link;
+ * other host arrays are copied through device buffers.  Both give the same bits. */
 int  lgame_emu_infer(lgame_emu* emu, const float* x, long long n, float* y);
 /* Tensor-core GEMM C = A * B^T (BF16 bit patterns in, FP32 out, host arrays), A: M x K,
  * B: N x K, both row-major; M % 128 == 0, K % 64 == 0, N % 64 == 0.  Exposed for tests. */
