@@ -460,6 +460,8 @@ def run_ours(args):
             # end to end through the C ABI with pinned host buffers
             e2e = measure_e2e(L, g, hm, args)
             results[prec]["e2e"] = e2e
+            if rank == 0 and ws == 1:
+                results[prec]["output"] = measure_output(L, g, n, peaks)
         g.close()
         results[prec].pop("model")
         torch.cuda.synchronize()
@@ -502,6 +504,8 @@ def run_ours(args):
                         "kernel_shares": fp64["profile"]["shares"]}
         if head_prec != L.PRECISION_FP64:
             line["split_speedup_vs_fp64"] = fp64["s_per_step"] / head["s_per_step"]
+    if "output" in head:
+        line["output"] = head["output"]
     if "e2e" in head:
         line["e2e"] = head["e2e"]
     else:
@@ -572,6 +576,53 @@ def boundary_bench(args, peaks, n_swamp: int = 5, reps: int = 20) -> dict:
             "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": gbs / peaks["hbm_gbs"], "peak_src": peaks["src"]},
             "finite": finite}
+
+
+def measure_output(L, g, n, peaks, reps: int = 5) -> dict:
+    """The output fields of the time loop (lgame_gpu_output: linear_combine_two_states and
+    write_output's variables as floats) for the two state slots.  Kernel: CUDA events on the
+    library's stream around calls that fetch no field (the kernel and the crash flag);
+    algorithmic bytes per cell: both states' rho (n_constituents), rhotheta_v, exner_pert,
+    u, v, w in FP64, theta_v_bg, exner_bg, z_scalar, z_w in FP64, n_constituents + 5 float
+    fields written.  End to end: every field copied into page-locked host arrays."""
+    import torch
+    ncons, cells = n.n_constituents, n.nx * n.ny * n.n_layers
+    per_cell = 2 * 8.0 * (ncons + 5) + 4 * 8.0 + 4.0 * (ncons + 5)
+    s = torch.cuda.ExternalStream(g.stream_handle())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g.output(0, 1, 0.5, 0.5, fields=[])
+    e0.record(s)
+    for _ in range(reps):
+        g.output(0, 1, 0.5, 0.5, fields=[])
+    e1.record(s)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    fp = []
+    host = {}
+    for f in L.OUTPUT_FIELDS:
+        if f == "rel_humidity" and ncons == 1:
+            continue
+        shape = (n.ny, n.nx, n.n_layers, ncons) if f == "rho" else (n.ny, n.nx, n.n_layers)
+        t = torch.empty(shape[::-1], dtype=torch.float32, pin_memory=True)
+        fp.append(t)
+        host[f] = t.numpy().T
+    import ctypes as C
+    ptrs = (C.POINTER(C.c_float) * len(L.OUTPUT_FIELDS))(
+        *[host[f].ctypes.data_as(C.POINTER(C.c_float)) if f in host else C.POINTER(C.c_float)()
+          for f in L.OUTPUT_FIELDS])
+    crashed = C.c_int()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        L.check(g.lib.lgame_gpu_output(g.h, 0, 1, 0.5, 0.5, ptrs, len(L.OUTPUT_FIELDS), C.byref(crashed)),
+                "lgame_gpu_output")
+    e2e_s = (time.perf_counter() - t0) / reps
+    d2h = sum(v.nbytes for v in host.values())
+    gbs = per_cell * cells / (ms * 1e-3) / 1e9
+    return {"kernel": "k_output", "avg_launch_ms": ms, "alg_bytes_per_cell": per_cell,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": gbs / peaks["hbm_gbs"], "peak_src": peaks["src"]},
+            "e2e_ms": e2e_s * 1e3, "d2h_bytes": d2h, "e2e_note": "all fields into page-locked host arrays",
+            "crashed": bool(crashed.value)}
 
 
 def measure_e2e(L, g, hm, args) -> dict:

@@ -162,6 +162,19 @@ enum lgame_diag_field {
   LGAME_DIAG_NFIELDS
 };
 
+/* ---- output fields (write_output, src/io/mo_write_out.F90:167-217) -------------------
+ * The variables of an output file, at the scalar points, as the file stores them (NF90_REAL:
+ * the FP64 values rounded to float), column-major host arrays. */
+enum lgame_output_field {
+  LGAME_OUTPUT_RHO = 0,          /* (ny,nx,nl,n_constituents)  mass densities          */
+  LGAME_OUTPUT_TEMPERATURE,      /* (ny,nx,nl)  (theta_v_bg + theta_v_pert)*(exner_bg + exner_pert) */
+  LGAME_OUTPUT_REL_HUMIDITY,     /* (ny,nx,nl)  rel_humidity (moist runs only)         */
+  LGAME_OUTPUT_WIND_U,           /* (ny,nx,nl)  0.5*(u(jk) + u(jk+1))                  */
+  LGAME_OUTPUT_WIND_V,           /* (ny,nx,nl)  0.5*(v(ji) + v(ji+1))                  */
+  LGAME_OUTPUT_WIND_W,           /* (ny,nx,nl)  w interpolated to the layer's z_scalar */
+  LGAME_OUTPUT_NFIELDS
+};
+
 /* Budget vector of lgame_gpu_budgets (mo_write_out.F90:226-304):
  *   out[0 .. n_constituents-1]  sum(rho(:,:,:,jc)*volume)        (masses)
  *   out[n_constituents]         sum(rhotheta_v*volume)
@@ -279,6 +292,17 @@ int  lgame_gpu_profile_report(lgame_gpu* ctx, char* buf, int len);
  * kernels are short (small grids).  Results are the same bits either way.  Graphs are not
  * used while per-kernel tracing is on.  No counterpart in the reference (a CPU program). */
 int  lgame_gpu_set_graphs(lgame_gpu* ctx, int enable);
+
+/* The output of the reference's time loop (control.F90:535-537): the state
+ *   state_write = coeff_1*state[slot_1] + coeff_2*state[slot_2]
+ * (linear_combine_two_states, mo_linear_combination.F90:15-37, which recomputes theta_v_pert
+ * from the combined rho and rhotheta_v), then the fields write_output puts in the file
+ * (mo_write_out.F90:167-217), in the order of enum lgame_output_field, as floats.  NULL
+ * entries are skipped; LGAME_OUTPUT_REL_HUMIDITY is not written in dry runs.  *crashed
+ * (if given) becomes 1 when the combined exner_pert holds a NaN, the reference's "model
+ * crashed" check (mo_write_out.F90:60-67), else 0.  Synchronous. */
+int  lgame_gpu_output(lgame_gpu* ctx, int slot_1, int slot_2, double coeff_1, double coeff_2,
+                      float* const* fields, int nfields, int* crashed);
 
 /* ---- lateral boundary relaxation (src/io/mo_boundaries.F90) --------------------------
  * Turns on the relaxation of a non-periodic run (lperiodic = 0; else LGAME_ERR_STATE):

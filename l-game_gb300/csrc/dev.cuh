@@ -109,6 +109,7 @@ constexpr double kC_D_V = 717.942189;
 constexpr double kC_V_V = 1396.475121;
 constexpr double kC_D_P = 1005.0;
 constexpr double kP_0 = 100000.0;
+constexpr double kR_V = 461.524879;
 constexpr double kM_D = 6.02214076e23 * 0.004810e-23;
 constexpr double kM_V = 6.02214076e23 * 0.002991e-23;
 constexpr double kIMPL_THERMO_WEIGHT = 717.942189 / 1005.0;
@@ -307,6 +308,29 @@ __device__ __forceinline__ double c_p_ice(double temperature) {
   return c / kM_V;
 }
 
+// saturation_pressure_ice_huang and _murphy, mo_dictionary.F90:416-442
+__device__ __forceinline__ double sat_ice_huang(double temperature) {
+  const double temp_c = temperature - kT_0;
+  const double d = temp_c + 868.0;
+  return exp(43.494 - 6545.8 / (temp_c + 278.0)) / (d * d);
+}
+__device__ __forceinline__ double sat_ice_murphy(double temperature) {
+  return exp(9.550426 - 5723.265 / temperature + 3.53068 * log(temperature) - 0.00728332 * temperature);
+}
+// saturation_pressure_over_ice, mo_dictionary.F90:318-353 (its blend is written "+ (1-w) +")
+__device__ __forceinline__ double sat_ice(double temperature) {
+  double t_local = temperature;
+  const double temp_c = t_local - kT_0;
+  if (temp_c >= -80.0) {
+    if (t_local > kT_0) t_local = kT_0;
+    return sat_ice_huang(t_local);
+  } else if (temp_c >= -100.0) {
+    const double huang_weight = (temp_c + 100.0) / 20.0;
+    return huang_weight * sat_ice_huang(t_local) + (1.0 - huang_weight) + sat_ice_murphy(t_local);
+  }
+  if (t_local < 110.0) t_local = 110.0;
+  return sat_ice_murphy(t_local);
+}
 // c_p_cond, mo_dictionary.F90:175-189 (odd constituents are ice, even are water)
 __device__ __forceinline__ double c_p_cond(int jc, double temperature) {
   return ((jc - 1) % 2 == 0) ? c_p_ice(temperature) : c_p_water(temperature);

@@ -80,6 +80,8 @@ struct lgame_gpu {
   double *bcf_s = nullptr, *bcf_u = nullptr, *bcf_v = nullptr;
   int* bc_rim = nullptr;  // plane indices of the swamp layer (any factor nonzero), split path
   int bc_nrim = 0;
+  // output fields (compact FP32, rho then T, RH, u, v, w), allocated at the first output
+  float* out_buf = nullptr;
   // per-kernel tracing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -280,6 +282,72 @@ __global__ void k_bc_update(Dims D, State S, StateF M, State B0, State B1, const
   }
   if (ji <= D.ny && jk <= D.nx + 1 && jl <= D.nl) relax(fu[p], B0.u, B1.u, S.u, M.u, IX(D, ji, jk, jl));
   if (ji <= D.ny + 1 && jk <= D.nx && jl <= D.nl) relax(fv[p], B0.v, B1.v, S.v, M.v, IX(D, ji, jk, jl));
+}
+
+// rel_humidity of mo_derived.F90:131-155 with the quotient by the saturation pressure folded
+// into one exponential: Huang's formulas are exp(a)/d^1.57 over water and exp(a)/d^2 over
+// ice, so vp/sat = vp*exp(1.57*log(d) - a) and vp*d*d*exp(-a), the same values to a few FP64
+// ulps with two transcendental calls fewer per point (the kernel below is bound by the FP64
+// pipe); below -80 C (Murphy's formula and the blend) the reference's form is kept.
+__device__ __forceinline__ double rel_humidity_out(double abs_humidity, double temperature) {
+  const double vp = abs_humidity * kR_V * temperature;
+  const double tc = temperature - kT_0;
+  if (temperature > kT_0) {
+    const double tw = tc > 100.0 ? 100.0 : tc;
+    return vp * exp(1.57 * log(tw + 105.0) - (34.494 - 4924.99 / (tw + 237.1)));
+  }
+  if (tc >= -80.0) {  // min(T, t_0) = T here
+    const double d = tc + 868.0;
+    return vp * (d * d) * exp(-(43.494 - 6545.8 / (tc + 278.0)));
+  }
+  return vp / sat_ice(temperature);
+}
+// FP64 -> float rounded to nearest, zeros included, in integer operations (narrow)
+__device__ __forceinline__ float to_f32(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  if (((hi & 0x7FFFFFFFu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+  return narrow(x);
+}
+
+// The output of the time loop: linear_combine_two_states (mo_linear_combination.F90:26-35)
+// of states A and B, then the fields of write_output (mo_write_out.F90:167-217), one thread per
+// scalar point, in the reference's order of operations (this file is compiled without fused
+// multiply-adds; the relative humidity as rel_humidity_out), rounded to float as the file
+// stores them.  out: compact column-major fields
+// of ny*nx*nl floats, rho (ncons of them), T, RH, u, v, w.  *nan_flag = 1 if a combined
+// exner_pert is NaN (mo_write_out.F90:60-67).
+__global__ void k_output(Dims D, Grid<double> G, State A, State B, double c1, double c2, float* out, int* nan_flag) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 1;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  const long long nS = (long long)D.ny * D.nx * D.nl;
+  const long long o = (long long)(ji - 1) + (long long)D.ny * ((long long)(jk - 1) + (long long)D.nx * (jl - 1));
+  double rho_g = 0.0, rho_v = 0.0;
+  for (int jc = 0; jc < D.ncons; ++jc) {
+    const long long qc = q + (long long)jc * D.fstride;
+    const double r = c1 * A.rho[qc] + c2 * B.rho[qc];
+    out[jc * nS + o] = to_f32(r);
+    if (jc == D.g - 1) rho_g = r;
+    if (jc == D.g) rho_v = r;  // water vapour follows the gas
+  }
+  const double rt = c1 * A.rt[q] + c2 * B.rt[q];
+  const double tp = rt / rho_g - G.theta_v_bg[q];
+  const double ep = c1 * A.ep[q] + c2 * B.ep[q];
+  if (isnan(ep)) atomicExch(nan_flag, 1);
+  float* f = out + (long long)D.ncons * nS;
+  const double temperature = (G.theta_v_bg[q] + tp) * (G.exner_bg[q] + ep);
+  f[o] = to_f32(temperature);
+  if (D.ncons > 1) f[nS + o] = to_f32(rel_humidity_out(rho_v, temperature));
+  const long long qu = IX(D, ji, jk + 1, jl), qv = IX(D, ji + 1, jk, jl), qw = IX(D, ji, jk, jl + 1);
+  const double u0 = c1 * A.u[q] + c2 * B.u[q], u1 = c1 * A.u[qu] + c2 * B.u[qu];
+  const double v0 = c1 * A.v[q] + c2 * B.v[q], v1 = c1 * A.v[qv] + c2 * B.v[qv];
+  const double w0 = c1 * A.w[q] + c2 * B.w[q], w1 = c1 * A.w[qw] + c2 * B.w[qw];
+  f[2 * nS + o] = to_f32(0.5 * (u0 + u1));
+  f[3 * nS + o] = to_f32(0.5 * (v0 + v1));
+  const double upper_weight = (G.z_scalar[q] - G.z_w[qw]) / (G.z_w[q] - G.z_w[qw]);
+  f[4 * nS + o] = to_f32(upper_weight * w0 + (1.0 - upper_weight) * w1);
 }
 
 // deterministic FP64 sums: every block sums a fixed strided subset in a fixed order;
@@ -961,6 +1029,39 @@ void trace_end(lgame_gpu* c, int slot) { cudaEventRecord(c->ev_pool[slot + 1], c
 }  // namespace lg
 
 extern "C" void* lgame_gpu_stream(const lgame_gpu* c) { return c ? (void*)c->stream : nullptr; }
+
+extern "C" int lgame_gpu_output(lgame_gpu* c, int slot_1, int slot_2, double coeff_1, double coeff_2,
+                                float* const* fields, int nfields, int* crashed) {
+  if (!c || !fields || nfields != LGAME_OUTPUT_NFIELDS || slot_1 < 0 || slot_1 > 1 || slot_2 < 0 || slot_2 > 1)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_output: bad arguments");
+  if (!c->grid_set) return set_err(LGAME_ERR_STATE, "lgame_gpu_output: lgame_gpu_set_grid has not been called");
+  const Dims& D = c->D;
+  const size_t nS = (size_t)D.ny * D.nx * D.nl;
+  if (!c->out_buf) {
+    const size_t n = (size_t)(D.ncons + 5) * nS;
+    CK(cudaMalloc(&c->out_buf, n * sizeof(float)));
+    c->allocations.push_back(c->out_buf);
+    c->bytes += (long long)(n * sizeof(float));
+  }
+  CK(cudaMemsetAsync(c->flag, 0, sizeof(int), c->stream));
+  k_output<<<grd(D, D.ny, D.nx, D.nl), blk(), 0, c->stream>>>(D, c->G, c->st[slot_1], c->st[slot_2], coeff_1, coeff_2,
+                                                              c->out_buf, c->flag);
+  int rc = klaunch_check(c, "k_output");
+  if (rc) return rc;
+  if (fields[LGAME_OUTPUT_RHO])
+    CK(cudaMemcpyAsync(fields[LGAME_OUTPUT_RHO], c->out_buf, sizeof(float) * nS * D.ncons, cudaMemcpyDeviceToHost,
+                       c->stream));
+  for (int k = LGAME_OUTPUT_TEMPERATURE; k < LGAME_OUTPUT_NFIELDS; ++k) {
+    if (!fields[k] || (k == LGAME_OUTPUT_REL_HUMIDITY && D.ncons == 1)) continue;
+    CK(cudaMemcpyAsync(fields[k], c->out_buf + (size_t)(D.ncons + k - 1) * nS, sizeof(float) * nS,
+                       cudaMemcpyDeviceToHost, c->stream));
+  }
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (crashed) *crashed = h;
+  return LGAME_OK;
+}
 
 // ---- lateral boundary relaxation, src/io/mo_boundaries.F90 -----------------------------
 

@@ -28,10 +28,26 @@ GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "are
                "exner_bg_grad_w", "gravity_m_v", "gravity_potential", "fvec_x", "fvec_y", "fvec_z",
                "trsk_weights_u", "trsk_weights_v"]
 STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w"]
+# fields of an output file (enum lgame_output_field), float32, scalar points
+OUTPUT_FIELDS = ["rho", "temperature", "rel_humidity", "wind_u", "wind_v", "wind_w"]
 # one level of lateral boundary data (t_bc, mo_definitions.F90:117-131), state-field shapes
 BC_FIELDS = ["rho", "rhotheta_v", "wind_u", "wind_v", "wind_w"]
 # lgame_bc_loader: (user, t_update, time_index) -> 0 on success
 BC_LOADER = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_double, C.c_int)
+
+
+def output_arrays(ny, nx, nl, ncons, fields=OUTPUT_FIELDS):
+    """Fortran-ordered float32 arrays for the selected output fields (no relative humidity in
+    dry runs) and the pointer array of lgame_gpu_output / oracle_output."""
+    out = {}
+    for f in fields:
+        if f == "rel_humidity" and ncons == 1:
+            continue
+        shape = (ny, nx, nl, ncons) if f == "rho" else (ny, nx, nl)
+        out[f] = np.zeros(shape, np.float32, order="F")
+    fp = C.POINTER(C.c_float)
+    ptrs = (fp * len(OUTPUT_FIELDS))(*[out[f].ctypes.data_as(fp) if f in out else fp() for f in OUTPUT_FIELDS])
+    return out, ptrs
 
 
 def bc_callback(model, loader):
@@ -146,6 +162,7 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_stream": (vp, [vp]),
         "lgame_gpu_set_profiling": (i, [vp, i]),
         "lgame_gpu_set_graphs": (i, [vp, i]),
+        "lgame_gpu_output": (i, [vp, i, i, d, d, C.POINTER(C.POINTER(C.c_float)), i, C.POINTER(i)]),
         "lgame_gpu_bc_setup": (i, [vp, i, i, d, BC_LOADER, vp]),
         "lgame_gpu_set_bc": (i, [vp, i] + [C.POINTER(C.c_double)] * 5),
         "lgame_gpu_update_boundaries": (i, [vp, i, d]),
@@ -369,6 +386,15 @@ class GpuModel:
     def set_graphs(self, enable: bool):
         """Launch each step after step 0 as a captured CUDA graph (the default) or kernel by kernel."""
         check(self.lib.lgame_gpu_set_graphs(self.h, 1 if enable else 0), "lgame_gpu_set_graphs")
+
+    def output(self, slot_1: int, slot_2: int, coeff_1: float, coeff_2: float, fields=OUTPUT_FIELDS):
+        """The fields of an output file for coeff_1*state[slot_1] + coeff_2*state[slot_2]
+        (float32 arrays, scalar points) and the crash flag; `fields` selects which to fetch."""
+        out, ptrs = output_arrays(self.ny, self.nx, self.nl, self.ncons, fields)
+        crashed = C.c_int()
+        check(self.lib.lgame_gpu_output(self.h, slot_1, slot_2, coeff_1, coeff_2, ptrs, len(OUTPUT_FIELDS),
+                                        C.byref(crashed)), "lgame_gpu_output")
+        return out, bool(crashed.value)
 
     # lateral boundary relaxation (mo_boundaries.F90)
     def bc_setup(self, n_swamp: int, dtime_bc: int, t_latest_bc: float = 0.0, loader=None):

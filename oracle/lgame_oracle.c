@@ -37,6 +37,7 @@ static const double c_d_p = 1005.0;
 #define IMPL_THERMO_WEIGHT (717.942189 / 1005.0)
 static const double M_PI_ = 3.14159265358979323846;  /* 4._wp*atan(1._wp) */
 static const double p_0 = 100000.0;
+static const double r_v = 461.524879;
 
 struct oracle_ctx {
   int ny, nx, nl, n_levels, n_oro_layers, n_flat_layers;
@@ -439,6 +440,97 @@ int oracle_bc_factors(oracle_ctx* o, double* scalar_f, double* u_f, double* v_f)
   if (scalar_f) memcpy(scalar_f, o->scalar_bc_factor, (size_t)ny*nx*sizeof(double));
   if (u_f) memcpy(u_f, o->u_bc_factor, (size_t)ny*(nx+1)*sizeof(double));
   if (v_f) memcpy(v_f, o->v_bc_factor, (size_t)(ny+1)*nx*sizeof(double));
+  return LGAME_OK;
+}
+
+/* ---- output fields, mo_write_out.F90:167-217 after linear_combine_two_states ---------- */
+
+/* saturation_pressure_over_water (mo_dictionary.F90:256-291) for temperatures above t_0,
+ * the only ones rel_humidity passes to it (temp_c > 0: Huang's formula) */
+static double sat_water_warm(double temperature) {
+  double temp_c = temperature - t_0;
+  if (temp_c > 100.0) temp_c = 100.0;
+  return exp(34.494 - 4924.99/(temp_c + 237.1))/pow(temp_c + 105.0, 1.57);
+}
+/* saturation_pressure_ice_huang and _murphy, mo_dictionary.F90:416-442 */
+static double sat_ice_huang(double temperature) {
+  const double temp_c = temperature - t_0;
+  const double d = temp_c + 868.0;
+  return exp(43.494 - 6545.8/(temp_c + 278.0))/(d*d);
+}
+static double sat_ice_murphy(double temperature) {
+  return exp(9.550426 - 5723.265/temperature + 3.53068*log(temperature) - 0.00728332*temperature);
+}
+/* saturation_pressure_over_ice, mo_dictionary.F90:318-353 (with its "+ (1-w) +" blend) */
+static double sat_ice(double temperature) {
+  double t_local = temperature;
+  const double temp_c = t_local - t_0;
+  if (temp_c >= -80.0) {
+    if (t_local > t_0) t_local = t_0;
+    return sat_ice_huang(t_local);
+  } else if (temp_c >= -100.0) {
+    const double huang_weight = (temp_c + 100.0)/20.0;
+    return huang_weight*sat_ice_huang(t_local) + (1.0 - huang_weight) + sat_ice_murphy(t_local);
+  }
+  if (t_local < 110.0) t_local = 110.0;
+  return sat_ice_murphy(t_local);
+}
+/* rel_humidity, mo_derived.F90:131-155 */
+static double rel_humidity(double abs_humidity, double temperature) {
+  const double vapour_pressure = abs_humidity*r_v*temperature;
+  double saturation_pressure = 0.0;
+  if (temperature > t_0) saturation_pressure = sat_water_warm(temperature);
+  if (temperature <= t_0) saturation_pressure = sat_ice(temperature);
+  return vapour_pressure/saturation_pressure;
+}
+
+int oracle_output(oracle_ctx* o, int slot_1, int slot_2, double coeff_1, double coeff_2, float* const* fields,
+                  int nfields, int* crashed) {
+  if (!o || !fields || nfields != LGAME_OUTPUT_NFIELDS || slot_1 < 0 || slot_1 > 1 || slot_2 < 0 || slot_2 > 1)
+    return LGAME_ERR_INVALID_ARG;
+  DIMS;
+  const int nc = o->nc, ncons = o->ncons;
+  const size_t nS = (size_t)ny*nx*nl;
+  /* state_write = linear_combine_two_states(state_1, state_2, ...), mo_linear_combination.F90:26-35 */
+  double* rho = (double*)malloc(nS*ncons*sizeof(double));
+  double* rt = (double*)malloc(nS*sizeof(double));
+  double* tp = (double*)malloc(nS*sizeof(double));
+  double* ep = (double*)malloc(nS*sizeof(double));
+  double* u = (double*)malloc((size_t)ny*(nx+1)*nl*sizeof(double));
+  double* v = (double*)malloc((size_t)(ny+1)*nx*nl*sizeof(double));
+  double* w = (double*)malloc((size_t)ny*nx*(nl+1)*sizeof(double));
+  if (!rho || !rt || !tp || !ep || !u || !v || !w) {
+    free(rho); free(rt); free(tp); free(ep); free(u); free(v); free(w);
+    return LGAME_ERR_ALLOC;
+  }
+  for (size_t i = 0; i < nS*ncons; ++i) rho[i] = coeff_1*o->rho[slot_1][i] + coeff_2*o->rho[slot_2][i];
+  for (size_t i = 0; i < nS; ++i) rt[i] = coeff_1*o->rhotheta_v[slot_1][i] + coeff_2*o->rhotheta_v[slot_2][i];
+  for (size_t i = 0; i < nS; ++i) tp[i] = rt[i]/rho[nS*(size_t)nc + i] - o->theta_v_bg[i];
+  for (size_t i = 0; i < nS; ++i) ep[i] = coeff_1*o->exner_pert[slot_1][i] + coeff_2*o->exner_pert[slot_2][i];
+  for (size_t i = 0; i < (size_t)ny*(nx+1)*nl; ++i) u[i] = coeff_1*o->wind_u[slot_1][i] + coeff_2*o->wind_u[slot_2][i];
+  for (size_t i = 0; i < (size_t)(ny+1)*nx*nl; ++i) v[i] = coeff_1*o->wind_v[slot_1][i] + coeff_2*o->wind_v[slot_2][i];
+  for (size_t i = 0; i < (size_t)ny*nx*(nl+1); ++i) w[i] = coeff_1*o->wind_w[slot_1][i] + coeff_2*o->wind_w[slot_2][i];
+  /* the crash check of write_output, mo_write_out.F90:60-67 */
+  int nan = 0;
+  for (size_t i = 0; i < nS; ++i) nan |= isnan(ep[i]);
+  if (crashed) *crashed = nan;
+  /* the fields as stored (NF90_REAL: rounded to float) */
+  if (fields[0]) for (size_t i = 0; i < nS*ncons; ++i) fields[0][i] = (float)rho[i];
+  for (int jl = 1; jl <= nl; ++jl)
+    for (int jk = 1; jk <= nx; ++jk)
+      for (int ji = 1; ji <= ny; ++ji) {
+        const size_t q = IS(ji,jk,jl);
+        const double temperature = (o->theta_v_bg[q] + tp[q])*(o->exner_bg[q] + ep[q]);
+        if (fields[1]) fields[1][q] = (float)temperature;
+        if (fields[2] && ncons > 1) fields[2][q] = (float)rel_humidity(rho[IRHO(ji,jk,jl,nc+2)], temperature);
+        if (fields[3]) fields[3][q] = (float)(0.5*(u[IU(ji,jk,jl)] + u[IU(ji,jk+1,jl)]));
+        if (fields[4]) fields[4][q] = (float)(0.5*(v[IV(ji,jk,jl)] + v[IV(ji+1,jk,jl)]));
+        if (fields[5]) {
+          const double upper_weight = (o->z_scalar[q] - o->z_w[IS(ji,jk,jl+1)])/(o->z_w[IS(ji,jk,jl)] - o->z_w[IS(ji,jk,jl+1)]);
+          fields[5][q] = (float)(upper_weight*w[IS(ji,jk,jl)] + (1.0 - upper_weight)*w[IS(ji,jk,jl+1)]);
+        }
+      }
+  free(rho); free(rt); free(tp); free(ep); free(u); free(v); free(w);
   return LGAME_OK;
 }
 

@@ -45,6 +45,10 @@ int  oracle_set_bc(oracle_ctx* o, int time_index, const double* rho, const doubl
                    const double* wind_u, const double* wind_v, const double* wind_w);
 int  oracle_update_boundaries(oracle_ctx* o, int slot, double t_now);
 int  oracle_bc_state(oracle_ctx* o, int* index_old, int* index_new, double* t_latest_bc);
+/* the output fields of write_output for coeff_1*state[slot_1] + coeff_2*state[slot_2]
+ * (same contract as lgame_gpu_output) */
+int  oracle_output(oracle_ctx* o, int slot_1, int slot_2, double coeff_1, double coeff_2, float* const* fields,
+                   int nfields, int* crashed);
 /* the rescale factors of setup_bc_factor (mo_boundaries.F90:125-170) after oracle_bc_setup:
  * scalar (ny x nx), u (ny x (nx+1)), v ((ny+1) x nx), column-major */
 int  oracle_bc_factors(oracle_ctx* o, double* scalar_f, double* u_f, double* v_f);

@@ -52,6 +52,8 @@ def load():
             ("oracle_update_boundaries", i, [vp, i, C.c_double]),
             ("oracle_bc_state", i, [vp, C.POINTER(i), C.POINTER(i), dp]),
             ("oracle_bc_factors", i, [vp, dp, dp, dp]),
+            ("oracle_output", i, [vp, i, i, C.c_double, C.c_double, C.POINTER(C.POINTER(C.c_float)), i,
+                                  C.POINTER(i)]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -103,6 +105,16 @@ class Oracle:
         rc = self.lib.oracle_pchevi(self.h, old_slot, new_slot, step)
         if rc != 0:
             raise RuntimeError(f"oracle_pchevi failed: {rc}")
+
+    def output(self, slot_1, slot_2, coeff_1, coeff_2):
+        from lgame_gpu import OUTPUT_FIELDS, output_arrays
+        ny, nx, nl = self.shapes["rhotheta_v"]
+        out, ptrs = output_arrays(ny, nx, nl, self.ncons)
+        crashed = C.c_int()
+        rc = self.lib.oracle_output(self.h, slot_1, slot_2, coeff_1, coeff_2, ptrs, len(OUTPUT_FIELDS), C.byref(crashed))
+        if rc != 0:
+            raise RuntimeError(f"oracle_output failed: {rc}")
+        return out, bool(crashed.value)
 
     # lateral boundary relaxation (mo_boundaries.F90), as lgame_gpu.GpuModel
     def bc_setup(self, n_swamp, dtime_bc, t_latest_bc=0.0, loader=None):
