@@ -654,8 +654,34 @@ def measure_e2e(L, g, hm, args) -> dict:
     for k in range(k_e2e):
         g.pchevi_host(old, new, k + 1)
     el = time.perf_counter() - t0
+    link = link_rates()
+    floor_ms = (h2d / link["h2d_gbs"] + d2h / link["d2h_gbs"]) / 1e6
     return {"value": k_e2e / el, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-            "steps": k_e2e, "note": "lgame_gpu_pchevi_host: pinned host state in, new state out, every step"}
+            "steps": k_e2e, "note": "lgame_gpu_pchevi_host: pinned host state in, new state out, every step",
+            "ms_per_step": el / k_e2e * 1e3, "link": link, "transfer_floor_ms": floor_ms}
+
+
+def link_rates(nbytes: int = 1 << 31, reps: int = 3) -> dict:
+    """Copy-engine rates of the CPU-GPU link between page-locked host memory and the device
+    (CUDA events around torch copies of nbytes, each direction alone).  The state transfer of
+    lgame_gpu_pchevi_host moves its bytes one direction at a time, so in + out at these rates
+    is its floor."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = {}
+    for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        out[name] = reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del h, d
+    return out
 
 
 def main():
