@@ -4,7 +4,8 @@
 
 CPU: the oracle against a numpy restatement of the Fortran; density, temperature and the
 centred winds bit for bit (same operations, same order, then rounded to float), relative
-humidity within one float ulp (exp, log and pow of two libraries).  GPU: lgame_gpu_output
+humidity within two float ulps (exp, log and pow of two libraries), over every branch of
+its saturation pressures.  GPU: lgame_gpu_output
 against the oracle on the same two states, with the same bars, in both precision modes (the
 output reads the FP64 state either way).
 """
@@ -32,7 +33,8 @@ def _sat_ice_murphy(t):
 def _rel_humidity(rho_v, t):
     vp = rho_v * R_V * t
     tcw = np.minimum(t - T_0, 100.0)
-    warm = np.exp(34.494 - 4924.99 / (tcw + 237.1)) / np.power(tcw + 105.0, 1.57)
+    with np.errstate(invalid="ignore"):  # the warm formula at cold points, discarded below
+        warm = np.exp(34.494 - 4924.99 / (tcw + 237.1)) / np.power(tcw + 105.0, 1.57)
     tc = t - T_0
     ice = np.where(tc >= -80.0, _sat_ice_huang(np.minimum(t, T_0)),
                    np.where(tc >= -100.0,
@@ -101,6 +103,46 @@ def test_output_crash_flag_oracle():
     assert crashed is True
     _, crashed = o.output(1, 1, 0.5, 0.5)
     assert crashed is False
+    o.close()
+
+
+def _all_branch_states():
+    """The small jet's state with rhotheta_v rewritten so that the output temperature spans
+    100-400 K: every branch of rel_humidity (Huang over water with the 100 C clip, Huang over
+    ice, the blend between -100 C and -80 C, Murphy with the 110 K clip)."""
+    hm, cfg, o = _two_states("jet", 1)
+    g = hm.ncons - 2
+    out = []
+    for slot in (0, 1):
+        st = o.get_state(slot)
+        exner = hm.grid["exner_bg"] + st["exner_pert"]
+        t_target = np.linspace(100.0, 400.0, exner.size).reshape(exner.shape, order="F")
+        st["rhotheta_v"] = st["rho"][..., g] * t_target / exner
+        o.set_state(slot, st)
+        out.append(st)
+    return hm, cfg, o, out
+
+
+def test_output_humidity_all_branches_oracle():
+    hm, cfg, o, (a, b) = _all_branch_states()
+    got, _ = o.output(0, 1, 0.5, 0.5)
+    exp, _ = _expected(a, b, hm.grid, 0.5, 0.5, hm.ncons)
+    t = exp["temperature"]
+    assert t.min() < 150.0 and t.max() > 380.0
+    _compare(got, exp)
+    o.close()
+
+
+@pytest.mark.gpu
+def test_output_humidity_all_branches_gpu():
+    hm, cfg, o, _ = _all_branch_states()
+    g = L.GpuModel(cfg, hm.grid)
+    for s in (0, 1):
+        g.set_state(s, o.get_state(s))
+    got, _ = g.output(0, 1, 0.5, 0.5)
+    ref, _ = o.output(0, 1, 0.5, 0.5)
+    _compare(got, {f: v.astype(np.float64) if f == "rel_humidity" else v for f, v in ref.items()})
+    g.close()
     o.close()
 
 
