@@ -74,4 +74,9 @@ def test_null_arguments_are_errors():
     assert lib.lgame_gpu_create(None, None) == L.ERR_INVALID_ARG
     assert lib.lgame_gpu_pchevi(None, 0, 1, 0, 0, 0.0) == L.ERR_INVALID_ARG
     assert lib.lgame_gpu_set_grid(None, None, 0) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_output(None, 0, 1, 0.5, 0.5, None, 6, None) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_bc_setup(None, 5, 10800, 0.0, L.BC_LOADER(), None) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_set_bc(None, 1, None, None, None, None, None) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_update_boundaries(None, 0, 0.0) == L.ERR_INVALID_ARG
+    assert lib.lgame_gpu_bc_state(None, None, None, None) == L.ERR_INVALID_ARG
     lib.lgame_gpu_destroy(None)
