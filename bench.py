@@ -663,9 +663,9 @@ def measure_e2e(L, g, hm, args) -> dict:
 
 def link_rates(nbytes: int = 1 << 31, reps: int = 3) -> dict:
     """Copy-engine rates of the CPU-GPU link between page-locked host memory and the device
-    (CUDA events around torch copies of nbytes, each direction alone).  The state transfer of
-    lgame_gpu_pchevi_host moves its bytes one direction at a time, so in + out at these rates
-    is its floor."""
+    (CUDA events around torch copies of nbytes, each direction alone).  In + out at these
+    rates is the floor of lgame_gpu_pchevi_host's state transfer, which moves one direction at
+    a time; part of the copy-out runs while the step still computes."""
     import torch
     h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
     d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")

@@ -233,7 +233,9 @@ int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
  * When every array is page-locked and mapped (cudaHostAlloc / cudaHostRegister with
  * mapping; on Grace systems the GPU then reaches it over the coherent CPU-GPU link), the
  * GPU reads and writes the host arrays itself and fills the FP32 state mirror in the
- * same pass; otherwise the copy engines move the state.  Slots 0 and 1 are used. */
+ * same pass; otherwise the copy engines move the state.  In split precision (without a
+ * boundary relaxation), fields of the new state that are final before the step ends are
+ * copied out on a second stream while the step still runs.  Slots 0 and 1 are used. */
 int  lgame_gpu_pchevi_host(lgame_gpu* ctx, const double* const* state_old,
                            double* const* state_new, int nfields,
                            int total_step_counter, int lrad_update, double t_0);

@@ -82,6 +82,12 @@ struct lgame_gpu {
   int bc_nrim = 0;
   // output fields (compact FP32, rho then T, RH, u, v, w), allocated at the first output
   float* out_buf = nullptr;
+  // lgame_gpu_pchevi_host: a second stream that copies the fields of the new state out while
+  // the step still runs, and the two events the step records when they are final
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_mark[2] = {nullptr, nullptr};
+  bool mark_on = false;
+  int marks[2] = {0, 0};
   // per-kernel tracing
   bool profiling = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -161,13 +167,13 @@ int copy_h2d(lgame_gpu* c, double* dev, const double* host, Ext e) {
   CK(cudaMemcpy3DAsync(&p, c->stream));
   return LGAME_OK;
 }
-int copy_d2h(lgame_gpu* c, double* host, const double* dev, Ext e) {
+int copy_d2h(lgame_gpu* c, double* host, const double* dev, Ext e, cudaStream_t stream = nullptr) {
   cudaMemcpy3DParms p = {};
   p.srcPtr = make_cudaPitchedPtr((void*)dev, (size_t)c->D.P * sizeof(double), (size_t)c->D.P, (size_t)c->D.NX1);
   p.dstPtr = make_cudaPitchedPtr(host, e.n1 * sizeof(double), e.n1, e.n2);
   p.extent = make_cudaExtent(e.n1 * sizeof(double), e.n2, e.n3);
   p.kind = cudaMemcpyDeviceToHost;
-  CK(cudaMemcpy3DAsync(&p, c->stream));
+  CK(cudaMemcpy3DAsync(&p, stream ? stream : c->stream));
   return LGAME_OK;
 }
 
@@ -553,6 +559,19 @@ int split_sync_carried(lgame_gpu* c, bool to_split) {
 
 int trace_begin_cb(void* c, const char* name) { return lg::trace_begin((lgame_gpu*)c, name); }
 void trace_end_cb(void* c, int slot) { lg::trace_end((lgame_gpu*)c, slot); }
+// marks of the split step for lgame_gpu_pchevi_host: event 0 after the second substep's wind
+// update (u and v final), event 1 after its vertical solve (rhotheta_v, theta_v_pert,
+// exner_pert, w and the gas density final; the tracer solver writes only the other densities)
+int mark_begin_cb(void* p, const char* name) {
+  auto* c = (lgame_gpu*)p;
+  if (std::strcmp(name, "ks_tend_wind") == 0 && ++c->marks[0] == 2) return 0;
+  if (std::strcmp(name, "ks_column_ver") == 0 && ++c->marks[1] == 2) return 1;
+  return -1;
+}
+void mark_end_cb(void* p, int k) {
+  auto* c = (lgame_gpu*)p;
+  if (cudaEventRecord(c->ev_mark[k], c->stream) != cudaSuccess) c->marks[k] = -1;  // no early copy
+}
 
 int check_cfg(const lgame_config* cfg) {
   if (cfg->ny < 3 || cfg->nx < 3) return set_err(LGAME_ERR_BAD_DIMS, "ny and nx must be >= 3");
@@ -869,14 +888,15 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
                       c->pgcw};
       return split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
                         total_step_counter, c->stream, &c->kernels_last_step,
-                        c->profiling ? trace_begin_cb : nullptr, trace_end_cb, c);
+                        c->profiling ? trace_begin_cb : (c->mark_on ? mark_begin_cb : nullptr),
+                        c->profiling ? trace_end_cb : mark_end_cb, c);
     }
     return step_fp64(c, old_slot, new_slot, total_step_counter);
   };
   // After step 0 a step is the same sequence of launches for a given slot pair, so it runs as
   // a CUDA graph (one launch from the host instead of ~30).  Not with per-kernel tracing,
   // whose events are recorded between the launches.
-  if (c->use_graphs && !c->profiling && total_step_counter > 0) {
+  if (c->use_graphs && !c->profiling && !c->mark_on && total_step_counter > 0) {
     cudaGraphExec_t& exec = c->graph[old_slot];
     if (!exec) {
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
@@ -971,9 +991,42 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     CK(cudaMemcpyAsync(B.v, A.v, F, cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaMemcpyAsync(B.w, A.w, F, cudaMemcpyDeviceToDevice, c->stream));
   }
+  // Split step without a boundary relaxation at its end: the copy engines move the fields that
+  // are final before the step ends on a second stream while the step runs (u, v after the
+  // second wind update; rhotheta_v, theta_v_pert, exner_pert, w and the gas density after the
+  // second vertical solve); the step is then launched kernel by kernel, not as a graph, so that
+  // it can record the two events.  The tracer densities follow the step.
+  const bool overlap = direct_out && c->split && !c->profiling && !(c->bc_on && !c->cfg.lperiodic);
+  if (overlap && !c->side) {
+    CK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : c->ev_mark) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  c->mark_on = overlap;
+  c->marks[0] = c->marks[1] = 0;
   int rc = lgame_gpu_pchevi(c, 0, 1, total_step_counter, lrad_update, t_0);
+  c->mark_on = false;
   if (rc != LGAME_OK) return rc;
-  if (direct_out) {
+  const bool early = overlap && c->marks[0] == 2 && c->marks[1] == 2;
+  if (direct_out && early) {
+    const long long nS = (long long)D.ny * D.nx * D.nl;
+    const int gi = D.g - 1;
+    CK(cudaStreamWaitEvent(c->side, c->ev_mark[0], 0));
+    for (int f : {LGAME_STATE_WIND_U, LGAME_STATE_WIND_V})
+      if ((rc = copy_d2h(c, state_new[f], db[f], ex[f], c->side)) != LGAME_OK) return rc;
+    CK(cudaStreamWaitEvent(c->side, c->ev_mark[1], 0));
+    for (int f : {LGAME_STATE_RHOTHETA_V, LGAME_STATE_THETA_V_PERT, LGAME_STATE_EXNER_PERT, LGAME_STATE_WIND_W})
+      if ((rc = copy_d2h(c, state_new[f], db[f], ex[f], c->side)) != LGAME_OK) return rc;
+    if ((rc = copy_d2h(c, state_new[LGAME_STATE_RHO] + gi * nS, B.rho + (size_t)gi * D.fstride, ex[0], c->side)) != LGAME_OK)
+      return rc;
+    const dim3 g1((unsigned)((ex[0].n1 + 255) / 256), (unsigned)ex[0].n2, (unsigned)ex[0].n3);
+    for (int jc = 0; jc < D.ncons; ++jc) {
+      if (jc == gi) continue;
+      k_state_out<<<g1, 256, 0, c->stream>>>(D, B.rho + (size_t)jc * D.fstride, (int)ex[0].n1, (int)ex[0].n2,
+                                             (int)ex[0].n3, vout[LGAME_STATE_RHO] + jc * nS);
+      CK(cudaGetLastError());
+    }
+    CK(cudaStreamSynchronize(c->side));
+  } else if (direct_out) {
     for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
       k_state_out<<<grid_of(f), 256, 0, c->stream>>>(D, db[f], (int)ex[f].n1, (int)ex[f].n2, (int)ex[f].n3, vout[f]);
       CK(cudaGetLastError());
@@ -1245,6 +1298,8 @@ extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
   for (void* p : c->allocations) cudaFree(p);
   if (c->bc_rim) cudaFree(c->bc_rim);
+  for (cudaEvent_t e : c->ev_mark) if (e) cudaEventDestroy(e);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
