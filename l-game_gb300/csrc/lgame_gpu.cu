@@ -1293,6 +1293,7 @@ extern "C" long long lgame_gpu_device_bytes(const lgame_gpu* c) { return c ? c->
 extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
   if (!c) return;
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->side) cudaStreamSynchronize(c->side);  // copies of an lgame_gpu_pchevi_host that failed
   for (cudaGraphExec_t g : c->graph) if (g) cudaGraphExecDestroy(g);
   if (c->split) split_destroy(c->split);
   for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
