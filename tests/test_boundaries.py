@@ -169,6 +169,24 @@ def test_oracle_step_relaxes_the_rim():
     assert not np.array_equal(runs[0]["rhotheta_v"][ring], runs[1]["rhotheta_v"][ring])
 
 
+def test_golden_boundaries_and_output():
+    """The oracle reproduces the committed vectors of tests/golden/hills_nonperiodic_bc.npz
+    (five relaxed steps and the output fields, from tests/golden/make_golden.py)."""
+    import importlib.util
+    from pathlib import Path
+    here = Path(__file__).resolve().parent / "golden"
+    spec = importlib.util.spec_from_file_location("make_golden", here / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(here / "hills_nonperiodic_bc.npz")
+    st, out, bc = mg.boundary_output_case()
+    np.testing.assert_array_equal(bc, g["bc_state"])
+    for f in L.STATE_FIELDS:
+        assert cases.rel_err(st[f], g[f]) <= 1e-12, f
+    for f, v in out.items():
+        np.testing.assert_allclose(v, g["out_" + f], rtol=1e-6, atol=0, err_msg=f)
+
+
 # ---- GPU ------------------------------------------------------------------------------
 def _gpu_pair(key, precision=L.PRECISION_FP64, with_oracle=True):
     n = _namelist(key)
