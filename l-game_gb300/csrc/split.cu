@@ -594,17 +594,15 @@ __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, Gri
 
 // the potential vorticity and its flux (calc_pot_vort, mo_vorticities.F90:189-421; vorticity
 // flux, mo_vorticity_flux.F90:16-171) of the split step: the FP32 bodies of k_eta_xy, k_eta_z
-// and k_vort_flux with register caps that keep six to seven blocks of 256 threads resident
-__global__ void __launch_bounds__(256, 6) ks_eta_xy(Dims D, Grid<float> G, StateF S, float* ex, float* ey) {
+// and k_vort_flux with register caps that keep six blocks of 256 threads resident
+// eta_x, eta_y and eta_z in one launch: the three components read the same u, v and gas
+// density around a point, which then come through the cache once
+__global__ void __launch_bounds__(256, 6) ks_eta(Dims D, Grid<float> G, StateF S, float* ex, float* ey, float* ez) {
   LG_IDX3;
   if (jl > D.NL) return;
   if (ji <= D.ny + 1 && jk <= D.nx) ex[IX(D, ji, jk, jl)] = eta_x_at<float>(D, G, S, ji, jk, jl);
   if (ji <= D.ny && jk <= D.nx + 1) ey[IX(D, ji, jk, jl)] = eta_y_at<float>(D, G, S, ji, jk, jl);
-}
-__global__ void __launch_bounds__(256, 7) ks_eta_z(Dims D, Grid<float> G, StateF S, float* ez) {
-  LG_IDX3;
-  if (ji > D.ny + 1 || jk > D.nx + 1) return;
-  ez[IX(D, ji, jk, jl)] = eta_z_at<float>(D, G, S, ji, jk, jl);
+  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx + 1) ez[IX(D, ji, jk, jl)] = eta_z_at<float>(D, G, S, ji, jk, jl);
 }
 __global__ void __launch_bounds__(256, 6) ks_vort_flux(Dims D, Grid<float> G, StateF S, const float* ex,
                                                        const float* ey, const float* ez, const float* uph,
@@ -1345,8 +1343,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
          s->tvv, s->tpu, s->tpv, pg, C, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
-      SL("ks_eta_xy", ks_eta_xy, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey);
-      SL("ks_eta_z", ks_eta_z, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ez);
+      SL("ks_eta", ks_eta, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey, s->ez);
       SL("ks_mass_flux", (k_mass_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->uph, s->vph,
          s->wph);
       SL("ks_vort_flux", ks_vort_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
