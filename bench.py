@@ -138,7 +138,7 @@ MEASURED_DRAM_BYTES_PER_CELL = {
     "ks_column_tracers": 321.0, "ks_column_ver": 238.5, "ks_tracers": 102.2, "ks_pgrad": 221.9,
     "ks_tend_wind": 112.8, "ks_gas_div": 89.2, "ks_vort_flux": 60.7, "ks_div_h": 45.3,
     "ks_ke": 80.1, "ks_theta_edges": 48.0, "ks_gas_flux": 35.8, "ks_gzp": 41.5,
-    "ks_mass_flux": 27.5, "ks_temperature": 27.8, "ks_csh_sum": 23.8,
+    "ks_temperature": 27.8, "ks_csh_sum": 23.8,
 }
 
 

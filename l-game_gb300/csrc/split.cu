@@ -595,14 +595,30 @@ __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, Gri
 // the potential vorticity and its flux (calc_pot_vort, mo_vorticities.F90:189-421; vorticity
 // flux, mo_vorticity_flux.F90:16-171) of the split step: the FP32 bodies of k_eta_xy, k_eta_z
 // and k_vort_flux with register caps that keep six blocks of 256 threads resident
-// eta_x, eta_y and eta_z in one launch: the three components read the same u, v and gas
-// density around a point, which then come through the cache once
-__global__ void __launch_bounds__(256, 6) ks_eta(Dims D, Grid<float> G, StateF S, float* ex, float* ey, float* ez) {
+// eta_x, eta_y, eta_z and the mass flux densities (mo_vector_tend_expl.F90:64-66) in one
+// launch: they read the same u, v, w and gas density around a point, which then come through
+// the cache once
+__global__ void __launch_bounds__(256, 6) ks_eta(Dims D, Grid<float> G, StateF S, float* ex, float* ey, float* ez,
+                                                 float* uph, float* vph, float* wph) {
   LG_IDX3;
   if (jl > D.NL) return;
   if (ji <= D.ny + 1 && jk <= D.nx) ex[IX(D, ji, jk, jl)] = eta_x_at<float>(D, G, S, ji, jk, jl);
   if (ji <= D.ny && jk <= D.nx + 1) ey[IX(D, ji, jk, jl)] = eta_y_at<float>(D, G, S, ji, jk, jl);
-  if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx + 1) ez[IX(D, ji, jk, jl)] = eta_z_at<float>(D, G, S, ji, jk, jl);
+  if (jl > D.nl) return;
+  if (ji <= D.ny + 1 && jk <= D.nx + 1) ez[IX(D, ji, jk, jl)] = eta_z_at<float>(D, G, S, ji, jk, jl);
+  const float* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    float f;
+    if (stv_h_x<float>(D, rg, S.u, ji, jk, jl, &f)) uph[IX(D, ji, jk, jl)] = f;
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    float f;
+    if (stv_h_y<float>(D, rg, S.v, ji, jk, jl, &f)) vph[IX(D, ji, jk, jl)] = f;
+  }
+  if (jl >= 2 && ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    wph[q] = 0.5f * (rg[IX(D, ji, jk, jl - 1)] + rg[q]) * S.w[q];
+  }
 }
 __global__ void __launch_bounds__(256, 6) ks_vort_flux(Dims D, Grid<float> G, StateF S, const float* ex,
                                                        const float* ey, const float* ez, const float* uph,
@@ -1343,9 +1359,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
          s->tvv, s->tpu, s->tpv, pg, C, C.pgcw, step == 0 ? 1 : 0);
     }
     if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
-      SL("ks_eta", ks_eta, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey, s->ez);
-      SL("ks_mass_flux", (k_mass_flux<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->uph, s->vph,
-         s->wph);
+      SL("ks_eta", ks_eta, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey, s->ez, s->uph, s->vph, s->wph);
       SL("ks_vort_flux", ks_vort_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
          s->ez, s->uph, s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
       if (!D.llinear) {
