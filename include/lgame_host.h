@@ -105,6 +105,48 @@ double* lgame_host_diag_field(lgame_host_model* m, int field, size_t* n);
 /* 2-D surface fields: 0 oro, 1 sfc_albedo, 2 lat_geo_scalar, 3 lon_geo_scalar */
 double* lgame_host_surface_field(lgame_host_model* m, int field, size_t* n);
 
+/* ---- raw binary files where the reference uses netCDF (absent here) ------------------------
+ * A 64-byte little-endian header (magic "LGAMESNP" or "LGAMEBCL", int32 version 1, int32 ny,
+ * nx, n_layers, n_constituents, then the int64 step counter or the FP64 valid time) followed by
+ * FP64 arrays in the reference layout (column-major, reference extents).  Readers check the
+ * magic, the version, the dimensions and the length, and fail with LGAME_ERR_BAD_DIMS or
+ * LGAME_ERR_INVALID_ARG. */
+
+/* Restart snapshot: the 7 fields of state slot 0 and of slot 1 (enum lgame_state_field order,
+ * as lgame_gpu_get_state returns them), the LGAME_DIAG_NFIELDS carried diagnostics (as
+ * lgame_gpu_get_diag returns them) and the step counter: a run resumed from it with
+ * lgame_gpu_set_state, lgame_gpu_set_diag and the next step number continues bit for bit.
+ * Replaces restart() (mo_set_initial_state.F90:259-320), which reads one state's rho,
+ * rhotheta_v and winds from netCDF and is unreachable in the reference (no lrestart in the
+ * namelist). */
+int  lgame_host_write_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, long long step,
+                               const double* const* slot0, const double* const* slot1, const double* const* diag);
+int  lgame_host_read_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, long long* step,
+                              double* const* slot0, double* const* slot1, double* const* diag);
+
+/* Lateral boundary level: the t_bc arrays of one time index (rho, rhotheta_v, wind_u, wind_v,
+ * wind_w, extents as lgame_gpu_set_bc takes them) and their valid time (s); what
+ * read_boundaries (mo_boundaries.F90:99-123) reads from netCDF. */
+int  lgame_host_write_bc_level(const char* path, int ny, int nx, int n_layers, int n_constituents, double t_valid,
+                               const double* rho, const double* rhotheta_v, const double* wind_u,
+                               const double* wind_v, const double* wind_w);
+int  lgame_host_read_bc_level(const char* path, int ny, int nx, int n_layers, int n_constituents, double* t_valid,
+                              double* rho, double* rhotheta_v, double* wind_u, double* wind_v, double* wind_w);
+/* read_boundaries' file name (mo_boundaries.F90:112-113) with a .bin suffix:
+ * "<root>+<int(t_update - t_init)>s.bin" (seconds truncated toward zero) into out[n]. */
+int  lgame_host_bc_filename(const char* root, double t_update, double t_init, char* out, int n);
+
+/* A ready-made lgame_bc_loader for lgame_gpu_bc_setup: user points to an lgame_bc_files; a new
+ * level comes from the file lgame_host_bc_filename(root, t_update, t_init) and goes to the
+ * context with lgame_gpu_set_bc. */
+typedef struct lgame_bc_files {
+  lgame_gpu*  ctx;
+  const char* root;
+  double      t_init;
+  int         ny, nx, n_layers, n_constituents;
+} lgame_bc_files;
+int  lgame_bc_file_loader(void* user, double t_update, int time_index);
+
 #ifdef __cplusplus
 }
 #endif

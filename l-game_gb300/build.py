@@ -40,6 +40,7 @@ CXX_UNITS = [
     ("host/namelist.cpp", []),
     ("host/setup.cpp", []),
     ("host/teacher.cpp", []),
+    ("host/files.cpp", []),
 ]
 
 

@@ -50,6 +50,65 @@ def output_arrays(ny, nx, nl, ncons, fields=OUTPUT_FIELDS):
     return out, ptrs
 
 
+# ---- raw binary files (include/lgame_host.h) -------------------------------------------------
+class BcFiles(C.Structure):
+    """lgame_bc_files (include/lgame_host.h)."""
+    _fields_ = [("ctx", C.c_void_p), ("root", C.c_char_p), ("t_init", C.c_double), ("ny", C.c_int),
+                ("nx", C.c_int), ("n_layers", C.c_int), ("n_constituents", C.c_int)]
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def write_snapshot(path, ny, nx, nl, ncons, step, slot0: dict, slot1: dict, diag: dict):
+    """Restart snapshot of both state slots, the carried diagnostics and the step counter."""
+    lib = load_library()
+    arr = lambda d, names: [np.asfortranarray(d[f], dtype=np.float64) for f in names]
+    a0, a1, ad = arr(slot0, STATE_FIELDS), arr(slot1, STATE_FIELDS), arr(diag, DIAG_FIELDS)
+    check(lib.lgame_host_write_snapshot(str(path).encode(), ny, nx, nl, ncons, step, ptr_array(a0), ptr_array(a1),
+                                        ptr_array(ad)), "lgame_host_write_snapshot")
+
+
+def read_snapshot(path, ny, nx, nl, ncons):
+    """(step, slot 0 state, slot 1 state, diagnostics) of a snapshot written for these dimensions."""
+    lib = load_library()
+    sh = field_shapes(ny, nx, nl, ncons)
+    s0 = {f: np.zeros(sh[f], order="F") for f in STATE_FIELDS}
+    s1 = {f: np.zeros(sh[f], order="F") for f in STATE_FIELDS}
+    dg = {f: np.zeros(sh[f], order="F") for f in DIAG_FIELDS}
+    step = C.c_longlong()
+    check(lib.lgame_host_read_snapshot(str(path).encode(), ny, nx, nl, ncons, C.byref(step),
+                                       ptr_array([s0[f] for f in STATE_FIELDS]), ptr_array([s1[f] for f in STATE_FIELDS]),
+                                       ptr_array([dg[f] for f in DIAG_FIELDS])), "lgame_host_read_snapshot")
+    return step.value, s0, s1, dg
+
+
+def write_bc_level(path, ny, nx, nl, ncons, t_valid, level: dict):
+    lib = load_library()
+    a = [np.asfortranarray(level[f], dtype=np.float64) for f in BC_FIELDS]
+    check(lib.lgame_host_write_bc_level(str(path).encode(), ny, nx, nl, ncons, t_valid, *[_dp(x) for x in a]),
+          "lgame_host_write_bc_level")
+
+
+def read_bc_level(path, ny, nx, nl, ncons):
+    """(valid time, level) of a boundary level file."""
+    lib = load_library()
+    sh = field_shapes(ny, nx, nl, ncons)
+    lev = {f: np.zeros(sh[f], order="F") for f in BC_FIELDS}
+    t = C.c_double()
+    check(lib.lgame_host_read_bc_level(str(path).encode(), ny, nx, nl, ncons, C.byref(t),
+                                       *[_dp(lev[f]) for f in BC_FIELDS]), "lgame_host_read_bc_level")
+    return t.value, lev
+
+
+def bc_filename(root, t_update, t_init) -> str:
+    lib = load_library()
+    buf = C.create_string_buffer(4096)
+    check(lib.lgame_host_bc_filename(str(root).encode(), t_update, t_init, buf, len(buf)), "lgame_host_bc_filename")
+    return buf.value.decode()
+
+
 def bc_callback(model, loader):
     """A C loader for model.bc_setup: loader(t_update, time_index) returns the level (a dict
     of BC_FIELDS arrays), which goes to model.set_bc(time_index, ...); None gives a null loader."""
@@ -164,6 +223,12 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_set_graphs": (i, [vp, i]),
         "lgame_gpu_output": (i, [vp, i, i, d, d, C.POINTER(C.POINTER(C.c_float)), i, C.POINTER(i)]),
         "lgame_gpu_bc_setup": (i, [vp, i, i, d, BC_LOADER, vp]),
+        "lgame_host_write_snapshot": (i, [C.c_char_p, i, i, i, i, ll, pp, pp, pp]),
+        "lgame_host_read_snapshot": (i, [C.c_char_p, i, i, i, i, C.POINTER(ll), pp, pp, pp]),
+        "lgame_host_write_bc_level": (i, [C.c_char_p, i, i, i, i, d] + [C.POINTER(C.c_double)] * 5),
+        "lgame_host_read_bc_level": (i, [C.c_char_p, i, i, i, i, C.POINTER(d)] + [C.POINTER(C.c_double)] * 5),
+        "lgame_host_bc_filename": (i, [C.c_char_p, d, d, C.c_char_p, i]),
+        "lgame_bc_file_loader": (i, [vp, d, i]),
         "lgame_gpu_set_bc": (i, [vp, i] + [C.POINTER(C.c_double)] * 5),
         "lgame_gpu_update_boundaries": (i, [vp, i, d]),
         "lgame_gpu_bc_state": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(d)]),
@@ -403,6 +468,15 @@ class GpuModel:
         self._bc_cb = bc_callback(self, loader)
         check(self.lib.lgame_gpu_bc_setup(self.h, n_swamp, dtime_bc, t_latest_bc, self._bc_cb, None),
               "lgame_gpu_bc_setup")
+
+    def bc_setup_files(self, n_swamp: int, dtime_bc: int, root, t_init: float = 0.0, t_latest_bc: float = 0.0):
+        """Relaxation with later levels read by the library's own loader (lgame_bc_file_loader)
+        from the files bc_filename(root, t_update, t_init)."""
+        self._bc_root = str(root).encode()
+        self._bc_files = BcFiles(self.h, self._bc_root, t_init, self.ny, self.nx, self.nl, self.ncons)
+        self._bc_cb = C.cast(self.lib.lgame_bc_file_loader, BC_LOADER)
+        check(self.lib.lgame_gpu_bc_setup(self.h, n_swamp, dtime_bc, t_latest_bc, self._bc_cb,
+                                          C.cast(C.pointer(self._bc_files), C.c_void_p)), "lgame_gpu_bc_setup")
 
     def set_bc(self, time_index: int, bc: dict):
         arrs = [np.asfortranarray(bc[f], dtype=np.float64) for f in BC_FIELDS]
