@@ -47,3 +47,32 @@ def test_pinned_host_step_equals_pageable_host_step(precision):
             pag_old[f][...] = pag_new[f]
     for g in models:
         g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [L.PRECISION_FP64, L.PRECISION_SPLIT])
+def test_nonfinite_state_is_reported(precision):
+    """Failure detection without a fault: a NaN planted in the host state before upload makes
+    the step of a context with check_finite return LGAME_ERR_NONFINITE, and the context keeps
+    answering (the NaN reaches the carried diagnostics too, so a host that goes on restores
+    the state and the diagnostics, as from a restart snapshot)."""
+    n = cases.small_case("hills")
+    hm = L.HostModel(n)
+    cfg = L.config_from_namelist(n)
+    cfg.precision = precision
+    cfg.check_finite = 1
+    g = L.GpuModel(cfg, hm.grid)
+    g.set_diag(hm.diag)
+    bad = hm.copy_state()
+    bad["rhotheta_v"][2, 3, 4] = np.nan
+    g.set_state(0, bad)
+    g.set_state(1, bad)
+    with pytest.raises(L.LgameError) as e:
+        g.pchevi(0, 1, 0)
+    assert e.value.code == L.ERR_NONFINITE
+    assert not np.isfinite(g.get_state(1)["rhotheta_v"]).all()
+    g.set_state(0, hm.state)
+    back = g.get_state(0)
+    for f in L.STATE_FIELDS:
+        np.testing.assert_array_equal(back[f], hm.state[f], err_msg=f)
+    g.close()
