@@ -80,3 +80,24 @@ def test_null_arguments_are_errors():
     assert lib.lgame_gpu_update_boundaries(None, 0, 0.0) == L.ERR_INVALID_ARG
     assert lib.lgame_gpu_bc_state(None, None, None, None) == L.ERR_INVALID_ARG
     lib.lgame_gpu_destroy(None)
+
+
+def test_c_driver(tmp_path):
+    """The headers compile as C99 (-Wall -Werror) and a C program linked against the library
+    uses the ABI: namelist, host set-up, snapshot round trip, file names, context creation."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    here = Path(__file__).resolve().parent
+    lib = Path(L.LIB_PATH)
+    exe = tmp_path / "c_driver"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", str(INCLUDE), str(here / "c_driver.c"),
+                    str(lib), f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    nml = tmp_path / "namelist.nml"
+    nml.write_text(cases.namelist_text(*cases.SMALL["hills_nonperiodic"][0:1], **cases.SMALL["hills_nonperiodic"][1]))
+    out = subprocess.run([str(exe), str(nml), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip().endswith("ok")
+
