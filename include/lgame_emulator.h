@@ -100,6 +100,21 @@ int  lgame_gpu_rad_apply_heating(lgame_gpu* ctx, int slot, const float* heating)
 int  lgame_gpu_rad_update(lgame_gpu* ctx, lgame_emu* emu, int slot, double t, int sample_stride,
                           double bound_k_per_day, double* report);
 
+/* Attaches an emulator to the context (NULL detaches it), so that the step's own radiation
+ * switch drives it: lgame_gpu_pchevi(ctx, old, new, counter, lrad_update = 1, t_0) then runs
+ * lgame_gpu_rad_update(ctx, emu, old, t_0 + dtime_rad/2, sample_stride, bound_k_per_day)
+ * before the substeps, as the reference's pchevi calls update_rad_fluxes(state_old, grid,
+ * diag, t_0) (src/time_stepping/mo_manage_pchevi.F90:56-58), which evaluates the zenith angle
+ * at t_0 + 0.5*dtime_rad (src/radiation/mo_manage_radiation_calls.F90:46-51).  The radiation
+ * update synchronises (the sampled check runs on the CPU), so a step with lrad_update = 1
+ * returns after its radiation update has finished.  Without an attached emulator
+ * lrad_update is ignored and the radiation tendency stays what the host last set. */
+int  lgame_gpu_rad_attach(lgame_gpu* ctx, lgame_emu* emu, double dtime_rad, int sample_stride,
+                          double bound_k_per_day);
+/* The report of the last radiation update lgame_gpu_pchevi ran (the layout of
+ * lgame_gpu_rad_update's report) and the number of such updates since the attach. */
+int  lgame_gpu_rad_last_report(const lgame_gpu* ctx, double* report, int* updates);
+
 #ifdef __cplusplus
 }
 #endif

@@ -219,10 +219,13 @@ int  lgame_gpu_get_diag(lgame_gpu* ctx, double* const* fields, int nfields);
  *   call pchevi(state_old,state_new,tend,bc,grid,diag,total_step_counter,lrad_update,t_0)
  * In a non-periodic run with boundary data set up (lgame_gpu_bc_setup), the step ends
  * with lgame_gpu_update_boundaries(ctx, new_slot, (total_step_counter+1)*dtime), as the
- * reference's does (mo_manage_pchevi.F90:114-116).  lrad_update and t_0 are accepted for
- * interface parity; the radiation tendency is whatever the host last set (or the
- * emulator wrote).  Stream-ordered: returns after enqueueing unless check_finite is on
- * or a boundary level has to be loaded. */
+ * reference's does (mo_manage_pchevi.F90:114-116).  With a radiation emulator attached
+ * (lgame_gpu_rad_attach, lgame_emulator.h), lrad_update = 1 runs the emulator's radiation
+ * update on state_old before the substeps, at t_0 + dtime_rad/2, as the reference's
+ * update_rad_fluxes (mo_manage_pchevi.F90:56-58); without one, lrad_update is ignored and
+ * the radiation tendency is whatever the host last set.  Stream-ordered: returns after
+ * enqueueing unless check_finite is on, a boundary level has to be loaded or a radiation
+ * update ran. */
 int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
                       int total_step_counter, int lrad_update, double t_0);
 
@@ -258,8 +261,12 @@ int  lgame_gpu_budgets(lgame_gpu* ctx, int slot, double* out, int nout);
  * 1024*11 + 11 doubles (90,200 bytes) per device, which is why at most LGAME_BUDGETS_MAX
  * (11) quantities, i.e. n_constituents <= 7, are accepted (more: LGAME_ERR_INVALID_ARG).
  *
- * - The first call on each device looks up the scratch address (cudaGetSymbolAddress)
- *   with that device current; make that first call before any stream capture begins.
+ * - lgame_gpu_create loads the module that holds the scratch array and the two reduction
+ *   kernels on its device (under CUDA's lazy loading that load takes device memory), so
+ *   the calls of this function inside a time loop allocate nothing.  Every call looks the
+ *   scratch address up again (cudaGetSymbolAddress, with the context's device current):
+ *   after a cudaDeviceReset the next context loads the module anew and the address may
+ *   change, so nothing is cached across calls.
  * - There is one scratch array per device, shared by all contexts on that device: calls
  *   that overlap in time on one device (several host threads, or several contexts of the
  *   same device used concurrently) race on it and return wrong sums.  Calls from a single

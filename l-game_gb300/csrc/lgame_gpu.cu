@@ -82,6 +82,14 @@ struct lgame_gpu {
   int bc_nrim = 0;
   // output fields (compact FP32, rho then T, RH, u, v, w), allocated at the first output
   float* out_buf = nullptr;
+  // radiation emulator attached with lgame_gpu_rad_attach: run by lgame_gpu_pchevi when its
+  // lrad_update is set (update_rad_fluxes, mo_manage_pchevi.F90:56-58), with the zenith angle
+  // at t_0 + dtime_rad/2 (mo_manage_radiation_calls.F90:46-51); the report of the last update
+  lgame_emu* rad_emu = nullptr;
+  double rad_dtime = 0.0, rad_bound = 0.0;
+  int rad_stride = 0;
+  double rad_report[4] = {0.0, 0.0, 0.0, 0.0};
+  int rad_updates = 0;
   // lgame_gpu_pchevi_host: a second stream that copies the fields of the new state out while
   // the step still runs, and the two events the step records when they are final
   cudaStream_t side = nullptr;
@@ -398,6 +406,29 @@ __global__ void k_budget_final(const double* part, double* out, int nq) {
   }
 }
 
+// Scratch of lgame_gpu_budgets_static: kRedBlocks partial sums for each of at most
+// LGAME_BUDGETS_MAX budget quantities, plus the LGAME_BUDGETS_MAX results, (1024 * 11 + 11)
+// doubles = 90,200 bytes per device, part of the loaded module (no cudaMalloc).  Nothing in it
+// has to start at zero: k_budget_partial writes every partial sum before k_budget_final reads
+// it, and k_budget_final writes every result before it is copied out.
+constexpr int kStaticBudgetDoubles = kRedBlocks * LGAME_BUDGETS_MAX + LGAME_BUDGETS_MAX;
+static __device__ __align__(256) double g_budget_scratch[kStaticBudgetDoubles];
+
+// Loads, on the current device, the module that holds g_budget_scratch and the two reduction
+// kernels (under CUDA's lazy loading a module or a kernel is loaded, and its memory taken, at
+// its first use).  lgame_gpu_create calls this, so that lgame_gpu_budgets_static itself never
+// triggers a load inside a host's time loop.
+int preload_budget_scratch() {
+  void* p = nullptr;
+  cudaFuncAttributes fa;
+  if (cudaGetSymbolAddress(&p, g_budget_scratch) != cudaSuccess || !p ||
+      cudaFuncGetAttributes(&fa, k_budget_partial) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, k_budget_final) != cudaSuccess)
+    return set_err(LGAME_ERR_CUDA, std::string("loading the budget reduction module: ") +
+                                       cudaGetErrorString(cudaGetLastError()));
+  return LGAME_OK;
+}
+
 // FP64 instantiations of the kernel templates of kernels.cuh (this file is compiled with
 // -fmad=false like the rest of the FP64 step)
 namespace kd {
@@ -629,6 +660,7 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   auto fail = [&](int code) { lgame_gpu_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(LGAME_ERR_CUDA, "cudaStreamCreate failed"));
+  if ((rc = preload_budget_scratch()) != LGAME_OK) return fail(rc);
   const size_t F = (size_t)D.fstride;
   // grid
   for (int f = 0; f < LGAME_GRID_NFIELDS; ++f) {
@@ -868,12 +900,19 @@ extern "C" int lgame_gpu_get_diag(lgame_gpu* c, double* const* f, int nfields) {
 
 extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int total_step_counter, int lrad_update,
                                 double t_0) {
-  (void)lrad_update; (void)t_0;
   if (!c || old_slot < 0 || old_slot > 1 || new_slot < 0 || new_slot > 1 || old_slot == new_slot || total_step_counter < 0)
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi: bad arguments");
   if (!c->grid_set) return set_err(LGAME_ERR_STATE, "lgame_gpu_pchevi: lgame_gpu_set_grid has not been called");
   c->kernels_last_step = 0;
   int rc;
+  // update_rad_fluxes(state_old, grid, diag, t_0) before the substeps (mo_manage_pchevi.F90:56-58)
+  // when an emulator is attached; otherwise the radiation tendency is whatever the host set
+  if (lrad_update && c->rad_emu) {
+    if ((rc = lgame_gpu_rad_update(c, c->rad_emu, old_slot, t_0 + 0.5 * c->rad_dtime, c->rad_stride, c->rad_bound,
+                                   c->rad_report)) != LGAME_OK)
+      return rc;
+    ++c->rad_updates;
+  }
   if (c->split) {
     for (int slot : {old_slot, new_slot}) {
       if (c->mirror_valid[slot]) continue;
@@ -1307,39 +1346,28 @@ extern "C" void lgame_gpu_destroy(lgame_gpu* c) {
 
 // ---- lgame_gpu_budgets_static: the budget sums without any allocation -------------------
 // The same two reduction kernels as lgame_gpu_budgets (so the same sums, bit for bit), with
-// their scratch in a file-scope device array instead of the context's reduce_buf.  The
-// array is part of the loaded module: one instance per device, no cudaMalloc, and the call
-// allocates no host memory either (the result is copied straight into the caller's array).
-//
-// Size: kRedBlocks partial sums for each of at most LGAME_BUDGETS_MAX budget quantities,
-// plus the LGAME_BUDGETS_MAX results: (1024 * 11 + 11) doubles = 90,200 bytes per device.
-// Nothing in it has to start at zero: k_budget_partial writes every partial sum before
-// k_budget_final reads it, and k_budget_final writes every result before it is copied out.
-constexpr int kStaticBudgetDoubles = kRedBlocks * LGAME_BUDGETS_MAX + LGAME_BUDGETS_MAX;
-static __device__ __align__(256) double g_budget_scratch[kStaticBudgetDoubles];
-
+// their scratch in the file-scope device array g_budget_scratch (defined beside the kernels)
+// instead of the context's reduce_buf.  The array is part of the loaded module: one instance
+// per device, no cudaMalloc, and the call allocates no host memory either (the result is
+// copied straight into the caller's array).
 namespace {
 constexpr int kMaxDevices = 64;
-std::mutex g_budget_scratch_mu;
-double* g_budget_scratch_addr[kMaxDevices] = {};
 
-// Device address of g_budget_scratch on device dev (which must be current), looked up
-// with cudaGetSymbolAddress the first time dev is seen and cached afterwards.
+// Device address of g_budget_scratch on device dev (which must be current).  It is looked up
+// on every call and never cached: after a cudaDeviceReset the module is loaded again by the
+// next context and the array may then sit at another address.  lgame_gpu_create has loaded
+// the module, so the lookup allocates nothing.
 int budget_scratch_address(int dev, double** out) {
-  std::lock_guard<std::mutex> lock(g_budget_scratch_mu);
-  if (!g_budget_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_budget_scratch);
-    if (e != cudaSuccess || !p) {
-      char msg[256];
-      std::snprintf(msg, sizeof msg, "lgame_gpu_budgets_static: cudaGetSymbolAddress of the scratch array on device %d: %s",
-                    dev, cudaGetErrorString(e));
-      lgame_set_error(msg);
-      return LGAME_ERR_CUDA;
-    }
-    g_budget_scratch_addr[dev] = static_cast<double*>(p);
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_budget_scratch);
+  if (e != cudaSuccess || !p) {
+    char msg[256];
+    std::snprintf(msg, sizeof msg, "lgame_gpu_budgets_static: cudaGetSymbolAddress of the scratch array on device %d: %s",
+                  dev, cudaGetErrorString(e));
+    lgame_set_error(msg);
+    return LGAME_ERR_CUDA;
   }
-  *out = g_budget_scratch_addr[dev];
+  *out = static_cast<double*>(p);
   return LGAME_OK;
 }
 
@@ -1620,5 +1648,27 @@ extern "C" int lgame_gpu_rad_update(lgame_gpu* c, lgame_emu* emu, int slot, doub
     report[2] = (double)nsample;
     report[3] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_rad_attach(lgame_gpu* c, lgame_emu* emu, double dtime_rad, int sample_stride,
+                                    double bound_k_per_day) {
+  if (!c || sample_stride < 0 || (emu && dtime_rad < 0.0))
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_attach: bad arguments");
+  if (emu && emu::nlev_of(emu) != c->D.nl)
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_attach: the emulator's nlev differs from n_layers");
+  c->rad_emu = emu;
+  c->rad_dtime = dtime_rad;
+  c->rad_stride = sample_stride;
+  c->rad_bound = bound_k_per_day;
+  c->rad_updates = 0;
+  for (double& r : c->rad_report) r = 0.0;
+  return LGAME_OK;
+}
+
+extern "C" int lgame_gpu_rad_last_report(const lgame_gpu* c, double* report, int* updates) {
+  if (!c || !report) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_rad_last_report: bad arguments");
+  for (int k = 0; k < 4; ++k) report[k] = c->rad_report[k];
+  if (updates) *updates = c->rad_updates;
   return LGAME_OK;
 }

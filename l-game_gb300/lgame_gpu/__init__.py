@@ -267,6 +267,8 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_rad_features": (i, [vp, i, d, fp]),
         "lgame_gpu_rad_apply_heating": (i, [vp, i, fp]),
         "lgame_gpu_rad_update": (i, [vp, vp, i, d, i, d, C.POINTER(d)]),
+        "lgame_gpu_rad_attach": (i, [vp, vp, d, i, d]),
+        "lgame_gpu_rad_last_report": (i, [vp, C.POINTER(d), C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

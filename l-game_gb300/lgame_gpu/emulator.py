@@ -194,5 +194,23 @@ def rad_update(model, emu: Emulator, slot: int, t: float, sample_stride: int, bo
     return {"rms_k_per_day": rep[0], "fallback": bool(rep[1]), "sampled": int(rep[2]), "wall_s": rep[3]}
 
 
+def rad_attach(model, emu, dtime_rad: float, sample_stride: int, bound: float):
+    """Lets lgame_gpu_pchevi(..., lrad_update=1, t_0) run the emulator's radiation update
+    (emu None: detach)."""
+    lib = load_library()
+    check(lib.lgame_gpu_rad_attach(model.h, emu.h if emu is not None else None, C.c_double(dtime_rad), sample_stride,
+                                   C.c_double(bound)), "lgame_gpu_rad_attach")
+
+
+def rad_last_report(model) -> dict:
+    lib = load_library()
+    rep = np.zeros(4)
+    n = C.c_int(0)
+    check(lib.lgame_gpu_rad_last_report(model.h, rep.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n)),
+          "lgame_gpu_rad_last_report")
+    return {"rms_k_per_day": rep[0], "fallback": bool(rep[1]), "sampled": int(rep[2]), "wall_s": rep[3],
+            "updates": n.value}
+
+
 __all__ = ["Emulator", "teacher", "bf16_bits", "bf16_round", "normalization_from", "rad_set_surface",
-           "rad_features", "rad_apply_heating", "rad_update", "LgameError"]
+           "rad_features", "rad_apply_heating", "rad_update", "rad_attach", "rad_last_report", "LgameError"]

@@ -207,3 +207,45 @@ def test_coupling_features_and_update():
     g.pchevi(0, 1, 0)
     assert all(np.isfinite(v).all() for v in g.get_state(1).values())
     emu.close()
+
+
+@pytest.mark.gpu
+def test_lrad_update_drives_attached_emulator():
+    """pchevi(..., lrad_update=1, t_0) with an attached emulator equals the host calling
+    lgame_gpu_rad_update(old slot, t_0 + dtime_rad/2) itself before the step
+    (mo_manage_pchevi.F90:56-58, mo_manage_radiation_calls.F90:46-51), bit for bit; with
+    lrad_update=0, or with no emulator attached, the radiation tendency is left alone."""
+    n = cases.small_case("jet")
+    hm = L.HostModel(n)
+    nl = n.n_layers
+    emu = E.Emulator(nlev=nl, hidden=256, batch_max=256, seed=3)
+    t0, dtime_rad = 1576843200.0 + 5 * 3600.0, 900.0
+    models = []
+    for _ in range(2):
+        g = L.GpuModel(L.config_from_namelist(n), hm.grid)
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        E.rad_set_surface(g, hm.surface["sfc_albedo"], hm.surface["lat_geo_scalar"], hm.surface["lon_geo_scalar"])
+        models.append(g)
+    a, b = models
+    E.rad_attach(a, emu, dtime_rad, 4, 1e9)
+    a.pchevi(0, 1, 0, 1, t0)
+    rep = E.rad_last_report(a)
+    assert rep["updates"] == 1 and rep["sampled"] > 0 and not rep["fallback"]
+    E.rad_update(b, emu, 0, t0 + 0.5 * dtime_rad, 4, 1e9)
+    b.pchevi(0, 1, 0, 0, t0)
+    for f, v in a.get_state(1).items():
+        np.testing.assert_array_equal(v, b.get_state(1)[f], err_msg=f)
+    rad = a.get_diag()["radiation_tendency"]
+    assert np.abs(rad).max() > 0.0
+    np.testing.assert_array_equal(rad, b.get_diag()["radiation_tendency"])
+    # lrad_update = 0 runs no update; detached, lrad_update = 1 is ignored
+    a.pchevi(1, 0, 1, 0, t0 + 4.0)
+    assert E.rad_last_report(a)["updates"] == 1
+    E.rad_attach(a, None, 0.0, 0, 0.0)
+    a.pchevi(0, 1, 2, 1, t0 + 8.0)
+    np.testing.assert_array_equal(a.get_diag()["radiation_tendency"], rad)
+    a.close()
+    b.close()
+    emu.close()

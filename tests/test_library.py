@@ -101,3 +101,32 @@ def test_c_driver(tmp_path):
     assert out.returncode == 0, out.stderr
     assert out.stdout.strip().endswith("ok")
 
+
+def _build_c_driver(tmp_path):
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    here = Path(__file__).resolve().parent
+    lib = Path(L.LIB_PATH)
+    exe = tmp_path / "c_driver"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-I", str(INCLUDE), str(here / "c_driver.c"),
+                    str(lib), f"-Wl,-rpath,{lib.parent}", "-o", str(exe)], check=True)
+    return exe
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", ["jet", "hills"])
+def test_c_driver_steps(tmp_path, key):
+    """A C host steps the model: two lgame_gpu_pchevi calls against two lgame_gpu_pchevi_host
+    calls, FP64 and split, finite and bit-equal (checked inside the C program)."""
+    import subprocess
+    exe = _build_c_driver(tmp_path)
+    nml = tmp_path / "namelist.nml"
+    nml.write_text(cases.namelist_text(*cases.SMALL[key][0:1], **cases.SMALL[key][1]))
+    out = subprocess.run([str(exe), str(nml), str(tmp_path), "step"], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.count("pchevi == pchevi_host") == 2, out.stdout
+    assert out.stdout.strip().endswith("ok")
+
