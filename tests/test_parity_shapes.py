@@ -89,8 +89,13 @@ def test_fp64_parity_full_shape(key):
             assert not bad, f"{key} step {step}: {bad}"
             if relax:
                 assert g.bc_state() == o.bc_state(), step
+        # The budget terms are sums of n non-negative cell values, and the GPU's reduction
+        # tree adds them in another order than the oracle's threads: any two orders agree to
+        # 2(n-1)u relative (u = 2^-53), which at 13 M cells is above 1e-12.  A resting
+        # atmosphere's kinetic energy (round-off winds) shows it.
+        ncell = n.nx * n.ny * n.n_layers
         bg, br = g.budgets(nsteps % 2), o.budgets(nsteps % 2)
-        np.testing.assert_allclose(bg, br, rtol=1e-12, atol=0)
+        np.testing.assert_allclose(bg, br, rtol=max(TOL, 2.0 * ncell * 2.0 ** -53), atol=0)
     finally:
         g.close()
         o.close()
