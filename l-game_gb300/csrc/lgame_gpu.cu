@@ -37,6 +37,15 @@ int set_err(int code, const std::string& msg) {
 
 }  // namespace
 
+// device buffers of the radiation coupling (lgame_emulator.h): surface albedo, latitude and
+// longitude per column, the feature rows and the heating rates of every column
+struct RadBuffers {
+  double *albedo = nullptr, *lat = nullptr, *lon = nullptr;
+  float *features = nullptr, *heating = nullptr;
+  long long ncol = 0;
+  int nlev = 0;
+};
+
 struct lgame_gpu {
   lgame_config cfg;
   Dims D;
@@ -85,6 +94,7 @@ struct lgame_gpu {
   // radiation emulator attached with lgame_gpu_rad_attach: run by lgame_gpu_pchevi when its
   // lrad_update is set (update_rad_fluxes, mo_manage_pchevi.F90:56-58), with the zenith angle
   // at t_0 + dtime_rad/2 (mo_manage_radiation_calls.F90:46-51); the report of the last update
+  RadBuffers radbuf;
   lgame_emu* rad_emu = nullptr;
   double rad_dtime = 0.0, rad_bound = 0.0;
   int rad_stride = 0;
@@ -1439,20 +1449,6 @@ extern "C" int lgame_gpu_budgets_static(lgame_gpu* c, int slot, double* out, int
 // src/radiation/mo_manage_radiation_calls.F90:17-59)
 namespace {
 
-struct RadBuffers {
-  double *albedo = nullptr, *lat = nullptr, *lon = nullptr;
-  float *features = nullptr, *heating = nullptr;
-  long long ncol = 0;
-  int nlev = 0;
-};
-std::mutex g_rad_mu;
-std::vector<std::pair<const lgame_gpu*, RadBuffers>> g_rad;  // per context
-
-RadBuffers* rad_of(const lgame_gpu* c) {
-  for (auto& p : g_rad)
-    if (p.first == c) return &p.second;
-  return nullptr;
-}
 
 // coszenith, mo_rterrtmgp_coupler.F90:550-629 (the sun's direction from the Earth's rotation
 // and revolution relative to the winter solstice 2019-12-20 12:00 UTC), 0 at night
@@ -1512,13 +1508,10 @@ __global__ void k_rad_apply(Dims D, State S, const float* heat, double* rad, flo
   if (rad_f) rad_f[i] = (float)q;
 }
 
+// the context's radiation buffers, allocated at the first radiation call (they live and die
+// with the context: its allocation list frees them)
 int rad_buffers(lgame_gpu* c, RadBuffers** out) {
-  std::lock_guard<std::mutex> lk(g_rad_mu);
-  RadBuffers* r = rad_of(c);
-  if (!r) {
-    g_rad.push_back({c, RadBuffers{}});
-    r = &g_rad.back().second;
-  }
+  RadBuffers* r = &c->radbuf;
   const Dims& D = c->D;
   if (!r->features) {
     r->ncol = (long long)D.ny * D.nx;

@@ -881,156 +881,294 @@ __device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>
 }
 
 // ---- three_band_solver_gen_densities, mo_column_solvers.F90:353-604 ----------------------
-// One thread per (column, tracer), one top-to-bottom elimination and one bottom-to-top
-// substitution.  The reference's system  d_l s_l + e_l s_{l+1} + c_{l-1} s_{l-1} = rho_l + inc_l
-// (implicit-upwind vertical flux and sedimentation, inc = dt*tendency + explicit flux part)
-// is solved for the increment delta = s - rho_old:
+// The reference's system per (column, tracer)  d_l s_l + e_l s_{l+1} + c_{l-1} s_{l-1} = rho_l + inc_l
+// (implicit-upwind vertical flux and sedimentation, inc = dt*tendency + explicit flux part) is
+// solved for the increment delta = s - rho_old:
 //   d_l delta_l + e_l delta_{l+1} + c_{l-1} delta_{l-1} = inc_l - (d_l - 1) rho_l - e_l rho_{l+1} - c_{l-1} rho_{l-1}
-// The coefficients are FP32 (fall speeds and fluxes from the mirror), and so are the right-hand
-// side and both substitutions, whose rounding errors are then relative to the flux terms (the
-// size of delta) and not to the density; the new density rho_old + delta is formed in FP64,
-// the one FP64 operation per cell.  d - 1 is accumulated on its own, so the diagonal's
-// rounding near 1 does not enter.  Each interface couples its two cells in one direction only
-// (the upwind side), so the pivots are the diagonal entries themselves.  The tracer is the
-// fastest block index, so the blocks of one column tile run together and share the column's
-// w, temperature and volume reads through L2.  A condensate's sediment heating goes to its own
-// plane of csh_part (rk_step 1 only); ks_csh_sum adds the planes in condensate order.  The
-// level loop waits on memory, so the register cap buys residency: twelve blocks per SM
-// (40 registers) ran 6 % faster than nine.
-__global__ void __launch_bounds__(128, 12) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So, State Sn,
-                                                         StateF Mo, StateF Mn, const float* t_rho_all,
-                                                         const float* Tm, float* csh_part, int rk_step) {
-  const int ji = blockIdx.y * blockDim.x + threadIdx.x + 1;
-  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
-  const int jc = (int)blockIdx.x + 1 + ((int)blockIdx.x + 1 >= D.g ? 1 : 0);
-  if (ji > D.ny || jk > D.nx || jc > D.ncons) return;
-  const int nl = D.nl, NL = D.NL, nc = D.nc;
+// in FP32 (coefficients from the mirror; the right-hand side's rounding is then relative to the
+// flux terms, the size of delta, and not to the density), and the new density rho_old + delta
+// is formed in FP64.  d - 1 is accumulated on its own, so the diagonal's rounding near 1 does
+// not enter.  Each interface couples its two cells in one direction only (the upwind side:
+// e_l = 0 or c_l = 0), so Thomas's pivots are the diagonal entries themselves and its sweeps
+// are the affine recurrences
+//   forward   r_l     = alpha_l r_{l-1} + beta_l,     alpha_l = -c_{l-1}/d_l, beta_l = rhs_l/d_l
+//   backward  delta_l = r_l - e'_l delta_{l+1},        e'_l = e_l/d_l.
+//
+// A block owns 32 columns (a row tile, one per lane) and three tracers, in three phases:
+//   1. the eight warps take contiguous chunks of levels (ten at 80 layers); a thread walks its
+//      chunk top down and forms alpha, beta, e' of the three tracers into shared memory, and the
+//      sediment heating.  What the three tracers share -- volume, area, old and new w,
+//      temperature and heat capacities at each interface, the cloud droplets' fall speed -- is
+//      loaded and formed once, the values of the interface below a level are carried to the next
+//      level as the interface above it, and inputs are loaded two levels ahead;
+//   2. three warps run the two sweeps of one tracer each, a lane per column, from shared memory
+//      (no memory latency in the level chain), while the old FP64 densities of phase 3 arrive;
+//   3. the chunks again: rho_old + delta in FP64, clipped (mo_column_solvers.F90:587-591), and
+//      its rounded mirror.
+// The elimination data never leave the chip: as a per-thread local stack (one thread per column
+// and tracer walking all levels) they spilled through L2 to DRAM, 321 bytes per cell moved
+// against 202.  The two blocks of a row tile are consecutive in the grid and read the tile's
+// shared inputs once from DRAM.  A condensate's sediment heating goes to its own plane of
+// csh_part (rk_step 1 only, FP32 heat capacities); ks_csh_sum adds the planes in order.
+constexpr int kTrWarps = 8;   // level chunks in phases 1 and 3
+constexpr int kTrSet = 3;     // tracers per block
+constexpr int kTrPitch = 33;  // shared-memory row pitch (32 columns + 1)
+constexpr int kTrPre = 10;    // levels per thread whose old densities are loaded before the sweeps
+constexpr int kTrRow = 3 * kTrSet * kTrPitch;  // shared-memory floats per level
+
+// inputs of one level m of a column for the three tracers of a block: the tracers' old mirror
+// densities and tendencies, and at the interface above the level (w level m) area, old and
+// new w; the level's 1/volume and temperature; for the cloud droplets' fall speed (second set
+// only) the gas density, gravity at w levels m and m+1 and the two vertical weights
+struct TrLevel { float ro[kTrSet], tr[kTrSet], az, wo, wn, iv, tm, rg, gm, gm1, w5, w6; };
+
+// v_fall_liquid, mo_derived.F90:218-263, in FP32, at level m from its prefetched inputs
+__device__ __forceinline__ float vfall_liquid_l(const TrLevel& L, float radius, int m, int nl) {
+  const float g = (m == 1) ? L.gm1 : (m == nl) ? L.gm : L.w5 * L.gm + L.w6 * L.gm1;
+  const float rg = L.rg;
+  const float pm = float(kM_D / kN_A);
+  const float tv = sqrtf(8.f * float(kK_B) / (float(kPI) * pm) * L.tm);
+  const float mfp = 1.f / (1.41421356f * (rg / pm) * (4.f * float(kPI) * (130e-12f * 130e-12f)));
+  const float nu = (1.f / 3.f) * tv * mfp;
+  float v = 2.f * (radius * radius) * (float(kRHO_H2O) - rg) * g / (9.f * rg * nu);
+  if (v * radius / nu > 10.f) v = sqrtf(8.f * radius * float(kRHO_H2O) * g / (3.f * rg * 0.8f));
+  return v;
+}
+
+// properties of the block's tracers, fixed at compile time (the split path runs the moist
+// constituent layout: 1 snow, 2 rain, 3 cloud ice, 4 cloud water, 5 graupel, 6 gas, 7 vapour):
+// constituent index, condensate or not, ice or water heat capacity (odd constituents are ice,
+// mo_dictionary.F90:175-189), fall speed (snow 1 m/s: radius 500 um above 250 um; cloud ice
+// 0.001 m/s; cloud water v_fall_liquid at radius 12 um; rain, graupel and vapour 0, their
+// radius never being set), and whether the surface sink's heat term applies (jc > nc/4)
+template <int SET>
+struct TrSet {
+  __device__ static constexpr int jc(int q) { return SET == 0 ? q + 1 : (q == 2 ? 7 : q + 4); }
+  __device__ static constexpr bool cond(int q) { return jc(q) <= 5; }
+  __device__ static constexpr bool ice(int q) { return (jc(q) - 1) % 2 == 0; }
+  __device__ static constexpr bool cloud(int q) { return jc(q) == 4; }
+  __device__ static constexpr float vfix(int q) { return jc(q) == 1 ? 1.f : jc(q) == 3 ? 0.001f : 0.f; }
+  __device__ static constexpr bool sfc_heat(int q) { return jc(q) > 1; }  // jc > nc/4 = 1
+};
+
+// One block: phases 1-3 above for tracer set SET; HEAT: the first substep, which also stores
+// the sediment heating.  Shared memory [level-1][tracer q][alpha, beta, e'][33]: the nine values
+// of a level sit at fixed offsets from one row address.
+template <int SET, bool HEAT>
+__device__ __forceinline__ void tracer_block(const Dims& D, const Grid<float>& GF, const GridX& X, const State& So,
+                                             const State& Sn, const StateF& Mo, const StateF& Mn,
+                                             const float* t_rho_all, const float* Tm, float* csh_part, float* sm) {
+  using P = TrSet<SET>;
+  const int nl = D.nl;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int ji = blockIdx.y * 32 + lane + 1;
+  const int jk = blockIdx.z + 1;
+  const bool valid = ji <= D.ny;
   const float dt = float(D.dtime);
   const float itw = 0.5f, ew = 0.5f;
-  const float* rho_g_o = Mo.rho + (long long)(D.g - 1) * D.fstride;
-  const float az_sfc = GF.area_z[IX(D, ji, jk, NL)];
-  const long long off = (long long)(jc - 1) * D.fstride;
-  const double* rho_o = So.rho + off;
-  const float* mro = Mo.rho + off;
-  double* rho_n = Sn.rho + off;
-  float* mrn = Mn.rho + off;
-  const float* t_rho = t_rho_all + off;
-  float* csh = csh_part + off;  // condensates only: jc <= nc
-  const bool ice = (jc - 1) % 2 == 0;
-  const bool cond = jc <= nc;
-  const bool heat = rk_step == 1 && cond;
-  float epr[kMaxL + 1];  // elimination multipliers
-  float rpr[kMaxL + 1];  // eliminated right-hand sides of the increment
-  // fall speeds: snow (radius 500 um above 250 um) 1 m/s, cloud ice 0.001 m/s, cloud water
-  // v_fall_liquid at radius 12 um, rain and graupel 0 (their radius is never set)
-  float vcl_a = (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, 1) : 0.f;
-  const float vsurf = (jc == 1) ? 1.f : (jc == 3) ? 0.001f
-                    : (jc == 4) ? vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, nl) : 0.f;
-  // The level loop is software-pipelined: the inputs of level m (1/volume, area_z, the old
-  // mirror density, old and new w, temperature, tendency) are loaded two iterations ahead,
-  // before the current level's results are stored, so two levels of loads are in flight per
-  // thread (a store may alias a later load, which stops the compiler from doing this).
-  struct LevelIn { float iv, az, ro, wo, wn, tm, tr; };
-  auto level_in = [&](int m) {
-    LevelIn r;
-    const long long p = IX(D, ji, jk, m);
-    r.iv = X.inv_volume_f[p];
-    r.az = GF.area_z[p];
-    r.ro = mro[p];
-    r.wo = Mo.w[p];
-    r.wn = Mn.w[p];
-    r.tm = cond ? Tm[p] : 0.f;  // condensates only
-    r.tr = t_rho[p];
-    return r;
+  const int pl = (int)D.plane;  // level stride; fstride*ncons < 2^31 for every supported grid
+  // 32-bit element indices off the arrays' base addresses, which stay kernel parameters: level
+  // jl of tracer q is at tq[q] + (jl-1)*pl
+  const int c32 = (int)IX(D, valid ? ji : 1, jk, 1);
+  int tq[kTrSet];
+#pragma unroll
+  for (int q = 0; q < kTrSet; ++q) tq[q] = (P::jc(q) - 1) * (int)D.fstride + c32;
+  const int grg = (D.g - 1) * (int)D.fstride + c32;
+  const int chunk = (nl + kTrWarps - 1) / kTrWarps;
+  const int l0 = w * chunk + 1, l1 = min(nl, (w + 1) * chunk);
+  auto load = [&](int m, TrLevel& L) {
+    const int o = (m - 1) * pl;
+#pragma unroll
+    for (int q = 0; q < kTrSet; ++q) {
+      L.ro[q] = Mo.rho[tq[q] + o];
+      L.tr[q] = t_rho_all[tq[q] + o];
+    }
+    const int e = c32 + o;
+    L.az = GF.area_z[e];
+    L.wo = Mo.w[e];
+    L.wn = Mn.w[e];
+    L.iv = X.inv_volume_f[e];
+    if (HEAT || SET == 1) L.tm = Tm[e];
+    if (SET == 1) {
+      L.rg = Mo.rho[grg + o];
+      L.gm = GF.gm[e];
+      L.gm1 = GF.gm[e + pl];
+      L.w5 = GF.ipw[4][e];
+      L.w6 = GF.ipw[5][e];
+    }
   };
-  LevelIn cur = level_in(1), nxt{}, nn{};
-  if (nl >= 2) nxt = level_in(2);
-  float vfi_up = 0.f, vfr_up = 0.f, vefv_up = 0.f;  // the interface above the current cell
-  float itv_a = itw * dt * cur.iv;
-  float epr_prev = 0.f, cv_prev = 0.f, rpr_prev = 0.f;
-  float ro_up = 0.f;  // mirror density of the cell above
-  for (int jl = 1; jl <= nl; ++jl) {
-    if (jl + 2 <= nl) nn = level_in(jl + 2);
-    const long long i = IX(D, ji, jk, jl);
-    const float iv = cur.iv, ro = cur.ro;
-    // the interface below the cell (between jl and jl+1)
-    float vfi = 0.f, vfr = 0.f, vefv = 0.f, itv_b = 0.f, ro_dn = 0.f;
-    if (jl <= nl - 1) {
-      itv_b = itw * dt * nxt.iv;
-      float vf = 0.f;
-      if (jc == 1) vf = 1.f;
-      else if (jc == 3) vf = 0.001f;
-      else if (jc == 4) {
-        const float vcl_b = vfall_liquid_f(D, GF, rho_g_o, Tm, 12.e-6f, ji, jk, jl + 1);
-        vf = 0.5f * (vcl_a + vcl_b);
-        vcl_a = vcl_b;
+  auto vf_of = [&](int q, float vcl) -> float { return P::cloud(q) ? vcl : P::vfix(q); };
+  auto cp_t = [&](int q, float tm) -> float { return (P::ice(q) ? c_p_ice(tm) : c_p_water(tm)) * tm; };
+  // ---- phase 1: coefficients, a thread walking its chunk of levels ----------------------------
+  // ring of level inputs: level jl in slot k, jl+1 in k+1, jl+2 and jl+3 loading (two levels of
+  // look-ahead: the interface below level jl+1 needs level jl+2 in the next iteration)
+  if (valid && l0 <= l1) {
+    TrLevel ring[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) ring[k] = TrLevel{};
+    load(l0, ring[0]);
+    if (l0 + 1 <= nl) load(l0 + 1, ring[1]);
+    if (l0 + 2 <= min(l1 + 1, nl)) load(l0 + 2, ring[2]);
+    // carried from the interface above the current level: flux coefficient, flux, heat flux of
+    // each tracer, the densities of the level above, and the cloud droplets' fall speed at the
+    // current level
+    float vfi_up[kTrSet], vfr_up[kTrSet], vefv_up[kTrSet], ro_up[kTrSet];
+    float vcl_cur = (SET == 1) ? vfall_liquid_l(ring[0], 12.e-6f, l0, nl) : 0.f;
+#pragma unroll
+    for (int q = 0; q < kTrSet; ++q) vfi_up[q] = vfr_up[q] = vefv_up[q] = ro_up[q] = 0.f;
+    if (l0 >= 2) {  // the interface above the chunk's first level, formed from scratch
+      TrLevel up{};
+      load(l0 - 1, up);
+      const TrLevel& cur = ring[0];
+      const float vcl_i = (SET == 1) ? 0.5f * (vfall_liquid_l(up, 12.e-6f, l0 - 1, nl) + vcl_cur) : 0.f;
+#pragma unroll
+      for (int q = 0; q < kTrSet; ++q) {
+        const float vf = vf_of(q, vcl_i);
+        vfi_up[q] = cur.az * (cur.wo - vf);
+        float fr = cur.az * (cur.wn - vf);
+        fr = ((fr >= 0.f) ? cur.ro[q] : up.ro[q]) * fr;
+        vfr_up[q] = fr;
+        if (HEAT && P::cond(q)) vefv_up[q] = cp_t(q, cur.tm) * fr;
+        ro_up[q] = up.ro[q];
       }
-      const float az = nxt.az;
-      ro_dn = nxt.ro;
-      vfi = az * (nxt.wo - vf);
-      float fr = az * (nxt.wn - vf);
-      fr = ((fr >= 0.f) ? ro_dn : ro) * fr;
-      vfr = fr;
-      if (cond) vefv = (ice ? c_p_ice(nxt.tm) : c_p_water(nxt.tm)) * nxt.tm * fr;
     }
-    // d - 1, explicit flux part and sediment heating of cell jl
-    float dm1, fl, h = 0.f;
-    if (jl == 1) {
-      dm1 = (vfi >= 0.f) ? 0.f : -itv_a * vfi;
-      fl = ew * dt * vfr * iv;
-      h = vefv * iv;
-    } else if (jl == nl) {
-      dm1 = (vfi_up >= 0.f) ? itv_a * vfi_up : 0.f;
-      fl = -ew * dt * vfr_up * iv;
-      h = -vefv_up * iv;
-      if (cond) {
-        dm1 += itw * vsurf * dt * az_sfc * iv;
-        fl -= ew * vsurf * dt * ro * az_sfc * iv;
-        if (jc > nc / 4) {
-          const float Tn = cur.tm;
-          h -= vsurf * Tn * (ice ? c_p_ice(Tn) : c_p_water(Tn)) * ro * az_sfc * iv;
+    for (int base = l0; base <= l1; base += 4) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int jl = base + k;
+        if (jl > l1) break;
+        if (jl + 3 <= min(l1 + 1, nl)) load(jl + 3, ring[(k + 3) % 4]);
+        const TrLevel& cur = ring[k];
+        const TrLevel& nxt = ring[(k + 1) % 4];
+        const int o = (jl - 1) * pl;
+        const float iv = cur.iv;
+        const float itv_a = itw * dt * iv;
+        const bool below = jl <= nl - 1;
+        // shared parts of the interface below the level (w level jl+1)
+        float vcl_b = 0.f, vcl_i = 0.f;
+        if (SET == 1 && below) {
+          vcl_b = vfall_liquid_l(nxt, 12.e-6f, jl + 1, nl);
+          vcl_i = 0.5f * (vcl_cur + vcl_b);
         }
+        const float az_sfc = (jl == nl) ? GF.area_z[c32 + o + pl] : 0.f;
+        float* row = sm + (jl - 1) * kTrRow + lane;
+#pragma unroll
+        for (int q = 0; q < kTrSet; ++q) {
+          const float ro = cur.ro[q];
+          float vfi = 0.f, vfr = 0.f, vefv = 0.f, ro_dn = 0.f;
+          if (below) {
+            const float vf = vf_of(q, vcl_i);
+            ro_dn = nxt.ro[q];
+            vfi = nxt.az * (nxt.wo - vf);
+            float fr = nxt.az * (nxt.wn - vf);
+            fr = ((fr >= 0.f) ? ro_dn : ro) * fr;
+            vfr = fr;
+            if (HEAT && P::cond(q)) vefv = cp_t(q, nxt.tm) * fr;
+          }
+          // d - 1, explicit flux part and sediment heating of cell jl
+          float dm1, fl, h = 0.f;
+          if (jl == 1) {
+            dm1 = (vfi >= 0.f) ? 0.f : -itv_a * vfi;
+            fl = ew * dt * vfr * iv;
+            h = vefv * iv;
+          } else if (jl == nl) {
+            dm1 = (vfi_up[q] >= 0.f) ? itv_a * vfi_up[q] : 0.f;
+            fl = -ew * dt * vfr_up[q] * iv;
+            h = -vefv_up[q] * iv;
+            if (P::cond(q)) {
+              const float vsurf = vf_of(q, vcl_cur);  // the lowest layer's own fall speed
+              dm1 += itw * vsurf * dt * az_sfc * iv;
+              fl -= ew * vsurf * dt * ro * az_sfc * iv;
+              if (HEAT && P::sfc_heat(q)) {
+                const float tn = cur.tm;
+                h -= vsurf * tn * (P::ice(q) ? c_p_ice(tn) : c_p_water(tn)) * ro * az_sfc * iv;
+              }
+            }
+          } else {
+            dm1 = 0.f;
+            if (vfi_up[q] >= 0.f) dm1 += itv_a * vfi_up[q];
+            if (vfi < 0.f) dm1 -= itv_a * vfi;
+            fl = ew * dt * (vfr - vfr_up[q]) * iv;
+            h = (vefv - vefv_up[q]) * iv;
+          }
+          if (HEAT && P::cond(q)) csh_part[tq[q] + o] = h;
+          // couplings: row jl to jl+1 (upward flux below), row jl to jl-1 (downward flux above);
+          // the pivot is the diagonal 1 + (d - 1)
+          const float ev = (below && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
+          const float cv_up = (jl >= 2 && vfi_up[q] < 0.f) ? itv_a * vfi_up[q] : 0.f;
+          const float rhs = (dt * cur.tr[q] + fl) - dm1 * ro - ev * ro_dn - cv_up * ro_up[q];
+          const float ip = 1.f / (1.f + dm1);
+          row[(3 * q + 0) * kTrPitch] = -cv_up * ip;
+          row[(3 * q + 1) * kTrPitch] = rhs * ip;
+          row[(3 * q + 2) * kTrPitch] = ev * ip;
+          vfi_up[q] = vfi;
+          vfr_up[q] = vfr;
+          vefv_up[q] = vefv;
+          ro_up[q] = ro;
+        }
+        vcl_cur = vcl_b;
       }
-    } else {
-      dm1 = 0.f;
-      if (vfi_up >= 0.f) dm1 += itv_a * vfi_up;
-      if (vfi < 0.f) dm1 -= itv_a * vfi;
-      fl = ew * dt * (vfr - vfr_up) * iv;
-      h = (vefv - vefv_up) * iv;
     }
-    if (heat) csh[i] = h;
-    // couplings: row jl to jl+1 (upward flux below) and row jl+1 to jl (downward flux below)
-    const float ev = (jl <= nl - 1 && vfi >= 0.f) ? -(itv_a * vfi) : 0.f;
-    const float cv = (jl <= nl - 1 && vfi < 0.f) ? itv_b * vfi : 0.f;
-    // right-hand side of the increment and forward elimination (pivot = d: one of e, c of an
-    // interface is 0)
-    const float rhs = (dt * cur.tr + fl) - dm1 * ro - ev * ro_dn - cv_prev * ro_up;
-    const float piv = (1.f + dm1) - epr_prev * cv_prev;
-    rpr_prev = (rhs - cv_prev * rpr_prev) / piv;
-    rpr[jl] = rpr_prev;
-    epr_prev = ev / piv;
-    epr[jl] = epr_prev;
-    cv_prev = cv;
-    vfi_up = vfi; vfr_up = vfr; vefv_up = vefv; itv_a = itv_b;
-    ro_up = ro;
-    cur = nxt;
-    nxt = nn;
   }
-  // back substitution; the new density rho_old + delta in FP64, negative densities clipped on
-  // output (mo_column_solvers.F90:587-591; the sign is read from the high word).  The old
-  // density of the next level up is loaded before the current level is stored.
-  float dl = 0.f;
-  double ro_next = rho_o[IX(D, ji, jk, nl)];
-  for (int jl = nl; jl >= 1; --jl) {
-    const long long i = IX(D, ji, jk, jl);
-    const double ro_old = ro_next;
-    if (jl > 1) ro_next = rho_o[i - D.plane];
-    dl = rpr[jl] - epr[jl] * dl;
-    const double sn = ro_old + wide(dl);
-    const double o = __double2hiint(sn) < 0 ? 0.0 : sn;
-    rho_n[i] = o;
-    mrn[i] = narrow(o);
+  // the old FP64 densities of phase 3, loaded before the sweeps so that they arrive meanwhile
+  // (the registers of phase 1 are free by now); chunks longer than kTrPre levels load the rest
+  // in phase 3
+  double rq[kTrPre][kTrSet];
+#pragma unroll
+  for (int k = 0; k < kTrPre; ++k)
+#pragma unroll
+    for (int q = 0; q < kTrSet; ++q) rq[k][q] = (valid && l0 + k <= l1) ? So.rho[tq[q] + (l0 + k - 1) * pl] : 0.0;
+  __syncthreads();
+  // ---- phase 2: the sweeps, warp q for tracer q, a lane per column -----------------------------
+  if (w < kTrSet) {
+    float* row = sm + lane + 3 * w * kTrPitch;
+    float r = 0.f;
+#pragma unroll 4
+    for (int jl = 1; jl <= nl; ++jl, row += kTrRow) {
+      r = row[0] * r + row[kTrPitch];
+      row[kTrPitch] = r;
+    }
+    float dl = 0.f;
+#pragma unroll 4
+    for (int jl = nl; jl >= 1; --jl) {
+      row -= kTrRow;
+      dl = row[kTrPitch] - row[2 * kTrPitch] * dl;
+      row[kTrPitch] = dl;
+    }
   }
+  __syncthreads();
+  // ---- phase 3: new densities rho_old + delta (FP64), clipped, and their mirror ---------------
+  if (!valid || l0 > l1) return;
+  // the mirror is rounded by the hardware conversion here (the bits of narrow() in one issue
+  // slot): the FP64 pipe carries only this and the addition per value, against a dozen integer
+  // operations for narrow()
+  auto update = [&](int jl, int q, double ro_old) {
+    const int e = tq[q] + (jl - 1) * pl;
+    const double sn = ro_old + wide(sm[(jl - 1) * kTrRow + lane + (3 * q + 1) * kTrPitch]);
+    const double v = __double2hiint(sn) < 0 ? 0.0 : sn;
+    Sn.rho[e] = v;
+    Mn.rho[e] = __double2float_rn(v);
+  };
+#pragma unroll
+  for (int k = 0; k < kTrPre; ++k)
+#pragma unroll
+    for (int q = 0; q < kTrSet; ++q)
+      if (l0 + k <= l1) update(l0 + k, q, rq[k][q]);
+  for (int jl = l0 + kTrPre; jl <= l1; ++jl)
+#pragma unroll
+    for (int q = 0; q < kTrSet; ++q) update(jl, q, So.rho[tq[q] + (jl - 1) * pl]);
+}
+
+// grid (2 tracer sets, row tiles, nx), 256 threads, dynamic shared memory tracer_smem(D);
+// HEAT: the first substep
+template <bool HEAT>
+__global__ void __launch_bounds__(kTrWarps * 32, 2) ks_column_tracers(Dims D, Grid<float> GF, GridX X, State So,
+                                                                      State Sn, StateF Mo, StateF Mn,
+                                                                      const float* t_rho_all, const float* Tm,
+                                                                      float* csh_part) {
+  extern __shared__ float sm[];
+  if (blockIdx.x == 0) tracer_block<0, HEAT>(D, GF, X, So, Sn, Mo, Mn, t_rho_all, Tm, csh_part, sm);
+  else tracer_block<1, HEAT>(D, GF, X, So, Sn, Mo, Mn, t_rho_all, Tm, csh_part, sm);
 }
 
 // sediment heating of all condensates: the per-condensate planes of ks_column_tracers added
@@ -1043,6 +1181,9 @@ __global__ void ks_csh_sum(Dims D, const float* csh_part, float* csh) {
   for (int jc = 0; jc < D.nc; ++jc) h += csh_part[q + (long long)jc * D.fstride];
   csh[q] = h;
 }
+
+// dynamic shared memory of ks_column_tracers: alpha, beta and e' of three tracers, 32 columns
+size_t tracer_smem(const Dims& D) { return (size_t)D.nl * kTrRow * sizeof(float); }
 
 dim3 sblk() { return dim3(32, 8, 1); }
 // x: row tiles, y: levels, z: column tiles (see LG_IDX3)
@@ -1058,6 +1199,15 @@ dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsig
 int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
   if (D.ncons > 1 && D.ncons != kTracers + 1) {
     lgame_set_error("split precision: the tracer kernel is built for five condensates and water vapour");
+    return LGAME_ERR_UNSUPPORTED;
+  }
+  if (D.ncons > 1 &&
+      (D.nl > 128 ||
+       cudaFuncSetAttribute(ks_column_tracers<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)tracer_smem(D)) != cudaSuccess ||
+       cudaFuncSetAttribute(ks_column_tracers<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)tracer_smem(D)) != cudaSuccess)) {
+    lgame_set_error("split precision: the tracer solver supports at most 128 layers");
     return LGAME_ERR_UNSUPPORTED;
   }
   auto* s = new SplitCtx();
@@ -1318,10 +1468,11 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
   const StateF& Mo = s->mir[so];
   const StateF& Mn = s->mir[sn];
   int launches = 0;
-#define SL(name, kernel, grid_, block_, ...)                                    \
+#define SL(name, kernel, grid_, block_, ...) SLS(name, kernel, grid_, block_, 0, __VA_ARGS__)
+#define SLS(name, kernel, grid_, block_, smem_, ...)                            \
   do {                                                                          \
     const int tr_ = tb ? tb(tracer, name) : -1;                                 \
-    kernel<<<grid_, block_, 0, stream>>>(__VA_ARGS__);                          \
+    kernel<<<grid_, block_, smem_, stream>>>(__VA_ARGS__);                      \
     if (tr_ >= 0) te(tracer, tr_);                                              \
     cudaError_t e_ = cudaGetLastError();                                        \
     if (e_ != cudaSuccess) {                                                    \
@@ -1387,14 +1538,16 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     const dim3 gc = cgrd(D.ny, D.nx);
     SL("ks_column_ver", ks_column_ver, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
     if (D.ncons > 1) {
-      const dim3 gt((unsigned)(D.ncons - 1), gc.x, gc.y);
-      SL("ks_column_tracers", ks_column_tracers, gt, cblk(), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature,
-         s->csh_part, rk);
+      // the two tracer sets fastest (the blocks of a row tile run together), row tiles, columns
+      const dim3 gt(2u, (unsigned)((D.ny + 31) / 32), (unsigned)D.nx);
+      SLS("ks_column_tracers", (rk == 1 ? ks_column_tracers<true> : ks_column_tracers<false>), gt,
+          dim3(kTrWarps * 32), tracer_smem(D), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature, s->csh_part);
       if (rk == 1 && D.nc > 0)
         SL("ks_csh_sum", ks_csh_sum, sgrd(D.ny, D.nx, D.nl), B, D, s->csh_part, C.csh);
     }
   }
 #undef SL
+#undef SLS
   *nk = launches;
   return LGAME_OK;
 }

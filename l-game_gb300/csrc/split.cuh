@@ -8,8 +8,11 @@
 // FP64: the state, its accumulation state_old + dt*tendency, the gradient of the Exner
 //       pressure perturbation and both pressure-gradient products (the hydrostatic
 //       background subtraction), the kinetic energy and its differences (a vertical
-//       difference over a thin layer cancels most of its digits), the right-hand sides and
-//       substitution sweeps of the vertically implicit column solves, the budget sums.
+//       difference over a thin layer cancels most of its digits), the right-hand side and
+//       both substitution sweeps of the vertical acoustic solve (its coefficients and
+//       elimination multipliers are FP32), the budget sums.  The tracer solve is FP32 for
+//       the increment delta = rho_new - rho_old (coefficients, right-hand side, both sweeps),
+//       so its rounding is relative to the flux terms; only rho_old + delta is FP64.
 #pragma once
 
 #include <cuda_runtime.h>
