@@ -417,7 +417,7 @@ def run_ours(args):
     ncons = n.n_constituents
     f_oro = (n.n_oro_layers + 1) / n.n_layers
     results = {}
-    precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64]
+    precisions = [L.PRECISION_SPLIT, L.PRECISION_FP64, L.PRECISION_SPLIT_FP64_COLUMN]
     if args.fp64_only:
         precisions = [L.PRECISION_FP64]
     elif args.split_only:
@@ -451,7 +451,7 @@ def run_ours(args):
         el = reduce_max(dist, el)
         nk = g.kernels_per_step()
         prof = profile_kernels(g, 2, args.warmup + args.steps, ncons, cells, peaks["hbm_gbs"],
-                               prec == L.PRECISION_SPLIT, f_oro)
+                               prec != L.PRECISION_FP64, f_oro)
         st = g.get_state((args.warmup + args.steps + 2) % 2)
         finite = all(bool(np.isfinite(v).all()) for v in st.values())
         results[prec] = {"s_per_step": el / args.steps, "kernels_per_step": nk, "profile": prof, "finite": finite,
@@ -504,6 +504,13 @@ def run_ours(args):
                         "kernel_shares": fp64["profile"]["shares"]}
         if head_prec != L.PRECISION_FP64:
             line["split_speedup_vs_fp64"] = fp64["s_per_step"] / head["s_per_step"]
+    col64 = results.get(L.PRECISION_SPLIT_FP64_COLUMN)
+    if col64 is not None:
+        # the split step with the vertical acoustic solve wholly in FP64 (precision mode 2)
+        line["split_fp64_column"] = {"value": ws / col64["s_per_step"], "ms_per_step": col64["s_per_step"] * 1e3,
+                                     "column_ver_ms_per_launch": {k: v["ms"] / v["launches"]
+                                                                  for k, v in col64["profile"]["rows"]}.get("ks_column_ver"),
+                                     "speedup_vs_fp64": (fp64["s_per_step"] / col64["s_per_step"]) if fp64 else None}
     if "output" in head:
         line["output"] = head["output"]
     if "e2e" in head:

@@ -49,9 +49,14 @@ extern "C" {
 
 /* ---- precision modes ---------------------------------------------------- */
 #define LGAME_PRECISION_FP64   0  /* every operation in FP64, reference operation order */
-#define LGAME_PRECISION_SPLIT  1  /* FP32 explicit stencils and tracer fluxes; FP64
-                                     column solves, background subtraction in the
-                                     pressure gradient, state accumulation and budgets */
+#define LGAME_PRECISION_SPLIT  1  /* FP32 explicit stencils, tracer fluxes and the
+                                     coefficients and multipliers of the column solves;
+                                     FP64 right-hand side and substitutions of the vertical
+                                     acoustic solve, background subtraction in the pressure
+                                     gradient, state accumulation and budgets */
+#define LGAME_PRECISION_SPLIT_FP64_COLUMN 2  /* as LGAME_PRECISION_SPLIT, with the vertical
+                                     acoustic solve wholly in FP64 (coefficients,
+                                     multipliers, quotients from the FP64 state) */
 
 /* ---- run configuration ----------------------------------------------------
  * One field per namelist variable the HEVI step reads (the src/namelists modules),

@@ -29,6 +29,7 @@ struct Dims {
   int periodic, freeslip, lcorio, llinear, luse_bg, lmoist, theta_order, lklemp;
   double dtime, toa, dxn, dyn;  // namelist dx, dy
   double theta_edge_c;          // 1/8*dy*dx of the third-order theta edges, formed once on the host
+  int ndamp;                    // n_damping_levels: levels whose highest z_w lies above klemp_begin_rel*toa
 };
 
 // ---- FP32 <-> FP64 conversions in integer operations ------------------------------

@@ -343,8 +343,9 @@ extern "C" int lgame_namelist_parse(const char* text, lgame_namelist* n) {
   if (n->lpbl && !n->lmom_diff_h) return fail(LGAME_ERR_BAD_CONFIG, "Error: lmom_diff_h must be true is lpbl is true.");
   // control.F90:94-97
   if (n->dtime > n->dt_write) return fail(LGAME_ERR_BAD_CONFIG, "Error: It must be dtime <= dt_write.");
-  if (n->precision != LGAME_PRECISION_FP64 && n->precision != LGAME_PRECISION_SPLIT)
-    return fail(LGAME_ERR_BAD_CONFIG, "&gpu: precision must be 0 (fp64) or 1 (split).");
+  if (n->precision != LGAME_PRECISION_FP64 && n->precision != LGAME_PRECISION_SPLIT &&
+      n->precision != LGAME_PRECISION_SPLIT_FP64_COLUMN)
+    return fail(LGAME_ERR_BAD_CONFIG, "&gpu: precision must be 0 (fp64), 1 (split) or 2 (split, fp64 column solve).");
   return LGAME_OK;
 }
 

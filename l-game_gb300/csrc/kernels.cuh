@@ -687,7 +687,8 @@ __global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const
 // scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177
 template <class T, class V = double>
 __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, const T* tvu,
-                            const T* tvv, const T* Tm, const T* rad, const T* csh, T* t_rho, T* t_rt) {
+                            const T* tvv, const T* Tm, const T* hd, const T* rad, const T* csh, T* t_rho,
+                            T* t_rt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -707,7 +708,9 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
     auto gy = [&](int i, int j, int k) { return tvv[IX(D, i, j, k)] * fy(i, j, k); };
     div_t = div_h_at<T>(D, G, gx, gy, ji, jk, jl);
   }
-  const T heat = rad[q] + csh[q];
+  // dissipative heating, radiation, sediment heating (phase transitions and temperature
+  // diffusion are zero), in the reference's order
+  const T heat = hd[q] + rad[q] + csh[q];
   T x = T(0);
   if (heat != T(0)) {
     const T cv = c_v_mass_weighted_air<T>(D, Ss.rho, Tm, q);

@@ -64,6 +64,7 @@ struct lgame_gpu {
   Tend<double> tend;
   double *pg_nl_u, *pg_nl_v, *pg_nl_w, *pg_l_u, *pg_l_v, *pg_l_w, *pg_old_u, *pg_old_v, *pgcw;
   double *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
+  double* hdiss;  // heating_diss: dissipative heating of the swamp layer, formed at each step's first substep
   // scratch
   double *theta, *gz, *gx, *gy, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph, *vsq;
   double* staging = nullptr;
@@ -374,6 +375,27 @@ __global__ void k_output(Dims D, Grid<double> G, State A, State B, double c1, do
   f[4 * nS + o] = to_f32(upper_weight * w0 + (1.0 - upper_weight) * w1);
 }
 
+// simple_dissipation_rate, mo_momentum_diff_diss.F90:333-389, with the diffusion accelerations
+// zero (diffusion is not in the step): the Klemp swamp layer's deceleration of w,
+// (w/damping_prefactor - w)/dtime at w levels 2..n_damping_levels, its inner product with the
+// wind (only the two vertical terms are nonzero) times -sum(rho(1:nc+1)).  damping_prefactor =
+// 1 + dtime*damping_coeff is the column solver's prefactor G.damp (the same bits); it is 1 at the
+// top level and wherever z_w lies below the layer, where the deceleration is then 0 as in the
+// reference's loop bounds.  One thread per scalar point of layers 1..min(nl, n_damping_levels);
+// the deeper layers stay 0.
+__global__ void k_heating_diss(Dims D, Grid<double> G, State S, double* hd) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  const long long q = IX(D, ji, jk, jl), b = q + D.plane;
+  auto decel = [&](long long p, int lev) -> double {
+    if (lev < 2 || lev > D.ndamp) return 0.0;
+    const double w = S.w[p];
+    return 0.0 + (w / G.damp[p] - w) / D.dtime;  // mom_diff_tend_z (0) plus the swamp layer's part
+  };
+  const double ip = G.ipw[4][q] * S.w[q] * decel(q, jl) + G.ipw[5][q] * S.w[b] * decel(b, jl + 1);
+  hd[q] = -rho_sum_cond_gas<double, double>(D, S.rho, q) * ip;
+}
+
 // deterministic FP64 sums: every block sums a fixed strided subset in a fixed order;
 // the partial sums are then added by one thread in block order.
 constexpr int kRedBlocks = 1024, kRedThreads = 256;
@@ -539,6 +561,10 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       int rc = advection(c, Sv);
       if (rc != LGAME_OK) return rc;
     }
+    // momentum diffusion and dissipation at the first substep (mo_vector_tend_expl.F90:100-126):
+    // with the Klemp layer on, its dissipative heating from state_old
+    if (rk == 1 && D.lklemp && D.ndamp > 0)
+      LAUNCH(k_heating_diss, grd(D, D.ny, D.nx, std::min(D.nl, D.ndamp)), D, G, So, c->hdiss);
     Tend<double> T = c->tend;
     LAUNCH(kd::k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk, (float*)nullptr, (float*)nullptr);
     // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
@@ -552,8 +578,8 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       int rc = theta3(c, Ss.tp, 0, Ss.u, Ss.v, c->tvu, c->tvv);
       if (rc != LGAME_OK) return rc;
     }
-    LAUNCH(kd::k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->rad,
-           c->csh, T.rho, T.rt);
+    LAUNCH(kd::k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->hdiss,
+           c->rad, c->csh, T.rho, T.rt);
     // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
     {
       dim3 g2((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 7) / 8), 1);
@@ -623,8 +649,10 @@ int check_cfg(const lgame_config* cfg) {
     return set_err(LGAME_ERR_BAD_CONFIG, "theta_adv_order must be 2 or 3");
   if (!(cfg->dtime > 0.0) || !(cfg->toa > 0.0) || !(cfg->dx > 0.0) || !(cfg->dy > 0.0))
     return set_err(LGAME_ERR_BAD_CONFIG, "dtime, toa, dx and dy must be positive");
-  if (cfg->precision != LGAME_PRECISION_FP64 && cfg->precision != LGAME_PRECISION_SPLIT)
-    return set_err(LGAME_ERR_BAD_CONFIG, "precision must be LGAME_PRECISION_FP64 or LGAME_PRECISION_SPLIT");
+  if (cfg->precision != LGAME_PRECISION_FP64 && cfg->precision != LGAME_PRECISION_SPLIT &&
+      cfg->precision != LGAME_PRECISION_SPLIT_FP64_COLUMN)
+    return set_err(LGAME_ERR_BAD_CONFIG,
+                   "precision must be LGAME_PRECISION_FP64, LGAME_PRECISION_SPLIT or LGAME_PRECISION_SPLIT_FP64_COLUMN");
   if (cfg->lmom_diff_h || cfg->lmom_diff_v || cfg->ltemp_diff_h || cfg->ltemp_diff_v || cfg->lmass_diff_h || cfg->lmass_diff_v)
     return set_err(LGAME_ERR_UNSUPPORTED, "diffusion (&diff lmom_diff_h ... lmass_diff_v) is not part of the GPU step");
   if (cfg->lprog_soil_temp || cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl)
@@ -667,6 +695,7 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   D.luse_bg = cfg->luse_bg_state; D.lmoist = cfg->lmoist; D.theta_order = cfg->theta_adv_order; D.lklemp = cfg->lklemp;
   D.dtime = cfg->dtime; D.toa = cfg->toa; D.dxn = cfg->dx; D.dyn = cfg->dy;
   D.theta_edge_c = 1.0 / 8.0 * D.dyn * D.dxn;  // the device expression, evaluated once
+  D.ndamp = 0;                                  // set with the grid
   auto fail = [&](int code) { lgame_gpu_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
     return fail(set_err(LGAME_ERR_CUDA, "cudaStreamCreate failed"));
@@ -694,7 +723,7 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     return fail(rc);
   double** carried[] = {&c->pg_nl_u, &c->pg_nl_v, &c->pg_nl_w, &c->pg_l_u, &c->pg_l_v, &c->pg_l_w, &c->pg_old_u,
                         &c->pg_old_v, &c->pgcw, &c->vsg_x, &c->vsg_y, &c->vsg_z, &c->pvt_x, &c->pvt_y, &c->pvt_z,
-                        &c->csh, &c->rad, &c->temperature};
+                        &c->csh, &c->rad, &c->temperature, &c->hdiss};
   for (double** p : carried) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
   double** scratch[] = {&c->theta, &c->gz, &c->gx, &c->gy, &c->divf, &c->tvu, &c->tvv, &c->tpu, &c->tpv,
                         &c->ex, &c->ey, &c->ez, &c->uph, &c->vph, &c->wph, &c->vsq};
@@ -725,8 +754,9 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   for (int k = 0; k < 3; ++k) G.trsk_u[k] = c->trsk_u[k];
   for (int k = 0; k < 2; ++k) G.trsk_v[k] = c->trsk_v[k];
   G.damp = c->damp;
-  if (cfg->precision == LGAME_PRECISION_SPLIT) {
-    if ((rc = split_create(c->D, &c->split, &c->bytes)) != LGAME_OK) return fail(rc);
+  if (cfg->precision != LGAME_PRECISION_FP64) {
+    if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, &c->split, &c->bytes)) != LGAME_OK)
+      return fail(rc);
   }
   *out = c;
   return LGAME_OK;
@@ -782,6 +812,16 @@ extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfie
         }
     if ((rc = copy_h2d(c, c->damp, dp.data(), ext_w(D))) != LGAME_OK) return rc;
     CK(cudaStreamSynchronize(c->stream));
+    // n_damping_levels, mo_grid_generator.F90:1049-1058: the levels whose highest z_w lies above
+    // the damping layer's lower boundary (the swamp layer's dissipation is formed there)
+    int ndamp = 0;
+    for (int jl = 0; jl <= D.nl; ++jl) {
+      double max_z = -1e300;
+      for (size_t p = 0; p < ny * nx; ++p) max_z = std::max(max_z, zw[p + ny * nx * (size_t)jl]);
+      if (max_z > dsh) ++ndamp;
+    }
+    c->D.ndamp = ndamp;
+    CK(cudaMemsetAsync(c->hdiss, 0, sizeof(double) * (size_t)D.fstride, c->stream));
   }
   if (c->split) {
     if ((rc = split_set_grid(c->split, c->D, c->G, c->stream)) != LGAME_OK) return rc;

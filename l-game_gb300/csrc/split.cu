@@ -17,6 +17,7 @@
 #include "common.h"
 #include "lgame_gpu.h"
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -31,6 +32,9 @@ struct GridX {  // FP64 reciprocal metrics and FP32 metric differences of the FP
   // FP32: 1/volume, 1/area_z, and at w level jl (2..nl) z_scalar(jl-1)-z_scalar(jl) and
   // exner_bg(jl-1)-exner_bg(jl), differenced in FP64 before rounding (no cancellation)
   const float *inv_volume_f, *inv_area_z_f, *dzs_f, *deb_f;
+  // FP32: the swamp layer's deceleration per unit w, (1/damping_prefactor - 1)/dtime, formed in
+  // FP64 (w/p - w would cancel where the prefactor is near 1); 0 at the top level
+  const float* kdamp_f;
 };
 
 // x / d to FP64 accuracy for an FP32 divisor d in the normal range.  r = 1/d correctly
@@ -74,6 +78,9 @@ struct SplitCtx {
   SplitCarriedF C{};
   // rhotheta_v of the background state, p_0/r_d*exner_bg^(c_d_v/r_d) (boundary relaxation)
   double* rtbg = nullptr;
+  // the vertical acoustic solve with FP64 coefficients and elimination (precision mode
+  // LGAME_PRECISION_SPLIT_FP64_COLUMN)
+  bool column_fp64 = false;
 };
 
 namespace {
@@ -110,11 +117,12 @@ __global__ void k_recip(const double* a, double* b, long long n) {
     b[i] = (a[i] != 0.0) ? 1.0 / a[i] : 0.0;
 }
 // FP32 metric reciprocals and vertical differences of the column solver (set-up only)
-__global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, float* dzs, float* deb) {
+__global__ void k_grid_extra(Dims D, Grid<double> G, float* ivol, float* iaz, float* dzs, float* deb, float* kd) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx || jl > D.NL) return;
   const long long q = IX(D, ji, jk, jl);
   iaz[q] = (G.area_z[q] != 0.0) ? float(1.0 / G.area_z[q]) : 0.f;
+  kd[q] = (jl >= 2) ? float((1.0 / G.damp[q] - 1.0) / D.dtime) : 0.f;
   if (jl <= D.nl) ivol[q] = float(1.0 / G.volume[q]);
   if (jl >= 2 && jl <= D.nl) {
     const long long a = IX(D, ji, jk, jl - 1);
@@ -383,6 +391,21 @@ __global__ void k_bg_faces(Dims D, Grid<double> G, float2* tbu, float2* tbv) {
   }
 }
 
+// simple_dissipation_rate, mo_momentum_diff_diss.F90:333-389, split step: the swamp layer's
+// dissipative heating -sum(rho(1:nc+1))*(W5 w(jl) d(jl) + W6 w(jl+1) d(jl+1)), d = w*kdamp the
+// deceleration at w levels 2..n_damping_levels, in FP32 from the mirror (a heating term, as
+// the radiation and sediment heating it is added to)
+__global__ void ks_heating_diss(Dims D, Grid<float> GF, GridX X, StateF M, float* hd) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  const long long q = IX(D, ji, jk, jl), b = q + D.plane;
+  const float wa = M.w[q], wb = M.w[b];
+  const float da = (jl >= 2 && jl <= D.ndamp) ? wa * X.kdamp_f[q] : 0.f;
+  const float db = (jl + 1 <= D.ndamp) ? wb * X.kdamp_f[b] : 0.f;
+  const float ip = GF.ipw[4][q] * wa * da + GF.ipw[5][q] * wb * db;
+  hd[q] = -rho_sum_cond_gas<float, float>(D, M.rho, q) * ip;
+}
+
 // ---- column-marching divergences -------------------------------------------------------
 // div_h with the contravariant vertical correction (div_h_at above: div_h,
 // mo_divergence_operators.F90:16-68, and vertical_contravariant_corr, mo_averaging.F90:16-54)
@@ -468,7 +491,8 @@ __global__ void __launch_bounds__(128) ks_div_h(Dims D, Grid<float> GF, GridX X,
 // mo_scalar_tend_expl.F90:106-177 (the gas has old_weight 0, new_weight 1), column-marching
 __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* fu,
                                                   const float* fv, const float* gu, const float* gv, const float* Tm,
-                                                  const float* rad, const float* csh, float* t_rho, float* t_rt) {
+                                                  const float* hd, const float* rad, const float* csh, float* t_rho,
+                                                  float* t_rt) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
@@ -488,7 +512,7 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
       mn = layer_faces(D, GF, fx, fy, ji, jk, jl + 1);
       tn = layer_faces(D, GF, gx, gy, ji, jk, jl + 1);
     }
-    const float heat = rad[q] + csh[q];
+    const float heat = hd[q] + rad[q] + csh[q];  // dissipative, radiative, sediment heating
     const float div_m = div_col(D, GF, X, mc, vert_faces(D, mh_prev, mc.h, mn.h, jl), ji, jk, jl);
     const float div_t = div_col(D, GF, X, tc, vert_faces(D, th_prev, tc.h, tn.h, jl), ji, jk, jl);
     float x = 0.f;
@@ -673,112 +697,139 @@ __global__ void ks_tend_wind(Dims D, State So, State Sn, Tend<float> Tn, Carried
 
 // ---- three_band_solver_ver, mo_column_solvers.F90:21-351 --------------------------------
 // The reference's implicit system for the vertical mass-flux increments at levels 2..nl,
-// one thread per column, streamed top to bottom.  FP32 (from the mirror): the partial
-// derivatives alpha, beta, gamma, the interface theta and density weights, the matrix and
-// its elimination multipliers.  FP64: the explicit predictions of theta' and exner', the
-// right-hand side (where the pressure-gradient and buoyancy terms balance), the forward
-// and back substitution, and the new rho_g, rho*theta_v, exner', w.  theta' is formed as
-// (rho*theta_v - theta_bg*rho)/rho with the small numerator in FP64.
+// one thread per column, streamed top to bottom.  C = float (LGAME_PRECISION_SPLIT): from the
+// FP32 mirror, the partial derivatives alpha, beta, gamma, the interface theta and density
+// weights, the matrix and its elimination multipliers; FP64: the explicit predictions of theta'
+// and exner', the right-hand side (where the pressure-gradient and buoyancy terms balance), the
+// forward and back substitution, and the new rho_g, rho*theta_v, exner', w; theta' is formed as
+// (rho*theta_v - theta_bg*rho)/rho with the small numerator in FP64.  C = double
+// (LGAME_PRECISION_SPLIT_FP64_COLUMN): the same from the FP64 state, FP64 metric differences and
+// reciprocals, with FP64 coefficients, multipliers and quotients -- the column solve wholly in
+// FP64 (only the explicit tendencies it reads are FP32).
+template <class C>
 __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, Grid<float> GF, GridX X, State So,
                                                      State Sn, StateF Mo, StateF Mn, Tend<float> Tn, int rk_step) {
+  constexpr bool F64 = sizeof(C) == 8;
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
   const int nl = D.nl, n = nl - 1;
-  const float dtf = float(D.dtime), idtf = float(1.0 / D.dtime);
+  const C dtf = C(D.dtime), idtf = C(1.0 / D.dtime);
   const double idtd = 1.0 / D.dtime;
   const long long goff = (long long)(D.g - 1) * D.fstride;
-  const float rdcv = float(kR_D / kC_D_V);
-  const float ic2 = float(1.0 / (kIMPL_THERMO_WEIGHT * (D.dtime * D.dtime) * kC_D_P));
-  const float ic1 = float(1.0 / (kIMPL_THERMO_WEIGHT * D.dtime * kC_D_P));
+  const C rdcv = C(kR_D / kC_D_V);
+  const C ic2 = C(1.0 / (kIMPL_THERMO_WEIGHT * (D.dtime * D.dtime) * kC_D_P));
+  const C ic1 = C(1.0 / (kIMPL_THERMO_WEIGHT * D.dtime * kC_D_P));
   const StateF& Mu = (rk_step == 1) ? Mo : Mn;  // state_new_used, mo_column_solvers.F90:69-73
-
-  // unscaled alpha, beta, gamma; theta of state_new_used (FP32, and FP64 without a background
-  // state, where theta * d(exner')/dz carries the whole hydrostatic balance)
-  struct Lay { float a, b, g, th, ro, iv; double thd; };
   const State& Su = (rk_step == 1) ? So : Sn;
+  // the inputs of the coefficients, from the FP32 mirror or the FP64 state and metrics
+  auto rho_o = [&](long long i) -> C { if constexpr (F64) return So.rho[goff + i]; else return Mo.rho[goff + i]; };
+  auto rt_o = [&](long long i) -> C { if constexpr (F64) return So.rt[i]; else return Mo.rt[i]; };
+  auto ep_o = [&](long long i) -> C { if constexpr (F64) return So.ep[i]; else return Mo.ep[i]; };
+  auto rho_u = [&](long long i) -> C { if constexpr (F64) return Su.rho[goff + i]; else return Mu.rho[goff + i]; };
+  auto rt_u = [&](long long i) -> C { if constexpr (F64) return Su.rt[i]; else return Mu.rt[i]; };
+  auto ep_u = [&](long long i) -> C { if constexpr (F64) return Su.ep[i]; else return Mu.ep[i]; };
+  auto w_o = [&](long long i) -> C { if constexpr (F64) return So.w[i]; else return Mo.w[i]; };
+  auto ebg = [&](long long i) -> C { if constexpr (F64) return G.exner_bg[i]; else return GF.exner_bg[i]; };
+  auto ivol = [&](long long i) -> C { if constexpr (F64) return X.inv_volume[i]; else return X.inv_volume_f[i]; };
+  auto iarz = [&](long long i) -> C { if constexpr (F64) return X.inv_area_z[i]; else return X.inv_area_z_f[i]; };
+  auto damp = [&](long long i) -> C { if constexpr (F64) return G.damp[i]; else return GF.damp[i]; };
+  // at w level jl (2..nl): z_scalar(jl-1) - z_scalar(jl) and exner_bg(jl-1) - exner_bg(jl)
+  auto dzs = [&](long long i) -> C {
+    if constexpr (F64) return G.z_scalar[i - D.plane] - G.z_scalar[i]; else return X.dzs_f[i];
+  };
+  auto debg = [&](long long i) -> C {
+    if constexpr (F64) return G.exner_bg[i - D.plane] - G.exner_bg[i]; else return X.deb_f[i];
+  };
+  auto W = [](C x) -> double { if constexpr (F64) return x; else return wide(x); };
+  auto Nr = [](double x) -> float { return narrow(x); };
+  auto quot = [](double x, C d) -> double { if constexpr (F64) return x / d; else return div_f(x, d); };
+
+  // unscaled alpha, beta, gamma; theta of state_new_used (type C, and FP64 without a background
+  // state, where theta * d(exner')/dz carries the whole hydrostatic balance)
+  struct Lay { C a, b, g, th, ro, iv; double thd; };
   auto layer = [&](int jl) -> Lay {
     const long long i = IX(D, ji, jk, jl);
     Lay L;
     L.thd = D.luse_bg ? 0.0 : Su.rt[i] / Su.rho[goff + i];
-    const float ro = Mo.rho[goff + i], rto = Mo.rt[i];
-    const float iro = 1.f / ro, irto = 1.f / rto;
+    const C ro = rho_o(i), rto = rt_o(i);
+    const C iro = C(1) / ro, irto = C(1) / rto;
     L.a = -rto * iro * iro;
     L.b = iro;
-    L.g = rdcv * irto * (GF.exner_bg[i] + Mo.ep[i]);
+    L.g = rdcv * irto * (ebg(i) + ep_o(i));
     if (rk_step == 2) {
-      const float ru = Mu.rho[goff + i], rtu = Mu.rt[i];
-      const float iru = 1.f / ru, irtu = 1.f / rtu;
-      L.a = 0.5f * (L.a - rtu * iru * iru);
-      L.b = 0.5f * (L.b + iru);
-      L.g = 0.5f * (L.g + rdcv * irtu * (GF.exner_bg[i] + Mu.ep[i]));
+      const C ru = rho_u(i), rtu = rt_u(i);
+      const C iru = C(1) / ru, irtu = C(1) / rtu;
+      L.a = C(0.5) * (L.a - rtu * iru * iru);
+      L.b = C(0.5) * (L.b + iru);
+      L.g = C(0.5) * (L.g + rdcv * irtu * (ebg(i) + ep_u(i)));
       L.th = rtu * iru;
     } else {
       L.th = rto * iro;
     }
     L.ro = ro;
-    L.iv = X.inv_volume_f[i];
+    L.iv = ivol(i);
     return L;
   };
-  // explicit predictions of theta_v' and exner' (FP64 state plus FP32 increments) and of rho_g (FP32)
-  auto predict = [&](int jl, const Lay& L, double* tpe, double* epe, float* rhe) {
+  // explicit predictions of theta_v' and exner' (FP64 state plus increments) and of rho_g
+  auto predict = [&](int jl, const Lay& L, double* tpe, double* epe, C* rhe) {
     const long long i = IX(D, ji, jk, jl);
-    const float tr = Tn.rho[goff + i], trt = Tn.rt[i];
-    *tpe = So.tp[i] + wide(dtf * (L.a * tr + L.b * trt));
-    *epe = So.ep[i] + wide(dtf * L.g * trt);
+    const C tr = C(Tn.rho[goff + i]), trt = C(Tn.rt[i]);
+    *tpe = So.tp[i] + W(dtf * (L.a * tr + L.b * trt));
+    *epe = So.ep[i] + W(dtf * L.g * trt);
     *rhe = L.ro + dtf * tr;
   };
 
-  float epr[kMaxL + 1];   // elimination multipliers (FP32)
+  C epr[kMaxL + 1];       // elimination multipliers
   double rpr[kMaxL + 1];  // substituted right-hand side, then the solution (FP64)
-  float tis[kMaxL + 1];   // interface theta
-  float gs[kMaxL + 1];    // gamma of each layer
+  C tis[kMaxL + 1];       // interface theta
+  C gs[kMaxL + 1];        // gamma of each layer
   Lay L0 = layer(1), L1 = layer(2), L2{};
   double tpe0, epe0, tpe1, epe1, tpe2 = 0.0, epe2 = 0.0;
-  float rhe0, rhe1, rhe2 = 0.f;
+  C rhe0, rhe1, rhe2 = C(0);
   predict(1, L0, &tpe0, &epe0, &rhe0);
   predict(2, L1, &tpe1, &epe1, &rhe1);
   gs[1] = L0.g;
-  float cv_prev = 0.f, epr_prev = 0.f;
+  C cv_prev = C(0), epr_prev = C(0);
   double rpr_prev = 0.0;
   for (int jl = 1; jl <= n; ++jl) {  // row jl: level jl+1 between layers jl (a) and jl+1 (b)
     const long long ib = IX(D, ji, jk, jl + 1);
     gs[jl + 1] = L1.g;
-    const float ti = 0.5f * (L0.th + L1.th);
+    const C ti = C(0.5) * (L0.th + L1.th);
     tis[jl] = ti;
-    const float irio = 2.f / (L0.ro + L1.ro);
-    const float dz = X.dzs_f[ib], deb = X.deb_f[ib], dp = GF.damp[ib];
+    const C irio = C(2) / (L0.ro + L1.ro);
+    const C dz = dzs(ib), deb = debg(ib), dp = damp(ib);
     const double wo = So.w[ib];
-    const float wof = Mo.w[ib];
-    const float al0 = L0.a * L0.iv, al1 = L1.a * L1.iv, be0 = L0.b * L0.iv, be1 = L1.b * L1.iv;
-    const float ga0 = L0.g * L0.iv, ga1 = L1.g * L1.iv;
-    const float dv = -(ti * ti) * (ga0 + ga1) + 0.5f * deb * (al1 - al0 + ti * (be1 - be0))
-                     - dz * ic2 * irio * (2.f * X.inv_area_z_f[ib] + dtf * wof * 0.5f * (L1.iv - L0.iv)) * dp;
-    const float rie = 0.5f * (rhe0 + rhe1);
+    const C wof = w_o(ib);
+    const C al0 = L0.a * L0.iv, al1 = L1.a * L1.iv, be0 = L0.b * L0.iv, be1 = L1.b * L1.iv;
+    const C ga0 = L0.g * L0.iv, ga1 = L1.g * L1.iv;
+    const C dv = -(ti * ti) * (ga0 + ga1) + C(0.5) * deb * (al1 - al0 + ti * (be1 - be0))
+                 - dz * ic2 * irio * (C(2) * iarz(ib) + dtf * wof * C(0.5) * (L1.iv - L0.iv)) * dp;
+    const C rie = C(0.5) * (rhe0 + rhe1);
     // The products of FP32 coefficients with FP64 values here and in the state update below
     // stay FP64 products of the FP32 factors: merging two FP32 factors into one rounded
     // coefficient (e.g. -dz*ic2*(1 + rie*irio) for w_old) saves two FP64 operations per cell
     // but lets an atmosphere at rest over hills drift about four times faster (1e-8 instead
     // of 3e-9 m/s of spurious wind after 3 h at 256 x 256 x 50).
-    double rv = (wo + wide(dtf * Tn.w[ib])) * wide(-dz * ic2);
-    rv = fma(D.luse_bg ? wide(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
-    rv = fma(wide(0.5f * idtf * deb), tpe0 + tpe1, rv);
-    rv = fma(wide(-dz * ic2 * rie * irio), wo, rv);
+    double rv = (wo + W(dtf * C(Tn.w[ib]))) * W(-dz * ic2);
+    rv = fma(D.luse_bg ? W(ti * idtf) : 0.5 * (L0.thd + L1.thd) * idtd, epe0 - epe1, rv);
+    rv = fma(W(C(0.5) * idtf * deb), tpe0 + tpe1, rv);
+    rv = fma(W(-dz * ic2 * rie * irio), wo, rv);
     // couplings with row jl+1 (layer b's derivatives), which need layer jl+2
-    float cv = 0.f, ev = 0.f;
+    C cv = C(0), ev = C(0);
     if (jl < n) {
       L2 = layer(jl + 2);
       predict(jl + 2, L2, &tpe2, &epe2, &rhe2);
       const long long ic = IX(D, ji, jk, jl + 2);
-      const float ti_n = 0.5f * (L1.th + L2.th);
-      const float irio_n = 2.f / (L1.ro + L2.ro);
-      cv = ti_n * ga1 * ti + 0.5f * X.deb_f[ic] * (al1 + be1 * ti)
-           - X.dzs_f[ic] * ic1 * 0.5f * Mo.w[ic] * L1.iv * irio_n * GF.damp[ic];
-      ev = ti * ga1 * ti_n - 0.5f * deb * (al1 + be1 * ti_n) + dz * ic1 * 0.5f * wof * L1.iv * irio * dp;
+      const C ti_n = C(0.5) * (L1.th + L2.th);
+      const C irio_n = C(2) / (L1.ro + L2.ro);
+      cv = ti_n * ga1 * ti + C(0.5) * debg(ic) * (al1 + be1 * ti)
+           - dzs(ic) * ic1 * C(0.5) * w_o(ic) * L1.iv * irio_n * damp(ic);
+      ev = ti * ga1 * ti_n - C(0.5) * deb * (al1 + be1 * ti_n) + dz * ic1 * C(0.5) * wof * L1.iv * irio * dp;
     }
-    const float piv = dv - epr_prev * cv_prev;
-    const double x = (jl == 1) ? rv : fma(-wide(cv_prev), rpr_prev, rv);
-    rpr_prev = div_f(x, piv);
+    const C piv = dv - epr_prev * cv_prev;
+    const double x = (jl == 1) ? rv : fma(-W(cv_prev), rpr_prev, rv);
+    rpr_prev = quot(x, piv);
     rpr[jl] = rpr_prev;
     epr_prev = ev / piv;
     epr[jl] = epr_prev;
@@ -793,7 +844,7 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
   // substitution has reached row jl-1.  The inputs of the layer above are loaded before the
   // current layer's results are stored (a store may alias a later load, which stops the
   // compiler from moving the loads itself).
-  struct StateIn { double rt, rho, ep, bg, w; float ivf, iaz, mro, trho, trt; };
+  struct StateIn { double rt, rho, ep, bg, w; C ivf, iaz, mro; float trho, trt; };
   auto state_in = [&](int m) {
     StateIn r;
     const long long p = IX(D, ji, jk, m);
@@ -802,51 +853,58 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
     r.ep = So.ep[p];
     r.bg = G.theta_v_bg[p];
     r.w = So.w[p];
-    r.ivf = X.inv_volume_f[p];
-    r.iaz = X.inv_area_z_f[p];
-    r.mro = Mo.rho[goff + p];
+    r.ivf = ivol(p);
+    r.iaz = iarz(p);
+    r.mro = rho_o(p);
     r.trho = Tn.rho[goff + p];
     r.trt = Tn.rt[p];
     return r;
   };
   StateIn in_cur = state_in(nl), in_up{}, in_below{};
-  double s1 = 0.0;        // solution at the interface below the layer (w level jl+1)
-  float rnf_below = 0.f;  // new rho_g of the layer below
+  double s1 = 0.0;     // solution at the interface below the layer (w level jl+1)
+  C rnf_below = C(0);  // new rho_g of the layer below (FP32: rounded)
   for (int jl = nl; jl >= 1; --jl) {
     if (jl > 1) in_up = state_in(jl - 1);
     const long long i = IX(D, ji, jk, jl);
     // solution of row jl-1 (w level jl), the interface above the layer
     double s0 = 0.0;
-    if (jl >= 2) s0 = (jl - 1 == n) ? rpr[n] : fma(-wide(epr[jl - 1]), s1, rpr[jl - 1]);
-    const float t0 = (jl >= 2) ? tis[jl - 1] : 0.f;
-    const float t1 = (jl <= n) ? tis[jl] : 0.f;
-    const double dtv = wide(dtf * in_cur.ivf);
+    if (jl >= 2) s0 = (jl - 1 == n) ? rpr[n] : fma(-W(epr[jl - 1]), s1, rpr[jl - 1]);
+    const C t0 = (jl >= 2) ? tis[jl - 1] : C(0);
+    const C t1 = (jl <= n) ? tis[jl] : C(0);
+    const double dtv = W(dtf * in_cur.ivf);
     const double rto = in_cur.rt;
-    const double rho_e = in_cur.rho + wide(dtf * in_cur.trho);
-    const double rt_e = rto + wide(dtf * in_cur.trt);
+    const double rho_e = in_cur.rho + W(dtf * C(in_cur.trho));
+    const double rt_e = rto + W(dtf * C(in_cur.trt));
     const double rn = fma(dtv, s1 - s0, rho_e);
-    const double rtn = fma(dtv, fma(-wide(t0), s0, wide(t1) * s1), rt_e);
-    const double epn = fma(wide(gs[jl]), rtn - rto, in_cur.ep);
-    const float rnf = narrow(rn);
-    const float tpf = narrow(fma(-in_cur.bg, rn, rtn)) / rnf;
+    const double rtn = fma(dtv, fma(-W(t0), s0, W(t1) * s1), rt_e);
+    const double epn = fma(W(gs[jl]), rtn - rto, in_cur.ep);
+    const float rnf = Nr(rn);
+    const C rnc = F64 ? C(rn) : C(rnf);
+    if constexpr (F64) {
+      const double tpn = fma(-in_cur.bg, rn, rtn) / rn;
+      Sn.tp[i] = tpn;
+      Mn.tp[i] = Nr(tpn);
+    } else {
+      const float tpf = narrow(fma(-in_cur.bg, rn, rtn)) / rnf;
+      Sn.tp[i] = wide(tpf);
+      Mn.tp[i] = tpf;
+    }
     Sn.rho[goff + i] = rn;
     Sn.rt[i] = rtn;
     Sn.ep[i] = epn;
-    Sn.tp[i] = wide(tpf);
     Mn.rho[goff + i] = rnf;
-    Mn.rt[i] = narrow(rtn);
-    Mn.ep[i] = narrow(epn);
-    Mn.tp[i] = tpf;
+    Mn.rt[i] = Nr(rtn);
+    Mn.ep[i] = Nr(epn);
     if (jl <= n) {  // w at level jl+1 from the increment there, between this layer and the one below
       const long long ib = i + D.plane;
-      const float rin = 0.5f * (rnf + rnf_below);
-      const float irio = 2.f / (in_cur.mro + in_below.mro);
-      const double wn = fma(-wide(rin), in_below.w, wide(2.f * in_below.iaz) * s1) * wide(irio);
+      const C rin = C(0.5) * (rnc + rnf_below);
+      const C irio = C(2) / (in_cur.mro + in_below.mro);
+      const double wn = fma(-W(rin), in_below.w, W(C(2) * in_below.iaz) * s1) * W(irio);
       Sn.w[ib] = wn;
-      Mn.w[ib] = narrow(wn);
+      Mn.w[ib] = Nr(wn);
     }
     s1 = s0;
-    rnf_below = rnf;
+    rnf_below = rnc;
     in_below = in_cur;
     in_cur = in_up;
   }
@@ -1196,7 +1254,7 @@ dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsig
 
 }  // namespace
 
-int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
+int split_create(const Dims& D, bool column_fp64, SplitCtx** out, long long* bytes) {
   if (D.ncons > 1 && D.ncons != kTracers + 1) {
     lgame_set_error("split precision: the tracer kernel is built for five condensates and water vapour");
     return LGAME_ERR_UNSUPPORTED;
@@ -1211,6 +1269,7 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
     return LGAME_ERR_UNSUPPORTED;
   }
   auto* s = new SplitCtx();
+  s->column_fp64 = column_fp64;
   const size_t F = (size_t)D.fstride;
   int rc = LGAME_OK;
   auto fail = [&](int code) { split_destroy(s); *out = nullptr; return code; };
@@ -1240,6 +1299,7 @@ int split_create(const Dims& D, SplitCtx** out, long long* bytes) {
   }
   SplitCarriedF& C = s->C;
   float** car[] = {&C.pgcw, &C.vsg_x, &C.vsg_y, &C.vsg_z, &C.pvt_x, &C.pvt_y, &C.pvt_z, &C.csh, &C.rad, &C.temperature,
+                   &C.hdiss,
                    &C.tend.rt, &C.tend.u, &C.tend.v, &C.tend.w, &C.pnet_u, &C.pnet_v, &C.pnet_w, &C.pold_u,
                    &C.pold_v};
   for (float** p : car) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
@@ -1420,7 +1480,8 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   float* iaz = s->gf[29];
   float* dzs = s->gf[30];
   float* deb = s->gf[31];
-  k_grid_extra<<<sgrd(D.ny, D.nx, D.NL), sblk(), 0, stream>>>(D, G, ivol, iaz, dzs, deb);
+  float* kd = s->gf[32];
+  k_grid_extra<<<sgrd(D.ny, D.nx, D.NL), sblk(), 0, stream>>>(D, G, ivol, iaz, dzs, deb, kd);
   if (cudaGetLastError() != cudaSuccess) return LGAME_ERR_CUDA;
   Grid<float>& GF = s->GF;
   float** g = s->gf;
@@ -1432,7 +1493,7 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   for (int k = 0; k < 6; ++k) GF.ipw[k] = s->ipw[k];
   for (int k = 0; k < 3; ++k) GF.trsk_u[k] = s->trsk_u[k];
   for (int k = 0; k < 2; ++k) GF.trsk_v[k] = s->trsk_v[k];
-  s->GX = GridX{s->inv_dx, s->inv_dy, s->inv_dz, s->inv_volume, s->inv_area_z, ivol, iaz, dzs, deb};
+  s->GX = GridX{s->inv_dx, s->inv_dy, s->inv_dz, s->inv_volume, s->inv_area_z, ivol, iaz, dzs, deb, kd};
   // the third-order theta chain of the background, in FP64 on temporary arrays that start at 0
   // (the levels and boundary faces the chain does not write are read as 0)
   double* tmp[4] = {};
@@ -1520,6 +1581,10 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
            C.vsg_x, C.vsg_y);
       }
     }
+    // the swamp layer's dissipative heating from state_old at the first substep
+    // (mo_vector_tend_expl.F90:100-126)
+    if (rk == 1 && D.lklemp && D.ndamp > 0)
+      SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
     SL("ks_tend_wind", ks_tend_wind, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, C, rk, Mn.u, Mn.v);
     const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (D.ncons > 1)
@@ -1534,9 +1599,12 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
        s->fv, s->gu, s->gv);
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
-       C.temperature, C.rad, C.csh, T.rho, T.rt);
+       C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt);
     const dim3 gc = cgrd(D.ny, D.nx);
-    SL("ks_column_ver", ks_column_ver, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
+    if (s->column_fp64)
+      SL("ks_column_ver", ks_column_ver<double>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
+    else
+      SL("ks_column_ver", ks_column_ver<float>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
     if (D.ncons > 1) {
       // the two tracer sets fastest (the blocks of a row tile run together), row tiles, columns
       const dim3 gt(2u, (unsigned)((D.ny + 31) / 32), (unsigned)D.nx);

@@ -26,13 +26,15 @@ struct SplitCtx;
 // diagnostic buffers of the split step that correspond to lgame_gpu.h's carried fields
 struct SplitCarriedF {
   float *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
+  float* hdiss;  // dissipative heating of the swamp layer, formed at each step's first substep
   Tend<float> tend;
   // with a background state: the net pressure-gradient terms nl + l of u, v, w and the previous
   // substep's values -(nl + l) of u, v, rounded to FP32 (the only form the wind update uses)
   float *pnet_u, *pnet_v, *pnet_w, *pold_u, *pold_v;
 };
 
-int split_create(const Dims& D, SplitCtx** out, long long* bytes);
+// column_fp64: the vertical acoustic solve with FP64 coefficients and elimination
+int split_create(const Dims& D, bool column_fp64, SplitCtx** out, long long* bytes);
 void split_destroy(SplitCtx* s);
 // builds the FP32 metric copies and the FP64 reciprocal metrics from the FP64 grid
 int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream);

@@ -80,6 +80,9 @@ def main():
     ap.add_argument("--set", action="append", default=[], metavar="KEY=VALUE")
     ap.add_argument("--twin", type=float, default=0.0, metavar="EPS",
                     help="compare FP64 with FP64 from a u wind perturbed by relative EPS")
+    ap.add_argument("--variants", default="1",
+                    help="split precision modes to compare with FP64: 1 (FP32 column-solve coefficients), "
+                         "2 (FP64 vertical acoustic solve), or 1,2")
     args = ap.parse_args()
     over = {"nx": args.nx, "ny": args.nx} if args.nx else {}
     for kv in args.set:
@@ -88,13 +91,14 @@ def main():
     n = cases.namelist(args.config, **over)
     hm = L.HostModel(n)
     models = []
-    second = L.PRECISION_FP64 if args.twin else L.PRECISION_SPLIT
-    for idx, prec in enumerate((L.PRECISION_FP64, second)):
+    others = [L.PRECISION_FP64] if args.twin else [int(v) for v in args.variants.split(",")]
+    names = {L.PRECISION_SPLIT: "split", L.PRECISION_SPLIT_FP64_COLUMN: "split_fp64_column"}
+    for idx, prec in enumerate([L.PRECISION_FP64] + others):
         cfg = L.config_from_namelist(n)
         cfg.precision = prec
         g = L.GpuModel(cfg, hm.grid)
         state = hm.state
-        if idx == 1 and args.twin:
+        if idx >= 1 and args.twin:
             state = dict(hm.state)
             r = np.random.default_rng(12345).uniform(-1.0, 1.0, size=state["wind_u"].shape)
             state["wind_u"] = np.asfortranarray(state["wind_u"] * (1.0 + args.twin * r))
@@ -114,17 +118,20 @@ def main():
             g.pchevi(step % 2, (step + 1) % 2, step)
         if step + 1 in marks:
             s64 = models[0].get_state((step + 1) % 2)
-            ssp = models[1].get_state((step + 1) % 2)
-            fin = {k: all(bool(np.isfinite(v).all()) for v in s.values()) for k, s in (("fp64", s64), ("split", ssp))}
-            line = {"config": args.config, "overrides": {k: v for k, v in over.items() if k not in ("nx", "ny")},
-                    "compare": f"fp64 twin eps={args.twin:g}" if args.twin else "split vs fp64",
-                    "nx": n.nx, "ny": n.ny, "n_layers": n.n_layers, "dtime": n.dtime,
-                    "steps": step + 1, "hours": (step + 1) * n.dtime / 3600.0, "finite": fin,
-                    "errors": field_errors(ssp, s64), "winds_fp64": winds(s64), "winds_split": winds(ssp),
-                    "wall_s": round(time.time() - t0, 1)}
-            line["worst_max"] = max(v["max"] for v in line["errors"].values())
-            print(json.dumps(line), flush=True)
-            if not all(fin.values()):
+            stop = False
+            for prec, m in zip(others, models[1:]):
+                ssp = m.get_state((step + 1) % 2)
+                fin = {k: all(bool(np.isfinite(v).all()) for v in s.values()) for k, s in (("fp64", s64), ("split", ssp))}
+                line = {"config": args.config, "overrides": {k: v for k, v in over.items() if k not in ("nx", "ny")},
+                        "compare": f"fp64 twin eps={args.twin:g}" if args.twin else f"{names[prec]} vs fp64",
+                        "nx": n.nx, "ny": n.ny, "n_layers": n.n_layers, "dtime": n.dtime,
+                        "steps": step + 1, "hours": (step + 1) * n.dtime / 3600.0, "finite": fin,
+                        "errors": field_errors(ssp, s64), "winds_fp64": winds(s64), "winds_split": winds(ssp),
+                        "wall_s": round(time.time() - t0, 1)}
+                line["worst_max"] = max(v["max"] for v in line["errors"].values())
+                print(json.dumps(line), flush=True)
+                stop = stop or not all(fin.values())
+            if stop:
                 break
 
 

@@ -20,7 +20,7 @@ LIB_PATH = _PKG / "_build" / "liblgame_gpu.so"
 # ---- status codes and enums (include/lgame_gpu.h) ------------------------------
 OK, ERR_INVALID_ARG, ERR_BAD_DIMS, ERR_BAD_CONFIG, ERR_UNSUPPORTED = 0, -1, -2, -3, -4
 ERR_ALLOC, ERR_CUDA, ERR_NONFINITE, ERR_NO_DEVICE, ERR_STATE = -5, -6, -7, -8, -9
-PRECISION_FP64, PRECISION_SPLIT = 0, 1
+PRECISION_FP64, PRECISION_SPLIT, PRECISION_SPLIT_FP64_COLUMN = 0, 1, 2
 
 GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "area_x", "area_y", "area_z",
                "area_dual_x", "area_dual_y", "area_dual_z", "z_area_dual_z", "slope_x", "slope_y",

@@ -45,6 +45,7 @@ struct oracle_ctx {
   int ncons;   /* n_constituents */
   int lmoist, lperiodic, lfreeslip, lcorio, llinear, luse_bg_state, lklemp, theta_adv_order;
   double dtime, toa, dx, dy, klemp_damp_max, klemp_begin_rel;
+  int n_damping_levels;  /* levels whose highest z_w lies above klemp_begin_rel*toa */
   /* grid */
   double *z_scalar, *z_u, *z_v, *z_w, *gdx, *gdy, *gdz, *volume, *area_x, *area_y, *area_z;
   double *area_dual_x, *area_dual_y, *area_dual_z, *z_area_dual_z, *slope_x, *slope_y, *ipw;
@@ -205,6 +206,22 @@ int oracle_set_grid(oracle_ctx* o, const double* const* f, int nfields) {
     if (!f[i]) return LGAME_ERR_INVALID_ARG;
     memcpy(dst[i], f[i], grid_size(o, i)*sizeof(double));
   }
+  /* n_damping_levels, mo_grid_generator.F90:1049-1058 */
+  o->n_damping_levels = 0;
+  for (int jl = 1; jl <= o->n_levels; ++jl) {
+    double max_z = -1e300;
+    for (size_t c = 0; c < (size_t)o->ny*o->nx; ++c) {
+      const double z = o->z_w[c + (size_t)o->ny*o->nx*(jl - 1)];
+      if (z > max_z) max_z = z;
+    }
+    if (max_z > o->klemp_begin_rel*o->toa) o->n_damping_levels = o->n_damping_levels + 1;
+  }
+  return LGAME_OK;
+}
+
+int oracle_heating_diss(const oracle_ctx* o, double* out) {
+  if (!o || !out) return LGAME_ERR_INVALID_ARG;
+  memcpy(out, o->heating_diss, (size_t)o->ny*o->nx*o->nl*sizeof(double));
   return LGAME_OK;
 }
 

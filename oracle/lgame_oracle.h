@@ -30,6 +30,8 @@ typedef struct oracle_ctx oracle_ctx;
 int  oracle_create(const lgame_config* cfg, oracle_ctx** out);
 void oracle_destroy(oracle_ctx* o);
 int  oracle_set_grid(oracle_ctx* o, const double* const* fields, int nfields);
+/* diag%heating_diss of the last step (ny,nx,nl), the dissipative heating power density */
+int  oracle_heating_diss(const oracle_ctx* o, double* out);
 int  oracle_set_state(oracle_ctx* o, int slot, const double* const* fields, int nfields);
 int  oracle_get_state(oracle_ctx* o, int slot, double* const* fields, int nfields);
 int  oracle_set_diag(oracle_ctx* o, const double* const* fields, int nfields);

@@ -52,6 +52,7 @@ def load():
             ("oracle_update_boundaries", i, [vp, i, C.c_double]),
             ("oracle_bc_state", i, [vp, C.POINTER(i), C.POINTER(i), dp]),
             ("oracle_bc_factors", i, [vp, dp, dp, dp]),
+            ("oracle_heating_diss", i, [vp, C.POINTER(C.c_double)]),
             ("oracle_output", i, [vp, i, i, C.c_double, C.c_double, C.POINTER(C.POINTER(C.c_float)), i,
                                   C.POINTER(i)]),
         ]:
@@ -146,6 +147,15 @@ class Oracle:
         dp = C.POINTER(C.c_double)
         assert self.lib.oracle_bc_factors(self.h, *[a.ctypes.data_as(dp) for a in (fs, fu, fv)]) == 0
         return fs, fu, fv
+
+    def heating_diss(self):
+        """diag%heating_diss of the last step, (ny, nx, n_layers)."""
+        ny, nx, nl = self.shapes["theta_v_pert"]
+        out = np.zeros((ny, nx, nl), order="F")
+        rc = self.lib.oracle_heating_diss(self.h, out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise RuntimeError(f"oracle_heating_diss failed: {rc}")
+        return out
 
     def budgets(self, slot):
         out = np.zeros(11)

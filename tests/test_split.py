@@ -77,3 +77,39 @@ def test_split_diag_roundtrip_and_budgets():
         np.testing.assert_array_equal(d[f], d2[f])
     b64, bsp = g64.budgets(0), gsp.budgets(0)
     np.testing.assert_allclose(bsp[:-1], b64[:-1], rtol=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", ["schaer_odd", "mountain_rest", "jet", "hills_nonperiodic"])
+def test_split_fp64_column_close_to_fp64(key):
+    """LGAME_PRECISION_SPLIT_FP64_COLUMN (the vertical acoustic solve wholly in FP64) against
+    the FP64 step, with the bars of the split mode; it must not be farther from FP64 than
+    the split mode with FP32 coefficients after ten steps."""
+    n = cases.small_case(key)
+    hm = L.HostModel(n)
+    models = []
+    for prec in (L.PRECISION_FP64, L.PRECISION_SPLIT, L.PRECISION_SPLIT_FP64_COLUMN):
+        cfg = L.config_from_namelist(n)
+        cfg.precision = prec
+        g = L.GpuModel(cfg, hm.grid)
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        models.append(g)
+    for step in range(10):
+        for g in models:
+            g.pchevi(step % 2, (step + 1) % 2, step)
+        if step not in (0, 9):
+            continue
+        b = models[0].get_state((step + 1) % 2)
+        e32 = field_errors(models[1].get_state((step + 1) % 2), b)
+        a = models[2].get_state((step + 1) % 2)
+        for f in L.STATE_FIELDS:
+            assert np.isfinite(a[f]).all(), (key, step, f)
+        e64 = field_errors(a, b)
+        bar = 1e-5 if step == 0 else 3e-5
+        assert max(e64.values()) <= bar, (key, step + 1, e64)
+        if step == 9:
+            assert max(e64.values()) <= 2.0 * max(e32.values()), (key, e64, e32)
+    for g in models:
+        g.close()
