@@ -145,6 +145,7 @@ def main():
         t_all = time.time()
         for s in range(nsteps):
             if s % steps_15 == 0:
+                g2.synchronize()  # the queued model steps are not radiation time
                 t = time.time()
                 tt = T0 + s * n.dtime
                 if kind == "emulator":
@@ -154,6 +155,7 @@ def main():
                 else:
                     xf = E.rad_features(g2, s % 2, tt)
                     E.rad_apply_heating(g2, s % 2, E.teacher(xf, nl))
+                g2.synchronize()
                 t_rad += time.time() - t
             g2.pchevi(s % 2, (s + 1) % 2, s)
         g2.synchronize()
