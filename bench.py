@@ -130,15 +130,16 @@ def _kernel_fields(ncons: int) -> dict:
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per cell of one launch of each
-# split-step kernel, averaged over its launches in one step, from the one-pass ncu launch list
-# of the full 1024x1024x80 workload summarised in profiles/split_step_jet_1024_launches.md.
-# `roofline.traffic` is this figure times the cells of the run (bytes moved per launch of the
-# dominant kernel); traffic above the algorithmic bytes is re-reads and per-thread stacks.
+# split-step kernel, averaged over its launches, from a one-pass ncu capture of the moist jet
+# at 256x256x80 (5.2 M cells, inputs about 5 GB, larger than L2, so the per-cell figures carry
+# over to 1024x1024x80).  `roofline.traffic` is this figure times the cells of the run (bytes
+# moved per launch of the dominant kernel); traffic above the algorithmic bytes is re-reads and
+# per-thread stacks.
 MEASURED_DRAM_BYTES_PER_CELL = {
-    "ks_column_tracers": 321.0, "ks_column_ver": 238.5, "ks_tracers": 102.2, "ks_pgrad": 221.9,
-    "ks_tend_wind": 112.8, "ks_gas_div": 89.2, "ks_vort_flux": 60.7, "ks_div_h": 45.3,
-    "ks_ke": 80.1, "ks_theta_edges": 48.0, "ks_gas_flux": 35.8, "ks_gzp": 41.5,
-    "ks_temperature": 27.8, "ks_csh_sum": 23.8,
+    "ks_column_tracers": 206.0, "ks_column_ver": 228.4, "ks_tracers": 98.5, "ks_pgrad": 213.6,
+    "ks_tend_wind": 109.8, "ks_gas_div": 98.7, "ks_eta": 82.9, "ks_vort_flux": 59.6, "ks_div_h": 45.0,
+    "ks_ke": 78.6, "ks_theta_edges": 44.7, "ks_gas_flux": 29.4, "ks_gzp": 36.4,
+    "ks_temperature": 25.4, "ks_csh_sum": 21.0, "ks_heating_diss": 16.1,
 }
 
 
@@ -487,8 +488,8 @@ def run_ours(args):
         "column_updates_per_s": value * n.nx * n.ny,
         "roofline": {"bound": "hbm", "kernel": prof["kernel"], "achieved": prof["achieved_gbs"],
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": prof["frac"], "traffic": prof["traffic"],
-                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum per cell, "
-                                    "profiles/split_step_jet_1024_launches.md, times the cells of this run",
+                     "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum per cell (one-pass capture "
+                                    "of the 256x256x80 jet), times the cells of this run",
                      "peak_src": peaks["src"], "avg_launch_ms": prof["avg_launch_ms"],
                      "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"]},
         "step_roofline": {"alg_bytes_per_cell": step_b, "alg_bytes_per_step": step_b * cells,
@@ -662,10 +663,67 @@ def measure_e2e(L, g, hm, args) -> dict:
         g.pchevi_host(old, new, k + 1)
     el = time.perf_counter() - t0
     link = link_rates()
+    link["numa"] = {"state_in": host_numa_pages(keep[0].data_ptr()), "state_out": host_numa_pages(keep[1].data_ptr()),
+                    "gpu_pci_node": gpu_numa_node(), "process_cpu_nodes": cpu_numa_nodes()}
     floor_ms = (h2d / link["h2d_gbs"] + d2h / link["d2h_gbs"]) / 1e6
     return {"value": k_e2e / el, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": k_e2e, "note": "lgame_gpu_pchevi_host: pinned host state in, new state out, every step",
             "ms_per_step": el / k_e2e * 1e3, "link": link, "transfer_floor_ms": floor_ms}
+
+
+def host_numa_pages(addr: int):
+    """{NUMA node: resident pages} of the mapping that holds host address `addr`, from
+    /proc/self/numa_maps (None where the kernel does not provide it)."""
+    try:
+        maps = open("/proc/self/maps").read().splitlines()
+        start = None
+        for ln in maps:
+            a, b = (int(x, 16) for x in ln.split()[0].split("-"))
+            if a <= addr < b:
+                start = a
+                break
+        if start is None:
+            return None
+        for ln in open("/proc/self/numa_maps").read().splitlines():
+            f = ln.split()
+            if int(f[0], 16) == start:
+                return {k[1:]: int(v) for k, v in (x.split("=") for x in f[1:] if x[:1] == "N" and "=" in x)}
+    except (OSError, ValueError):
+        return None
+    return None
+
+
+def gpu_numa_node():
+    """NUMA node the GPU's PCI function reports (sysfs), or None."""
+    import subprocess
+    try:
+        bus = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader", "-i",
+                              str(__import__("torch").cuda.current_device())],
+                             capture_output=True, text=True, timeout=20).stdout.strip()
+        dom, rest = bus.split(":", 1)
+        path = f"/sys/bus/pci/devices/{int(dom, 16):04x}:{rest.lower()}/numa_node"
+        return int(open(path).read().strip())
+    except (OSError, ValueError, RuntimeError, subprocess.SubprocessError):
+        return None
+
+
+def cpu_numa_nodes():
+    """NUMA nodes whose CPUs this process may run on."""
+    import glob
+    cpus = os.sched_getaffinity(0)
+    nodes = []
+    for d in sorted(glob.glob("/sys/devices/system/node/node[0-9]*")):
+        try:
+            lst = open(d + "/cpulist").read().strip()
+        except OSError:
+            continue
+        ids = set()
+        for part in filter(None, lst.split(",")):
+            a, _, b = part.partition("-")
+            ids.update(range(int(a), int(b or a) + 1))
+        if ids & cpus:
+            nodes.append(int(d.rsplit("node", 1)[1]))
+    return nodes
 
 
 def link_rates(nbytes: int = 1 << 31, reps: int = 3) -> dict:
