@@ -87,7 +87,15 @@ typedef struct lgame_config {
   int    precision;             /* LGAME_PRECISION_* */
   int    check_finite;          /* 1: scan the new state for NaN/Inf after every step */
   int    device;                /* CUDA device ordinal the context lives on          */
+  /* &diff, the diffusion closure (mo_diff_nml.F90:12-26; appended, so that the fields above
+   * keep their offsets): the horizontal coefficient scheme (the vertical one is always tke),
+   * the minimum background shear (1/s) and the Smagorinsky parameter */
+  int    diff_coeff_scheme_h;   /* LGAME_DIFF_COEFF_SMAG or LGAME_DIFF_COEFF_TKE */
+  double bg_shear, c_s;
 } lgame_config;
+
+#define LGAME_DIFF_COEFF_SMAG 0  /* diff_coeff_scheme_h = "smag" */
+#define LGAME_DIFF_COEFF_TKE  1  /* diff_coeff_scheme_h = "tke"  */
 
 /* ---- grid arrays (t_grid, src/mo_definitions.F90:29-91) --------------------
  * Extents in brackets; all double, column-major.  These are exactly the grid
@@ -123,6 +131,10 @@ enum lgame_grid_field {
   LGAME_GRID_FVEC_Z,                /* (ny+1,nx+1)     */
   LGAME_GRID_TRSK_WEIGHTS_U,        /* (3,ny)          */
   LGAME_GRID_TRSK_WEIGHTS_V,        /* (2,ny+1)        */
+  /* the metrics of the diffusion closure (mo_grid_generator.F90:1012-1031, 1060-1064) */
+  LGAME_GRID_DX_DUAL,               /* (ny+1,nx,nl)    */
+  LGAME_GRID_DY_DUAL,               /* (ny,nx+1,nl)    */
+  LGAME_GRID_LAYER_THICKNESS,       /* (ny,nx,nl)      */
   LGAME_GRID_NFIELDS
 };
 
@@ -164,6 +176,14 @@ enum lgame_diag_field {
   LGAME_DIAG_TEND_WIND_U,             /* (ny,nx+1,nl)   */
   LGAME_DIAG_TEND_WIND_V,             /* (ny+1,nx,nl)   */
   LGAME_DIAG_TEND_WIND_W,             /* (ny,nx,nl+1)   */
+  /* carried by the diffusion closure (a step's first substep reads them before it forms them
+   * anew), and the swamp layer's dissipation */
+  LGAME_DIAG_TKE,                     /* (ny,nx,nl)  specific turbulent kinetic energy (J/kg) */
+  LGAME_DIAG_VISCOSITY,               /* (ny,nx,nl)  horizontal dynamic viscosity (kg m^-1 s^-1) */
+  LGAME_DIAG_HEATING_DISS,            /* (ny,nx,nl)  dissipative heating power density (W m^-3) */
+  LGAME_DIAG_MOM_DIFF_TEND_X,         /* (ny,nx+1,nl) momentum diffusion acceleration, x  */
+  LGAME_DIAG_MOM_DIFF_TEND_Y,         /* (ny+1,nx,nl) momentum diffusion acceleration, y  */
+  LGAME_DIAG_MOM_DIFF_TEND_Z,         /* (ny,nx,nl+1) momentum diffusion acceleration, z  */
   LGAME_DIAG_NFIELDS
 };
 

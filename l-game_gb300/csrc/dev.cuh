@@ -88,6 +88,7 @@ struct Grid {
   const T *fvec_x, *fvec_y, *fvec_z;        // one plane each
   const T *trsk_u[3], *trsk_v[2];           // length P each
   const T* damp;                            // Klemp prefactor 1+damping_coeff*dtime at w points
+  const T *dx_dual, *dy_dual, *layer_thickness;  // diffusion closure: dual distances (v, u points), layers
 };
 
 // prognostic state on the device; V = double: the state proper, V = float: the FP32 mirror

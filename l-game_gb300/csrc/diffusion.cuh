@@ -1,0 +1,448 @@
+// diffusion.cuh -- the diffusion closure of the HEVI step (TKE, Smagorinsky/TKE horizontal
+// viscosity, momentum diffusion, temperature and mass diffusion), templated like kernels.cuh
+// on the type T of the metrics and the arithmetic and the type V of the state read:
+//
+//   T = double, V = double: the FP64 step (lgame_gpu.cu, -fmad=false), every expression in the
+//                           reference's operand order;
+//   T = float,  V = float:  the split step (split.cu), the same expressions in FP32 on the FP32
+//                           metric copies and the FP32 mirror of the state.
+//
+// Reference routines: update_n_squared, tke2hor/vert_diff_coeff, hor_viscosity(_smag/_tke),
+// hor_diff_coeff_postprocessing, vert_vert_mom_viscosity, scalar_diff_coeffs
+// (src/subgrid_scale/mo_eff_diff_coeffs.F90), tke_update (mo_tke.F90:19-66), mom_diff_h and
+// mom_diff_v (mo_momentum_diff_diss.F90:25-331), the diffusion part of scalar_tend_expl
+// (mo_scalar_tend_expl.F90:60-101) and add_vertical_div (mo_divergence_operators.F90:149-186).
+//
+// The reference passes these quantities through shared work arrays (scalar_placeholder,
+// u/v/w_placeholder, flux_density_*), some of whose points an operator reads without having
+// written them.  What such a point holds is fixed by the step's order of operations:
+//   - grad_vert writes w levels 2..nl only; w_placeholder's levels 1 and n_levels are written
+//     only by whole-array products of zeros (the copy of mom_diff_tend_z, whose top and bottom
+//     levels no operator writes, and the free-slip reset), so every vertical gradient below is
+//     0 at those levels;
+//   - at non-periodic boundary edges grad_hor and scalar_times_vector_h write nothing: the
+//     diffusive flux densities stay at their initial zero there, and the gradient read by
+//     tke_update's inner product holds the zero that the previous step's whole-array writers
+//     left (mom_diff_v's products with vert_hor_viscosity, which the reference never sets, or
+//     theta_v_adv_3rd_order's theta_v_u*flux_density_u); lgame_gpu_create accepts
+//     non-periodic diffusion only in those configurations;
+//   - vert_hor_mom_viscosity is never called, so vert_hor_viscosity_u/v keep their initial
+//     zeros: the vertical diffusion of u and v and the horizontal diffusion of w in mom_diff_v
+//     add exact zeros and are not evaluated.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace lg {
+
+// device buffers of the closure (T: FP64 step double, split step float)
+template <class T>
+struct DiffBuf {
+  T *tke, *tke_new;      // specific TKE (carried) and its update of this step
+  T *visc, *vmol;        // viscosity (rho * (molecular + eddy), carried) and viscosity_molecular
+  T *nsq;                // n_squared at scalar points
+  T *vz;                 // viscosity_dual * zeta_z at dual points (ny+1, nx+1, nl)
+  T *mdtx, *mdty, *mdtz; // mom_diff_tend_x/y/z (carried)
+  T *mdt, *tdh;          // mass_diff_tendency (ncons fields), temp_diff_heating
+  T* hd;                 // heating_diss (carried; formed by the dissipation kernel)
+};
+
+// run-time constants of the closure
+struct DiffPar {
+  double mva;            // mean_velocity_area, mo_grid_generator.F90:1111
+  double eff_hor_res;    // sqrt(dx*dy), mo_run_nml.F90:93
+  double c_s, bg_shear;  // Smagorinsky parameter, minimum shear
+  int tke_h;             // diff_coeff_scheme_h == "tke"
+  int mom_v;             // lmom_diff_v
+};
+
+template <class T> __device__ __forceinline__ T dsqrt(T x) { return sqrt(x); }
+template <> __device__ __forceinline__ float dsqrt<float>(float x) { return sqrtf(x); }
+
+// tke2hor_diff_coeff, mo_eff_diff_coeffs.F90:671-686.  (2*tke)**0.5: the square root, the
+// correctly rounded value of the power (the reference's pow differs from it by at most the
+// last bit in rare cases)
+template <class T>
+__device__ __forceinline__ T tke2hor(const DiffPar& P, T tke) {
+  const T mean_velocity = dsqrt<T>(T(2) * tke);
+  const T mean_free_path = T(P.eff_hor_res) / T(6);
+  return T(1.0 / 6.0) * mean_free_path * mean_velocity;
+}
+
+// tke2vert_diff_coeff, mo_eff_diff_coeffs.F90:688-713
+template <class T>
+__device__ __forceinline__ T tke2vert(T tke, T n_squared, T layer_thickness) {
+  const T tke_vert = T(3.0 * 1e-3) * tke;
+  const T mean_velocity = dsqrt<T>(T(2) * tke_vert);
+  const T n_used = dsqrt<T>(n_squared > T(1e-4) ? n_squared : T(1e-4));
+  T mean_free_path = dsqrt<T>(T(2) * tke_vert) / n_used;
+  mean_free_path = mean_free_path < layer_thickness ? mean_free_path : layer_thickness;
+  return T(1.0 / 6.0) * mean_free_path * mean_velocity;
+}
+
+// calc_diff_coeff, mo_derived.F90:189-216, in type T
+template <class T>
+__device__ __forceinline__ T diff_coeff_t(T temperature, T density) {
+  if constexpr (sizeof(T) == 8) {
+    return calc_diff_coeff(temperature, density);
+  } else {
+    const float particle_mass = float(kM_D / kN_A);
+    const float thermal_velocity = sqrtf(float(8.0 * kK_B) * temperature / float(kPI * (kM_D / kN_A)));
+    const float particle_density = density / particle_mass;
+    const float cross_section = float(4.0 * kPI * (130e-12 * 130e-12));
+    const float mean_free_path = 1.f / (1.4142135f * particle_density * cross_section);
+    return (1.f / 3.f) * thermal_velocity * mean_free_path;
+  }
+}
+
+// relative vorticity at a dual point, rel_vort (mo_vorticities.F90:181)
+template <class T, class V>
+__device__ __forceinline__ T zeta_z_at(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
+  return rel_vort_z_local<T, V>(D, G, S.u, S.v, ji, jk, jl) / G.area_dual_z[IX(D, ji, jk, jl)];
+}
+
+// divergence of the horizontal wind at a scalar point, div_h (mo_divergence_operators.F90:16-68)
+template <class T, class V>
+__device__ __forceinline__ T div_wind_at(const Dims& D, const Grid<T>& G, const StateT<V>& S, int ji, int jk, int jl) {
+  auto fx = [&](int i, int j, int k) { return T(S.u[IX(D, i, j, k)]); };
+  auto fy = [&](int i, int j, int k) { return T(S.v[IX(D, i, j, k)]); };
+  return div_h_at<T>(D, G, fx, fy, ji, jk, jl);
+}
+
+// ---- 1. update_n_squared and tke_update (first substep, any horizontal diffusion on) ----------
+// One thread per scalar point.  Reads the old TKE, viscosity and heating_diss; writes the
+// updated TKE to tke_new (the old one is still read by neighbours) and n_squared.
+template <class T, class V>
+__global__ void k_diff_tke(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B, DiffPar P) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  // update_n_squared, mo_eff_diff_coeffs.F90:620-669: g * 0.5*(1/theta(l-1) + 1/theta(l)) *
+  // dtheta/dz at w level l in 2..nl, zero at levels 1 and nl+1
+  auto nz = [&](int l) -> T {
+    if (l < 2 || l > D.nl) return T(0);
+    const long long a = IX(D, ji, jk, l - 1), b = IX(D, ji, jk, l);
+    const T th_a = G.theta_v_bg[a] + T(S.tp[a]), th_b = G.theta_v_bg[b] + T(S.tp[b]);
+    const T grad = (th_a - th_b) / G.dz[b];
+    return G.gm[b] * (T(0.5) * (T(1) / th_a + T(1) / th_b) * grad);
+  };
+  T nsq;
+  if (jl == 1) nsq = nz(1);
+  else if (jl == D.nl) nsq = nz(D.nl + 1);
+  else nsq = W_(5, ji, jk, jl) * nz(jl) + W_(6, ji, jk, jl) * nz(jl + 1);
+  B.nsq[q] = nsq;
+  // tke_update, mo_tke.F90:19-66: the inner product of the wind with grad(tke)
+  const T* tke = B.tke;
+  auto gz = [&](int i, int j, int l) -> T {  // grad_vert(tke), zero at levels 1 and nl+1
+    if (l < 2 || l > D.nl) return T(0);
+    return (tke[IX(D, i, j, l - 1)] - tke[IX(D, i, j, l)]) / G.dz[IX(D, i, j, l)];
+  };
+  auto remap_gx = [&](int i, int j, int l) -> T {  // remap_ver2hor_x of gz
+    T r = T(0);
+    if (j == 1 || j == D.nx + 1) {
+      if (!D.periodic) return r;
+      r = r + W_(5, i, D.nx, l) * gz(i, D.nx, l);
+      r = r + W_(5, i, 1, l) * gz(i, 1, l);
+      if (l < D.nl || D.freeslip) { r = r + W_(6, i, D.nx, l) * gz(i, D.nx, l + 1); r = r + W_(6, i, 1, l) * gz(i, 1, l + 1); }
+    } else {
+      r = r + W_(5, i, j - 1, l) * gz(i, j - 1, l);
+      r = r + W_(5, i, j, l) * gz(i, j, l);
+      if (l < D.nl || D.freeslip) { r = r + W_(6, i, j - 1, l) * gz(i, j - 1, l + 1); r = r + W_(6, i, j, l) * gz(i, j, l + 1); }
+    }
+    return T(0.5) * r;
+  };
+  auto remap_gy = [&](int i, int j, int l) -> T {  // remap_ver2hor_y of gz
+    T r = T(0);
+    if (i == 1 || i == D.ny + 1) {
+      if (!D.periodic) return r;
+      r = r + W_(5, D.ny, j, l) * gz(D.ny, j, l);
+      r = r + W_(5, 1, j, l) * gz(1, j, l);
+      if (l < D.nl || D.freeslip) { r = r + W_(6, D.ny, j, l) * gz(D.ny, j, l + 1); r = r + W_(6, 1, j, l) * gz(1, j, l + 1); }
+    } else {
+      r = r + W_(5, i - 1, j, l) * gz(i - 1, j, l);
+      r = r + W_(5, i, j, l) * gz(i, j, l);
+      if (l < D.nl || D.freeslip) { r = r + W_(6, i - 1, j, l) * gz(i - 1, j, l + 1); r = r + W_(6, i, j, l) * gz(i, j, l + 1); }
+    }
+    return T(0.5) * r;
+  };
+  auto gx = [&](int i, int j, int l) -> T {  // grad_hor x at a u point; non-periodic boundary: 0
+    T r;
+    if (!grad_x_cov<T, T>(D, G, tke, i, j, l, &r)) return T(0);
+    if (l > D.nf) r = r - G.slope_x[IX(D, i, j, l)] * remap_gx(i, j, l);
+    return r;
+  };
+  auto gy = [&](int i, int j, int l) -> T {
+    T r;
+    if (!grad_y_cov<T, T>(D, G, tke, i, j, l, &r)) return T(0);
+    if (l > D.nf) r = r - G.slope_y[IX(D, i, j, l)] * remap_gy(i, j, l);
+    return r;
+  };
+  const T adv = W_(1, ji, jk, jl) * T(S.u[IX(D, ji, jk + 1, jl)]) * gx(ji, jk + 1, jl)
+              + W_(2, ji, jk, jl) * T(S.v[q]) * gy(ji, jk, jl)
+              + W_(3, ji, jk, jl) * T(S.u[q]) * gx(ji, jk, jl)
+              + W_(4, ji, jk, jl) * T(S.v[IX(D, ji + 1, jk, jl)]) * gy(ji + 1, jk, jl)
+              + W_(5, ji, jk, jl) * T(S.w[q]) * gz(ji, jk, jl)
+              + W_(6, ji, jk, jl) * T(S.w[q + D.plane]) * gz(ji, jk, jl + 1);
+  const T rg = T(S.rho[q + (long long)(D.g - 1) * D.fstride]);
+  const T decay_constant = T(8.0 * (kPI * kPI)) / T(P.mva) * B.visc[q] / rg;
+  T t = tke[q] + T(D.dtime) * (-adv + B.hd[q] / rg - decay_constant * tke[q]);
+  if (t < T(0)) t = T(0);
+  B.tke_new[q] = t;
+}
+
+// ---- 2. hor_viscosity (mo_eff_diff_coeffs.F90:24-159) -------------------------------------
+// One thread per scalar point: viscosity_molecular, the eddy viscosity (Smagorinsky from the
+// vorticity averaged to the cell and the divergence of the wind, or from the updated TKE), their
+// sum times the gas density.  Also moves the updated TKE into place.
+template <class T, class V>
+__global__ void k_diff_visc(Dims D, Grid<T> G, StateT<V> S, const T* Tm, DiffBuf<T> B, DiffPar P) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  const T rg = T(S.rho[q + (long long)(D.g - 1) * D.fstride]);
+  const T tke = B.tke_new[q];
+  const T vmol = diff_coeff_t<T>(Tm[q], rg);
+  T eddy;
+  if (P.tke_h) {
+    eddy = tke2hor<T>(P, tke);
+  } else {
+    const T vac = T(0.25) * (zeta_z_at<T, V>(D, G, S, ji, jk, jl) + zeta_z_at<T, V>(D, G, S, ji, jk + 1, jl)
+                           + zeta_z_at<T, V>(D, G, S, ji + 1, jk, jl) + zeta_z_at<T, V>(D, G, S, ji + 1, jk + 1, jl));
+    const T dv = div_wind_at<T, V>(D, G, S, ji, jk, jl);
+    const T a = vac * vac + dv * dv, b = T(P.bg_shear) * T(P.bg_shear);
+    eddy = T(P.c_s) * T(P.mva) * dsqrt<T>(a > b ? a : b);
+  }
+  B.vmol[q] = vmol;
+  B.visc[q] = rg * (vmol + eddy);
+  B.tke[q] = tke;
+}
+
+// ---- 3. hor_diff_coeff_postprocessing (mo_eff_diff_coeffs.F90:161-310) and rel_vort ----------
+// One thread per dual point (ny+1, nx+1, nl): viscosity_dual (the molecular pass the reference
+// makes first is overwritten by the turbulent one, which already holds both parts) times
+// zeta_z, the product mom_diff_h differentiates.  Non-periodic boundary dual points keep the
+// initial zero of viscosity_dual.
+template <class T, class V>
+__global__ void k_diff_vz(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
+  LG_IDX3;
+  if (ji > D.ny + 1 || jk > D.nx + 1) return;
+  const long long q = IX(D, ji, jk, jl);
+  const T* v = B.visc;
+  const V* rg = S.rho + (long long)(D.g - 1) * D.fstride;
+  auto vs = [&](int i, int j) { return v[IX(D, i, j, jl)]; };
+  auto rs = [&](int i, int j) { return T(rg[IX(D, i, j, jl)]); };
+  const bool in_i = ji >= 2 && ji <= D.ny, in_k = jk >= 2 && jk <= D.nx;
+  T vd = T(0);
+  if (in_i && in_k) {
+    vd = T(0.25) * (vs(ji - 1, jk - 1) + vs(ji - 1, jk) + vs(ji, jk - 1) + vs(ji, jk));
+    vd = T(0.25) * (rs(ji - 1, jk - 1) + rs(ji - 1, jk) + rs(ji, jk - 1) + rs(ji, jk)) * vd;
+  } else if (D.periodic) {
+    if (in_k) {  // ji = 1 or ny+1 (the copy of 1)
+      vd = T(0.25) * (vs(1, jk - 1) + vs(D.ny, jk - 1) + vs(1, jk) + vs(D.ny, jk));
+      vd = vd * (T(0.25) * (rs(1, jk - 1) + rs(D.ny, jk - 1) + rs(1, jk) + rs(D.ny, jk)));
+    } else if (in_i) {  // jk = 1 or nx+1
+      vd = T(0.25) * (vs(ji - 1, D.nx) + vs(ji - 1, 1) + vs(ji, D.nx) + vs(ji, 1));
+      vd = vd * (T(0.25) * (rs(ji - 1, D.nx) + rs(ji - 1, 1) + rs(ji, D.nx) + rs(ji, 1)));
+    } else {  // corners
+      vd = T(0.25) * (vs(1, 1) + vs(D.ny, 1) + vs(1, D.nx) + vs(D.ny, D.nx));
+      vd = vd * (T(0.25) * (rs(D.ny, D.nx) + rs(D.ny, 1) + rs(1, D.nx) + rs(1, 1)));
+    }
+  }
+  B.vz[q] = vd * zeta_z_at<T, V>(D, G, S, ji, jk, jl);
+}
+
+// ---- 4. mom_diff_h (mo_momentum_diff_diss.F90:25-160) ----------------------------------------
+// u and v points: the gradient of viscosity*divergence (grad_hor, whose terrain correction
+// reads mom_diff_tend_z as the previous step left it: the reference passes that array as
+// grad_hor's vertical component without forming it first), plus the curl of viscosity_dual *
+// zeta_z with its terrain-following correction, divided by the averaged density.  The thread
+// of jk = 1 (ji = 1) also writes the copy at nx+1 (ny+1); at non-periodic boundary edges the
+// reference keeps the previous value (less slope times a zero remap).
+template <class T, class V>
+__global__ void k_mom_diff_h(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
+  LG_IDX3;
+  auto sdiv = [&](int i, int j, int l) { return B.visc[IX(D, i, j, l)] * div_wind_at<T, V>(D, G, S, i, j, l); };
+  auto rsum = [&](int i, int j, int l) { return rho_sum_cond_gas<T, V>(D, S.rho, IX(D, i, j, l)); };
+  const T* vz = B.vz;
+  const T* zd = G.z_area_dual_z;
+  const int ui = jl - 1 > 1 ? jl - 1 : 1, li = jl + 1 < D.nl ? jl + 1 : D.nl;
+  // u points
+  if (ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    const bool inner = jk >= 2;
+    T r;
+    if (inner || D.periodic) {
+      const int kk = jk;  // jk = 1 evaluates the periodic formula; nx+1 is its copy
+      const int ka = inner ? jk - 1 : D.nx;
+      r = (sdiv(ji, kk, jl) - sdiv(ji, ka, jl)) / G.dx[IX(D, ji, kk, jl)];
+      if (jl > D.nf) r = r - G.slope_x[q] * remap_x<T, T>(D, G, B.mdtz, ji, kk, jl);
+      const T dyd = G.dy_dual[q];
+      T up = (vz[IX(D, ji + 1, kk, jl)] - vz[IX(D, ji, kk, jl)]) / dyd;
+      const T slope = (zd[IX(D, ji + 1, kk, jl)] - zd[IX(D, ji, kk, jl)]) / dyd;
+      const T vg = T(0.5) * (vz[IX(D, ji + 1, kk, ui)] - vz[IX(D, ji + 1, kk, li)])
+                     / (zd[IX(D, ji + 1, kk, ui)] - zd[IX(D, ji + 1, kk, li)])
+                 + T(0.5) * (vz[IX(D, ji, kk, ui)] - vz[IX(D, ji, kk, li)])
+                     / (zd[IX(D, ji, kk, ui)] - zd[IX(D, ji, kk, li)]);
+      up = up - slope * vg;
+      r = (r + up) / (T(0.5) * (rsum(ji, ka, jl) + rsum(ji, kk, jl)));
+    } else {
+      r = B.mdtx[q];
+      if (jl > D.nf) r = r - G.slope_x[q] * T(0);
+    }
+    B.mdtx[q] = r;
+    if (jk == 1) B.mdtx[IX(D, ji, D.nx + 1, jl)] = r;
+  }
+  // v points
+  if (ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    const bool inner = ji >= 2;
+    T r;
+    if (inner || D.periodic) {
+      const int ia = inner ? ji - 1 : D.ny;
+      r = (sdiv(ia, jk, jl) - sdiv(ji, jk, jl)) / G.dy[q];
+      if (jl > D.nf) r = r - G.slope_y[q] * remap_y<T, T>(D, G, B.mdtz, ji, jk, jl);
+      const T dxd = G.dx_dual[q];
+      T vp = (vz[IX(D, ji, jk + 1, jl)] - vz[q]) / dxd;
+      const T slope = (zd[IX(D, ji, jk + 1, jl)] - zd[q]) / dxd;
+      const T vg = T(0.5) * (vz[IX(D, ji, jk + 1, ui)] - vz[IX(D, ji, jk + 1, li)])
+                     / (zd[IX(D, ji, jk + 1, ui)] - zd[IX(D, ji, jk + 1, li)])
+                 + T(0.5) * (vz[IX(D, ji, jk, ui)] - vz[IX(D, ji, jk, li)])
+                     / (zd[IX(D, ji, jk, ui)] - zd[IX(D, ji, jk, li)]);
+      vp = vp - slope * vg;
+      r = (r + vp) / (T(0.5) * (rsum(ia, jk, jl) + rsum(ji, jk, jl)));
+    } else {
+      r = B.mdty[q];
+      if (jl > D.nf) r = r - G.slope_y[q] * T(0);
+    }
+    B.mdty[q] = r;
+    if (ji == 1) B.mdty[IX(D, D.ny + 1, jk, jl)] = r;
+  }
+}
+
+// ---- 5. mom_diff_v, vertical diffusion of w (mo_momentum_diff_diss.F90:277-329) -----------------
+// w levels 2..nl: grad_vert of rho_g * (viscosity_molecular + the TKE's vertical coefficient) *
+// add_vertical_div(w), divided by the averaged density (the horizontal diffusion of w in
+// between adds zeros).  Levels 1 and nl+1 are not written.
+template <class T, class V>
+__global__ void k_mom_diff_v(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
+  const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  const int jk = blockIdx.z * blockDim.y + threadIdx.y + 1;
+  const int jl = blockIdx.y + 2;
+  if (ji > D.ny || jk > D.nx || jl > D.nl) return;
+  auto sp = [&](int l) -> T {
+    const long long p = IX(D, ji, jk, l);
+    const T cu = (l == 1) ? T(0) : T(S.w[p]);
+    const T cl = (l == D.nl) ? T(0) : T(S.w[p + D.plane]);
+    const T comp_v = cu * G.area_z[p] - cl * G.area_z[p + D.plane];
+    const T dwdz = T(0) + comp_v / G.volume[p];
+    const T coeff = B.vmol[p] + tke2vert<T>(B.tke[p], B.nsq[p], G.layer_thickness[p]);
+    return T(S.rho[p + (long long)(D.g - 1) * D.fstride]) * coeff * dwdz;
+  };
+  const long long q = IX(D, ji, jk, jl);
+  T m = (sp(jl - 1) - sp(jl)) / G.dz[q];
+  m = m / (T(0.5) * (rho_sum_cond_gas<T, V>(D, S.rho, q - D.plane) + rho_sum_cond_gas<T, V>(D, S.rho, q)));
+  B.mdtz[q] = m;
+}
+
+// ---- 6. simple_dissipation_rate (mo_momentum_diff_diss.F90:333-389) ------------------------------
+// One thread per scalar point: the inner product of the wind with the momentum diffusion
+// acceleration, whose w part carries the Klemp swamp layer's deceleration at w levels
+// 2..n_damping_levels (damping_prefactor = damp, the column solver's prefactor), times
+// -sum(rho(1:nc+1)).
+// kdamp (split step, may be null): (1/damping_prefactor - 1)/dtime formed in FP64 per w point,
+// so that the deceleration is w*kdamp without the cancellation of w/p - w in FP32
+template <class T, class V>
+__global__ void k_diss_rate(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B, const T* damp, const T* kdamp) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl), b = q + D.plane;
+  auto wp = [&](long long p, int lev) -> T {
+    T x = B.mdtz[p];
+    if (D.lklemp && lev >= 2 && lev <= D.ndamp) {
+      const T w = T(S.w[p]);
+      x = x + (kdamp ? w * kdamp[p] : (w / damp[p] - w) / T(D.dtime));
+    }
+    return x;
+  };
+  const long long qu = IX(D, ji, jk + 1, jl), qv = IX(D, ji + 1, jk, jl);
+  const T ip = W_(1, ji, jk, jl) * T(S.u[qu]) * B.mdtx[qu] + W_(2, ji, jk, jl) * T(S.v[q]) * B.mdty[q]
+             + W_(3, ji, jk, jl) * T(S.u[q]) * B.mdtx[q] + W_(4, ji, jk, jl) * T(S.v[qv]) * B.mdty[qv]
+             + W_(5, ji, jk, jl) * T(S.w[q]) * wp(q, jl) + W_(6, ji, jk, jl) * T(S.w[b]) * wp(b, jl + 1);
+  B.hd[q] = -rho_sum_cond_gas<T, V>(D, S.rho, q) * ip;
+}
+
+// ---- 7. temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101) ----------------------------
+// The effective coefficients of scalar_diff_coeffs (mo_eff_diff_coeffs.F90:526-618) at a scalar
+// point: horizontal and vertical, for mass (kind 0) and temperature (kind 1).  The specific
+// heat c_g_v of spec_heat_cap_diagnostics_v (mo_derived.F90:40-68) is rho_g/rho_g*c_d_v.
+template <class T, class V>
+__device__ __forceinline__ T diff_coeff_h(const Dims& D, const StateT<V>& S, const DiffBuf<T>& B, int kind, long long p) {
+  const T rg = T(S.rho[p + (long long)(D.g - 1) * D.fstride]);
+  if (kind == 0) return B.visc[p] / rg;
+  const T c_g_v = T(0) + rg / rg * T(kC_D_V);
+  return c_g_v * B.visc[p];
+}
+template <class T, class V>
+__device__ __forceinline__ T diff_coeff_v(const Dims& D, const Grid<T>& G, const StateT<V>& S, const DiffBuf<T>& B,
+                                          int kind, long long p) {
+  const T t2v = B.vmol[p] + tke2vert<T>(B.tke[p], B.nsq[p], G.layer_thickness[p]);
+  if (kind == 0) return t2v;
+  const T rg = T(S.rho[p + (long long)(D.g - 1) * D.fstride]);
+  const T c_g_v = T(0) + rg / rg * T(kC_D_V);
+  return rg * c_g_v * t2v;
+}
+
+// diffusive flux densities of the scalar s (grad_hor with gz = grad_vert(s) as its vertical
+// component, zero at levels 1 and nl+1; then scalar_times_vector_h/_v with the coefficients):
+// fx, fy at u and v points (zero at non-periodic boundary edges, which the reference never
+// writes), fw at w levels 2..nl (only when the vertical diffusion is on)
+template <class T, class V, class SF>
+__global__ void k_diff_flux(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B, const SF* s, const T* gz, int kind,
+                            int vertical, T* fx, T* fy, T* fw) {
+  LG_IDX3;
+  auto ch = [&](int i, int j) { return diff_coeff_h<T, V>(D, S, B, kind, IX(D, i, j, jl)); };
+  if (ji <= D.ny && jk <= D.nx + 1) {
+    const long long q = IX(D, ji, jk, jl);
+    T f = T(0), g;
+    if (grad_x_cov<T, SF>(D, G, s, ji, jk, jl, &g)) {
+      if (jl > D.nf) g = g - G.slope_x[q] * remap_x<T, T>(D, G, gz, ji, jk, jl);
+      if (jk >= 2 && jk <= D.nx) f = T(0.5) * (ch(ji, jk - 1) + ch(ji, jk)) * g;
+      else f = T(0.5) * (ch(ji, 1) + ch(ji, D.nx)) * g;
+    }
+    fx[q] = f;
+  }
+  if (ji <= D.ny + 1 && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    T f = T(0), g;
+    if (grad_y_cov<T, SF>(D, G, s, ji, jk, jl, &g)) {
+      if (jl > D.nf) g = g - G.slope_y[q] * remap_y<T, T>(D, G, gz, ji, jk, jl);
+      if (ji >= 2 && ji <= D.ny) f = T(0.5) * (ch(ji - 1, jk) + ch(ji, jk)) * g;
+      else f = T(0.5) * (ch(1, jk) + ch(D.ny, jk)) * g;
+    }
+    fy[q] = f;
+  }
+  if (vertical && jl >= 2 && ji <= D.ny && jk <= D.nx) {
+    const long long q = IX(D, ji, jk, jl);
+    fw[q] = T(0.5) * (diff_coeff_v<T, V>(D, G, S, B, kind, q - D.plane) + diff_coeff_v<T, V>(D, G, S, B, kind, q)) * gz[q];
+  }
+}
+
+// div_h of the flux densities plus, with the vertical diffusion on, add_vertical_div of fw
+template <class T>
+__global__ void k_diff_div(Dims D, Grid<T> G, const T* fx, const T* fy, const T* fw, int vertical, T* out) {
+  LG_IDX3;
+  if (ji > D.ny || jk > D.nx) return;
+  const long long q = IX(D, ji, jk, jl);
+  auto ax = [&](int i, int j, int k) { return fx[IX(D, i, j, k)]; };
+  auto ay = [&](int i, int j, int k) { return fy[IX(D, i, j, k)]; };
+  T r = div_h_at<T>(D, G, ax, ay, ji, jk, jl);
+  if (vertical) {
+    const T cu = (jl == 1) ? T(0) : fw[q];
+    const T cl = (jl == D.nl) ? T(0) : fw[q + D.plane];
+    const T comp_v = cu * G.area_z[q] - cl * G.area_z[q + D.plane];
+    r = r + comp_v / G.volume[q];
+  }
+  out[q] = r;
+}
+
+}  // namespace lg

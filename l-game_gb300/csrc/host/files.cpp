@@ -4,7 +4,7 @@
 // Every file is a 64-byte header followed by FP64 arrays in the reference's layout
 // (column-major, reference extents), all little-endian:
 //   bytes 0-7    magic, "LGAMESNP" (snapshot) or "LGAMEBCL" (boundary level)
-//   bytes 8-11   int32 format version (1)
+//   bytes 8-11   int32 format version (2: the diagnostics of the diffusion closure appended)
 //   bytes 12-27  int32 ny, nx, n_layers, n_constituents
 //   bytes 28-35  int64 step counter (snapshot) or the valid time in seconds as FP64 (level)
 //   bytes 36-63  zero
@@ -27,7 +27,7 @@
 
 namespace {
 
-constexpr int kVersion = 1;
+constexpr int kVersion = 2;
 
 struct Header {
   char magic[8];
@@ -62,11 +62,13 @@ size_t diag_n(int f, int ny, int nx, int nl, int ncons) {
                w = (size_t)ny * nx * (nl + 1);
   switch (f) {
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_U: case LGAME_DIAG_P_GRAD_ACC_NEG_L_U: case LGAME_DIAG_P_GRAD_ACC_OLD_U:
-    case LGAME_DIAG_POT_VORT_TEND_X: case LGAME_DIAG_V_SQUARED_GRAD_X: case LGAME_DIAG_TEND_WIND_U: return u;
+    case LGAME_DIAG_POT_VORT_TEND_X: case LGAME_DIAG_V_SQUARED_GRAD_X: case LGAME_DIAG_TEND_WIND_U:
+    case LGAME_DIAG_MOM_DIFF_TEND_X: return u;
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_V: case LGAME_DIAG_P_GRAD_ACC_NEG_L_V: case LGAME_DIAG_P_GRAD_ACC_OLD_V:
-    case LGAME_DIAG_POT_VORT_TEND_Y: case LGAME_DIAG_V_SQUARED_GRAD_Y: case LGAME_DIAG_TEND_WIND_V: return v;
+    case LGAME_DIAG_POT_VORT_TEND_Y: case LGAME_DIAG_V_SQUARED_GRAD_Y: case LGAME_DIAG_TEND_WIND_V:
+    case LGAME_DIAG_MOM_DIFF_TEND_Y: return v;
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: case LGAME_DIAG_POT_VORT_TEND_Z:
-    case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: return w;
+    case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: case LGAME_DIAG_MOM_DIFF_TEND_Z: return w;
     case LGAME_DIAG_TEND_RHO: return s * ncons;
     default: return s;
   }

@@ -373,5 +373,7 @@ extern "C" int lgame_config_from_namelist(const lgame_namelist* n, lgame_config*
   c->lsfc_phase_trans = n->lsfc_phase_trans; c->lpbl = n->lpbl;
   c->lperiodic = n->lperiodic; c->lfreeslip = n->lfreeslip;
   c->precision = n->precision; c->check_finite = n->check_finite;
+  c->diff_coeff_scheme_h = (trim(n->diff_coeff_scheme_h) == "tke") ? LGAME_DIFF_COEFF_TKE : LGAME_DIFF_COEFF_SMAG;
+  c->bg_shear = n->bg_shear; c->c_s = n->c_s;
   return LGAME_OK;
 }

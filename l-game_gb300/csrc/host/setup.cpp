@@ -69,7 +69,7 @@ struct lgame_host_model {
   Vec z_scalar, oro, oro_smoothed, dx, dy, dz, z_u, z_v, z_w, gravity_potential, gravity_m_v, volume;
   Vec area_x, area_y, area_z, slope_x, slope_y, ipw, area_dual_x, area_dual_y, area_dual_z, z_area_dual_z;
   Vec fvec_x, fvec_y, fvec_z, trsk_u, trsk_v, exner_bg_grad_u, exner_bg_grad_v, exner_bg_grad_w;
-  Vec theta_v_bg, exner_bg, sfc_albedo;
+  Vec theta_v_bg, exner_bg, sfc_albedo, dx_dual, dy_dual, layer_thickness;
   // state
   Vec rho, rhotheta_v, theta_v_pert, exner_pert, wind_u, wind_v, wind_w;
   // carried diagnostics (only the ones the set-up writes; the rest start at zero)
@@ -489,6 +489,19 @@ int grid_setup(M& m) {
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny + 1; ++ji)
         m.dy[m.IV(ji, jk, jl)] = n.lplane ? n.dy : n.dy * (r_e + m.z_v[m.IV(ji, jk, jl)]) / r_e;
+  // dx_dual, dy_dual, :1012-1032
+#pragma omp parallel for schedule(static)
+  for (int jl = 1; jl <= nl; ++jl)
+    for (int jk = 1; jk <= nx; ++jk)
+      for (int ji = 1; ji <= ny + 1; ++ji) {
+        const double lat = (ji == ny + 1) ? m.lat_scalar[ji - 2] - 0.5 * dlat : m.lat_scalar[ji - 1] + 0.5 * dlat;
+        m.dx_dual[m.IV(ji, jk, jl)] = n.lplane ? n.dx : n.dx * std::cos(lat) * (r_e + m.z_v[m.IV(ji, jk, jl)]) / r_e;
+      }
+#pragma omp parallel for schedule(static)
+  for (int jl = 1; jl <= nl; ++jl)
+    for (int jk = 1; jk <= nx + 1; ++jk)
+      for (int ji = 1; ji <= ny; ++ji)
+        m.dy_dual[m.IU(ji, jk, jl)] = n.lplane ? n.dy : n.dy * (r_e + m.z_u[m.IU(ji, jk, jl)]) / r_e;
   // slopes, :1036
   grad_hor_cov(m, m.z_scalar, m.slope_x, m.slope_y);
   // z_w, :1039-1047
@@ -497,6 +510,12 @@ int grid_setup(M& m) {
     for (int jk = 1; jk <= nx; ++jk)
       for (int ji = 1; ji <= ny; ++ji)
         m.z_w[m.IS(ji, jk, jl)] = (jl == 1) ? n.toa : 0.5 * (m.z_scalar[m.IS(ji, jk, jl - 1)] + m.z_scalar[m.IS(ji, jk, jl)]);
+  // layer thicknesses, :1060-1064
+#pragma omp parallel for schedule(static)
+  for (int jl = 1; jl <= nl; ++jl)
+    for (int jk = 1; jk <= nx; ++jk)
+      for (int ji = 1; ji <= ny; ++ji)
+        m.layer_thickness[m.IS(ji, jk, jl)] = m.z_w[m.IS(ji, jk, jl)] - m.z_w[m.IS(ji, jk, jl + 1)];
   // dz, :1068-1078
 #pragma omp parallel for schedule(static)
   for (int jl = 1; jl <= NL; ++jl)
@@ -954,11 +973,12 @@ extern "C" int lgame_host_setup(const lgame_namelist* nml, lgame_host_model** ou
   m->trsk_u.assign(3 * ny, 0); m->trsk_v.assign(2 * (ny + 1), 0);
   m->exner_bg_grad_u.assign(nU, 0); m->exner_bg_grad_v.assign(nV, 0); m->exner_bg_grad_w.assign(nW, 0);
   m->theta_v_bg.assign(nS, 0); m->exner_bg.assign(nS, 0); m->sfc_albedo.assign(ny * nx, 0);
+  m->dx_dual.assign(nV, 0); m->dy_dual.assign(nU, 0); m->layer_thickness.assign(nS, 0);
   const int ncons = nml->n_constituents;
   m->rho.assign(nS * ncons, 0); m->rhotheta_v.assign(nS, 0); m->theta_v_pert.assign(nS, 0);
   m->exner_pert.assign(nS, 0); m->wind_u.assign(nU, 0); m->wind_v.assign(nV, 0); m->wind_w.assign(nW, 0);
   const size_t dsz[LGAME_DIAG_NFIELDS] = {nU, nV, nW, nU, nV, nW, nU, nV, nU, nV, nW, nU, nV, nW, nS, nS, nS,
-                                          nS * ncons, nS, nU, nV, nW};
+                                          nS * ncons, nS, nU, nV, nW, nS, nS, nS, nU, nV, nW};
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f) m->diag[f].assign(dsz[f], 0.0);
   int rc = grid_setup(*m);
   if (rc == LGAME_OK) rc = bg_setup(*m);
@@ -1004,6 +1024,9 @@ extern "C" double* lgame_host_grid_field(lgame_host_model* m, int f, size_t* n) 
     case LGAME_GRID_FVEC_Z: v = &m->fvec_z; break;
     case LGAME_GRID_TRSK_WEIGHTS_U: v = &m->trsk_u; break;
     case LGAME_GRID_TRSK_WEIGHTS_V: v = &m->trsk_v; break;
+    case LGAME_GRID_DX_DUAL: v = &m->dx_dual; break;
+    case LGAME_GRID_DY_DUAL: v = &m->dy_dual; break;
+    case LGAME_GRID_LAYER_THICKNESS: v = &m->layer_thickness; break;
     default: return nullptr;
   }
   if (n) *n = v->size();

@@ -28,6 +28,7 @@ template <class T>
 struct Carried {  // read-only view of the diagnostics combined into the wind tendency
   const double *nl_u, *nl_v, *nl_w, *l_u, *l_v, *l_w, *old_u, *old_v;
   const T *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z;
+  const T *mdt_x = nullptr, *mdt_y = nullptr, *mdt_z = nullptr;  // momentum diffusion (null: off)
 };
 
 // ---- edge operators with the reference's boundary branches --------------------
@@ -611,7 +612,9 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
   };
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
-    const T t = old_weight * Tn.u[q] + new_weight * (pg_h(C.old_u, C.nl_u, C.l_u, q) - T(0.5) * C.vsg_x[q] + C.pvt_x[q]);
+    T f = pg_h(C.old_u, C.nl_u, C.l_u, q) - T(0.5) * C.vsg_x[q] + C.pvt_x[q];
+    if (C.mdt_x) f = f + C.mdt_x[q];
+    const T t = old_weight * Tn.u[q] + new_weight * f;
     Tn.u[q] = t;
     const double un = So.u[q] + D.dtime * cvt<double>(t);
     Sn.u[q] = un;
@@ -619,7 +622,9 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    const T t = old_weight * Tn.v[q] + new_weight * (pg_h(C.old_v, C.nl_v, C.l_v, q) - T(0.5) * C.vsg_y[q] + C.pvt_y[q]);
+    T f = pg_h(C.old_v, C.nl_v, C.l_v, q) - T(0.5) * C.vsg_y[q] + C.pvt_y[q];
+    if (C.mdt_y) f = f + C.mdt_y[q];
+    const T t = old_weight * Tn.v[q] + new_weight * f;
     Tn.v[q] = t;
     const double vn = So.v[q] + D.dtime * cvt<double>(t);
     Sn.v[q] = vn;
@@ -630,7 +635,9 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
     T pg;
     if (pg32) pg = -(T(cvw_d) * cvt<T>(C.nl_w[q] + C.l_w[q]));
     else pg = cvt<T>(-(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q]);
-    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (pg - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+    T f = pg - T(0.5) * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q];
+    if (C.mdt_z) f = f + C.mdt_z[q];
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * f;
   }
 }
 
@@ -639,7 +646,7 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
 // (mo_divergence_operators.F90:70-147) evaluated inline.
 template <class T, class V = double>
 __device__ __forceinline__ void tracers_body(const Dims& D, const Grid<T>& G, const StateT<V>& Ss, const V* u_new,
-                                             const V* v_new, T* t_rho, int rk_step) {
+                                             const V* v_new, T* t_rho, int rk_step, const T* mdt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -675,20 +682,23 @@ __device__ __forceinline__ void tracers_body(const Dims& D, const Grid<T>& G, co
     }
     const T div = (comp_h + comp_v) / G.volume[q];
     T* t = t_rho + (long long)(jc - 1) * D.fstride;
-    t[q] = old_weight * t[q] + new_weight * (-div);
+    T f = -div;
+    if (mdt) f = f + mdt[q + (long long)(jc - 1) * D.fstride];  // mass diffusion (phase transitions: 0)
+    t[q] = old_weight * t[q] + new_weight * f;
   }
 }
 
 template <class T, class V = double>
-__global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, T* t_rho, int rk_step) {
-  tracers_body<T, V>(D, G, Ss, u_new, v_new, t_rho, rk_step);
+__global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, T* t_rho, int rk_step,
+                          const T* mdt) {
+  tracers_body<T, V>(D, G, Ss, u_new, v_new, t_rho, rk_step, mdt);
 }
 
 // scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177
 template <class T, class V = double>
 __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, const T* tvu,
                             const T* tvv, const T* Tm, const T* hd, const T* rad, const T* csh, T* t_rho,
-                            T* t_rt) {
+                            T* t_rt, const T* mdt, const T* tdh) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -696,7 +706,9 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
   auto fx = [&](int i, int j, int k) { T f; return stv_h_x<T>(D, rg, u_new, i, j, k, &f) ? f : T(0); };
   auto fy = [&](int i, int j, int k) { T f; return stv_h_y<T>(D, rg, v_new, i, j, k, &f) ? f : T(0); };
   const T div_m = div_h_at<T>(D, G, fx, fy, ji, jk, jl);
-  t_rho[q + (long long)(D.g - 1) * D.fstride] = -div_m;  // old_weight 0, new_weight 1 for the gas
+  // old_weight 0, new_weight 1 for the gas; mass diffusion (null: off)
+  const T mdg = mdt ? mdt[q + (long long)(D.g - 1) * D.fstride] : T(0);
+  t_rho[q + (long long)(D.g - 1) * D.fstride] = mdt ? -div_m + mdg : -div_m;
   T div_t;
   if (D.theta_order == 2) {
     auto th = [&](int i, int j, int k) { const long long p = IX(D, i, j, k); return G.theta_v_bg[p] + T(Ss.tp[p]); };
@@ -708,15 +720,19 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
     auto gy = [&](int i, int j, int k) { return tvv[IX(D, i, j, k)] * fy(i, j, k); };
     div_t = div_h_at<T>(D, G, gx, gy, ji, jk, jl);
   }
-  // dissipative heating, radiation, sediment heating (phase transitions and temperature
-  // diffusion are zero), in the reference's order
-  const T heat = hd[q] + rad[q] + csh[q];
+  // dissipative heating, radiation, sediment heating and temperature diffusion (phase
+  // transitions are zero), in the reference's order
+  T heat = hd[q] + rad[q] + csh[q];
+  if (tdh) heat = heat + tdh[q];
   T x = T(0);
   if (heat != T(0)) {
     const T cv = c_v_mass_weighted_air<T>(D, Ss.rho, Tm, q);
     x = T(kC_D_V) * T(rg[q]) / cv * heat / (T(kC_D_P) * (G.exner_bg[q] + T(Ss.ep[q])));
   }
-  t_rt[q] = -div_t + x;
+  T r = -div_t + x;
+  // (phase transition rate + mass diffusion of the gas) * theta_v
+  if (mdt) r = r + mdg * (G.theta_v_bg[q] + T(Ss.tp[q]));
+  t_rt[q] = r;
 }
 
 // ---- FP64-only kernels (kernels_fp64.cu, column_fp64.cu) -------------------------------

@@ -4,6 +4,7 @@
 #include "lgame_emulator.h"
 #include "common.h"
 #include "emulator.cuh"
+#include "diffusion.cuh"
 #include "kernels.cuh"
 #include "split.cuh"
 
@@ -64,7 +65,13 @@ struct lgame_gpu {
   Tend<double> tend;
   double *pg_nl_u, *pg_nl_v, *pg_nl_w, *pg_l_u, *pg_l_v, *pg_l_w, *pg_old_u, *pg_old_v, *pgcw;
   double *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
-  double* hdiss;  // heating_diss: dissipative heating of the swamp layer, formed at each step's first substep
+  double* hdiss;  // heating_diss: dissipative heating, formed at each step's first substep
+  // diffusion closure (&diff): which parts run, their buffers (tke, viscosity and the momentum
+  // diffusion accelerations are carried diagnostics, allocated always) and constants
+  bool diff_mom_h = false, diff_mom_v = false, diff_temp_h = false, diff_temp_v = false;
+  bool diff_mass_h = false, diff_mass_v = false;
+  DiffBuf<double> dbuf{};
+  DiffPar dpar{};
   // scratch
   double *theta, *gz, *gx, *gy, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph, *vsq;
   double* staging = nullptr;
@@ -160,6 +167,9 @@ Ext grid_ext(const Dims& d, int f) {
     case LGAME_GRID_FVEC_X: return {(size_t)d.ny + 1, (size_t)d.nx, 1};
     case LGAME_GRID_FVEC_Y: return {(size_t)d.ny, (size_t)d.nx + 1, 1};
     case LGAME_GRID_FVEC_Z: return {(size_t)d.ny + 1, (size_t)d.nx + 1, 1};
+    case LGAME_GRID_DX_DUAL: return ext_v(d);
+    case LGAME_GRID_DY_DUAL: return ext_u(d);
+    case LGAME_GRID_LAYER_THICKNESS: return ext_s(d);
   }
   return {0, 0, 0};
 }
@@ -172,6 +182,9 @@ Ext diag_ext(const Dims& d, int f) {
     case LGAME_DIAG_POT_VORT_TEND_Y: case LGAME_DIAG_V_SQUARED_GRAD_Y: case LGAME_DIAG_TEND_WIND_V: return ext_v(d);
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: case LGAME_DIAG_POT_VORT_TEND_Z:
     case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: return ext_w(d);
+    case LGAME_DIAG_MOM_DIFF_TEND_X: return ext_u(d);
+    case LGAME_DIAG_MOM_DIFF_TEND_Y: return ext_v(d);
+    case LGAME_DIAG_MOM_DIFF_TEND_Z: return ext_w(d);
     default: return ext_s(d);
   }
 }
@@ -481,6 +494,14 @@ const auto k_gas_theta = lg::k_gas_theta<double>;
 const auto k_pgrad = lg::k_pgrad;
 const auto k_column_ver = lg::k_column_ver;
 const auto k_column_tracers = lg::k_column_tracers;
+const auto k_diff_tke = lg::k_diff_tke<double, double>;
+const auto k_diff_visc = lg::k_diff_visc<double, double>;
+const auto k_diff_vz = lg::k_diff_vz<double, double>;
+const auto k_mom_diff_h = lg::k_mom_diff_h<double, double>;
+const auto k_mom_diff_v = lg::k_mom_diff_v<double, double>;
+const auto k_diss_rate = lg::k_diss_rate<double, double>;
+const auto k_diff_flux = lg::k_diff_flux<double, double, double>;
+const auto k_diff_div = lg::k_diff_div<double>;
 }  // namespace kd
 
 dim3 blk() { return dim3(32, 8, 1); }
@@ -533,6 +554,53 @@ int advection(lgame_gpu* c, const State& S) {
   return LGAME_OK;
 }
 
+// momentum diffusion and dissipation at the first substep, mo_vector_tend_expl.F90:100-126:
+// n_squared and the TKE (the vertical coefficient scheme is always tke), the viscosity,
+// mom_diff_h, mom_diff_v, then the dissipation rate (with the Klemp layer alone, its part)
+int diffusion_vector(lgame_gpu* c, const State& So) {
+  const Dims& D = c->D;
+  const Grid<double>& G = c->G;
+  const DiffBuf<double>& B = c->dbuf;
+  if (c->diff_mom_h) {
+    LAUNCH(kd::k_diff_tke, grd(D, D.ny, D.nx, D.nl), D, G, So, B, c->dpar);
+    LAUNCH(kd::k_diff_visc, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature, B, c->dpar);
+    LAUNCH(kd::k_diff_vz, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, B);
+    LAUNCH(kd::k_mom_diff_h, grd(D, D.ny, D.nx, D.nl), D, G, So, B);
+    if (c->diff_mom_v) LAUNCH(kd::k_mom_diff_v, grd(D, D.ny, D.nx, D.nl - 1), D, G, So, B);
+    LAUNCH(kd::k_diss_rate, grd(D, D.ny, D.nx, D.nl), D, G, So, B, G.damp, (const double*)nullptr);
+  } else if (D.lklemp && D.ndamp > 0) {
+    LAUNCH(k_heating_diss, grd(D, D.ny, D.nx, std::min(D.nl, D.ndamp)), D, G, So, c->hdiss);
+  }
+  return LGAME_OK;
+}
+
+// temperature and mass diffusion of scalar_tend_expl's first substep, mo_scalar_tend_expl.F90:
+// 60-101 (the second substep's temperature diffusion repeats the first's: same temperature,
+// same coefficients, so its result is reused)
+int diffusion_scalar(lgame_gpu* c, const State& So) {
+  const Dims& D = c->D;
+  const Grid<double>& G = c->G;
+  const DiffBuf<double>& B = c->dbuf;
+  const dim3 gs = grd(D, D.ny, D.nx, D.nl), ge = grd(D, D.ny + 1, D.nx + 1, D.nl), gv = grd(D, D.ny, D.nx, D.nl - 1);
+  if (c->diff_temp_h) {
+    const int vert = c->diff_temp_v ? 1 : 0;
+    LAUNCH(kd::k_grad_vert, gv, D, G, (const double*)c->temperature, c->gz);
+    LAUNCH(kd::k_diff_flux, ge, D, G, So, B, (const double*)c->temperature, (const double*)c->gz, 1, vert, c->uph,
+           c->vph, c->wph);
+    LAUNCH(kd::k_diff_div, gs, D, G, c->uph, c->vph, c->wph, vert, B.tdh);
+  }
+  if (c->diff_mass_h) {
+    const int vert = c->diff_mass_v ? 1 : 0;
+    for (int jc = 0; jc < D.ncons; ++jc) {
+      const double* r = So.rho + (long long)jc * D.fstride;
+      LAUNCH(kd::k_grad_vert, gv, D, G, r, c->gz);
+      LAUNCH(kd::k_diff_flux, ge, D, G, So, B, r, (const double*)c->gz, 0, vert, c->uph, c->vph, c->wph);
+      LAUNCH(kd::k_diff_div, gs, D, G, c->uph, c->vph, c->wph, vert, B.mdt + (long long)jc * D.fstride);
+    }
+  }
+  return LGAME_OK;
+}
+
 int step_fp64(lgame_gpu* c, int so, int sn, int step) {
   const Dims& D = c->D;
   const State& So = c->st[so];
@@ -561,15 +629,23 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       int rc = advection(c, Sv);
       if (rc != LGAME_OK) return rc;
     }
-    // momentum diffusion and dissipation at the first substep (mo_vector_tend_expl.F90:100-126):
-    // with the Klemp layer on, its dissipative heating from state_old
-    if (rk == 1 && D.lklemp && D.ndamp > 0)
-      LAUNCH(k_heating_diss, grd(D, D.ny, D.nx, std::min(D.nl, D.ndamp)), D, G, So, c->hdiss);
+    // momentum diffusion and dissipation at the first substep (mo_vector_tend_expl.F90:100-126)
+    if (rk == 1) {
+      const int rc = diffusion_vector(c, So);
+      if (rc != LGAME_OK) return rc;
+    }
     Tend<double> T = c->tend;
+    if (c->diff_mom_h) { C.mdt_x = c->dbuf.mdtx; C.mdt_y = c->dbuf.mdty; C.mdt_z = c->dbuf.mdtz; }
     LAUNCH(kd::k_tend_wind, grd(D, D.ny + 1, D.nx + 1, D.NL), D, So, Sn, T, C, rk, (float*)nullptr, (float*)nullptr);
     // scalar_tend_expl (mo_scalar_tend_expl.F90:24-181)
     const State& Ss = (rk == 1) ? So : Sn;
-    if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk);
+    if (rk == 1) {
+      const int rc = diffusion_scalar(c, So);
+      if (rc != LGAME_OK) return rc;
+    }
+    const double* mdt = c->diff_mass_h ? c->dbuf.mdt : nullptr;
+    const double* tdh = c->diff_temp_h ? c->dbuf.tdh : nullptr;
+    if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk, mdt);
     // theta_v_adv_3rd_order of the state used here: in the first substep that is state_old,
     // whose edges manage_p_grad's call above already left in tvu/tvv (nothing in between
     // writes state_old or tvu/tvv), so only the second substep recomputes them -- the same
@@ -579,7 +655,7 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       if (rc != LGAME_OK) return rc;
     }
     LAUNCH(kd::k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->hdiss,
-           c->rad, c->csh, T.rho, T.rt);
+           c->rad, c->csh, T.rho, T.rt, mdt, tdh);
     // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
     {
       dim3 g2((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 7) / 8), 1);
@@ -600,8 +676,11 @@ int split_sync_carried(lgame_gpu* c, bool to_split) {
                         {c->pvt_x, F.pvt_x, n}, {c->pvt_y, F.pvt_y, n}, {c->pvt_z, F.pvt_z, n}, {c->csh, F.csh, n},
                         {c->rad, F.rad, n}, {c->temperature, F.temperature, n}, {c->tend.rho, F.tend.rho, n * c->D.ncons},
                         {c->tend.rt, F.tend.rt, n}, {c->tend.u, F.tend.u, n}, {c->tend.v, F.tend.v, n},
-                        {c->tend.w, F.tend.w, n}};
+                        {c->tend.w, F.tend.w, n}, {c->hdiss, F.hdiss, n},
+                        {c->dbuf.tke, F.tke, n}, {c->dbuf.visc, F.visc, n}, {c->dbuf.mdtx, F.mdtx, n},
+                        {c->dbuf.mdty, F.mdty, n}, {c->dbuf.mdtz, F.mdtz, n}};
   for (const Pair& p : pairs) {
+    if (!p.f) continue;  // diffusion off: no FP32 copy
     const int rc = to_split ? split_convert(p.d, p.f, p.n, c->stream) : split_convert_back(p.f, p.d, p.n, c->stream);
     if (rc != LGAME_OK) return set_err(rc, "conversion of the split-mode diagnostics failed");
   }
@@ -653,8 +732,21 @@ int check_cfg(const lgame_config* cfg) {
       cfg->precision != LGAME_PRECISION_SPLIT_FP64_COLUMN)
     return set_err(LGAME_ERR_BAD_CONFIG,
                    "precision must be LGAME_PRECISION_FP64, LGAME_PRECISION_SPLIT or LGAME_PRECISION_SPLIT_FP64_COLUMN");
-  if (cfg->lmom_diff_h || cfg->lmom_diff_v || cfg->ltemp_diff_h || cfg->ltemp_diff_v || cfg->lmass_diff_h || cfg->lmass_diff_v)
-    return set_err(LGAME_ERR_UNSUPPORTED, "diffusion (&diff lmom_diff_h ... lmass_diff_v) is not part of the GPU step");
+  if (cfg->diff_coeff_scheme_h != LGAME_DIFF_COEFF_SMAG && cfg->diff_coeff_scheme_h != LGAME_DIFF_COEFF_TKE)
+    return set_err(LGAME_ERR_BAD_CONFIG, "diff_coeff_scheme_h must be LGAME_DIFF_COEFF_SMAG or LGAME_DIFF_COEFF_TKE");
+  // the reference's diffusion reads coefficients and TKE values only horizontal momentum
+  // diffusion forms in the same step (mo_eff_diff_coeffs.F90:541-596, mo_momentum_diff_diss.F90:
+  // 286, mo_vector_tend_expl.F90:104-117): without it they are those of earlier calls
+  if ((cfg->ltemp_diff_h || cfg->lmass_diff_h || cfg->lmom_diff_v) && !cfg->lmom_diff_h)
+    return set_err(LGAME_ERR_UNSUPPORTED, "temperature, mass or vertical momentum diffusion without horizontal momentum "
+                                          "diffusion (lmom_diff_h) is not part of the GPU step");
+  // non-periodic: tke_update's inner product reads grad(tke) at the boundary edges, which the
+  // reference leaves at the zero of mom_diff_v's or the third-order theta advection's last
+  // whole-array write only in these configurations
+  if (cfg->lmom_diff_h && !cfg->lperiodic && !cfg->lmom_diff_v && cfg->theta_adv_order != 3)
+    return set_err(LGAME_ERR_UNSUPPORTED, "non-periodic horizontal momentum diffusion without lmom_diff_v needs "
+                                          "theta_adv_order 3 in the GPU step");
+
   if (cfg->lprog_soil_temp || cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl)
     return set_err(LGAME_ERR_UNSUPPORTED, "surface physics (&surface lprog_soil_temp, lsfc_*, lpbl) is not part of the GPU step");
   return LGAME_OK;
@@ -728,6 +820,28 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   double** scratch[] = {&c->theta, &c->gz, &c->gx, &c->gy, &c->divf, &c->tvu, &c->tvv, &c->tpu, &c->tpv,
                         &c->ex, &c->ey, &c->ez, &c->uph, &c->vph, &c->wph, &c->vsq};
   for (double** p : scratch) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+  // diffusion closure: the carried diagnostics always, the work arrays when a part is on
+  {
+    DiffBuf<double>& B = c->dbuf;
+    double** carried_d[] = {&B.tke, &B.visc, &B.mdtx, &B.mdty, &B.mdtz};
+    for (double** p : carried_d) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+    B.hd = c->hdiss;
+    c->diff_mom_h = cfg->lmom_diff_h; c->diff_mom_v = cfg->lmom_diff_v;
+    c->diff_temp_h = cfg->ltemp_diff_h; c->diff_temp_v = cfg->ltemp_diff_v;
+    c->diff_mass_h = cfg->lmass_diff_h; c->diff_mass_v = cfg->lmass_diff_v;
+    if (c->diff_mom_h) {
+      double** work[] = {&B.tke_new, &B.vmol, &B.nsq, &B.vz};
+      for (double** p : work) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+      if (c->diff_temp_h && (rc = dalloc(c, &B.tdh, F)) != LGAME_OK) return fail(rc);
+      if (c->diff_mass_h && (rc = dalloc(c, &B.mdt, F * D.ncons)) != LGAME_OK) return fail(rc);
+    }
+    DiffPar& P = c->dpar;
+    P.eff_hor_res = std::sqrt(cfg->dx * cfg->dy);
+    P.c_s = cfg->c_s; P.bg_shear = cfg->bg_shear;
+    P.tke_h = cfg->diff_coeff_scheme_h == LGAME_DIFF_COEFF_TKE;
+    P.mom_v = cfg->lmom_diff_v;
+    P.mva = 0.0;  // set with the grid
+  }
   c->staging_elems = 6 * (size_t)D.ny * D.nx * D.nl;
   if ((rc = dalloc(c, &c->staging, c->staging_elems)) != LGAME_OK) return fail(rc);
   if ((rc = dalloc(c, &c->reduce_buf, (size_t)kRedBlocks * LGAME_BUDGETS_MAX + LGAME_BUDGETS_MAX)) != LGAME_OK) return fail(rc);
@@ -754,8 +868,14 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   for (int k = 0; k < 3; ++k) G.trsk_u[k] = c->trsk_u[k];
   for (int k = 0; k < 2; ++k) G.trsk_v[k] = c->trsk_v[k];
   G.damp = c->damp;
+  G.dx_dual = c->grid[LGAME_GRID_DX_DUAL]; G.dy_dual = c->grid[LGAME_GRID_DY_DUAL];
+  G.layer_thickness = c->grid[LGAME_GRID_LAYER_THICKNESS];
   if (cfg->precision != LGAME_PRECISION_FP64) {
-    if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, &c->split, &c->bytes)) != LGAME_OK)
+    SplitDiff sd;
+    sd.mom_h = c->diff_mom_h; sd.mom_v = c->diff_mom_v; sd.temp_h = c->diff_temp_h; sd.temp_v = c->diff_temp_v;
+    sd.mass_h = c->diff_mass_h; sd.mass_v = c->diff_mass_v; sd.par = c->dpar;
+    if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, sd, &c->split, &c->bytes)) !=
+        LGAME_OK)
       return fail(rc);
   }
   *out = c;
@@ -822,6 +942,16 @@ extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfie
     }
     c->D.ndamp = ndamp;
     CK(cudaMemsetAsync(c->hdiss, 0, sizeof(double) * (size_t)D.fstride, c->stream));
+  }
+  // mean_velocity_area, mo_grid_generator.F90:1111: twice the surface areas' sum (array order)
+  // over their number
+  {
+    const size_t n2 = (size_t)D.ny * D.nx;
+    const double* az = f[LGAME_GRID_AREA_Z] + n2 * (size_t)D.nl;
+    double sum = 0.0;
+    for (size_t p = 0; p < n2; ++p) sum = sum + az[p];
+    c->dpar.mva = 2.0 * sum / (double)n2;
+    if (c->split) split_set_diff_par(c->split, c->dpar);
   }
   if (c->split) {
     if ((rc = split_set_grid(c->split, c->D, c->G, c->stream)) != LGAME_OK) return rc;
@@ -903,6 +1033,12 @@ double* diag_dev(lgame_gpu* c, int f) {
     case LGAME_DIAG_TEND_WIND_U: return c->tend.u;
     case LGAME_DIAG_TEND_WIND_V: return c->tend.v;
     case LGAME_DIAG_TEND_WIND_W: return c->tend.w;
+    case LGAME_DIAG_TKE: return c->dbuf.tke;
+    case LGAME_DIAG_VISCOSITY: return c->dbuf.visc;
+    case LGAME_DIAG_HEATING_DISS: return c->hdiss;
+    case LGAME_DIAG_MOM_DIFF_TEND_X: return c->dbuf.mdtx;
+    case LGAME_DIAG_MOM_DIFF_TEND_Y: return c->dbuf.mdty;
+    case LGAME_DIAG_MOM_DIFF_TEND_Z: return c->dbuf.mdtz;
   }
   return nullptr;
 }

@@ -81,6 +81,9 @@ struct SplitCtx {
   // the vertical acoustic solve with FP64 coefficients and elimination (precision mode
   // LGAME_PRECISION_SPLIT_FP64_COLUMN)
   bool column_fp64 = false;
+  // diffusion closure: configuration and FP32 buffers (the carried ones are in C)
+  SplitDiff diff{};
+  DiffBuf<float> db{};
 };
 
 namespace {
@@ -492,7 +495,7 @@ __global__ void __launch_bounds__(128) ks_div_h(Dims D, Grid<float> GF, GridX X,
 __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* fu,
                                                   const float* fv, const float* gu, const float* gv, const float* Tm,
                                                   const float* hd, const float* rad, const float* csh, float* t_rho,
-                                                  float* t_rt) {
+                                                  float* t_rt, const float* mdt, const float* tdh) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
@@ -512,7 +515,8 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
       mn = layer_faces(D, GF, fx, fy, ji, jk, jl + 1);
       tn = layer_faces(D, GF, gx, gy, ji, jk, jl + 1);
     }
-    const float heat = hd[q] + rad[q] + csh[q];  // dissipative, radiative, sediment heating
+    float heat = hd[q] + rad[q] + csh[q];  // dissipative, radiative, sediment heating
+    if (tdh) heat = heat + tdh[q];         // temperature diffusion
     const float div_m = div_col(D, GF, X, mc, vert_faces(D, mh_prev, mc.h, mn.h, jl), ji, jk, jl);
     const float div_t = div_col(D, GF, X, tc, vert_faces(D, th_prev, tc.h, tn.h, jl), ji, jk, jl);
     float x = 0.f;
@@ -520,8 +524,14 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
       const float cv = c_v_mass_weighted_air<float>(D, Ss.rho, Tm, q);
       x = float(kC_D_V) * Ss.rho[q + goff] / cv * heat / (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
     }
-    t_rho[q + goff] = -div_m;
-    t_rt[q] = -div_t + x;
+    if (mdt) {  // mass diffusion of the gas, in its tendency and times theta_v in rho*theta_v's
+      const float mdg = mdt[q + goff];
+      t_rho[q + goff] = -div_m + mdg;
+      t_rt[q] = -div_t + x + mdg * (GF.theta_v_bg[q] + Ss.tp[q]);
+    } else {
+      t_rho[q + goff] = -div_m;
+      t_rt[q] = -div_t + x;
+    }
     mh_prev = mc.h;
     th_prev = tc.h;
     mc = mn;
@@ -539,7 +549,8 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
 // Five resident blocks of 256 threads per SM (48 registers) ran 4 % faster than four.
 constexpr int kTracers = 6;  // moist: five condensates and water vapour (the gas has its own kernel)
 __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* u_new,
-                                                     const float* v_new, float* t_rho, int rk_step) {
+                                                     const float* v_new, float* t_rho, int rk_step,
+                                                     const float* mdt) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -594,6 +605,13 @@ __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, Gri
     const float* r = Ss.rho + (long long)(jc - 1) * D.fstride;
     const float comp = r[i_e] * a_e + r[i_n] * a_n - r[i_w] * a_w - r[i_s] * a_s + r[i_u] * a_u - r[i_l] * a_l;
     dv[t] = comp * iv;
+  }
+  if (mdt) {  // mass diffusion: -div + mass_diff_tendency
+#pragma unroll
+    for (int t = 0; t < kTracers; ++t) {
+      const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+      dv[t] = dv[t] - mdt[q + (long long)(jc - 1) * D.fstride];
+    }
   }
   if (rk_step == 1) {
 #pragma unroll
@@ -671,8 +689,9 @@ __global__ void ks_tend_wind(Dims D, State So, State Sn, Tend<float> Tn, Carried
   };
   if (jl <= D.nl && ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
-    const float t = old_weight * Tn.u[q] +
-                    new_weight * (pg_h(PF.pold_u, PF.pnet_u, C.old_u, C.nl_u, C.l_u, q) - 0.5f * C.vsg_x[q] + C.pvt_x[q]);
+    float f = pg_h(PF.pold_u, PF.pnet_u, C.old_u, C.nl_u, C.l_u, q) - 0.5f * C.vsg_x[q] + C.pvt_x[q];
+    if (C.mdt_x) f = f + C.mdt_x[q];
+    const float t = old_weight * Tn.u[q] + new_weight * f;
     Tn.u[q] = t;
     const double un = So.u[q] + D.dtime * wide(t);
     Sn.u[q] = un;
@@ -680,8 +699,9 @@ __global__ void ks_tend_wind(Dims D, State So, State Sn, Tend<float> Tn, Carried
   }
   if (jl <= D.nl && ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    const float t = old_weight * Tn.v[q] +
-                    new_weight * (pg_h(PF.pold_v, PF.pnet_v, C.old_v, C.nl_v, C.l_v, q) - 0.5f * C.vsg_y[q] + C.pvt_y[q]);
+    float f = pg_h(PF.pold_v, PF.pnet_v, C.old_v, C.nl_v, C.l_v, q) - 0.5f * C.vsg_y[q] + C.pvt_y[q];
+    if (C.mdt_y) f = f + C.mdt_y[q];
+    const float t = old_weight * Tn.v[q] + new_weight * f;
     Tn.v[q] = t;
     const double vn = So.v[q] + D.dtime * wide(t);
     Sn.v[q] = vn;
@@ -691,7 +711,9 @@ __global__ void ks_tend_wind(Dims D, State So, State Sn, Tend<float> Tn, Carried
     const long long q = IX(D, ji, jk, jl);
     const float pg = D.luse_bg ? -(float(cvw_d) * PF.pnet_w[q])
                                : narrow(-(cvw_d * (C.nl_w[q] + C.l_w[q])) - no_bg_d * (1.0 - cvw_d) * C.l_w[q]);
-    Tn.w[q] = old_weight * Tn.w[q] + new_weight * (pg - 0.5f * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q]);
+    float f = pg - 0.5f * C.vsg_z[q] + C.pvt_z[q] + C.pgcw[q];
+    if (C.mdt_z) f = f + C.mdt_z[q];
+    Tn.w[q] = old_weight * Tn.w[q] + new_weight * f;
   }
 }
 
@@ -1254,7 +1276,7 @@ dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsig
 
 }  // namespace
 
-int split_create(const Dims& D, bool column_fp64, SplitCtx** out, long long* bytes) {
+int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCtx** out, long long* bytes) {
   if (D.ncons > 1 && D.ncons != kTracers + 1) {
     lgame_set_error("split precision: the tracer kernel is built for five condensates and water vapour");
     return LGAME_ERR_UNSUPPORTED;
@@ -1304,9 +1326,19 @@ int split_create(const Dims& D, bool column_fp64, SplitCtx** out, long long* byt
                    &C.pold_v};
   for (float** p : car) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &C.tend.rho, F * D.ncons, bytes))) return fail(rc);
+  s->diff = diff;
+  if (diff.mom_h) {
+    DiffBuf<float>& B = s->db;
+    float** dfl[] = {&C.tke, &C.visc, &C.mdtx, &C.mdty, &C.mdtz, &B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.tdh};
+    for (float** p : dfl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
+    if ((rc = salloc(s, &B.mdt, F * D.ncons, bytes))) return fail(rc);
+    B.tke = C.tke; B.visc = C.visc; B.mdtx = C.mdtx; B.mdty = C.mdty; B.mdtz = C.mdtz; B.hd = C.hdiss;
+  }
   *out = s;
   return LGAME_OK;
 }
+
+void split_set_diff_par(SplitCtx* s, const DiffPar& par) { s->diff.par = par; }
 
 void split_destroy(SplitCtx* s) {
   if (!s) return;
@@ -1463,11 +1495,13 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
                          G.area_dual_x, G.area_dual_y, G.area_dual_z, G.z_area_dual_z, G.slope_x, G.slope_y,
                          G.theta_v_bg, G.exner_bg, G.egu, G.egv, G.egw, G.gm, G.gp, G.fvec_x, G.fvec_y, G.fvec_z,
                          G.damp};
+  const double* src2[] = {G.dx_dual, G.dy_dual, G.layer_thickness};  // -> gf[33..35]
   const int nsrc = sizeof(src) / sizeof(src[0]);
   for (int k = 0; k < nsrc; ++k) {
     const long long n = (src[k] == G.fvec_x || src[k] == G.fvec_y || src[k] == G.fvec_z) ? D.plane : F;
     if (split_convert(src[k], s->gf[k], n, stream)) return LGAME_ERR_CUDA;
   }
+  for (int k = 0; k < 3; ++k) if (split_convert(src2[k], s->gf[33 + k], F, stream)) return LGAME_ERR_CUDA;
   for (int k = 0; k < 6; ++k) if (split_convert(G.ipw[k], s->ipw[k], F, stream)) return LGAME_ERR_CUDA;
   for (int k = 0; k < 3; ++k) if (split_convert(G.trsk_u[k], s->trsk_u[k], D.P, stream)) return LGAME_ERR_CUDA;
   for (int k = 0; k < 2; ++k) if (split_convert(G.trsk_v[k], s->trsk_v[k], D.P, stream)) return LGAME_ERR_CUDA;
@@ -1490,6 +1524,7 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
   GF.area_dual_y = g[12]; GF.area_dual_z = g[13]; GF.z_area_dual_z = g[14]; GF.slope_x = g[15]; GF.slope_y = g[16];
   GF.theta_v_bg = g[17]; GF.exner_bg = g[18]; GF.egu = g[19]; GF.egv = g[20]; GF.egw = g[21]; GF.gm = g[22];
   GF.gp = g[23]; GF.fvec_x = g[24]; GF.fvec_y = g[25]; GF.fvec_z = g[26]; GF.damp = g[27];
+  GF.dx_dual = g[33]; GF.dy_dual = g[34]; GF.layer_thickness = g[35];
   for (int k = 0; k < 6; ++k) GF.ipw[k] = s->ipw[k];
   for (int k = 0; k < 3; ++k) GF.trsk_u[k] = s->trsk_u[k];
   for (int k = 0; k < 2; ++k) GF.trsk_v[k] = s->trsk_v[k];
@@ -1581,14 +1616,50 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
            C.vsg_x, C.vsg_y);
       }
     }
-    // the swamp layer's dissipative heating from state_old at the first substep
-    // (mo_vector_tend_expl.F90:100-126)
-    if (rk == 1 && D.lklemp && D.ndamp > 0)
+    // momentum diffusion and dissipation at the first substep (mo_vector_tend_expl.F90:100-126),
+    // from state_old's mirror; with the Klemp layer alone, the swamp layer's heating
+    const SplitDiff& SD = s->diff;
+    const DiffBuf<float>& DB = s->db;
+    if (rk == 1 && SD.mom_h) {
+      const dim3 gs = sgrd(D.ny, D.nx, D.nl);
+      SL("ks_diff_tke", (k_diff_tke<float, float>), gs, B, D, GF, Mo, DB, SD.par);
+      SL("ks_diff_visc", (k_diff_visc<float, float>), gs, B, D, GF, Mo, (const float*)C.temperature, DB, SD.par);
+      SL("ks_diff_vz", (k_diff_vz<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
+      SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
+      if (SD.mom_v) SL("ks_mom_diff_v", (k_mom_diff_v<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, Mo, DB);
+      SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
+      CC.mdt_x = DB.mdtx; CC.mdt_y = DB.mdty; CC.mdt_z = DB.mdtz;
+    } else if (rk == 1 && D.lklemp && D.ndamp > 0) {
       SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
+    }
     SL("ks_tend_wind", ks_tend_wind, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, C, rk, Mn.u, Mn.v);
     const StateF& Ms = (rk == 1) ? Mo : Mn;
+    // temperature and mass diffusion at the first substep (mo_scalar_tend_expl.F90:60-101); the
+    // second substep's temperature diffusion is the same (same temperature and coefficients)
+    if (rk == 1 && SD.mom_h && (SD.temp_h || SD.mass_h)) {
+      const dim3 gs = sgrd(D.ny, D.nx, D.nl), ge = sgrd(D.ny + 1, D.nx + 1, D.nl), gv = sgrd(D.ny, D.nx, D.nl - 1);
+      if (SD.temp_h) {
+        const int vert = SD.temp_v ? 1 : 0;
+        SL("ks_grad_vert", (k_grad_vert<float, float>), gv, B, D, GF, (const float*)C.temperature, s->gz);
+        SL("ks_diff_flux", (k_diff_flux<float, float, float>), ge, B, D, GF, Mo, DB, (const float*)C.temperature,
+           (const float*)s->gz, 1, vert, s->uph, s->vph, s->wph);
+        SL("ks_diff_div", k_diff_div<float>, gs, B, D, GF, s->uph, s->vph, s->wph, vert, DB.tdh);
+      }
+      if (SD.mass_h) {
+        const int vert = SD.mass_v ? 1 : 0;
+        for (int jc = 0; jc < D.ncons; ++jc) {
+          const float* r = Mo.rho + (long long)jc * D.fstride;
+          SL("ks_grad_vert", (k_grad_vert<float, float>), gv, B, D, GF, r, s->gz);
+          SL("ks_diff_flux", (k_diff_flux<float, float, float>), ge, B, D, GF, Mo, DB, r, (const float*)s->gz, 0, vert,
+             s->uph, s->vph, s->wph);
+          SL("ks_diff_div", k_diff_div<float>, gs, B, D, GF, s->uph, s->vph, s->wph, vert, DB.mdt + (long long)jc * D.fstride);
+        }
+      }
+    }
+    const float* mdt = (SD.mom_h && SD.mass_h) ? DB.mdt : nullptr;
+    const float* tdh = (SD.mom_h && SD.temp_h) ? DB.tdh : nullptr;
     if (D.ncons > 1)
-      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk);
+      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk, mdt);
     // third-order theta edges of the state used here; in the first substep that is the old
     // state, whose edges the pressure gradient's call above already left in tvu/tvv (nothing
     // in between writes the old mirror or tvu/tvv), so only the second substep recomputes them
@@ -1599,7 +1670,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
        s->fv, s->gu, s->gv);
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
-       C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt);
+       C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh);
     const dim3 gc = cgrd(D.ny, D.nx);
     if (s->column_fp64)
       SL("ks_column_ver", ks_column_ver<double>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);

@@ -17,6 +17,7 @@
 
 #include <cuda_runtime.h>
 
+#include "diffusion.cuh"
 #include "kernels.cuh"
 
 namespace lg {
@@ -26,15 +27,27 @@ struct SplitCtx;
 // diagnostic buffers of the split step that correspond to lgame_gpu.h's carried fields
 struct SplitCarriedF {
   float *pgcw, *vsg_x, *vsg_y, *vsg_z, *pvt_x, *pvt_y, *pvt_z, *csh, *rad, *temperature;
-  float* hdiss;  // dissipative heating of the swamp layer, formed at each step's first substep
+  float* hdiss;  // dissipative heating, formed at each step's first substep
+  // the carried diagnostics of the diffusion closure (null when horizontal momentum diffusion
+  // is off): TKE, viscosity, momentum diffusion accelerations
+  float *tke, *visc, *mdtx, *mdty, *mdtz;
   Tend<float> tend;
   // with a background state: the net pressure-gradient terms nl + l of u, v, w and the previous
   // substep's values -(nl + l) of u, v, rounded to FP32 (the only form the wind update uses)
   float *pnet_u, *pnet_v, *pnet_w, *pold_u, *pold_v;
 };
 
-// column_fp64: the vertical acoustic solve with FP64 coefficients and elimination
-int split_create(const Dims& D, bool column_fp64, SplitCtx** out, long long* bytes);
+// the diffusion closure of the split step: which parts run and their constants
+struct SplitDiff {
+  bool mom_h = false, mom_v = false, temp_h = false, temp_v = false, mass_h = false, mass_v = false;
+  DiffPar par{};
+};
+
+// column_fp64: the vertical acoustic solve with FP64 coefficients and elimination; diff: the
+// diffusion closure (its buffers are allocated when horizontal momentum diffusion is on)
+int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCtx** out, long long* bytes);
+// the closure's constants once the grid is known (mean_velocity_area)
+void split_set_diff_par(SplitCtx* s, const DiffPar& par);
 void split_destroy(SplitCtx* s);
 // builds the FP32 metric copies and the FP64 reciprocal metrics from the FP64 grid
 int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream_t stream);

@@ -21,12 +21,15 @@ LIB_PATH = _PKG / "_build" / "liblgame_gpu.so"
 OK, ERR_INVALID_ARG, ERR_BAD_DIMS, ERR_BAD_CONFIG, ERR_UNSUPPORTED = 0, -1, -2, -3, -4
 ERR_ALLOC, ERR_CUDA, ERR_NONFINITE, ERR_NO_DEVICE, ERR_STATE = -5, -6, -7, -8, -9
 PRECISION_FP64, PRECISION_SPLIT, PRECISION_SPLIT_FP64_COLUMN = 0, 1, 2
+# diff_coeff_scheme_h (lgame_config)
+DIFF_COEFF_SMAG = 0
+DIFF_COEFF_TKE = 1
 
 GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "area_x", "area_y", "area_z",
                "area_dual_x", "area_dual_y", "area_dual_z", "z_area_dual_z", "slope_x", "slope_y",
                "inner_product_weights", "theta_v_bg", "exner_bg", "exner_bg_grad_u", "exner_bg_grad_v",
                "exner_bg_grad_w", "gravity_m_v", "gravity_potential", "fvec_x", "fvec_y", "fvec_z",
-               "trsk_weights_u", "trsk_weights_v"]
+               "trsk_weights_u", "trsk_weights_v", "dx_dual", "dy_dual", "layer_thickness"]
 STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w"]
 # fields of an output file (enum lgame_output_field), float32, scalar points
 OUTPUT_FIELDS = ["rho", "temperature", "rel_humidity", "wind_u", "wind_v", "wind_w"]
@@ -128,7 +131,8 @@ DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_
                "p_grad_acc_neg_l_v", "p_grad_acc_neg_l_w", "p_grad_acc_old_u", "p_grad_acc_old_v",
                "pot_vort_tend_x", "pot_vort_tend_y", "pot_vort_tend_z", "v_squared_grad_x", "v_squared_grad_y",
                "v_squared_grad_z", "condensates_sediment_heat", "radiation_tendency", "temperature",
-               "tend_rho", "tend_rhotheta_v", "tend_wind_u", "tend_wind_v", "tend_wind_w"]
+               "tend_rho", "tend_rhotheta_v", "tend_wind_u", "tend_wind_v", "tend_wind_w",
+               "tke", "viscosity", "heating_diss", "mom_diff_tend_x", "mom_diff_tend_y", "mom_diff_tend_z"]
 
 
 class Config(C.Structure):
@@ -143,7 +147,8 @@ class Config(C.Structure):
                 ("lprog_soil_temp", C.c_int), ("lsfc_sensible_heat_flux", C.c_int),
                 ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lperiodic", C.c_int),
                 ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("diff_coeff_scheme_h", C.c_int), ("bg_shear", C.c_double),
+                ("c_s", C.c_double)]
 
 
 def _s(n):
@@ -307,6 +312,9 @@ def field_shapes(ny: int, nx: int, nl: int, ncons: int) -> dict[str, tuple]:
         "pot_vort_tend_z": w, "v_squared_grad_x": u, "v_squared_grad_y": v, "v_squared_grad_z": w,
         "condensates_sediment_heat": s, "radiation_tendency": s, "temperature": s,
         "tend_rho": (ny, nx, nl, ncons), "tend_rhotheta_v": s, "tend_wind_u": u, "tend_wind_v": v, "tend_wind_w": w,
+        "dx_dual": v, "dy_dual": u, "layer_thickness": s,
+        "tke": s, "viscosity": s, "heating_diss": s, "mom_diff_tend_x": u, "mom_diff_tend_y": v,
+        "mom_diff_tend_z": w,
     }
 
 

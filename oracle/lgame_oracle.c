@@ -46,6 +46,11 @@ struct oracle_ctx {
   int lmoist, lperiodic, lfreeslip, lcorio, llinear, luse_bg_state, lklemp, theta_adv_order;
   double dtime, toa, dx, dy, klemp_damp_max, klemp_begin_rel;
   int n_damping_levels;  /* levels whose highest z_w lies above klemp_begin_rel*toa */
+  /* &diff (mo_diff_nml.F90:12-26) and the derived scalars of the diffusion closure:
+   * eff_hor_res = sqrt(dx*dy) (mo_run_nml.F90:93), mean_velocity_area =
+   * 2*sum(area_z(:,:,n_levels))/(ny*nx) (mo_grid_generator.F90:1111) */
+  int lmom_diff_h, lmom_diff_v, ltemp_diff_h, ltemp_diff_v, lmass_diff_h, lmass_diff_v, diff_h_tke;
+  double bg_shear, c_s, eff_hor_res, mean_velocity_area;
   /* grid */
   double *z_scalar, *z_u, *z_v, *z_w, *gdx, *gdy, *gdz, *volume, *area_x, *area_y, *area_z;
   double *area_dual_x, *area_dual_y, *area_dual_z, *z_area_dual_z, *slope_x, *slope_y, *ipw;
@@ -63,6 +68,11 @@ struct oracle_ctx {
   double *radiation_tendency, *flux_density_u, *flux_density_v, *flux_density_div;
   double *p_grad_decel_factor, *mom_diff_tend_x, *mom_diff_tend_y, *mom_diff_tend_z;
   double *heating_diss, *phase_trans_rates, *phase_trans_heating_rate, *temp_diff_heating;
+  /* diffusion closure: the grid's dual distances and layer thicknesses; its diagnostics */
+  double *dx_dual, *dy_dual, *layer_thickness;
+  double *tke, *viscosity, *viscosity_molecular, *viscosity_dual, *n_squared, *du_dz, *dv_dz;
+  double *vert_hor_viscosity_u, *vert_hor_viscosity_v, *mass_diff_coeff_eff_h, *mass_diff_coeff_eff_v;
+  double *temp_diff_coeff_eff_h, *temp_diff_coeff_eff_v, *flux_density_w;
   double *condensates_sediment_heat, *mass_diff_tendency, *a_rain;
   /* lateral boundary conditions (t_bc, mo_definitions.F90:117-131): two time levels, the
    * rescale factors, the level indices (1-based) and the time of the older level */
@@ -112,6 +122,10 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   o->theta_adv_order = cfg->theta_adv_order; o->dtime = cfg->dtime; o->toa = cfg->toa;
   o->dx = cfg->dx; o->dy = cfg->dy; o->klemp_damp_max = cfg->klemp_damp_max;
   o->klemp_begin_rel = cfg->klemp_begin_rel;
+  o->lmom_diff_h = cfg->lmom_diff_h; o->lmom_diff_v = cfg->lmom_diff_v; o->ltemp_diff_h = cfg->ltemp_diff_h;
+  o->ltemp_diff_v = cfg->ltemp_diff_v; o->lmass_diff_h = cfg->lmass_diff_h; o->lmass_diff_v = cfg->lmass_diff_v;
+  o->diff_h_tke = cfg->diff_coeff_scheme_h == LGAME_DIFF_COEFF_TKE;
+  o->bg_shear = cfg->bg_shear; o->c_s = cfg->c_s; o->eff_hor_res = sqrt(cfg->dx*cfg->dy);
   DIMS;
   const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
   const size_t nW = (size_t)ny*nx*(nl+1), nZ = (size_t)(ny+1)*(nx+1)*nl;
@@ -148,8 +162,16 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   o->heating_diss = zalloc(nS); o->phase_trans_rates = zalloc(nS*(o->nc+1));
   o->phase_trans_heating_rate = zalloc(nS); o->temp_diff_heating = zalloc(nS);
   o->condensates_sediment_heat = zalloc(nS); o->mass_diff_tendency = zalloc(nS*o->ncons);
+  o->dx_dual = zalloc(nV); o->dy_dual = zalloc(nU); o->layer_thickness = zalloc(nS);
+  o->tke = zalloc(nS); o->viscosity = zalloc(nS); o->viscosity_molecular = zalloc(nS);
+  o->viscosity_dual = zalloc(nZ); o->n_squared = zalloc(nS);
+  o->du_dz = zalloc((size_t)ny*(nx+1)*(nl+1)); o->dv_dz = zalloc((size_t)(ny+1)*nx*(nl+1));
+  o->vert_hor_viscosity_u = zalloc((size_t)ny*(nx+1)*(nl+1)); o->vert_hor_viscosity_v = zalloc((size_t)(ny+1)*nx*(nl+1));
+  o->mass_diff_coeff_eff_h = zalloc(nS); o->mass_diff_coeff_eff_v = zalloc(nS);
+  o->temp_diff_coeff_eff_h = zalloc(nS); o->temp_diff_coeff_eff_v = zalloc(nS); o->flux_density_w = zalloc(nW);
   o->a_rain = zalloc(nS);
-  if (!o->a_rain || !o->mass_diff_tendency || !o->rho[1] || !o->ipw) { oracle_destroy(o); return LGAME_ERR_ALLOC; }
+  for (double** q = &o->z_scalar; q <= &o->a_rain; ++q)
+    if (!*q) { oracle_destroy(o); return LGAME_ERR_ALLOC; }
   *out = o;
   return LGAME_OK;
 }
@@ -190,6 +212,9 @@ static size_t grid_size(const oracle_ctx* o, int f) {
     case LGAME_GRID_FVEC_Z: return (size_t)(ny+1)*(nx+1);
     case LGAME_GRID_TRSK_WEIGHTS_U: return 3*(size_t)ny;
     case LGAME_GRID_TRSK_WEIGHTS_V: return 2*(size_t)(ny+1);
+    case LGAME_GRID_DX_DUAL: return nV;
+    case LGAME_GRID_DY_DUAL: return nU;
+    case LGAME_GRID_LAYER_THICKNESS: return nS;
   }
   return 0;
 }
@@ -201,10 +226,17 @@ int oracle_set_grid(oracle_ctx* o, const double* const* f, int nfields) {
     o->area_z, o->area_dual_x, o->area_dual_y, o->area_dual_z, o->z_area_dual_z, o->slope_x,
     o->slope_y, o->ipw, o->theta_v_bg, o->exner_bg, o->exner_bg_grad_u, o->exner_bg_grad_v,
     o->exner_bg_grad_w, o->gravity_m_v, o->gravity_potential, o->fvec_x, o->fvec_y, o->fvec_z,
-    o->trsk_u, o->trsk_v};
+    o->trsk_u, o->trsk_v, o->dx_dual, o->dy_dual, o->layer_thickness};
   for (int i = 0; i < LGAME_GRID_NFIELDS; ++i) {
     if (!f[i]) return LGAME_ERR_INVALID_ARG;
     memcpy(dst[i], f[i], grid_size(o, i)*sizeof(double));
+  }
+  /* mean_velocity_area, mo_grid_generator.F90:1111: the surface areas summed in array order */
+  {
+    const size_t n2 = (size_t)o->ny*o->nx, base = n2*(size_t)o->nl;
+    double sum = 0.0;
+    for (size_t c = 0; c < n2; ++c) sum = sum + o->area_z[base + c];
+    o->mean_velocity_area = 2.0*sum/(double)n2;
   }
   /* n_damping_levels, mo_grid_generator.F90:1049-1058 */
   o->n_damping_levels = 0;
@@ -216,6 +248,14 @@ int oracle_set_grid(oracle_ctx* o, const double* const* f, int nfields) {
     }
     if (max_z > o->klemp_begin_rel*o->toa) o->n_damping_levels = o->n_damping_levels + 1;
   }
+  return LGAME_OK;
+}
+
+int oracle_scalar_diffusion(const oracle_ctx* o, double* mass_diff_tendency, double* temp_diff_heating) {
+  if (!o || !mass_diff_tendency || !temp_diff_heating) return LGAME_ERR_INVALID_ARG;
+  const size_t nS = (size_t)o->ny*o->nx*o->nl;
+  memcpy(mass_diff_tendency, o->mass_diff_tendency, nS*(size_t)o->ncons*sizeof(double));
+  memcpy(temp_diff_heating, o->temp_diff_heating, nS*sizeof(double));
   return LGAME_OK;
 }
 
@@ -283,6 +323,12 @@ static void diag_ptrs(oracle_ctx* o, double** p, size_t* n) {
   p[LGAME_DIAG_TEND_WIND_U] = o->t_wind_u; n[LGAME_DIAG_TEND_WIND_U] = nU;
   p[LGAME_DIAG_TEND_WIND_V] = o->t_wind_v; n[LGAME_DIAG_TEND_WIND_V] = nV;
   p[LGAME_DIAG_TEND_WIND_W] = o->t_wind_w; n[LGAME_DIAG_TEND_WIND_W] = nW;
+  p[LGAME_DIAG_TKE] = o->tke; n[LGAME_DIAG_TKE] = nS;
+  p[LGAME_DIAG_VISCOSITY] = o->viscosity; n[LGAME_DIAG_VISCOSITY] = nS;
+  p[LGAME_DIAG_HEATING_DISS] = o->heating_diss; n[LGAME_DIAG_HEATING_DISS] = nS;
+  p[LGAME_DIAG_MOM_DIFF_TEND_X] = o->mom_diff_tend_x; n[LGAME_DIAG_MOM_DIFF_TEND_X] = nU;
+  p[LGAME_DIAG_MOM_DIFF_TEND_Y] = o->mom_diff_tend_y; n[LGAME_DIAG_MOM_DIFF_TEND_Y] = nV;
+  p[LGAME_DIAG_MOM_DIFF_TEND_Z] = o->mom_diff_tend_z; n[LGAME_DIAG_MOM_DIFF_TEND_Z] = nW;
 }
 
 int oracle_set_diag(oracle_ctx* o, const double* const* f, int nfields) {

@@ -32,6 +32,9 @@ void oracle_destroy(oracle_ctx* o);
 int  oracle_set_grid(oracle_ctx* o, const double* const* fields, int nfields);
 /* diag%heating_diss of the last step (ny,nx,nl), the dissipative heating power density */
 int  oracle_heating_diss(const oracle_ctx* o, double* out);
+/* the scalar diffusion of the last step: mass_diff_tendency (ny,nx,nl,ncons) and
+ * temp_diff_heating (ny,nx,nl) */
+int  oracle_scalar_diffusion(const oracle_ctx* o, double* mass_diff_tendency, double* temp_diff_heating);
 int  oracle_set_state(oracle_ctx* o, int slot, const double* const* fields, int nfields);
 int  oracle_get_state(oracle_ctx* o, int slot, double* const* fields, int nfields);
 int  oracle_set_diag(oracle_ctx* o, const double* const* fields, int nfields);

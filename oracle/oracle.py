@@ -53,6 +53,7 @@ def load():
             ("oracle_bc_state", i, [vp, C.POINTER(i), C.POINTER(i), dp]),
             ("oracle_bc_factors", i, [vp, dp, dp, dp]),
             ("oracle_heating_diss", i, [vp, C.POINTER(C.c_double)]),
+            ("oracle_scalar_diffusion", i, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             ("oracle_output", i, [vp, i, i, C.c_double, C.c_double, C.POINTER(C.POINTER(C.c_float)), i,
                                   C.POINTER(i)]),
         ]:
@@ -147,6 +148,18 @@ class Oracle:
         dp = C.POINTER(C.c_double)
         assert self.lib.oracle_bc_factors(self.h, *[a.ctypes.data_as(dp) for a in (fs, fu, fv)]) == 0
         return fs, fu, fv
+
+    def scalar_diffusion(self):
+        """(mass_diff_tendency (ny, nx, n_layers, ncons), temp_diff_heating (ny, nx, n_layers))
+        of the last step."""
+        ny, nx, nl = self.shapes["theta_v_pert"]
+        mdt = np.zeros((ny, nx, nl, self.shapes["rho"][3]), order="F")
+        tdh = np.zeros((ny, nx, nl), order="F")
+        rc = self.lib.oracle_scalar_diffusion(self.h, mdt.ctypes.data_as(C.POINTER(C.c_double)),
+                                              tdh.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise RuntimeError(f"oracle_scalar_diffusion failed: {rc}")
+        return mdt, tdh
 
     def heating_diss(self):
         """diag%heating_diss of the last step, (ny, nx, n_layers)."""

@@ -35,7 +35,9 @@ def namelist_text(name: str, **overrides) -> str:
 GROUP_OF = {
     "luse_bg_state": "run", "llinear": "run", "lcorio": "run", "lplane": "run", "theta_adv_order": "run",
     "stretching_parameter": "run", "lat_center": "run", "lon_center": "run", "scenario": "run",
-    "lklemp": "diff", "klemp_damp_max": "diff", "klemp_begin_rel": "diff",
+    "lklemp": "diff", "klemp_damp_max": "diff", "klemp_begin_rel": "diff", "lmom_diff_h": "diff",
+    "lmom_diff_v": "diff", "ltemp_diff_h": "diff", "ltemp_diff_v": "diff", "lmass_diff_h": "diff",
+    "lmass_diff_v": "diff", "diff_coeff_scheme_h": "diff", "bg_shear": "diff", "c_s": "diff",
     "lperiodic": "bc", "lfreeslip": "bc", "lmoist": "constituents", "orography_id": "surface", "lsleve": "surface",
 }
 

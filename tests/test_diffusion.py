@@ -1,0 +1,250 @@
+"""Diffusion closure of the HEVI step: TKE, horizontal viscosity (Smagorinsky or TKE),
+momentum diffusion, temperature and mass diffusion (src/subgrid_scale/mo_eff_diff_coeffs.F90,
+mo_tke.F90, src/spatial_operators/mo_momentum_diff_diss.F90, mo_vector_tend_expl.F90:100-126,
+mo_scalar_tend_expl.F90:60-101).
+
+CPU: the oracle's restatement against a second, vectorised numpy restatement on a flat plane
+(no terrain terms): the viscosity and the vertical diffusion of w after the first step (the
+TKE is still zero then); the gas mass is conserved with mass diffusion on in a periodic
+domain; the namelist defaults of &diff are the reference's (all diffusion on, smag, tke).
+GPU: the FP64 step against the oracle, state and the carried diffusion diagnostics, on
+periodic and non-periodic cases with orography, Smagorinsky and TKE horizontal schemes, and
+with horizontal momentum diffusion alone.
+"""
+import numpy as np
+import pytest
+
+import cases
+import lgame_gpu as L
+import oracle as O
+
+DIFF_ON = dict(lmom_diff_h=True, lmom_diff_v=True, ltemp_diff_h=True, ltemp_diff_v=True, lmass_diff_h=True,
+               lmass_diff_v=True)
+DIFF_FIELDS = ["tke", "viscosity", "heating_diss", "mom_diff_tend_x", "mom_diff_tend_y", "mom_diff_tend_z"]
+
+
+def diff_case(key: str, **kw):
+    cfg_name, ov = cases.SMALL[key]
+    return cases.namelist(cfg_name, **{**ov, **DIFF_ON, **kw})
+
+
+def _oracle(n):
+    hm = L.HostModel(n)
+    cfg = L.config_from_namelist(n)
+    o = O.Oracle(cfg, hm.grid)
+    o.set_state(0, hm.state)
+    o.set_state(1, hm.state)
+    o.set_diag(hm.diag)
+    return hm, cfg, o
+
+
+def test_namelist_defaults_of_diff():
+    """&diff left out: the reference's defaults (mo_diff_nml.F90:38-53)."""
+    text = (cases.CONFIGS / "jet_1024x1024x80.nml").read_text()
+    start = text.index("&diff")
+    end = text.index("/", start)
+    n = L.namelist_from_text(text[:start] + text[end + 1:])
+    cfg = L.config_from_namelist(n)
+    assert (cfg.lmom_diff_h, cfg.lmom_diff_v, cfg.ltemp_diff_h, cfg.ltemp_diff_v, cfg.lmass_diff_h,
+            cfg.lmass_diff_v) == (1, 1, 1, 1, 1, 1)
+    assert cfg.diff_coeff_scheme_h == L.DIFF_COEFF_SMAG
+    assert (cfg.bg_shear, cfg.c_s) == (1.5e-5, 0.2)
+    n2 = cases.namelist("jet_1024x1024x80", diff_coeff_scheme_h="tke", c_s=0.25, bg_shear=2e-5)
+    cfg2 = L.config_from_namelist(n2)
+    assert (cfg2.diff_coeff_scheme_h, cfg2.c_s, cfg2.bg_shear) == (L.DIFF_COEFF_TKE, 0.25, 2e-5)
+
+
+# ---- numpy restatement on a flat plane (periodic, no terrain) ---------------------------------
+
+K_B, N_A, M_D = 1.380649e-23, 6.02214076e23, 6.02214076e23 * 0.004810e-23
+
+
+def _calc_diff_coeff(t, rho):
+    """calc_diff_coeff, mo_derived.F90:189-216."""
+    m = M_D / N_A
+    thermal_velocity = np.sqrt(8.0 * K_B * t / (np.pi * m))
+    particle_density = rho / m
+    cross_section = 4.0 * np.pi * (130e-12 * 130e-12)
+    mean_free_path = 1.0 / (np.sqrt(2.0) * particle_density * cross_section)
+    return 1.0 / 3.0 * thermal_velocity * mean_free_path
+
+
+def _plane_fields(hm, st, nc):
+    g = hm.grid
+    u, v = st["wind_u"], st["wind_v"]
+    rg = st["rho"][..., nc]
+    # relative vorticity at the dual points (rel_vort_z_local's flat formula with the periodic
+    # wrap, mo_vorticities.F90:423-538): +dy v(i,k) - dx u(i-1,k) - dy v(i,k-1) + dx u(i,k)
+    ny, nx = rg.shape[:2]
+    dy, dx = g["dy"], g["dx"]
+    ii = np.arange(ny + 1)
+    kk = np.arange(nx + 1)
+    i0 = np.where(ii == ny, 0, ii)            # v row ji (ny+1 -> 1)
+    im = np.where(ii == 0, ny - 1, ii - 1)    # u row ji-1 (1 -> ny)
+    k0 = np.where(kk == nx, 0, kk)            # u column jk (nx+1 -> 1)
+    km = np.where(kk == 0, nx - 1, kk - 1)    # v column jk-1 (1 -> nx)
+    A = dy[ii][:, k0] * v[ii][:, k0]
+    B = dx[im][:, kk] * u[im][:, kk]
+    Cc = dy[ii][:, km] * v[ii][:, km]
+    Dd = dx[i0][:, kk] * u[i0][:, kk]
+    zeta = (((A + (-1.0) * B) + (-1.0) * Cc) + Dd) / g["area_dual_z"]
+    div = (u[:, 1:] * g["area_x"][:, 1:] + v[:-1] * g["area_y"][:-1] - u[:, :-1] * g["area_x"][:, :-1]
+           - v[1:] * g["area_y"][1:]) / g["volume"]
+    return zeta, div, rg
+
+
+def test_oracle_viscosity_and_vertical_w_diffusion_plane():
+    """After the first step of the flat plane case (TKE zero, so the vertical coefficient is the
+    molecular one alone): viscosity = rho_g*(molecular + c_s*mean_velocity_area*max(|(zeta,
+    div)|, bg_shear)) and mom_diff_tend_z = grad_vert(rho_g*nu_mol*dw/dz)/rho averaged."""
+    n = diff_case("jet_plane")
+    hm, cfg, o = _oracle(n)
+    nc = 5 if n.lmoist else 0
+    st0 = o.get_state(0)
+    o.pchevi(0, 1, 0)
+    dg = o.get_diag()
+    T0 = dg["temperature"]
+    o.close()
+    g = hm.grid
+    zeta, div, rg = _plane_fields(hm, st0, nc)
+    vac = 0.25 * (zeta[:-1, :-1] + zeta[:-1, 1:] + zeta[1:, :-1] + zeta[1:, 1:])
+    mva = 2.0 * g["area_z"][:, :, -1].sum() / g["area_z"][:, :, -1].size
+    eddy = cfg.c_s * mva * np.sqrt(np.maximum(vac * vac + div * div, cfg.bg_shear ** 2))
+    vmol = _calc_diff_coeff(T0, rg)
+    visc = rg * (vmol + eddy)
+    np.testing.assert_allclose(dg["viscosity"], visc, rtol=1e-12)
+    assert not np.any(dg["tke"]), "the TKE stays zero in the first step (no gradient, no heating yet)"
+    # vertical diffusion of w
+    w = st0["wind_w"]
+    cu = w[:, :, :-1].copy()
+    cu[:, :, 0] = 0.0
+    cl = w[:, :, 1:].copy()
+    cl[:, :, -1] = 0.0
+    az = g["area_z"]
+    dwdz = (cu * az[:, :, :-1] - cl * az[:, :, 1:]) / g["volume"]
+    sp = rg * vmol * dwdz
+    mz = (sp[:, :, :-1] - sp[:, :, 1:]) / g["dz"][:, :, 1:-1]
+    rsum = st0["rho"][..., 0].copy()
+    for jc in range(1, nc + 1):
+        rsum = rsum + st0["rho"][..., jc]
+    mz = mz / (0.5 * (rsum[:, :, :-1] + rsum[:, :, 1:]))
+    np.testing.assert_allclose(dg["mom_diff_tend_z"][:, :, 1:-1], mz, rtol=1e-10,
+                               atol=1e-12 * np.abs(mz).max())
+    assert not np.any(dg["mom_diff_tend_z"][:, :, [0, -1]])
+
+
+@pytest.mark.parametrize("key", ["jet_plane", "hills_nonperiodic"])
+def test_oracle_scalar_diffusion_is_conservative(key):
+    """The mass and temperature diffusion are flux divergences whose boundary fluxes vanish
+    (periodic wrap, or never-written boundary edges): sum(tendency * volume) is zero to
+    rounding for every constituent and for the heating, after three steps.  A flat periodic
+    plane and a non-periodic domain: where the periodic wrap joins faces of different areas
+    (area_y of rows 1 and ny+1 on the rotated sphere; area_x of columns 1 and nx+1 over
+    periodic terrain, whose boundary faces the grid generator extrapolates one-sidedly,
+    mo_grid_generator.F90:1113-1123), the reference's sums are not zero."""
+    n = diff_case(key)
+    hm, cfg, o = _oracle(n)
+    for k in range(3):
+        o.pchevi(k % 2, (k + 1) % 2, k)
+    mdt, tdh = o.scalar_diffusion()
+    o.close()
+    vol = hm.grid["volume"]
+    fields = [tdh] + [mdt[..., jc] for jc in range(mdt.shape[3])]
+    nc = 5 if n.lmoist else 0
+    assert np.abs(tdh).max() > 0.0 and np.abs(mdt[..., nc]).max() > 0.0
+    for jc, x in enumerate(fields):  # constituents absent from the case diffuse nothing
+        xv = x * vol
+        scale = np.abs(xv).sum()
+        assert abs(xv.sum()) <= 1e-12 * scale, (jc, xv.sum(), scale)
+
+
+def test_oracle_diffusion_changes_the_step():
+    """The closure is live: with diffusion on the state after two steps differs from the run
+    without, the TKE has grown where the dissipation heats, and the heating is finite."""
+    outs = []
+    for on in (True, False):
+        n = diff_case("jet") if on else cases.small_case("jet")
+        hm, cfg, o = _oracle(n)
+        for k in range(3):
+            o.pchevi(k % 2, (k + 1) % 2, k)
+        outs.append((o.get_state(1), o.get_diag()))
+        o.close()
+    (s_on, d_on), (s_off, _) = outs
+    assert np.abs(s_on["wind_u"] - s_off["wind_u"]).max() > 0.0
+    assert np.all(np.isfinite(d_on["heating_diss"])) and np.all(d_on["tke"] >= 0.0)
+    assert d_on["tke"].max() > 0.0
+    assert np.abs(d_on["mom_diff_tend_x"]).max() > 0.0
+
+
+# ---- GPU: the FP64 step against the oracle ------------------------------------------------------
+
+GPU_CASES = {
+    "jet": {},
+    "jet_tke": dict(diff_coeff_scheme_h="tke"),
+    "jet_mom_h_only": dict(lmom_diff_v=False, ltemp_diff_h=False, lmass_diff_h=False),
+    "hills_nonperiodic": {},
+    "schaer": {},
+}
+
+
+def _gpu_case(name):
+    kw = dict(GPU_CASES[name])
+    key = name.split("_tke")[0].split("_mom_h_only")[0]
+    return diff_case(key, **kw)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(GPU_CASES))
+def test_fp64_diffusion_matches_oracle(name):
+    n = _gpu_case(name)
+    hm, cfg, o = _oracle(n)
+    cfg.precision = L.PRECISION_FP64
+    g = L.GpuModel(cfg, hm.grid)
+    g.set_state(0, hm.state)
+    g.set_state(1, hm.state)
+    g.set_diag(hm.diag)
+    nsteps = 4
+    for k in range(nsteps):
+        o.pchevi(k % 2, (k + 1) % 2, k)
+        g.pchevi(k % 2, (k + 1) % 2, k)
+    so, sg = o.get_state(nsteps % 2), g.get_state(nsteps % 2)
+    do, dgpu = o.get_diag(), g.get_diag()
+    g.close()
+    o.close()
+    for f in so:
+        assert cases.rel_err(sg[f], so[f]) <= 1e-12, (f, cases.rel_err(sg[f], so[f]))
+    for f in DIFF_FIELDS:
+        assert cases.rel_err(dgpu[f], do[f]) <= 1e-11, (f, cases.rel_err(dgpu[f], do[f]))
+    assert do["viscosity"].max() > 0.0 and np.abs(do["mom_diff_tend_x"]).max() > 0.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["jet", "hills_nonperiodic"])
+def test_split_diffusion_close_to_fp64(name):
+    """The split step's FP32 closure against the FP64 step: the state after ten steps within
+    the split step's bar (3e-5 of each field's maximum), the carried diffusion diagnostics
+    within FP32 accuracy of theirs."""
+    from test_split import field_errors
+    n = _gpu_case(name)
+    hm = L.HostModel(n)
+    gs = []
+    for prec in (L.PRECISION_FP64, L.PRECISION_SPLIT):
+        cfg = L.config_from_namelist(n)
+        cfg.precision = prec
+        g = L.GpuModel(cfg, hm.grid)
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        gs.append(g)
+    for step in range(10):
+        for g in gs:
+            g.pchevi(step % 2, (step + 1) % 2, step)
+    a, b = gs[1].get_state(0), gs[0].get_state(0)
+    da, db = gs[1].get_diag(), gs[0].get_diag()
+    for g in gs:
+        g.close()
+    errs = field_errors(a, b)
+    assert max(errs.values()) <= 3e-5, errs
+    for f in DIFF_FIELDS:
+        assert np.all(np.isfinite(da[f])), f
+        assert cases.rel_err(da[f], db[f]) <= 2e-3, (f, cases.rel_err(da[f], db[f]))

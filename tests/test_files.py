@@ -45,7 +45,7 @@ def test_snapshot_round_trip_and_header(tmp_path):
             np.testing.assert_array_equal(a[f], b[f], err_msg=f)
     raw = path.read_bytes()
     magic, version, ny, nx, nl, nc, st = struct.unpack_from("<8s5iq", raw, 0)
-    assert (magic, version, ny, nx, nl, nc, st) == (b"LGAMESNP", 1, hm.ny, hm.nx, hm.nl, hm.ncons, 2)
+    assert (magic, version, ny, nx, nl, nc, st) == (b"LGAMESNP", 2, hm.ny, hm.nx, hm.nl, hm.ncons, 2)
     assert raw[36:64] == bytes(28)
     n_doubles = 2 * sum(v.size for v in s0.values()) + sum(v.size for v in dg.values())
     assert len(raw) == 64 + 8 * n_doubles

@@ -50,7 +50,10 @@ def _cfg(**kw):
     ("theta_adv_order", 5, L.ERR_BAD_CONFIG),
     ("dtime", -1.0, L.ERR_BAD_CONFIG),
     ("precision", 9, L.ERR_BAD_CONFIG),
-    ("lmom_diff_h", 1, L.ERR_UNSUPPORTED),
+    ("diff_coeff_scheme_h", 7, L.ERR_BAD_CONFIG),
+    ("ltemp_diff_h", 1, L.ERR_UNSUPPORTED),
+    ("lmass_diff_h", 1, L.ERR_UNSUPPORTED),
+    ("lmom_diff_v", 1, L.ERR_UNSUPPORTED),
     ("lpbl", 1, L.ERR_UNSUPPORTED),
 ])
 def test_create_rejects_bad_config(field, value, code):
@@ -58,6 +61,17 @@ def test_create_rejects_bad_config(field, value, code):
     h = C.c_void_p()
     rc = lib.lgame_gpu_create(C.byref(_cfg(**{field: value})), C.byref(h))
     assert rc == code and not h.value
+
+
+@pytest.mark.parametrize("kw", [
+    # non-periodic horizontal momentum diffusion needs lmom_diff_v or third-order theta
+    dict(lmom_diff_h=1, lperiodic=0, theta_adv_order=2),
+])
+def test_create_rejects_unsupported_diffusion(kw):
+    lib = L.load_library()
+    h = C.c_void_p()
+    rc = lib.lgame_gpu_create(C.byref(_cfg(**kw)), C.byref(h))
+    assert rc == L.ERR_UNSUPPORTED and not h.value
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device path")
