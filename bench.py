@@ -520,9 +520,11 @@ def run_ours(args):
         for r in results.values():
             if "e2e" in r:
                 line["e2e"] = r["e2e"]
+    hm = None  # the sub-benchmarks below set up their own host models
     if rank == 0 and ws == 1 and not args.no_boundaries:
-        del hm
         line["boundary_relaxation"] = boundary_bench(args, peaks)
+    if rank == 0 and ws == 1 and not args.no_diffusion:
+        line["diffusion"] = diffusion_bench(args, results)
     if rank == 0 and ws == 1 and not args.no_emulator:
         line["emulator"] = emulator_bench(peaks)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -531,6 +533,55 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     barrier(dist)
     return 0
+
+
+DIFF_DEFAULT = dict(lmom_diff_h=True, lmom_diff_v=True, ltemp_diff_h=True, ltemp_diff_v=True, lmass_diff_h=True,
+                    lmass_diff_v=True, diff_coeff_scheme_h="smag")
+
+
+def diffusion_bench(args, results: dict) -> dict:
+    """The workload with the reference's default &diff (mo_diff_nml.F90:38-53: momentum,
+    temperature and mass diffusion on, horizontally and vertically, Smagorinsky horizontal
+    coefficient, TKE vertical one): the split and the FP64 step (CUDA events on the library's
+    stream), their cost against the same steps without diffusion, and the closure's kernels'
+    share of the split step."""
+    import cases
+    import lgame_gpu as L
+    n = cases.namelist(WORKLOAD, **DIFF_DEFAULT, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    hm = L.HostModel(n)
+    out = {"config": "reference default &diff: all six switches on, smag/tke"}
+    runs = [(L.PRECISION_SPLIT, "split", args.steps), (L.PRECISION_FP64, "fp64", min(args.steps, 3))]
+    if args.split_only or args.fp64_only:
+        runs = [r for r in runs if (r[1] == "split") == args.split_only]
+    for prec, name, steps in runs:
+        cfg = L.config_from_namelist(n)
+        cfg.precision = prec
+        g = L.GpuModel(cfg, hm.grid)
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        for k in range(3):
+            g.pchevi(k % 2, (k + 1) % 2, k)
+        el = time_steps(L, g, steps, 3) / steps
+        e = {"value": 1.0 / el, "ms_per_step": el * 1e3, "kernels_per_step": g.kernels_per_step()}
+        base = results.get(prec)
+        if base is not None:
+            e["ms_per_step_without"] = base["s_per_step"] * 1e3
+            e["cost_of_diffusion"] = el / base["s_per_step"] - 1.0
+        if prec == L.PRECISION_SPLIT:
+            g.set_profiling(True)
+            for k in range(3 + steps, 5 + steps):
+                g.pchevi(k % 2, (k + 1) % 2, k)
+            rep = g.profile_report()
+            g.set_profiling(False)
+            tot = sum(v["ms"] for v in rep.values())
+            e["closure_kernel_shares"] = {k: round(v["ms"] / tot, 4) for k, v in rep.items()
+                                          if k.startswith(("ks_diff", "ks_mom_diff", "ks_diss"))}
+        st = g.get_state((3 + steps) % 2)
+        e["finite"] = all(bool(np.isfinite(v).all()) for v in st.values())
+        g.close()
+        out[name] = e
+    return out
 
 
 def boundary_bench(args, peaks, n_swamp: int = 5, reps: int = 20) -> dict:
@@ -760,6 +811,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-emulator", action="store_true")
     ap.add_argument("--no-boundaries", action="store_true", help="skip the non-periodic boundary-relaxation run")
+    ap.add_argument("--no-diffusion", action="store_true", help="skip the run with the default diffusion closure")
     ap.add_argument("--nx", type=int, default=0, help="override nx=ny (smaller runs for testing)")
     ap.add_argument("--ny", type=int, default=0)
     args = ap.parse_args()

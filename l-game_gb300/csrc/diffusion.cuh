@@ -45,6 +45,9 @@ struct DiffBuf {
   T *mdtx, *mdty, *mdtz; // mom_diff_tend_x/y/z (carried)
   T *mdt, *tdh;          // mass_diff_tendency (ncons fields), temp_diff_heating
   T* hd;                 // heating_diss (carried; formed by the dissipation kernel)
+  T *flx, *fly, *flw;    // diffusive flux densities of the scalar diffusion (one field per constituent)
+  T *zz;                 // zeta_z at dual points (rel_vort of the state of the first substep)
+  T *vdiv;               // viscosity * div_h(wind) at scalar points (mom_diff_h's scalar_placeholder)
 };
 
 // run-time constants of the closure
@@ -202,19 +205,29 @@ __global__ void k_diff_visc(Dims D, Grid<T> G, StateT<V> S, const T* Tm, DiffBuf
   const T rg = T(S.rho[q + (long long)(D.g - 1) * D.fstride]);
   const T tke = B.tke_new[q];
   const T vmol = diff_coeff_t<T>(Tm[q], rg);
+  const T dv = div_wind_at<T, V>(D, G, S, ji, jk, jl);
   T eddy;
   if (P.tke_h) {
     eddy = tke2hor<T>(P, tke);
   } else {
-    const T vac = T(0.25) * (zeta_z_at<T, V>(D, G, S, ji, jk, jl) + zeta_z_at<T, V>(D, G, S, ji, jk + 1, jl)
-                           + zeta_z_at<T, V>(D, G, S, ji + 1, jk, jl) + zeta_z_at<T, V>(D, G, S, ji + 1, jk + 1, jl));
-    const T dv = div_wind_at<T, V>(D, G, S, ji, jk, jl);
+    const T* zz = B.zz;
+    const T vac = T(0.25) * (zz[q] + zz[q + D.P] + zz[q + 1] + zz[q + D.P + 1]);
     const T a = vac * vac + dv * dv, b = T(P.bg_shear) * T(P.bg_shear);
     eddy = T(P.c_s) * T(P.mva) * dsqrt<T>(a > b ? a : b);
   }
+  const T visc = rg * (vmol + eddy);
   B.vmol[q] = vmol;
-  B.visc[q] = rg * (vmol + eddy);
+  B.visc[q] = visc;
+  B.vdiv[q] = visc * dv;
   B.tke[q] = tke;
+}
+
+// zeta_z of the wind at the dual points (ny+1, nx+1, nl), rel_vort (mo_vorticities.F90:19-187)
+template <class T, class V>
+__global__ void k_diff_zeta(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
+  LG_IDX3;
+  if (ji > D.ny + 1 || jk > D.nx + 1) return;
+  B.zz[IX(D, ji, jk, jl)] = zeta_z_at<T, V>(D, G, S, ji, jk, jl);
 }
 
 // ---- 3. hor_diff_coeff_postprocessing (mo_eff_diff_coeffs.F90:161-310) and rel_vort ----------
@@ -248,7 +261,7 @@ __global__ void k_diff_vz(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
       vd = vd * (T(0.25) * (rs(D.ny, D.nx) + rs(D.ny, 1) + rs(1, D.nx) + rs(1, 1)));
     }
   }
-  B.vz[q] = vd * zeta_z_at<T, V>(D, G, S, ji, jk, jl);
+  B.vz[q] = vd * B.zz[q];
 }
 
 // ---- 4. mom_diff_h (mo_momentum_diff_diss.F90:25-160) ----------------------------------------
@@ -261,7 +274,7 @@ __global__ void k_diff_vz(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
 template <class T, class V>
 __global__ void k_mom_diff_h(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B) {
   LG_IDX3;
-  auto sdiv = [&](int i, int j, int l) { return B.visc[IX(D, i, j, l)] * div_wind_at<T, V>(D, G, S, i, j, l); };
+  auto sdiv = [&](int i, int j, int l) { return B.vdiv[IX(D, i, j, l)]; };
   auto rsum = [&](int i, int j, int l) { return rho_sum_cond_gas<T, V>(D, S.rho, IX(D, i, j, l)); };
   const T* vz = B.vz;
   const T* zd = G.z_area_dual_z;
@@ -392,57 +405,156 @@ __device__ __forceinline__ T diff_coeff_v(const Dims& D, const Grid<T>& G, const
   return rg * c_g_v * t2v;
 }
 
-// diffusive flux densities of the scalar s (grad_hor with gz = grad_vert(s) as its vertical
-// component, zero at levels 1 and nl+1; then scalar_times_vector_h/_v with the coefficients):
-// fx, fy at u and v points (zero at non-periodic boundary edges, which the reference never
-// writes), fw at w levels 2..nl (only when the vertical diffusion is on)
-template <class T, class V, class SF>
-__global__ void k_diff_flux(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B, const SF* s, const T* gz, int kind,
-                            int vertical, T* fx, T* fy, T* fw) {
+// diffusive flux densities of nf scalar fields s0 + f*fstride (f = 0..nf-1): grad_hor with
+// grad_vert of the field as its vertical component (mo_gradient_operators.F90:65-130; the
+// vertical gradient formed inline, zero at levels 1 and nl+1), then scalar_times_vector_h/_v
+// with the coefficients of `kind`, which are formed once per point for all fields.  fx, fy at
+// u and v points (zero at non-periodic boundary edges, which the reference never writes), fw at
+// w levels 2..nl (only with the vertical diffusion on); field f at offset f*fstride.  The
+// addresses of the two cells of an edge and their metrics are formed once for all fields.
+template <class T, class V, class SF, int NF>
+__global__ void k_diff_fluxes(Dims D, Grid<T> G, StateT<V> S, DiffBuf<T> B, const SF* __restrict__ s0, int kind,
+                              int vertical, T* __restrict__ fx, T* __restrict__ fy, T* __restrict__ fw) {
   LG_IDX3;
-  auto ch = [&](int i, int j) { return diff_coeff_h<T, V>(D, S, B, kind, IX(D, i, j, jl)); };
+  constexpr int nf = NF;
+  const long long pl = D.plane;
+  const bool terrain = jl > D.nf;
+  const bool lower = jl < D.nl || D.freeslip;
+  const bool g_up = jl >= 2, g_lo = jl + 1 <= D.nl;  // grad_vert levels jl and jl+1 exist
+  // the edge between cells a and b (b - a is the difference grad_hor_cov takes): slope, the
+  // remap weights and the dz of the two vertical gradients of each cell
+  struct Edge { long long a, b; T h, dxy, slope, w5a, w5b, w6a, w6b, dza, dzb, dza1, dzb1; };
+  auto edge = [&](long long a, long long b, T h, T dxy, T slope) {
+    Edge e{a, b, h, dxy, slope, T(0), T(0), T(0), T(0), T(1), T(1), T(1), T(1)};
+    if (terrain) {
+      e.w5a = G.ipw[4][a]; e.w5b = G.ipw[4][b];
+      if (g_up) { e.dza = G.dz[a]; e.dzb = G.dz[b]; }
+      if (lower) {
+        e.w6a = G.ipw[5][a]; e.w6b = G.ipw[5][b];
+        if (g_lo) { e.dza1 = G.dz[a + pl]; e.dzb1 = G.dz[b + pl]; }
+      }
+    }
+    return e;
+  };
+  // grad_hor of one field at the edge: grad_hor_cov, minus slope times remap_ver2hor of the
+  // vertical gradient (mo_averaging.F90:56-136, same order)
+  auto grad = [&](const SF* s, const Edge& e, bool x) -> T {
+    T g = x ? cvt<T>(s[e.b] - s[e.a]) / e.dxy : cvt<T>(s[e.a] - s[e.b]) / e.dxy;
+    if (terrain) {
+      const T gza = g_up ? cvt<T>(s[e.a - pl] - s[e.a]) / e.dza : T(0);
+      const T gzb = g_up ? cvt<T>(s[e.b - pl] - s[e.b]) / e.dzb : T(0);
+      T r = T(0);
+      r = r + e.w5a * gza;
+      r = r + e.w5b * gzb;
+      if (lower) {
+        const T gza1 = g_lo ? cvt<T>(s[e.a] - s[e.a + pl]) / e.dza1 : T(0);
+        const T gzb1 = g_lo ? cvt<T>(s[e.b] - s[e.b + pl]) / e.dzb1 : T(0);
+        r = r + e.w6a * gza1;
+        r = r + e.w6b * gzb1;
+      }
+      g = g - e.slope * (T(0.5) * r);
+    }
+    return g;
+  };
+  auto ch = [&](long long p) { return diff_coeff_h<T, V>(D, S, B, kind, p); };
   if (ji <= D.ny && jk <= D.nx + 1) {
     const long long q = IX(D, ji, jk, jl);
-    T f = T(0), g;
-    if (grad_x_cov<T, SF>(D, G, s, ji, jk, jl, &g)) {
-      if (jl > D.nf) g = g - G.slope_x[q] * remap_x<T, T>(D, G, gz, ji, jk, jl);
-      if (jk >= 2 && jk <= D.nx) f = T(0.5) * (ch(ji, jk - 1) + ch(ji, jk)) * g;
-      else f = T(0.5) * (ch(ji, 1) + ch(ji, D.nx)) * g;
+    const bool inner = jk >= 2 && jk <= D.nx;
+    if (!inner && !D.periodic) {
+#pragma unroll
+      for (int f = 0; f < nf; ++f) fx[q + (long long)f * D.fstride] = T(0);
+    } else {
+      // cells west (a = jk-1, periodic nx) and east (b = jk, periodic 1) of the u point
+      const long long a = inner ? q - D.P : IX(D, ji, D.nx, jl), b = inner ? q : IX(D, ji, 1, jl);
+      const T h = inner ? T(0.5) * (ch(a) + ch(b)) : T(0.5) * (ch(b) + ch(a));
+      const Edge e = edge(a, b, h, G.dx[b], G.slope_x[q]);
+#pragma unroll
+      for (int f = 0; f < nf; ++f) fx[q + (long long)f * D.fstride] = e.h * grad(s0 + (long long)f * D.fstride, e, true);
     }
-    fx[q] = f;
   }
   if (ji <= D.ny + 1 && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    T f = T(0), g;
-    if (grad_y_cov<T, SF>(D, G, s, ji, jk, jl, &g)) {
-      if (jl > D.nf) g = g - G.slope_y[q] * remap_y<T, T>(D, G, gz, ji, jk, jl);
-      if (ji >= 2 && ji <= D.ny) f = T(0.5) * (ch(ji - 1, jk) + ch(ji, jk)) * g;
-      else f = T(0.5) * (ch(1, jk) + ch(D.ny, jk)) * g;
+    const bool inner = ji >= 2 && ji <= D.ny;
+    if (!inner && !D.periodic) {
+#pragma unroll
+      for (int f = 0; f < nf; ++f) fy[q + (long long)f * D.fstride] = T(0);
+    } else {
+      // cells north (a = ji-1, periodic ny) and south (b = ji, periodic 1) of the v point
+      const long long a = inner ? q - 1 : IX(D, D.ny, jk, jl), b = inner ? q : IX(D, 1, jk, jl);
+      const T h = inner ? T(0.5) * (ch(a) + ch(b)) : T(0.5) * (ch(b) + ch(a));
+      const Edge e = edge(a, b, h, G.dy[b], G.slope_y[q]);
+#pragma unroll
+      for (int f = 0; f < nf; ++f) fy[q + (long long)f * D.fstride] = e.h * grad(s0 + (long long)f * D.fstride, e, false);
     }
-    fy[q] = f;
   }
   if (vertical && jl >= 2 && ji <= D.ny && jk <= D.nx) {
     const long long q = IX(D, ji, jk, jl);
-    fw[q] = T(0.5) * (diff_coeff_v<T, V>(D, G, S, B, kind, q - D.plane) + diff_coeff_v<T, V>(D, G, S, B, kind, q)) * gz[q];
+    const T h = T(0.5) * (diff_coeff_v<T, V>(D, G, S, B, kind, q - pl) + diff_coeff_v<T, V>(D, G, S, B, kind, q));
+    const T dz = G.dz[q];
+#pragma unroll
+    for (int f = 0; f < nf; ++f) {
+      const SF* s = s0 + (long long)f * D.fstride;
+      fw[q + (long long)f * D.fstride] = h * (cvt<T>(s[q - pl] - s[q]) / dz);
+    }
   }
 }
 
-// div_h of the flux densities plus, with the vertical diffusion on, add_vertical_div of fw
-template <class T>
-__global__ void k_diff_div(Dims D, Grid<T> G, const T* fx, const T* fy, const T* fw, int vertical, T* out) {
+// div_h of the flux densities of each of nf fields plus, with the vertical diffusion on,
+// add_vertical_div of its fw (mo_divergence_operators.F90:16-68, 149-186).  The same expressions
+// and order as div_h_at / vertical_contravariant_corr (mo_averaging.F90:16-54), with the
+// addresses of the cell's faces and the metrics of the three layers the contravariant
+// corrections read formed once per cell for all fields.
+template <class T, int NF>
+__global__ void k_diff_divs(Dims D, Grid<T> G, const T* __restrict__ fx, const T* __restrict__ fy,
+                            const T* __restrict__ fw, int vertical, T* __restrict__ out) {
   LG_IDX3;
+  constexpr int nf = NF;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
-  auto ax = [&](int i, int j, int k) { return fx[IX(D, i, j, k)]; };
-  auto ay = [&](int i, int j, int k) { return fy[IX(D, i, j, k)]; };
-  T r = div_h_at<T>(D, G, ax, ay, ji, jk, jl);
-  if (vertical) {
-    const T cu = (jl == 1) ? T(0) : fw[q];
-    const T cl = (jl == D.nl) ? T(0) : fw[q + D.plane];
-    const T comp_v = cu * G.area_z[q] - cl * G.area_z[q + D.plane];
-    r = r + comp_v / G.volume[q];
+  const long long qe = q + D.P, qs = q + 1, pl = D.plane;
+  // metrics of layer l (dl = -1, 0, +1 relative to jl) for the correction terms
+  struct LM { T sxe, sy, sx, sys, w1, w2, w3, w4; };
+  auto lm = [&](long long d) {
+    LM m;
+    m.sxe = G.slope_x[qe + d]; m.sy = G.slope_y[q + d]; m.sx = G.slope_x[q + d]; m.sys = G.slope_y[qs + d];
+    m.w1 = G.ipw[0][q + d]; m.w2 = G.ipw[1][q + d]; m.w3 = G.ipw[2][q + d]; m.w4 = G.ipw[3][q + d];
+    return m;
+  };
+  // which interfaces carry a correction: upper (jl) and lower (jl+1)
+  const bool up_t = jl >= D.nf + 1, lo_t = jl + 1 >= D.nf + 1 && jl < D.nl;
+  LM mu{}, mc{}, md{};
+  if (jl >= D.nf + 2) mu = lm(-pl);
+  if (jl >= D.nf) mc = lm(0);
+  if (jl + 1 >= D.nf + 1 && jl < D.nl) md = lm(pl);
+  const T ax_e = G.area_x[qe], ay_n = G.area_y[q], ax_w = G.area_x[q], ay_s = G.area_y[qs];
+  const T az_u = G.area_z[q], az_l = G.area_z[q + pl], vol = G.volume[q];
+#pragma unroll
+  for (int f = 0; f < nf; ++f) {
+    const long long o = (long long)f * D.fstride;
+    const T* X = fx + o;
+    const T* Y = fy + o;
+    // r - 0.5*vx(e)*slope_x(e)*W1 - 0.5*vy(n)*slope_y(n)*W2 - 0.5*vx(w)*slope_x(w)*W3 - 0.5*vy(s)*slope_y(s)*W4
+    auto terms = [&](T r, const LM& m, long long d) {
+      return r - T(0.5) * X[qe + d] * m.sxe * m.w1 - T(0.5) * Y[q + d] * m.sy * m.w2
+               - T(0.5) * X[q + d] * m.sx * m.w3 - T(0.5) * Y[qs + d] * m.sys * m.w4;
+    };
+    // vertical_contravariant_corr at interface jl (cu) and jl+1 (cl)
+    T cu = T(0), cl = T(0);
+    if (up_t) cu = (jl == D.nf + 1) ? terms(T(0), mc, 0) : terms(terms(T(0), mu, -pl), mc, 0);
+    if (lo_t) cl = (jl + 1 == D.nf + 1) ? terms(T(0), md, pl) : terms(terms(T(0), mc, 0), md, pl);
+    const T comp_h = X[qe] * ax_e + Y[q] * ay_n - X[q] * ax_w - Y[qs] * ay_s;
+    T comp_v = T(0);
+    if (jl == D.nf) comp_v = -cl * az_l;
+    else if (jl == D.nl) comp_v = cu * az_u;
+    else if (jl > D.nf) comp_v = cu * az_u - cl * az_l;
+    T r = (comp_h + comp_v) / vol;
+    if (vertical) {
+      const T wu = (jl == 1) ? T(0) : fw[o + q];
+      const T wl = (jl == D.nl) ? T(0) : fw[o + q + pl];
+      r = r + (wu * az_u - wl * az_l) / vol;
+    }
+    out[o + q] = r;
   }
-  out[q] = r;
 }
 
 }  // namespace lg

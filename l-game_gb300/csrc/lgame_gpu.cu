@@ -496,12 +496,15 @@ const auto k_column_ver = lg::k_column_ver;
 const auto k_column_tracers = lg::k_column_tracers;
 const auto k_diff_tke = lg::k_diff_tke<double, double>;
 const auto k_diff_visc = lg::k_diff_visc<double, double>;
+const auto k_diff_zeta = lg::k_diff_zeta<double, double>;
 const auto k_diff_vz = lg::k_diff_vz<double, double>;
 const auto k_mom_diff_h = lg::k_mom_diff_h<double, double>;
 const auto k_mom_diff_v = lg::k_mom_diff_v<double, double>;
 const auto k_diss_rate = lg::k_diss_rate<double, double>;
-const auto k_diff_flux = lg::k_diff_flux<double, double, double>;
-const auto k_diff_div = lg::k_diff_div<double>;
+const auto k_diff_fluxes1 = lg::k_diff_fluxes<double, double, double, 1>;
+const auto k_diff_fluxes7 = lg::k_diff_fluxes<double, double, double, 7>;
+const auto k_diff_divs1 = lg::k_diff_divs<double, 1>;
+const auto k_diff_divs7 = lg::k_diff_divs<double, 7>;
 }  // namespace kd
 
 dim3 blk() { return dim3(32, 8, 1); }
@@ -563,6 +566,7 @@ int diffusion_vector(lgame_gpu* c, const State& So) {
   const DiffBuf<double>& B = c->dbuf;
   if (c->diff_mom_h) {
     LAUNCH(kd::k_diff_tke, grd(D, D.ny, D.nx, D.nl), D, G, So, B, c->dpar);
+    LAUNCH(kd::k_diff_zeta, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, B);
     LAUNCH(kd::k_diff_visc, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature, B, c->dpar);
     LAUNCH(kd::k_diff_vz, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, B);
     LAUNCH(kd::k_mom_diff_h, grd(D, D.ny, D.nx, D.nl), D, G, So, B);
@@ -581,21 +585,20 @@ int diffusion_scalar(lgame_gpu* c, const State& So) {
   const Dims& D = c->D;
   const Grid<double>& G = c->G;
   const DiffBuf<double>& B = c->dbuf;
-  const dim3 gs = grd(D, D.ny, D.nx, D.nl), ge = grd(D, D.ny + 1, D.nx + 1, D.nl), gv = grd(D, D.ny, D.nx, D.nl - 1);
+  const dim3 gs = grd(D, D.ny, D.nx, D.nl), ge = grd(D, D.ny + 1, D.nx + 1, D.nl);
   if (c->diff_temp_h) {
     const int vert = c->diff_temp_v ? 1 : 0;
-    LAUNCH(kd::k_grad_vert, gv, D, G, (const double*)c->temperature, c->gz);
-    LAUNCH(kd::k_diff_flux, ge, D, G, So, B, (const double*)c->temperature, (const double*)c->gz, 1, vert, c->uph,
-           c->vph, c->wph);
-    LAUNCH(kd::k_diff_div, gs, D, G, c->uph, c->vph, c->wph, vert, B.tdh);
+    LAUNCH(kd::k_diff_fluxes1, ge, D, G, So, B, (const double*)c->temperature, 1, vert, B.flx, B.fly, B.flw);
+    LAUNCH(kd::k_diff_divs1, gs, D, G, B.flx, B.fly, B.flw, vert, B.tdh);
   }
-  if (c->diff_mass_h) {
+  if (c->diff_mass_h) {  // every constituent in one launch each (1 dry, 7 moist)
     const int vert = c->diff_mass_v ? 1 : 0;
-    for (int jc = 0; jc < D.ncons; ++jc) {
-      const double* r = So.rho + (long long)jc * D.fstride;
-      LAUNCH(kd::k_grad_vert, gv, D, G, r, c->gz);
-      LAUNCH(kd::k_diff_flux, ge, D, G, So, B, r, (const double*)c->gz, 0, vert, c->uph, c->vph, c->wph);
-      LAUNCH(kd::k_diff_div, gs, D, G, c->uph, c->vph, c->wph, vert, B.mdt + (long long)jc * D.fstride);
+    if (D.ncons == 7) {
+      LAUNCH(kd::k_diff_fluxes7, ge, D, G, So, B, (const double*)So.rho, 0, vert, B.flx, B.fly, B.flw);
+      LAUNCH(kd::k_diff_divs7, gs, D, G, B.flx, B.fly, B.flw, vert, B.mdt);
+    } else {
+      LAUNCH(kd::k_diff_fluxes1, ge, D, G, So, B, (const double*)So.rho, 0, vert, B.flx, B.fly, B.flw);
+      LAUNCH(kd::k_diff_divs1, gs, D, G, B.flx, B.fly, B.flw, vert, B.mdt);
     }
   }
   return LGAME_OK;
@@ -830,10 +833,15 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     c->diff_temp_h = cfg->ltemp_diff_h; c->diff_temp_v = cfg->ltemp_diff_v;
     c->diff_mass_h = cfg->lmass_diff_h; c->diff_mass_v = cfg->lmass_diff_v;
     if (c->diff_mom_h) {
-      double** work[] = {&B.tke_new, &B.vmol, &B.nsq, &B.vz};
+      double** work[] = {&B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.zz, &B.vdiv};
       for (double** p : work) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
       if (c->diff_temp_h && (rc = dalloc(c, &B.tdh, F)) != LGAME_OK) return fail(rc);
       if (c->diff_mass_h && (rc = dalloc(c, &B.mdt, F * D.ncons)) != LGAME_OK) return fail(rc);
+      if (c->diff_temp_h || c->diff_mass_h) {
+        const size_t nf = c->diff_mass_h ? (size_t)D.ncons : 1;
+        if ((rc = dalloc(c, &B.flx, F * nf)) || (rc = dalloc(c, &B.fly, F * nf)) || (rc = dalloc(c, &B.flw, F * nf)))
+          return fail(rc);
+      }
     }
     DiffPar& P = c->dpar;
     P.eff_hor_res = std::sqrt(cfg->dx * cfg->dy);

@@ -1329,9 +1329,13 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCt
   s->diff = diff;
   if (diff.mom_h) {
     DiffBuf<float>& B = s->db;
-    float** dfl[] = {&C.tke, &C.visc, &C.mdtx, &C.mdty, &C.mdtz, &B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.tdh};
+    float** dfl[] = {&C.tke, &C.visc, &C.mdtx, &C.mdty, &C.mdtz, &B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.tdh,
+                     &B.zz, &B.vdiv};
     for (float** p : dfl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
     if ((rc = salloc(s, &B.mdt, F * D.ncons, bytes))) return fail(rc);
+    if ((rc = salloc(s, &B.flx, F * D.ncons, bytes)) || (rc = salloc(s, &B.fly, F * D.ncons, bytes)) ||
+        (rc = salloc(s, &B.flw, F * D.ncons, bytes)))
+      return fail(rc);
     B.tke = C.tke; B.visc = C.visc; B.mdtx = C.mdtx; B.mdty = C.mdty; B.mdtz = C.mdtz; B.hd = C.hdiss;
   }
   *out = s;
@@ -1623,6 +1627,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     if (rk == 1 && SD.mom_h) {
       const dim3 gs = sgrd(D.ny, D.nx, D.nl);
       SL("ks_diff_tke", (k_diff_tke<float, float>), gs, B, D, GF, Mo, DB, SD.par);
+      SL("ks_diff_zeta", (k_diff_zeta<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
       SL("ks_diff_visc", (k_diff_visc<float, float>), gs, B, D, GF, Mo, (const float*)C.temperature, DB, SD.par);
       SL("ks_diff_vz", (k_diff_vz<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
       SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
@@ -1637,22 +1642,23 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     // temperature and mass diffusion at the first substep (mo_scalar_tend_expl.F90:60-101); the
     // second substep's temperature diffusion is the same (same temperature and coefficients)
     if (rk == 1 && SD.mom_h && (SD.temp_h || SD.mass_h)) {
-      const dim3 gs = sgrd(D.ny, D.nx, D.nl), ge = sgrd(D.ny + 1, D.nx + 1, D.nl), gv = sgrd(D.ny, D.nx, D.nl - 1);
+      const dim3 gs = sgrd(D.ny, D.nx, D.nl), ge = sgrd(D.ny + 1, D.nx + 1, D.nl);
       if (SD.temp_h) {
         const int vert = SD.temp_v ? 1 : 0;
-        SL("ks_grad_vert", (k_grad_vert<float, float>), gv, B, D, GF, (const float*)C.temperature, s->gz);
-        SL("ks_diff_flux", (k_diff_flux<float, float, float>), ge, B, D, GF, Mo, DB, (const float*)C.temperature,
-           (const float*)s->gz, 1, vert, s->uph, s->vph, s->wph);
-        SL("ks_diff_div", k_diff_div<float>, gs, B, D, GF, s->uph, s->vph, s->wph, vert, DB.tdh);
+        SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)C.temperature,
+           1, vert, DB.flx, DB.fly, DB.flw);
+        SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.tdh);
       }
-      if (SD.mass_h) {
+      if (SD.mass_h) {  // every constituent in one launch each (1 dry, 7 moist)
         const int vert = SD.mass_v ? 1 : 0;
-        for (int jc = 0; jc < D.ncons; ++jc) {
-          const float* r = Mo.rho + (long long)jc * D.fstride;
-          SL("ks_grad_vert", (k_grad_vert<float, float>), gv, B, D, GF, r, s->gz);
-          SL("ks_diff_flux", (k_diff_flux<float, float, float>), ge, B, D, GF, Mo, DB, r, (const float*)s->gz, 0, vert,
-             s->uph, s->vph, s->wph);
-          SL("ks_diff_div", k_diff_div<float>, gs, B, D, GF, s->uph, s->vph, s->wph, vert, DB.mdt + (long long)jc * D.fstride);
+        if (D.ncons == 7) {
+          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 7>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho, 0,
+             vert, DB.flx, DB.fly, DB.flw);
+          SL("ks_diff_divs", (k_diff_divs<float, 7>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
+        } else {
+          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho, 0,
+             vert, DB.flx, DB.fly, DB.flw);
+          SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
         }
       }
     }
