@@ -74,8 +74,12 @@ __device__ __forceinline__ T cvt(S x) {
   else return T(x);
 }
 
+// Offset of point (i, j, k) in a field.  A field's padded extent (fstride) is below 2^31
+// (lgame_gpu_create checks it), so the offset is formed in 32-bit signed arithmetic: two
+// integer multiply-adds, and the compiler folds the offsets of neighbouring points (+-1, +-P,
+// +-plane) into one base; offsets of further fields (constituents) are added in 64 bits.
 __host__ __device__ __forceinline__ long long IX(const Dims& d, int i, int j, int k) {
-  return (long long)(i - 1) + (long long)d.P * ((long long)(j - 1) + (long long)d.NX1 * (long long)(k - 1));
+  return (long long)((i - 1) + d.P * ((j - 1) + d.NX1 * (k - 1)));
 }
 
 // grid metrics (read-only), one pointer per reference array; ipw = inner_product_weights

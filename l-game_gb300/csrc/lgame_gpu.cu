@@ -725,6 +725,11 @@ void mark_end_cb(void* p, int k) {
 int check_cfg(const lgame_config* cfg) {
   if (cfg->ny < 3 || cfg->nx < 3) return set_err(LGAME_ERR_BAD_DIMS, "ny and nx must be >= 3");
   if (cfg->n_layers < 3 || cfg->n_layers > 128) return set_err(LGAME_ERR_BAD_DIMS, "n_layers must be in 3..128");
+  {  // one field's padded extent must stay below 2^31 points (32-bit offsets within a field)
+    const long long P = ((long long)cfg->ny + 1 + 31) / 32 * 32;
+    if (P * ((long long)cfg->nx + 1) * ((long long)cfg->n_layers + 1) >= (1LL << 31))
+      return set_err(LGAME_ERR_BAD_DIMS, "the grid is too large: (ny+1 rounded up to 32)*(nx+1)*(n_layers+1) must be < 2^31");
+  }
   if (cfg->n_oro_layers < 1 || cfg->n_oro_layers >= cfg->n_layers)
     return set_err(LGAME_ERR_BAD_DIMS, "it must be 1 <= n_oro_layers < n_layers");
   if (cfg->theta_adv_order != 2 && cfg->theta_adv_order != 3)
