@@ -403,6 +403,16 @@ def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak
             "traffic": None if dram is None else dram * cells}
 
 
+def size_overrides(args) -> dict:
+    """Namelist overrides of a reduced-size run (profiling captures): nx = ny, and n_layers with
+    the orography-following layers kept at the workload's fraction."""
+    ov = {"nx": args.nx, "ny": args.ny} if args.nx else {}
+    if args.nl:
+        ov["n_layers"] = args.nl
+        ov["n_oro_layers"] = max(1, min(args.nl - 1, round(args.nl * 60 / 80)))
+    return ov
+
+
 def run_ours(args):
     import torch
     import cases
@@ -411,7 +421,7 @@ def run_ours(args):
     dist = dist_init(ws)
     peaks = read_peaks()
     t_setup = time.perf_counter()
-    n = cases.namelist(WORKLOAD, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    n = cases.namelist(WORKLOAD, **size_overrides(args))
     hm = L.HostModel(n)
     t_setup = time.perf_counter() - t_setup
     cells = n.nx * n.ny * n.n_layers
@@ -547,7 +557,7 @@ def diffusion_bench(args, results: dict) -> dict:
     share of the split step."""
     import cases
     import lgame_gpu as L
-    n = cases.namelist(WORKLOAD, **DIFF_DEFAULT, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    n = cases.namelist(WORKLOAD, **DIFF_DEFAULT, **size_overrides(args))
     hm = L.HostModel(n)
     out = {"config": "reference default &diff: all six switches on, smag/tke"}
     runs = [(L.PRECISION_SPLIT, "split", args.steps), (L.PRECISION_FP64, "fp64", min(args.steps, 3))]
@@ -597,7 +607,7 @@ def boundary_bench(args, peaks, n_swamp: int = 5, reps: int = 20) -> dict:
     import torch
     import cases
     import lgame_gpu as L
-    n = cases.namelist(WORKLOAD, lperiodic=False, **({"nx": args.nx, "ny": args.ny} if args.nx else {}))
+    n = cases.namelist(WORKLOAD, lperiodic=False, **size_overrides(args))
     hm = L.HostModel(n)
     cfg = L.config_from_namelist(n)
     cfg.precision = L.PRECISION_SPLIT
@@ -814,6 +824,7 @@ def main():
     ap.add_argument("--no-diffusion", action="store_true", help="skip the run with the default diffusion closure")
     ap.add_argument("--nx", type=int, default=0, help="override nx=ny (smaller runs for testing)")
     ap.add_argument("--ny", type=int, default=0)
+    ap.add_argument("--nl", type=int, default=0, help="override n_layers (profiling captures of column kernels)")
     args = ap.parse_args()
     if args.nx and not args.ny:
         args.ny = args.nx
