@@ -1,17 +1,19 @@
 // emulator.cu -- radiation emulator: an MLP trained and run on the GPU with hand-written
 // BF16 tensor-core kernels (tcgen05.mma, accumulators in tensor memory).
 //
-// GEMM kernel: one CTA of 128 threads computes a 128 x BN tile of C = A * B^T (A: M x K,
-// B: N x K, both K-major BF16).  The K blocks of 64 reach shared memory by TMA
+// GEMM kernel (persistent, one CTA per SM): C = A * B^T (A: M x K, B: N x K, both K-major
+// BF16) in tiles of 128 x BN.  The K blocks of 64 reach shared memory by TMA
 // (cp.async.bulk.tensor, 128-byte swizzle: 8-row x 128-byte atoms, 16-byte chunks XOR-ed by
-// the row), issued by one producer thread into a three-stage ring; one MMA thread waits for
-// a stage to fill, issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and
-// an FP32 accumulator in BN columns of tensor memory; the K=16 steps advance the descriptors
-// 32 bytes inside the swizzle atom) and commits them to the stage's "empty" mbarrier, which
-// releases it to the producer.  A last commit signals the epilogue, which reads the
-// accumulator with tcgen05.ld (warp w owns tensor-memory lanes 32w..32w+31 = tile rows) and
-// applies one of the fused epilogues (bias + GELU with BF16 and transposed BF16 copies,
-// bias only, GELU derivative for the backward pass, or plain FP32 partial sums for split-K).
+// the row), issued by a producer warp into a ring of stages; an MMA warp waits for a stage to
+// fill, issues four tcgen05.mma (M=128, N=BN, K=16, kind::f16 with BF16 inputs and an FP32
+// accumulator in tensor memory; the K=16 steps advance the descriptors 32 bytes inside the
+// swizzle atom) and commits them to the stage's "empty" mbarrier, which releases it to the
+// producer.  Two accumulators alternate between tiles: four epilogue warps read a finished one
+// with tcgen05.ld (warp w owns tensor-memory lanes 32*(w%4).. = tile rows) and apply one of the
+// fused epilogues (bias + GELU with BF16 and transposed BF16 copies, bias only, GELU derivative
+// for the backward pass, or plain FP32 partial sums for split-K) while the next tile's MMAs run.
+// Launched with programmatic stream serialisation, so a GEMM's set-up overlaps the previous
+// kernel's tail.
 //
 // Every wait on an mbarrier is bounded; on time-out the kernel records an error code, waits
 // (bounded) once more for its own tensor-core work, frees its tensor memory and returns.
@@ -128,134 +130,249 @@ __device__ __forceinline__ float gelu_grad(float z) {
 }
 
 // ---- the GEMM -------------------------------------------------------------------------------
-constexpr int kStages = 3;
+// Persistent: one CTA per SM loops over the output tiles (tile t, t + gridDim.x, ...), with the
+// warps specialised:
+//   warp 0 (lane 0)  TMA producer: the K blocks of every tile of the CTA into a ring of stages,
+//                    running ahead across tile boundaries;
+//   warp 1 (lane 0)  MMA issuer: four tcgen05.mma per K block into one of two accumulators in
+//                    tensor memory, alternating per tile; the stage is released by a commit to its
+//                    "empty" barrier, the finished accumulator by a commit to its "full" barrier;
+//   warps 2-5        epilogue: warp w reads tensor-memory lanes 32*(w%4).. (tile rows) of the
+//                    finished accumulator, applies the fused epilogue, and arrives on the
+//                    accumulator's "empty" barrier, so that the MMAs of the next tile run while
+//                    the previous one drains.
+// Every wait is bounded and also ends when another role has given up (a shared abort flag);
+// the CTA then waits (bounded) for its own copies and MMAs before freeing tensor memory.
+constexpr int kGemmThreads = 192;
 
 template <int BN>
-__global__ void __launch_bounds__(128, 1) k_gemm(const __grid_constant__ CUtensorMap tmA,
-                                                 const __grid_constant__ CUtensorMap tmB, int M, int N, int K,
-                                                 int kchunk, Epi ep, int* err) {
-  constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;
-  constexpr uint32_t kA = 128 * 64 * 2, kB = BN * 64 * 2, kStage = kA + kB;  // bytes per stage
+struct GemmCfg {
+  static constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;  // one accumulator
+  static constexpr uint32_t kA = 128 * 64 * 2, kB = BN * 64 * 2, kStage = kA + kB;             // bytes per stage
+  static constexpr int kStages = (BN <= 128) ? 6 : 4;
+  static constexpr size_t kSmem = (size_t)kStages * kStage + 1024;  // + alignment slack of the swizzle atoms
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint32_t mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// bounded wait that also gives up once *abort is set
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parity, const volatile int* abort) {
+  for (int it = 0; it < (1 << 22); ++it) {
+    if (mbar_test(mbar, parity)) return true;
+    if (it > 64) {
+      if (*abort) return false;
+      __nanosleep(64);
+    }
+  }
+  return false;
+}
+
+// the fused epilogue of 16 accumulator columns (nb..nb+15) of tile row m, split z
+__device__ __forceinline__ void epilogue16(const Epi& ep, int m, int nb, int z, float* v) {
+  switch (ep.kind) {
+    case kEpiF32:
+    case kEpiBias: {
+      float4* out = reinterpret_cast<float4*>(ep.c + (ep.kind == kEpiF32 ? (size_t)z * ep.split_stride : 0) +
+                                              (size_t)m * ep.ldc + nb);
+      if (ep.kind == kEpiBias)
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] += ep.bias[nb + j];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      break;
+    }
+    case kEpiBiasGelu:
+    case kEpiGeluBwd: {
+      float zz[16];
+      if (ep.kind == kEpiBiasGelu) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) zz[j] = v[j] + ep.bias[nb + j];
+      } else {
+        const float4* zp = reinterpret_cast<const float4*>(ep.zprev + (size_t)m * ep.ldc + nb);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 t = zp[q];
+          zz[4 * q] = v[4 * q] * gelu_grad(t.x);
+          zz[4 * q + 1] = v[4 * q + 1] * gelu_grad(t.y);
+          zz[4 * q + 2] = v[4 * q + 2] * gelu_grad(t.z);
+          zz[4 * q + 3] = v[4 * q + 3] * gelu_grad(t.w);
+        }
+      }
+      float4* zo = reinterpret_cast<float4*>(ep.c + (size_t)m * ep.ldc + nb);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) zo[q] = make_float4(zz[4 * q], zz[4 * q + 1], zz[4 * q + 2], zz[4 * q + 3]);
+      __align__(16) bf16 hb[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(ep.kind == kEpiBiasGelu ? gelu(zz[j]) : zz[j]);
+      uint4* ho = reinterpret_cast<uint4*>(ep.h + (size_t)m * ep.ldh + nb);
+      ho[0] = reinterpret_cast<const uint4*>(hb)[0];
+      ho[1] = reinterpret_cast<const uint4*>(hb)[1];
+      // the transposed BF16 copy element-wise, coalesced across the warp's rows
+#pragma unroll
+      for (int j = 0; j < 16; ++j) ep.ht[(size_t)(nb + j) * ep.ldt + m] = hb[j];
+      break;
+    }
+    default: break;
+  }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant__ CUtensorMap tmA,
+                                                          const __grid_constant__ CUtensorMap tmB, int K, int kchunk,
+                                                          int tiles_n, int tiles_m, int splits, Epi ep, int* err) {
+  using Cfg = GemmCfg<BN>;
+  constexpr int S = Cfg::kStages;
+  constexpr uint32_t kCols = Cfg::kCols, kA = Cfg::kA, kStage = Cfg::kStage;
   extern __shared__ uint8_t smem_raw[];
-  __shared__ uint64_t full[kStages], empty[kStages], done;
+  __shared__ uint64_t full[S], empty[S], acc_full[2], acc_empty[2], done;
   __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  const volatile int* abort_v = &abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * 128;
-  const int k0 = blockIdx.z * kchunk, k1 = min(K, k0 + kchunk);
-  const int nk = (k1 - k0) / 64;
+  const int ntiles = tiles_n * tiles_m * splits;
   const uint32_t sbase = (smem_u32(smem_raw) + 1023u) & ~1023u;  // swizzle atoms are 1024-byte aligned
-  if (warp == 0) tc_alloc(smem_u32(&tmem_base), kCols);
+  // launched with programmatic stream serialisation: the next kernel of the stream may be
+  // scheduled now (it waits for this grid's completion before touching memory), and this
+  // grid's set-up below overlaps the previous kernel's tail until griddepcontrol.wait
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   if (tid == 0) {
-    for (int i = 0; i < kStages; ++i) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmA) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmB) : "memory");
+  }
+  if (warp == 0) tc_alloc(smem_u32(&tmem_base), 2 * kCols);
+  if (tid == 0) {
+    for (int i = 0; i < S; ++i) {
       mbar_init(smem_u32(&full[i]), 1);
       mbar_init(smem_u32(&empty[i]), 1);
     }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(smem_u32(&acc_full[i]), 1);
+      mbar_init(smem_u32(&acc_empty[i]), 4);  // one arrival per epilogue warp
+    }
     mbar_init(smem_u32(&done), 1);
+    abort_flag = 0;
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  // the previous kernel's results (A, B, bias, the epilogue's inputs) are complete and visible,
+  // and its reads of what this grid writes are done
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const uint32_t tmem = tmem_base;
+  // tile t: n tile fastest, so the CTAs that run at the same time share an A tile through L2
+  auto tile_of = [&](int t, int* tn, int* tm, int* z) {
+    *tn = t % tiles_n;
+    const int r = t / tiles_n;
+    *tm = r % tiles_m;
+    *z = r / tiles_m;
+  };
+  auto nk_of = [&](int z) { const int k0 = z * kchunk; return (min(K, k0 + kchunk) - k0) / 64; };
   bool failed = false;
-  if (warp == 0 && lane == 0) {
-    // producer: K block it into stage it % kStages once the MMAs of block it - kStages released it
-    int issued = 0;
-    for (; issued < nk; ++issued) {
-      const int st = issued % kStages;
-      if (issued >= kStages && !mbar_wait(smem_u32(&empty[st]), (uint32_t)((issued / kStages - 1) & 1))) {
-        failed = true;
-        break;
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;  // K blocks issued, over all tiles
+      for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x) {
+        int tn, tm, z;
+        tile_of(t, &tn, &tm, &z);
+        const int nk = nk_of(z), k0 = z * kchunk;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int st = it % S;
+          if (it >= S && !mbar_wait_or_abort(smem_u32(&empty[st]), (uint32_t)((it / S - 1) & 1), abort_v)) {
+            failed = true;
+            break;
+          }
+          const uint32_t a = sbase + st * kStage;
+          mbar_arrive_expect_tx(smem_u32(&full[st]), kStage);
+          tma_load_2d(a, &tmA, k0 + 64 * kb, tm * 128, smem_u32(&full[st]));
+          tma_load_2d(a + kA, &tmB, k0 + 64 * kb, tn * BN, smem_u32(&full[st]));
+        }
       }
-      const uint32_t a = sbase + st * kStage;
-      mbar_arrive_expect_tx(smem_u32(&full[st]), kStage);
-      tma_load_2d(a, &tmA, k0 + 64 * issued, m0, smem_u32(&full[st]));
-      tma_load_2d(a + kA, &tmB, k0 + 64 * issued, n0, smem_u32(&full[st]));
+      if (failed) {
+        abort_flag = 1;
+        // the copies still in flight land before the CTA exits (bounded)
+        for (int j = max(0, it - S); j < it; ++j) mbar_wait(smem_u32(&full[j % S]), (uint32_t)((j / S) & 1));
+      }
     }
-    // after a time-out, wait (bounded) for the copies still in flight before the CTA exits
-    if (failed)
-      for (int it = max(0, issued - kStages); it < issued; ++it)
-        mbar_wait(smem_u32(&full[it % kStages]), (uint32_t)((it / kStages) & 1));
-  } else if (warp == 1 && lane == 0) {
-    // MMA thread: four K=16 steps per block, the block's stage released by its commit
-    const uint32_t idesc = instr_desc(128, BN);
-    for (int it = 0; it < nk; ++it) {
-      const int st = it % kStages;
-      if (!mbar_wait(smem_u32(&full[st]), (uint32_t)((it / kStages) & 1))) {
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(128, BN);
+      int it = 0, lt = 0;  // K blocks consumed, tiles of this CTA
+      for (int t = blockIdx.x; t < ntiles && !failed; t += gridDim.x, ++lt) {
+        int tn, tm, z;
+        tile_of(t, &tn, &tm, &z);
+        const int nk = nk_of(z), b = lt & 1;
+        // the accumulator's previous tile (lt - 2) must have been read out
+        if (lt >= 2 && !mbar_wait_or_abort(smem_u32(&acc_empty[b]), (uint32_t)((lt / 2 - 1) & 1), abort_v)) {
+          failed = true;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)b * kCols;
+        for (int kb = 0; kb < nk; ++kb, ++it) {
+          const int st = it % S;
+          if (!mbar_wait_or_abort(smem_u32(&full[st]), (uint32_t)((it / S) & 1), abort_v)) {
+            failed = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a = sbase + st * kStage;
+#pragma unroll
+          for (int s = 0; s < 4; ++s)
+            tc_mma(acc, smem_desc_sw128(a + s * 32), smem_desc_sw128(a + kA + s * 32), idesc,
+                   (kb > 0 || s > 0) ? 1u : 0u);
+          tc_commit(smem_u32(&empty[st]));
+        }
+        if (failed) break;
+        tc_commit(smem_u32(&acc_full[b]));
+      }
+      if (failed) abort_flag = 1;
+      // arrives once every tensor-core operation issued above has completed (also after a failure)
+      tc_commit(smem_u32(&done));
+    }
+  } else {
+    const int qw = warp & 3;  // tensor-memory lanes 32*qw.. = tile rows
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      int tn, tm, z;
+      tile_of(t, &tn, &tm, &z);
+      const int b = lt & 1;
+      bool ok = mbar_wait_or_abort(smem_u32(&acc_full[b]), (uint32_t)((lt / 2) & 1), abort_v);
+      ok = __all_sync(0xffffffffu, ok);  // the tensor-memory loads below need the whole warp
+      if (!ok) {
         failed = true;
         break;
       }
       tc_fence_after();
-      const uint32_t a = sbase + st * kStage;
-#pragma unroll
-      for (int s = 0; s < 4; ++s)
-        tc_mma(tmem, smem_desc_sw128(a + s * 32), smem_desc_sw128(a + kA + s * 32), idesc, (it > 0 || s > 0) ? 1u : 0u);
-      tc_commit(smem_u32(&empty[st]));
+      const int m = tm * 128 + qw * 32 + lane;
+      for (int c = 0; c < BN; c += 16) {
+        float v[16];
+        tc_ld16(tmem + (uint32_t)b * kCols + ((uint32_t)(qw * 32) << 16) + (uint32_t)c, v);
+        epilogue16(ep, m, tn * BN + c, z, v);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&acc_empty[b]));
     }
-    // arrives once every tensor-core operation issued above has completed (also after a failure)
-    tc_commit(smem_u32(&done));
+    if (failed && lane == 0) abort_flag = 1;
   }
   __syncwarp();
   const bool ok = mbar_wait(smem_u32(&done), 0);
   tc_fence_after();
-  if (__syncthreads_or(failed || !ok)) {
-    if (tid == 0) atomicExch(err, 1);
-  } else {
-    const int m = m0 + warp * 32 + lane;  // tile row of this thread
-    for (int c = 0; c < BN; c += 16) {
-      float v[16];
-      tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, v);
-      const int nb = n0 + c;
-      // row-major outputs as 16-byte vector stores (16 FP32 = 4 x float4, 16 BF16 = 2 x uint4);
-      // the transposed BF16 copies are written element-wise, coalesced across the warp's rows
-      switch (ep.kind) {
-        case kEpiF32:
-        case kEpiBias: {
-          float4* out = reinterpret_cast<float4*>(ep.c + (ep.kind == kEpiF32 ? (size_t)blockIdx.z * ep.split_stride : 0) +
-                                                  (size_t)m * ep.ldc + nb);
-          if (ep.kind == kEpiBias)
-#pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] += ep.bias[nb + j];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-          break;
-        }
-        case kEpiBiasGelu:
-        case kEpiGeluBwd: {
-          float z[16];
-          if (ep.kind == kEpiBiasGelu) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) z[j] = v[j] + ep.bias[nb + j];
-          } else {
-            const float4* zp = reinterpret_cast<const float4*>(ep.zprev + (size_t)m * ep.ldc + nb);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              const float4 t = zp[q];
-              z[4 * q] = v[4 * q] * gelu_grad(t.x);
-              z[4 * q + 1] = v[4 * q + 1] * gelu_grad(t.y);
-              z[4 * q + 2] = v[4 * q + 2] * gelu_grad(t.z);
-              z[4 * q + 3] = v[4 * q + 3] * gelu_grad(t.w);
-            }
-          }
-          float4* zo = reinterpret_cast<float4*>(ep.c + (size_t)m * ep.ldc + nb);
-#pragma unroll
-          for (int q = 0; q < 4; ++q) zo[q] = make_float4(z[4 * q], z[4 * q + 1], z[4 * q + 2], z[4 * q + 3]);
-          __align__(16) bf16 hb[16];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(ep.kind == kEpiBiasGelu ? gelu(z[j]) : z[j]);
-          uint4* ho = reinterpret_cast<uint4*>(ep.h + (size_t)m * ep.ldh + nb);
-          ho[0] = reinterpret_cast<const uint4*>(hb)[0];
-          ho[1] = reinterpret_cast<const uint4*>(hb)[1];
-#pragma unroll
-          for (int j = 0; j < 16; ++j) ep.ht[(size_t)(nb + j) * ep.ldt + m] = hb[j];
-          break;
-        }
-        default: break;
-      }
-    }
-  }
+  if (__syncthreads_or(failed || !ok) && tid == 0) atomicExch(err, 1);
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc_dealloc(tmem, kCols);
+  if (warp == 0) tc_dealloc(tmem, 2 * kCols);
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no link to the driver library)
@@ -291,10 +408,14 @@ int tensor_map(CUtensorMap* map, const bf16* base, int rows, int K, int ld, int 
 template <int BN>
 int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
                    int* err, cudaStream_t st) {
-  const size_t shm = kStages * ((size_t)128 * 64 * 2 + (size_t)BN * 64 * 2) + 1024;  // + alignment slack
+  const size_t shm = GemmCfg<BN>::kSmem;
   static bool attr_set = false;
+  static int nsm = 0;
   if (!attr_set) {
     if (cudaFuncSetAttribute(k_gemm<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+      return LGAME_ERR_CUDA;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return LGAME_ERR_CUDA;
     attr_set = true;
   }
@@ -303,20 +424,36 @@ int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N,
   if (rc == LGAME_OK) rc = tensor_map(&mb, B, N, K, ldb, BN);
   if (rc != LGAME_OK) return rc;
   const int kchunk = ((K / splits + 63) / 64) * 64;
-  const dim3 grid((unsigned)(N / BN), (unsigned)(M / 128), (unsigned)((K + kchunk - 1) / kchunk));
-  k_gemm<BN><<<grid, 128, shm, st>>>(ma, mb, M, N, K, kchunk, ep, err);
+  const int zs = (K + kchunk - 1) / kchunk;
+  const int tiles_n = N / BN, tiles_m = M / 128;
+  const long long ntiles = (long long)tiles_n * tiles_m * zs;
+  const int grid = (int)std::min<long long>(ntiles, nsm);
+  // programmatic dependent launch: see griddepcontrol in k_gemm
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(kGemmThreads);
+  cfg.dynamicSmemBytes = shm;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, k_gemm<BN>, ma, mb, K, kchunk, tiles_n, tiles_m, zs, ep, err) != cudaSuccess)
+    return LGAME_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
 }
 
 int launch_gemm(const bf16* A, int lda, const bf16* B, int ldb, int M, int N, int K, int splits, const Epi& ep,
                 int* err, cudaStream_t st) {
   if (M % 128 || K % 64 || N % 64 || splits < 1) return LGAME_ERR_INVALID_ARG;
-  // the widest tile that still gives at least one CTA per SM (152), else the narrowest
+  // the widest tile that still gives about two thirds of the SMs a tile (wider tiles issue
+  // fuller MMAs and move fewer operand bytes from L2), else the narrowest
   const long long tiles_m = (long long)(M / 128) * splits;
   const int cand[4] = {256, 192, 128, 64};
   int bn = 0;
   for (int c : cand)
-    if (N % c == 0 && tiles_m * (N / c) >= 152) { bn = c; break; }
+    if (N % c == 0 && tiles_m * (N / c) >= 100) { bn = c; break; }
   if (!bn)
     for (int c : {64, 128, 192, 256})
       if (N % c == 0) { bn = c; break; }
