@@ -62,6 +62,11 @@ def emulator_bench(peaks: dict, nlev: int = 80, hidden: int = 512, batch: int = 
     gemm_bytes = 2.0 * (batch * hidden + hidden * hidden) + 4.0 * batch * hidden
     t_tensor = 2.0 * batch * hidden * hidden / (peaks["bf16_tflops"] * 1e12)
     t_hbm = gemm_bytes / (peaks["hbm_gbs"] * 1e9)
+    # the same layer over the 65,536-row chunks inference streams (several tiles per SM)
+    ml = 65536
+    ms_l = emu.time_gemm(ml, hidden, hidden, reps=20)
+    bytes_l = 2.0 * (ml * hidden + hidden * hidden) + 4.0 * ml * hidden
+    roof_l = max(2.0 * ml * hidden * hidden / (peaks["bf16_tflops"] * 1e12), bytes_l / (peaks["hbm_gbs"] * 1e9))
     rng = np.random.default_rng(0)
     nin, nout = 4 * nlev + 2, 2 * nlev
     x = rng.normal(size=(8 * batch, nin)).astype(np.float32)
@@ -89,6 +94,9 @@ def emulator_bench(peaks: dict, nlev: int = 80, hidden: int = 512, batch: int = 
                      "frac": tflops / peaks["bf16_tflops"], "peak_src": peaks["src"] + " (burst)",
                      "hbm_bytes": gemm_bytes, "roofline_ms": max(t_tensor, t_hbm) * 1e3,
                      "frac_of_roofline": max(t_tensor, t_hbm) * 1e3 / ms},
+            "gemm_large": {"m": ml, "n": hidden, "k": hidden, "avg_launch_ms": ms_l,
+                           "achieved_tflops": 2.0 * ml * hidden * hidden / (ms_l * 1e-3) / 1e12,
+                           "hbm_bytes": bytes_l, "roofline_ms": roof_l * 1e3, "frac_of_roofline": roof_l * 1e3 / ms_l},
             "training_columns_per_s": 3 * 8 * batch / dt, "training_tflops_whole_step": flop / dt / 1e12,
             "inference_columns_per_s": ni / di,
             "inference_note": "page-locked host features in, heating rates out, accessed by the GPU directly"}

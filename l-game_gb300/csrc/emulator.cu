@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -150,8 +151,21 @@ struct GemmCfg {
   static constexpr uint32_t kCols = (BN <= 32) ? 32 : (BN <= 64) ? 64 : (BN <= 128) ? 128 : 256;  // one accumulator
   static constexpr uint32_t kA = 128 * 64 * 2, kB = BN * 64 * 2, kStage = kA + kB;             // bytes per stage
   static constexpr int kStages = (BN <= 128) ? 6 : 4;
-  static constexpr size_t kSmem = (size_t)kStages * kStage + 1024;  // + alignment slack of the swizzle atoms
+  // per epilogue warp a 32 x 32 FP32 staging tile (4 KB, 128-byte swizzle) for the TMA store
+  static constexpr uint32_t kStg = 32 * 32 * 4;
+  static constexpr size_t kSmem = (size_t)kStages * kStage + 4 * kStg + 1024;  // + alignment slack of the atoms
 };
+
+// TMA tensor store of a 3-D box from shared memory (bulk group), and its completion waits
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, uint32_t src, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(map), "r"(c0),
+               "r"(c1), "r"(c2), "r"(src)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(mbar) : "memory");
@@ -178,43 +192,37 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parit
   return false;
 }
 
-// the fused epilogue of 16 accumulator columns (nb..nb+15) of tile row m, split z
-__device__ __forceinline__ void epilogue16(const Epi& ep, int m, int nb, int z, float* v) {
+// the fused epilogue of 16 accumulator columns (nb..nb+15) of tile row m: the FP32 output
+// values into f (stored by the caller), the BF16 outputs written here
+__device__ __forceinline__ void epilogue16(const Epi& ep, int m, int nb, const float* v, float* f) {
   switch (ep.kind) {
     case kEpiF32:
-    case kEpiBias: {
-      float4* out = reinterpret_cast<float4*>(ep.c + (ep.kind == kEpiF32 ? (size_t)z * ep.split_stride : 0) +
-                                              (size_t)m * ep.ldc + nb);
-      if (ep.kind == kEpiBias)
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] += ep.bias[nb + j];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) out[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+      for (int j = 0; j < 16; ++j) f[j] = v[j];
       break;
-    }
+    case kEpiBias:
+#pragma unroll
+      for (int j = 0; j < 16; ++j) f[j] = v[j] + ep.bias[nb + j];
+      break;
     case kEpiBiasGelu:
     case kEpiGeluBwd: {
-      float zz[16];
       if (ep.kind == kEpiBiasGelu) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) zz[j] = v[j] + ep.bias[nb + j];
+        for (int j = 0; j < 16; ++j) f[j] = v[j] + ep.bias[nb + j];
       } else {
         const float4* zp = reinterpret_cast<const float4*>(ep.zprev + (size_t)m * ep.ldc + nb);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const float4 t = zp[q];
-          zz[4 * q] = v[4 * q] * gelu_grad(t.x);
-          zz[4 * q + 1] = v[4 * q + 1] * gelu_grad(t.y);
-          zz[4 * q + 2] = v[4 * q + 2] * gelu_grad(t.z);
-          zz[4 * q + 3] = v[4 * q + 3] * gelu_grad(t.w);
+          f[4 * q] = v[4 * q] * gelu_grad(t.x);
+          f[4 * q + 1] = v[4 * q + 1] * gelu_grad(t.y);
+          f[4 * q + 2] = v[4 * q + 2] * gelu_grad(t.z);
+          f[4 * q + 3] = v[4 * q + 3] * gelu_grad(t.w);
         }
       }
-      float4* zo = reinterpret_cast<float4*>(ep.c + (size_t)m * ep.ldc + nb);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) zo[q] = make_float4(zz[4 * q], zz[4 * q + 1], zz[4 * q + 2], zz[4 * q + 3]);
       __align__(16) bf16 hb[16];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(ep.kind == kEpiBiasGelu ? gelu(zz[j]) : zz[j]);
+      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(ep.kind == kEpiBiasGelu ? gelu(f[j]) : f[j]);
       uint4* ho = reinterpret_cast<uint4*>(ep.h + (size_t)m * ep.ldh + nb);
       ho[0] = reinterpret_cast<const uint4*>(hb)[0];
       ho[1] = reinterpret_cast<const uint4*>(hb)[1];
@@ -229,7 +237,8 @@ __device__ __forceinline__ void epilogue16(const Epi& ep, int m, int nb, int z, 
 
 template <int BN>
 __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant__ CUtensorMap tmA,
-                                                          const __grid_constant__ CUtensorMap tmB, int K, int kchunk,
+                                                          const __grid_constant__ CUtensorMap tmB,
+                                                          const __grid_constant__ CUtensorMap tmC, int K, int kchunk,
                                                           int tiles_n, int tiles_m, int splits, Epi ep, int* err) {
   using Cfg = GemmCfg<BN>;
   constexpr int S = Cfg::kStages;
@@ -249,6 +258,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant_
   if (tid == 0) {
     asm volatile("prefetch.tensormap [%0];" ::"l"(&tmA) : "memory");
     asm volatile("prefetch.tensormap [%0];" ::"l"(&tmB) : "memory");
+    asm volatile("prefetch.tensormap [%0];" ::"l"(&tmC) : "memory");
   }
   if (warp == 0) tc_alloc(smem_u32(&tmem_base), 2 * kCols);
   if (tid == 0) {
@@ -342,6 +352,9 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant_
     }
   } else {
     const int qw = warp & 3;  // tensor-memory lanes 32*qw.. = tile rows
+    // this warp's staging tile, after the stages (1024-byte aligned: 128-byte swizzle atoms)
+    const uint32_t stg = sbase + (uint32_t)S * kStage + (uint32_t)qw * Cfg::kStg;
+    uint8_t* stg_ptr = smem_raw + (stg - smem_u32(smem_raw));
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
       int tn, tm, z;
@@ -354,17 +367,36 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant_
         break;
       }
       tc_fence_after();
-      const int m = tm * 128 + qw * 32 + lane;
-      for (int c = 0; c < BN; c += 16) {
-        float v[16];
-        tc_ld16(tmem + (uint32_t)b * kCols + ((uint32_t)(qw * 32) << 16) + (uint32_t)c, v);
-        epilogue16(ep, m, tn * BN + c, z, v);
+      const int m0 = tm * 128 + qw * 32, m = m0 + lane;
+      for (int c = 0; c < BN; c += 32) {
+        float v[32], f[32];
+        const uint32_t ta = tmem + (uint32_t)b * kCols + ((uint32_t)(qw * 32) << 16) + (uint32_t)c;
+        tc_ld16(ta, v);
+        tc_ld16(ta + 16, v + 16);
+        const int nb = tn * BN + c;
+        epilogue16(ep, m, nb, v, f);
+        epilogue16(ep, m, nb + 16, v + 16, f + 16);
+        // the FP32 values through the staging tile: row `lane` in the 128-byte swizzle (its
+        // 16-byte chunk j at position j ^ (row % 8), so the warp's stores hit distinct banks),
+        // then one TMA store of the 32 x 32 box; the previous box's read of the tile first
+        if (lane == 0) bulk_wait_read0();
+        __syncwarp();
+        float4* row = reinterpret_cast<float4*>(stg_ptr + lane * 128);
+#pragma unroll
+        for (int j = 0; j < 8; ++j) row[j ^ (lane & 7)] = make_float4(f[4 * j], f[4 * j + 1], f[4 * j + 2], f[4 * j + 3]);
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          tma_store_3d(&tmC, stg, nb, m0, ep.kind == kEpiF32 ? z : 0);
+          bulk_commit();
+        }
       }
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&acc_empty[b]));
     }
     if (failed && lane == 0) abort_flag = 1;
+    if (lane == 0) bulk_wait0();  // the tensor stores complete before the CTA exits
   }
   __syncwarp();
   const bool ok = mbar_wait(smem_u32(&done), 0);
@@ -390,19 +422,56 @@ EncodeTiledFn encode_tiled() {
   }
   return fn;
 }
+// encoded tensor maps, kept by their parameters: the training and inference loops use the same
+// few buffers again and again, and encoding costs host time on every launch otherwise
+struct MapKey {
+  const void* base;
+  int dtype, rank;
+  cuuint64_t dims[3], strides[2];
+  cuuint32_t box[3];
+  bool operator==(const MapKey& o) const { return std::memcmp(this, &o, sizeof(MapKey)) == 0; }
+};
+int encode_cached(CUtensorMap* map, const MapKey& k) {
+  static std::mutex mu;
+  static std::vector<std::pair<MapKey, CUtensorMap>> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& e : cache)
+    if (e.first == k) { *map = e.second; return LGAME_OK; }
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return LGAME_ERR_CUDA;
+  const cuuint32_t estride[3] = {1u, 1u, 1u};
+  const CUresult r = enc(map, (CUtensorMapDataType)k.dtype, (cuuint32_t)k.rank, (void*)k.base, k.dims, k.strides, k.box,
+                         estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return LGAME_ERR_INVALID_ARG;
+  if (cache.size() >= 256) cache.erase(cache.begin());
+  cache.emplace_back(k, *map);
+  return LGAME_OK;
+}
 // tensor map of a K-major BF16 matrix (rows x K, leading dimension ld elements) in boxes of
 // 64 (K) x box_rows with the 128-byte swizzle; the encoder rejects unaligned bases and strides
 int tensor_map(CUtensorMap* map, const bf16* base, int rows, int K, int ld, int box_rows) {
-  const EncodeTiledFn enc = encode_tiled();
-  if (!enc) return LGAME_ERR_CUDA;
-  const cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-  const cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(bf16)};
-  const cuuint32_t box[2] = {64u, (cuuint32_t)box_rows};
-  const cuuint32_t estride[2] = {1u, 1u};
-  const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides, box, estride,
-                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? LGAME_OK : LGAME_ERR_INVALID_ARG;
+  MapKey k{};
+  k.base = base;
+  k.dtype = CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+  k.rank = 2;
+  k.dims[0] = (cuuint64_t)K; k.dims[1] = (cuuint64_t)rows;
+  k.strides[0] = (cuuint64_t)ld * sizeof(bf16);
+  k.box[0] = 64u; k.box[1] = (cuuint32_t)box_rows;
+  return encode_cached(map, k);
+}
+// tensor map of the FP32 output: columns x rows x splits (leading dimension ldc elements, split
+// stride elements) in 32 x 32 x 1 boxes with the 128-byte swizzle (the epilogue's staging tile)
+int tensor_map_c(CUtensorMap* map, const float* base, int cols, int rows, int splits, int ldc, long long split_stride) {
+  MapKey k{};
+  k.base = base;
+  k.dtype = CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  k.rank = 3;
+  k.dims[0] = (cuuint64_t)cols; k.dims[1] = (cuuint64_t)rows; k.dims[2] = (cuuint64_t)splits;
+  k.strides[0] = (cuuint64_t)ldc * sizeof(float);
+  k.strides[1] = (cuuint64_t)(splits > 1 ? split_stride : (long long)ldc * rows) * sizeof(float);
+  k.box[0] = 32u; k.box[1] = 32u; k.box[2] = 1u;
+  return encode_cached(map, k);
 }
 
 template <int BN>
@@ -419,12 +488,13 @@ int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N,
       return LGAME_ERR_CUDA;
     attr_set = true;
   }
-  CUtensorMap ma, mb;
-  int rc = tensor_map(&ma, A, M, K, lda, 128);
-  if (rc == LGAME_OK) rc = tensor_map(&mb, B, N, K, ldb, BN);
-  if (rc != LGAME_OK) return rc;
+  CUtensorMap ma, mb, mc;
   const int kchunk = ((K / splits + 63) / 64) * 64;
   const int zs = (K + kchunk - 1) / kchunk;
+  int rc = tensor_map(&ma, A, M, K, lda, 128);
+  if (rc == LGAME_OK) rc = tensor_map(&mb, B, N, K, ldb, BN);
+  if (rc == LGAME_OK) rc = tensor_map_c(&mc, ep.c, N, M, ep.kind == kEpiF32 ? zs : 1, ep.ldc, ep.split_stride);
+  if (rc != LGAME_OK) return rc;
   const int tiles_n = N / BN, tiles_m = M / 128;
   const long long ntiles = (long long)tiles_n * tiles_m * zs;
   const int grid = (int)std::min<long long>(ntiles, nsm);
@@ -439,7 +509,7 @@ int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N,
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, k_gemm<BN>, ma, mb, K, kchunk, tiles_n, tiles_m, zs, ep, err) != cudaSuccess)
+  if (cudaLaunchKernelEx(&cfg, k_gemm<BN>, ma, mb, mc, K, kchunk, tiles_n, tiles_m, zs, ep, err) != cudaSuccess)
     return LGAME_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? LGAME_OK : LGAME_ERR_CUDA;
 }
