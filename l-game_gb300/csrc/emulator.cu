@@ -204,6 +204,15 @@ __device__ __forceinline__ void epilogue16(const Epi& ep, int m, int nb, const f
 #pragma unroll
       for (int j = 0; j < 16; ++j) f[j] = v[j] + ep.bias[nb + j];
       break;
+    case kEpiBiasGeluH: {
+      __align__(16) bf16 hb[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(v[j] + ep.bias[nb + j]));
+      uint4* ho = reinterpret_cast<uint4*>(ep.h + (size_t)m * ep.ldh + nb);
+      ho[0] = reinterpret_cast<const uint4*>(hb)[0];
+      ho[1] = reinterpret_cast<const uint4*>(hb)[1];
+      break;
+    }
     case kEpiBiasGelu:
     case kEpiGeluBwd: {
       if (ep.kind == kEpiBiasGelu) {
@@ -376,6 +385,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) k_gemm(const __grid_constant_
         const int nb = tn * BN + c;
         epilogue16(ep, m, nb, v, f);
         epilogue16(ep, m, nb + 16, v + 16, f + 16);
+        if (ep.kind == kEpiBiasGeluH) continue;  // no FP32 output
         // the FP32 values through the staging tile: row `lane` in the 128-byte swizzle (its
         // 16-byte chunk j at position j ^ (row % 8), so the warp's stores hit distinct banks),
         // then one TMA store of the 32 x 32 box; the previous box's read of the tile first
@@ -493,7 +503,10 @@ int launch_gemm_bn(const bf16* A, int lda, const bf16* B, int ldb, int M, int N,
   const int zs = (K + kchunk - 1) / kchunk;
   int rc = tensor_map(&ma, A, M, K, lda, 128);
   if (rc == LGAME_OK) rc = tensor_map(&mb, B, N, K, ldb, BN);
-  if (rc == LGAME_OK) rc = tensor_map_c(&mc, ep.c, N, M, ep.kind == kEpiF32 ? zs : 1, ep.ldc, ep.split_stride);
+  if (rc == LGAME_OK) {
+    if (ep.kind == kEpiBiasGeluH) mc = ma;  // no FP32 output; the map is not used
+    else rc = tensor_map_c(&mc, ep.c, N, M, ep.kind == kEpiF32 ? zs : 1, ep.ldc, ep.split_stride);
+  }
   if (rc != LGAME_OK) return rc;
   const int tiles_n = N / BN, tiles_m = M / 128;
   const long long ntiles = (long long)tiles_n * tiles_m * zs;
@@ -553,6 +566,7 @@ __global__ void __launch_bounds__(256) k_prep_x(const float* __restrict__ x, int
     X[(size_t)r * nin_pad + c] = b;
     t[j][threadIdx.x] = b;
   }
+  if (!XT) return;  // inference: no transposed copy (only the backward pass reads it)
   __syncthreads();
   for (int j = threadIdx.y; j < 32; j += 8)
     XT[(size_t)(blockIdx.x * 32 + j) * batch + r0 + threadIdx.x] = t[threadIdx.x][j];
@@ -766,13 +780,15 @@ int gemm(lgame_emu* e, const bf16* A, int lda, const bf16* B, int ldb, int M, in
 }
 
 // forward pass of `batch` prepared rows (X, XT); output Y (standardised, padded)
-int forward(lgame_emu* e, int batch) {
+// infer: only the BF16 activations each layer feeds the next (no FP32 pre-activations and
+// no transposed copies, which only the backward pass reads)
+int forward(lgame_emu* e, int batch, bool infer = false) {
   const int Hd = e->hidden;
   const bf16* in = e->X;
   int ldin = e->nin_pad;
   for (int l = 0; l < 3; ++l) {
     Epi ep{};
-    ep.kind = kEpiBiasGelu;
+    ep.kind = infer ? kEpiBiasGeluH : kEpiBiasGelu;
     ep.bias = e->b[l];
     ep.c = e->Z[l];
     ep.ldc = Hd;
@@ -795,9 +811,10 @@ int forward(lgame_emu* e, int batch) {
 
 // prepared inputs of `batch` rows (a multiple of 128) from raw rows the GPU can read (device
 // memory or page-locked host memory), of which the first `valid` hold data
-int prep_x(lgame_emu* e, const float* xraw_dev, int batch, int valid) {
+int prep_x(lgame_emu* e, const float* xraw_dev, int batch, int valid, bool infer = false) {
   k_prep_x<<<dim3(e->nin_pad / 32, batch / 32), dim3(32, 8), 0, e->st>>>(xraw_dev, e->nin, e->nin_pad, batch, valid,
-                                                                        e->xmean, e->xistd, e->X, e->XT);
+                                                                        e->xmean, e->xistd, e->X,
+                                                                        infer ? nullptr : e->XT);
   ECK(cudaGetLastError());
   return LGAME_OK;
 }
@@ -905,9 +922,9 @@ int infer_device(lgame_emu* e, const float* x_dev, long long n, float* y_dev, cu
   for (long long r0 = 0; r0 < n; r0 += e->bmax) {
     const int b = (int)std::min<long long>(e->bmax, n - r0);
     const int bp = ((b + 127) / 128) * 128;
-    int rc = prep_x(e, x_dev + r0 * e->nin, bp, b);
+    int rc = prep_x(e, x_dev + r0 * e->nin, bp, b, true);
     if (rc) return rc;
-    rc = forward(e, bp);
+    rc = forward(e, bp, true);
     if (rc) return rc;
     k_denorm<<<blocks((long long)b * e->nout), 256, 0, e->st>>>(e->Y, e->nout, e->nout_pad, b, e->ymean, e->ystd,
                                                                  y_dev + r0 * e->nout);
@@ -1211,8 +1228,8 @@ extern "C" int lgame_emu_infer(lgame_emu* e, const float* x, long long n, float*
     const float* src = xv ? xv + r0 * e->nin : e->xraw;
     if (!xv)
       ECK(cudaMemcpyAsync(e->xraw, x + r0 * e->nin, sizeof(float) * (size_t)b * e->nin, cudaMemcpyHostToDevice, e->st));
-    int rc = prep_x(e, src, bp, b);
-    if (!rc) rc = forward(e, bp);
+    int rc = prep_x(e, src, bp, b, true);
+    if (!rc) rc = forward(e, bp, true);
     if (rc) return rc;
     k_denorm<<<blocks((long long)b * e->nout), 256, 0, e->st>>>(e->Y, e->nout, e->nout_pad, b, e->ymean, e->ystd,
                                                                  yv ? yv + r0 * e->nout : e->yout);

@@ -8,13 +8,14 @@ struct lgame_emu;
 
 namespace emu {
 
-enum EpiKind { kEpiF32 = 0, kEpiBias = 1, kEpiBiasGelu = 2, kEpiGeluBwd = 3 };
+enum EpiKind { kEpiF32 = 0, kEpiBias = 1, kEpiBiasGelu = 2, kEpiGeluBwd = 3, kEpiBiasGeluH = 4 };
 
 // epilogue of the tensor-core GEMM (fields used depend on kind):
 //   kEpiF32      c[z*split_stride + m*ldc + n] = acc               (split-K partials)
 //   kEpiBias     c[m*ldc + n] = acc + bias[n]
 //   kEpiBiasGelu c[m*ldc + n] = z = acc + bias[n]; h[m*ldh + n] = ht[n*ldt + m] = bf16(gelu(z))
 //   kEpiGeluBwd  c[m*ldc + n] = d = acc * gelu'(zprev[m*ldc + n]); h, ht = bf16(d)
+//   kEpiBiasGeluH h[m*ldh + n] = bf16(gelu(acc + bias[n])) alone (inference)
 struct Epi {
   int kind;
   const float* bias;
