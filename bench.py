@@ -411,6 +411,28 @@ def profile_kernels(g, steps: int, first_step: int, ncons: int, cells: int, peak
             "traffic": None if dram is None else dram * cells}
 
 
+# FP64 thread instructions per cell of one launch of the split step's FP64-heavy kernels:
+# sm__inst_executed_pipe_fp64.sum x 32 / cells from an ncu capture of the moist jet at
+# 192x192x80 (ks_column_ver: 2,597,768 warp instructions, 2,949,120 cells).  The FP64 pipe
+# issues 1.68 operations per clock per SM on this GPU (register-only probe; FMA and add alike).
+FP64_INST_PER_CELL = {"ks_column_ver": 28.2}
+FP64_OPS_PER_CLK_SM = 1.68
+
+
+def fp64_pipe_roofline(kernel: str, avg_ms: float, cells: int, clocks) -> dict | None:
+    """The FP64-pipe bound of an FP64-heavy split kernel: its FP64 instructions per launch over
+    the pipe's rate at the SM clock measured during the run (152 SMs)."""
+    per = FP64_INST_PER_CELL.get(kernel)
+    mhz = (clocks or {}).get("sm_mhz")
+    if per is None or not mhz or avg_ms <= 0:
+        return None
+    peak = FP64_OPS_PER_CLK_SM * 152 * mhz * 1e6
+    achieved = per * cells / (avg_ms * 1e-3)
+    return {"achieved_ops_per_s": achieved, "peak_ops_per_s": peak, "frac": achieved / peak,
+            "fp64_inst_per_cell": per, "src": "ncu sm__inst_executed_pipe_fp64 at 192x192x80; 1.68 FP64 ops/clk/SM "
+                                              "(probe) at the sampled SM clock"}
+
+
 def size_overrides(args) -> dict:
     """Namelist overrides of a reduced-size run (profiling captures): nx = ny, and n_layers with
     the orography-following layers kept at the workload's fraction."""
@@ -509,7 +531,8 @@ def run_ours(args):
                      "traffic_src": "ncu dram__bytes_read.sum + dram__bytes_write.sum per cell (one-pass capture "
                                     "of the 256x256x80 jet), times the cells of this run",
                      "peak_src": peaks["src"], "avg_launch_ms": prof["avg_launch_ms"],
-                     "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"]},
+                     "alg_bytes_per_launch": prof["alg_bytes_per_launch"], "kernel_shares": prof["shares"],
+                     "fp64_pipe": fp64_pipe_roofline(prof["kernel"], prof["avg_launch_ms"], cells, clocks)},
         "step_roofline": {"alg_bytes_per_cell": step_b, "alg_bytes_per_step": step_b * cells,
                           "achieved_gbs": step_b * cells / head["s_per_step"] / 1e9,
                           "peak_gbs": peaks["hbm_gbs"], "frac": step_b * cells / head["s_per_step"] / 1e9 / peaks["hbm_gbs"]},
