@@ -740,7 +740,10 @@ def measure_e2e(L, g, hm, args) -> dict:
 
     keep = []
     old, new = {}, {}
-    for f in L.STATE_FIELDS:
+    # the soil temperature is part of the state only with the prognostic soil or the sensible
+    # heat flux on
+    soil = g.cfg.lprog_soil_temp or g.cfg.lsfc_sensible_heat_flux
+    for f in (L.STATE_FIELDS if soil else L.ATMOS_FIELDS):
         a, t = pinned_like(hm.state[f])
         b, t2 = pinned_like(np.zeros_like(hm.state[f], order="F"))
         keep += [t, t2]

@@ -63,9 +63,8 @@ extern "C" {
  * plus the derived quantities the reference computes once at start-up
  * (n_levels, n_flat_layers, dtime: mo_run_nml.F90:89-94; n_constituents:
  * mo_constituents_nml.F90:246-253).  Logical switches are 0/1 ints.
- * Switches of physics that the GPU step does not implement (diffusion, PBL,
- * surface fluxes, prognostic soil, non-periodic boundary relaxation) must be 0;
- * lgame_gpu_create rejects them with LGAME_ERR_UNSUPPORTED. */
+ * Combinations of switches that the reference cannot run as specified (see
+ * lgame_gpu_create) are rejected with LGAME_ERR_UNSUPPORTED or LGAME_ERR_BAD_CONFIG. */
 typedef struct lgame_config {
   /* &run (mo_run_nml.F90:44-46) */
   int    ny, nx, n_layers, n_oro_layers;
@@ -92,7 +91,14 @@ typedef struct lgame_config {
    * the minimum background shear (1/s) and the Smagorinsky parameter */
   int    diff_coeff_scheme_h;   /* LGAME_DIFF_COEFF_SMAG or LGAME_DIFF_COEFF_TKE */
   double bg_shear, c_s;
+  /* &surface and the surface-layer constants of &diff (mo_surface_nml.F90:14, mo_diff_nml.F90:
+   * 18-19; appended): the number of soil layers (2..LGAME_MAX_SOIL_LAYERS when the soil or the
+   * sensible heat flux is on), the height of the Prandtl layer (m) and von Karman's constant */
+  int    nsoillays;
+  double h_prandtl, karman;
 } lgame_config;
+
+#define LGAME_MAX_SOIL_LAYERS 16
 
 #define LGAME_DIFF_COEFF_SMAG 0  /* diff_coeff_scheme_h = "smag" */
 #define LGAME_DIFF_COEFF_TKE  1  /* diff_coeff_scheme_h = "tke"  */
@@ -135,6 +141,16 @@ enum lgame_grid_field {
   LGAME_GRID_DX_DUAL,               /* (ny+1,nx,nl)    */
   LGAME_GRID_DY_DUAL,               /* (ny,nx+1,nl)    */
   LGAME_GRID_LAYER_THICKNESS,       /* (ny,nx,nl)      */
+  /* the surface and the soil (mo_definitions.F90:70-88; mo_grid_generator.F90:746-813, 1360-1378) */
+  LGAME_GRID_LAND_FRACTION,         /* (ny,nx)         */
+  LGAME_GRID_LAKE_FRACTION,         /* (ny,nx)         */
+  LGAME_GRID_ROUGHNESS_LENGTH,      /* (ny,nx)  m, of the land                      */
+  LGAME_GRID_SFC_RHO_C,             /* (ny,nx)  volumetric heat capacity of the soil */
+  LGAME_GRID_T_CONDUC_SOIL,         /* (ny,nx)  temperature conductivity of the soil */
+  LGAME_GRID_T_CONST_SOIL,          /* (ny,nx)  K, temperature at depth z_t_const    */
+  LGAME_GRID_Z_SOIL_INTERFACE,      /* (nsoillays+1) m, 0 at the surface, downward negative */
+  LGAME_GRID_Z_SOIL_CENTER,         /* (nsoillays)   m                               */
+  LGAME_GRID_Z_T_CONST,             /* (1)      m, depth of the constant soil temperature */
   LGAME_GRID_NFIELDS
 };
 
@@ -147,8 +163,13 @@ enum lgame_state_field {
   LGAME_STATE_WIND_U,         /* (ny,nx+1,nl)   */
   LGAME_STATE_WIND_V,         /* (ny+1,nx,nl)   */
   LGAME_STATE_WIND_W,         /* (ny,nx,nl+1)   */
+  LGAME_STATE_TEMPERATURE_SOIL, /* (ny,nx,nsoillays) */
   LGAME_STATE_NFIELDS
 };
+/* The state calls take either all LGAME_STATE_NFIELDS arrays or only the first
+ * LGAME_STATE_NFIELDS_ATMOS (the atmosphere; the soil temperature on the device is then left
+ * as it is, which a run without prognostic soil and sensible heat flux never reads). */
+#define LGAME_STATE_NFIELDS_ATMOS 7
 
 /* ---- diagnostics carried between steps (t_diag, t_tend) -------------------
  * These are the arrays whose values survive from one call of pchevi to the next
@@ -184,6 +205,19 @@ enum lgame_diag_field {
   LGAME_DIAG_MOM_DIFF_TEND_X,         /* (ny,nx+1,nl) momentum diffusion acceleration, x  */
   LGAME_DIAG_MOM_DIFF_TEND_Y,         /* (ny+1,nx,nl) momentum diffusion acceleration, y  */
   LGAME_DIAG_MOM_DIFF_TEND_Z,         /* (ny,nx,nl+1) momentum diffusion acceleration, z  */
+  /* the surface layer (mo_definitions.F90:137, 172-181, 185): v_squared and the roughness length
+   * are carried (the next step's surface update reads them before they are formed anew); the
+   * sea surface temperature and the surface radiation fluxes are provided by the host */
+  LGAME_DIAG_V_SQUARED,               /* (ny,nx,nl)  specific kinetic energy (m^2 s^-2)   */
+  LGAME_DIAG_ROUGHNESS_LENGTH,        /* (ny,nx)  m, actual (sea: from the 10 m wind)     */
+  LGAME_DIAG_ROUGHNESS_VELOCITY,      /* (ny,nx)  m/s                                     */
+  LGAME_DIAG_MONIN_OBUKHOV_LENGTH,    /* (ny,nx)  m                                       */
+  LGAME_DIAG_SCALAR_FLUX_RESISTANCE,  /* (ny,nx)  s/m                                     */
+  LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL, /* (ny,nx) W m^-2, sensible heat into the soil */
+  LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA,  /* (ny,nx) W m^-2, sensible heat into the sea  */
+  LGAME_DIAG_SST,                     /* (ny,nx)  K, sea surface temperature (host)       */
+  LGAME_DIAG_SFC_SW_IN,               /* (ny,nx)  W m^-2, shortwave into the surface (host) */
+  LGAME_DIAG_SFC_LW_OUT,              /* (ny,nx)  W m^-2, longwave out of the surface (host) */
   LGAME_DIAG_NFIELDS
 };
 
@@ -224,11 +258,15 @@ int  lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out);
 /* Copies the grid (host, reference layout) to the device once, precomputing nothing
  * that changes the arithmetic of the FP64 path.  Replaces the grid argument of pchevi
  * (mo_manage_pchevi.F90:35) for the lifetime of the context.  nfields must equal
- * LGAME_GRID_NFIELDS. */
+ * LGAME_GRID_NFIELDS.  The surface and soil fields may be NULL when the surface switches
+ * (lprog_soil_temp, lsfc_sensible_heat_flux, lsfc_phase_trans, lpbl) are all off.  The call
+ * also sets the carried roughness length to the grid's (diag%roughness_length =
+ * grid%roughness_length, control.F90:458). */
 int  lgame_gpu_set_grid(lgame_gpu* ctx, const double* const* fields, int nfields);
 
 /* Host -> device copy of one state slot (slot 0 or 1, the reference's state_1/state_2,
- * control.F90:30-31).  nfields must equal LGAME_STATE_NFIELDS. */
+ * control.F90:30-31).  nfields must be LGAME_STATE_NFIELDS, or LGAME_STATE_NFIELDS_ATMOS
+ * to leave the soil temperature as it is (get_state: not to copy it). */
 int  lgame_gpu_set_state(lgame_gpu* ctx, int slot, const double* const* fields, int nfields);
 /* Device -> host copy of one state slot; synchronises. */
 int  lgame_gpu_get_state(lgame_gpu* ctx, int slot, double* const* fields, int nfields);
@@ -263,7 +301,9 @@ int  lgame_gpu_pchevi(lgame_gpu* ctx, int old_slot, int new_slot,
  * GPU reads and writes the host arrays itself and fills the FP32 state mirror in the
  * same pass; otherwise the copy engines move the state.  In split precision (without a
  * boundary relaxation), fields of the new state that are final before the step ends are
- * copied out on a second stream while the step still runs.  Slots 0 and 1 are used. */
+ * copied out on a second stream while the step still runs.  Slots 0 and 1 are used.
+ * nfields is LGAME_STATE_NFIELDS, or LGAME_STATE_NFIELDS_ATMOS when neither the soil
+ * temperature nor the sensible heat flux is on (the soil temperature is then not moved). */
 int  lgame_gpu_pchevi_host(lgame_gpu* ctx, const double* const* state_old,
                            double* const* state_new, int nfields,
                            int total_step_counter, int lrad_update, double t_0);

@@ -106,23 +106,26 @@ double* lgame_host_diag_field(lgame_host_model* m, int field, size_t* n);
 double* lgame_host_surface_field(lgame_host_model* m, int field, size_t* n);
 
 /* ---- raw binary files where the reference uses netCDF (absent here) ------------------------
- * A 64-byte little-endian header (magic "LGAMESNP" or "LGAMEBCL", int32 version 1, int32 ny,
- * nx, n_layers, n_constituents, then the int64 step counter or the FP64 valid time) followed by
+ * A 64-byte little-endian header (magic "LGAMESNP" or "LGAMEBCL", int32 version 3, int32 ny,
+ * nx, n_layers, n_constituents, then the int64 step counter or the FP64 valid time, then int32
+ * nsoillays (0 in a boundary level)) followed by
  * FP64 arrays in the reference layout (column-major, reference extents).  Readers check the
  * magic, the version, the dimensions and the length, and fail with LGAME_ERR_BAD_DIMS or
  * LGAME_ERR_INVALID_ARG. */
 
-/* Restart snapshot: the 7 fields of state slot 0 and of slot 1 (enum lgame_state_field order,
- * as lgame_gpu_get_state returns them), the LGAME_DIAG_NFIELDS carried diagnostics (as
+/* Restart snapshot: the LGAME_STATE_NFIELDS fields of state slot 0 and of slot 1 (enum
+ * lgame_state_field order, as lgame_gpu_get_state returns them; the soil temperature has
+ * nsoillays layers and may be NULL when nsoillays is 0), the LGAME_DIAG_NFIELDS carried diagnostics (as
  * lgame_gpu_get_diag returns them) and the step counter: a run resumed from it with
  * lgame_gpu_set_state, lgame_gpu_set_diag and the next step number continues bit for bit.
  * Replaces restart() (mo_set_initial_state.F90:259-320), which reads one state's rho,
  * rhotheta_v and winds from netCDF and is unreachable in the reference (no lrestart in the
  * namelist). */
-int  lgame_host_write_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, long long step,
-                               const double* const* slot0, const double* const* slot1, const double* const* diag);
-int  lgame_host_read_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, long long* step,
-                              double* const* slot0, double* const* slot1, double* const* diag);
+int  lgame_host_write_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, int nsoillays,
+                               long long step, const double* const* slot0, const double* const* slot1,
+                               const double* const* diag);
+int  lgame_host_read_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents, int nsoillays,
+                              long long* step, double* const* slot0, double* const* slot1, double* const* diag);
 
 /* Lateral boundary level: the t_bc arrays of one time index (rho, rhotheta_v, wind_u, wind_v,
  * wind_w, extents as lgame_gpu_set_bc takes them) and their valid time (s); what

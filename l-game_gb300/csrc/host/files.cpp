@@ -4,12 +4,14 @@
 // Every file is a 64-byte header followed by FP64 arrays in the reference's layout
 // (column-major, reference extents), all little-endian:
 //   bytes 0-7    magic, "LGAMESNP" (snapshot) or "LGAMEBCL" (boundary level)
-//   bytes 8-11   int32 format version (2: the diagnostics of the diffusion closure appended)
+//   bytes 8-11   int32 format version (3: the soil temperature and the surface diagnostics)
 //   bytes 12-27  int32 ny, nx, n_layers, n_constituents
 //   bytes 28-35  int64 step counter (snapshot) or the valid time in seconds as FP64 (level)
-//   bytes 36-63  zero
-// Snapshot arrays: the 7 state fields of slot 0, then of slot 1 (enum lgame_state_field
-// order), then the LGAME_DIAG_NFIELDS carried diagnostics (enum lgame_diag_field order): what
+//   bytes 36-39  int32 nsoillays (snapshot; 0 in a boundary level)
+//   bytes 40-63  zero
+// Snapshot arrays: the LGAME_STATE_NFIELDS state fields of slot 0, then of slot 1 (enum
+// lgame_state_field order, the soil temperature last), then the LGAME_DIAG_NFIELDS carried
+// diagnostics (enum lgame_diag_field order): what
 // resuming a run bit for bit needs (the reference's restart, mo_set_initial_state.F90:259-320,
 // reads rho, rhotheta_v and the winds of one state from netCDF, and its output is FP32).
 // Boundary level arrays: rho, rhotheta_v, wind_u, wind_v, wind_w of one time index of t_bc
@@ -27,13 +29,14 @@
 
 namespace {
 
-constexpr int kVersion = 2;
+constexpr int kVersion = 3;
 
 struct Header {
   char magic[8];
   int32_t version, ny, nx, nl, ncons;
   unsigned char tag[8];  // int64 step or FP64 valid time
-  unsigned char pad[28];
+  int32_t nsoil;
+  unsigned char pad[24];
 };
 static_assert(sizeof(Header) == 64, "header is 64 bytes");
 
@@ -47,10 +50,11 @@ bool dims_ok(int ny, int nx, int nl, int ncons) {
 }
 
 // element counts of the state and diagnostic fields (reference extents)
-size_t state_n(int f, int ny, int nx, int nl, int ncons) {
+size_t state_n(int f, int ny, int nx, int nl, int ncons, int ns) {
   const size_t s = (size_t)ny * nx * nl;
   switch (f) {
     case LGAME_STATE_RHO: return s * ncons;
+    case LGAME_STATE_TEMPERATURE_SOIL: return (size_t)ny * nx * (size_t)ns;
     case LGAME_STATE_WIND_U: return (size_t)ny * (nx + 1) * nl;
     case LGAME_STATE_WIND_V: return (size_t)(ny + 1) * nx * nl;
     case LGAME_STATE_WIND_W: return (size_t)ny * nx * (nl + 1);
@@ -70,6 +74,10 @@ size_t diag_n(int f, int ny, int nx, int nl, int ncons) {
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: case LGAME_DIAG_POT_VORT_TEND_Z:
     case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: case LGAME_DIAG_MOM_DIFF_TEND_Z: return w;
     case LGAME_DIAG_TEND_RHO: return s * ncons;
+    case LGAME_DIAG_ROUGHNESS_LENGTH: case LGAME_DIAG_ROUGHNESS_VELOCITY: case LGAME_DIAG_MONIN_OBUKHOV_LENGTH:
+    case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL:
+    case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: case LGAME_DIAG_SST: case LGAME_DIAG_SFC_SW_IN:
+    case LGAME_DIAG_SFC_LW_OUT: return (size_t)ny * nx;
     default: return s;
   }
 }
@@ -118,7 +126,7 @@ class File {
   std::FILE* f_;
 };
 
-Header make_header(const char* magic, int ny, int nx, int nl, int ncons, const void* tag8) {
+Header make_header(const char* magic, int ny, int nx, int nl, int ncons, int ns, const void* tag8) {
   Header h;
   std::memset(&h, 0, sizeof h);
   std::memcpy(h.magic, magic, 8);
@@ -127,9 +135,10 @@ Header make_header(const char* magic, int ny, int nx, int nl, int ncons, const v
   h.nx = nx;
   h.nl = nl;
   h.ncons = ncons;
+  h.nsoil = ns;
   std::memcpy(h.tag, tag8, 8);
   if (!little_endian()) {  // the header's integers little-endian too
-    for (int32_t* v : {&h.version, &h.ny, &h.nx, &h.nl, &h.ncons}) {
+    for (int32_t* v : {&h.version, &h.ny, &h.nx, &h.nl, &h.ncons, &h.nsoil}) {
       unsigned char* b = reinterpret_cast<unsigned char*>(v);
       std::swap(b[0], b[3]);
       std::swap(b[1], b[2]);
@@ -139,9 +148,9 @@ Header make_header(const char* magic, int ny, int nx, int nl, int ncons, const v
   return h;
 }
 
-int check_header(Header h, const char* magic, const char* path, int ny, int nx, int nl, int ncons, void* tag8) {
+int check_header(Header h, const char* magic, const char* path, int ny, int nx, int nl, int ncons, int ns, void* tag8) {
   if (!little_endian()) {
-    for (int32_t* v : {&h.version, &h.ny, &h.nx, &h.nl, &h.ncons}) {
+    for (int32_t* v : {&h.version, &h.ny, &h.nx, &h.nl, &h.ncons, &h.nsoil}) {
       unsigned char* b = reinterpret_cast<unsigned char*>(v);
       std::swap(b[0], b[3]);
       std::swap(b[1], b[2]);
@@ -151,7 +160,7 @@ int check_header(Header h, const char* magic, const char* path, int ny, int nx, 
   if (std::memcmp(h.magic, magic, 8) != 0)
     return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": not a file of this kind (magic)");
   if (h.version != kVersion) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": unknown format version");
-  if (h.ny != ny || h.nx != nx || h.nl != nl || h.ncons != ncons)
+  if (h.ny != ny || h.nx != nx || h.nl != nl || h.ncons != ncons || h.nsoil != ns)
     return fail(LGAME_ERR_BAD_DIMS, std::string(path) + ": written for other dimensions");
   std::memcpy(tag8, h.tag, 8);
   return LGAME_OK;
@@ -160,22 +169,24 @@ int check_header(Header h, const char* magic, const char* path, int ny, int nx, 
 }  // namespace
 
 extern "C" int lgame_host_write_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents,
-                                         long long step, const double* const* slot0, const double* const* slot1,
-                                         const double* const* diag) {
-  if (!path || !slot0 || !slot1 || !diag || !dims_ok(ny, nx, n_layers, n_constituents) || step < 0)
+                                         int nsoillays, long long step, const double* const* slot0,
+                                         const double* const* slot1, const double* const* diag) {
+  if (!path || !slot0 || !slot1 || !diag || !dims_ok(ny, nx, n_layers, n_constituents) || step < 0 ||
+      nsoillays < 0 || nsoillays > LGAME_MAX_SOIL_LAYERS)
     return fail(LGAME_ERR_INVALID_ARG, "lgame_host_write_snapshot: bad arguments");
   for (int f = 0; f < LGAME_STATE_NFIELDS; ++f)
-    if (!slot0[f] || !slot1[f]) return fail(LGAME_ERR_INVALID_ARG, "lgame_host_write_snapshot: a state array is null");
+    if ((!slot0[f] || !slot1[f]) && state_n(f, ny, nx, n_layers, n_constituents, nsoillays) > 0)
+      return fail(LGAME_ERR_INVALID_ARG, "lgame_host_write_snapshot: a state array is null");
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f)
     if (!diag[f]) return fail(LGAME_ERR_INVALID_ARG, "lgame_host_write_snapshot: a diagnostic array is null");
   File out(path, "wb");
   if (!out.ok()) return fail(LGAME_ERR_INVALID_ARG, std::string("lgame_host_write_snapshot: cannot open ") + path);
   const int64_t s = step;
-  const Header h = make_header("LGAMESNP", ny, nx, n_layers, n_constituents, &s);
+  const Header h = make_header("LGAMESNP", ny, nx, n_layers, n_constituents, nsoillays, &s);
   bool ok = out.write(&h, sizeof h);
   for (const double* const* slot : {slot0, slot1})
     for (int f = 0; f < LGAME_STATE_NFIELDS && ok; ++f)
-      ok = out.write_doubles(slot[f], state_n(f, ny, nx, n_layers, n_constituents));
+      ok = out.write_doubles(slot[f], state_n(f, ny, nx, n_layers, n_constituents, nsoillays));
   for (int f = 0; f < LGAME_DIAG_NFIELDS && ok; ++f)
     ok = out.write_doubles(diag[f], diag_n(f, ny, nx, n_layers, n_constituents));
   if (!out.close() || !ok) return fail(LGAME_ERR_INVALID_ARG, std::string("lgame_host_write_snapshot: write failed: ") + path);
@@ -183,12 +194,14 @@ extern "C" int lgame_host_write_snapshot(const char* path, int ny, int nx, int n
 }
 
 extern "C" int lgame_host_read_snapshot(const char* path, int ny, int nx, int n_layers, int n_constituents,
-                                        long long* step, double* const* slot0, double* const* slot1,
+                                        int nsoillays, long long* step, double* const* slot0, double* const* slot1,
                                         double* const* diag) {
-  if (!path || !slot0 || !slot1 || !diag || !dims_ok(ny, nx, n_layers, n_constituents))
+  if (!path || !slot0 || !slot1 || !diag || !dims_ok(ny, nx, n_layers, n_constituents) || nsoillays < 0 ||
+      nsoillays > LGAME_MAX_SOIL_LAYERS)
     return fail(LGAME_ERR_INVALID_ARG, "lgame_host_read_snapshot: bad arguments");
   for (int f = 0; f < LGAME_STATE_NFIELDS; ++f)
-    if (!slot0[f] || !slot1[f]) return fail(LGAME_ERR_INVALID_ARG, "lgame_host_read_snapshot: a state array is null");
+    if ((!slot0[f] || !slot1[f]) && state_n(f, ny, nx, n_layers, n_constituents, nsoillays) > 0)
+      return fail(LGAME_ERR_INVALID_ARG, "lgame_host_read_snapshot: a state array is null");
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f)
     if (!diag[f]) return fail(LGAME_ERR_INVALID_ARG, "lgame_host_read_snapshot: a diagnostic array is null");
   File in(path, "rb");
@@ -196,12 +209,12 @@ extern "C" int lgame_host_read_snapshot(const char* path, int ny, int nx, int n_
   Header h;
   if (!in.read(&h, sizeof h)) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": truncated header");
   int64_t s = 0;
-  int rc = check_header(h, "LGAMESNP", path, ny, nx, n_layers, n_constituents, &s);
+  int rc = check_header(h, "LGAMESNP", path, ny, nx, n_layers, n_constituents, nsoillays, &s);
   if (rc) return rc;
   bool ok = true;
   for (double* const* slot : {slot0, slot1})
     for (int f = 0; f < LGAME_STATE_NFIELDS && ok; ++f)
-      ok = in.read_doubles(slot[f], state_n(f, ny, nx, n_layers, n_constituents));
+      ok = in.read_doubles(slot[f], state_n(f, ny, nx, n_layers, n_constituents, nsoillays));
   for (int f = 0; f < LGAME_DIAG_NFIELDS && ok; ++f)
     ok = in.read_doubles(diag[f], diag_n(f, ny, nx, n_layers, n_constituents));
   if (!ok) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": truncated");
@@ -217,11 +230,11 @@ extern "C" int lgame_host_write_bc_level(const char* path, int ny, int nx, int n
     return fail(LGAME_ERR_INVALID_ARG, "lgame_host_write_bc_level: bad arguments");
   File out(path, "wb");
   if (!out.ok()) return fail(LGAME_ERR_INVALID_ARG, std::string("lgame_host_write_bc_level: cannot open ") + path);
-  const Header h = make_header("LGAMEBCL", ny, nx, n_layers, n_constituents, &t_valid);
+  const Header h = make_header("LGAMEBCL", ny, nx, n_layers, n_constituents, 0, &t_valid);
   const double* a[5] = {rho, rhotheta_v, wind_u, wind_v, wind_w};
   const int f[5] = {LGAME_STATE_RHO, LGAME_STATE_RHOTHETA_V, LGAME_STATE_WIND_U, LGAME_STATE_WIND_V, LGAME_STATE_WIND_W};
   bool ok = out.write(&h, sizeof h);
-  for (int k = 0; k < 5 && ok; ++k) ok = out.write_doubles(a[k], state_n(f[k], ny, nx, n_layers, n_constituents));
+  for (int k = 0; k < 5 && ok; ++k) ok = out.write_doubles(a[k], state_n(f[k], ny, nx, n_layers, n_constituents, 0));
   if (!out.close() || !ok) return fail(LGAME_ERR_INVALID_ARG, std::string("lgame_host_write_bc_level: write failed: ") + path);
   return LGAME_OK;
 }
@@ -236,12 +249,12 @@ extern "C" int lgame_host_read_bc_level(const char* path, int ny, int nx, int n_
   Header h;
   if (!in.read(&h, sizeof h)) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": truncated header");
   double t = 0.0;
-  int rc = check_header(h, "LGAMEBCL", path, ny, nx, n_layers, n_constituents, &t);
+  int rc = check_header(h, "LGAMEBCL", path, ny, nx, n_layers, n_constituents, 0, &t);
   if (rc) return rc;
   double* a[5] = {rho, rhotheta_v, wind_u, wind_v, wind_w};
   const int f[5] = {LGAME_STATE_RHO, LGAME_STATE_RHOTHETA_V, LGAME_STATE_WIND_U, LGAME_STATE_WIND_V, LGAME_STATE_WIND_W};
   bool ok = true;
-  for (int k = 0; k < 5 && ok; ++k) ok = in.read_doubles(a[k], state_n(f[k], ny, nx, n_layers, n_constituents));
+  for (int k = 0; k < 5 && ok; ++k) ok = in.read_doubles(a[k], state_n(f[k], ny, nx, n_layers, n_constituents, 0));
   if (!ok) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": truncated");
   if (!in.at_end()) return fail(LGAME_ERR_INVALID_ARG, std::string(path) + ": longer than its header says");
   if (t_valid) *t_valid = t;
@@ -266,9 +279,9 @@ extern "C" int lgame_bc_file_loader(void* user, double t_update, int time_index)
   int rc = lgame_host_bc_filename(u->root, t_update, u->t_init, name, (int)sizeof name);
   if (rc) return rc;
   const int ny = u->ny, nx = u->nx, nl = u->n_layers, nc = u->n_constituents;
-  std::vector<double> rho(state_n(LGAME_STATE_RHO, ny, nx, nl, nc)), rt(state_n(LGAME_STATE_RHOTHETA_V, ny, nx, nl, nc)),
-      wu(state_n(LGAME_STATE_WIND_U, ny, nx, nl, nc)), wv(state_n(LGAME_STATE_WIND_V, ny, nx, nl, nc)),
-      ww(state_n(LGAME_STATE_WIND_W, ny, nx, nl, nc));
+  std::vector<double> rho(state_n(LGAME_STATE_RHO, ny, nx, nl, nc, 0)), rt(state_n(LGAME_STATE_RHOTHETA_V, ny, nx, nl, nc, 0)),
+      wu(state_n(LGAME_STATE_WIND_U, ny, nx, nl, nc, 0)), wv(state_n(LGAME_STATE_WIND_V, ny, nx, nl, nc, 0)),
+      ww(state_n(LGAME_STATE_WIND_W, ny, nx, nl, nc, 0));
   double t = 0.0;
   rc = lgame_host_read_bc_level(name, ny, nx, nl, nc, &t, rho.data(), rt.data(), wu.data(), wv.data(), ww.data());
   if (rc) return rc;

@@ -375,5 +375,6 @@ extern "C" int lgame_config_from_namelist(const lgame_namelist* n, lgame_config*
   c->precision = n->precision; c->check_finite = n->check_finite;
   c->diff_coeff_scheme_h = (trim(n->diff_coeff_scheme_h) == "tke") ? LGAME_DIFF_COEFF_TKE : LGAME_DIFF_COEFF_SMAG;
   c->bg_shear = n->bg_shear; c->c_s = n->c_s;
+  c->nsoillays = n->nsoillays; c->h_prandtl = n->h_prandtl; c->karman = n->karman;
   return LGAME_OK;
 }

@@ -11,6 +11,7 @@
 #include "lgame_host.h"
 #include "common.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -70,8 +71,11 @@ struct lgame_host_model {
   Vec area_x, area_y, area_z, slope_x, slope_y, ipw, area_dual_x, area_dual_y, area_dual_z, z_area_dual_z;
   Vec fvec_x, fvec_y, fvec_z, trsk_u, trsk_v, exner_bg_grad_u, exner_bg_grad_v, exner_bg_grad_w;
   Vec theta_v_bg, exner_bg, sfc_albedo, dx_dual, dy_dual, layer_thickness;
+  // surface and soil (grid%roughness_length is `roughness_length`)
+  Vec land_fraction, lake_fraction, roughness_length, sfc_rho_c, t_conduc_soil, t_const_soil;
+  Vec z_soil_interface, z_soil_center, z_t_const;
   // state
-  Vec rho, rhotheta_v, theta_v_pert, exner_pert, wind_u, wind_v, wind_w;
+  Vec rho, rhotheta_v, theta_v_pert, exner_pert, wind_u, wind_v, wind_w, temperature_soil;
   // carried diagnostics (only the ones the set-up writes; the rest start at zero)
   Vec diag[LGAME_DIAG_NFIELDS];
 
@@ -326,7 +330,8 @@ int grid_setup(M& m) {
     }
   // orography, :325-737
   switch (n.orography_id) {
-    case 0:
+    case 0:  // mean surface temperature of an Earth without orography, :333
+      for (size_t p = 0; p < m.t_const_soil.size(); ++p) m.t_const_soil[p] = 273.15 + 25.0 * std::cos(2.0 * m.lat_geo_scalar[p]);
       break;
     case 2: {  // Schaer wave test, :703-711
       const double h = 250.0;
@@ -366,7 +371,9 @@ int grid_setup(M& m) {
       // U[hill_height_min,hill_height_max], half-widths U[hill_width_min,hill_width_max]
       // and centres uniform over the domain, drawn from a splitmix64 stream seeded by
       // &gpu seed.  On a periodic domain the distance to each centre is the shortest
-      // periodic distance, so the orography is periodic too.  oro_smoothed = 0.5*oro.
+      // periodic distance, so the orography is periodic too.  oro_smoothed = 0.5*oro.  The
+      // soil's constant deep temperature is that of orography_id 0.
+      for (size_t p = 0; p < m.t_const_soil.size(); ++p) m.t_const_soil[p] = 273.15 + 25.0 * std::cos(2.0 * m.lat_geo_scalar[p]);
       Rng rng((uint64_t)n.seed);
       const double Lx = nx * n.dx, Ly = ny * n.dy;
       std::vector<double> hh(n.n_hills), ww(n.n_hills), xc(n.n_hills), yc(n.n_hills);
@@ -398,19 +405,49 @@ int grid_setup(M& m) {
   }
   for (int jk = 1; jk <= nx; ++jk)
     for (int ji = 1; ji <= ny; ++ji) m.z_w[m.IS(ji, jk, NL)] = m.oro[m.I2(ji, jk)];
-  // surface albedo (lread_geo=.false. branch, :746-813): water everywhere, land for the
-  // seabreeze mask; only the albedo is kept (the emulator input).
+  // physical surface properties (lread_geo=.false. branch, :746-813): water everywhere, land
+  // for the seabreeze mask, no lakes; albedo, roughness length (of an idealised vegetation
+  // height, :1636-1652), volumetric heat capacity and temperature conductivity
   for (int jk = 1; jk <= nx; ++jk)
     for (int ji = 1; ji <= ny; ++ji) {
-      double land = 0.0;
-      if (std::string(n.scenario) == "seabreeze" && jk >= nx / 4 && jk <= 3 * nx / 4) land = 1.0;
-      double alb = 0.06;
+      const size_t p = m.I2(ji, jk);
+      if (std::string(n.scenario) == "seabreeze" && jk >= nx / 4 && jk <= 3 * nx / 4) m.land_fraction[p] = 1.0;
+      const double land = m.land_fraction[p], lake = m.lake_fraction[p];
+      m.sfc_albedo[p] = 0.06;
+      m.roughness_length[p] = 0.08;
+      m.sfc_rho_c[p] = 1024.0 * 4184.0;
+      m.t_conduc_soil[p] = 1.4e-7;
       if (land > 1e-10) {
-        if (std::fabs(360.0 / (2.0 * M_PI_) * m.lat_geo_scalar[m.I2(ji, jk)]) > 70.0) alb = land * 0.8 + (1.0 - land) * 0.06;
-        else alb = land * 0.12 + (1.0 - land) * 0.06;
+        m.t_conduc_soil[p] = (land * 7.5e-7 + lake * 1.4e-7) / (land + lake);
+        m.sfc_rho_c[p] = (land * 1442.0 * 830.0 + lake * 1024.0 * 4184.0) / (land + lake);
+        if (std::fabs(360.0 / (2.0 * M_PI_) * m.lat_geo_scalar[p]) > 70.0) m.sfc_albedo[p] = land * 0.8 + (1.0 - land) * 0.06;
+        else m.sfc_albedo[p] = land * 0.12 + (1.0 - land) * 0.06;
+        const double vegetation_height = 20.0 * std::cos(m.lat_geo_scalar[p]) * std::exp(-m.z_w[m.IS(ji, jk, NL)] / 1500.0);
+        m.roughness_length[p] = vegetation_height / 8.0;
       }
-      m.sfc_albedo[m.I2(ji, jk)] = alb;
+      m.roughness_length[p] = std::fmax(0.0001, m.roughness_length[p]);
     }
+  // soil grid, :1360-1378: interfaces spaced by powers of sigma_soil, rescaled to reach
+  // z_t_const at the bottom (the integer powers by repeated squaring, as Fortran's real**integer)
+  if (n.nsoillays >= 1) {
+    const int ns = n.nsoillays;
+    const double sigma_soil = 0.352;
+    auto powi = [](double x, int e) {
+      unsigned k = e < 0 ? 0u - (unsigned)e : (unsigned)e;
+      double y = (k & 1u) ? x : 1.0;
+      while (k >>= 1) {
+        x = x * x;
+        if (k & 1u) y = y * x;
+      }
+      return e < 0 ? 1.0 / y : y;
+    };
+    m.z_t_const[0] = -10.0;
+    m.z_soil_interface[0] = 0.0;
+    for (int jl = 2; jl <= ns + 1; ++jl) m.z_soil_interface[jl - 1] = m.z_soil_interface[jl - 2] + powi(sigma_soil, ns - jl);
+    const double rescale_factor = m.z_t_const[0] / m.z_soil_interface[ns];
+    for (int jl = 2; jl <= ns + 1; ++jl) m.z_soil_interface[jl - 1] = rescale_factor * m.z_soil_interface[jl - 1];
+    for (int jl = 1; jl <= ns; ++jl) m.z_soil_center[jl - 1] = 0.5 * (m.z_soil_interface[jl - 1] + m.z_soil_interface[jl]);
+  }
   // vertical grid, :894-951
   double max_oro = -1e300;
   for (double v : m.oro) max_oro = std::fmax(max_oro, v);
@@ -974,16 +1011,32 @@ extern "C" int lgame_host_setup(const lgame_namelist* nml, lgame_host_model** ou
   m->exner_bg_grad_u.assign(nU, 0); m->exner_bg_grad_v.assign(nV, 0); m->exner_bg_grad_w.assign(nW, 0);
   m->theta_v_bg.assign(nS, 0); m->exner_bg.assign(nS, 0); m->sfc_albedo.assign(ny * nx, 0);
   m->dx_dual.assign(nV, 0); m->dy_dual.assign(nU, 0); m->layer_thickness.assign(nS, 0);
+  if (nml->nsoillays < 0 || nml->nsoillays > LGAME_MAX_SOIL_LAYERS) {
+    delete m;
+    return fail(LGAME_ERR_BAD_CONFIG, "nsoillays must lie in 0.." + std::to_string(LGAME_MAX_SOIL_LAYERS));
+  }
+  const size_t n2 = ny * nx, ns = (size_t)nml->nsoillays;
+  for (Vec* v : {&m->land_fraction, &m->lake_fraction, &m->roughness_length, &m->sfc_rho_c, &m->t_conduc_soil,
+                 &m->t_const_soil})
+    v->assign(n2, 0);
+  m->z_soil_interface.assign(ns + 1, 0); m->z_soil_center.assign(ns, 0); m->z_t_const.assign(1, 0);
   const int ncons = nml->n_constituents;
   m->rho.assign(nS * ncons, 0); m->rhotheta_v.assign(nS, 0); m->theta_v_pert.assign(nS, 0);
   m->exner_pert.assign(nS, 0); m->wind_u.assign(nU, 0); m->wind_v.assign(nV, 0); m->wind_w.assign(nW, 0);
+  m->temperature_soil.assign(n2 * ns, 0);
   const size_t dsz[LGAME_DIAG_NFIELDS] = {nU, nV, nW, nU, nV, nW, nU, nV, nU, nV, nW, nU, nV, nW, nS, nS, nS,
-                                          nS * ncons, nS, nU, nV, nW, nS, nS, nS, nU, nV, nW};
+                                          nS * ncons, nS, nU, nV, nW, nS, nS, nS, nU, nV, nW,
+                                          nS, n2, n2, n2, n2, n2, n2, n2, n2, n2};
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f) m->diag[f].assign(dsz[f], 0.0);
   int rc = grid_setup(*m);
   if (rc == LGAME_OK) rc = bg_setup(*m);
   if (rc == LGAME_OK) rc = ideal_init(*m);
   if (rc != LGAME_OK) { delete m; return rc; }
+  // soil temperature and sea surface temperature, mo_set_initial_state.F90:237-247; the
+  // carried roughness length starts at the grid's, control.F90:458
+  std::fill(m->temperature_soil.begin(), m->temperature_soil.end(), 280.0);
+  if (ns > 0) std::copy(m->temperature_soil.begin(), m->temperature_soil.begin() + n2, m->diag[LGAME_DIAG_SST].begin());
+  m->diag[LGAME_DIAG_ROUGHNESS_LENGTH] = m->roughness_length;
   *out = m;
   return LGAME_OK;
 }
@@ -1027,6 +1080,15 @@ extern "C" double* lgame_host_grid_field(lgame_host_model* m, int f, size_t* n) 
     case LGAME_GRID_DX_DUAL: v = &m->dx_dual; break;
     case LGAME_GRID_DY_DUAL: v = &m->dy_dual; break;
     case LGAME_GRID_LAYER_THICKNESS: v = &m->layer_thickness; break;
+    case LGAME_GRID_LAND_FRACTION: v = &m->land_fraction; break;
+    case LGAME_GRID_LAKE_FRACTION: v = &m->lake_fraction; break;
+    case LGAME_GRID_ROUGHNESS_LENGTH: v = &m->roughness_length; break;
+    case LGAME_GRID_SFC_RHO_C: v = &m->sfc_rho_c; break;
+    case LGAME_GRID_T_CONDUC_SOIL: v = &m->t_conduc_soil; break;
+    case LGAME_GRID_T_CONST_SOIL: v = &m->t_const_soil; break;
+    case LGAME_GRID_Z_SOIL_INTERFACE: v = &m->z_soil_interface; break;
+    case LGAME_GRID_Z_SOIL_CENTER: v = &m->z_soil_center; break;
+    case LGAME_GRID_Z_T_CONST: v = &m->z_t_const; break;
     default: return nullptr;
   }
   if (n) *n = v->size();
@@ -1044,6 +1106,7 @@ extern "C" double* lgame_host_state_field(lgame_host_model* m, int f, size_t* n)
     case LGAME_STATE_WIND_U: v = &m->wind_u; break;
     case LGAME_STATE_WIND_V: v = &m->wind_v; break;
     case LGAME_STATE_WIND_W: v = &m->wind_w; break;
+    case LGAME_STATE_TEMPERATURE_SOIL: v = &m->temperature_soil; break;
     default: return nullptr;
   }
   if (n) *n = v->size();

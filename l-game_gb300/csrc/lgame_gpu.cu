@@ -7,6 +7,7 @@
 #include "diffusion.cuh"
 #include "kernels.cuh"
 #include "split.cuh"
+#include "surface.cuh"
 
 #include <cuda_runtime.h>
 
@@ -72,6 +73,13 @@ struct lgame_gpu {
   bool diff_mass_h = false, diff_mass_v = false;
   DiffBuf<double> dbuf{};
   DiffPar dpar{};
+  // surface layer, PBL and soil (&surface): which parts run, the surface grid planes and
+  // diagnostics, the soil temperature of the two slots (nsoillays planes each)
+  bool sfc_turb = false, sfc_pbl = false, sfc_sens = false, sfc_soil = false;
+  SfcBuf sbuf{};
+  SfcPar spar{};
+  double* sfc_grid[6] = {};  // land, lake, roughness length, rho_c, conductivity, constant temperature
+  double* tsoil[2] = {};
   // scratch
   double *theta, *gz, *gx, *gy, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph, *vsq;
   double* staging = nullptr;
@@ -170,6 +178,9 @@ Ext grid_ext(const Dims& d, int f) {
     case LGAME_GRID_DX_DUAL: return ext_v(d);
     case LGAME_GRID_DY_DUAL: return ext_u(d);
     case LGAME_GRID_LAYER_THICKNESS: return ext_s(d);
+    case LGAME_GRID_LAND_FRACTION: case LGAME_GRID_LAKE_FRACTION: case LGAME_GRID_ROUGHNESS_LENGTH:
+    case LGAME_GRID_SFC_RHO_C: case LGAME_GRID_T_CONDUC_SOIL: case LGAME_GRID_T_CONST_SOIL:
+      return {(size_t)d.ny, (size_t)d.nx, 1};
   }
   return {0, 0, 0};
 }
@@ -185,6 +196,11 @@ Ext diag_ext(const Dims& d, int f) {
     case LGAME_DIAG_MOM_DIFF_TEND_X: return ext_u(d);
     case LGAME_DIAG_MOM_DIFF_TEND_Y: return ext_v(d);
     case LGAME_DIAG_MOM_DIFF_TEND_Z: return ext_w(d);
+    case LGAME_DIAG_ROUGHNESS_LENGTH: case LGAME_DIAG_ROUGHNESS_VELOCITY: case LGAME_DIAG_MONIN_OBUKHOV_LENGTH:
+    case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL:
+    case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: case LGAME_DIAG_SST: case LGAME_DIAG_SFC_SW_IN:
+    case LGAME_DIAG_SFC_LW_OUT:
+      return {(size_t)d.ny, (size_t)d.nx, 1};
     default: return ext_s(d);
   }
 }
@@ -505,6 +521,9 @@ const auto k_diff_fluxes1 = lg::k_diff_fluxes<double, double, double, 1>;
 const auto k_diff_fluxes7 = lg::k_diff_fluxes<double, double, double, 7>;
 const auto k_diff_divs1 = lg::k_diff_divs<double, 1>;
 const auto k_diff_divs7 = lg::k_diff_divs<double, 7>;
+const auto k_sfc_turb = lg::k_sfc_turb;
+const auto k_pbl = lg::k_pbl<double>;
+const auto k_sfc_column = lg::k_sfc_column<double>;
 }  // namespace kd
 
 dim3 blk() { return dim3(32, 8, 1); }
@@ -571,6 +590,9 @@ int diffusion_vector(lgame_gpu* c, const State& So) {
     LAUNCH(kd::k_diff_vz, grd(D, D.ny + 1, D.nx + 1, D.nl), D, G, So, B);
     LAUNCH(kd::k_mom_diff_h, grd(D, D.ny, D.nx, D.nl), D, G, So, B);
     if (c->diff_mom_v) LAUNCH(kd::k_mom_diff_v, grd(D, D.ny, D.nx, D.nl - 1), D, G, So, B);
+    // pbl_wind_tendency (mo_vector_tend_expl.F90:119-121), before the dissipation reads the
+    // momentum diffusion acceleration
+    if (c->sfc_pbl) LAUNCH(kd::k_pbl, grd(D, D.ny, D.nx, 1), D, G, So, c->vsq, c->sbuf, c->spar, B.mdtx, B.mdty);
     LAUNCH(kd::k_diss_rate, grd(D, D.ny, D.nx, D.nl), D, G, So, B, G.damp, (const double*)nullptr);
   } else if (D.lklemp && D.ndamp > 0) {
     LAUNCH(k_heating_diss, grd(D, D.ny, D.nx, std::min(D.nl, D.ndamp)), D, G, So, c->hdiss);
@@ -610,6 +632,8 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
   const State& Sn = c->st[sn];
   const Grid<double>& G = c->G;
   LAUNCH(kd::k_temperature, grd(D, D.ny, D.nx, D.nl), D, G, So, c->temperature);
+  // update_sfc_turb_quantities (mo_manage_pchevi.F90:51-53)
+  if (c->sfc_turb) LAUNCH(kd::k_sfc_turb, grd(D, D.ny, D.nx, 1), D, G, So, c->vsq, c->sbuf, c->spar);
   PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw};
   Carried<double> C{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v, c->pgcw,
             c->vsg_x, c->vsg_y, c->vsg_z, c->pvt_x, c->pvt_y, c->pvt_z};
@@ -661,6 +685,11 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
            c->rad, c->csh, T.rho, T.rt, mdt, tdh);
     // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
     {
+      // the sensible heat flux and the soil rows of three_band_solver_ver (mo_column_solvers.F90:
+      // 80-120, 228-300), ahead of its atmospheric rows, which read the heated tendency
+      if (c->sfc_sens || c->sfc_soil)
+        LAUNCH(kd::k_sfc_column, grd(D, D.ny, D.nx, 1), D, G, So, rk == 1 ? So : Sn, T.rt, c->sbuf, c->spar,
+               c->tsoil[so], c->tsoil[rk == 1 ? so : sn], c->tsoil[sn]);
       dim3 g2((unsigned)((D.ny + 31) / 32), (unsigned)((D.nx + 7) / 8), 1);
       LAUNCH(kd::k_column_ver, g2, D, G, So, Sn, T, rk);
       if (D.ncons > 1) LAUNCH(kd::k_column_tracers, g2, D, G, So, Sn, T.rho, c->temperature, c->csh, rk);
@@ -755,8 +784,23 @@ int check_cfg(const lgame_config* cfg) {
     return set_err(LGAME_ERR_UNSUPPORTED, "non-periodic horizontal momentum diffusion without lmom_diff_v needs "
                                           "theta_adv_order 3 in the GPU step");
 
-  if (cfg->lprog_soil_temp || cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl)
-    return set_err(LGAME_ERR_UNSUPPORTED, "surface physics (&surface lprog_soil_temp, lsfc_*, lpbl) is not part of the GPU step");
+  // &surface: the reference stops when lpbl is on without lmom_diff_h (mo_surface_nml.F90:46-49);
+  // its sensible heat flux divides by the scalar flux resistance, which only the prognostic
+  // soil's branch of update_sfc_turb_quantities forms (mo_pbl.F90:96-106), so without it the
+  // flux is x/0
+  if (cfg->lpbl && !cfg->lmom_diff_h)
+    return set_err(LGAME_ERR_BAD_CONFIG, "lpbl needs lmom_diff_h (mo_surface_nml.F90:46-49)");
+  if (cfg->lsfc_sensible_heat_flux && !cfg->lprog_soil_temp)
+    return set_err(LGAME_ERR_UNSUPPORTED, "lsfc_sensible_heat_flux without lprog_soil_temp divides by a zero scalar flux "
+                                          "resistance in the reference");
+  if ((cfg->lprog_soil_temp || cfg->lsfc_sensible_heat_flux) &&
+      (cfg->nsoillays < 2 || cfg->nsoillays > LGAME_MAX_SOIL_LAYERS))
+    return set_err(LGAME_ERR_BAD_CONFIG, "nsoillays must lie in 2.." + std::to_string(LGAME_MAX_SOIL_LAYERS) +
+                                         " with the prognostic soil");
+  if (cfg->nsoillays < 0 || cfg->nsoillays > LGAME_MAX_SOIL_LAYERS)
+    return set_err(LGAME_ERR_BAD_CONFIG, "nsoillays out of range");
+  if ((cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl) && !(cfg->karman > 0.0 && cfg->h_prandtl > 0.0))
+    return set_err(LGAME_ERR_BAD_CONFIG, "karman and h_prandtl must be positive with the surface layer on");
   return LGAME_OK;
 }
 
@@ -802,10 +846,30 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
   if ((rc = preload_budget_scratch()) != LGAME_OK) return fail(rc);
   const size_t F = (size_t)D.fstride;
   // grid
-  for (int f = 0; f < LGAME_GRID_NFIELDS; ++f) {
+  for (int f = 0; f < LGAME_GRID_LAND_FRACTION; ++f) {
     if (f == LGAME_GRID_INNER_PRODUCT_WEIGHTS || f == LGAME_GRID_TRSK_WEIGHTS_U || f == LGAME_GRID_TRSK_WEIGHTS_V) continue;
     size_t n = (f == LGAME_GRID_FVEC_X || f == LGAME_GRID_FVEC_Y || f == LGAME_GRID_FVEC_Z) ? (size_t)D.plane : F;
     if ((rc = dalloc(c, &c->grid[f], n)) != LGAME_OK) return fail(rc);
+  }
+  // surface layer and soil: one plane per surface field, nsoillays planes of soil temperature
+  // per slot, the soil grid in the kernels' parameter block
+  {
+    c->sfc_soil = cfg->lprog_soil_temp;
+    c->sfc_sens = cfg->lsfc_sensible_heat_flux;
+    c->sfc_pbl = cfg->lpbl;
+    c->sfc_turb = cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl;
+    for (double*& p : c->sfc_grid) if ((rc = dalloc(c, &p, (size_t)D.plane)) != LGAME_OK) return fail(rc);
+    SfcBuf& B = c->sbuf;
+    double** diag[] = {&B.rl, &B.rv, &B.mol, &B.sfr, &B.sens_soil, &B.sens_sea, &B.sst, &B.sw_in, &B.lw_out};
+    for (double** p : diag) if ((rc = dalloc(c, p, (size_t)D.plane)) != LGAME_OK) return fail(rc);
+    B.land = c->sfc_grid[0]; B.lake = c->sfc_grid[1]; B.rl_grid = c->sfc_grid[2];
+    B.rhoc = c->sfc_grid[3]; B.tcond = c->sfc_grid[4]; B.tconst = c->sfc_grid[5];
+    const int ns = cfg->nsoillays;
+    if (ns > 0)
+      for (double*& p : c->tsoil) if ((rc = dalloc(c, &p, (size_t)D.plane * ns)) != LGAME_OK) return fail(rc);
+    SfcPar& P = c->spar;
+    P.h_prandtl = cfg->h_prandtl; P.karman = cfg->karman; P.dtime = cfg->dtime; P.z_t_const = 0.0;
+    P.ns = ns; P.prog_soil = cfg->lprog_soil_temp; P.sens = cfg->lsfc_sensible_heat_flux;
   }
   for (int k = 0; k < 6; ++k) if ((rc = dalloc(c, &c->ipw[k], F)) != LGAME_OK) return fail(rc);
   for (int k = 0; k < 3; ++k) if ((rc = dalloc(c, &c->trsk_u[k], (size_t)D.P)) != LGAME_OK) return fail(rc);
@@ -887,7 +951,10 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     SplitDiff sd;
     sd.mom_h = c->diff_mom_h; sd.mom_v = c->diff_mom_v; sd.temp_h = c->diff_temp_h; sd.temp_v = c->diff_temp_v;
     sd.mass_h = c->diff_mass_h; sd.mass_v = c->diff_mass_v; sd.par = c->dpar;
-    if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, sd, &c->split, &c->bytes)) !=
+    SplitSfc sf;
+    sf.turb = c->sfc_turb; sf.pbl = c->sfc_pbl; sf.sens = c->sfc_sens; sf.soil = c->sfc_soil;
+    sf.buf = c->sbuf; sf.par = c->spar; sf.vsq = c->vsq; sf.tsoil[0] = c->tsoil[0]; sf.tsoil[1] = c->tsoil[1];
+    if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, sd, sf, &c->split, &c->bytes)) !=
         LGAME_OK)
       return fail(rc);
   }
@@ -897,12 +964,30 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
 
 extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfields) {
   if (!c || !f || nfields != LGAME_GRID_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_grid: bad arguments");
-  for (int i = 0; i < nfields; ++i) if (!f[i]) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_grid: null field");
+  const bool sfc_on = c->cfg.lprog_soil_temp || c->cfg.lsfc_sensible_heat_flux || c->cfg.lsfc_phase_trans || c->cfg.lpbl;
+  for (int i = 0; i < nfields; ++i)
+    if (!f[i] && (i < LGAME_GRID_LAND_FRACTION || sfc_on))
+      return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_grid: null field");
   const Dims& D = c->D;
   int rc;
-  for (int i = 0; i < LGAME_GRID_NFIELDS; ++i) {
+  for (int i = 0; i < LGAME_GRID_LAND_FRACTION; ++i) {
     if (i == LGAME_GRID_INNER_PRODUCT_WEIGHTS || i == LGAME_GRID_TRSK_WEIGHTS_U || i == LGAME_GRID_TRSK_WEIGHTS_V) continue;
     if ((rc = copy_h2d(c, c->grid[i], f[i], grid_ext(D, i))) != LGAME_OK) return rc;
+  }
+  // surface planes, the soil grid (parameters of the surface kernels), and the carried
+  // roughness length set to the grid's (control.F90:458)
+  for (int k = 0; k < 6; ++k) {
+    const int i = LGAME_GRID_LAND_FRACTION + k;
+    if (f[i] && (rc = copy_h2d(c, c->sfc_grid[k], f[i], grid_ext(D, i))) != LGAME_OK) return rc;
+  }
+  if (f[LGAME_GRID_ROUGHNESS_LENGTH])
+    CK(cudaMemcpyAsync(c->sbuf.rl, c->sfc_grid[2], sizeof(double) * (size_t)D.plane, cudaMemcpyDeviceToDevice, c->stream));
+  if (f[LGAME_GRID_Z_SOIL_INTERFACE] && f[LGAME_GRID_Z_SOIL_CENTER] && f[LGAME_GRID_Z_T_CONST]) {
+    SfcPar& P = c->spar;
+    for (int k = 0; k <= P.ns; ++k) P.zi[k] = f[LGAME_GRID_Z_SOIL_INTERFACE][k];
+    for (int k = 0; k < P.ns; ++k) P.zc[k] = f[LGAME_GRID_Z_SOIL_CENTER][k];
+    P.z_t_const = f[LGAME_GRID_Z_T_CONST][0];
+    if (c->split) split_set_sfc_par(c->split, P);
   }
   // inner product weights: (6,ny,nx,nl) -> six padded fields
   CK(cudaMemcpyAsync(c->staging, f[LGAME_GRID_INNER_PRODUCT_WEIGHTS], 6 * sizeof(double) * (size_t)D.ny * D.nx * D.nl,
@@ -977,13 +1062,17 @@ extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfie
 }
 
 namespace {
-int state_copy(lgame_gpu* c, int slot, double* const* hf, const double* const* cf, bool h2d) {
+// the first nfields state fields (LGAME_STATE_NFIELDS_ATMOS or LGAME_STATE_NFIELDS) of a slot
+int state_copy(lgame_gpu* c, int slot, double* const* hf, const double* const* cf, bool h2d,
+               int nfields = LGAME_STATE_NFIELDS_ATMOS) {
   const Dims& D = c->D;
   const State& S = c->st[slot];
-  double* dev[LGAME_STATE_NFIELDS] = {S.rho, S.rt, S.tp, S.ep, S.u, S.v, S.w};
-  const Ext ex[LGAME_STATE_NFIELDS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D)};
+  double* dev[LGAME_STATE_NFIELDS] = {S.rho, S.rt, S.tp, S.ep, S.u, S.v, S.w, c->tsoil[slot]};
+  const Ext ex[LGAME_STATE_NFIELDS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D),
+                                       {(size_t)D.ny, (size_t)D.nx, (size_t)c->spar.ns}};
   int rc;
-  for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+  for (int f = 0; f < nfields; ++f) {
+    if (f == LGAME_STATE_TEMPERATURE_SOIL && c->spar.ns == 0) continue;
     const int nrep = (f == LGAME_STATE_RHO) ? D.ncons : 1;
     const size_t hs = ex[f].n1 * ex[f].n2 * ex[f].n3;
     for (int r = 0; r < nrep; ++r) {
@@ -1003,9 +1092,9 @@ int state_copy(lgame_gpu* c, int slot, double* const* hf, const double* const* c
 }  // namespace
 
 extern "C" int lgame_gpu_set_state(lgame_gpu* c, int slot, const double* const* f, int nfields) {
-  if (!c || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS)
+  if (!c || !f || slot < 0 || slot > 1 || (nfields != LGAME_STATE_NFIELDS && nfields != LGAME_STATE_NFIELDS_ATMOS))
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_state: bad arguments");
-  int rc = state_copy(c, slot, nullptr, f, true);
+  int rc = state_copy(c, slot, nullptr, f, true, nfields);
   if (rc != LGAME_OK) return rc;
   c->mirror_valid[slot] = false;
   CK(cudaStreamSynchronize(c->stream));
@@ -1013,9 +1102,9 @@ extern "C" int lgame_gpu_set_state(lgame_gpu* c, int slot, const double* const* 
 }
 
 extern "C" int lgame_gpu_get_state(lgame_gpu* c, int slot, double* const* f, int nfields) {
-  if (!c || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS)
+  if (!c || !f || slot < 0 || slot > 1 || (nfields != LGAME_STATE_NFIELDS && nfields != LGAME_STATE_NFIELDS_ATMOS))
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_get_state: bad arguments");
-  int rc = state_copy(c, slot, f, nullptr, false);
+  int rc = state_copy(c, slot, f, nullptr, false, nfields);
   if (rc != LGAME_OK) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return LGAME_OK;
@@ -1052,6 +1141,16 @@ double* diag_dev(lgame_gpu* c, int f) {
     case LGAME_DIAG_MOM_DIFF_TEND_X: return c->dbuf.mdtx;
     case LGAME_DIAG_MOM_DIFF_TEND_Y: return c->dbuf.mdty;
     case LGAME_DIAG_MOM_DIFF_TEND_Z: return c->dbuf.mdtz;
+    case LGAME_DIAG_V_SQUARED: return c->vsq;
+    case LGAME_DIAG_ROUGHNESS_LENGTH: return c->sbuf.rl;
+    case LGAME_DIAG_ROUGHNESS_VELOCITY: return c->sbuf.rv;
+    case LGAME_DIAG_MONIN_OBUKHOV_LENGTH: return c->sbuf.mol;
+    case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: return c->sbuf.sfr;
+    case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL: return c->sbuf.sens_soil;
+    case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: return c->sbuf.sens_sea;
+    case LGAME_DIAG_SST: return c->sbuf.sst;
+    case LGAME_DIAG_SFC_SW_IN: return c->sbuf.sw_in;
+    case LGAME_DIAG_SFC_LW_OUT: return c->sbuf.lw_out;
   }
   return nullptr;
 }
@@ -1181,20 +1280,35 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
 
 extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_old, double* const* state_new,
                                      int nfields, int total_step_counter, int lrad_update, double t_0) {
-  if (!c || !state_old || !state_new || nfields != LGAME_STATE_NFIELDS)
+  if (!c || !state_old || !state_new || (nfields != LGAME_STATE_NFIELDS && nfields != LGAME_STATE_NFIELDS_ATMOS))
     return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: bad arguments");
+  const bool soil = nfields == LGAME_STATE_NFIELDS && c->spar.ns > 0;
+  if (!soil && (c->sfc_soil || c->sfc_sens))
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: the soil temperature is part of this run's state "
+                                          "(pass LGAME_STATE_NFIELDS arrays)");
+  if (soil && (!state_old[LGAME_STATE_TEMPERATURE_SOIL] || !state_new[LGAME_STATE_TEMPERATURE_SOIL]))
+    return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_pchevi_host: null soil temperature");
   const Dims& D = c->D;
-  const Ext ex[LGAME_STATE_NFIELDS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D)};
+  const Ext ex[LGAME_STATE_NFIELDS_ATMOS] = {ext_s(D), ext_s(D), ext_s(D), ext_s(D), ext_u(D), ext_v(D), ext_w(D)};
+  const Ext ex_soil{(size_t)D.ny, (size_t)D.nx, (size_t)c->spar.ns};
   const State& A = c->st[0];
   const State& B = c->st[1];
-  double* da[LGAME_STATE_NFIELDS] = {A.rho, A.rt, A.tp, A.ep, A.u, A.v, A.w};
-  double* db[LGAME_STATE_NFIELDS] = {B.rho, B.rt, B.tp, B.ep, B.u, B.v, B.w};
-  const double* vin[LGAME_STATE_NFIELDS];
-  double* vout[LGAME_STATE_NFIELDS];
+  double* da[LGAME_STATE_NFIELDS_ATMOS] = {A.rho, A.rt, A.tp, A.ep, A.u, A.v, A.w};
+  double* db[LGAME_STATE_NFIELDS_ATMOS] = {B.rho, B.rt, B.tp, B.ep, B.u, B.v, B.w};
+  const double* vin[LGAME_STATE_NFIELDS_ATMOS];
+  double* vout[LGAME_STATE_NFIELDS_ATMOS];
+  // the soil temperature (a few planes) takes the copy engines: into slots 0 and 1 (the new
+  // state starts as a copy of the old one), out of slot 1 after the step
+  if (soil) {
+    int rc = copy_h2d(c, c->tsoil[0], state_old[LGAME_STATE_TEMPERATURE_SOIL], ex_soil);
+    if (rc != LGAME_OK) return rc;
+    CK(cudaMemcpyAsync(c->tsoil[1], c->tsoil[0], sizeof(double) * (size_t)D.plane * c->spar.ns,
+                       cudaMemcpyDeviceToDevice, c->stream));
+  }
   // the GPU moves the state itself when every array is one it can address; a null array (not
   // copied) or an unregistered one takes the copy engines, as before
   bool direct_in = true, direct_out = true;
-  for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+  for (int f = 0; f < LGAME_STATE_NFIELDS_ATMOS; ++f) {
     direct_in = direct_in && (vin[f] = device_view(state_old[f])) != nullptr;
     direct_out = direct_out && (vout[f] = const_cast<double*>(device_view(state_new[f]))) != nullptr;
   }
@@ -1207,9 +1321,9 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     // state_old, into slot 1, with the FP32 mirrors of both in split mode
     StateF m0{}, m1{};
     if (c->split) { m0 = split_mirror(c->split, 0); m1 = split_mirror(c->split, 1); }
-    float* ma[LGAME_STATE_NFIELDS] = {m0.rho, m0.rt, m0.tp, m0.ep, m0.u, m0.v, m0.w};
-    float* mb[LGAME_STATE_NFIELDS] = {m1.rho, m1.rt, m1.tp, m1.ep, m1.u, m1.v, m1.w};
-    for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+    float* ma[LGAME_STATE_NFIELDS_ATMOS] = {m0.rho, m0.rt, m0.tp, m0.ep, m0.u, m0.v, m0.w};
+    float* mb[LGAME_STATE_NFIELDS_ATMOS] = {m1.rho, m1.rt, m1.tp, m1.ep, m1.u, m1.v, m1.w};
+    for (int f = 0; f < LGAME_STATE_NFIELDS_ATMOS; ++f) {
       k_state_in<<<grid_of(f), 256, 0, c->stream>>>(D, vin[f], (int)ex[f].n1, (int)ex[f].n2, (int)ex[f].n3, da[f],
                                                      db[f], ma[f], mb[f]);
       CK(cudaGetLastError());
@@ -1265,7 +1379,7 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     }
     CK(cudaStreamSynchronize(c->side));
   } else if (direct_out) {
-    for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
+    for (int f = 0; f < LGAME_STATE_NFIELDS_ATMOS; ++f) {
       k_state_out<<<grid_of(f), 256, 0, c->stream>>>(D, db[f], (int)ex[f].n1, (int)ex[f].n2, (int)ex[f].n3, vout[f]);
       CK(cudaGetLastError());
     }
@@ -1273,6 +1387,7 @@ extern "C" int lgame_gpu_pchevi_host(lgame_gpu* c, const double* const* state_ol
     rc = state_copy(c, 1, state_new, nullptr, false);
     if (rc != LGAME_OK) return rc;
   }
+  if (soil && (rc = copy_d2h(c, state_new[LGAME_STATE_TEMPERATURE_SOIL], c->tsoil[1], ex_soil)) != LGAME_OK) return rc;
   CK(cudaStreamSynchronize(c->stream));
   return LGAME_OK;
 }

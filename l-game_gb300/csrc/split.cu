@@ -84,6 +84,8 @@ struct SplitCtx {
   // diffusion closure: configuration and FP32 buffers (the carried ones are in C)
   SplitDiff diff{};
   DiffBuf<float> db{};
+  // surface layer, PBL and soil (FP64 buffers of the FP64 step)
+  SplitSfc sfc{};
 };
 
 namespace {
@@ -1276,7 +1278,8 @@ dim3 cgrd(int rows, int cols) { return dim3((unsigned)((rows + 31) / 32), (unsig
 
 }  // namespace
 
-int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCtx** out, long long* bytes) {
+int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const SplitSfc& sfc, SplitCtx** out,
+                 long long* bytes) {
   if (D.ncons > 1 && D.ncons != kTracers + 1) {
     lgame_set_error("split precision: the tracer kernel is built for five condensates and water vapour");
     return LGAME_ERR_UNSUPPORTED;
@@ -1306,7 +1309,9 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCt
   float** scratch[] = {&s->gx, &s->gy, &s->gz, &s->divf, &s->tvu, &s->tvv, &s->tpu, &s->tpv,
                        &s->ex, &s->ey, &s->ez, &s->uph, &s->vph, &s->wph};
   for (float** p : scratch) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
-  if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
+  s->sfc = sfc;
+  if (sfc.vsq) s->vsq = sfc.vsq;
+  else if ((rc = salloc(s, &s->vsq, F, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->gzd, F, bytes)) || (rc = salloc(s, &s->rmz, F, bytes))) return fail(rc);
   if (D.nc > 0 && (rc = salloc(s, &s->csh_part, F * D.nc, bytes))) return fail(rc);
   if ((rc = salloc(s, &s->dbg, F, bytes)) || (rc = salloc(s, &s->tbu, F, bytes)) || (rc = salloc(s, &s->tbv, F, bytes)))
@@ -1343,6 +1348,7 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCt
 }
 
 void split_set_diff_par(SplitCtx* s, const DiffPar& par) { s->diff.par = par; }
+void split_set_sfc_par(SplitCtx* s, const SfcPar& par) { s->sfc.par = par; }
 
 void split_destroy(SplitCtx* s) {
   if (!s) return;
@@ -1594,6 +1600,10 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     return LGAME_OK;
   };
   SL("ks_temperature", (k_temperature<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, GF, Mo, C.temperature);
+  // the surface parts in FP64 on the FP64 state (two-dimensional): update_sfc_turb_quantities
+  // before the substeps (mo_manage_pchevi.F90:51-53)
+  const SplitSfc& SF = s->sfc;
+  if (SF.turb) SL("ks_sfc_turb", k_sfc_turb, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par);
   Carried<float> CC{pg.nl_u, pg.nl_v, pg.nl_w, pg.l_u, pg.l_v, pg.l_w, pg.old_u, pg.old_v, C.pgcw,
                     C.vsg_x, C.vsg_y, C.vsg_z, C.pvt_x, C.pvt_y, C.pvt_z};
   for (int rk = 1; rk <= 2; ++rk) {
@@ -1632,6 +1642,8 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
       SL("ks_diff_vz", (k_diff_vz<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
       SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
       if (SD.mom_v) SL("ks_mom_diff_v", (k_mom_diff_v<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, Mo, DB);
+      if (SF.pbl)
+        SL("ks_pbl", k_pbl<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
       SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
       CC.mdt_x = DB.mdtx; CC.mdt_y = DB.mdty; CC.mdt_z = DB.mdtz;
     } else if (rk == 1 && D.lklemp && D.ndamp > 0) {
@@ -1677,6 +1689,9 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
        s->fv, s->gu, s->gv);
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
        C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh);
+    if (SF.sens || SF.soil)
+      SL("ks_sfc_column", k_sfc_column<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, rk == 1 ? So : Sn, T.rt, SF.buf,
+         SF.par, SF.tsoil[so], SF.tsoil[rk == 1 ? so : sn], SF.tsoil[sn]);
     const dim3 gc = cgrd(D.ny, D.nx);
     if (s->column_fp64)
       SL("ks_column_ver", ks_column_ver<double>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);

@@ -19,6 +19,7 @@
 
 #include "diffusion.cuh"
 #include "kernels.cuh"
+#include "surface.cuh"
 
 namespace lg {
 
@@ -43,9 +44,23 @@ struct SplitDiff {
   DiffPar par{};
 };
 
+// the surface layer, PBL and soil of the split step: which parts run and the FP64 buffers they
+// share with the FP64 step (surface planes, soil temperature of the two slots, v_squared)
+struct SplitSfc {
+  bool turb = false, pbl = false, sens = false, soil = false;
+  SfcBuf buf{};
+  SfcPar par{};
+  double* vsq = nullptr;
+  double* tsoil[2] = {nullptr, nullptr};
+};
+
 // column_fp64: the vertical acoustic solve with FP64 coefficients and elimination; diff: the
-// diffusion closure (its buffers are allocated when horizontal momentum diffusion is on)
-int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, SplitCtx** out, long long* bytes);
+// diffusion closure (its buffers are allocated when horizontal momentum diffusion is on);
+// sfc: the surface parts, whose kinetic-energy array the split step uses as its own
+int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const SplitSfc& sfc, SplitCtx** out,
+                 long long* bytes);
+// the surface kernels' parameters once the soil grid is known
+void split_set_sfc_par(SplitCtx* s, const SfcPar& par);
 // the closure's constants once the grid is known (mean_velocity_area)
 void split_set_diff_par(SplitCtx* s, const DiffPar& par);
 void split_destroy(SplitCtx* s);

@@ -29,8 +29,12 @@ GRID_FIELDS = ["z_scalar", "z_u", "z_v", "z_w", "dx", "dy", "dz", "volume", "are
                "area_dual_x", "area_dual_y", "area_dual_z", "z_area_dual_z", "slope_x", "slope_y",
                "inner_product_weights", "theta_v_bg", "exner_bg", "exner_bg_grad_u", "exner_bg_grad_v",
                "exner_bg_grad_w", "gravity_m_v", "gravity_potential", "fvec_x", "fvec_y", "fvec_z",
-               "trsk_weights_u", "trsk_weights_v", "dx_dual", "dy_dual", "layer_thickness"]
-STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w"]
+               "trsk_weights_u", "trsk_weights_v", "dx_dual", "dy_dual", "layer_thickness",
+               "land_fraction", "lake_fraction", "roughness_length", "sfc_rho_c", "t_conduc_soil", "t_const_soil",
+               "z_soil_interface", "z_soil_center", "z_t_const"]
+STATE_FIELDS = ["rho", "rhotheta_v", "theta_v_pert", "exner_pert", "wind_u", "wind_v", "wind_w", "temperature_soil"]
+# the atmosphere's fields (LGAME_STATE_NFIELDS_ATMOS): a state dict without the soil temperature
+ATMOS_FIELDS = STATE_FIELDS[:7]
 # fields of an output file (enum lgame_output_field), float32, scalar points
 OUTPUT_FIELDS = ["rho", "temperature", "rel_humidity", "wind_u", "wind_v", "wind_w"]
 # one level of lateral boundary data (t_bc, mo_definitions.F90:117-131), state-field shapes
@@ -64,24 +68,26 @@ def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
-def write_snapshot(path, ny, nx, nl, ncons, step, slot0: dict, slot1: dict, diag: dict):
-    """Restart snapshot of both state slots, the carried diagnostics and the step counter."""
+def write_snapshot(path, ny, nx, nl, ncons, step, slot0: dict, slot1: dict, diag: dict, ns: int = 0):
+    """Restart snapshot of both state slots (ns soil layers), the carried diagnostics and the
+    step counter."""
     lib = load_library()
-    arr = lambda d, names: [np.asfortranarray(d[f], dtype=np.float64) for f in names]
+    sh = field_shapes(ny, nx, nl, ncons, ns)
+    arr = lambda d, names: [np.asfortranarray(d[f] if f in d else np.zeros(sh[f]), dtype=np.float64) for f in names]
     a0, a1, ad = arr(slot0, STATE_FIELDS), arr(slot1, STATE_FIELDS), arr(diag, DIAG_FIELDS)
-    check(lib.lgame_host_write_snapshot(str(path).encode(), ny, nx, nl, ncons, step, ptr_array(a0), ptr_array(a1),
-                                        ptr_array(ad)), "lgame_host_write_snapshot")
+    check(lib.lgame_host_write_snapshot(str(path).encode(), ny, nx, nl, ncons, ns, step, ptr_array(a0),
+                                        ptr_array(a1), ptr_array(ad)), "lgame_host_write_snapshot")
 
 
-def read_snapshot(path, ny, nx, nl, ncons):
+def read_snapshot(path, ny, nx, nl, ncons, ns: int = 0):
     """(step, slot 0 state, slot 1 state, diagnostics) of a snapshot written for these dimensions."""
     lib = load_library()
-    sh = field_shapes(ny, nx, nl, ncons)
+    sh = field_shapes(ny, nx, nl, ncons, ns)
     s0 = {f: np.zeros(sh[f], order="F") for f in STATE_FIELDS}
     s1 = {f: np.zeros(sh[f], order="F") for f in STATE_FIELDS}
     dg = {f: np.zeros(sh[f], order="F") for f in DIAG_FIELDS}
     step = C.c_longlong()
-    check(lib.lgame_host_read_snapshot(str(path).encode(), ny, nx, nl, ncons, C.byref(step),
+    check(lib.lgame_host_read_snapshot(str(path).encode(), ny, nx, nl, ncons, ns, C.byref(step),
                                        ptr_array([s0[f] for f in STATE_FIELDS]), ptr_array([s1[f] for f in STATE_FIELDS]),
                                        ptr_array([dg[f] for f in DIAG_FIELDS])), "lgame_host_read_snapshot")
     return step.value, s0, s1, dg
@@ -132,7 +138,10 @@ DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_
                "pot_vort_tend_x", "pot_vort_tend_y", "pot_vort_tend_z", "v_squared_grad_x", "v_squared_grad_y",
                "v_squared_grad_z", "condensates_sediment_heat", "radiation_tendency", "temperature",
                "tend_rho", "tend_rhotheta_v", "tend_wind_u", "tend_wind_v", "tend_wind_w",
-               "tke", "viscosity", "heating_diss", "mom_diff_tend_x", "mom_diff_tend_y", "mom_diff_tend_z"]
+               "tke", "viscosity", "heating_diss", "mom_diff_tend_x", "mom_diff_tend_y", "mom_diff_tend_z",
+               "v_squared", "roughness_length_diag", "roughness_velocity", "monin_obukhov_length",
+               "scalar_flux_resistance", "power_flux_density_sens_soil", "power_flux_density_sens_sea", "sst",
+               "sfc_sw_in", "sfc_lw_out"]
 
 
 class Config(C.Structure):
@@ -148,7 +157,7 @@ class Config(C.Structure):
                 ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lperiodic", C.c_int),
                 ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int),
                 ("device", C.c_int), ("diff_coeff_scheme_h", C.c_int), ("bg_shear", C.c_double),
-                ("c_s", C.c_double)]
+                ("c_s", C.c_double), ("nsoillays", C.c_int), ("h_prandtl", C.c_double), ("karman", C.c_double)]
 
 
 def _s(n):
@@ -228,8 +237,8 @@ def load_library(path: str | os.PathLike | None = None):
         "lgame_gpu_set_graphs": (i, [vp, i]),
         "lgame_gpu_output": (i, [vp, i, i, d, d, C.POINTER(C.POINTER(C.c_float)), i, C.POINTER(i)]),
         "lgame_gpu_bc_setup": (i, [vp, i, i, d, BC_LOADER, vp]),
-        "lgame_host_write_snapshot": (i, [C.c_char_p, i, i, i, i, ll, pp, pp, pp]),
-        "lgame_host_read_snapshot": (i, [C.c_char_p, i, i, i, i, C.POINTER(ll), pp, pp, pp]),
+        "lgame_host_write_snapshot": (i, [C.c_char_p, i, i, i, i, i, ll, pp, pp, pp]),
+        "lgame_host_read_snapshot": (i, [C.c_char_p, i, i, i, i, i, C.POINTER(ll), pp, pp, pp]),
         "lgame_host_write_bc_level": (i, [C.c_char_p, i, i, i, i, d] + [C.POINTER(C.c_double)] * 5),
         "lgame_host_read_bc_level": (i, [C.c_char_p, i, i, i, i, C.POINTER(d)] + [C.POINTER(C.c_double)] * 5),
         "lgame_host_bc_filename": (i, [C.c_char_p, d, d, C.c_char_p, i]),
@@ -294,8 +303,10 @@ def check(rc: int, what: str = ""):
 
 
 # ---- shapes (Fortran order, the reference's extents) ----------------------------
-def field_shapes(ny: int, nx: int, nl: int, ncons: int) -> dict[str, tuple]:
+def field_shapes(ny: int, nx: int, nl: int, ncons: int, ns: int = 0) -> dict[str, tuple]:
+    """Shapes of every grid, state and diagnostic field; ns = nsoillays."""
     s, u, v, w = (ny, nx, nl), (ny, nx + 1, nl), (ny + 1, nx, nl), (ny, nx, nl + 1)
+    p = (ny, nx)
     z, ex, ey = (ny + 1, nx + 1, nl), (ny + 1, nx, nl + 1), (ny, nx + 1, nl + 1)
     return {
         "z_scalar": s, "z_u": u, "z_v": v, "z_w": w, "dx": u, "dy": v, "dz": w, "volume": s,
@@ -315,7 +326,18 @@ def field_shapes(ny: int, nx: int, nl: int, ncons: int) -> dict[str, tuple]:
         "dx_dual": v, "dy_dual": u, "layer_thickness": s,
         "tke": s, "viscosity": s, "heating_diss": s, "mom_diff_tend_x": u, "mom_diff_tend_y": v,
         "mom_diff_tend_z": w,
+        "land_fraction": p, "lake_fraction": p, "roughness_length": p, "sfc_rho_c": p, "t_conduc_soil": p,
+        "t_const_soil": p, "z_soil_interface": (ns + 1,), "z_soil_center": (ns,), "z_t_const": (1,),
+        "temperature_soil": (ny, nx, ns),
+        "v_squared": s, "roughness_length_diag": p, "roughness_velocity": p, "monin_obukhov_length": p,
+        "scalar_flux_resistance": p, "power_flux_density_sens_soil": p, "power_flux_density_sens_sea": p,
+        "sst": p, "sfc_sw_in": p, "sfc_lw_out": p,
     }
+
+
+def state_fields(state: dict) -> list:
+    """The state fields a dict carries: all of STATE_FIELDS, or the atmosphere's alone."""
+    return STATE_FIELDS if "temperature_soil" in state else ATMOS_FIELDS
 
 
 def ptr_array(arrays: list) -> C.Array:
@@ -358,7 +380,8 @@ class HostModel:
         check(self.lib.lgame_host_setup(C.byref(nml), C.byref(self.h)), "lgame_host_setup")
         self.ny, self.nx, self.nl = nml.ny, nml.nx, nml.n_layers
         self.ncons = nml.n_constituents
-        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons)
+        self.ns = nml.nsoillays
+        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons, self.ns)
         self.grid = {f: self._view(self.lib.lgame_host_grid_field, k, f) for k, f in enumerate(GRID_FIELDS)}
         self.state = {f: self._view(self.lib.lgame_host_state_field, k, f) for k, f in enumerate(STATE_FIELDS)}
         self.diag = {f: self._view(self.lib.lgame_host_diag_field, k, f) for k, f in enumerate(DIAG_FIELDS)}
@@ -403,18 +426,19 @@ class GpuModel:
         check(self.lib.lgame_gpu_create(C.byref(cfg), C.byref(self.h)), "lgame_gpu_create")
         self.ny, self.nx, self.nl = cfg.ny, cfg.nx, cfg.n_layers
         self.ncons = 7 if cfg.lmoist else 1
-        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons)
-        arrs = [np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
+        self.ns = cfg.nsoillays
+        self.shapes = field_shapes(self.ny, self.nx, self.nl, self.ncons, self.ns)
+        arrs = [None if grid.get(f) is None else np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
         check(self.lib.lgame_gpu_set_grid(self.h, ptr_array(arrs), len(arrs)), "lgame_gpu_set_grid")
 
     def set_state(self, slot: int, state: dict):
-        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in STATE_FIELDS]
+        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in state_fields(state)]
         check(self.lib.lgame_gpu_set_state(self.h, slot, ptr_array(arrs), len(arrs)), "lgame_gpu_set_state")
 
     def get_state(self, slot: int) -> dict:
         out = {f: np.zeros(self.shapes[f], order="F") for f in STATE_FIELDS}
-        check(self.lib.lgame_gpu_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]), 7),
-              "lgame_gpu_get_state")
+        check(self.lib.lgame_gpu_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]),
+                                           len(STATE_FIELDS)), "lgame_gpu_get_state")
         return out
 
     def set_diag(self, diag: dict):
@@ -431,9 +455,10 @@ class GpuModel:
         check(self.lib.lgame_gpu_pchevi(self.h, old_slot, new_slot, step, lrad_update, t0), "lgame_gpu_pchevi")
 
     def pchevi_host(self, state_old: dict, state_new: dict, step: int):
-        a = [state_old[f] for f in STATE_FIELDS]
-        b = [state_new[f] for f in STATE_FIELDS]
-        check(self.lib.lgame_gpu_pchevi_host(self.h, ptr_array(a), ptr_array(b), 7, step, 0, 0.0),
+        names = state_fields(state_old)
+        a = [state_old[f] for f in names]
+        b = [state_new[f] for f in names]
+        check(self.lib.lgame_gpu_pchevi_host(self.h, ptr_array(a), ptr_array(b), len(names), step, 0, 0.0),
               "lgame_gpu_pchevi_host")
 
     def budgets(self, slot: int) -> np.ndarray:

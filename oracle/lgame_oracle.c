@@ -38,6 +38,7 @@ static const double c_d_p = 1005.0;
 static const double M_PI_ = 3.14159265358979323846;  /* 4._wp*atan(1._wp) */
 static const double p_0 = 100000.0;
 static const double r_v = 461.524879;
+#define GRAVITY 9.80616                               /* gravity, mo_constants.F90:21 */
 
 struct oracle_ctx {
   int ny, nx, nl, n_levels, n_oro_layers, n_flat_layers;
@@ -51,6 +52,10 @@ struct oracle_ctx {
    * 2*sum(area_z(:,:,n_levels))/(ny*nx) (mo_grid_generator.F90:1111) */
   int lmom_diff_h, lmom_diff_v, ltemp_diff_h, ltemp_diff_v, lmass_diff_h, lmass_diff_v, diff_h_tke;
   double bg_shear, c_s, eff_hor_res, mean_velocity_area;
+  /* &surface (mo_surface_nml.F90:12-20) and the surface-layer constants of &diff; the soil grid's
+   * depth of the constant temperature (mo_grid_generator.F90:1363) */
+  int lprog_soil_temp, lsfc_sensible_heat_flux, lsfc_phase_trans, lpbl, nsoil;
+  double h_prandtl, karman, z_t_const;
   /* grid */
   double *z_scalar, *z_u, *z_v, *z_w, *gdx, *gdy, *gdz, *volume, *area_x, *area_y, *area_z;
   double *area_dual_x, *area_dual_y, *area_dual_z, *z_area_dual_z, *slope_x, *slope_y, *ipw;
@@ -73,7 +78,15 @@ struct oracle_ctx {
   double *tke, *viscosity, *viscosity_molecular, *viscosity_dual, *n_squared, *du_dz, *dv_dz;
   double *vert_hor_viscosity_u, *vert_hor_viscosity_v, *mass_diff_coeff_eff_h, *mass_diff_coeff_eff_v;
   double *temp_diff_coeff_eff_h, *temp_diff_coeff_eff_v, *flux_density_w;
-  double *condensates_sediment_heat, *mass_diff_tendency, *a_rain;
+  double *condensates_sediment_heat, *mass_diff_tendency;
+  /* the surface and the soil: grid (roughness_length_grid is grid%roughness_length), the soil
+   * temperature of the two states, the surface diagnostics (roughness_length is
+   * diag%roughness_length) */
+  double *land_fraction, *lake_fraction, *roughness_length_grid, *sfc_rho_c, *t_conduc_soil, *t_const_soil;
+  double *z_soil_interface, *z_soil_center, *temperature_soil[2];
+  double *roughness_length, *roughness_velocity, *monin_obukhov_length, *scalar_flux_resistance;
+  double *sens_soil, *sens_sea, *sst, *sfc_sw_in, *sfc_lw_out;
+  double *a_rain;
   /* lateral boundary conditions (t_bc, mo_definitions.F90:117-131): two time levels, the
    * rescale factors, the level indices (1-based) and the time of the older level */
   int bc_on, bc_index_old, bc_index_new, dtime_bc;
@@ -126,6 +139,11 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   o->ltemp_diff_v = cfg->ltemp_diff_v; o->lmass_diff_h = cfg->lmass_diff_h; o->lmass_diff_v = cfg->lmass_diff_v;
   o->diff_h_tke = cfg->diff_coeff_scheme_h == LGAME_DIFF_COEFF_TKE;
   o->bg_shear = cfg->bg_shear; o->c_s = cfg->c_s; o->eff_hor_res = sqrt(cfg->dx*cfg->dy);
+  o->lprog_soil_temp = cfg->lprog_soil_temp; o->lsfc_sensible_heat_flux = cfg->lsfc_sensible_heat_flux;
+  o->lsfc_phase_trans = cfg->lsfc_phase_trans; o->lpbl = cfg->lpbl;
+  o->nsoil = cfg->nsoillays > 0 ? cfg->nsoillays : 0;
+  o->h_prandtl = cfg->h_prandtl; o->karman = cfg->karman;
+  if (o->nsoil > LGAME_MAX_SOIL_LAYERS) { free(o); return LGAME_ERR_BAD_CONFIG; }
   DIMS;
   const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
   const size_t nW = (size_t)ny*nx*(nl+1), nZ = (size_t)(ny+1)*(nx+1)*nl;
@@ -169,6 +187,16 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   o->vert_hor_viscosity_u = zalloc((size_t)ny*(nx+1)*(nl+1)); o->vert_hor_viscosity_v = zalloc((size_t)(ny+1)*nx*(nl+1));
   o->mass_diff_coeff_eff_h = zalloc(nS); o->mass_diff_coeff_eff_v = zalloc(nS);
   o->temp_diff_coeff_eff_h = zalloc(nS); o->temp_diff_coeff_eff_v = zalloc(nS); o->flux_density_w = zalloc(nW);
+  {
+    const size_t n2 = (size_t)ny*nx;
+    o->land_fraction = zalloc(n2); o->lake_fraction = zalloc(n2); o->roughness_length_grid = zalloc(n2);
+    o->sfc_rho_c = zalloc(n2); o->t_conduc_soil = zalloc(n2); o->t_const_soil = zalloc(n2);
+    o->z_soil_interface = zalloc((size_t)o->nsoil + 1); o->z_soil_center = zalloc((size_t)o->nsoil);
+    o->temperature_soil[0] = zalloc(n2*(size_t)o->nsoil); o->temperature_soil[1] = zalloc(n2*(size_t)o->nsoil);
+    o->roughness_length = zalloc(n2); o->roughness_velocity = zalloc(n2); o->monin_obukhov_length = zalloc(n2);
+    o->scalar_flux_resistance = zalloc(n2); o->sens_soil = zalloc(n2); o->sens_sea = zalloc(n2);
+    o->sst = zalloc(n2); o->sfc_sw_in = zalloc(n2); o->sfc_lw_out = zalloc(n2);
+  }
   o->a_rain = zalloc(nS);
   for (double** q = &o->z_scalar; q <= &o->a_rain; ++q)
     if (!*q) { oracle_destroy(o); return LGAME_ERR_ALLOC; }
@@ -215,6 +243,11 @@ static size_t grid_size(const oracle_ctx* o, int f) {
     case LGAME_GRID_DX_DUAL: return nV;
     case LGAME_GRID_DY_DUAL: return nU;
     case LGAME_GRID_LAYER_THICKNESS: return nS;
+    case LGAME_GRID_LAND_FRACTION: case LGAME_GRID_LAKE_FRACTION: case LGAME_GRID_ROUGHNESS_LENGTH:
+    case LGAME_GRID_SFC_RHO_C: case LGAME_GRID_T_CONDUC_SOIL: case LGAME_GRID_T_CONST_SOIL: return (size_t)ny*nx;
+    case LGAME_GRID_Z_SOIL_INTERFACE: return (size_t)o->nsoil + 1;
+    case LGAME_GRID_Z_SOIL_CENTER: return (size_t)o->nsoil;
+    case LGAME_GRID_Z_T_CONST: return 1;
   }
   return 0;
 }
@@ -226,11 +259,19 @@ int oracle_set_grid(oracle_ctx* o, const double* const* f, int nfields) {
     o->area_z, o->area_dual_x, o->area_dual_y, o->area_dual_z, o->z_area_dual_z, o->slope_x,
     o->slope_y, o->ipw, o->theta_v_bg, o->exner_bg, o->exner_bg_grad_u, o->exner_bg_grad_v,
     o->exner_bg_grad_w, o->gravity_m_v, o->gravity_potential, o->fvec_x, o->fvec_y, o->fvec_z,
-    o->trsk_u, o->trsk_v, o->dx_dual, o->dy_dual, o->layer_thickness};
+    o->trsk_u, o->trsk_v, o->dx_dual, o->dy_dual, o->layer_thickness, o->land_fraction, o->lake_fraction,
+    o->roughness_length_grid, o->sfc_rho_c, o->t_conduc_soil, o->t_const_soil, o->z_soil_interface,
+    o->z_soil_center, &o->z_t_const};
+  const int sfc_on = o->lprog_soil_temp || o->lsfc_sensible_heat_flux || o->lsfc_phase_trans || o->lpbl;
   for (int i = 0; i < LGAME_GRID_NFIELDS; ++i) {
-    if (!f[i]) return LGAME_ERR_INVALID_ARG;
+    if (!f[i]) {
+      if (i >= LGAME_GRID_LAND_FRACTION && !sfc_on) continue;  /* surface fields, surface off */
+      return LGAME_ERR_INVALID_ARG;
+    }
     memcpy(dst[i], f[i], grid_size(o, i)*sizeof(double));
   }
+  /* diag%roughness_length = grid%roughness_length, control.F90:458 */
+  memcpy(o->roughness_length, o->roughness_length_grid, (size_t)o->ny*o->nx*sizeof(double));
   /* mean_velocity_area, mo_grid_generator.F90:1111: the surface areas summed in array order */
   {
     const size_t n2 = (size_t)o->ny*o->nx, base = n2*(size_t)o->nl;
@@ -275,24 +316,30 @@ static void state_ptrs(oracle_ctx* o, int s, double** p, size_t* n) {
   p[4] = o->wind_u[s]; n[4] = (size_t)ny*(nx+1)*nl;
   p[5] = o->wind_v[s]; n[5] = (size_t)(ny+1)*nx*nl;
   p[6] = o->wind_w[s]; n[6] = (size_t)ny*nx*(nl+1);
+  p[7] = o->temperature_soil[s]; n[7] = (size_t)ny*nx*(size_t)o->nsoil;
 }
 
 int oracle_set_state(oracle_ctx* o, int slot, const double* const* f, int nfields) {
-  if (!o || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  if (!o || !f || slot < 0 || slot > 1 || (nfields != LGAME_STATE_NFIELDS && nfields != LGAME_STATE_NFIELDS_ATMOS))
+    return LGAME_ERR_INVALID_ARG;
   double* p[LGAME_STATE_NFIELDS]; size_t n[LGAME_STATE_NFIELDS];
   state_ptrs(o, slot, p, n);
-  for (int i = 0; i < LGAME_STATE_NFIELDS; ++i) {
-    if (!f[i]) return LGAME_ERR_INVALID_ARG;
+  for (int i = 0; i < nfields; ++i) {
+    if (!f[i]) {
+      if (i == LGAME_STATE_TEMPERATURE_SOIL && n[i] == 0) continue;
+      return LGAME_ERR_INVALID_ARG;
+    }
     memcpy(p[i], f[i], n[i]*sizeof(double));
   }
   return LGAME_OK;
 }
 
 int oracle_get_state(oracle_ctx* o, int slot, double* const* f, int nfields) {
-  if (!o || !f || slot < 0 || slot > 1 || nfields != LGAME_STATE_NFIELDS) return LGAME_ERR_INVALID_ARG;
+  if (!o || !f || slot < 0 || slot > 1 || (nfields != LGAME_STATE_NFIELDS && nfields != LGAME_STATE_NFIELDS_ATMOS))
+    return LGAME_ERR_INVALID_ARG;
   double* p[LGAME_STATE_NFIELDS]; size_t n[LGAME_STATE_NFIELDS];
   state_ptrs(o, slot, p, n);
-  for (int i = 0; i < LGAME_STATE_NFIELDS; ++i)
+  for (int i = 0; i < nfields; ++i)
     if (f[i]) memcpy(f[i], p[i], n[i]*sizeof(double));
   return LGAME_OK;
 }
@@ -329,6 +376,17 @@ static void diag_ptrs(oracle_ctx* o, double** p, size_t* n) {
   p[LGAME_DIAG_MOM_DIFF_TEND_X] = o->mom_diff_tend_x; n[LGAME_DIAG_MOM_DIFF_TEND_X] = nU;
   p[LGAME_DIAG_MOM_DIFF_TEND_Y] = o->mom_diff_tend_y; n[LGAME_DIAG_MOM_DIFF_TEND_Y] = nV;
   p[LGAME_DIAG_MOM_DIFF_TEND_Z] = o->mom_diff_tend_z; n[LGAME_DIAG_MOM_DIFF_TEND_Z] = nW;
+  const size_t n2 = (size_t)ny*nx;
+  p[LGAME_DIAG_V_SQUARED] = o->v_squared; n[LGAME_DIAG_V_SQUARED] = nS;
+  p[LGAME_DIAG_ROUGHNESS_LENGTH] = o->roughness_length; n[LGAME_DIAG_ROUGHNESS_LENGTH] = n2;
+  p[LGAME_DIAG_ROUGHNESS_VELOCITY] = o->roughness_velocity; n[LGAME_DIAG_ROUGHNESS_VELOCITY] = n2;
+  p[LGAME_DIAG_MONIN_OBUKHOV_LENGTH] = o->monin_obukhov_length; n[LGAME_DIAG_MONIN_OBUKHOV_LENGTH] = n2;
+  p[LGAME_DIAG_SCALAR_FLUX_RESISTANCE] = o->scalar_flux_resistance; n[LGAME_DIAG_SCALAR_FLUX_RESISTANCE] = n2;
+  p[LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL] = o->sens_soil; n[LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL] = n2;
+  p[LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA] = o->sens_sea; n[LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA] = n2;
+  p[LGAME_DIAG_SST] = o->sst; n[LGAME_DIAG_SST] = n2;
+  p[LGAME_DIAG_SFC_SW_IN] = o->sfc_sw_in; n[LGAME_DIAG_SFC_SW_IN] = n2;
+  p[LGAME_DIAG_SFC_LW_OUT] = o->sfc_lw_out; n[LGAME_DIAG_SFC_LW_OUT] = n2;
 }
 
 int oracle_set_diag(oracle_ctx* o, const double* const* f, int nfields) {

@@ -20,7 +20,8 @@ _lib = None
 
 def build(force: bool = False) -> Path:
     srcs = [HERE / "lgame_oracle.c", HERE / "lgame_oracle_ops.inc", HERE / "lgame_oracle_step.inc",
-            HERE / "lgame_oracle.h", HERE.parent / "include" / "lgame_gpu.h", HERE / "Makefile"]
+            HERE / "lgame_oracle_diff.inc", HERE / "lgame_oracle_sfc.inc", HERE / "lgame_oracle.h",
+            HERE.parent / "include" / "lgame_gpu.h", HERE / "Makefile"]
     if force or not LIB_PATH.exists() or any(s.stat().st_mtime > LIB_PATH.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "all"], check=True)
     return LIB_PATH
@@ -75,21 +76,21 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle_create failed: {rc}")
         self.ncons = 7 if cfg.lmoist else 1
-        self.shapes = field_shapes(cfg.ny, cfg.nx, cfg.n_layers, self.ncons)
-        arrs = [np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
+        self.shapes = field_shapes(cfg.ny, cfg.nx, cfg.n_layers, self.ncons, cfg.nsoillays)
+        arrs = [None if grid.get(f) is None else np.asfortranarray(grid[f], dtype=np.float64) for f in GRID_FIELDS]
         rc = self.lib.oracle_set_grid(self.h, ptr_array(arrs), len(arrs))
         if rc != 0:
             raise RuntimeError(f"oracle_set_grid failed: {rc}")
 
     def set_state(self, slot, state):
-        from lgame_gpu import STATE_FIELDS, ptr_array
-        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in STATE_FIELDS]
+        from lgame_gpu import ptr_array, state_fields
+        arrs = [np.asfortranarray(state[f], dtype=np.float64) for f in state_fields(state)]
         assert self.lib.oracle_set_state(self.h, slot, ptr_array(arrs), len(arrs)) == 0
 
     def get_state(self, slot):
         from lgame_gpu import STATE_FIELDS, ptr_array
         out = {f: np.zeros(self.shapes[f], order="F") for f in STATE_FIELDS}
-        assert self.lib.oracle_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]), 7) == 0
+        assert self.lib.oracle_get_state(self.h, slot, ptr_array([out[f] for f in STATE_FIELDS]), len(STATE_FIELDS)) == 0
         return out
 
     def set_diag(self, diag):

@@ -37,15 +37,15 @@ static int step_both_ways(lgame_host_model* hm, const lgame_config* cfg0, int pr
   for (int f = 0; f < LGAME_GRID_NFIELDS; ++f) {
     size_t n = 0;
     grid[f] = lgame_host_grid_field(hm, f, &n);
-    if (!grid[f]) return 1;
+    if (!grid[f] && n) return 1;
   }
   double* dev_out[LGAME_STATE_NFIELDS];
   double* host_mid[LGAME_STATE_NFIELDS];
   double* host_out[LGAME_STATE_NFIELDS];
   for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
-    dev_out[f] = malloc(nst[f] * sizeof(double));
-    host_mid[f] = malloc(nst[f] * sizeof(double));
-    host_out[f] = malloc(nst[f] * sizeof(double));
+    dev_out[f] = malloc((nst[f] ? nst[f] : 1) * sizeof(double));
+    host_mid[f] = malloc((nst[f] ? nst[f] : 1) * sizeof(double));
+    host_out[f] = malloc((nst[f] ? nst[f] : 1) * sizeof(double));
     if (!dev_out[f] || !host_mid[f] || !host_out[f]) return 1;
   }
   lgame_gpu* a = NULL;
@@ -108,9 +108,9 @@ int main(int argc, char** argv) {
   size_t nst[LGAME_STATE_NFIELDS], ndg[LGAME_DIAG_NFIELDS];
   for (int f = 0; f < LGAME_STATE_NFIELDS; ++f) {
     st[f] = lgame_host_state_field(hm, f, &nst[f]);
-    st2[0][f] = malloc(nst[f] * sizeof(double));
-    st2[1][f] = malloc(nst[f] * sizeof(double));
-    if (!st[f] || !st2[0][f] || !st2[1][f]) return 1;
+    st2[0][f] = malloc((nst[f] ? nst[f] : 1) * sizeof(double));
+    st2[1][f] = malloc((nst[f] ? nst[f] : 1) * sizeof(double));
+    if ((!st[f] && nst[f]) || !st2[0][f] || !st2[1][f]) return 1;
   }
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f) {
     dg[f] = lgame_host_diag_field(hm, f, &ndg[f]);
@@ -119,10 +119,11 @@ int main(int argc, char** argv) {
   }
   char path[1024];
   snprintf(path, sizeof path, "%s/c_driver.snap", argv[2]);
-  CHECK(lgame_host_write_snapshot(path, cfg.ny, cfg.nx, cfg.n_layers, nml.n_constituents, 7, st, st, dg));
+  CHECK(lgame_host_write_snapshot(path, cfg.ny, cfg.nx, cfg.n_layers, nml.n_constituents, nml.nsoillays, 7, st, st,
+                                  dg));
   long long step = -1;
-  CHECK(lgame_host_read_snapshot(path, cfg.ny, cfg.nx, cfg.n_layers, nml.n_constituents, &step, st2[0], st2[1],
-                                 dg2));
+  CHECK(lgame_host_read_snapshot(path, cfg.ny, cfg.nx, cfg.n_layers, nml.n_constituents, nml.nsoillays, &step, st2[0],
+                                 st2[1], dg2));
   if (step != 7) return 1;
   for (int f = 0; f < LGAME_STATE_NFIELDS; ++f)
     for (int s = 0; s < 2; ++s)
@@ -136,8 +137,8 @@ int main(int argc, char** argv) {
       return 1;
     }
   /* a snapshot of other dimensions is refused */
-  if (lgame_host_read_snapshot(path, cfg.ny + 2, cfg.nx, cfg.n_layers, nml.n_constituents, &step, st2[0], st2[1],
-                               dg2) != LGAME_ERR_BAD_DIMS)
+  if (lgame_host_read_snapshot(path, cfg.ny + 2, cfg.nx, cfg.n_layers, nml.n_constituents, nml.nsoillays, &step,
+                               st2[0], st2[1], dg2) != LGAME_ERR_BAD_DIMS)
     return 1;
 
   char name[256];

@@ -39,6 +39,8 @@ GROUP_OF = {
     "lmom_diff_v": "diff", "ltemp_diff_h": "diff", "ltemp_diff_v": "diff", "lmass_diff_h": "diff",
     "lmass_diff_v": "diff", "diff_coeff_scheme_h": "diff", "bg_shear": "diff", "c_s": "diff",
     "lperiodic": "bc", "lfreeslip": "bc", "lmoist": "constituents", "orography_id": "surface", "lsleve": "surface",
+    "lprog_soil_temp": "surface", "nsoillays": "surface", "lsfc_sensible_heat_flux": "surface",
+    "lsfc_phase_trans": "surface", "lpbl": "surface", "h_prandtl": "diff", "karman": "diff",
 }
 
 

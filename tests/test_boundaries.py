@@ -181,7 +181,7 @@ def test_golden_boundaries_and_output():
     g = np.load(here / "hills_nonperiodic_bc.npz")
     st, out, bc = mg.boundary_output_case()
     np.testing.assert_array_equal(bc, g["bc_state"])
-    for f in L.STATE_FIELDS:
+    for f in L.ATMOS_FIELDS:
         assert cases.rel_err(st[f], g[f]) <= 1e-12, f
     for f, v in out.items():
         np.testing.assert_allclose(v, g["out_" + f], rtol=1e-6, atol=0, err_msg=f)

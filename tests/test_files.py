@@ -37,16 +37,16 @@ def test_snapshot_round_trip_and_header(tmp_path):
     hm, o = _oracle_run("jet", 2)
     s0, s1, dg = o.get_state(0), o.get_state(1), o.get_diag()
     path = tmp_path / "run.snap"
-    L.write_snapshot(path, *_dims(hm), 2, s0, s1, dg)
-    step, r0, r1, rd = L.read_snapshot(path, *_dims(hm))
+    L.write_snapshot(path, *_dims(hm), 2, s0, s1, dg, ns=hm.ns)
+    step, r0, r1, rd = L.read_snapshot(path, *_dims(hm), ns=hm.ns)
     assert step == 2
     for a, b in ((s0, r0), (s1, r1), (dg, rd)):
         for f in a:
             np.testing.assert_array_equal(a[f], b[f], err_msg=f)
     raw = path.read_bytes()
-    magic, version, ny, nx, nl, nc, st = struct.unpack_from("<8s5iq", raw, 0)
-    assert (magic, version, ny, nx, nl, nc, st) == (b"LGAMESNP", 2, hm.ny, hm.nx, hm.nl, hm.ncons, 2)
-    assert raw[36:64] == bytes(28)
+    magic, version, ny, nx, nl, nc, st, ns = struct.unpack_from("<8s5iqi", raw, 0)
+    assert (magic, version, ny, nx, nl, nc, st, ns) == (b"LGAMESNP", 3, hm.ny, hm.nx, hm.nl, hm.ncons, 2, hm.ns)
+    assert raw[40:64] == bytes(24)
     n_doubles = 2 * sum(v.size for v in s0.values()) + sum(v.size for v in dg.values())
     assert len(raw) == 64 + 8 * n_doubles
     first = np.frombuffer(raw, dtype="<f8", count=4, offset=64)
@@ -59,14 +59,17 @@ def test_files_reject_wrong_kind_dims_and_length(tmp_path):
     d = _dims(hm)
     s, dg = o.get_state(0), o.get_diag()
     snap = tmp_path / "a.snap"
-    L.write_snapshot(snap, *d, 0, s, s, dg)
+    L.write_snapshot(snap, *d, 0, s, s, dg, ns=hm.ns)
     with pytest.raises(L.LgameError) as e:
-        L.read_snapshot(snap, d[0] + 1, d[1], d[2], d[3])
+        L.read_snapshot(snap, d[0] + 1, d[1], d[2], d[3], ns=hm.ns)
+    assert e.value.code == L.ERR_BAD_DIMS
+    with pytest.raises(L.LgameError) as e:      # other number of soil layers
+        L.read_snapshot(snap, *d, ns=hm.ns + 1)
     assert e.value.code == L.ERR_BAD_DIMS
     lev = tmp_path / "bc+0s.bin"
     L.write_bc_level(lev, *d, 0.0, _level(hm, 0.0))
     with pytest.raises(L.LgameError):
-        L.read_snapshot(lev, *d)              # a boundary level is not a snapshot
+        L.read_snapshot(lev, *d, ns=hm.ns)    # a boundary level is not a snapshot
     with pytest.raises(L.LgameError):
         L.read_bc_level(snap, *d)             # and the other way round
     raw = snap.read_bytes()
@@ -74,9 +77,9 @@ def test_files_reject_wrong_kind_dims_and_length(tmp_path):
     (tmp_path / "long.snap").write_bytes(raw + b"\0")
     for name in ("short.snap", "long.snap"):
         with pytest.raises(L.LgameError):
-            L.read_snapshot(tmp_path / name, *d)
+            L.read_snapshot(tmp_path / name, *d, ns=hm.ns)
     with pytest.raises(L.LgameError):
-        L.read_snapshot(tmp_path / "missing.snap", *d)
+        L.read_snapshot(tmp_path / "missing.snap", *d, ns=hm.ns)
     o.close()
 
 
@@ -101,9 +104,9 @@ def test_oracle_resume_from_snapshot_is_bit_identical(key, tmp_path):
     The non-periodic case keeps edge values of the state it overwrites, so both slots matter."""
     hm, ref = _oracle_run(key, 4)
     hm2, o = _oracle_run(key, 2)
-    L.write_snapshot(tmp_path / "s.snap", *_dims(hm2), 2, o.get_state(0), o.get_state(1), o.get_diag())
+    L.write_snapshot(tmp_path / "s.snap", *_dims(hm2), 2, o.get_state(0), o.get_state(1), o.get_diag(), ns=hm2.ns)
     o.close()
-    step, s0, s1, dg = L.read_snapshot(tmp_path / "s.snap", *_dims(hm2))
+    step, s0, s1, dg = L.read_snapshot(tmp_path / "s.snap", *_dims(hm2), ns=hm2.ns)
     r = O.Oracle(L.config_from_namelist(_namelist(key)), hm2.grid)
     r.set_state(0, s0)
     r.set_state(1, s1)
@@ -173,9 +176,9 @@ def test_gpu_resume_from_snapshot_is_bit_identical(precision, tmp_path):
     g = fresh()
     for k in range(2):
         g.pchevi(k % 2, (k + 1) % 2, k)
-    L.write_snapshot(tmp_path / "s.snap", *_dims(hm), 2, g.get_state(0), g.get_state(1), g.get_diag())
+    L.write_snapshot(tmp_path / "s.snap", *_dims(hm), 2, g.get_state(0), g.get_state(1), g.get_diag(), ns=hm.ns)
     g.close()
-    step, s0, s1, dg = L.read_snapshot(tmp_path / "s.snap", *_dims(hm))
+    step, s0, s1, dg = L.read_snapshot(tmp_path / "s.snap", *_dims(hm), ns=hm.ns)
     r = L.GpuModel(cfg, hm.grid)
     r.set_state(0, s0)
     r.set_state(1, s1)

@@ -54,7 +54,10 @@ def _cfg(**kw):
     ("ltemp_diff_h", 1, L.ERR_UNSUPPORTED),
     ("lmass_diff_h", 1, L.ERR_UNSUPPORTED),
     ("lmom_diff_v", 1, L.ERR_UNSUPPORTED),
-    ("lpbl", 1, L.ERR_UNSUPPORTED),
+    ("lpbl", 1, L.ERR_BAD_CONFIG),                    # the PBL needs lmom_diff_h
+    ("lsfc_sensible_heat_flux", 1, L.ERR_UNSUPPORTED),  # divides by a zero resistance without the soil
+    ("nsoillays", 17, L.ERR_BAD_CONFIG),
+    ("nsoillays", -1, L.ERR_BAD_CONFIG),
 ])
 def test_create_rejects_bad_config(field, value, code):
     lib = L.load_library()
@@ -63,15 +66,19 @@ def test_create_rejects_bad_config(field, value, code):
     assert rc == code and not h.value
 
 
-@pytest.mark.parametrize("kw", [
+@pytest.mark.parametrize("kw,code", [
     # non-periodic horizontal momentum diffusion needs lmom_diff_v or third-order theta
-    dict(lmom_diff_h=1, lperiodic=0, theta_adv_order=2),
+    (dict(lmom_diff_h=1, lperiodic=0, theta_adv_order=2), L.ERR_UNSUPPORTED),
+    # the prognostic soil needs at least two soil layers
+    (dict(lprog_soil_temp=1, nsoillays=1), L.ERR_BAD_CONFIG),
+    # the surface layer needs positive karman and h_prandtl
+    (dict(lmom_diff_h=1, lpbl=1, karman=0.0), L.ERR_BAD_CONFIG),
 ])
-def test_create_rejects_unsupported_diffusion(kw):
+def test_create_rejects_unsupported_combinations(kw, code):
     lib = L.load_library()
     h = C.c_void_p()
     rc = lib.lgame_gpu_create(C.byref(_cfg(**kw)), C.byref(h))
-    assert rc == L.ERR_UNSUPPORTED and not h.value
+    assert rc == code and not h.value
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device path")

@@ -106,7 +106,7 @@ def test_golden_vectors(key):
     path = GOLDEN / f"{key}.npz"
     g = np.load(path)
     hm, o, b0, b1, st = _run(key, int(g["nsteps"]))
-    for f in L.STATE_FIELDS:
+    for f in L.ATMOS_FIELDS:
         ref = g[f]
         e = cases.rel_err(st[f], ref)
         assert e <= 1e-12, (key, f, e)
