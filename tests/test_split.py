@@ -39,8 +39,9 @@ FLOOR = {"wind_u": 1.0, "wind_v": 1.0, "wind_w": 1.0, "theta_v_pert": 1.0, "exne
 
 
 def field_errors(a, b):
+    """max|a-b| over max|b| (or the field's floor) of each atmospheric state field."""
     out = {}
-    for f in L.STATE_FIELDS:
+    for f in L.ATMOS_FIELDS:
         d = float(np.abs(a[f] - b[f]).max())
         out[f] = d / max(float(np.abs(b[f]).max()), FLOOR.get(f, 0.0))
     return out

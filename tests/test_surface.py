@@ -371,7 +371,7 @@ def test_split_surface_close_to_fp64(name):
     da, db = gs[1].get_diag(), gs[0].get_diag()
     for g in gs:
         g.close()
-    errs = field_errors({f: a[f] for f in L.ATMOS_FIELDS}, {f: b[f] for f in L.ATMOS_FIELDS})
+    errs = field_errors(a, b)
     assert max(errs.values()) <= 3e-5, errs
     assert cases.rel_err(a["temperature_soil"] - 280.0, b["temperature_soil"] - 280.0) <= 1e-3
     for f in ("roughness_velocity", "monin_obukhov_length", "scalar_flux_resistance", "power_flux_density_sens_sea"):
