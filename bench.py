@@ -566,6 +566,7 @@ def run_ours(args):
         line["boundary_relaxation"] = boundary_bench(args, peaks)
     if rank == 0 and ws == 1 and not args.no_diffusion:
         line["diffusion"] = diffusion_bench(args, results)
+        line["default_physics"] = diffusion_bench(args, results, surface=True)
     if rank == 0 and ws == 1 and not args.no_emulator:
         line["emulator"] = emulator_bench(peaks)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -578,19 +579,23 @@ def run_ours(args):
 
 DIFF_DEFAULT = dict(lmom_diff_h=True, lmom_diff_v=True, ltemp_diff_h=True, ltemp_diff_v=True, lmass_diff_h=True,
                     lmass_diff_v=True, diff_coeff_scheme_h="smag")
+SFC_DEFAULT = dict(lprog_soil_temp=True, nsoillays=5, lsfc_sensible_heat_flux=True, lsfc_phase_trans=True, lpbl=True)
 
 
-def diffusion_bench(args, results: dict) -> dict:
+def diffusion_bench(args, results: dict, surface: bool = False) -> dict:
     """The workload with the reference's default &diff (mo_diff_nml.F90:38-53: momentum,
     temperature and mass diffusion on, horizontally and vertically, Smagorinsky horizontal
-    coefficient, TKE vertical one): the split and the FP64 step (CUDA events on the library's
-    stream), their cost against the same steps without diffusion, and the closure's kernels'
-    share of the split step."""
+    coefficient, TKE vertical one) and, with `surface`, its default &surface as well
+    (mo_surface_nml.F90:30-37: prognostic soil of five layers, sensible heat flux, surface
+    phase-transition switch, PBL): the split and the FP64 step (CUDA events on the library's
+    stream), their cost against the same steps without these, and the closure's (and surface
+    kernels') share of the split step."""
     import cases
     import lgame_gpu as L
-    n = cases.namelist(WORKLOAD, **DIFF_DEFAULT, **size_overrides(args))
+    n = cases.namelist(WORKLOAD, **DIFF_DEFAULT, **(SFC_DEFAULT if surface else {}), **size_overrides(args))
     hm = L.HostModel(n)
-    out = {"config": "reference default &diff: all six switches on, smag/tke"}
+    out = {"config": "reference default &diff: all six switches on, smag/tke" +
+           ("; reference default &surface: soil (5 layers), sensible heat flux, PBL" if surface else "")}
     runs = [(L.PRECISION_SPLIT, "split", args.steps), (L.PRECISION_FP64, "fp64", min(args.steps, 3))]
     if args.split_only or args.fp64_only:
         runs = [r for r in runs if (r[1] == "split") == args.split_only]
@@ -617,7 +622,7 @@ def diffusion_bench(args, results: dict) -> dict:
             g.set_profiling(False)
             tot = sum(v["ms"] for v in rep.values())
             e["closure_kernel_shares"] = {k: round(v["ms"] / tot, 4) for k, v in rep.items()
-                                          if k.startswith(("ks_diff", "ks_mom_diff", "ks_diss"))}
+                                          if k.startswith(("ks_diff", "ks_mom_diff", "ks_diss", "ks_sfc", "ks_pbl"))}
         st = g.get_state((3 + steps) % 2)
         e["finite"] = all(bool(np.isfinite(v).all()) for v in st.values())
         g.close()
