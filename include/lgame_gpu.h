@@ -96,6 +96,14 @@ typedef struct lgame_config {
    * sensible heat flux is on), the height of the Prandtl layer (m) and von Karman's constant */
   int    nsoillays;
   double h_prandtl, karman;
+  /* extension (appended): the phase transitions of the water constituents
+   * (calc_h2otracers_source_rates, mo_phase_trans.F90:22-330), which the reference compiles but
+   * never calls, so its rates stay zero there.  1: formed at the first substep of every step
+   * from state_old and its temperature, read by both substeps' scalar tendencies as the
+   * reference's scalar_tend_expl reads them (mo_scalar_tend_expl.F90:127, 163, 170), with the
+   * surface evaporation of lsfc_phase_trans and the latent heat flux over lakes into the soil.
+   * Needs lmoist. */
+  int    lphase_trans;
 } lgame_config;
 
 #define LGAME_MAX_SOIL_LAYERS 16
@@ -218,6 +226,11 @@ enum lgame_diag_field {
   LGAME_DIAG_SST,                     /* (ny,nx)  K, sea surface temperature (host)       */
   LGAME_DIAG_SFC_SW_IN,               /* (ny,nx)  W m^-2, shortwave into the surface (host) */
   LGAME_DIAG_SFC_LW_OUT,              /* (ny,nx)  W m^-2, longwave out of the surface (host) */
+  /* the phase transitions (lphase_trans; zero otherwise, as in the reference's step) */
+  LGAME_DIAG_PHASE_TRANS_RATES,       /* (ny,nx,nl,n_condensed_constituents+1) kg m^-3 s^-1 */
+  LGAME_DIAG_PHASE_TRANS_HEATING_RATE,/* (ny,nx,nl)  W m^-3                                 */
+  LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE, /* (ny,nx) W m^-2, latent heat into lakes       */
+  LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA,  /* (ny,nx) W m^-2, latent heat into the sea     */
   LGAME_DIAG_NFIELDS
 };
 

@@ -72,6 +72,7 @@ typedef struct lgame_namelist {
   double jet_speed, jet_pressure;  /* scenario "baroclinic_jet" */
   double t_pert_sigma, rh_mean;
   int    check_finite;
+  int    lphase_trans;       /* 1: the phase transitions the reference never calls (lgame_config) */
   /* derived (mo_run_nml.F90:89-101, mo_constituents_nml.F90:246-253, mo_io_nml.F90:266) */
   int    n_levels, n_flat_layers, n_condensed_constituents, n_constituents;
   double eff_hor_res, dtime, dt_write, t_init;

@@ -77,7 +77,9 @@ size_t diag_n(int f, int ny, int nx, int nl, int ncons) {
     case LGAME_DIAG_ROUGHNESS_LENGTH: case LGAME_DIAG_ROUGHNESS_VELOCITY: case LGAME_DIAG_MONIN_OBUKHOV_LENGTH:
     case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL:
     case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: case LGAME_DIAG_SST: case LGAME_DIAG_SFC_SW_IN:
-    case LGAME_DIAG_SFC_LW_OUT: return (size_t)ny * nx;
+    case LGAME_DIAG_SFC_LW_OUT: case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE:
+    case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA: return (size_t)ny * nx;
+    case LGAME_DIAG_PHASE_TRANS_RATES: return s * (ncons == 7 ? 6 : 1);
     default: return s;
   }
 }

@@ -105,6 +105,7 @@ std::vector<Item> items_of(lgame_namelist* n) {
   R("gpu", "jet_speed", &n->jet_speed); R("gpu", "jet_pressure", &n->jet_pressure);
   R("gpu", "t_pert_sigma", &n->t_pert_sigma); R("gpu", "rh_mean", &n->rh_mean);
   L("gpu", "check_finite", &n->check_finite);
+  L("gpu", "lphase_trans", &n->lphase_trans);
   return v;
 }
 
@@ -376,5 +377,6 @@ extern "C" int lgame_config_from_namelist(const lgame_namelist* n, lgame_config*
   c->diff_coeff_scheme_h = (trim(n->diff_coeff_scheme_h) == "tke") ? LGAME_DIFF_COEFF_TKE : LGAME_DIFF_COEFF_SMAG;
   c->bg_shear = n->bg_shear; c->c_s = n->c_s;
   c->nsoillays = n->nsoillays; c->h_prandtl = n->h_prandtl; c->karman = n->karman;
+  c->lphase_trans = n->lphase_trans;
   return LGAME_OK;
 }

@@ -646,7 +646,8 @@ __global__ void k_tend_wind(Dims D, State So, State Sn, Tend<T> Tn, Carried<T> C
 // (mo_divergence_operators.F90:70-147) evaluated inline.
 template <class T, class V = double>
 __device__ __forceinline__ void tracers_body(const Dims& D, const Grid<T>& G, const StateT<V>& Ss, const V* u_new,
-                                             const V* v_new, T* t_rho, int rk_step, const T* mdt) {
+                                             const V* v_new, T* t_rho, int rk_step, const T* mdt,
+                                             const T* ptr) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -683,22 +684,24 @@ __device__ __forceinline__ void tracers_body(const Dims& D, const Grid<T>& G, co
     const T div = (comp_h + comp_v) / G.volume[q];
     T* t = t_rho + (long long)(jc - 1) * D.fstride;
     T f = -div;
-    if (mdt) f = f + mdt[q + (long long)(jc - 1) * D.fstride];  // mass diffusion (phase transitions: 0)
+    if (mdt) f = f + mdt[q + (long long)(jc - 1) * D.fstride];  // mass diffusion
+    // phase transitions (null: off, the reference's zero); vapour takes rate nc+1
+    if (ptr) f = f + ptr[q + (long long)((jc < D.g ? jc : D.g) - 1) * D.fstride];
     t[q] = old_weight * t[q] + new_weight * f;
   }
 }
 
 template <class T, class V = double>
 __global__ void k_tracers(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, T* t_rho, int rk_step,
-                          const T* mdt) {
-  tracers_body<T, V>(D, G, Ss, u_new, v_new, t_rho, rk_step, mdt);
+                          const T* mdt, const T* ptr) {
+  tracers_body<T, V>(D, G, Ss, u_new, v_new, t_rho, rk_step, mdt, ptr);
 }
 
 // scalar_tend_expl for the gas and the rho*theta_v tendency, mo_scalar_tend_expl.F90:106-177
 template <class T, class V = double>
 __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, const V* v_new, const T* tvu,
                             const T* tvv, const T* Tm, const T* hd, const T* rad, const T* csh, T* t_rho,
-                            T* t_rt, const T* mdt, const T* tdh) {
+                            T* t_rt, const T* mdt, const T* tdh, const T* ptr, const T* pth) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -706,9 +709,13 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
   auto fx = [&](int i, int j, int k) { T f; return stv_h_x<T>(D, rg, u_new, i, j, k, &f) ? f : T(0); };
   auto fy = [&](int i, int j, int k) { T f; return stv_h_y<T>(D, rg, v_new, i, j, k, &f) ? f : T(0); };
   const T div_m = div_h_at<T>(D, G, fx, fy, ji, jk, jl);
-  // old_weight 0, new_weight 1 for the gas; mass diffusion (null: off)
+  // old_weight 0, new_weight 1 for the gas; mass diffusion and the phase transitions' vapour
+  // rate (null: off)
   const T mdg = mdt ? mdt[q + (long long)(D.g - 1) * D.fstride] : T(0);
-  t_rho[q + (long long)(D.g - 1) * D.fstride] = mdt ? -div_m + mdg : -div_m;
+  const T ptg = ptr ? ptr[q + (long long)(D.g - 1) * D.fstride] : T(0);
+  T tg = mdt ? -div_m + mdg : -div_m;
+  if (ptr) tg = tg + ptg;
+  t_rho[q + (long long)(D.g - 1) * D.fstride] = tg;
   T div_t;
   if (D.theta_order == 2) {
     auto th = [&](int i, int j, int k) { const long long p = IX(D, i, j, k); return G.theta_v_bg[p] + T(Ss.tp[p]); };
@@ -720,9 +727,11 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
     auto gy = [&](int i, int j, int k) { return tvv[IX(D, i, j, k)] * fy(i, j, k); };
     div_t = div_h_at<T>(D, G, gx, gy, ji, jk, jl);
   }
-  // dissipative heating, radiation, sediment heating and temperature diffusion (phase
-  // transitions are zero), in the reference's order
-  T heat = hd[q] + rad[q] + csh[q];
+  // dissipative heating, radiation, phase transitions (null: off), sediment heating and
+  // temperature diffusion, in the reference's order
+  T heat = hd[q] + rad[q];
+  if (pth) heat = heat + pth[q];
+  heat = heat + csh[q];
   if (tdh) heat = heat + tdh[q];
   T x = T(0);
   if (heat != T(0)) {
@@ -731,7 +740,8 @@ __global__ void k_gas_theta(Dims D, Grid<T> G, StateT<V> Ss, const V* u_new, con
   }
   T r = -div_t + x;
   // (phase transition rate + mass diffusion of the gas) * theta_v
-  if (mdt) r = r + mdg * (G.theta_v_bg[q] + T(Ss.tp[q]));
+  if (ptr) r = r + (ptg + mdg) * (G.theta_v_bg[q] + T(Ss.tp[q]));
+  else if (mdt) r = r + mdg * (G.theta_v_bg[q] + T(Ss.tp[q]));
   t_rt[q] = r;
 }
 

@@ -6,6 +6,7 @@
 #include "emulator.cuh"
 #include "diffusion.cuh"
 #include "kernels.cuh"
+#include "phase.cuh"
 #include "split.cuh"
 #include "surface.cuh"
 
@@ -80,6 +81,9 @@ struct lgame_gpu {
   SfcPar spar{};
   double* sfc_grid[6] = {};  // land, lake, roughness length, rho_c, conductivity, constant temperature
   double* tsoil[2] = {};
+  // the phase transitions (lphase_trans extension): rates (nc+1 fields) and heating rate
+  bool phase = false;
+  double *ptr = nullptr, *pth = nullptr;
   // scratch
   double *theta, *gz, *gx, *gy, *divf, *tvu, *tvv, *tpu, *tpv, *ex, *ey, *ez, *uph, *vph, *wph, *vsq;
   double* staging = nullptr;
@@ -199,7 +203,7 @@ Ext diag_ext(const Dims& d, int f) {
     case LGAME_DIAG_ROUGHNESS_LENGTH: case LGAME_DIAG_ROUGHNESS_VELOCITY: case LGAME_DIAG_MONIN_OBUKHOV_LENGTH:
     case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL:
     case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: case LGAME_DIAG_SST: case LGAME_DIAG_SFC_SW_IN:
-    case LGAME_DIAG_SFC_LW_OUT:
+    case LGAME_DIAG_SFC_LW_OUT: case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE: case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA:
       return {(size_t)d.ny, (size_t)d.nx, 1};
     default: return ext_s(d);
   }
@@ -524,6 +528,7 @@ const auto k_diff_divs7 = lg::k_diff_divs<double, 7>;
 const auto k_sfc_turb = lg::k_sfc_turb;
 const auto k_pbl = lg::k_pbl<double>;
 const auto k_sfc_column = lg::k_sfc_column<double>;
+const auto k_phase_trans = lg::k_phase_trans<double, double>;
 }  // namespace kd
 
 dim3 blk() { return dim3(32, 8, 1); }
@@ -672,7 +677,14 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
     }
     const double* mdt = c->diff_mass_h ? c->dbuf.mdt : nullptr;
     const double* tdh = c->diff_temp_h ? c->dbuf.tdh : nullptr;
-    if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk, mdt);
+    // the phase transitions (extension; the reference never calls them) at the first substep,
+    // from state_old and the temperature diagnosed from it; both substeps read the rates
+    if (rk == 1 && c->phase)
+      LAUNCH(kd::k_phase_trans, grd(D, D.ny, D.nx, D.nl), D, G, So, (const double*)c->temperature, c->sbuf,
+             (const double*)c->tsoil[so], c->cfg.lsfc_phase_trans, D.dtime, c->ptr, c->pth);
+    const double* ptr = c->phase ? c->ptr : nullptr;
+    const double* pth = c->phase ? c->pth : nullptr;
+    if (D.ncons > 1) LAUNCH(kd::k_tracers, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, T.rho, rk, mdt, ptr);
     // theta_v_adv_3rd_order of the state used here: in the first substep that is state_old,
     // whose edges manage_p_grad's call above already left in tvu/tvv (nothing in between
     // writes state_old or tvu/tvv), so only the second substep recomputes them -- the same
@@ -682,7 +694,7 @@ int step_fp64(lgame_gpu* c, int so, int sn, int step) {
       if (rc != LGAME_OK) return rc;
     }
     LAUNCH(kd::k_gas_theta, grd(D, D.ny, D.nx, D.nl), D, G, Ss, Sn.u, Sn.v, c->tvu, c->tvv, c->temperature, c->hdiss,
-           c->rad, c->csh, T.rho, T.rt, mdt, tdh);
+           c->rad, c->csh, T.rho, T.rt, mdt, tdh, ptr, pth);
     // three_band_solver_ver (+ w_free_slip), three_band_solver_gen_densities
     {
       // the sensible heat flux and the soil rows of three_band_solver_ver (mo_column_solvers.F90:
@@ -710,7 +722,8 @@ int split_sync_carried(lgame_gpu* c, bool to_split) {
                         {c->tend.rt, F.tend.rt, n}, {c->tend.u, F.tend.u, n}, {c->tend.v, F.tend.v, n},
                         {c->tend.w, F.tend.w, n}, {c->hdiss, F.hdiss, n},
                         {c->dbuf.tke, F.tke, n}, {c->dbuf.visc, F.visc, n}, {c->dbuf.mdtx, F.mdtx, n},
-                        {c->dbuf.mdty, F.mdty, n}, {c->dbuf.mdtz, F.mdtz, n}};
+                        {c->dbuf.mdty, F.mdty, n}, {c->dbuf.mdtz, F.mdtz, n},
+                        {c->ptr, F.ptr, n * (c->D.nc + 1)}, {c->pth, F.pth, n}};
   for (const Pair& p : pairs) {
     if (!p.f) continue;  // diffusion off: no FP32 copy
     const int rc = to_split ? split_convert(p.d, p.f, p.n, c->stream) : split_convert_back(p.f, p.d, p.n, c->stream);
@@ -801,6 +814,13 @@ int check_cfg(const lgame_config* cfg) {
     return set_err(LGAME_ERR_BAD_CONFIG, "nsoillays out of range");
   if ((cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl) && !(cfg->karman > 0.0 && cfg->h_prandtl > 0.0))
     return set_err(LGAME_ERR_BAD_CONFIG, "karman and h_prandtl must be positive with the surface layer on");
+  // the phase transitions (extension) act on the water constituents; their surface evaporation
+  // divides by the scalar flux resistance, which only the prognostic soil forms
+  if (cfg->lphase_trans && !cfg->lmoist)
+    return set_err(LGAME_ERR_BAD_CONFIG, "lphase_trans needs lmoist");
+  if (cfg->lphase_trans && cfg->lsfc_phase_trans && !cfg->lprog_soil_temp)
+    return set_err(LGAME_ERR_UNSUPPORTED, "the surface phase transitions without lprog_soil_temp divide by a zero scalar "
+                                          "flux resistance");
   return LGAME_OK;
 }
 
@@ -860,7 +880,8 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     c->sfc_turb = cfg->lsfc_sensible_heat_flux || cfg->lsfc_phase_trans || cfg->lpbl;
     for (double*& p : c->sfc_grid) if ((rc = dalloc(c, &p, (size_t)D.plane)) != LGAME_OK) return fail(rc);
     SfcBuf& B = c->sbuf;
-    double** diag[] = {&B.rl, &B.rv, &B.mol, &B.sfr, &B.sens_soil, &B.sens_sea, &B.sst, &B.sw_in, &B.lw_out};
+    double** diag[] = {&B.rl, &B.rv, &B.mol, &B.sfr, &B.sens_soil, &B.sens_sea, &B.sst, &B.sw_in, &B.lw_out,
+                       &B.lat_lake, &B.lat_sea};
     for (double** p : diag) if ((rc = dalloc(c, p, (size_t)D.plane)) != LGAME_OK) return fail(rc);
     B.land = c->sfc_grid[0]; B.lake = c->sfc_grid[1]; B.rl_grid = c->sfc_grid[2];
     B.rhoc = c->sfc_grid[3]; B.tcond = c->sfc_grid[4]; B.tconst = c->sfc_grid[5];
@@ -870,6 +891,8 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     SfcPar& P = c->spar;
     P.h_prandtl = cfg->h_prandtl; P.karman = cfg->karman; P.dtime = cfg->dtime; P.z_t_const = 0.0;
     P.ns = ns; P.prog_soil = cfg->lprog_soil_temp; P.sens = cfg->lsfc_sensible_heat_flux;
+    c->phase = cfg->lphase_trans;
+    if (c->phase && ((rc = dalloc(c, &c->ptr, F * (size_t)(D.nc + 1))) || (rc = dalloc(c, &c->pth, F)))) return fail(rc);
   }
   for (int k = 0; k < 6; ++k) if ((rc = dalloc(c, &c->ipw[k], F)) != LGAME_OK) return fail(rc);
   for (int k = 0; k < 3; ++k) if ((rc = dalloc(c, &c->trsk_u[k], (size_t)D.P)) != LGAME_OK) return fail(rc);
@@ -953,6 +976,7 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     sd.mass_h = c->diff_mass_h; sd.mass_v = c->diff_mass_v; sd.par = c->dpar;
     SplitSfc sf;
     sf.turb = c->sfc_turb; sf.pbl = c->sfc_pbl; sf.sens = c->sfc_sens; sf.soil = c->sfc_soil;
+    sf.phase = c->phase; sf.phase_sfc = c->phase && cfg->lsfc_phase_trans;
     sf.buf = c->sbuf; sf.par = c->spar; sf.vsq = c->vsq; sf.tsoil[0] = c->tsoil[0]; sf.tsoil[1] = c->tsoil[1];
     if ((rc = split_create(c->D, cfg->precision == LGAME_PRECISION_SPLIT_FP64_COLUMN, sd, sf, &c->split, &c->bytes)) !=
         LGAME_OK)
@@ -1111,6 +1135,12 @@ extern "C" int lgame_gpu_get_state(lgame_gpu* c, int slot, double* const* f, int
 }
 
 namespace {
+// fields of one diagnostic: the constituents of the rho tendency, nc+1 phase transition rates
+int diag_nrep(const Dims& D, int f) {
+  if (f == LGAME_DIAG_TEND_RHO) return D.ncons;
+  if (f == LGAME_DIAG_PHASE_TRANS_RATES) return D.nc + 1;
+  return 1;
+}
 double* diag_dev(lgame_gpu* c, int f) {
   switch (f) {
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_U: return c->pg_nl_u;
@@ -1151,6 +1181,10 @@ double* diag_dev(lgame_gpu* c, int f) {
     case LGAME_DIAG_SST: return c->sbuf.sst;
     case LGAME_DIAG_SFC_SW_IN: return c->sbuf.sw_in;
     case LGAME_DIAG_SFC_LW_OUT: return c->sbuf.lw_out;
+    case LGAME_DIAG_PHASE_TRANS_RATES: return c->ptr;
+    case LGAME_DIAG_PHASE_TRANS_HEATING_RATE: return c->pth;
+    case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE: return c->sbuf.lat_lake;
+    case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA: return c->sbuf.lat_sea;
   }
   return nullptr;
 }
@@ -1160,9 +1194,9 @@ extern "C" int lgame_gpu_set_diag(lgame_gpu* c, const double* const* f, int nfie
   if (!c || !f || nfields != LGAME_DIAG_NFIELDS) return set_err(LGAME_ERR_INVALID_ARG, "lgame_gpu_set_diag: bad arguments");
   const Dims& D = c->D;
   for (int i = 0; i < nfields; ++i) {
-    if (!f[i]) continue;
+    if (!f[i] || !diag_dev(c, i)) continue;  // not given, or not formed in this run (phase transitions off)
     const Ext e = diag_ext(D, i);
-    const int nrep = (i == LGAME_DIAG_TEND_RHO) ? D.ncons : 1;
+    const int nrep = diag_nrep(D, i);
     for (int r = 0; r < nrep; ++r) {
       int rc = copy_h2d(c, diag_dev(c, i) + (size_t)r * D.fstride, f[i] + r * e.n1 * e.n2 * e.n3, e);
       if (rc != LGAME_OK) return rc;
@@ -1186,7 +1220,11 @@ extern "C" int lgame_gpu_get_diag(lgame_gpu* c, double* const* f, int nfields) {
   for (int i = 0; i < nfields; ++i) {
     if (!f[i]) continue;
     const Ext e = diag_ext(D, i);
-    const int nrep = (i == LGAME_DIAG_TEND_RHO) ? D.ncons : 1;
+    const int nrep = diag_nrep(D, i);
+    if (!diag_dev(c, i)) {  // not formed in this run: the reference's zero
+      std::memset(f[i], 0, sizeof(double) * e.n1 * e.n2 * e.n3 * (size_t)nrep);
+      continue;
+    }
     for (int r = 0; r < nrep; ++r) {
       int rc = copy_d2h(c, f[i] + r * e.n1 * e.n2 * e.n3, diag_dev(c, i) + (size_t)r * D.fstride, e);
       if (rc != LGAME_OK) return rc;

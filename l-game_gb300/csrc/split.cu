@@ -497,7 +497,8 @@ __global__ void __launch_bounds__(128) ks_div_h(Dims D, Grid<float> GF, GridX X,
 __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* fu,
                                                   const float* fv, const float* gu, const float* gv, const float* Tm,
                                                   const float* hd, const float* rad, const float* csh, float* t_rho,
-                                                  float* t_rt, const float* mdt, const float* tdh) {
+                                                  float* t_rt, const float* mdt, const float* tdh,
+                                                  const float* ptr, const float* pth) {
   const int ji = blockIdx.x * blockDim.x + threadIdx.x + 1;
   const int jk = blockIdx.y * blockDim.y + threadIdx.y + 1;
   if (ji > D.ny || jk > D.nx) return;
@@ -517,7 +518,9 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
       mn = layer_faces(D, GF, fx, fy, ji, jk, jl + 1);
       tn = layer_faces(D, GF, gx, gy, ji, jk, jl + 1);
     }
-    float heat = hd[q] + rad[q] + csh[q];  // dissipative, radiative, sediment heating
+    float heat = hd[q] + rad[q];           // dissipative, radiative heating
+    if (pth) heat = heat + pth[q];         // phase transitions
+    heat = heat + csh[q];                  // sediment heating
     if (tdh) heat = heat + tdh[q];         // temperature diffusion
     const float div_m = div_col(D, GF, X, mc, vert_faces(D, mh_prev, mc.h, mn.h, jl), ji, jk, jl);
     const float div_t = div_col(D, GF, X, tc, vert_faces(D, th_prev, tc.h, tn.h, jl), ji, jk, jl);
@@ -526,7 +529,11 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
       const float cv = c_v_mass_weighted_air<float>(D, Ss.rho, Tm, q);
       x = float(kC_D_V) * Ss.rho[q + goff] / cv * heat / (float(kC_D_P) * (GF.exner_bg[q] + Ss.ep[q]));
     }
-    if (mdt) {  // mass diffusion of the gas, in its tendency and times theta_v in rho*theta_v's
+    if (ptr) {  // phase transitions' vapour rate and mass diffusion of the gas
+      const float mdg = mdt ? mdt[q + goff] : 0.f, ptg = ptr[q + goff];
+      t_rho[q + goff] = -div_m + mdg + ptg;
+      t_rt[q] = -div_t + x + (ptg + mdg) * (GF.theta_v_bg[q] + Ss.tp[q]);
+    } else if (mdt) {  // mass diffusion of the gas, in its tendency and times theta_v in rho*theta_v's
       const float mdg = mdt[q + goff];
       t_rho[q + goff] = -div_m + mdg;
       t_rt[q] = -div_t + x + mdg * (GF.theta_v_bg[q] + Ss.tp[q]);
@@ -552,7 +559,7 @@ __global__ void __launch_bounds__(128) ks_gas_div(Dims D, Grid<float> GF, GridX 
 constexpr int kTracers = 6;  // moist: five condensates and water vapour (the gas has its own kernel)
 __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, GridX X, StateF Ss, const float* u_new,
                                                      const float* v_new, float* t_rho, int rk_step,
-                                                     const float* mdt) {
+                                                     const float* mdt, const float* ptr) {
   LG_IDX3;
   if (ji > D.ny || jk > D.nx) return;
   const long long q = IX(D, ji, jk, jl);
@@ -613,6 +620,13 @@ __global__ void __launch_bounds__(256, 5) ks_tracers(Dims D, Grid<float> GF, Gri
     for (int t = 0; t < kTracers; ++t) {
       const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
       dv[t] = dv[t] - mdt[q + (long long)(jc - 1) * D.fstride];
+    }
+  }
+  if (ptr) {  // phase transitions: the condensates' own rates, vapour's rate nc+1
+#pragma unroll
+    for (int t = 0; t < kTracers; ++t) {
+      const int jc = t + 1 + (t + 1 >= D.g ? 1 : 0);
+      dv[t] = dv[t] - ptr[q + (long long)((jc < D.g ? jc : D.g) - 1) * D.fstride];
     }
   }
   if (rk_step == 1) {
@@ -1343,6 +1357,9 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const S
       return fail(rc);
     B.tke = C.tke; B.visc = C.visc; B.mdtx = C.mdtx; B.mdty = C.mdty; B.mdtz = C.mdtz; B.hd = C.hdiss;
   }
+  if (sfc.phase) {  // the phase transitions' rates (graupel's is never written: stays zero) and heating
+    if ((rc = salloc(s, &C.ptr, F * (size_t)(D.nc + 1), bytes)) || (rc = salloc(s, &C.pth, F, bytes))) return fail(rc);
+  }
   *out = s;
   return LGAME_OK;
 }
@@ -1676,8 +1693,15 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     }
     const float* mdt = (SD.mom_h && SD.mass_h) ? DB.mdt : nullptr;
     const float* tdh = (SD.mom_h && SD.temp_h) ? DB.tdh : nullptr;
+    // the phase transitions (extension) at the first substep, from state_old and its temperature,
+    // in FP64 on the FP64 state; both substeps read the rates
+    if (rk == 1 && SF.phase)
+      SL("ks_phase_trans", (k_phase_trans<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, G, So, (const float*)C.temperature,
+         SF.buf, SF.tsoil[so], SF.phase_sfc ? 1 : 0, D.dtime, C.ptr, C.pth);
+    const float* ptr = SF.phase ? C.ptr : nullptr;
+    const float* pth = SF.phase ? C.pth : nullptr;
     if (D.ncons > 1)
-      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk, mdt);
+      SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk, mdt, ptr);
     // third-order theta edges of the state used here; in the first substep that is the old
     // state, whose edges the pressure gradient's call above already left in tvu/tvv (nothing
     // in between writes the old mirror or tvu/tvv), so only the second substep recomputes them
@@ -1688,7 +1712,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
        s->fv, s->gu, s->gv);
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
-       C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh);
+       C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh, ptr, pth);
     if (SF.sens || SF.soil)
       SL("ks_sfc_column", k_sfc_column<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, rk == 1 ? So : Sn, T.rt, SF.buf,
          SF.par, SF.tsoil[so], SF.tsoil[rk == 1 ? so : sn], SF.tsoil[sn]);

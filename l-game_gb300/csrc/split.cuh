@@ -19,6 +19,7 @@
 
 #include "diffusion.cuh"
 #include "kernels.cuh"
+#include "phase.cuh"
 #include "surface.cuh"
 
 namespace lg {
@@ -32,6 +33,8 @@ struct SplitCarriedF {
   // the carried diagnostics of the diffusion closure (null when horizontal momentum diffusion
   // is off): TKE, viscosity, momentum diffusion accelerations
   float *tke, *visc, *mdtx, *mdty, *mdtz;
+  // the phase transitions' rates (nc+1 fields) and heating rate (null when lphase_trans is off)
+  float *ptr, *pth;
   Tend<float> tend;
   // with a background state: the net pressure-gradient terms nl + l of u, v, w and the previous
   // substep's values -(nl + l) of u, v, rounded to FP32 (the only form the wind update uses)
@@ -48,6 +51,7 @@ struct SplitDiff {
 // share with the FP64 step (surface planes, soil temperature of the two slots, v_squared)
 struct SplitSfc {
   bool turb = false, pbl = false, sens = false, soil = false;
+  bool phase = false, phase_sfc = false;  // lphase_trans, and its surface part (lsfc_phase_trans)
   SfcBuf buf{};
   SfcPar par{};
   double* vsq = nullptr;

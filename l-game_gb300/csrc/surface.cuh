@@ -41,6 +41,7 @@ struct SfcPar {
 struct SfcBuf {
   const double *land, *lake, *rl_grid, *rhoc, *tcond, *tconst;
   double *rl, *rv, *mol, *sfr, *sens_soil, *sens_sea, *sst, *sw_in, *lw_out;
+  double *lat_lake, *lat_sea;  // latent heat flux densities (formed by the phase transitions)
 };
 
 // roughness_length_from_u10_sea, mo_pbl.F90:253-282
@@ -214,9 +215,9 @@ __global__ void k_sfc_column(Dims D, Grid<double> G, State So, State Snu, T* __r
   for (int jl = 1; jl <= ns - 1; ++jl)
     h[jl] = -(rc * tc * (ts_o[c + (jl - 1) * pl] - ts_o[c + jl * pl]) / (zc[jl] - zc[jl + 1]));
   h[ns] = -(rc * tc * (ts_o[c + (ns - 1) * pl] - B.tconst[c]) / (2.0 * (zc[ns] - P.z_t_const)));
-  // the latent heat flux over lakes is formed only by the phase transitions, which the step
-  // never calls: 0
-  const double lat_lake = 0.0;
+  // the latent heat flux over lakes is formed only by the phase transitions, which the
+  // reference's step never calls (its initial zero then; with lphase_trans, their value)
+  const double lat_lake = B.lat_lake[c];
   rv[1] = ts_o[c] + (B.sens_soil[c] + lat_lake + B.sw_in[c] - B.lw_out[c] + 0.5 * h[1]) / ((zi[1] - zi[2]) * rc) * dt;
 #pragma unroll 1
   for (int jl = 2; jl <= ns; ++jl)

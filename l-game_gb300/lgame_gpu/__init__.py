@@ -141,7 +141,8 @@ DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_
                "tke", "viscosity", "heating_diss", "mom_diff_tend_x", "mom_diff_tend_y", "mom_diff_tend_z",
                "v_squared", "roughness_length_diag", "roughness_velocity", "monin_obukhov_length",
                "scalar_flux_resistance", "power_flux_density_sens_soil", "power_flux_density_sens_sea", "sst",
-               "sfc_sw_in", "sfc_lw_out"]
+               "sfc_sw_in", "sfc_lw_out", "phase_trans_rates", "phase_trans_heating_rate",
+               "power_flux_density_lat_lake", "power_flux_density_lat_sea"]
 
 
 class Config(C.Structure):
@@ -157,7 +158,8 @@ class Config(C.Structure):
                 ("lsfc_phase_trans", C.c_int), ("lpbl", C.c_int), ("lperiodic", C.c_int),
                 ("lfreeslip", C.c_int), ("precision", C.c_int), ("check_finite", C.c_int),
                 ("device", C.c_int), ("diff_coeff_scheme_h", C.c_int), ("bg_shear", C.c_double),
-                ("c_s", C.c_double), ("nsoillays", C.c_int), ("h_prandtl", C.c_double), ("karman", C.c_double)]
+                ("c_s", C.c_double), ("nsoillays", C.c_int), ("h_prandtl", C.c_double), ("karman", C.c_double),
+                ("lphase_trans", C.c_int)]
 
 
 def _s(n):
@@ -192,7 +194,7 @@ class Namelist(C.Structure):
         ("seed", C.c_longlong), ("n_hills", C.c_int), ("hill_height_min", C.c_double),
         ("hill_height_max", C.c_double), ("hill_width_min", C.c_double), ("hill_width_max", C.c_double),
         ("jet_speed", C.c_double), ("jet_pressure", C.c_double), ("t_pert_sigma", C.c_double),
-        ("rh_mean", C.c_double), ("check_finite", C.c_int),
+        ("rh_mean", C.c_double), ("check_finite", C.c_int), ("lphase_trans", C.c_int),
         ("n_levels", C.c_int), ("n_flat_layers", C.c_int), ("n_condensed_constituents", C.c_int),
         ("n_constituents", C.c_int), ("eff_hor_res", C.c_double), ("dtime", C.c_double), ("dt_write", C.c_double),
         ("t_init", C.c_double)]
@@ -332,6 +334,8 @@ def field_shapes(ny: int, nx: int, nl: int, ncons: int, ns: int = 0) -> dict[str
         "v_squared": s, "roughness_length_diag": p, "roughness_velocity": p, "monin_obukhov_length": p,
         "scalar_flux_resistance": p, "power_flux_density_sens_soil": p, "power_flux_density_sens_sea": p,
         "sst": p, "sfc_sw_in": p, "sfc_lw_out": p,
+        "phase_trans_rates": (ny, nx, nl, 6 if ncons == 7 else 1), "phase_trans_heating_rate": s,
+        "power_flux_density_lat_lake": p, "power_flux_density_lat_sea": p,
     }
 
 

@@ -55,6 +55,7 @@ struct oracle_ctx {
   /* &surface (mo_surface_nml.F90:12-20) and the surface-layer constants of &diff; the soil grid's
    * depth of the constant temperature (mo_grid_generator.F90:1363) */
   int lprog_soil_temp, lsfc_sensible_heat_flux, lsfc_phase_trans, lpbl, nsoil;
+  int lphase_trans;  /* extension: calc_h2otracers_source_rates at the first substep */
   double h_prandtl, karman, z_t_const;
   /* grid */
   double *z_scalar, *z_u, *z_v, *z_w, *gdx, *gdy, *gdz, *volume, *area_x, *area_y, *area_z;
@@ -85,7 +86,7 @@ struct oracle_ctx {
   double *land_fraction, *lake_fraction, *roughness_length_grid, *sfc_rho_c, *t_conduc_soil, *t_const_soil;
   double *z_soil_interface, *z_soil_center, *temperature_soil[2];
   double *roughness_length, *roughness_velocity, *monin_obukhov_length, *scalar_flux_resistance;
-  double *sens_soil, *sens_sea, *sst, *sfc_sw_in, *sfc_lw_out;
+  double *sens_soil, *sens_sea, *sst, *sfc_sw_in, *sfc_lw_out, *lat_lake, *lat_sea;
   double *a_rain;
   /* lateral boundary conditions (t_bc, mo_definitions.F90:117-131): two time levels, the
    * rescale factors, the level indices (1-based) and the time of the older level */
@@ -125,6 +126,7 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   if (cfg->ny < 3 || cfg->nx < 3 || cfg->n_layers < 3 || cfg->n_oro_layers < 1 ||
       cfg->n_oro_layers >= cfg->n_layers || cfg->n_layers > 250) return LGAME_ERR_BAD_DIMS;
   if (cfg->theta_adv_order != 2 && cfg->theta_adv_order != 3) return LGAME_ERR_BAD_CONFIG;
+  if (cfg->lphase_trans && !cfg->lmoist) return LGAME_ERR_BAD_CONFIG;
   oracle_ctx* o = (oracle_ctx*)calloc(1, sizeof(oracle_ctx));
   if (!o) return LGAME_ERR_ALLOC;
   o->ny = cfg->ny; o->nx = cfg->nx; o->nl = cfg->n_layers; o->n_levels = cfg->n_layers + 1;
@@ -142,7 +144,7 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
   o->lprog_soil_temp = cfg->lprog_soil_temp; o->lsfc_sensible_heat_flux = cfg->lsfc_sensible_heat_flux;
   o->lsfc_phase_trans = cfg->lsfc_phase_trans; o->lpbl = cfg->lpbl;
   o->nsoil = cfg->nsoillays > 0 ? cfg->nsoillays : 0;
-  o->h_prandtl = cfg->h_prandtl; o->karman = cfg->karman;
+  o->h_prandtl = cfg->h_prandtl; o->karman = cfg->karman; o->lphase_trans = cfg->lphase_trans;
   if (o->nsoil > LGAME_MAX_SOIL_LAYERS) { free(o); return LGAME_ERR_BAD_CONFIG; }
   DIMS;
   const size_t nS = (size_t)ny*nx*nl, nU = (size_t)ny*(nx+1)*nl, nV = (size_t)(ny+1)*nx*nl;
@@ -196,6 +198,7 @@ int oracle_create(const lgame_config* cfg, oracle_ctx** out) {
     o->roughness_length = zalloc(n2); o->roughness_velocity = zalloc(n2); o->monin_obukhov_length = zalloc(n2);
     o->scalar_flux_resistance = zalloc(n2); o->sens_soil = zalloc(n2); o->sens_sea = zalloc(n2);
     o->sst = zalloc(n2); o->sfc_sw_in = zalloc(n2); o->sfc_lw_out = zalloc(n2);
+    o->lat_lake = zalloc(n2); o->lat_sea = zalloc(n2);
   }
   o->a_rain = zalloc(nS);
   for (double** q = &o->z_scalar; q <= &o->a_rain; ++q)
@@ -387,6 +390,10 @@ static void diag_ptrs(oracle_ctx* o, double** p, size_t* n) {
   p[LGAME_DIAG_SST] = o->sst; n[LGAME_DIAG_SST] = n2;
   p[LGAME_DIAG_SFC_SW_IN] = o->sfc_sw_in; n[LGAME_DIAG_SFC_SW_IN] = n2;
   p[LGAME_DIAG_SFC_LW_OUT] = o->sfc_lw_out; n[LGAME_DIAG_SFC_LW_OUT] = n2;
+  p[LGAME_DIAG_PHASE_TRANS_RATES] = o->phase_trans_rates; n[LGAME_DIAG_PHASE_TRANS_RATES] = nS*(size_t)(o->nc+1);
+  p[LGAME_DIAG_PHASE_TRANS_HEATING_RATE] = o->phase_trans_heating_rate; n[LGAME_DIAG_PHASE_TRANS_HEATING_RATE] = nS;
+  p[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE] = o->lat_lake; n[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE] = n2;
+  p[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA] = o->lat_sea; n[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA] = n2;
 }
 
 int oracle_set_diag(oracle_ctx* o, const double* const* f, int nfields) {

@@ -20,7 +20,7 @@ _lib = None
 
 def build(force: bool = False) -> Path:
     srcs = [HERE / "lgame_oracle.c", HERE / "lgame_oracle_ops.inc", HERE / "lgame_oracle_step.inc",
-            HERE / "lgame_oracle_diff.inc", HERE / "lgame_oracle_sfc.inc", HERE / "lgame_oracle.h",
+            HERE / "lgame_oracle_diff.inc", HERE / "lgame_oracle_sfc.inc", HERE / "lgame_oracle_phase.inc", HERE / "lgame_oracle.h",
             HERE.parent / "include" / "lgame_gpu.h", HERE / "Makefile"]
     if force or not LIB_PATH.exists() or any(s.stat().st_mtime > LIB_PATH.stat().st_mtime for s in srcs):
         subprocess.run(["make", "-s", "-C", str(HERE), "-B" if force else "all"], check=True)
