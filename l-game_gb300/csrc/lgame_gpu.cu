@@ -1264,7 +1264,7 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
       return split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
                         total_step_counter, c->stream, &c->kernels_last_step,
                         c->profiling ? trace_begin_cb : (c->mark_on ? mark_begin_cb : nullptr),
-                        c->profiling ? trace_end_cb : mark_end_cb, c);
+                        c->profiling ? trace_end_cb : mark_end_cb, c, c->profiling);
     }
     return step_fp64(c, old_slot, new_slot, total_step_counter);
   };

@@ -86,6 +86,9 @@ struct SplitCtx {
   DiffBuf<float> db{};
   // surface layer, PBL and soil (FP64 buffers of the FP64 step)
   SplitSfc sfc{};
+  // the step's concurrent branches: two side streams and the events of their forks and joins
+  cudaStream_t br[2] = {nullptr, nullptr};
+  cudaEvent_t ev[8] = {};
 };
 
 namespace {
@@ -1360,6 +1363,16 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const S
   if (sfc.phase) {  // the phase transitions' rates (graupel's is never written: stays zero) and heating
     if ((rc = salloc(s, &C.ptr, F * (size_t)(D.nc + 1), bytes)) || (rc = salloc(s, &C.pth, F, bytes))) return fail(rc);
   }
+  for (cudaStream_t& b : s->br)
+    if (cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking) != cudaSuccess) {
+      lgame_set_error("split precision: cudaStreamCreate failed");
+      return fail(LGAME_ERR_CUDA);
+    }
+  for (cudaEvent_t& e : s->ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      lgame_set_error("split precision: cudaEventCreate failed");
+      return fail(LGAME_ERR_CUDA);
+    }
   *out = s;
   return LGAME_OK;
 }
@@ -1370,6 +1383,8 @@ void split_set_sfc_par(SplitCtx* s, const SfcPar& par) { s->sfc.par = par; }
 void split_destroy(SplitCtx* s) {
   if (!s) return;
   for (void* p : s->allocs) cudaFree(p);
+  for (cudaEvent_t e : s->ev) if (e) cudaEventDestroy(e);
+  for (cudaStream_t b : s->br) if (b) cudaStreamDestroy(b);
   delete s;
 }
 
@@ -1584,18 +1599,40 @@ int split_set_grid(SplitCtx* s, const Dims& D, const Grid<double>& G, cudaStream
 
 int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn, int so, int sn,
                const PGrad<double>& pg, int step, cudaStream_t stream, int* nk,
-               int (*tb)(void*, const char*), void (*te)(void*, int), void* tracer) {
+               int (*tb)(void*, const char*), void (*te)(void*, int), void* tracer, bool serial) {
   const Grid<float>& GF = s->GF;
   const SplitCarriedF& C = s->C;
   const Tend<float> T = C.tend;
   const StateF& Mo = s->mir[so];
   const StateF& Mn = s->mir[sn];
   int launches = 0;
+  // Kernels that do not depend on each other run on side streams, forked from and joined back
+  // into `stream` by events (inside a graph capture these become the graph's edges):
+  //   first substep:  the closure, swamp-layer heating and phase transitions (FP32 and
+  //                   latency-bound) beside the theta edges and the FP64 pressure gradient;
+  //   both substeps:  the tracer tendencies beside the gas fluxes, divergences and vertical solve;
+  //   between them:   the first substep's tracer solver beside the second substep's vorticity,
+  //                   kinetic energy (FP64, on a second side stream) and wind update.
+  // Every pair was checked for the arrays one writes and the other reads (the comments at each
+  // fork); with `serial` (per-kernel tracing) everything runs on `stream` in the same order.
+  const bool conc = !serial;
+  cudaStream_t cur = stream;
+  cudaStream_t side = conc ? s->br[0] : stream, side2 = conc ? s->br[1] : stream;
+  enum { EV_A = 0, EV_JA, EV_B, EV_C, EV_CSH, EV_KE, EV_JKE, EV_END };
+  // `to` starts after everything enqueued on `from` so far
+  auto after = [&](cudaStream_t to, cudaStream_t from, int k) -> int {
+    if (!conc || to == from) return LGAME_OK;
+    if (cudaEventRecord(s->ev[k], from) != cudaSuccess || cudaStreamWaitEvent(to, s->ev[k], 0) != cudaSuccess) {
+      lgame_set_error("split step: fork/join event failed");
+      return LGAME_ERR_CUDA;
+    }
+    return LGAME_OK;
+  };
 #define SL(name, kernel, grid_, block_, ...) SLS(name, kernel, grid_, block_, 0, __VA_ARGS__)
 #define SLS(name, kernel, grid_, block_, smem_, ...)                            \
   do {                                                                          \
     const int tr_ = tb ? tb(tracer, name) : -1;                                 \
-    kernel<<<grid_, block_, smem_, stream>>>(__VA_ARGS__);                      \
+    kernel<<<grid_, block_, smem_, cur>>>(__VA_ARGS__);                         \
     if (tr_ >= 0) te(tracer, tr_);                                              \
     cudaError_t e_ = cudaGetLastError();                                        \
     if (e_ != cudaSuccess) {                                                    \
@@ -1603,6 +1640,11 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
       return LGAME_ERR_CUDA;                                                    \
     }                                                                           \
     ++launches;                                                                 \
+  } while (0)
+#define SYNC(call)                   \
+  do {                               \
+    const int rc_ = (call);          \
+    if (rc_ != LGAME_OK) return rc_; \
   } while (0)
   const dim3 B = sblk();
   // third-order theta edges: the gradient of theta' (read from the mirror), its divergence and
@@ -1623,10 +1665,93 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
   if (SF.turb) SL("ks_sfc_turb", k_sfc_turb, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par);
   Carried<float> CC{pg.nl_u, pg.nl_v, pg.nl_w, pg.l_u, pg.l_v, pg.l_w, pg.old_u, pg.old_v, C.pgcw,
                     C.vsg_x, C.vsg_y, C.vsg_z, C.pvt_x, C.pvt_y, C.pvt_z};
+  const SplitDiff& SD = s->diff;
+  const DiffBuf<float>& DB = s->db;
+  const bool vort = !D.llinear || D.lcorio, tracers = D.ncons > 1;
+  const float* mdt = (SD.mom_h && SD.mass_h) ? DB.mdt : nullptr;
+  const float* tdh = (SD.mom_h && SD.temp_h) ? DB.tdh : nullptr;
+  const float* ptr = SF.phase ? C.ptr : nullptr;
+  const float* pth = SF.phase ? C.pth : nullptr;
+  if (SD.mom_h) { CC.mdt_x = DB.mdtx; CC.mdt_y = DB.mdty; CC.mdt_z = DB.mdtz; }
+  // the vorticity flux and the kinetic-energy gradient of state Sv (mirror Mv); with `branch`
+  // the kinetic energy (FP64) runs on the second side stream beside the vorticity (FP32)
+  auto vector_terms = [&](const State& Sv, const StateF& Mv, bool branch) -> int {
+    if (!vort) return LGAME_OK;
+    const bool ke = !D.llinear;
+    if (ke && branch) {
+      SYNC(after(side2, stream, EV_KE));
+      cur = side2;
+    }
+    if (ke) {
+      SL("ks_ke", (k_ke<double, double>), sgrd(D.ny, D.nx, D.nl), B, D, G, Sv, s->vsq);
+      SL("ks_grad_vert", (k_grad_vert<float, double>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->vsq, C.vsg_z);
+      SL("ks_grad_hor", (k_grad_hor<float, double>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->vsq, C.vsg_z,
+         C.vsg_x, C.vsg_y);
+    }
+    cur = stream;
+    SL("ks_eta", ks_eta, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey, s->ez, s->uph, s->vph, s->wph);
+    SL("ks_vort_flux", ks_vort_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
+       s->ez, s->uph, s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
+    if (ke && branch) SYNC(after(stream, side2, EV_JKE));
+    return LGAME_OK;
+  };
   for (int rk = 1; rk <= 2; ++rk) {
-    const State& Sv = (rk == 1) ? So : Sn;
-    const StateF& Mv = (rk == 1) ? Mo : Mn;
+    const StateF& Ms = (rk == 1) ? Mo : Mn;
     if (rk == 1) {
+      // side: the closure (momentum diffusion, dissipation, scalar diffusion), or the swamp
+      // layer's heating, and the phase transitions: they read the old mirror, its temperature
+      // and the surface quantities, and write only their own buffers (DB, hdiss, ptr/pth, the
+      // latent fluxes).  main: theta edges, gzp, pressure gradient (scratch gx..divf, tvu..tpv,
+      // gzd, rmz, the pressure-gradient arrays).  Joined before the wind update.
+      const bool side_work = SD.mom_h || (D.lklemp && D.ndamp > 0) || SF.phase;
+      // step 0 forms the vector terms at the first substep too (mo_vector_tend_expl.F90:41-98),
+      // before the closure: the PBL reads the kinetic energy they form
+      if (step == 0) SYNC(vector_terms(So, Mo, false));
+      if (side_work) {
+        SYNC(after(side, stream, EV_A));
+        cur = side;
+      }
+      if (SD.mom_h) {
+        const dim3 gs = sgrd(D.ny, D.nx, D.nl);
+        SL("ks_diff_tke", (k_diff_tke<float, float>), gs, B, D, GF, Mo, DB, SD.par);
+        SL("ks_diff_zeta", (k_diff_zeta<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
+        SL("ks_diff_visc", (k_diff_visc<float, float>), gs, B, D, GF, Mo, (const float*)C.temperature, DB, SD.par);
+        SL("ks_diff_vz", (k_diff_vz<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
+        SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
+        if (SD.mom_v) SL("ks_mom_diff_v", (k_mom_diff_v<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, Mo, DB);
+        if (SF.pbl)
+          SL("ks_pbl", k_pbl<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
+        SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
+        // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101); the second substep's
+        // temperature diffusion is the same (same temperature and coefficients)
+        const dim3 ge = sgrd(D.ny + 1, D.nx + 1, D.nl);
+        if (SD.temp_h) {
+          const int vert = SD.temp_v ? 1 : 0;
+          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB,
+             (const float*)C.temperature, 1, vert, DB.flx, DB.fly, DB.flw);
+          SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.tdh);
+        }
+        if (SD.mass_h) {  // every constituent in one launch each (1 dry, 7 moist)
+          const int vert = SD.mass_v ? 1 : 0;
+          if (D.ncons == 7) {
+            SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 7>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho,
+               0, vert, DB.flx, DB.fly, DB.flw);
+            SL("ks_diff_divs", (k_diff_divs<float, 7>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
+          } else {
+            SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho,
+               0, vert, DB.flx, DB.fly, DB.flw);
+            SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
+          }
+        }
+      } else if (D.lklemp && D.ndamp > 0) {
+        SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
+      }
+      // the phase transitions (extension) from state_old and its temperature, in FP64 on the FP64
+      // state; both substeps read the rates
+      if (SF.phase)
+        SL("ks_phase_trans", (k_phase_trans<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, G, So,
+           (const float*)C.temperature, SF.buf, SF.tsoil[so], SF.phase_sfc ? 1 : 0, D.dtime, C.ptr, C.pth);
+      cur = stream;
       if (D.theta_order == 3) {  // the edges of theta_v and, with a background state, of theta'
         const int rc = theta3f(Mo.tp, Mo.u, Mo.v, s->tvu, s->tvv, D.luse_bg ? s->tpu : nullptr,
                                D.luse_bg ? s->tpv : nullptr);
@@ -1635,73 +1760,23 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
       SL("ks_gzp", ks_gzp, sgrd(D.ny, D.nx, D.nl), B, D, G, s->GX, So.ep, s->gzd, s->rmz);
       SL("ks_pgrad", ks_pgrad, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, G, s->GX, So, s->gzd, s->rmz, Mo.rho, s->tvu,
          s->tvv, s->tpu, s->tpv, pg, C, C.pgcw, step == 0 ? 1 : 0);
-    }
-    if ((rk == 2 || step == 0) && (!D.llinear || D.lcorio)) {
-      SL("ks_eta", ks_eta, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, GF, Mv, s->ex, s->ey, s->ez, s->uph, s->vph, s->wph);
-      SL("ks_vort_flux", ks_vort_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mv, s->ex, s->ey,
-         s->ez, s->uph, s->vph, s->wph, C.pvt_x, C.pvt_y, C.pvt_z);
-      if (!D.llinear) {
-        SL("ks_ke", (k_ke<double, double>), sgrd(D.ny, D.nx, D.nl), B, D, G, Sv, s->vsq);
-        SL("ks_grad_vert", (k_grad_vert<float, double>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, s->vsq, C.vsg_z);
-        SL("ks_grad_hor", (k_grad_hor<float, double>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, s->vsq, C.vsg_z,
-           C.vsg_x, C.vsg_y);
-      }
-    }
-    // momentum diffusion and dissipation at the first substep (mo_vector_tend_expl.F90:100-126),
-    // from state_old's mirror; with the Klemp layer alone, the swamp layer's heating
-    const SplitDiff& SD = s->diff;
-    const DiffBuf<float>& DB = s->db;
-    if (rk == 1 && SD.mom_h) {
-      const dim3 gs = sgrd(D.ny, D.nx, D.nl);
-      SL("ks_diff_tke", (k_diff_tke<float, float>), gs, B, D, GF, Mo, DB, SD.par);
-      SL("ks_diff_zeta", (k_diff_zeta<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
-      SL("ks_diff_visc", (k_diff_visc<float, float>), gs, B, D, GF, Mo, (const float*)C.temperature, DB, SD.par);
-      SL("ks_diff_vz", (k_diff_vz<float, float>), sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Mo, DB);
-      SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
-      if (SD.mom_v) SL("ks_mom_diff_v", (k_mom_diff_v<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, Mo, DB);
-      if (SF.pbl)
-        SL("ks_pbl", k_pbl<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
-      SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
-      CC.mdt_x = DB.mdtx; CC.mdt_y = DB.mdty; CC.mdt_z = DB.mdtz;
-    } else if (rk == 1 && D.lklemp && D.ndamp > 0) {
-      SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
+      if (side_work) SYNC(after(stream, side, EV_JA));
+    } else {
+      // main: vorticity of the new state; side 2: its kinetic energy (FP64); both read the state
+      // of the first substep (u, v from its wind update, w and rho_g from its vertical solve),
+      // which the tracer solver still running on the side stream does not write
+      SYNC(vector_terms(Sn, Mn, true));
     }
     SL("ks_tend_wind", ks_tend_wind, sgrd(D.ny + 1, D.nx + 1, D.NL), B, D, So, Sn, T, CC, C, rk, Mn.u, Mn.v);
-    const StateF& Ms = (rk == 1) ? Mo : Mn;
-    // temperature and mass diffusion at the first substep (mo_scalar_tend_expl.F90:60-101); the
-    // second substep's temperature diffusion is the same (same temperature and coefficients)
-    if (rk == 1 && SD.mom_h && (SD.temp_h || SD.mass_h)) {
-      const dim3 gs = sgrd(D.ny, D.nx, D.nl), ge = sgrd(D.ny + 1, D.nx + 1, D.nl);
-      if (SD.temp_h) {
-        const int vert = SD.temp_v ? 1 : 0;
-        SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)C.temperature,
-           1, vert, DB.flx, DB.fly, DB.flw);
-        SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.tdh);
-      }
-      if (SD.mass_h) {  // every constituent in one launch each (1 dry, 7 moist)
-        const int vert = SD.mass_v ? 1 : 0;
-        if (D.ncons == 7) {
-          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 7>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho, 0,
-             vert, DB.flx, DB.fly, DB.flw);
-          SL("ks_diff_divs", (k_diff_divs<float, 7>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
-        } else {
-          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho, 0,
-             vert, DB.flx, DB.fly, DB.flw);
-          SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
-        }
-      }
-    }
-    const float* mdt = (SD.mom_h && SD.mass_h) ? DB.mdt : nullptr;
-    const float* tdh = (SD.mom_h && SD.temp_h) ? DB.tdh : nullptr;
-    // the phase transitions (extension) at the first substep, from state_old and its temperature,
-    // in FP64 on the FP64 state; both substeps read the rates
-    if (rk == 1 && SF.phase)
-      SL("ks_phase_trans", (k_phase_trans<float, float>), sgrd(D.ny, D.nx, D.nl), B, D, G, So, (const float*)C.temperature,
-         SF.buf, SF.tsoil[so], SF.phase_sfc ? 1 : 0, D.dtime, C.ptr, C.pth);
-    const float* ptr = SF.phase ? C.ptr : nullptr;
-    const float* pth = SF.phase ? C.pth : nullptr;
-    if (D.ncons > 1)
+    // side: the tracer tendencies (read the tracer densities of Ms and the new u, v; write the
+    // tracer fields of T.rho), beside the gas fluxes, divergence and vertical solve, which write
+    // the gas field of T.rho, T.rt, the gas density, theta', exner', rhotheta_v and w
+    if (tracers) {
+      SYNC(after(side, stream, EV_B));
+      cur = side;
       SL("ks_tracers", ks_tracers, sgrd(D.ny, D.nx, D.nl), B, D, GF, s->GX, Ms, Mn.u, Mn.v, T.rho, rk, mdt, ptr);
+      cur = stream;
+    }
     // third-order theta edges of the state used here; in the first substep that is the old
     // state, whose edges the pressure gradient's call above already left in tvu/tvv (nothing
     // in between writes the old mirror or tvu/tvv), so only the second substep recomputes them
@@ -1711,6 +1786,14 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     }
     SL("ks_gas_flux", ks_gas_flux, sgrd(D.ny + 1, D.nx + 1, D.nl), B, D, GF, Ms, Mn.u, Mn.v, s->tvu, s->tvv, s->fu,
        s->fv, s->gu, s->gv);
+    // the second substep's gas divergence reads every density of the new mirror (the heat
+    // capacity) and the sediment heating: it waits for the first substep's tracer solver
+    if (rk == 2 && tracers && conc) {
+      if (cudaStreamWaitEvent(stream, s->ev[EV_CSH], 0) != cudaSuccess) {
+        lgame_set_error("split step: join event failed");
+        return LGAME_ERR_CUDA;
+      }
+    }
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
        C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh, ptr, pth);
     if (SF.sens || SF.soil)
@@ -1721,17 +1804,33 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
       SL("ks_column_ver", ks_column_ver<double>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
     else
       SL("ks_column_ver", ks_column_ver<float>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
-    if (D.ncons > 1) {
+    if (tracers) {
       // the two tracer sets fastest (the blocks of a row tile run together), row tiles, columns
       const dim3 gt(2u, (unsigned)((D.ny + 31) / 32), (unsigned)D.nx);
-      SLS("ks_column_tracers", (rk == 1 ? ks_column_tracers<true> : ks_column_tracers<false>), gt,
-          dim3(kTrWarps * 32), tracer_smem(D), D, GF, s->GX, So, Sn, Mo, Mn, T.rho, C.temperature, s->csh_part);
-      if (rk == 1 && D.nc > 0)
-        SL("ks_csh_sum", ks_csh_sum, sgrd(D.ny, D.nx, D.nl), B, D, s->csh_part, C.csh);
+      if (rk == 1) {
+        // side (after its tracer tendencies): the first substep's tracer solver and sediment
+        // heating, which read w old and new and the gas density (final now) and write the
+        // tracer densities and csh, beside the second substep's vorticity and wind update
+        SYNC(after(side, stream, EV_C));
+        cur = side;
+        SLS("ks_column_tracers", ks_column_tracers<true>, gt, dim3(kTrWarps * 32), tracer_smem(D), D, GF, s->GX, So,
+            Sn, Mo, Mn, T.rho, C.temperature, s->csh_part);
+        if (D.nc > 0) SL("ks_csh_sum", ks_csh_sum, sgrd(D.ny, D.nx, D.nl), B, D, s->csh_part, C.csh);
+        if (conc && cudaEventRecord(s->ev[EV_CSH], side) != cudaSuccess) {
+          lgame_set_error("split step: event record failed");
+          return LGAME_ERR_CUDA;
+        }
+        cur = stream;
+      } else {
+        SYNC(after(stream, side, EV_END));
+        SLS("ks_column_tracers", ks_column_tracers<false>, gt, dim3(kTrWarps * 32), tracer_smem(D), D, GF, s->GX, So,
+            Sn, Mo, Mn, T.rho, C.temperature, s->csh_part);
+      }
     }
   }
 #undef SL
 #undef SLS
+#undef SYNC
   *nk = launches;
   return LGAME_OK;
 }

@@ -94,6 +94,7 @@ int split_refresh_mirror(SplitCtx* s, const Dims& D, int slot, const State& S, c
 // arrays (shared with the FP64 path).  The mirrors of both slots must be current.
 int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& So, const State& Sn, int so, int sn,
                const PGrad<double>& pg, int step, cudaStream_t stream, int* nkernels,
-               int (*trace_begin)(void*, const char*), void (*trace_end)(void*, int), void* tracer);
+               int (*trace_begin)(void*, const char*), void (*trace_end)(void*, int), void* tracer,
+               bool serial);
 
 }  // namespace lg
