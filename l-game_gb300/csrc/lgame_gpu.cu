@@ -525,8 +525,8 @@ const auto k_diff_fluxes1 = lg::k_diff_fluxes<double, double, double, 1>;
 const auto k_diff_fluxes7 = lg::k_diff_fluxes<double, double, double, 7>;
 const auto k_diff_divs1 = lg::k_diff_divs<double, 1>;
 const auto k_diff_divs7 = lg::k_diff_divs<double, 7>;
-const auto k_sfc_turb = lg::k_sfc_turb;
-const auto k_pbl = lg::k_pbl<double>;
+const auto k_sfc_turb = lg::k_sfc_turb<double>;
+const auto k_pbl = lg::k_pbl<double, double>;
 const auto k_sfc_column = lg::k_sfc_column<double>;
 const auto k_phase_trans = lg::k_phase_trans<double, double>;
 }  // namespace kd
@@ -1011,6 +1011,9 @@ extern "C" int lgame_gpu_set_grid(lgame_gpu* c, const double* const* f, int nfie
     for (int k = 0; k <= P.ns; ++k) P.zi[k] = f[LGAME_GRID_Z_SOIL_INTERFACE][k];
     for (int k = 0; k < P.ns; ++k) P.zc[k] = f[LGAME_GRID_Z_SOIL_CENTER][k];
     P.z_t_const = f[LGAME_GRID_Z_T_CONST][0];
+    for (int k = 0; k < P.ns; ++k) P.idzi[k] = 1.0 / (P.zi[k] - P.zi[k + 1]);
+    for (int k = 0; k + 1 < P.ns; ++k) P.idzc[k] = 1.0 / (P.zc[k] - P.zc[k + 1]);
+    P.i2dzt = P.ns > 0 ? 1.0 / (2.0 * (P.zc[P.ns - 1] - P.z_t_const)) : 0.0;
     if (c->split) split_set_sfc_par(c->split, P);
   }
   // inner product weights: (6,ny,nx,nl) -> six padded fields

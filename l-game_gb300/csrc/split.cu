@@ -1662,7 +1662,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
   // the surface parts in FP64 on the FP64 state (two-dimensional): update_sfc_turb_quantities
   // before the substeps (mo_manage_pchevi.F90:51-53)
   const SplitSfc& SF = s->sfc;
-  if (SF.turb) SL("ks_sfc_turb", k_sfc_turb, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par);
+  if (SF.turb) SL("ks_sfc_turb", k_sfc_turb<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par);
   Carried<float> CC{pg.nl_u, pg.nl_v, pg.nl_w, pg.l_u, pg.l_v, pg.l_w, pg.old_u, pg.old_v, C.pgcw,
                     C.vsg_x, C.vsg_y, C.vsg_z, C.pvt_x, C.pvt_y, C.pvt_z};
   const SplitDiff& SD = s->diff;
@@ -1720,7 +1720,7 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
         SL("ks_mom_diff_h", (k_mom_diff_h<float, float>), gs, B, D, GF, Mo, DB);
         if (SD.mom_v) SL("ks_mom_diff_v", (k_mom_diff_v<float, float>), sgrd(D.ny, D.nx, D.nl - 1), B, D, GF, Mo, DB);
         if (SF.pbl)
-          SL("ks_pbl", k_pbl<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
+          SL("ks_pbl", (k_pbl<float, float>), sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
         SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
         // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101); the second substep's
         // temperature diffusion is the same (same temperature and coefficients)
@@ -1797,8 +1797,8 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
     SL("ks_gas_div", ks_gas_div, cgrd(D.ny, D.nx), cblk(), D, GF, s->GX, Ms, s->fu, s->fv, s->gu, s->gv,
        C.temperature, C.hdiss, C.rad, C.csh, T.rho, T.rt, mdt, tdh, ptr, pth);
     if (SF.sens || SF.soil)
-      SL("ks_sfc_column", k_sfc_column<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, rk == 1 ? So : Sn, T.rt, SF.buf,
-         SF.par, SF.tsoil[so], SF.tsoil[rk == 1 ? so : sn], SF.tsoil[sn]);
+      SL("ks_sfc_column", k_sfc_column_split<float>, sgrd(D.ny, D.nx, 1), B, D, G, So, rk == 1 ? So : Sn, T.rt,
+         SF.buf, SF.par, SF.tsoil[so], SF.tsoil[rk == 1 ? so : sn], SF.tsoil[sn]);
     const dim3 gc = cgrd(D.ny, D.nx);
     if (s->column_fp64)
       SL("ks_column_ver", ks_column_ver<double>, gc, cblk(), D, G, GF, s->GX, So, Sn, Mo, Mn, T, rk);
