@@ -9,7 +9,7 @@
  * tendency (src/time_stepping/mo_scalar_tend_expl.F90:157-166).  Here a small MLP predicts
  * the shortwave and longwave heating-rate profiles of every column from its state, on the
  * GPU, with BF16 tensor-core (tcgen05) kernels for training and inference; a CPU scheme
- * (lgame_rad_teacher) stands in for RRTMGP as the source of training targets, the judge of
+ * (lgame_rad_teacher) stands in for RRTMGP as the source of training targets, the check of
  * sampled columns and the fallback.
  *
  * Column features (float, one row of 4*nlev+2 per column, layer 1 = top):

@@ -1,5 +1,5 @@
 // teacher.cpp -- stand-in radiation scheme (CPU) that produces the training targets of the
-// radiation emulator and serves as its judge and fallback.
+// radiation emulator and serves as the check of its error and its fallback.
 //
 // The reference computes radiation with RTE+RRTMGP (src/radiation/mo_rterrtmgp_coupler.F90),
 // an external package that is not part of the reference tree and cannot be built here.  In

@@ -7,7 +7,7 @@ so it is the reference here.  Error of a field f:
 
 with a floor at the field's physical scale (1 m/s for the winds, 1 K for theta_v',
 1e-3 for exner'), so that fields which stay at round-off level (a fluid at rest over
-hills, where the FP64 winds are ~1e-14 m/s) are judged on an absolute scale rather
+hills, where the FP64 winds are ~1e-14 m/s) are measured on an absolute scale rather
 than relative to their own noise.  Bar: every field finite, error <= 1e-5 after one
 step and <= 3e-5 after ten.  The hour-scale error study is l-game_gb300/error_study.py.
 """
