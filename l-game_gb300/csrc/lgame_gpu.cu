@@ -1260,14 +1260,17 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
       c->mirror_valid[slot] = true;
     }
   }
-  auto launch_step = [&]() -> int {
+  // The split step's concurrent branches pay where its kernels are launched one by one (the
+  // host-buffer step, whose copy-out then starts earlier: 132.5 against 137-139 ms end to end
+  // at 1024x1024x80); a captured graph runs faster in the serial order (58.57 against 58.75 ms)
+  auto launch_step = [&](bool serial) -> int {
     if (c->split) {
       PGrad<double> P{c->pg_nl_u, c->pg_nl_v, c->pg_nl_w, c->pg_l_u, c->pg_l_v, c->pg_l_w, c->pg_old_u, c->pg_old_v,
                       c->pgcw};
       return split_step(c->split, c->D, c->G, c->st[old_slot], c->st[new_slot], old_slot, new_slot, P,
                         total_step_counter, c->stream, &c->kernels_last_step,
                         c->profiling ? trace_begin_cb : (c->mark_on ? mark_begin_cb : nullptr),
-                        c->profiling ? trace_end_cb : mark_end_cb, c, c->profiling);
+                        c->profiling ? trace_end_cb : mark_end_cb, c, serial || c->profiling);
     }
     return step_fp64(c, old_slot, new_slot, total_step_counter);
   };
@@ -1278,7 +1281,7 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
     cudaGraphExec_t& exec = c->graph[old_slot];
     if (!exec) {
       CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      rc = launch_step();
+      rc = launch_step(true);
       cudaGraph_t graph = nullptr;
       const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
       if (rc != LGAME_OK) {
@@ -1298,7 +1301,7 @@ extern "C" int lgame_gpu_pchevi(lgame_gpu* c, int old_slot, int new_slot, int to
     c->kernels_last_step = c->graph_kernels[old_slot];
     rc = LGAME_OK;
   } else {
-    rc = launch_step();
+    rc = launch_step(false);
   }
   if (rc != LGAME_OK) return rc;
   // mo_manage_pchevi.F90:114-116

@@ -1607,14 +1607,15 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
   const StateF& Mn = s->mir[sn];
   int launches = 0;
   // Kernels that do not depend on each other run on side streams, forked from and joined back
-  // into `stream` by events (inside a graph capture these become the graph's edges):
+  // into `stream` by events:
   //   first substep:  the closure, swamp-layer heating and phase transitions (FP32 and
   //                   latency-bound) beside the theta edges and the FP64 pressure gradient;
   //   both substeps:  the tracer tendencies beside the gas fluxes, divergences and vertical solve;
   //   between them:   the first substep's tracer solver beside the second substep's vorticity,
   //                   kinetic energy (FP64, on a second side stream) and wind update.
   // Every pair was checked for the arrays one writes and the other reads (the comments at each
-  // fork); with `serial` (per-kernel tracing) everything runs on `stream` in the same order.
+  // fork); with `serial` (per-kernel tracing, and the caller's graph capture, where the serial
+  // order measured faster) everything runs on `stream` in the same order.
   const bool conc = !serial;
   cudaStream_t cur = stream;
   cudaStream_t side = conc ? s->br[0] : stream, side2 = conc ? s->br[1] : stream;

@@ -45,10 +45,11 @@ BRANCH_PHYSICS = dict(lmom_diff_h=True, lmom_diff_v=True, ltemp_diff_h=True, lte
 @pytest.mark.gpu
 @pytest.mark.parametrize("physics", [False, True])
 def test_split_branches_equal_serial_order(physics):
-    """The split step's concurrent branches (side streams, joined by events; in the captured graph
-    after step 0) against the same kernels one after another on one stream (per-kernel tracing
-    runs them so): the same bits after five steps, with the plain step and with every physics
-    switch on (the branches that run the closure, the PBL and the phase transitions)."""
+    """The split step's concurrent branches (side streams joined by events, as the step runs when
+    launched kernel by kernel) against the same kernels one after another on one stream (as
+    per-kernel tracing and the captured graph run them): the same bits after five steps, with the
+    plain step and with every physics switch on (the branches that run the closure, the PBL and
+    the phase transitions)."""
     key, ov = cases.SMALL["jet"]
     n = cases.namelist(key, **{**ov, **(BRANCH_PHYSICS if physics else {})})
     hm = L.HostModel(n)
@@ -57,6 +58,7 @@ def test_split_branches_equal_serial_order(physics):
     models = []
     for serial in (False, True):
         g = L.GpuModel(cfg, hm.grid)
+        g.set_graphs(False)
         g.set_profiling(serial)
         g.set_state(0, hm.state)
         g.set_state(1, hm.state)
