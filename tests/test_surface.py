@@ -311,6 +311,12 @@ GPU_CASES = {
     "jet_soil_only": ("jet", dict(lsfc_sensible_heat_flux=False, lsfc_phase_trans=False, lpbl=False,
                                   lmom_diff_h=False, lmom_diff_v=False, ltemp_diff_h=False, ltemp_diff_v=False,
                                   lmass_diff_h=False, lmass_diff_v=False), True),
+    # the PBL alone: the turbulence update without the scalar flux resistance (no soil)
+    "jet_pbl_only": ("jet", dict(lprog_soil_temp=False, lsfc_sensible_heat_flux=False, lsfc_phase_trans=False), False),
+    # the surface phase-transition switch alone: only the turbulence update runs (the reference's
+    # step forms no phase transitions), and its roughness length is carried
+    "jet_sfc_phase_switch_only": ("jet", dict(lsfc_sensible_heat_flux=False, lpbl=False, lprog_soil_temp=False),
+                                  False),
 }
 
 
