@@ -231,6 +231,10 @@ enum lgame_diag_field {
   LGAME_DIAG_PHASE_TRANS_HEATING_RATE,/* (ny,nx,nl)  W m^-3                                 */
   LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE, /* (ny,nx) W m^-2, latent heat into lakes       */
   LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA,  /* (ny,nx) W m^-2, latent heat into the sea     */
+  /* the temperature and mass diffusion (mo_definitions.F90:207-209), formed at each step's first
+   * substep from state_old (zero when ltemp_diff_h / lmass_diff_h is off) */
+  LGAME_DIAG_TEMP_DIFF_HEATING,       /* (ny,nx,nl)  W m^-3, heating by temperature diffusion */
+  LGAME_DIAG_MASS_DIFF_TENDENCY,      /* (ny,nx,nl,n_constituents) kg m^-3 s^-1, mass diffusion */
   LGAME_DIAG_NFIELDS
 };
 

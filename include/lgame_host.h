@@ -107,7 +107,7 @@ double* lgame_host_diag_field(lgame_host_model* m, int field, size_t* n);
 double* lgame_host_surface_field(lgame_host_model* m, int field, size_t* n);
 
 /* ---- raw binary files where the reference uses netCDF (absent here) ------------------------
- * A 64-byte little-endian header (magic "LGAMESNP" or "LGAMEBCL", int32 version 3, int32 ny,
+ * A 64-byte little-endian header (magic "LGAMESNP" or "LGAMEBCL", int32 version 4, int32 ny,
  * nx, n_layers, n_constituents, then the int64 step counter or the FP64 valid time, then int32
  * nsoillays (0 in a boundary level)) followed by
  * FP64 arrays in the reference layout (column-major, reference extents).  Readers check the

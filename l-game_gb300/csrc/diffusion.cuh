@@ -557,4 +557,183 @@ __global__ void k_diff_divs(Dims D, Grid<T> G, const T* __restrict__ fx, const T
   }
 }
 
+// ---- 7b. temperature and mass diffusion of the split step, fluxes and divergence fused ----------
+// k_diff_fluxes followed by k_diff_divs in FP32, in one launch that marches down the levels, so
+// the flux densities never reach HBM.  A block owns a tile of DS_X rows (ji, a lane each) by
+// DS_Y columns (jk, a warp each) and walks it from the top layer to the bottom; three more warps
+// hold the tile's halo: the columns jk0-1 and jk0+DS_Y, and the rows ji0-1 and ji0+DS_X (a lane
+// per column).  Each level takes three phases, separated by barriers:
+//   A  every slot (tile or halo cell, the periodic wrap applied) puts into shared memory its
+//      field values, its half of the terrain remap of the vertical gradients,
+//      hc = ipw5*gz(l) + ipw6*gz(l+1), and its horizontal coefficient;
+//   B  each face is formed once, by the slot east (u point) or south (v point) of it:
+//      h*((s_b - s_a)/dx - slope*0.5*(hc_a + hc_b)) with h = 0.5*(coef_a + coef_b);
+//   C  each tile cell adds its four faces and the contravariant corrections of its two
+//      interfaces.  The correction at an interface is the sum of the slope-weighted face terms of
+//      the layers above and below it; a layer's term is formed once and carried to the next
+//      level, and so is the divergence itself, which is finished one level later, when its
+//      lower interface's correction and vertical flux are known.
+// The reference's sums (grad_hor's remap, vertical_contravariant_corr, div_h plus
+// add_vertical_div: mo_averaging.F90:16-136, mo_divergence_operators.F90:16-68, 149-186) are
+// regrouped, so the FP32 results differ from the two-kernel form in the last bits; the FP64
+// step keeps the two kernels and the reference's order.  KIND 0: mass (coefficient
+// viscosity/rho_gas), KIND 1: temperature (c_d_v*viscosity, the vertical one times rho_gas);
+// NF fields of fstride at s0, results into out.
+constexpr int DS_X = 32, DS_Y = 8, DS_THREADS = 32 * (DS_Y + 3);
+
+template <int NF, int KIND>
+__global__ void __launch_bounds__(DS_THREADS, 2)
+k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float* __restrict__ s0, int vertical,
+                  float* __restrict__ out) {
+  constexpr int SX = DS_X + 2, NS = SX * (DS_Y + 2);
+  __shared__ float sh_s[NF][NS], sh_h[NF][NS], sh_c[NS];
+  __shared__ float sh_fx[NF][DS_Y + 1][DS_X], sh_fy[NF][DS_Y][DS_X + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int ji0 = blockIdx.x * DS_X + 1, jk0 = blockIdx.y * DS_Y + 1;
+  // the slot: role 0 tile, 1 west halo, 2 east halo, 3 north halo, 4 south halo, -1 none
+  int ji = ji0, jk = jk0, role = -1;
+  if (warp < DS_Y) { ji = ji0 + lane; jk = jk0 + warp; role = 0; }
+  else if (warp == DS_Y) { ji = ji0 + lane; jk = jk0 - 1; role = 1; }
+  else if (warp == DS_Y + 1) { ji = ji0 + lane; jk = jk0 + DS_Y; role = 2; }
+  else if (lane < DS_Y) { ji = ji0 - 1; jk = jk0 + lane; role = 3; }
+  else if (lane < 2 * DS_Y) { ji = ji0 + DS_X; jk = jk0 + lane - DS_Y; role = 4; }
+  const int slot = (jk - jk0 + 1) * SX + (ji - ji0 + 1);
+  // the cell whose values the slot holds: itself, or its image across a periodic edge
+  bool has = role >= 0 && ji >= 0 && ji <= D.ny + 1 && jk >= 0 && jk <= D.nx + 1;
+  if (!D.periodic) has = has && ji >= 1 && ji <= D.ny && jk >= 1 && jk <= D.nx;
+  const int ci = ji < 1 ? D.ny : (ji > D.ny ? 1 : ji), ck = jk < 1 ? D.nx : (jk > D.nx ? 1 : jk);
+  // the faces formed here: the u point (ji, jk) west of the slot and the v point (ji, jk) north of
+  // it, zero at non-periodic edges (where the reference writes none)
+  const bool fx_own = (role == 0 || role == 2) && ji >= 1 && ji <= D.ny && jk <= D.nx + 1;
+  const bool fy_own = (role == 0 || role == 4) && ji <= D.ny + 1 && jk <= D.nx;
+  const bool fx_zero = !D.periodic && (jk == 1 || jk == D.nx + 1);
+  const bool fy_zero = !D.periodic && (ji == 1 || ji == D.ny + 1);
+  const bool cell = role == 0 && ji <= D.ny && jk <= D.nx;
+  const bool vert = vertical != 0 && cell;
+  const int fr = jk - jk0, fc = ji - ji0;  // the slot's u point in sh_fx, v point in sh_fy
+  const long long F = D.fstride, pl = D.plane, gF = (long long)(D.g - 1) * D.fstride;
+  const int nl = D.nl, nf = D.nf;
+  // u and v points of the slot at level 1 (dx, dy at the wrapped cell, slopes at the point itself)
+  const long long qu1 = IX(D, ji >= 1 ? ji : 1, jk >= 1 ? jk : 1, 1);
+  const long long qdx1 = IX(D, ji >= 1 ? ji : 1, jk == D.nx + 1 ? 1 : (jk >= 1 ? jk : 1), 1);
+  const long long qdy1 = IX(D, ji == D.ny + 1 ? 1 : (ji >= 1 ? ji : 1), jk >= 1 ? jk : 1, 1);
+  const long long c1 = has ? IX(D, ci, ck, 1) : 0;
+
+  float sv[NF], sn[NF], gz[NF], gn[NF], P[NF], tp[NF];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    sv[f] = has ? s0[c1 + f * F] : 0.f;
+    sn[f] = (has && nl >= 2) ? s0[c1 + pl + f * F] : 0.f;
+    gz[f] = 0.f;
+    gn[f] = 0.f;
+    P[f] = 0.f;
+    tp[f] = 0.f;
+  }
+  float cvp = 0.f, volp = 1.f;
+  for (int l = 1; l <= nl; ++l) {
+    const long long lo = (long long)(l - 1) * pl, q = c1 + lo;
+    const bool terrain = l > nf, g_lo = l < nl;
+    // ---- A: the slot's values, remap halves and coefficient; the cell's vertical coefficient
+    float hv = 0.f;
+    if (has) {
+      float w5 = 0.f, w6 = 0.f;
+      if (terrain) {
+        w5 = G.ipw[4][q];
+        if (g_lo || D.freeslip) w6 = G.ipw[5][q];
+      }
+      const float idz = g_lo ? 1.f / G.dz[q + pl] : 0.f;
+      const float vi = B.visc[q];
+      sh_c[slot] = KIND == 0 ? vi / S.rho[q + gF] : float(kC_D_V) * vi;
+      if (vert) {  // diff_coeff_v at the cell; the interface above takes the mean with the layer above
+        const float t2v = B.vmol[q] + tke2vert<float>(B.tke[q], B.nsq[q], G.layer_thickness[q]);
+        const float cvn = KIND == 0 ? t2v : S.rho[q + gF] * float(kC_D_V) * t2v;
+        hv = 0.5f * (cvp + cvn);
+        cvp = cvn;
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        gn[f] = g_lo ? (sv[f] - sn[f]) * idz : 0.f;
+        sh_s[f][slot] = sv[f];
+        if (terrain) sh_h[f][slot] = w5 * gz[f] + w6 * gn[f];
+        sv[f] = sn[f];
+        sn[f] = (l + 2 <= nl) ? s0[q + 2 * pl + f * F] : 0.f;
+      }
+    }
+    __syncthreads();
+    // ---- B: the faces
+    if (fx_own) {
+      float h = 0.f, idx = 0.f, sl = 0.f;
+      const int a = slot - SX;
+      if (!fx_zero) {
+        h = 0.5f * (sh_c[a] + sh_c[slot]);
+        idx = 1.f / G.dx[qdx1 + lo];
+        sl = 0.5f * G.slope_x[qu1 + lo];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        float g = 0.f;
+        if (!fx_zero) {
+          g = (sh_s[f][slot] - sh_s[f][a]) * idx;
+          if (terrain) g = g - sl * (sh_h[f][a] + sh_h[f][slot]);
+        }
+        sh_fx[f][fr][fc] = h * g;
+      }
+    }
+    if (fy_own) {
+      float h = 0.f, idy = 0.f, sl = 0.f;
+      const int a = slot - 1;
+      if (!fy_zero) {
+        h = 0.5f * (sh_c[a] + sh_c[slot]);
+        idy = 1.f / G.dy[qdy1 + lo];
+        sl = 0.5f * G.slope_y[qu1 + lo];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        float g = 0.f;
+        if (!fy_zero) {
+          g = (sh_s[f][a] - sh_s[f][slot]) * idy;
+          if (terrain) g = g - sl * (sh_h[f][a] + sh_h[f][slot]);
+        }
+        sh_fy[f][fr][fc] = h * g;
+      }
+    }
+    __syncthreads();
+    // ---- C: the divergence of the tile's cells
+    if (cell) {
+      const float ax_w = G.area_x[q], ax_e = G.area_x[q + D.P], ay_n = G.area_y[q], ay_s = G.area_y[q + 1];
+      const float az = G.area_z[q], vol = G.volume[q];
+      float k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f;
+      if (terrain) {  // a layer's slope-weighted face terms (vertical_contravariant_corr)
+        k1 = 0.5f * G.slope_x[q + D.P] * G.ipw[0][q];
+        k2 = 0.5f * G.slope_y[q] * G.ipw[1][q];
+        k3 = 0.5f * G.slope_x[q] * G.ipw[2][q];
+        k4 = 0.5f * G.slope_y[q + 1] * G.ipw[3][q];
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        const float xw = sh_fx[f][fr][fc], xe = sh_fx[f][fr + 1][fc];
+        const float yn = sh_fy[f][fr][fc], ys = sh_fy[f][fr][fc + 1];
+        const float comp_h = xe * ax_e + yn * ay_n - xw * ax_w - ys * ay_s;
+        const float t = terrain ? -(xe * k1 + yn * k2 + xw * k3 + ys * k4) : 0.f;
+        // the interface above the layer: correction (none above the terrain-following layers)
+        // and vertical flux density (none at the top)
+        const float corr = !terrain ? 0.f : (l == nf + 1 ? t : tp[f] + t);
+        const float fw = (vert && l >= 2) ? hv * gz[f] : 0.f;
+        const float U = (corr + fw) * az;
+        if (l >= 2) out[q - pl + f * F] = (P[f] - U) / volp;
+        P[f] = comp_h + U;
+        tp[f] = t;
+      }
+      volp = vol;
+    }
+#pragma unroll
+    for (int f = 0; f < NF; ++f) gz[f] = gn[f];
+  }
+  if (cell) {
+    const long long q = c1 + (long long)(nl - 1) * pl;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) out[q + f * F] = P[f] / volp;
+  }
+}
+
 }  // namespace lg

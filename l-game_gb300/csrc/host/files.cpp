@@ -29,7 +29,7 @@
 
 namespace {
 
-constexpr int kVersion = 3;
+constexpr int kVersion = 4;
 
 struct Header {
   char magic[8];
@@ -73,7 +73,7 @@ size_t diag_n(int f, int ny, int nx, int nl, int ncons) {
     case LGAME_DIAG_MOM_DIFF_TEND_Y: return v;
     case LGAME_DIAG_P_GRAD_ACC_NEG_NL_W: case LGAME_DIAG_P_GRAD_ACC_NEG_L_W: case LGAME_DIAG_POT_VORT_TEND_Z:
     case LGAME_DIAG_V_SQUARED_GRAD_Z: case LGAME_DIAG_TEND_WIND_W: case LGAME_DIAG_MOM_DIFF_TEND_Z: return w;
-    case LGAME_DIAG_TEND_RHO: return s * ncons;
+    case LGAME_DIAG_TEND_RHO: case LGAME_DIAG_MASS_DIFF_TENDENCY: return s * ncons;
     case LGAME_DIAG_ROUGHNESS_LENGTH: case LGAME_DIAG_ROUGHNESS_VELOCITY: case LGAME_DIAG_MONIN_OBUKHOV_LENGTH:
     case LGAME_DIAG_SCALAR_FLUX_RESISTANCE: case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SOIL:
     case LGAME_DIAG_POWER_FLUX_DENSITY_SENS_SEA: case LGAME_DIAG_SST: case LGAME_DIAG_SFC_SW_IN:

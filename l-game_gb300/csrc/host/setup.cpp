@@ -1027,7 +1027,8 @@ extern "C" int lgame_host_setup(const lgame_namelist* nml, lgame_host_model** ou
   const size_t dsz[LGAME_DIAG_NFIELDS] = {nU, nV, nW, nU, nV, nW, nU, nV, nU, nV, nW, nU, nV, nW, nS, nS, nS,
                                           nS * ncons, nS, nU, nV, nW, nS, nS, nS, nU, nV, nW,
                                           nS, n2, n2, n2, n2, n2, n2, n2, n2, n2,
-                                          nS * (size_t)(nml->n_condensed_constituents + 1), nS, n2, n2};
+                                          nS * (size_t)(nml->n_condensed_constituents + 1), nS, n2, n2,
+                                          nS, nS * ncons};
   for (int f = 0; f < LGAME_DIAG_NFIELDS; ++f) m->diag[f].assign(dsz[f], 0.0);
   int rc = grid_setup(*m);
   if (rc == LGAME_OK) rc = bg_setup(*m);

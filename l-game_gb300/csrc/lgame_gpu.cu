@@ -723,9 +723,10 @@ int split_sync_carried(lgame_gpu* c, bool to_split) {
                         {c->tend.w, F.tend.w, n}, {c->hdiss, F.hdiss, n},
                         {c->dbuf.tke, F.tke, n}, {c->dbuf.visc, F.visc, n}, {c->dbuf.mdtx, F.mdtx, n},
                         {c->dbuf.mdty, F.mdty, n}, {c->dbuf.mdtz, F.mdtz, n},
-                        {c->ptr, F.ptr, n * (c->D.nc + 1)}, {c->pth, F.pth, n}};
+                        {c->ptr, F.ptr, n * (c->D.nc + 1)}, {c->pth, F.pth, n},
+                        {c->dbuf.tdh, F.tdh, n}, {c->dbuf.mdt, F.mdt, n * c->D.ncons}};
   for (const Pair& p : pairs) {
-    if (!p.f) continue;  // diffusion off: no FP32 copy
+    if (!p.f || !p.d) continue;  // the part is off: no FP32 copy, or no FP64 array
     const int rc = to_split ? split_convert(p.d, p.f, p.n, c->stream) : split_convert_back(p.f, p.d, p.n, c->stream);
     if (rc != LGAME_OK) return set_err(rc, "conversion of the split-mode diagnostics failed");
   }
@@ -1140,7 +1141,7 @@ extern "C" int lgame_gpu_get_state(lgame_gpu* c, int slot, double* const* f, int
 namespace {
 // fields of one diagnostic: the constituents of the rho tendency, nc+1 phase transition rates
 int diag_nrep(const Dims& D, int f) {
-  if (f == LGAME_DIAG_TEND_RHO) return D.ncons;
+  if (f == LGAME_DIAG_TEND_RHO || f == LGAME_DIAG_MASS_DIFF_TENDENCY) return D.ncons;
   if (f == LGAME_DIAG_PHASE_TRANS_RATES) return D.nc + 1;
   return 1;
 }
@@ -1188,6 +1189,8 @@ double* diag_dev(lgame_gpu* c, int f) {
     case LGAME_DIAG_PHASE_TRANS_HEATING_RATE: return c->pth;
     case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE: return c->sbuf.lat_lake;
     case LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA: return c->sbuf.lat_sea;
+    case LGAME_DIAG_TEMP_DIFF_HEATING: return c->dbuf.tdh;
+    case LGAME_DIAG_MASS_DIFF_TENDENCY: return c->dbuf.mdt;
   }
   return nullptr;
 }

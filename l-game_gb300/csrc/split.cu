@@ -1355,10 +1355,9 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const S
                      &B.zz, &B.vdiv};
     for (float** p : dfl) if ((rc = salloc(s, p, F, bytes))) return fail(rc);
     if ((rc = salloc(s, &B.mdt, F * D.ncons, bytes))) return fail(rc);
-    if ((rc = salloc(s, &B.flx, F * D.ncons, bytes)) || (rc = salloc(s, &B.fly, F * D.ncons, bytes)) ||
-        (rc = salloc(s, &B.flw, F * D.ncons, bytes)))
-      return fail(rc);
+    // (no flux density arrays: the scalar diffusion forms its faces in shared memory)
     B.tke = C.tke; B.visc = C.visc; B.mdtx = C.mdtx; B.mdty = C.mdty; B.mdtz = C.mdtz; B.hd = C.hdiss;
+    C.tdh = B.tdh; C.mdt = B.mdt;
   }
   if (sfc.phase) {  // the phase transitions' rates (graupel's is never written: stays zero) and heating
     if ((rc = salloc(s, &C.ptr, F * (size_t)(D.nc + 1), bytes)) || (rc = salloc(s, &C.pth, F, bytes))) return fail(rc);
@@ -1723,26 +1722,21 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
         if (SF.pbl)
           SL("ks_pbl", (k_pbl<float, float>), sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
         SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
-        // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101); the second substep's
-        // temperature diffusion is the same (same temperature and coefficients)
-        const dim3 ge = sgrd(D.ny + 1, D.nx + 1, D.nl);
-        if (SD.temp_h) {
-          const int vert = SD.temp_v ? 1 : 0;
-          SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB,
-             (const float*)C.temperature, 1, vert, DB.flx, DB.fly, DB.flw);
-          SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.tdh);
-        }
-        if (SD.mass_h) {  // every constituent in one launch each (1 dry, 7 moist)
+        // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101), fluxes and divergence in
+        // one column-marching launch each; the second substep's temperature diffusion is the same
+        // (same temperature and coefficients)
+        const dim3 gd((D.ny + DS_X - 1) / DS_X, (D.nx + DS_Y - 1) / DS_Y);
+        if (SD.temp_h)
+          SL("ks_diff_scalar", (k_diff_scalar_col<1, 1>), gd, dim3(DS_THREADS), D, GF, Mo, DB,
+             (const float*)C.temperature, SD.temp_v ? 1 : 0, DB.tdh);
+        if (SD.mass_h) {  // every constituent in one launch (1 dry, 7 moist)
           const int vert = SD.mass_v ? 1 : 0;
-          if (D.ncons == 7) {
-            SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 7>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho,
-               0, vert, DB.flx, DB.fly, DB.flw);
-            SL("ks_diff_divs", (k_diff_divs<float, 7>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
-          } else {
-            SL("ks_diff_fluxes", (k_diff_fluxes<float, float, float, 1>), ge, B, D, GF, Mo, DB, (const float*)Mo.rho,
-               0, vert, DB.flx, DB.fly, DB.flw);
-            SL("ks_diff_divs", (k_diff_divs<float, 1>), gs, B, D, GF, DB.flx, DB.fly, DB.flw, vert, DB.mdt);
-          }
+          if (D.ncons == 7)
+            SL("ks_diff_scalar", (k_diff_scalar_col<7, 0>), gd, dim3(DS_THREADS), D, GF, Mo, DB, (const float*)Mo.rho,
+               vert, DB.mdt);
+          else
+            SL("ks_diff_scalar", (k_diff_scalar_col<1, 0>), gd, dim3(DS_THREADS), D, GF, Mo, DB, (const float*)Mo.rho,
+               vert, DB.mdt);
         }
       } else if (D.lklemp && D.ndamp > 0) {
         SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);

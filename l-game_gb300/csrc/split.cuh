@@ -33,6 +33,8 @@ struct SplitCarriedF {
   // the carried diagnostics of the diffusion closure (null when horizontal momentum diffusion
   // is off): TKE, viscosity, momentum diffusion accelerations
   float *tke, *visc, *mdtx, *mdty, *mdtz;
+  // temp_diff_heating and mass_diff_tendency (ncons fields), same condition
+  float *tdh, *mdt;
   // the phase transitions' rates (nc+1 fields) and heating rate (null when lphase_trans is off)
   float *ptr, *pth;
   Tend<float> tend;

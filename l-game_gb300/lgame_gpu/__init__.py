@@ -142,7 +142,8 @@ DIAG_FIELDS = ["p_grad_acc_neg_nl_u", "p_grad_acc_neg_nl_v", "p_grad_acc_neg_nl_
                "v_squared", "roughness_length_diag", "roughness_velocity", "monin_obukhov_length",
                "scalar_flux_resistance", "power_flux_density_sens_soil", "power_flux_density_sens_sea", "sst",
                "sfc_sw_in", "sfc_lw_out", "phase_trans_rates", "phase_trans_heating_rate",
-               "power_flux_density_lat_lake", "power_flux_density_lat_sea"]
+               "power_flux_density_lat_lake", "power_flux_density_lat_sea", "temp_diff_heating",
+               "mass_diff_tendency"]
 
 
 class Config(C.Structure):
@@ -336,6 +337,7 @@ def field_shapes(ny: int, nx: int, nl: int, ncons: int, ns: int = 0) -> dict[str
         "sst": p, "sfc_sw_in": p, "sfc_lw_out": p,
         "phase_trans_rates": (ny, nx, nl, 6 if ncons == 7 else 1), "phase_trans_heating_rate": s,
         "power_flux_density_lat_lake": p, "power_flux_density_lat_sea": p,
+        "temp_diff_heating": s, "mass_diff_tendency": (ny, nx, nl, ncons),
     }
 
 

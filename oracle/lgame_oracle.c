@@ -394,6 +394,9 @@ static void diag_ptrs(oracle_ctx* o, double** p, size_t* n) {
   p[LGAME_DIAG_PHASE_TRANS_HEATING_RATE] = o->phase_trans_heating_rate; n[LGAME_DIAG_PHASE_TRANS_HEATING_RATE] = nS;
   p[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE] = o->lat_lake; n[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_LAKE] = n2;
   p[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA] = o->lat_sea; n[LGAME_DIAG_POWER_FLUX_DENSITY_LAT_SEA] = n2;
+  p[LGAME_DIAG_TEMP_DIFF_HEATING] = o->temp_diff_heating; n[LGAME_DIAG_TEMP_DIFF_HEATING] = nS;
+  p[LGAME_DIAG_MASS_DIFF_TENDENCY] = o->mass_diff_tendency;
+  n[LGAME_DIAG_MASS_DIFF_TENDENCY] = nS*(size_t)o->ncons;
 }
 
 int oracle_set_diag(oracle_ctx* o, const double* const* f, int nfields) {

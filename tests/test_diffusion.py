@@ -213,7 +213,7 @@ def test_fp64_diffusion_matches_oracle(name):
     o.close()
     for f in so:
         assert cases.rel_err(sg[f], so[f]) <= 1e-12, (f, cases.rel_err(sg[f], so[f]))
-    for f in DIFF_FIELDS:
+    for f in DIFF_FIELDS + ["temp_diff_heating", "mass_diff_tendency"]:
         assert cases.rel_err(dgpu[f], do[f]) <= 1e-11, (f, cases.rel_err(dgpu[f], do[f]))
     assert do["viscosity"].max() > 0.0 and np.abs(do["mom_diff_tend_x"]).max() > 0.0
 
@@ -248,3 +248,37 @@ def test_split_diffusion_close_to_fp64(name):
     for f in DIFF_FIELDS:
         assert np.all(np.isfinite(da[f])), f
         assert cases.rel_err(da[f], db[f]) <= 2e-3, (f, cases.rel_err(da[f], db[f]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["jet", "hills_nonperiodic", "schaer"])
+def test_split_scalar_diffusion_close_to_fp64(name):
+    """The split step's temperature and mass diffusion (fluxes and divergence formed in one
+    column-marching launch, in FP32) against the FP64 step's two-kernel form, after one step
+    from the same state: temp_diff_heating and each constituent's mass_diff_tendency within
+    SCALAR_DIFF_TOL of the field's largest value."""
+    n = _gpu_case(name)
+    hm = L.HostModel(n)
+    out = {}
+    for prec in (L.PRECISION_FP64, L.PRECISION_SPLIT):
+        cfg = L.config_from_namelist(n)
+        cfg.precision = prec
+        g = L.GpuModel(cfg, hm.grid)
+        g.set_state(0, hm.state)
+        g.set_state(1, hm.state)
+        g.set_diag(hm.diag)
+        g.pchevi(0, 1, 0)
+        out[prec] = g.get_diag()
+        g.close()
+    a, b = out[L.PRECISION_SPLIT], out[L.PRECISION_FP64]
+    errs = {"temp_diff_heating": cases.rel_err(a["temp_diff_heating"], b["temp_diff_heating"])}
+    for jc in range(b["mass_diff_tendency"].shape[-1]):
+        ref = b["mass_diff_tendency"][..., jc]
+        if np.abs(ref).max() > 0.0:
+            errs[f"mass_diff_tendency[{jc}]"] = cases.rel_err(a["mass_diff_tendency"][..., jc], ref)
+    assert np.abs(b["temp_diff_heating"]).max() > 0.0 and np.abs(b["mass_diff_tendency"]).max() > 0.0
+    print(name, errs)
+    assert max(errs.values()) <= SCALAR_DIFF_TOL, errs
+
+
+SCALAR_DIFF_TOL = 1e-3

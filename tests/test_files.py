@@ -45,7 +45,7 @@ def test_snapshot_round_trip_and_header(tmp_path):
             np.testing.assert_array_equal(a[f], b[f], err_msg=f)
     raw = path.read_bytes()
     magic, version, ny, nx, nl, nc, st, ns = struct.unpack_from("<8s5iqi", raw, 0)
-    assert (magic, version, ny, nx, nl, nc, st, ns) == (b"LGAMESNP", 3, hm.ny, hm.nx, hm.nl, hm.ncons, 2, hm.ns)
+    assert (magic, version, ny, nx, nl, nc, st, ns) == (b"LGAMESNP", 4, hm.ny, hm.nx, hm.nl, hm.ncons, 2, hm.ns)
     assert raw[40:64] == bytes(24)
     n_doubles = 2 * sum(v.size for v in s0.values()) + sum(v.size for v in dg.values())
     assert len(raw) == 64 + 8 * n_doubles
