@@ -580,14 +580,33 @@ __global__ void k_diff_divs(Dims D, Grid<T> G, const T* __restrict__ fx, const T
 // viscosity/rho_gas), KIND 1: temperature (c_d_v*viscosity, the vertical one times rho_gas);
 // NF fields of fstride at s0, results into out.
 constexpr int DS_X = 32, DS_Y = 8, DS_THREADS = 32 * (DS_Y + 3);
+constexpr int DS_SLOTS = (DS_X + 2) * (DS_Y + 2);
+// dynamic shared memory of k_diff_scalar_col<NF, .>: the field values of three levels (a ring),
+// the remap halves and coefficients of the slots, and the faces of one level
+__host__ __device__ constexpr size_t diff_scalar_smem(int nf) {
+  return sizeof(float) * ((size_t)3 * nf * DS_SLOTS + (size_t)nf * DS_SLOTS + DS_SLOTS +
+                          (size_t)nf * (DS_Y + 1) * DS_X + (size_t)nf * DS_Y * (DS_X + 1));
+}
+
+// asynchronous 4-byte copy global -> shared (cp.async, no register staging) and its groups
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 template <int NF, int KIND>
 __global__ void __launch_bounds__(DS_THREADS, 2)
 k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float* __restrict__ s0, int vertical,
                   float* __restrict__ out) {
-  constexpr int SX = DS_X + 2, NS = SX * (DS_Y + 2);
-  __shared__ float sh_s[NF][NS], sh_h[NF][NS], sh_c[NS];
-  __shared__ float sh_fx[NF][DS_Y + 1][DS_X], sh_fy[NF][DS_Y][DS_X + 1];
+  constexpr int SX = DS_X + 2, NS = DS_SLOTS;
+  extern __shared__ float4 ds_smem[];
+  float* const ring = reinterpret_cast<float*>(ds_smem);  // [3][NF][NS]: level m at (m-1) % 3
+  float* const sh_h = ring + 3 * NF * NS;                 // [NF][NS]
+  float* const sh_c = sh_h + NF * NS;                     // [NS]
+  float* const sh_fx = sh_c + NS;                         // [NF][DS_Y+1][DS_X]
+  float* const sh_fy = sh_fx + NF * (DS_Y + 1) * DS_X;    // [NF][DS_Y][DS_X+1]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ji0 = blockIdx.x * DS_X + 1, jk0 = blockIdx.y * DS_Y + 1;
   // the slot: role 0 tile, 1 west halo, 2 east halo, 3 north halo, 4 south halo, -1 none
@@ -618,101 +637,132 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
   const long long qdx1 = IX(D, ji >= 1 ? ji : 1, jk == D.nx + 1 ? 1 : (jk >= 1 ? jk : 1), 1);
   const long long qdy1 = IX(D, ji == D.ny + 1 ? 1 : (ji >= 1 ? ji : 1), jk >= 1 ? jk : 1, 1);
   const long long c1 = has ? IX(D, ci, ck, 1) : 0;
-
-  float sv[NF], sn[NF], gz[NF], gn[NF], P[NF], tp[NF];
+  // the field values of level m into the ring (one commit group per level, empty past the bottom)
+  auto fetch = [&](int m) {
+    if (has && m <= nl) {
+      float* dst = ring + ((m - 1) % 3) * NF * NS + slot;
+      const float* src = s0 + c1 + (long long)(m - 1) * pl;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) cp_async4(dst + f * NS, src + f * F);
+    }
+    cp_async_commit();
+  };
+  // the inputs of phase A at one level, loaded a level ahead
+  struct AIn { float w5, w6, dz1, vi, rg, vmol, tke, nsq, lt; };
+  auto load_a = [&](int l) {
+    AIn a{0.f, 0.f, 1.f, 0.f, 1.f, 0.f, 0.f, 0.f, 0.f};
+    if (!has || l > nl) return a;
+    const long long q = c1 + (long long)(l - 1) * pl;
+    if (l > nf) {
+      a.w5 = G.ipw[4][q];
+      if (l < nl || D.freeslip) a.w6 = G.ipw[5][q];
+    }
+    if (l < nl) a.dz1 = G.dz[q + pl];
+    a.vi = B.visc[q];
+    a.rg = S.rho[q + gF];
+    if (vert) { a.vmol = B.vmol[q]; a.tke = B.tke[q]; a.nsq = B.nsq[q]; a.lt = G.layer_thickness[q]; }
+    return a;
+  };
+  float gz[NF], gn[NF], P[NF], tp[NF];
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    sv[f] = has ? s0[c1 + f * F] : 0.f;
-    sn[f] = (has && nl >= 2) ? s0[c1 + pl + f * F] : 0.f;
     gz[f] = 0.f;
     gn[f] = 0.f;
     P[f] = 0.f;
     tp[f] = 0.f;
   }
+  fetch(1);
+  fetch(2);
+  AIn ai = load_a(1);
   float cvp = 0.f, volp = 1.f;
   for (int l = 1; l <= nl; ++l) {
     const long long lo = (long long)(l - 1) * pl, q = c1 + lo;
     const bool terrain = l > nf, g_lo = l < nl;
-    // ---- A: the slot's values, remap halves and coefficient; the cell's vertical coefficient
+    // level l+2 into the slot of level l-1 (free since the last level's faces were formed);
+    // then levels l and l+1 are complete
+    fetch(l + 2);
+    cp_async_wait1();
+    // the metrics of phases B and C, issued first so that they arrive during phase A
+    float bdx = 1.f, bsx = 0.f, bdy = 1.f, bsy = 0.f;
+    if (fx_own && !fx_zero) {
+      bdx = G.dx[qdx1 + lo];
+      if (terrain) bsx = G.slope_x[qu1 + lo];
+    }
+    if (fy_own && !fy_zero) {
+      bdy = G.dy[qdy1 + lo];
+      if (terrain) bsy = G.slope_y[qu1 + lo];
+    }
+    float ax_w = 0.f, ax_e = 0.f, ay_n = 0.f, ay_s = 0.f, az = 0.f, vol = 1.f;
+    float sxe = 0.f, sy = 0.f, sx = 0.f, sys = 0.f, i0 = 0.f, i1 = 0.f, i2 = 0.f, i3 = 0.f;
+    if (cell) {
+      ax_w = G.area_x[q]; ax_e = G.area_x[q + D.P]; ay_n = G.area_y[q]; ay_s = G.area_y[q + 1];
+      az = G.area_z[q]; vol = G.volume[q];
+      if (terrain) {
+        sxe = G.slope_x[q + D.P]; sy = G.slope_y[q]; sx = G.slope_x[q]; sys = G.slope_y[q + 1];
+        i0 = G.ipw[0][q]; i1 = G.ipw[1][q]; i2 = G.ipw[2][q]; i3 = G.ipw[3][q];
+      }
+    }
+    const float* sc = ring + ((l - 1) % 3) * NF * NS;  // level l
+    const float* sd = ring + (l % 3) * NF * NS;        // level l+1
+    // ---- A: the slot's remap halves and coefficient; the cell's vertical coefficient
     float hv = 0.f;
     if (has) {
-      float w5 = 0.f, w6 = 0.f;
-      if (terrain) {
-        w5 = G.ipw[4][q];
-        if (g_lo || D.freeslip) w6 = G.ipw[5][q];
-      }
-      const float idz = g_lo ? 1.f / G.dz[q + pl] : 0.f;
-      const float vi = B.visc[q];
-      sh_c[slot] = KIND == 0 ? vi / S.rho[q + gF] : float(kC_D_V) * vi;
+      const float idz = g_lo ? 1.f / ai.dz1 : 0.f;
+      sh_c[slot] = KIND == 0 ? ai.vi / ai.rg : float(kC_D_V) * ai.vi;
       if (vert) {  // diff_coeff_v at the cell; the interface above takes the mean with the layer above
-        const float t2v = B.vmol[q] + tke2vert<float>(B.tke[q], B.nsq[q], G.layer_thickness[q]);
-        const float cvn = KIND == 0 ? t2v : S.rho[q + gF] * float(kC_D_V) * t2v;
+        const float t2v = ai.vmol + tke2vert<float>(ai.tke, ai.nsq, ai.lt);
+        const float cvn = KIND == 0 ? t2v : ai.rg * float(kC_D_V) * t2v;
         hv = 0.5f * (cvp + cvn);
         cvp = cvn;
       }
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
-        gn[f] = g_lo ? (sv[f] - sn[f]) * idz : 0.f;
-        sh_s[f][slot] = sv[f];
-        if (terrain) sh_h[f][slot] = w5 * gz[f] + w6 * gn[f];
-        sv[f] = sn[f];
-        sn[f] = (l + 2 <= nl) ? s0[q + 2 * pl + f * F] : 0.f;
+        gn[f] = g_lo ? (sc[f * NS + slot] - sd[f * NS + slot]) * idz : 0.f;
+        if (terrain) sh_h[f * NS + slot] = ai.w5 * gz[f] + ai.w6 * gn[f];
       }
     }
+    ai = load_a(l + 1);
     __syncthreads();
     // ---- B: the faces
     if (fx_own) {
-      float h = 0.f, idx = 0.f, sl = 0.f;
       const int a = slot - SX;
-      if (!fx_zero) {
-        h = 0.5f * (sh_c[a] + sh_c[slot]);
-        idx = 1.f / G.dx[qdx1 + lo];
-        sl = 0.5f * G.slope_x[qu1 + lo];
-      }
+      const float h = fx_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float idx = 1.f / bdx, sl = 0.5f * bsx;
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         float g = 0.f;
         if (!fx_zero) {
-          g = (sh_s[f][slot] - sh_s[f][a]) * idx;
-          if (terrain) g = g - sl * (sh_h[f][a] + sh_h[f][slot]);
+          g = (sc[f * NS + slot] - sc[f * NS + a]) * idx;
+          if (terrain) g = g - sl * (sh_h[f * NS + a] + sh_h[f * NS + slot]);
         }
-        sh_fx[f][fr][fc] = h * g;
+        sh_fx[(f * (DS_Y + 1) + fr) * DS_X + fc] = h * g;
       }
     }
     if (fy_own) {
-      float h = 0.f, idy = 0.f, sl = 0.f;
       const int a = slot - 1;
-      if (!fy_zero) {
-        h = 0.5f * (sh_c[a] + sh_c[slot]);
-        idy = 1.f / G.dy[qdy1 + lo];
-        sl = 0.5f * G.slope_y[qu1 + lo];
-      }
+      const float h = fy_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float idy = 1.f / bdy, sl = 0.5f * bsy;
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         float g = 0.f;
         if (!fy_zero) {
-          g = (sh_s[f][a] - sh_s[f][slot]) * idy;
-          if (terrain) g = g - sl * (sh_h[f][a] + sh_h[f][slot]);
+          g = (sc[f * NS + a] - sc[f * NS + slot]) * idy;
+          if (terrain) g = g - sl * (sh_h[f * NS + a] + sh_h[f * NS + slot]);
         }
-        sh_fy[f][fr][fc] = h * g;
+        sh_fy[(f * DS_Y + fr) * (DS_X + 1) + fc] = h * g;
       }
     }
     __syncthreads();
     // ---- C: the divergence of the tile's cells
     if (cell) {
-      const float ax_w = G.area_x[q], ax_e = G.area_x[q + D.P], ay_n = G.area_y[q], ay_s = G.area_y[q + 1];
-      const float az = G.area_z[q], vol = G.volume[q];
-      float k1 = 0.f, k2 = 0.f, k3 = 0.f, k4 = 0.f;
-      if (terrain) {  // a layer's slope-weighted face terms (vertical_contravariant_corr)
-        k1 = 0.5f * G.slope_x[q + D.P] * G.ipw[0][q];
-        k2 = 0.5f * G.slope_y[q] * G.ipw[1][q];
-        k3 = 0.5f * G.slope_x[q] * G.ipw[2][q];
-        k4 = 0.5f * G.slope_y[q + 1] * G.ipw[3][q];
-      }
+      // a layer's slope-weighted face terms (vertical_contravariant_corr)
+      const float k1 = 0.5f * sxe * i0, k2 = 0.5f * sy * i1, k3 = 0.5f * sx * i2, k4 = 0.5f * sys * i3;
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
-        const float xw = sh_fx[f][fr][fc], xe = sh_fx[f][fr + 1][fc];
-        const float yn = sh_fy[f][fr][fc], ys = sh_fy[f][fr][fc + 1];
+        const float* X = sh_fx + f * (DS_Y + 1) * DS_X;
+        const float* Y = sh_fy + f * DS_Y * (DS_X + 1);
+        const float xw = X[fr * DS_X + fc], xe = X[(fr + 1) * DS_X + fc];
+        const float yn = Y[fr * (DS_X + 1) + fc], ys = Y[fr * (DS_X + 1) + fc + 1];
         const float comp_h = xe * ax_e + yn * ay_n - xw * ax_w - ys * ay_s;
         const float t = terrain ? -(xe * k1 + yn * k2 + xw * k3 + ys * k4) : 0.f;
         // the interface above the layer: correction (none above the terrain-following layers)

@@ -1310,6 +1310,12 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const S
     lgame_set_error("split precision: the tracer solver supports at most 128 layers");
     return LGAME_ERR_UNSUPPORTED;
   }
+  if (diff.mom_h &&
+      cudaFuncSetAttribute(k_diff_scalar_col<7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)diff_scalar_smem(7)) != cudaSuccess) {
+    lgame_set_error("split precision: shared memory of the scalar diffusion kernel refused");
+    return LGAME_ERR_CUDA;
+  }
   auto* s = new SplitCtx();
   s->column_fp64 = column_fp64;
   const size_t F = (size_t)D.fstride;
@@ -1727,16 +1733,16 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
         // (same temperature and coefficients)
         const dim3 gd((D.ny + DS_X - 1) / DS_X, (D.nx + DS_Y - 1) / DS_Y);
         if (SD.temp_h)
-          SL("ks_diff_scalar", (k_diff_scalar_col<1, 1>), gd, dim3(DS_THREADS), D, GF, Mo, DB,
-             (const float*)C.temperature, SD.temp_v ? 1 : 0, DB.tdh);
+          SLS("ks_diff_scalar", (k_diff_scalar_col<1, 1>), gd, dim3(DS_THREADS), diff_scalar_smem(1), D, GF, Mo, DB,
+              (const float*)C.temperature, SD.temp_v ? 1 : 0, DB.tdh);
         if (SD.mass_h) {  // every constituent in one launch (1 dry, 7 moist)
           const int vert = SD.mass_v ? 1 : 0;
           if (D.ncons == 7)
-            SL("ks_diff_scalar", (k_diff_scalar_col<7, 0>), gd, dim3(DS_THREADS), D, GF, Mo, DB, (const float*)Mo.rho,
-               vert, DB.mdt);
+            SLS("ks_diff_scalar", (k_diff_scalar_col<7, 0>), gd, dim3(DS_THREADS), diff_scalar_smem(7), D, GF, Mo, DB,
+                (const float*)Mo.rho, vert, DB.mdt);
           else
-            SL("ks_diff_scalar", (k_diff_scalar_col<1, 0>), gd, dim3(DS_THREADS), D, GF, Mo, DB, (const float*)Mo.rho,
-               vert, DB.mdt);
+            SLS("ks_diff_scalar", (k_diff_scalar_col<1, 0>), gd, dim3(DS_THREADS), diff_scalar_smem(1), D, GF, Mo, DB,
+                (const float*)Mo.rho, vert, DB.mdt);
         }
       } else if (D.lklemp && D.ndamp > 0) {
         SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
