@@ -5,7 +5,8 @@
 //   T = double, V = double: the FP64 step (lgame_gpu.cu, -fmad=false), every expression in the
 //                           reference's operand order;
 //   T = float,  V = float:  the split step (split.cu), the same expressions in FP32 on the FP32
-//                           metric copies and the FP32 mirror of the state.
+//                           metric copies and the FP32 mirror of the state; its temperature and
+//                           mass diffusion is the fused kernel k_diff_scalar_col (FP32 only).
 //
 // Reference routines: update_n_squared, tke2hor/vert_diff_coeff, hor_viscosity(_smag/_tke),
 // hor_diff_coeff_postprocessing, vert_vert_mom_viscosity, scalar_diff_coeffs
@@ -405,6 +406,7 @@ __device__ __forceinline__ T diff_coeff_v(const Dims& D, const Grid<T>& G, const
   return rg * c_g_v * t2v;
 }
 
+// (the FP64 step's form of the scalar diffusion; the split step runs k_diff_scalar_col below)
 // diffusive flux densities of nf scalar fields s0 + f*fstride (f = 0..nf-1): grad_hor with
 // grad_vert of the field as its vertical component (mo_gradient_operators.F90:65-130; the
 // vertical gradient formed inline, zero at levels 1 and nl+1), then scalar_times_vector_h/_v
@@ -558,14 +560,15 @@ __global__ void k_diff_divs(Dims D, Grid<T> G, const T* __restrict__ fx, const T
 }
 
 // ---- 7b. temperature and mass diffusion of the split step, fluxes and divergence fused ----------
-// k_diff_fluxes followed by k_diff_divs in FP32, in one launch that marches down the levels, so
-// the flux densities never reach HBM.  A block owns a tile of DS_X rows (ji, a lane each) by
-// DS_Y columns (jk, a warp each) and walks it from the top layer to the bottom; three more warps
-// hold the tile's halo: the columns jk0-1 and jk0+DS_Y, and the rows ji0-1 and ji0+DS_X (a lane
-// per column).  Each level takes three phases, separated by barriers:
-//   A  every slot (tile or halo cell, the periodic wrap applied) puts into shared memory its
-//      field values, its half of the terrain remap of the vertical gradients,
-//      hc = ipw5*gz(l) + ipw6*gz(l+1), and its horizontal coefficient;
+// k_diff_fluxes followed by k_diff_divs, for the NM mass fields and (HT) the temperature
+// together, in FP32, in one launch that marches down the levels: the flux densities never reach
+// HBM and the metrics and coefficients are read once for all fields.  A block owns a tile of
+// DS_X rows (ji, a lane each) by DS_Y columns (jk, a warp each) and walks it from the top layer to
+// the bottom; three more warps hold the tile's halo: the columns jk0-1 and jk0+DS_Y, and the rows
+// ji0-1 and ji0+DS_X (a lane per column).  Each level takes three phases, separated by barriers:
+//   A  every slot (tile or halo cell, the periodic wrap applied) puts into shared memory its half
+//      of the terrain remap of each field's vertical gradients, hc = ipw5*gz(l) + ipw6*gz(l+1),
+//      and its horizontal coefficients;
 //   B  each face is formed once, by the slot east (u point) or south (v point) of it:
 //      h*((s_b - s_a)/dx - slope*0.5*(hc_a + hc_b)) with h = 0.5*(coef_a + coef_b);
 //   C  each tile cell adds its four faces and the contravariant corrections of its two
@@ -573,19 +576,24 @@ __global__ void k_diff_divs(Dims D, Grid<T> G, const T* __restrict__ fx, const T
 //      the layers above and below it; a layer's term is formed once and carried to the next
 //      level, and so is the divergence itself, which is finished one level later, when its
 //      lower interface's correction and vertical flux are known.
-// The reference's sums (grad_hor's remap, vertical_contravariant_corr, div_h plus
+// The field values arrive by cp.async into a ring of three levels (issued two levels ahead), so
+// they take no registers; the metrics of phases B and C are issued at the top of the level and
+// those of phase A a level ahead.  A column's vertical gradients and layer terms stay in shared
+// memory.  The reference's sums (grad_hor's remap, vertical_contravariant_corr, div_h plus
 // add_vertical_div: mo_averaging.F90:16-136, mo_divergence_operators.F90:16-68, 149-186) are
-// regrouped, so the FP32 results differ from the two-kernel form in the last bits; the FP64
-// step keeps the two kernels and the reference's order.  KIND 0: mass (coefficient
-// viscosity/rho_gas), KIND 1: temperature (c_d_v*viscosity, the vertical one times rho_gas);
-// NF fields of fstride at s0, results into out.
+// regrouped, so the FP32 results differ from the two-kernel form in the last bits; the FP64 step
+// keeps the two kernels and the reference's order.  Coefficients (scalar_diff_coeffs): mass
+// viscosity/rho_gas and, vertically, the TKE one; temperature c_d_v times both, the vertical one
+// also times rho_gas.
 constexpr int DS_X = 32, DS_Y = 8, DS_THREADS = 32 * (DS_Y + 3);
-constexpr int DS_SLOTS = (DS_X + 2) * (DS_Y + 2);
-// dynamic shared memory of k_diff_scalar_col<NF, .>: the field values of three levels (a ring),
-// the remap halves and coefficients of the slots, and the faces of one level
+constexpr int DS_SLOTS = (DS_X + 2) * (DS_Y + 2), DS_CELLS = DS_X * DS_Y;
+// dynamic shared memory of k_diff_scalar_col for nf fields in all: the field values of three
+// levels, the remap halves, the two coefficients, the vertical gradients of two levels and the
+// carried layer terms of the slots, and the faces of one level
 __host__ __device__ constexpr size_t diff_scalar_smem(int nf) {
-  return sizeof(float) * ((size_t)3 * nf * DS_SLOTS + (size_t)nf * DS_SLOTS + DS_SLOTS +
-                          (size_t)nf * (DS_Y + 1) * DS_X + (size_t)nf * DS_Y * (DS_X + 1));
+  return sizeof(float) * ((size_t)3 * nf * DS_SLOTS + (size_t)nf * DS_SLOTS + 2 * DS_SLOTS +
+                          (size_t)2 * nf * DS_SLOTS + (size_t)nf * DS_CELLS + (size_t)nf * (DS_Y + 1) * DS_X +
+                          (size_t)nf * DS_Y * (DS_X + 1));
 }
 
 // asynchronous 4-byte copy global -> shared (cp.async, no register staging) and its groups
@@ -596,16 +604,20 @@ __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-template <int NF, int KIND>
+// NM mass fields at sm (fstride apart; results into out_m, vertical part with vert_m) and, with
+// HT, the temperature at st (into out_t, vertical part with vert_t)
+template <int NM, int HT>
 __global__ void __launch_bounds__(DS_THREADS, 2)
-k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float* __restrict__ s0, int vertical,
-                  float* __restrict__ out) {
-  constexpr int SX = DS_X + 2, NS = DS_SLOTS;
+k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float* __restrict__ sm, int vert_m,
+                  float* __restrict__ out_m, const float* __restrict__ st, int vert_t, float* __restrict__ out_t) {
+  constexpr int NF = NM + HT, SX = DS_X + 2, NS = DS_SLOTS;
   extern __shared__ float4 ds_smem[];
   float* const ring = reinterpret_cast<float*>(ds_smem);  // [3][NF][NS]: level m at (m-1) % 3
   float* const sh_h = ring + 3 * NF * NS;                 // [NF][NS]
-  float* const sh_c = sh_h + NF * NS;                     // [NS]
-  float* const sh_fx = sh_c + NS;                         // [NF][DS_Y+1][DS_X]
+  float* const sh_c = sh_h + NF * NS;                     // [2][NS]: mass, temperature
+  float* const sh_g = sh_c + 2 * NS;                      // [2][NF][NS]: gz(m) at m % 2
+  float* const sh_t = sh_g + 2 * NF * NS;                 // [NF][DS_CELLS]
+  float* const sh_fx = sh_t + NF * DS_CELLS;              // [NF][DS_Y+1][DS_X]
   float* const sh_fy = sh_fx + NF * (DS_Y + 1) * DS_X;    // [NF][DS_Y][DS_X+1]
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ji0 = blockIdx.x * DS_X + 1, jk0 = blockIdx.y * DS_Y + 1;
@@ -628,8 +640,9 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
   const bool fx_zero = !D.periodic && (jk == 1 || jk == D.nx + 1);
   const bool fy_zero = !D.periodic && (ji == 1 || ji == D.ny + 1);
   const bool cell = role == 0 && ji <= D.ny && jk <= D.nx;
-  const bool vert = vertical != 0 && cell;
+  const bool vm = NM > 0 && vert_m != 0 && cell, vt = HT > 0 && vert_t != 0 && cell;
   const int fr = jk - jk0, fc = ji - ji0;  // the slot's u point in sh_fx, v point in sh_fy
+  const int tc = warp * DS_X + lane;       // the tile cell's index in sh_t
   const long long F = D.fstride, pl = D.plane, gF = (long long)(D.g - 1) * D.fstride;
   const int nl = D.nl, nf = D.nf;
   // u and v points of the slot at level 1 (dx, dy at the wrapped cell, slopes at the point itself)
@@ -637,13 +650,14 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
   const long long qdx1 = IX(D, ji >= 1 ? ji : 1, jk == D.nx + 1 ? 1 : (jk >= 1 ? jk : 1), 1);
   const long long qdy1 = IX(D, ji == D.ny + 1 ? 1 : (ji >= 1 ? ji : 1), jk >= 1 ? jk : 1, 1);
   const long long c1 = has ? IX(D, ci, ck, 1) : 0;
+  auto field = [&](int f) { return f < NM ? sm + (long long)f * F : st; };
   // the field values of level m into the ring (one commit group per level, empty past the bottom)
   auto fetch = [&](int m) {
     if (has && m <= nl) {
       float* dst = ring + ((m - 1) % 3) * NF * NS + slot;
-      const float* src = s0 + c1 + (long long)(m - 1) * pl;
+      const long long o = c1 + (long long)(m - 1) * pl;
 #pragma unroll
-      for (int f = 0; f < NF; ++f) cp_async4(dst + f * NS, src + f * F);
+      for (int f = 0; f < NF; ++f) cp_async4(dst + f * NS, field(f) + o);
     }
     cp_async_commit();
   };
@@ -660,21 +674,19 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
     if (l < nl) a.dz1 = G.dz[q + pl];
     a.vi = B.visc[q];
     a.rg = S.rho[q + gF];
-    if (vert) { a.vmol = B.vmol[q]; a.tke = B.tke[q]; a.nsq = B.nsq[q]; a.lt = G.layer_thickness[q]; }
+    if (vm || vt) { a.vmol = B.vmol[q]; a.tke = B.tke[q]; a.nsq = B.nsq[q]; a.lt = G.layer_thickness[q]; }
     return a;
   };
-  float gz[NF], gn[NF], P[NF], tp[NF];
+  float P[NF];
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
-    gz[f] = 0.f;
-    gn[f] = 0.f;
     P[f] = 0.f;
-    tp[f] = 0.f;
+    if (has) sh_g[(1 & 1) * NF * NS + f * NS + slot] = 0.f;  // no gradient above the top layer
   }
   fetch(1);
   fetch(2);
   AIn ai = load_a(1);
-  float cvp = 0.f, volp = 1.f;
+  float cvp0 = 0.f, cvp1 = 0.f, volp = 1.f;
   for (int l = 1; l <= nl; ++l) {
     const long long lo = (long long)(l - 1) * pl, q = c1 + lo;
     const bool terrain = l > nf, g_lo = l < nl;
@@ -704,21 +716,27 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
     }
     const float* sc = ring + ((l - 1) % 3) * NF * NS;  // level l
     const float* sd = ring + (l % 3) * NF * NS;        // level l+1
-    // ---- A: the slot's remap halves and coefficient; the cell's vertical coefficient
-    float hv = 0.f;
+    float* const gzl = sh_g + (l & 1) * NF * NS;       // gz(l)
+    float* const gzn = sh_g + ((l + 1) & 1) * NF * NS;  // gz(l+1)
+    // ---- A: the slot's remap halves and coefficients; the cell's vertical coefficients
+    float hv0 = 0.f, hv1 = 0.f;
     if (has) {
       const float idz = g_lo ? 1.f / ai.dz1 : 0.f;
-      sh_c[slot] = KIND == 0 ? ai.vi / ai.rg : float(kC_D_V) * ai.vi;
-      if (vert) {  // diff_coeff_v at the cell; the interface above takes the mean with the layer above
+      if (NM > 0) sh_c[slot] = ai.vi / ai.rg;
+      if (HT > 0) sh_c[NS + slot] = float(kC_D_V) * ai.vi;
+      if (vm || vt) {  // diff_coeff_v at the cell; the interface above takes the mean with the layer above
         const float t2v = ai.vmol + tke2vert<float>(ai.tke, ai.nsq, ai.lt);
-        const float cvn = KIND == 0 ? t2v : ai.rg * float(kC_D_V) * t2v;
-        hv = 0.5f * (cvp + cvn);
-        cvp = cvn;
+        const float cv1 = ai.rg * float(kC_D_V) * t2v;
+        hv0 = 0.5f * (cvp0 + t2v);
+        hv1 = 0.5f * (cvp1 + cv1);
+        cvp0 = t2v;
+        cvp1 = cv1;
       }
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
-        gn[f] = g_lo ? (sc[f * NS + slot] - sd[f * NS + slot]) * idz : 0.f;
-        if (terrain) sh_h[f * NS + slot] = ai.w5 * gz[f] + ai.w6 * gn[f];
+        const float gn = g_lo ? (sc[f * NS + slot] - sd[f * NS + slot]) * idz : 0.f;
+        if (terrain) sh_h[f * NS + slot] = ai.w5 * gzl[f * NS + slot] + ai.w6 * gn;
+        gzn[f * NS + slot] = gn;
       }
     }
     ai = load_a(l + 1);
@@ -726,7 +744,8 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
     // ---- B: the faces
     if (fx_own) {
       const int a = slot - SX;
-      const float h = fx_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float h0 = fx_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float h1 = fx_zero ? 0.f : 0.5f * (sh_c[NS + a] + sh_c[NS + slot]);
       const float idx = 1.f / bdx, sl = 0.5f * bsx;
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
@@ -735,12 +754,13 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
           g = (sc[f * NS + slot] - sc[f * NS + a]) * idx;
           if (terrain) g = g - sl * (sh_h[f * NS + a] + sh_h[f * NS + slot]);
         }
-        sh_fx[(f * (DS_Y + 1) + fr) * DS_X + fc] = h * g;
+        sh_fx[(f * (DS_Y + 1) + fr) * DS_X + fc] = (f < NM ? h0 : h1) * g;
       }
     }
     if (fy_own) {
       const int a = slot - 1;
-      const float h = fy_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float h0 = fy_zero ? 0.f : 0.5f * (sh_c[a] + sh_c[slot]);
+      const float h1 = fy_zero ? 0.f : 0.5f * (sh_c[NS + a] + sh_c[NS + slot]);
       const float idy = 1.f / bdy, sl = 0.5f * bsy;
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
@@ -749,7 +769,7 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
           g = (sc[f * NS + a] - sc[f * NS + slot]) * idy;
           if (terrain) g = g - sl * (sh_h[f * NS + a] + sh_h[f * NS + slot]);
         }
-        sh_fy[(f * DS_Y + fr) * (DS_X + 1) + fc] = h * g;
+        sh_fy[(f * DS_Y + fr) * (DS_X + 1) + fc] = (f < NM ? h0 : h1) * g;
       }
     }
     __syncthreads();
@@ -767,22 +787,23 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
         const float t = terrain ? -(xe * k1 + yn * k2 + xw * k3 + ys * k4) : 0.f;
         // the interface above the layer: correction (none above the terrain-following layers)
         // and vertical flux density (none at the top)
-        const float corr = !terrain ? 0.f : (l == nf + 1 ? t : tp[f] + t);
-        const float fw = (vert && l >= 2) ? hv * gz[f] : 0.f;
+        float* const tpf = sh_t + f * DS_CELLS + tc;
+        const float corr = !terrain ? 0.f : (l == nf + 1 ? t : *tpf + t);
+        const bool vk = f < NM ? vm : vt;
+        const float fw = (vk && l >= 2) ? (f < NM ? hv0 : hv1) * gzl[f * NS + slot] : 0.f;
         const float U = (corr + fw) * az;
-        if (l >= 2) out[q - pl + f * F] = (P[f] - U) / volp;
+        float* const o = f < NM ? out_m + (long long)f * F : out_t;
+        if (l >= 2) o[q - pl] = (P[f] - U) / volp;
         P[f] = comp_h + U;
-        tp[f] = t;
+        *tpf = t;
       }
       volp = vol;
     }
-#pragma unroll
-    for (int f = 0; f < NF; ++f) gz[f] = gn[f];
   }
   if (cell) {
     const long long q = c1 + (long long)(nl - 1) * pl;
 #pragma unroll
-    for (int f = 0; f < NF; ++f) out[q + f * F] = P[f] / volp;
+    for (int f = 0; f < NF; ++f) (f < NM ? out_m + (long long)f * F : out_t)[q] = P[f] / volp;
   }
 }
 

@@ -926,10 +926,14 @@ extern "C" int lgame_gpu_create(const lgame_config* cfg, lgame_gpu** out) {
     c->diff_temp_h = cfg->ltemp_diff_h; c->diff_temp_v = cfg->ltemp_diff_v;
     c->diff_mass_h = cfg->lmass_diff_h; c->diff_mass_v = cfg->lmass_diff_v;
     if (c->diff_mom_h) {
-      double** work[] = {&B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.zz, &B.vdiv};
-      for (double** p : work) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
+      // temp_diff_heating and mass_diff_tendency in both modes (the C ABI's diagnostics), the work
+      // arrays for the FP64 step only (the split step keeps FP32 ones)
       if (c->diff_temp_h && (rc = dalloc(c, &B.tdh, F)) != LGAME_OK) return fail(rc);
       if (c->diff_mass_h && (rc = dalloc(c, &B.mdt, F * D.ncons)) != LGAME_OK) return fail(rc);
+    }
+    if (c->diff_mom_h && cfg->precision == LGAME_PRECISION_FP64) {
+      double** work[] = {&B.tke_new, &B.vmol, &B.nsq, &B.vz, &B.zz, &B.vdiv};
+      for (double** p : work) if ((rc = dalloc(c, p, F)) != LGAME_OK) return fail(rc);
       if (c->diff_temp_h || c->diff_mass_h) {
         const size_t nf = c->diff_mass_h ? (size_t)D.ncons : 1;
         if ((rc = dalloc(c, &B.flx, F * nf)) || (rc = dalloc(c, &B.fly, F * nf)) || (rc = dalloc(c, &B.flw, F * nf)))

@@ -1311,8 +1311,10 @@ int split_create(const Dims& D, bool column_fp64, const SplitDiff& diff, const S
     return LGAME_ERR_UNSUPPORTED;
   }
   if (diff.mom_h &&
-      cudaFuncSetAttribute(k_diff_scalar_col<7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)diff_scalar_smem(7)) != cudaSuccess) {
+      (cudaFuncSetAttribute(k_diff_scalar_col<7, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)diff_scalar_smem(8)) != cudaSuccess ||
+       cudaFuncSetAttribute(k_diff_scalar_col<7, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                            (int)diff_scalar_smem(7)) != cudaSuccess)) {
     lgame_set_error("split precision: shared memory of the scalar diffusion kernel refused");
     return LGAME_ERR_CUDA;
   }
@@ -1728,21 +1730,30 @@ int split_step(SplitCtx* s, const Dims& D, const Grid<double>& G, const State& S
         if (SF.pbl)
           SL("ks_pbl", (k_pbl<float, float>), sgrd(D.ny, D.nx, 1), B, D, G, So, s->vsq, SF.buf, SF.par, DB.mdtx, DB.mdty);
         SL("ks_diss_rate", (k_diss_rate<float, float>), gs, B, D, GF, Mo, DB, GF.damp, s->GX.kdamp_f);
-        // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101), fluxes and divergence in
-        // one column-marching launch each; the second substep's temperature diffusion is the same
-        // (same temperature and coefficients)
+        // temperature and mass diffusion (mo_scalar_tend_expl.F90:60-101): fluxes and divergence of
+        // every constituent and the temperature in one column-marching launch; the second
+        // substep's temperature diffusion is the same (same temperature and coefficients)
         const dim3 gd((D.ny + DS_X - 1) / DS_X, (D.nx + DS_Y - 1) / DS_Y);
-        if (SD.temp_h)
-          SLS("ks_diff_scalar", (k_diff_scalar_col<1, 1>), gd, dim3(DS_THREADS), diff_scalar_smem(1), D, GF, Mo, DB,
-              (const float*)C.temperature, SD.temp_v ? 1 : 0, DB.tdh);
-        if (SD.mass_h) {  // every constituent in one launch (1 dry, 7 moist)
-          const int vert = SD.mass_v ? 1 : 0;
-          if (D.ncons == 7)
-            SLS("ks_diff_scalar", (k_diff_scalar_col<7, 0>), gd, dim3(DS_THREADS), diff_scalar_smem(7), D, GF, Mo, DB,
-                (const float*)Mo.rho, vert, DB.mdt);
+        if (SD.temp_h || SD.mass_h) {
+          const float* tm = (const float*)C.temperature;
+          const float* rm = (const float*)Mo.rho;
+          const int vm = SD.mass_v ? 1 : 0, vt = SD.temp_v ? 1 : 0;
+          const dim3 bd(DS_THREADS);
+          if (SD.temp_h && SD.mass_h && D.ncons == 7)
+            SLS("ks_diff_scalar", (k_diff_scalar_col<7, 1>), gd, bd, diff_scalar_smem(8), D, GF, Mo, DB, rm, vm, DB.mdt,
+                tm, vt, DB.tdh);
+          else if (SD.temp_h && SD.mass_h)
+            SLS("ks_diff_scalar", (k_diff_scalar_col<1, 1>), gd, bd, diff_scalar_smem(2), D, GF, Mo, DB, rm, vm, DB.mdt,
+                tm, vt, DB.tdh);
+          else if (SD.temp_h)
+            SLS("ks_diff_scalar", (k_diff_scalar_col<0, 1>), gd, bd, diff_scalar_smem(1), D, GF, Mo, DB, rm, 0,
+                (float*)nullptr, tm, vt, DB.tdh);
+          else if (D.ncons == 7)
+            SLS("ks_diff_scalar", (k_diff_scalar_col<7, 0>), gd, bd, diff_scalar_smem(7), D, GF, Mo, DB, rm, vm, DB.mdt,
+                tm, 0, (float*)nullptr);
           else
-            SLS("ks_diff_scalar", (k_diff_scalar_col<1, 0>), gd, dim3(DS_THREADS), diff_scalar_smem(1), D, GF, Mo, DB,
-                (const float*)Mo.rho, vert, DB.mdt);
+            SLS("ks_diff_scalar", (k_diff_scalar_col<1, 0>), gd, bd, diff_scalar_smem(1), D, GF, Mo, DB, rm, vm, DB.mdt,
+                tm, 0, (float*)nullptr);
         }
       } else if (D.lklemp && D.ndamp > 0) {
         SL("ks_heating_diss", ks_heating_diss, sgrd(D.ny, D.nx, std::min(D.nl, D.ndamp)), B, D, GF, s->GX, Mo, C.hdiss);
