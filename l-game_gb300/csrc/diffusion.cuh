@@ -681,7 +681,7 @@ k_diff_scalar_col(Dims D, Grid<float> G, StateF S, DiffBuf<float> B, const float
 #pragma unroll
   for (int f = 0; f < NF; ++f) {
     P[f] = 0.f;
-    if (has) sh_g[(1 & 1) * NF * NS + f * NS + slot] = 0.f;  // no gradient above the top layer
+    if (has) sh_g[NF * NS + f * NS + slot] = 0.f;  // gz(1) (buffer 1 % 2): no gradient above the top layer
   }
   fetch(1);
   fetch(2);

@@ -147,7 +147,9 @@ def test_oracle_scalar_diffusion_is_conservative(key):
     for k in range(3):
         o.pchevi(k % 2, (k + 1) % 2, k)
     mdt, tdh = o.scalar_diffusion()
+    dg = o.get_diag()  # the same arrays as the C ABI's diagnostics
     o.close()
+    assert np.array_equal(dg["temp_diff_heating"], tdh) and np.array_equal(dg["mass_diff_tendency"], mdt)
     vol = hm.grid["volume"]
     fields = [tdh] + [mdt[..., jc] for jc in range(mdt.shape[3])]
     nc = 5 if n.lmoist else 0
