@@ -178,6 +178,89 @@ def test_oracle_diffusion_changes_the_step():
     assert np.abs(d_on["mom_diff_tend_x"]).max() > 0.0
 
 
+def fused_scalar_diffusion(grid, s, coef, nf, periodic, freeslip):
+    """The split step's column-marching form of the horizontal scalar diffusion
+    (k_diff_scalar_col in csrc/diffusion.cuh), restated in FP64 numpy as the kernel regroups it:
+    per level each cell's half of the terrain remap, hc = ipw5*gz(l) + ipw6*gz(l+1); each face
+    once, h*((s_b - s_a)/dx - slope*0.5*(hc_a + hc_b)); each cell's divergence finished a level
+    later, the interface correction being the sum of the layer terms above and below it.
+    s, coef: (ny, nx, nl) at scalar points; returns the divergence (ny, nx, nl)."""
+    ny, nx, nl = s.shape
+    ipw = grid["inner_product_weights"]
+    sx, sy, dx, dy = grid["slope_x"], grid["slope_y"], grid["dx"], grid["dy"]
+    ax, ay, az, vol, dz = grid["area_x"], grid["area_y"], grid["area_z"], grid["volume"], grid["dz"]
+    gz = np.zeros((ny, nx, nl + 1))  # vertical gradients at w levels, zero at the top and bottom
+    gz[:, :, 1:nl] = (s[:, :, :-1] - s[:, :, 1:]) / dz[:, :, 1:nl]
+    # cells either side of the u points 1..nx+1 (x) and v points 1..ny+1 (y), periodic wrap
+    ax_w, ax_e = np.r_[nx - 1, np.arange(nx)], np.r_[np.arange(nx), 0]
+    ay_n, ay_s = np.r_[ny - 1, np.arange(ny)], np.r_[np.arange(ny), 0]
+    out = np.zeros_like(s)
+    P = tp = volp = None
+    for l in range(nl):
+        terrain = l + 1 > nf
+        hc = np.zeros((ny, nx))
+        if terrain:
+            w6 = ipw[5][:, :, l] if (l + 1 < nl or freeslip) else 0.0
+            hc = ipw[4][:, :, l] * gz[:, :, l] + w6 * gz[:, :, l + 1]
+        sl, c = s[:, :, l], coef[:, :, l]
+        g = (sl[:, ax_e] - sl[:, ax_w]) / dx[:, ax_e, l]
+        if terrain:
+            g = g - 0.5 * sx[:, :, l] * (hc[:, ax_w] + hc[:, ax_e])
+        fx = 0.5 * (c[:, ax_w] + c[:, ax_e]) * g
+        g = (sl[ay_n, :] - sl[ay_s, :]) / dy[ay_s, :, l]
+        if terrain:
+            g = g - 0.5 * sy[:, :, l] * (hc[ay_n, :] + hc[ay_s, :])
+        fy = 0.5 * (c[ay_n, :] + c[ay_s, :]) * g
+        if not periodic:
+            fx[:, [0, nx]] = 0.0
+            fy[[0, ny], :] = 0.0
+        xw, xe, yn, ys = fx[:, :-1], fx[:, 1:], fy[:-1, :], fy[1:, :]
+        comp_h = xe * ax[:, 1:, l] + yn * ay[:-1, :, l] - xw * ax[:, :-1, l] - ys * ay[1:, :, l]
+        t = np.zeros((ny, nx))
+        if terrain:
+            t = -(xe * 0.5 * sx[:, 1:, l] * ipw[0][:, :, l] + yn * 0.5 * sy[:-1, :, l] * ipw[1][:, :, l]
+                  + xw * 0.5 * sx[:, :-1, l] * ipw[2][:, :, l] + ys * 0.5 * sy[1:, :, l] * ipw[3][:, :, l])
+        corr = 0.0 if not terrain else (t if l + 1 == nf + 1 else tp + t)
+        U = corr * az[:, :, l]
+        if l >= 1:
+            out[:, :, l - 1] = (P - U) / volp
+        P, tp, volp = comp_h + U, t, vol[:, :, l]
+    out[:, :, nl - 1] = P / volp
+    return out
+
+
+@pytest.mark.parametrize("key", ["jet", "hills_nonperiodic"])
+def test_fused_scalar_diffusion_algorithm_matches_oracle(key):
+    """The regrouped sums of the split step's fused scalar diffusion kernel, restated in FP64
+    (fused_scalar_diffusion), against the oracle's two-pass restatement of the reference
+    (fluxes, then div_h with vertical_contravariant_corr): temp_diff_heating and every
+    constituent's mass_diff_tendency after one step, horizontal diffusion only, within 1e-11 of
+    the field's largest value: the regrouping pinned at FP64 precision, far below the bar of the
+    GPU kernel's FP32 comparison (leaving out the contravariant correction moves the result by
+    0.1-0.2 of its largest value here)."""
+    n = diff_case(key, ltemp_diff_v=False, lmass_diff_v=False)
+    hm, cfg, o = _oracle(n)
+    state = hm.copy_state()
+    o.pchevi(0, 1, 0)
+    mdt, tdh = o.scalar_diffusion()
+    dg = o.get_diag()
+    o.close()
+    g = hm.grid
+    nf = n.n_layers - n.n_oro_layers
+    rho = state["rho"]
+    rho_g = rho[..., 5] if rho.shape[3] == 7 else rho[..., 0]
+    visc = dg["viscosity"]
+    args = (nf, bool(n.lperiodic), bool(n.lfreeslip))
+    t_ref = fused_scalar_diffusion(g, dg["temperature"], 717.942189 * visc, *args)
+    assert np.abs(tdh).max() > 0.0
+    assert cases.rel_err(t_ref, tdh) <= 1e-11, cases.rel_err(t_ref, tdh)
+    for jc in range(rho.shape[3]):
+        if np.abs(mdt[..., jc]).max() == 0.0:
+            continue
+        m_ref = fused_scalar_diffusion(g, rho[..., jc], visc / rho_g, *args)
+        assert cases.rel_err(m_ref, mdt[..., jc]) <= 1e-11, (jc, cases.rel_err(m_ref, mdt[..., jc]))
+
+
 # ---- GPU: the FP64 step against the oracle ------------------------------------------------------
 
 GPU_CASES = {
