@@ -6,10 +6,14 @@ mo_scalar_tend_expl.F90:60-101).
 CPU: the oracle's restatement against a second, vectorised numpy restatement on a flat plane
 (no terrain terms): the viscosity and the vertical diffusion of w after the first step (the
 TKE is still zero then); the gas mass is conserved with mass diffusion on in a periodic
-domain; the namelist defaults of &diff are the reference's (all diffusion on, smag, tke).
+domain; the namelist defaults of &diff are the reference's (all diffusion on, smag, tke); the
+split step's fused scalar diffusion, its regrouped sums restated in FP64 numpy, against the
+oracle's two-pass form.
 GPU: the FP64 step against the oracle, state and the carried diffusion diagnostics, on
-periodic and non-periodic cases with orography, Smagorinsky and TKE horizontal schemes, and
-with horizontal momentum diffusion alone.
+periodic and non-periodic cases with orography, Smagorinsky and TKE horizontal schemes, with
+horizontal momentum diffusion alone, and on a grid whose sizes are multiples of the fused
+kernel's tile; the split step against the FP64 step, after ten steps and, for the temperature
+and mass diffusion, after one.
 """
 import numpy as np
 import pytest
@@ -269,12 +273,15 @@ GPU_CASES = {
     "jet_mom_h_only": dict(lmom_diff_v=False, ltemp_diff_h=False, lmass_diff_h=False),
     "hills_nonperiodic": {},
     "schaer": {},
+    # ny a multiple of 32 and nx of 8: the split step's fused scalar diffusion forms the periodic
+    # wrap faces ny+1 and nx+1 in its halo lanes and warps rather than inside its tiles
+    "jet_tiles": dict(ny=32, nx=24),
 }
 
 
 def _gpu_case(name):
     kw = dict(GPU_CASES[name])
-    key = name.split("_tke")[0].split("_mom_h_only")[0]
+    key = name.split("_tke")[0].split("_mom_h_only")[0].split("_tiles")[0]
     return diff_case(key, **kw)
 
 
@@ -336,7 +343,7 @@ def test_split_diffusion_close_to_fp64(name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", ["jet", "hills_nonperiodic", "schaer"])
+@pytest.mark.parametrize("name", ["jet", "hills_nonperiodic", "schaer", "jet_tiles"])
 def test_split_scalar_diffusion_close_to_fp64(name):
     """The split step's temperature and mass diffusion (fluxes and divergence formed in one
     column-marching launch, in FP32) against the FP64 step's two-kernel form, after one step
