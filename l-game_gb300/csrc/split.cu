@@ -961,24 +961,6 @@ __global__ void __launch_bounds__(128, 6) ks_column_ver(Dims D, Grid<double> G, 
   }
 }
 
-// v_fall_liquid, mo_derived.F90:218-263, in FP32
-__device__ __forceinline__ float vfall_liquid_f(const Dims& D, const Grid<float>& GF, const float* rho_g,
-                                                const float* Tm, float radius, int ji, int jk, int jl) {
-  float g;
-  if (jl == 1) g = GF.gm[IX(D, ji, jk, jl + 1)];
-  else if (jl == D.nl) g = GF.gm[IX(D, ji, jk, jl)];
-  else g = GF.ipw[4][IX(D, ji, jk, jl)] * GF.gm[IX(D, ji, jk, jl)] + GF.ipw[5][IX(D, ji, jk, jl)] * GF.gm[IX(D, ji, jk, jl + 1)];
-  const long long i = IX(D, ji, jk, jl);
-  const float rg = rho_g[i];
-  const float pm = float(kM_D / kN_A);
-  const float tv = sqrtf(8.f * float(kK_B) / (float(kPI) * pm) * Tm[i]);
-  const float mfp = 1.f / (1.41421356f * (rg / pm) * (4.f * float(kPI) * (130e-12f * 130e-12f)));
-  const float nu = (1.f / 3.f) * tv * mfp;
-  float v = 2.f * (radius * radius) * (float(kRHO_H2O) - rg) * g / (9.f * rg * nu);
-  if (v * radius / nu > 10.f) v = sqrtf(8.f * radius * float(kRHO_H2O) * g / (3.f * rg * 0.8f));
-  return v;
-}
-
 // ---- three_band_solver_gen_densities, mo_column_solvers.F90:353-604 ----------------------
 // The reference's system per (column, tracer)  d_l s_l + e_l s_{l+1} + c_{l-1} s_{l-1} = rho_l + inc_l
 // (implicit-upwind vertical flux and sedimentation, inc = dt*tendency + explicit flux part) is

@@ -223,30 +223,30 @@ __global__ void k_sfc_column(Dims D, Grid<double> G, State So, State Snu, T* __r
   const double dt = P.dtime, rc = B.rhoc[c], tc = B.tcond[c];
   double h[LGAME_MAX_SOIL_LAYERS + 1], cv[LGAME_MAX_SOIL_LAYERS + 1], dv[LGAME_MAX_SOIL_LAYERS + 1];
   double ev[LGAME_MAX_SOIL_LAYERS + 1], rv[LGAME_MAX_SOIL_LAYERS + 1];
-  const double* zi = P.zi - 1;
-  const double* zc = P.zc - 1;
+  auto zi = [&](int k) { return P.zi[k - 1]; };  // z_soil_interface, 1-based like the reference
+  auto zc = [&](int k) { return P.zc[k - 1]; };  // z_soil_center, 1-based
 #pragma unroll 1
   for (int jl = 1; jl <= ns - 1; ++jl)
-    h[jl] = -(rc * tc * (ts_o[c + (jl - 1) * pl] - ts_o[c + jl * pl]) / (zc[jl] - zc[jl + 1]));
-  h[ns] = -(rc * tc * (ts_o[c + (ns - 1) * pl] - B.tconst[c]) / (2.0 * (zc[ns] - P.z_t_const)));
+    h[jl] = -(rc * tc * (ts_o[c + (jl - 1) * pl] - ts_o[c + jl * pl]) / (zc(jl) - zc(jl + 1)));
+  h[ns] = -(rc * tc * (ts_o[c + (ns - 1) * pl] - B.tconst[c]) / (2.0 * (zc(ns) - P.z_t_const)));
   // the latent heat flux over lakes is formed only by the phase transitions, which the
   // reference's step never calls (its initial zero then; with lphase_trans, their value)
   const double lat_lake = B.lat_lake[c];
-  rv[1] = ts_o[c] + (B.sens_soil[c] + lat_lake + B.sw_in[c] - B.lw_out[c] + 0.5 * h[1]) / ((zi[1] - zi[2]) * rc) * dt;
+  rv[1] = ts_o[c] + (B.sens_soil[c] + lat_lake + B.sw_in[c] - B.lw_out[c] + 0.5 * h[1]) / ((zi(1) - zi(2)) * rc) * dt;
 #pragma unroll 1
   for (int jl = 2; jl <= ns; ++jl)
-    rv[jl] = ts_o[c + (jl - 1) * pl] + 0.5 * (-h[jl - 1] + h[jl]) / ((zi[jl] - zi[jl + 1]) * rc) * dt;
+    rv[jl] = ts_o[c + (jl - 1) * pl] + 0.5 * (-h[jl - 1] + h[jl]) / ((zi(jl) - zi(jl + 1)) * rc) * dt;
 #pragma unroll 1
   for (int jl = 1; jl <= ns; ++jl) {
-    const double q = 0.5 * dt * rc * tc / ((zi[jl] - zi[jl + 1]) * rc);
-    if (jl == 1) dv[jl] = 1.0 + q * 1.0 / (zc[jl] - zc[jl + 1]);
-    else if (jl == ns) dv[jl] = 1.0 + q * 1.0 / (zc[jl - 1] - zc[jl]);
-    else dv[jl] = 1.0 + q * (1.0 / (zc[jl - 1] - zc[jl]) + 1.0 / (zc[jl] - zc[jl + 1]));
+    const double q = 0.5 * dt * rc * tc / ((zi(jl) - zi(jl + 1)) * rc);
+    if (jl == 1) dv[jl] = 1.0 + q * 1.0 / (zc(jl) - zc(jl + 1));
+    else if (jl == ns) dv[jl] = 1.0 + q * 1.0 / (zc(jl - 1) - zc(jl));
+    else dv[jl] = 1.0 + q * (1.0 / (zc(jl - 1) - zc(jl)) + 1.0 / (zc(jl) - zc(jl + 1)));
   }
 #pragma unroll 1
   for (int jl = 1; jl <= ns - 1; ++jl) {
-    cv[jl] = -(0.5 * dt * rc * tc / ((zi[jl + 1] - zi[jl + 2]) * rc) / (zc[jl] - zc[jl + 1]));
-    ev[jl] = -(0.5 * dt * rc * tc / ((zi[jl] - zi[jl + 1]) * rc) / (zc[jl] - zc[jl + 1]));
+    cv[jl] = -(0.5 * dt * rc * tc / ((zi(jl + 1) - zi(jl + 2)) * rc) / (zc(jl) - zc(jl + 1)));
+    ev[jl] = -(0.5 * dt * rc * tc / ((zi(jl) - zi(jl + 1)) * rc) / (zc(jl) - zc(jl + 1)));
   }
   // thomas_algorithm, mo_column_solvers.F90:606-640 (e' into ev, r' into rv)
   ev[1] = ev[1] / dv[1];
@@ -302,26 +302,26 @@ __global__ void k_sfc_column_split(Dims D, Grid<double> G, State So, State Snu, 
   const double dt = P.dtime, rc = B.rhoc[c], tc = B.tcond[c], irc_dt = dt / rc, htc = 0.5 * dt * tc;
   double h[LGAME_MAX_SOIL_LAYERS + 1], cv[LGAME_MAX_SOIL_LAYERS + 1], dv[LGAME_MAX_SOIL_LAYERS + 1];
   double ev[LGAME_MAX_SOIL_LAYERS + 1], rv[LGAME_MAX_SOIL_LAYERS + 1];
-  const double* idzi = P.idzi - 1;  // 1-based
-  const double* idzc = P.idzc - 1;
+  auto idzi = [&](int k) { return P.idzi[k - 1]; };  // 1-based
+  auto idzc = [&](int k) { return P.idzc[k - 1]; };
   const double rct = rc * tc;
 #pragma unroll 1
-  for (int jl = 1; jl <= ns - 1; ++jl) h[jl] = -(rct * (ts_o[c + (jl - 1) * pl] - ts_o[c + jl * pl]) * idzc[jl]);
+  for (int jl = 1; jl <= ns - 1; ++jl) h[jl] = -(rct * (ts_o[c + (jl - 1) * pl] - ts_o[c + jl * pl]) * idzc(jl));
   h[ns] = -(rct * (ts_o[c + (ns - 1) * pl] - B.tconst[c]) * P.i2dzt);
-  rv[1] = ts_o[c] + (B.sens_soil[c] + B.lat_lake[c] + B.sw_in[c] - B.lw_out[c] + 0.5 * h[1]) * idzi[1] * irc_dt;
+  rv[1] = ts_o[c] + (B.sens_soil[c] + B.lat_lake[c] + B.sw_in[c] - B.lw_out[c] + 0.5 * h[1]) * idzi(1) * irc_dt;
 #pragma unroll 1
   for (int jl = 2; jl <= ns; ++jl)
-    rv[jl] = ts_o[c + (jl - 1) * pl] + 0.5 * (h[jl] - h[jl - 1]) * idzi[jl] * irc_dt;
+    rv[jl] = ts_o[c + (jl - 1) * pl] + 0.5 * (h[jl] - h[jl - 1]) * idzi(jl) * irc_dt;
 #pragma unroll 1
   for (int jl = 1; jl <= ns; ++jl) {
-    const double q = htc * idzi[jl];
-    const double above = (jl >= 2) ? idzc[jl - 1] : 0.0, below = (jl <= ns - 1) ? idzc[jl] : 0.0;
+    const double q = htc * idzi(jl);
+    const double above = (jl >= 2) ? idzc(jl - 1) : 0.0, below = (jl <= ns - 1) ? idzc(jl) : 0.0;
     dv[jl] = 1.0 + q * (above + below);
   }
 #pragma unroll 1
   for (int jl = 1; jl <= ns - 1; ++jl) {
-    cv[jl] = -(htc * idzi[jl + 1] * idzc[jl]);
-    ev[jl] = -(htc * idzi[jl] * idzc[jl]);
+    cv[jl] = -(htc * idzi(jl + 1) * idzc(jl));
+    ev[jl] = -(htc * idzi(jl) * idzc(jl));
   }
   // Thomas sweep, one reciprocal per row
   double inv = 1.0 / dv[1];
