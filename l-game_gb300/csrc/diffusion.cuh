@@ -596,6 +596,9 @@ __host__ __device__ constexpr size_t diff_scalar_smem(int nf) {
                           (size_t)nf * DS_Y * (DS_X + 1));
 }
 
+// all eight fields (seven constituents and the temperature) within the 227 KB a block may opt into
+static_assert(diff_scalar_smem(8) <= 227 * 1024, "k_diff_scalar_col: shared memory of 8 fields");
+
 // asynchronous 4-byte copy global -> shared (cp.async, no register staging) and its groups
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
