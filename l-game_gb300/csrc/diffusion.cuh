@@ -46,7 +46,8 @@ struct DiffBuf {
   T *mdtx, *mdty, *mdtz; // mom_diff_tend_x/y/z (carried)
   T *mdt, *tdh;          // mass_diff_tendency (ncons fields), temp_diff_heating
   T* hd;                 // heating_diss (carried; formed by the dissipation kernel)
-  T *flx, *fly, *flw;    // diffusive flux densities of the scalar diffusion (one field per constituent)
+  T *flx, *fly, *flw;    // diffusive flux densities of the scalar diffusion, one field per constituent
+                         // (FP64 step only: the split step forms its faces in shared memory)
   T *zz;                 // zeta_z at dual points (rel_vort of the state of the first substep)
   T *vdiv;               // viscosity * div_h(wind) at scalar points (mom_diff_h's scalar_placeholder)
 };
