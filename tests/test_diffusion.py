@@ -8,7 +8,8 @@ CPU: the oracle's restatement against a second, vectorised numpy restatement on 
 TKE is still zero then); the gas mass is conserved with mass diffusion on in a periodic
 domain; the namelist defaults of &diff are the reference's (all diffusion on, smag, tke); the
 split step's fused scalar diffusion, its regrouped sums restated in FP64 numpy, against the
-oracle's two-pass form.
+oracle's two-pass form, and its tile, halo and face logic restated for its launch grid (every
+cell owned once, every face formed once from the right cells, every index in bounds).
 GPU: the FP64 step against the oracle, state and the carried diffusion diagnostics, on
 periodic and non-periodic cases with orography, Smagorinsky and TKE horizontal schemes, with
 horizontal momentum diffusion alone, and on a grid whose sizes are multiples of the fused
@@ -263,6 +264,81 @@ def test_fused_scalar_diffusion_algorithm_matches_oracle(key):
             continue
         m_ref = fused_scalar_diffusion(g, rho[..., jc], visc / rho_g, *args)
         assert cases.rel_err(m_ref, mdt[..., jc]) <= 1e-11, (jc, cases.rel_err(m_ref, mdt[..., jc]))
+
+
+def _tile_constants():
+    """DS_X, DS_Y of k_diff_scalar_col, read from its source so the check below follows it."""
+    import re
+    from pathlib import Path
+    src = (Path(__file__).resolve().parents[1] / "l-game_gb300" / "csrc" / "diffusion.cuh").read_text()
+    m = re.search(r"constexpr int DS_X = (\d+), DS_Y = (\d+), DS_THREADS = 32 \* \(DS_Y \+ 3\);", src)
+    assert m, "tile constants of k_diff_scalar_col not found"
+    return int(m.group(1)), int(m.group(2))
+
+
+@pytest.mark.parametrize("ny,nx,periodic", [(4, 40, True), (17, 21, False), (18, 20, True), (32, 24, True),
+                                            (65, 97, True), (65, 97, False), (64, 16, False), (3, 3, True)])
+def test_fused_scalar_diffusion_tiles_cover_the_grid(ny, nx, periodic):
+    """The slot, face and halo logic of k_diff_scalar_col (csrc/diffusion.cuh), restated on the
+    CPU for its launch grid: every cell belongs to one tile thread; each face a cell reads is
+    formed by exactly one thread of its block from two slots that hold data, the cells either
+    side of the face across the periodic edges as the reference's grad_hor takes them; every
+    shared-memory index lies in its array and every global point in its field's extent."""
+    DX, DY = _tile_constants()
+    SX, NS = DX + 2, (DX + 2) * (DY + 2)
+    wrap_y = lambda i: ny if i < 1 else (1 if i > ny else i)
+    wrap_x = lambda k: nx if k < 1 else (1 if k > nx else k)
+    owner = np.zeros((ny + 1, nx + 1), dtype=int)
+    for by in range((nx + DY - 1) // DY):
+        for bx in range((ny + DX - 1) // DX):
+            ji0, jk0 = bx * DX + 1, by * DY + 1
+            slots, fxw, fyw, cells = {}, {}, {}, []
+            for t in range(32 * (DY + 3)):
+                lane, warp = t % 32, t // 32
+                if warp < DY:
+                    ji, jk, role = ji0 + lane, jk0 + warp, 0
+                elif warp == DY:
+                    ji, jk, role = ji0 + lane, jk0 - 1, 1
+                elif warp == DY + 1:
+                    ji, jk, role = ji0 + lane, jk0 + DY, 2
+                elif lane < DY:
+                    ji, jk, role = ji0 - 1, jk0 + lane, 3
+                elif lane < 2 * DY:
+                    ji, jk, role = ji0 + DX, jk0 + lane - DY, 4
+                else:
+                    continue
+                slot = (jk - jk0 + 1) * SX + (ji - ji0 + 1)
+                assert 0 <= slot < NS and slot not in slots
+                has = 0 <= ji <= ny + 1 and 0 <= jk <= nx + 1
+                if not periodic:
+                    has = has and 1 <= ji <= ny and 1 <= jk <= nx
+                slots[slot] = (wrap_y(ji), wrap_x(jk)) if has else None
+                if has:
+                    assert 1 <= wrap_y(ji) <= ny and 1 <= wrap_x(jk) <= nx
+                fr, fc = jk - jk0, ji - ji0
+                if role in (0, 2) and 1 <= ji <= ny and jk <= nx + 1:  # u point (ji, jk)
+                    assert 0 <= fr <= DY and 0 <= fc < DX and (fr, fc) not in fxw
+                    zero = not periodic and jk in (1, nx + 1)
+                    fxw[(fr, fc)] = (slot - SX, slot, zero, (ji, jk))
+                if role in (0, 4) and ji <= ny + 1 and jk <= nx:  # v point (ji, jk)
+                    assert 0 <= fr < DY and 0 <= fc <= DX and (fr, fc) not in fyw
+                    zero = not periodic and ji in (1, ny + 1)
+                    fyw[(fr, fc)] = (slot - 1, slot, zero, (ji, jk))
+                if role == 0 and ji <= ny and jk <= nx:
+                    cells.append((ji, jk, fr, fc))
+            for (a, b, zero, (ji, jk)) in fxw.values():  # west cell jk-1, east cell jk
+                assert 0 <= a < NS
+                if not zero:
+                    assert slots.get(a) == (wrap_y(ji), wrap_x(jk - 1)) and slots.get(b) == (ji, wrap_x(jk))
+            for (a, b, zero, (ji, jk)) in fyw.values():  # north cell ji-1, south cell ji
+                assert 0 <= a < NS
+                if not zero:
+                    assert slots.get(a) == (wrap_y(ji - 1), jk) and slots.get(b) == (wrap_y(ji), jk)
+            for ji, jk, fr, fc in cells:
+                owner[ji, jk] += 1
+                assert fxw[(fr, fc)][3] == (ji, jk) and fxw[(fr + 1, fc)][3] == (ji, jk + 1)
+                assert fyw[(fr, fc)][3] == (ji, jk) and fyw[(fr, fc + 1)][3] == (ji + 1, jk)
+    assert np.all(owner[1:, 1:] == 1) and not owner[0].any() and not owner[:, 0].any()
 
 
 # ---- GPU: the FP64 step against the oracle ------------------------------------------------------
